@@ -1,0 +1,70 @@
+"""Builds libfalcon_gpu.so (sm_103a) in-tree under falcon-dns_gb300/_build/.
+
+Two translation units compiled in parallel: the CUDA kernels with nvcc
+(-gencode arch=compute_103a,code=sm_103a) and the host runtime with g++,
+then linked with nvcc.  Host code is compiled with -ffp-contract=off so that
+operator construction gives identical results on x86_64 and aarch64.
+"""
+import os
+import shutil
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+SRC = os.path.join(HERE, "csrc")
+OUT = os.path.join(HERE, "_build")
+LIB = os.path.join(OUT, "libfalcon_gpu.so")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def _cuda_home():
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    return os.path.dirname(os.path.dirname(os.path.realpath(nvcc))), nvcc
+
+
+def _run(cmd):
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        sys.stderr.write(" ".join(cmd) + "\n" + r.stdout + r.stderr)
+        raise RuntimeError("build step failed: " + cmd[0])
+    return r.stdout + r.stderr
+
+
+def sources():
+    return [os.path.join(SRC, f) for f in sorted(os.listdir(SRC))] + [
+        os.path.join(HERE, "..", "include", "falcon_gpu.h")]
+
+
+def up_to_date():
+    if not os.path.exists(LIB):
+        return False
+    t = os.path.getmtime(LIB)
+    return all(os.path.getmtime(s) <= t for s in sources())
+
+
+def build(force=False, verbose=False):
+    if not force and up_to_date():
+        return LIB
+    os.makedirs(OUT, exist_ok=True)
+    home, nvcc = _cuda_home()
+    kern_o = os.path.join(OUT, "falcon_kernels.o")
+    host_o = os.path.join(OUT, "falcon_host.o")
+    cmds = [
+        [nvcc] + ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xptxas", "-v",
+                         "-c", os.path.join(SRC, "falcon_kernels.cu"), "-o", kern_o],
+        ["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-pthread",
+         "-I" + os.path.join(home, "include"), "-c", os.path.join(SRC, "falcon_host.cpp"), "-o", host_o],
+    ]
+    with ThreadPoolExecutor(2) as ex:
+        logs = list(ex.map(_run, cmds))
+    if verbose:
+        print(logs[0])
+    tmp = LIB + ".tmp"
+    _run([nvcc] + ARCH + ["-shared", "-o", tmp, kern_o, host_o, "-lcudart", "-lpthread"])
+    os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))

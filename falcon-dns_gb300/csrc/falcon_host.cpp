@@ -1,0 +1,1988 @@
+// Host runtime of the GB300 FAlCon-DNS time step: parameters and namelist,
+// operator construction from the reference's LU factors, grouped device
+// state, step sequencing, batching, serving and the C ABI of falcon_gpu.h.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cctype>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <deque>
+#include <fstream>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <sstream>
+#include <string>
+#include <thread>
+#include <tuple>
+#include <vector>
+
+#include "../../include/falcon_gpu.h"
+#include "falcon_internal.h"
+
+using namespace falcon;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+
+#define CK(call)                                                                  \
+  do {                                                                            \
+    cudaError_t e_ = (call);                                                      \
+    if (e_ != cudaSuccess)                                                        \
+      return fail(FALCON_ECUDA, std::string(#call ": ") + cudaGetErrorString(e_)); \
+  } while (0)
+
+// ---------------------------------------------------------------------------
+// Dense algebra on the host (operator construction only).  dgetrf/dgetrs
+// restate LAPACK's partial-pivoting LU (src/algebra_lapack.F90:14-53).
+// ---------------------------------------------------------------------------
+int host_dgetrf(int n, double* a, int* ipiv) {
+  int info = 0;
+  for (int j = 0; j < n; ++j) {
+    int p = j;
+    double amax = std::fabs(a[j + (size_t)n * j]);
+    for (int i = j + 1; i < n; ++i) {
+      double v = std::fabs(a[i + (size_t)n * j]);
+      if (v > amax) { amax = v; p = i; }
+    }
+    ipiv[j] = p + 1;
+    if (a[p + (size_t)n * j] != 0.0) {
+      if (p != j)
+        for (int k = 0; k < n; ++k) std::swap(a[j + (size_t)n * k], a[p + (size_t)n * k]);
+      const double piv = a[j + (size_t)n * j];
+      if (std::fabs(piv) >= 2.2250738585072014e-308) {
+        const double rp = 1.0 / piv;
+        for (int i = j + 1; i < n; ++i) a[i + (size_t)n * j] *= rp;
+      } else {
+        for (int i = j + 1; i < n; ++i) a[i + (size_t)n * j] /= piv;
+      }
+    } else if (info == 0) {
+      info = j + 1;
+    }
+    for (int k = j + 1; k < n; ++k) {
+      const double akj = a[j + (size_t)n * k];
+      if (akj != 0.0)
+        for (int i = j + 1; i < n; ++i) a[i + (size_t)n * k] -= a[i + (size_t)n * j] * akj;
+    }
+  }
+  return info;
+}
+
+void host_dgetrs(int n, const double* a, const int* ipiv, double* b) {
+  for (int i = 0; i < n; ++i) {
+    const int p = ipiv[i] - 1;
+    if (p != i) std::swap(b[i], b[p]);
+  }
+  for (int j = 0; j < n; ++j) {
+    const double bj = b[j];
+    if (bj != 0.0)
+      for (int i = j + 1; i < n; ++i) b[i] -= bj * a[i + (size_t)n * j];
+  }
+  for (int j = n - 1; j >= 0; --j) {
+    if (b[j] != 0.0) {
+      b[j] = b[j] / a[j + (size_t)n * j];
+      const double bj = b[j];
+      for (int i = 0; i < j; ++i) b[i] -= bj * a[i + (size_t)n * j];
+    }
+  }
+}
+
+template <class F>
+void parallel_for(int n, F f) {
+  unsigned nt = std::max(1u, std::thread::hardware_concurrency());
+  nt = std::min<unsigned>(nt, (unsigned)std::max(1, n));
+  std::atomic<int> next(0);
+  std::vector<std::thread> th;
+  for (unsigned t = 0; t < nt; ++t)
+    th.emplace_back([&]() {
+      for (int i = next++; i < n; i = next++) f(i);
+    });
+  for (auto& t : th) t.join();
+}
+
+// ---------------------------------------------------------------------------
+// Chebyshev collocation (dcheb, src/chebyshev_fftw.F90:88-121) and grid
+// (init_grid, src/init.F90:120-162).
+// ---------------------------------------------------------------------------
+struct Cheb {
+  int R;
+  std::vector<double> xp, t, D, D2;  // column-major (R,R): t(i,j) = T_{j}(x_i)
+  std::vector<double> radius, inv_r, inv_r2, dr;
+  double rmin, rmax;
+};
+
+Cheb make_cheb(int R, double eta) {
+  Cheb c;
+  c.R = R;
+  c.rmin = eta / (1.0 - eta);
+  c.rmax = 1.0 / (1.0 - eta);
+  const double pi = 4.0 * std::atan(1.0);
+  c.xp.resize(R);
+  c.t.assign((size_t)R * R, 0.0);
+  c.D.assign((size_t)R * R, 0.0);
+  c.D2.assign((size_t)R * R, 0.0);
+  for (int i = 0; i < R; ++i) c.xp[i] = std::cos(((double)(R - 1 - i) * pi) / (double)(R - 1));
+  std::vector<double> tt(R), dt(R), d2t(R);
+  for (int i = 0; i < R; ++i) {
+    tt[0] = 1.0; tt[1] = c.xp[i];
+    dt[0] = 0.0; dt[1] = 1.0;
+    d2t[0] = 0.0; d2t[1] = 0.0;
+    for (int j = 2; j < R; ++j) {
+      tt[j] = 2.0 * c.xp[i] * tt[j - 1] - tt[j - 2];
+      dt[j] = 2.0 * tt[j - 1] + 2.0 * c.xp[i] * dt[j - 1] - dt[j - 2];
+      d2t[j] = 4.0 * dt[j - 1] + 2.0 * c.xp[i] * d2t[j - 1] - d2t[j - 2];
+    }
+    for (int j = 0; j < R; ++j) {
+      c.t[i + (size_t)R * j] = tt[j];
+      c.D[i + (size_t)R * j] = 2.0 * dt[j];
+      c.D2[i + (size_t)R * j] = 4.0 * d2t[j];
+    }
+  }
+  c.radius.resize(R); c.inv_r.resize(R); c.inv_r2.resize(R); c.dr.resize(R);
+  for (int i = 0; i < R; ++i) {
+    c.radius[i] = (c.rmin + (0.5 * (1.0 + std::cos((double)(R - 1 - i) * pi / (double)(R - 1)))));
+    c.inv_r[i] = 1.0 / c.radius[i];
+  }
+  for (int i = 0; i < R - 1; ++i) c.dr[i + 1] = c.radius[i + 1] - c.radius[i];
+  c.dr[0] = c.dr[1];
+  for (int i = 0; i < R; ++i) c.inv_r2[i] = c.inv_r[i] * c.inv_r[i];
+  return c;
+}
+
+// ---------------------------------------------------------------------------
+// Operator key and shared operator sets
+// ---------------------------------------------------------------------------
+struct OpKey {
+  int R, Nm, mbc, type, imp, exp;
+  double dt, pr, eta, wt;
+  bool operator<(const OpKey& o) const {
+    return std::tie(R, Nm, mbc, type, imp, exp, dt, pr, eta, wt) <
+           std::tie(o.R, o.Nm, o.mbc, o.type, o.imp, o.exp, o.dt, o.pr, o.eta, o.wt);
+  }
+};
+
+struct OpSet {
+  OpKey key;
+  int R = 0, M = 0;
+  // device, column-major (lda = rows)
+  double* D1p = nullptr;   // R x R physical d/dr
+  double* Lp = nullptr;    // R x R physical d2/dr2 + r^-1 d/dr
+  double* ST = nullptr;    // M blocks of R x R: chebinvtran o AT_m^-1
+  double* G = nullptr;     // M blocks of 3R x R: [Tinv X_w; Tinv X_psi; -D1inv X_psi]
+  double* U = nullptr;     // 2R x R: [Tinv A_u^-1; D1inv A_u^-1]
+  double* inv_r = nullptr;
+  double* inv_r2 = nullptr;
+  size_t bytes = 0;
+  ~OpSet() {
+    cudaFree(D1p); cudaFree(Lp); cudaFree(ST); cudaFree(G); cudaFree(U);
+    cudaFree(inv_r); cudaFree(inv_r2);
+  }
+};
+
+std::mutex g_ops_mu;
+std::map<OpKey, std::weak_ptr<OpSet>> g_ops;
+
+// Physical-space derivative matrices (the composition chebtransform ->
+// derivative recurrence -> inverse transform of src/chebyshev_fftw.F90 is
+// linear; its matrix is D H t^T diag(c') / (R-1), H = diag(1/2,1,..,1,1/2),
+// c' = (1,2,..,2,1), by discrete orthogonality at the Gauss-Lobatto points).
+void phys_deriv(const Cheb& c, std::vector<double>& D1p, std::vector<double>& Lp) {
+  const int R = c.R;
+  std::vector<double> W((size_t)R * R);  // W(j,i) = h_j t(i,j) c'_i / (R-1), coefficient j from value i
+  for (int j = 0; j < R; ++j) {
+    const double h = (j == 0 || j == R - 1) ? 0.5 : 1.0;
+    for (int i = 0; i < R; ++i) {
+      const double cp = (i == 0 || i == R - 1) ? 1.0 : 2.0;
+      W[j + (size_t)R * i] = h * c.t[i + (size_t)R * j] * cp / (double)(R - 1);
+    }
+  }
+  D1p.assign((size_t)R * R, 0.0);
+  Lp.assign((size_t)R * R, 0.0);
+  for (int i = 0; i < R; ++i)      // output point
+    for (int k = 0; k < R; ++k) {  // input point
+      double s1 = 0.0, s2 = 0.0;
+      for (int j = 0; j < R; ++j) {
+        const double w = W[j + (size_t)R * k];
+        s1 += c.D[i + (size_t)R * j] * w;
+        s2 += c.D2[i + (size_t)R * j] * w;
+      }
+      D1p[i + (size_t)R * k] = s1;
+      Lp[i + (size_t)R * k] = s2 + c.inv_r[i] * s1;
+    }
+}
+
+// mat_build / mat_build_IRK (src/mat_assembly.F90:68-187, :242-359) for one
+// mode: AT (R x R) and AF (2R x 2R), before factorisation.
+void assemble_AT_AF(const Cheb& c, int mbc, double dt, int n, double wt, double pr, bool irk,
+                    std::vector<double>& AT, std::vector<double>& AF) {
+  const int R = c.R, R2 = 2 * R;
+  const double C = std::pow(2.0 / (double)(R - 1), 0.5);
+  const double nn = (double)n * (double)n;
+  AT.assign((size_t)R * R, 0.0);
+  AF.assign((size_t)R2 * R2, 0.0);
+  auto t = [&](int i, int j) { return c.t[i + (size_t)R * j]; };
+  auto D = [&](int i, int j) { return c.D[i + (size_t)R * j]; };
+  auto D2 = [&](int i, int j) { return c.D2[i + (size_t)R * j]; };
+  auto at = [&](int i, int j) -> double& { return AT[i + (size_t)R * j]; };
+  auto af = [&](int i, int j) -> double& { return AF[i + (size_t)R2 * j]; };
+  auto bcp2 = [&](int side, int j) {
+    const int i = side ? R - 1 : 0;
+    return mbc == 0 ? D(i, j) : D2(i, j) - c.inv_r[i] * D(i, j);
+  };
+  for (int j = 0; j < R; ++j) {
+    for (int i = 0; i < R; ++i)
+      at(i, j) = t(i, j) - wt * dt * (1.0 / pr) * (c.inv_r[i] * D(i, j) + D2(i, j) - nn * c.inv_r2[i] * t(i, j));
+    at(0, j) = t(0, j);
+    at(R - 1, j) = t(R - 1, j);
+  }
+  for (int i = 0; i < R; ++i) { at(i, 0) *= 0.5; at(i, R - 1) *= 0.5; }
+  for (auto& v : AT) v = C * v;
+  for (int j = 0; j < R; ++j) {
+    for (int i = 0; i < R; ++i) {
+      const double L = c.inv_r[i] * D(i, j) + D2(i, j) - nn * c.inv_r2[i] * t(i, j);
+      af(i, j) = L;
+      af(i, R + j) = t(i, j);
+      af(R + i, j) = 0.0;
+      af(R + i, R + j) = t(i, j) - wt * dt * L;
+    }
+    if (irk) { af(0, j) = bcp2(0, j); af(R - 1, j) = bcp2(1, j); }
+    else { af(0, j) = t(0, j); af(R - 1, j) = t(R - 1, j); }
+    af(0, R + j) = 0.0; af(R - 1, R + j) = 0.0;
+    if (irk) { af(R, j) = t(0, j); af(R2 - 1, j) = t(R - 1, j); }
+    else { af(R, j) = bcp2(0, j); af(R2 - 1, j) = bcp2(1, j); }
+    af(R, R + j) = 0.0; af(R2 - 1, R + j) = 0.0;
+  }
+  for (int i = 0; i < R; ++i) {
+    af(i, 0) *= 0.5; af(i, R - 1) *= 0.5; af(i, R) *= 0.5; af(i, R2 - 1) *= 0.5;
+    af(R + i, 0) *= 0.5; af(R + i, R - 1) *= 0.5; af(R + i, R) *= 0.5; af(R + i, R2 - 1) *= 0.5;
+  }
+  for (auto& v : AF) v = C * v;
+}
+
+// mat_build_uphibar(_IRK) (src/mat_assembly.F90:189-240, :361-413)
+void assemble_Au(const Cheb& c, int mbc, double dt, double wt, std::vector<double>& A) {
+  const int R = c.R;
+  const double C = std::pow(2.0 / (double)(R - 1), 0.5);
+  A.assign((size_t)R * R, 0.0);
+  for (int j = 0; j < R; ++j) {
+    for (int i = 0; i < R; ++i)
+      A[i + (size_t)R * j] = c.t[i + (size_t)R * j] -
+                             wt * dt * (c.inv_r[i] * c.D[i + (size_t)R * j] + c.D2[i + (size_t)R * j] -
+                                        c.inv_r2[i] * c.t[i + (size_t)R * j]);
+    if (mbc == 0) {
+      A[0 + (size_t)R * j] = c.t[0 + (size_t)R * j];
+      A[R - 1 + (size_t)R * j] = c.t[R - 1 + (size_t)R * j];
+    } else {
+      A[0 + (size_t)R * j] = c.D[0 + (size_t)R * j] - c.inv_r[0] * c.t[0 + (size_t)R * j];
+      A[R - 1 + (size_t)R * j] = c.D[R - 1 + (size_t)R * j] - c.inv_r[R - 1] * c.t[R - 1 + (size_t)R * j];
+    }
+  }
+  for (int i = 0; i < R; ++i) { A[i] *= 0.5; A[i + (size_t)R * (R - 1)] *= 0.5; }
+  for (auto& v : A) v = C * v;
+}
+
+// Coefficients -> values (chebinvtran) and -> d/dr values (chebinvtranD1)
+// as matrices: Tinv = C t H, D1inv = C D H.
+void apply_inv(const Cheb& c, const double* coef, double* val, double* dval) {
+  const int R = c.R;
+  const double C = std::pow(2.0 / (double)(R - 1), 0.5);
+  for (int i = 0; i < R; ++i) {
+    double s = 0.0, d = 0.0;
+    for (int j = 0; j < R; ++j) {
+      const double h = (j == 0 || j == R - 1) ? 0.5 : 1.0;
+      s += c.t[i + (size_t)R * j] * h * coef[j];
+      d += c.D[i + (size_t)R * j] * h * coef[j];
+    }
+    if (val) val[i] = C * s;
+    if (dval) dval[i] = C * d;
+  }
+}
+
+template <class T>
+int upload(T** dst, const std::vector<T>& v, size_t* acc) {
+  CK(cudaMalloc(dst, sizeof(T) * v.size()));
+  CK(cudaMemcpy(*dst, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice));
+  if (acc) *acc += sizeof(T) * v.size();
+  return 0;
+}
+
+int build_opset(const OpKey& k, std::shared_ptr<OpSet>* out) {
+  {
+    std::lock_guard<std::mutex> lk(g_ops_mu);
+    auto it = g_ops.find(k);
+    if (it != g_ops.end()) {
+      if (auto sp = it->second.lock()) { *out = sp; return 0; }
+    }
+  }
+  auto ops = std::make_shared<OpSet>();
+  ops->key = k;
+  const int R = k.R, M = k.Nm + 1;
+  ops->R = R; ops->M = M;
+  const bool irk = (k.type == FALCON_IMEXRK);
+  Cheb c = make_cheb(R, k.eta);
+  std::vector<double> D1p, Lp;
+  phys_deriv(c, D1p, Lp);
+  std::vector<double> ST((size_t)M * R * R), G((size_t)M * 3 * R * R), U((size_t)2 * R * R);
+  std::atomic<int> bad(0);
+  parallel_for(M, [&](int m) {
+    std::vector<double> AT, AF;
+    assemble_AT_AF(c, k.mbc, k.dt, m, k.wt, k.pr, irk, AT, AF);
+    std::vector<int> p1(R), p2(2 * R);
+    if (host_dgetrf(R, AT.data(), p1.data()) != 0) bad = m + 1;
+    if (host_dgetrf(2 * R, AF.data(), p2.data()) != 0 && m > 0) bad = m + 1;
+    std::vector<double> x(2 * R), v(R), dv(R);
+    double* S = &ST[(size_t)m * R * R];
+    for (int j = 0; j < R; ++j) {
+      std::fill(x.begin(), x.end(), 0.0);
+      x[j] = 1.0;
+      host_dgetrs(R, AT.data(), p1.data(), x.data());
+      apply_inv(c, x.data(), v.data(), nullptr);
+      for (int i = 0; i < R; ++i) S[i + (size_t)R * j] = v[i];
+    }
+    if (m > 0) {
+      double* Gm = &G[(size_t)m * 3 * R * R];
+      for (int j = 0; j < R; ++j) {
+        std::fill(x.begin(), x.end(), 0.0);
+        x[R + j] = 1.0;
+        host_dgetrs(2 * R, AF.data(), p2.data(), x.data());
+        apply_inv(c, x.data() + R, v.data(), nullptr);  // omega coefficients
+        for (int i = 0; i < R; ++i) Gm[i + (size_t)3 * R * j] = v[i];
+        apply_inv(c, x.data(), v.data(), dv.data());    // psi coefficients
+        for (int i = 0; i < R; ++i) {
+          Gm[R + i + (size_t)3 * R * j] = v[i];
+          Gm[2 * R + i + (size_t)3 * R * j] = -dv[i];
+        }
+      }
+    }
+  });
+  if (bad) return fail(FALCON_ESINGULAR, "dgetrf: singular operator for mode " + std::to_string(bad - 1));
+  {
+    std::vector<double> Au;
+    assemble_Au(c, k.mbc, k.dt, k.wt, Au);
+    std::vector<int> pu(R);
+    if (host_dgetrf(R, Au.data(), pu.data()) != 0) return fail(FALCON_ESINGULAR, "dgetrf: singular uphi_bar operator");
+    std::vector<double> x(R), v(R), dv(R);
+    for (int j = 0; j < R; ++j) {
+      std::fill(x.begin(), x.end(), 0.0);
+      x[j] = 1.0;
+      host_dgetrs(R, Au.data(), pu.data(), x.data());
+      apply_inv(c, x.data(), v.data(), dv.data());
+      for (int i = 0; i < R; ++i) {
+        U[i + (size_t)2 * R * j] = v[i];
+        U[R + i + (size_t)2 * R * j] = dv[i];
+      }
+    }
+  }
+  int rc;
+  if ((rc = upload(&ops->D1p, D1p, &ops->bytes))) return rc;
+  if ((rc = upload(&ops->Lp, Lp, &ops->bytes))) return rc;
+  if ((rc = upload(&ops->ST, ST, &ops->bytes))) return rc;
+  if ((rc = upload(&ops->G, G, &ops->bytes))) return rc;
+  if ((rc = upload(&ops->U, U, &ops->bytes))) return rc;
+  if ((rc = upload(&ops->inv_r, c.inv_r, &ops->bytes))) return rc;
+  if ((rc = upload(&ops->inv_r2, c.inv_r2, &ops->bytes))) return rc;
+  {
+    std::lock_guard<std::mutex> lk(g_ops_mu);
+    g_ops[k] = ops;
+  }
+  *out = ops;
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// Scheme tables (src/timeschemes.F90)
+// ---------------------------------------------------------------------------
+struct Scheme {
+  int type = 0, imp = 0, exp = 0;
+  int n_imp = 0, n_exp = 0;       // IMEX orders, or IMEXRK stages (n_exp)
+  double w_imp[4] = {0}, w_exp[4] = {0}, wt_lhs = 0;
+  double aD[kMaxStages][kMaxStages] = {{0}}, aA[kMaxStages][kMaxStages] = {{0}};
+  double bD[kMaxStages] = {0}, bA[kMaxStages] = {0};
+  bool check_A = false, check_D = false;
+  int diag = 1;
+};
+
+// Constant-dt weights of rhs_update_wts_imp/_exp (src/timeschemes.F90:
+// 1004-1052, 1621-1701) with dt_array(:) = dt.
+int scheme_weights(int type, int imp, int exp, Scheme* s) {
+  s->type = type; s->imp = imp; s->exp = exp;
+  if (type == FALCON_IMEX) {
+    const double d[4] = {1, 1, 1, 1};
+    switch (imp) {
+      case FALCON_IMP_CN:
+        s->n_imp = 2; s->w_imp[0] = 0.5; s->wt_lhs = 0.5;
+        if (exp == FALCON_EXP_AB2) {
+          s->n_exp = 2;
+          s->w_exp[0] = 1.0 + 0.5 * d[0] / d[1];
+          s->w_exp[1] = -0.5 * d[0] / d[1];
+        } else if (exp == FALCON_EXP_AB3) {
+          s->n_exp = 3;
+          s->w_exp[1] = (d[0] * d[2] * 0.5 + (1.0 / 6.0) * d[0] * d[0]) / (d[1] * d[1] * 0.5 - d[1] * d[2]);
+          s->w_exp[2] = (-d[0] * 0.5 - d[1] * s->w_exp[1]) * 0.5 / (d[2]);
+          s->w_exp[0] = 1.0 - s->w_exp[1] - s->w_exp[2];
+        } else return -1;
+        return 0;
+      case FALCON_IMP_BDF2: {
+        if (exp != FALCON_EXP_AB2) return -1;
+        const double r1 = 1.0, a0 = (2.0 + r1) / (1.0 + r1), a1 = 1.0 + 1.0 / r1;
+        const double a2 = -1.0 * (1.0 / r1 / (1.0 + r1));
+        s->n_imp = 2; s->n_exp = 2;
+        s->wt_lhs = 1.0 / a0; s->w_imp[0] = a1 / a0; s->w_imp[1] = a2 / a0;
+        s->w_exp[0] = (1.0 + 1.0 / r1) / a0; s->w_exp[1] = (-1.0 / r1) / a0;
+        return 0;
+      }
+      case FALCON_IMP_BDF3: {
+        if (exp != FALCON_EXP_AB3) return -1;
+        const double r1 = 1.0, r2 = 1.0;
+        const double a0 = (1.0 + 1.0 / (1.0 + r1) + 1.0 / (1.0 + r1 + r2));
+        const double a1 = (((1.0 + r1) * (1.0 + r1 + r2)) / (r1 * (r1 + r2)));
+        const double a2 = (-1.0 * (1.0 + r1 + r2) / (r1 * r2 * (1.0 + r1)));
+        const double a3 = ((1.0 + r1) / (r2 * (r1 + r2) * (1.0 + r1 + r2)));
+        const double b0 = 1.0 * ((1.0 + r1) * (1.0 + r1 + r2)) / (r1 * (r1 + r2));
+        const double b1 = 1.0 * (-(1.0 + r1 + r2) / (r1 * r2));
+        const double b2 = 1.0 * (1.0 + r1) / (r2 * (r1 + r2));
+        s->n_imp = 3; s->n_exp = 3;
+        s->wt_lhs = 1.0 / a0;
+        s->w_imp[0] = a1 / a0; s->w_imp[1] = a2 / a0; s->w_imp[2] = a3 / a0;
+        s->w_exp[0] = b0 / a0; s->w_exp[1] = b1 / a0; s->w_exp[2] = b2 / a0;
+        return 0;
+      }
+      case FALCON_IMP_BDF4: {
+        if (exp != FALCON_EXP_AB4) return -1;
+        const double r1 = 1.0, r2 = 1.0, r3 = 1.0;
+        const double c1 = 1.0 + r3 * (1.0 + r2), c2 = 1.0 + r2 * (1.0 + r1), c3 = 1.0 + r3 * c2;
+        const double a0 = 1.0 + r1 / (1.0 + r1) + r2 * r1 / c2 + r3 * r2 * r1 / c3;
+        const double a1 = -1.0 - r1 * (1.0 + r2 * (1.0 + r1) * (1.0 + r3 * c2 / c1) / (1.0 + r2));
+        const double a2 = r1 * (r1 / (1.0 + r1) + r2 * r1 * (c3 + r3) / (1.0 + r3));
+        const double a3 = -std::pow(r2, 3) * std::pow(r1, 2) * (1.0 + r1) / (1.0 + r2) * c3 / c2;
+        const double a4 = (1.0 + r1) / (1.0 + r3) * c2 / c1 / c3 * (std::pow(r3, 4) * std::pow(r2, 3) * std::pow(r1, 2));
+        const double b3 = -std::pow(r3, 3) * std::pow(r2, 2) * r1 * (1.0 + r1) / (1.0 + r3) * c2 / c1;
+        const double b2 = std::pow(r2, 2) * r1 * (1.0 + r1) / (1.0 + r2) * c3;
+        const double b1 = -c2 * c3 * r1 / (1.0 + r3);
+        const double b0 = r2 * (1.0 + r1) / (1.0 + r2) * ((1.0 + r1) * (c3 + r3) + (1.0 + r3) / r2) / c1;
+        s->n_imp = 4; s->n_exp = 4;
+        s->wt_lhs = 1.0 / a0;
+        s->w_imp[0] = -a1 / a0; s->w_imp[1] = -a2 / a0; s->w_imp[2] = -a3 / a0; s->w_imp[3] = -a4 / a0;
+        s->w_exp[0] = b0 / a0; s->w_exp[1] = b1 / a0; s->w_exp[2] = b2 / a0; s->w_exp[3] = b3 / a0;
+        return 0;
+      }
+      default: return -1;
+    }
+  }
+  if (type == FALCON_IMEXRK) {
+    auto set = [&](int n, const double* aD, const double* bD, const double* aA, const double* bA) {
+      s->n_imp = n; s->n_exp = n;
+      for (int i = 0; i < n; ++i) {
+        for (int j = 0; j < n; ++j) { s->aD[i][j] = aD[i * n + j]; s->aA[i][j] = aA[i * n + j]; }
+        s->bD[i] = bD[i]; s->bA[i] = bA[i];
+      }
+      s->check_D = false; s->check_A = false;
+      for (int i = 0; i < n; ++i) if (s->aD[n - 1][i] == s->bD[i]) s->check_D = true;
+      for (int i = 0; i < n; ++i) if (s->aA[n - 1][i] == s->bA[i]) s->check_A = true;
+    };
+    switch (imp) {
+      case FALCON_IMP_ARS443: {  // src/timeschemes.F90:1215-1233, :1919-1940
+        if (exp != FALCON_EXP_ARS443) return -1;
+        const double aD[25] = {0, 0, 0, 0, 0, 0, 0.5, 0, 0, 0, 0, 1.0 / 6.0, 0.5, 0, 0,
+                               0, -0.5, 0.5, 0.5, 0, 0, 1.5, -1.5, 0.5, 0.5};
+        const double bD[5] = {0, 1.5, -1.5, 0.5, 0.5};
+        const double aA[25] = {0, 0, 0, 0, 0, 0.5, 0, 0, 0, 0, 11.0 / 18.0, 1.0 / 18.0, 0, 0, 0,
+                               5.0 / 6.0, -5.0 / 6.0, 0.5, 0, 0, 0.25, 7.0 / 4.0, 0.75, -7.0 / 4.0, 0};
+        const double bA[5] = {0.25, 7.0 / 4.0, 0.75, -7.0 / 4.0, 0};
+        set(5, aD, bD, aA, bA);
+        return 0;
+      }
+      case FALCON_IMP_BPR353: {  // :1277-1295, :1995-2015
+        if (exp != FALCON_EXP_BPR353) return -1;
+        const double aD[25] = {0, 0, 0, 0, 0, 0.5, 0.5, 0, 0, 0, 5.0 / 18.0, -1.0 / 9.0, 0.5, 0, 0,
+                               0.5, 0, 0, 0.5, 0, 0.25, 0, 0.75, -0.5, 0.5};
+        const double bD[5] = {0.25, 0, 0.75, -0.5, 0.5};
+        const double aA[25] = {0, 0, 0, 0, 0, 1.0, 0, 0, 0, 0, 4.0 / 9.0, 2.0 / 9.0, 0, 0, 0,
+                               0.25, 0, 0.75, 0, 0, 0.25, 0, 0.75, 0, 0};
+        const double bA[5] = {0.25, 0, 0.75, 0, 0};
+        set(5, aD, bD, aA, bA);
+        return 0;
+      }
+      case FALCON_IMP_ARS343: {  // :1107-1120, :1788-1804
+        if (exp != FALCON_EXP_ARS343) return -1;
+        const double g = 0.435866521508459;
+        const double bb1 = -1.5 * g * g + 4.0 * g - 0.25, bb2 = 1.5 * g * g - 5.0 * g + 1.25;
+        const double aD[16] = {0, 0, 0, 0, 0, g, 0, 0, 0, 0.5 * (1.0 - g), g, 0, 0, bb1, bb2, g};
+        const double bD[4] = {0, bb1, bb2, g};
+        const double aA[16] = {0, 0, 0, 0, g, 0, 0, 0, 0.3212788860286278, 0.3966543747256017, 0, 0,
+                               -0.1058582960718797, 0.5529291480359398, 0.5529291480359398, 0};
+        const double bA[4] = {0, bb1, bb2, g};
+        set(4, aD, bD, aA, bA);
+        s->check_D = true; s->check_A = false;  // set explicitly by the reference (:1117, :1802)
+        return 0;
+      }
+      case FALCON_IMP_ARS222: {  // :1065-1078, :1737-1751
+        if (exp != FALCON_EXP_ARS222) return -1;
+        const double g = (2.0 - std::sqrt(2.0)) / 2.0, dl = 1.0 - 1.0 / g / 2.0;
+        const double aD[9] = {0, 0, 0, 0, g, 0, 0, 1.0 - g, g};
+        const double bD[3] = {0, 1.0 - g, g};
+        const double aA[9] = {0, 0, 0, g, 0, 0, dl, 1.0 - dl, 0};
+        const double bA[3] = {dl, 1.0 - dl, 0};
+        set(3, aD, bD, aA, bA);
+        s->check_D = true; s->check_A = true;
+        return 0;
+      }
+      default: return -1;
+    }
+  }
+  return -1;
+}
+
+// ---------------------------------------------------------------------------
+// Azimuthal FFT plan (P = 3 Nm) and its device tables
+// ---------------------------------------------------------------------------
+struct FftTables {
+  FftPlan plan{};
+  double2* tw = nullptr;
+  int* pos = nullptr;
+  ~FftTables() { cudaFree(tw); cudaFree(pos); }
+};
+
+int make_fft(int P, std::unique_ptr<FftTables>* out) {
+  auto f = std::make_unique<FftTables>();
+  f->plan.P = P;
+  int n = P, k = 0;
+  std::vector<int> rad;
+  while (n % 4 == 0) { rad.push_back(4); n /= 4; }
+  while (n % 2 == 0) { rad.push_back(2); n /= 2; }
+  for (int p = 3; p * p <= n; p += 2)
+    while (n % p == 0) { rad.push_back(p); n /= p; }
+  if (n > 1) rad.push_back(n);
+  for (int p : rad)
+    if (p > 64) return fail(FALCON_EINVAL, "azimuthal length 3*Nm has a prime factor above 64");
+  if ((int)rad.size() > kMaxRadix) return fail(FALCON_EINVAL, "too many FFT stages");
+  f->plan.nrad = (int)rad.size();
+  for (int p : rad) f->plan.rad[k++] = p;
+  // digit-reversal positions: pos(n) = sum_s d_s(n) * P/(p_0..p_s)
+  std::vector<int> pos(P);
+  for (int i = 0; i < P; ++i) {
+    int x = i, span = P, pp = 0;
+    for (int p : rad) { int d = x % p; x /= p; span /= p; pp += d * span; }
+    pos[i] = pp;
+  }
+  std::vector<double2> tw(P);
+  const double two_pi = 8.0 * std::atan(1.0);
+  for (int i = 0; i < P; ++i) {
+    const double a = two_pi * (double)i / (double)P;
+    tw[i] = make_double2(std::cos(a), -std::sin(a));
+  }
+  int rc;
+  if ((rc = upload(&f->tw, tw, nullptr))) return rc;
+  if ((rc = upload(&f->pos, pos, nullptr))) return rc;
+  *out = std::move(f);
+  return 0;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Groups: instances sharing one operator set, stepped together
+// ---------------------------------------------------------------------------
+struct Group {
+  falcon_params p{};           // parameters of the first instance (shared part)
+  Scheme sch;
+  int R = 0, M = 0, Nm = 0, P = 0, B = 0;
+  std::shared_ptr<OpSet> ops;
+  std::unique_ptr<FftTables> fft;
+  std::vector<int> members;    // batch indices
+  std::vector<double> ra_pr_h; // per instance Ra/Pr
+  cudaStream_t stream = nullptr;
+  // device state
+  std::vector<void*> allocs;
+  double2 *th[4] = {}, *wh[4] = {}, *nth[4] = {}, *nwh[4] = {};
+  double *ubh[4] = {}, *uromh[4] = {};
+  double2 *up = nullptr, *ur = nullptr, *psi = nullptr;
+  double2 *ntp = nullptr, *ntr = nullptr, *nwp = nullptr, *nwr = nullptr, *dntr = nullptr, *dnwr = nullptr;
+  double2 *lt = nullptr, *lw = nullptr, *lu0 = nullptr, *rhs_t = nullptr, *rhs_w = nullptr;
+  double* ub = nullptr;        // 2R x 2B doubles (alias of ub2)
+  double2* ub2 = nullptr;
+  double* ra_pr = nullptr;
+  double2 *fat[kMaxStages] = {}, *fdt[kMaxStages] = {}, *faw[kMaxStages] = {}, *fdw[kMaxStages] = {},
+          *buo[kMaxStages] = {};
+  double2 *t0 = nullptr, *w0 = nullptr;
+  double* u0 = nullptr;
+  double2* stage_buf = nullptr;  // host staging (pinned) for one instance
+  int head = 0, head_e = 0;
+  int n_step = 0;
+  double tot_time = 0.0;
+  size_t bytes = 0;
+
+  ~Group() {
+    for (void* q : allocs) cudaFree(q);
+    if (stage_buf) cudaFreeHost(stage_buf);
+  }
+  size_t nel() const { return (size_t)R * M * B; }
+  // Every per-instance array is [rows][B] elements of `ew` doubles; the
+  // registry lets the serving loop repack instance columns when members
+  // join or leave.
+  struct Field { void** ptr; size_t rows; int ew; };
+  std::vector<Field> fields;
+  template <class T>
+  int alloc(T** q, size_t n) {
+    CK(cudaMalloc(q, sizeof(T) * (n ? n : 1)));
+    CK(cudaMemset(*q, 0, sizeof(T) * (n ? n : 1)));
+    allocs.push_back(*q);
+    bytes += sizeof(T) * n;
+    const int ew = (int)(sizeof(T) / sizeof(double));
+    fields.push_back(Field{reinterpret_cast<void**>(q), n / (size_t)std::max(B, 1), ew});
+    return 0;
+  }
+  double2* T() const { return th[head]; }
+  double2* W() const { return wh[head]; }
+};
+
+namespace {
+
+OpKey key_of(const falcon_params& p, const Scheme& s) {
+  OpKey k{};
+  k.R = p.nr_max; k.Nm = p.nm_max; k.mbc = p.mbc; k.type = p.scheme_type;
+  k.imp = p.scheme_imp; k.exp = p.scheme_exp; k.dt = p.dt; k.pr = p.pr; k.eta = p.eta;
+  k.wt = (p.scheme_type == FALCON_IMEX) ? s.wt_lhs : s.aD[s.diag][s.diag];
+  return k;
+}
+
+int validate(const falcon_params& p) {
+  if (p.nr_max < 4 || p.nr_max > 257) return fail(FALCON_EINVAL, "Nr_max must be in [4, 257]");
+  if (p.nm_max < 1 || p.nm_max > 4096) return fail(FALCON_EINVAL, "Nm_max must be in [1, 4096]");
+  if (!(p.eta > 0.0 && p.eta < 1.0)) return fail(FALCON_EINVAL, "eta must be in (0,1)");
+  if (!(p.dt > 0.0) || !std::isfinite(p.dt)) return fail(FALCON_EINVAL, "dt must be positive");
+  if (!(p.pr > 0.0)) return fail(FALCON_EINVAL, "Pr must be positive");
+  if (p.mbc != 0 && p.mbc != 1) return fail(FALCON_EINVAL, "mBC must be NS or SF");
+  if (p.scheme_type == FALCON_RK) return fail(FALCON_EINVAL, "time_scheme_type RK is not supported by this build");
+  if (p.l_vartimestep) return fail(FALCON_EINVAL, "l_vartimestep=.TRUE. is not supported by this build");
+  if (p.l_restart) return fail(FALCON_EINVAL, "l_restart=.TRUE. is not supported by this build");
+  Scheme s;
+  if (scheme_weights(p.scheme_type, p.scheme_imp, p.scheme_exp, &s) != 0)
+    return fail(FALCON_EINVAL, "unsupported time scheme combination");
+  if (p.scheme_type == FALCON_IMEXRK && !(s.check_A && s.check_D))
+    return fail(FALCON_EINVAL, "IMEXRK schemes that are not stiffly accurate (e.g. ARS343) are not supported yet");
+  return 0;
+}
+
+int group_init(Group* g, const std::vector<falcon_params>& ps, const std::vector<int>& members) {
+  g->p = ps[members[0]];
+  g->members = members;
+  g->R = g->p.nr_max; g->Nm = g->p.nm_max; g->M = g->Nm + 1; g->P = 3 * g->Nm;
+  g->B = (int)members.size();
+  if (scheme_weights(g->p.scheme_type, g->p.scheme_imp, g->p.scheme_exp, &g->sch) != 0)
+    return fail(FALCON_EINVAL, "unsupported scheme");
+  int rc;
+  if ((rc = build_opset(key_of(g->p, g->sch), &g->ops))) return rc;
+  if ((rc = make_fft(g->P, &g->fft))) return rc;
+  const size_t n = g->nel();
+  const int R = g->R, B = g->B;
+  if (g->p.scheme_type == FALCON_IMEX) {
+    for (int i = 0; i < g->sch.n_imp; ++i) {
+      if ((rc = g->alloc(&g->th[i], n)) || (rc = g->alloc(&g->wh[i], n)) ||
+          (rc = g->alloc(&g->ubh[i], (size_t)R * B)))
+        return rc;
+    }
+    for (int i = 0; i < g->sch.n_exp; ++i) {
+      if ((rc = g->alloc(&g->nth[i], n)) || (rc = g->alloc(&g->nwh[i], n)) ||
+          (rc = g->alloc(&g->uromh[i], (size_t)R * B)))
+        return rc;
+    }
+  } else {
+    if ((rc = g->alloc(&g->th[0], n)) || (rc = g->alloc(&g->wh[0], n))) return rc;
+    for (int i = 0; i < g->sch.n_exp; ++i) {
+      if ((rc = g->alloc(&g->fat[i], n)) || (rc = g->alloc(&g->fdt[i], n)) || (rc = g->alloc(&g->faw[i], n)) ||
+          (rc = g->alloc(&g->fdw[i], n)) || (rc = g->alloc(&g->buo[i], n)))
+        return rc;
+    }
+    if ((rc = g->alloc(&g->t0, n)) || (rc = g->alloc(&g->w0, n)) || (rc = g->alloc(&g->u0, (size_t)R * B)))
+      return rc;
+  }
+  if ((rc = g->alloc(&g->up, n)) || (rc = g->alloc(&g->ur, n)) || (rc = g->alloc(&g->psi, n)) ||
+      (rc = g->alloc(&g->ntp, n)) || (rc = g->alloc(&g->ntr, n)) || (rc = g->alloc(&g->nwp, n)) ||
+      (rc = g->alloc(&g->nwr, n)) || (rc = g->alloc(&g->dntr, n)) || (rc = g->alloc(&g->dnwr, n)) ||
+      (rc = g->alloc(&g->lt, n)) || (rc = g->alloc(&g->lw, n)) || (rc = g->alloc(&g->lu0, (size_t)R * B)) ||
+      (rc = g->alloc(&g->rhs_t, n)) || (rc = g->alloc(&g->rhs_w, n)) ||
+      (rc = g->alloc(&g->ub2, (size_t)2 * R * B)) || (rc = g->alloc(&g->ra_pr, (size_t)B)))
+    return rc;
+  g->ub = reinterpret_cast<double*>(g->ub2);
+  g->ra_pr_h.resize(B);
+  for (int i = 0; i < B; ++i) g->ra_pr_h[i] = ps[members[i]].ra / ps[members[i]].pr;
+  CK(cudaMemcpy(g->ra_pr, g->ra_pr_h.data(), sizeof(double) * B, cudaMemcpyHostToDevice));
+  CK(cudaMallocHost(&g->stage_buf, sizeof(double2) * (size_t)g->M * R * 2));
+  return 0;
+}
+
+// Radial GEMM over all modes and instances: Y = A (R x R) * X (R x 2MB).
+GemmArgs radial(const double* A, const double2* X, double2* Y, int R, int M, int B) {
+  GemmArgs g{};
+  g.A = A; g.lda = R;
+  g.X = reinterpret_cast<const double*>(X); g.ldx = 2L * M * B;
+  g.Y = reinterpret_cast<double*>(Y); g.ldy = 2L * M * B;
+  g.K = R; g.rows = R; g.N = 2 * M * B; g.batch = 1; g.alpha = 1.0;
+  return g;
+}
+
+// Per-mode GEMM over modes [m0, m0+nm): Y[:, m, :] = A_m(rows x R) X[:, m, :].
+GemmArgs per_mode(const double* A, long lda, long sA, const double2* X, double2* Y, int R, int M, int B,
+                  int m0, int nm, int rows) {
+  GemmArgs g{};
+  g.A = A + (size_t)m0 * sA; g.lda = lda; g.sA = sA;
+  g.X = reinterpret_cast<const double*>(X) + 2L * m0 * B; g.ldx = 2L * M * B; g.sX = 2L * B;
+  g.Y = reinterpret_cast<double*>(Y) + 2L * m0 * B; g.ldy = 2L * M * B; g.sY = 2L * B;
+  g.K = R; g.rows = rows; g.N = 2 * B; g.batch = nm; g.alpha = 1.0;
+  return g;
+}
+
+int run_nonlin(Group* g) {
+  NonlinArgs a{};
+  a.R = g->R; a.M = g->M; a.B = g->B; a.Nm = g->Nm;
+  a.plan = g->fft->plan; a.tw = g->fft->tw; a.pos = g->fft->pos;
+  a.t = g->T(); a.w = g->W(); a.up = g->up; a.ur = g->ur;
+  a.ntp = g->ntp; a.ntr = g->ntr; a.nwp = g->nwp; a.nwr = g->nwr;
+  a.umax = nullptr;
+  CK(launch_nonlin(a, g->stream));
+  return 0;
+}
+
+// The implicit solves shared by IMEX and IMEXRK: temperature, then
+// buoyancy, then (omega, psi, u_phi) for m >= 1 and uphi_bar for m = 0.
+int solve_all(Group* g, double2* t_out, double2* w_out, double buo_scale, double2* buo_store,
+              double* ubar_store) {
+  const int R = g->R, M = g->M, B = g->B;
+  OpSet* o = g->ops.get();
+  cudaStream_t s = g->stream;
+  CK(launch_gemm(per_mode(o->ST, R, (long)R * R, g->rhs_t, t_out, R, M, B, 0, M, R), s));
+  CK(launch_add_buoyancy(R, M, B, o->inv_r, g->ra_pr, buo_scale, t_out, g->rhs_w, buo_store, s));
+  if (M > 1) {
+    const long sG = 3L * R * R;
+    CK(launch_gemm(per_mode(o->G, 3 * R, sG, g->rhs_w, w_out, R, M, B, 1, M - 1, R), s));
+    CK(launch_gemm(per_mode(o->G + R, 3 * R, sG, g->rhs_w, g->psi, R, M, B, 1, M - 1, R), s));
+    CK(launch_gemm(per_mode(o->G + 2 * R, 3 * R, sG, g->rhs_w, g->up, R, M, B, 1, M - 1, R), s));
+  }
+  GemmArgs gu{};
+  gu.A = o->U; gu.lda = 2 * R;
+  gu.X = reinterpret_cast<const double*>(g->rhs_w); gu.ldx = 2L * M * B;
+  gu.Y = g->ub; gu.ldy = 2L * B;
+  gu.K = R; gu.rows = 2 * R; gu.N = 2 * B; gu.batch = 1; gu.alpha = 1.0;
+  CK(launch_gemm(gu, s));
+  CK(launch_post_w(R, M, B, o->inv_r, g->psi, g->ur, g->up, w_out, g->ub, ubar_store, s));
+  return 0;
+}
+
+int step_imex(Group* g) {
+  const int R = g->R, M = g->M, B = g->B;
+  const size_t n = g->nel();
+  OpSet* o = g->ops.get();
+  cudaStream_t s = g->stream;
+  const Scheme& sc = g->sch;
+  const int nstep = g->n_step + 1;
+  int rc;
+  if (nstep > 1) {
+    if ((rc = run_nonlin(g))) return rc;
+  } else {
+    CK(cudaMemsetAsync(g->ntp, 0, sizeof(double2) * n, s));
+    CK(cudaMemsetAsync(g->ntr, 0, sizeof(double2) * n, s));
+    CK(cudaMemsetAsync(g->nwp, 0, sizeof(double2) * n, s));
+    CK(cudaMemsetAsync(g->nwr, 0, sizeof(double2) * n, s));
+  }
+  CK(launch_gemm(radial(o->D1p, g->ntr, g->dntr, R, M, B), s));
+  CK(launch_gemm(radial(o->D1p, g->nwr, g->dnwr, R, M, B), s));
+  const bool cn = (sc.imp == FALCON_IMP_CN);
+  if (cn) {
+    CK(launch_gemm(radial(o->Lp, g->T(), g->lt, R, M, B), s));
+    CK(launch_gemm(radial(o->Lp, g->W(), g->lw, R, M, B), s));
+    GemmArgs gl = radial(o->Lp, g->up, g->lu0, R, M, B);
+    gl.N = 2 * B; gl.ldy = 2L * B;
+    CK(launch_gemm(gl, s));
+  }
+  const int ni = sc.n_imp, ne = sc.n_exp;
+  const int he_new = (g->head_e + ne - 1) % ne;
+  const int h_new = (g->head + ni - 1) % ni;
+  RhsArgs a{};
+  a.R = R; a.M = M; a.B = B;
+  a.inv_r = o->inv_r; a.inv_r2 = o->inv_r2; a.ra_pr = g->ra_pr;
+  a.dt = g->p.dt; a.inv_pr = 1.0 / g->p.pr;
+  a.scheme_cn = cn ? 1 : 0;
+  a.n_imp = ni; a.n_exp = ne; a.wt_lhs = sc.wt_lhs;
+  for (int i = 0; i < 4; ++i) { a.w_imp[i] = sc.w_imp[i]; a.w_exp[i] = sc.w_exp[i]; }
+  for (int i = 0; i < ni; ++i) {
+    a.th[i] = g->th[(g->head + i) % ni];
+    a.wh[i] = g->wh[(g->head + i) % ni];
+    a.ubh[i] = g->ubh[(g->head + i) % ni];
+  }
+  a.nt_new = g->nth[he_new]; a.nw_new = g->nwh[he_new]; a.urom_new = g->uromh[he_new];
+  for (int i = 0; i < ne; ++i) {
+    a.nth[i] = g->nth[(he_new + i) % ne];
+    a.nwh[i] = g->nwh[(he_new + i) % ne];
+    a.uromh[i] = g->uromh[(he_new + i) % ne];
+  }
+  a.ntp = g->ntp; a.ntr = g->ntr; a.dntr = g->dntr; a.nwp = g->nwp; a.nwr = g->nwr; a.dnwr = g->dnwr;
+  a.lt = g->lt; a.lw = g->lw; a.lu0 = g->lu0;
+  a.rhs_t = g->rhs_t; a.rhs_w = g->rhs_w;
+  CK(launch_imex_rhs(a, s));
+  const double buo_scale = g->p.dt * (cn ? 0.5 : sc.wt_lhs);
+  if ((rc = solve_all(g, g->th[h_new], g->wh[h_new], buo_scale, nullptr, g->ubh[h_new]))) return rc;
+  g->head = h_new;
+  g->head_e = he_new;
+  g->n_step = nstep;
+  g->tot_time += g->p.dt;
+  return 0;
+}
+
+int step_imexrk(Group* g) {
+  const int R = g->R, M = g->M, B = g->B;
+  const size_t n = g->nel();
+  OpSet* o = g->ops.get();
+  cudaStream_t s = g->stream;
+  const Scheme& sc = g->sch;
+  const int ns = sc.n_exp;
+  const int nstep = g->n_step + 1;
+  const bool sa = sc.check_A && sc.check_D;
+  int rc;
+  StageArgs a{};
+  a.R = R; a.M = M; a.B = B;
+  a.inv_r = o->inv_r; a.inv_r2 = o->inv_r2; a.ra_pr = g->ra_pr;
+  a.dt = g->p.dt; a.inv_pr = 1.0 / g->p.pr; a.buo_imp = g->p.buo_imp;
+  a.t0 = g->t0; a.w0 = g->w0; a.u0 = g->u0;
+  for (int i = 0; i < ns; ++i) {
+    a.fat[i] = g->fat[i]; a.fdt[i] = g->fdt[i]; a.faw[i] = g->faw[i]; a.fdw[i] = g->fdw[i]; a.buo[i] = g->buo[i];
+  }
+  a.rhs_t = g->rhs_t; a.rhs_w = g->rhs_w;
+  a.ntp = g->ntp; a.ntr = g->ntr; a.dntr = g->dntr; a.nwp = g->nwp; a.nwr = g->nwr; a.dnwr = g->dnwr;
+  a.lt = g->lt; a.lw = g->lw; a.lu0 = g->lu0; a.t = g->T(); a.w = g->W(); a.up = g->up;
+  for (int st = 0; st < ns; ++st) {
+    a.st = st;
+    for (int i = 0; i < kMaxStages; ++i) { a.aD[i] = sc.aD[st][i]; a.aA[i] = sc.aA[st][i]; }
+    a.aD_ss = sc.aD[st][st];
+    if (st > 0) {
+      CK(launch_stage_rhs(a, s));
+      const double scale = g->p.buo_imp ? g->p.dt * sc.aD[st][st] : 0.0;
+      if ((rc = solve_all(g, g->T(), g->W(), scale, g->buo[st], nullptr))) return rc;
+    }
+    double colsum = 0.0;
+    for (int i = 0; i < ns; ++i) colsum += sc.aA[i][st];
+    if ((nstep > 1 || st > 0) && (colsum + sc.bA[st] != 0.0)) {
+      if ((rc = run_nonlin(g))) return rc;
+    } else if (nstep == 1 && st == 0) {
+      CK(cudaMemsetAsync(g->ntp, 0, sizeof(double2) * n, s));
+      CK(cudaMemsetAsync(g->ntr, 0, sizeof(double2) * n, s));
+      CK(cudaMemsetAsync(g->nwp, 0, sizeof(double2) * n, s));
+      CK(cudaMemsetAsync(g->nwr, 0, sizeof(double2) * n, s));
+    }
+    if (sa && st == ns - 1) break;  // last-stage derivatives are unused by the SA assembly
+    CK(launch_gemm(radial(o->D1p, g->ntr, g->dntr, R, M, B), s));
+    CK(launch_gemm(radial(o->D1p, g->nwr, g->dnwr, R, M, B), s));
+    CK(launch_gemm(radial(o->Lp, g->T(), g->lt, R, M, B), s));
+    CK(launch_gemm(radial(o->Lp, g->W(), g->lw, R, M, B), s));
+    GemmArgs gl = radial(o->Lp, g->up, g->lu0, R, M, B);
+    gl.N = 2 * B; gl.ldy = 2L * B;
+    CK(launch_gemm(gl, s));
+    a.fat_out = g->fat[st]; a.fdt_out = g->fdt[st]; a.faw_out = g->faw[st]; a.fdw_out = g->fdw[st];
+    a.buo_out = (st == 0) ? g->buo[0] : nullptr;
+    CK(launch_stage_deriv(a, s));
+  }
+  // Assembly_stage_SA (src/fourierloop_imexrk.F90:653-665)
+  CK(cudaMemcpyAsync(g->t0, g->T(), sizeof(double2) * n, cudaMemcpyDeviceToDevice, s));
+  CK(cudaMemcpyAsync(g->w0, g->W(), sizeof(double2) * n, cudaMemcpyDeviceToDevice, s));
+  CK(launch_extract_mode0(R, M, B, g->up, g->u0, s));
+  g->n_step = nstep;
+  g->tot_time += g->p.dt;
+  return 0;
+}
+
+int group_step(Group* g) {
+  return g->p.scheme_type == FALCON_IMEX ? step_imex(g) : step_imexrk(g);
+}
+
+// After a state is loaded: histories zeroed, current slot = state,
+// Y0 = state (src/init.F90:393-395, src/timeschemes.F90:51-53).
+int group_reset(Group* g) {
+  const int R = g->R, M = g->M, B = g->B;
+  const size_t n = g->nel();
+  cudaStream_t s = g->stream;
+  g->n_step = 0;
+  g->tot_time = 0.0;
+  if (g->p.scheme_type == FALCON_IMEX) {
+    const int ni = g->sch.n_imp, ne = g->sch.n_exp;
+    for (int i = 0; i < ni; ++i)
+      if (i != g->head) {
+        CK(cudaMemsetAsync(g->th[i], 0, sizeof(double2) * n, s));
+        CK(cudaMemsetAsync(g->wh[i], 0, sizeof(double2) * n, s));
+        CK(cudaMemsetAsync(g->ubh[i], 0, sizeof(double) * R * B, s));
+      }
+    CK(launch_extract_mode0(R, M, B, g->up, g->ubh[g->head], s));
+    for (int i = 0; i < ne; ++i) {
+      CK(cudaMemsetAsync(g->nth[i], 0, sizeof(double2) * n, s));
+      CK(cudaMemsetAsync(g->nwh[i], 0, sizeof(double2) * n, s));
+      CK(cudaMemsetAsync(g->uromh[i], 0, sizeof(double) * R * B, s));
+    }
+  } else {
+    CK(cudaMemcpyAsync(g->t0, g->T(), sizeof(double2) * n, cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(g->w0, g->W(), sizeof(double2) * n, cudaMemcpyDeviceToDevice, s));
+    CK(launch_extract_mode0(R, M, B, g->up, g->u0, s));
+    for (int i = 0; i < g->sch.n_exp; ++i) {
+      CK(cudaMemsetAsync(g->fat[i], 0, sizeof(double2) * n, s));
+      CK(cudaMemsetAsync(g->fdt[i], 0, sizeof(double2) * n, s));
+      CK(cudaMemsetAsync(g->faw[i], 0, sizeof(double2) * n, s));
+      CK(cudaMemsetAsync(g->fdw[i], 0, sizeof(double2) * n, s));
+      CK(cudaMemsetAsync(g->buo[i], 0, sizeof(double2) * n, s));
+    }
+  }
+  CK(cudaMemsetAsync(g->psi, 0, sizeof(double2) * n, s));
+  return 0;
+}
+
+// Upload one instance's Fortran-layout fields (host) into the group.
+int group_set_instance(Group* g, int b, const double* t, const double* w, const double* up, const double* ur) {
+  const int R = g->R, M = g->M, B = g->B;
+  const size_t nb = sizeof(double2) * (size_t)M * R;
+  double2* d = nullptr;
+  CK(cudaMallocAsync(&d, nb, g->stream));
+  const double* src[4] = {t, w, up, ur};
+  double2* dst[4] = {g->T(), g->W(), g->up, g->ur};
+  for (int f = 0; f < 4; ++f) {
+    if (src[f]) {
+      std::memcpy(g->stage_buf, src[f], nb);
+      CK(cudaMemcpyAsync(d, g->stage_buf, nb, cudaMemcpyHostToDevice, g->stream));
+    } else {
+      CK(cudaMemsetAsync(d, 0, nb, g->stream));
+    }
+    CK(launch_scatter_instance(R, M, B, b, d, dst[f], g->stream));
+    CK(cudaStreamSynchronize(g->stream));
+  }
+  CK(cudaFreeAsync(d, g->stream));
+  return 0;
+}
+
+int group_get_instance(Group* g, int b, double* t, double* w, double* up, double* ur, double* psi) {
+  const int R = g->R, M = g->M, B = g->B;
+  const size_t nb = sizeof(double2) * (size_t)M * R;
+  double2* d = nullptr;
+  CK(cudaMallocAsync(&d, nb, g->stream));
+  double* dst[5] = {t, w, up, ur, psi};
+  const double2* src[5] = {g->T(), g->W(), g->up, g->ur, g->psi};
+  for (int f = 0; f < 5; ++f) {
+    if (!dst[f]) continue;
+    CK(launch_gather_instance(R, M, B, b, src[f], d, g->stream));
+    CK(cudaMemcpyAsync(g->stage_buf, d, nb, cudaMemcpyDeviceToHost, g->stream));
+    CK(cudaStreamSynchronize(g->stream));
+    std::memcpy(dst[f], g->stage_buf, nb);
+  }
+  CK(cudaFreeAsync(d, g->stream));
+  CK(cudaStreamSynchronize(g->stream));
+  return 0;
+}
+
+// Repack the instance columns of every per-instance array: slot j of the
+// new layout takes old slot map[j] (or zeros when map[j] < 0).
+int group_resize(Group* g, const std::vector<int>& map) {
+  const int Bn = (int)map.size();
+  int* dmap = nullptr;
+  CK(cudaMalloc(&dmap, sizeof(int) * std::max(Bn, 1)));
+  CK(cudaMemcpy(dmap, map.data(), sizeof(int) * Bn, cudaMemcpyHostToDevice));
+  size_t bytes = 0;
+  for (auto& f : g->fields) {
+    double* old = reinterpret_cast<double*>(*f.ptr);
+    double* nw = nullptr;
+    const size_t n = f.rows * (size_t)std::max(Bn, 1) * f.ew;
+    CK(cudaMalloc(&nw, sizeof(double) * n));
+    CK(launch_remap_cols(old, nw, f.rows, g->B, Bn, f.ew, dmap, g->stream));
+    CK(cudaStreamSynchronize(g->stream));
+    for (auto& a : g->allocs)
+      if (a == old) a = nw;
+    cudaFree(old);
+    *f.ptr = nw;
+    bytes += sizeof(double) * f.rows * (size_t)Bn * f.ew;
+  }
+  cudaFree(dmap);
+  g->ub = reinterpret_cast<double*>(g->ub2);
+  std::vector<double> ra(Bn, 0.0);
+  for (int j = 0; j < Bn; ++j) ra[j] = map[j] >= 0 ? g->ra_pr_h[map[j]] : 0.0;
+  g->ra_pr_h = ra;
+  g->B = Bn;
+  g->bytes = bytes;
+  return 0;
+}
+
+// Per-instance fresh start (the column of `b`): histories zeroed, current
+// slot and Y0 from the state (the group-wide counterpart is group_reset).
+int group_reset_instance(Group* g, int b) {
+  const int R = g->R, M = g->M, B = g->B;
+  std::vector<int> keep(B);
+  for (int j = 0; j < B; ++j) keep[j] = (j == b) ? -1 : j;
+  int* dmap = nullptr;
+  CK(cudaMalloc(&dmap, sizeof(int) * B));
+  CK(cudaMemcpy(dmap, keep.data(), sizeof(int) * B, cudaMemcpyHostToDevice));
+  auto zero_col = [&](void* q, size_t rows, int ew) -> int {
+    // in-place remap keeps other columns and zeroes column b
+    CK(launch_remap_cols(reinterpret_cast<double*>(q), reinterpret_cast<double*>(q), rows, B, B, ew, dmap, g->stream));
+    return 0;
+  };
+  const size_t n = (size_t)R * M;
+  int rc = 0;
+  if (g->p.scheme_type == FALCON_IMEX) {
+    for (int i = 0; i < g->sch.n_imp; ++i)
+      if (i != g->head) {
+        if ((rc = zero_col(g->th[i], n, 2)) || (rc = zero_col(g->wh[i], n, 2)) || (rc = zero_col(g->ubh[i], R, 1)))
+          break;
+      }
+    for (int i = 0; !rc && i < g->sch.n_exp; ++i)
+      if ((rc = zero_col(g->nth[i], n, 2)) || (rc = zero_col(g->nwh[i], n, 2)) || (rc = zero_col(g->uromh[i], R, 1)))
+        break;
+  } else {
+    for (int i = 0; !rc && i < g->sch.n_exp; ++i)
+      if ((rc = zero_col(g->fat[i], n, 2)) || (rc = zero_col(g->fdt[i], n, 2)) || (rc = zero_col(g->faw[i], n, 2)) ||
+          (rc = zero_col(g->fdw[i], n, 2)) || (rc = zero_col(g->buo[i], n, 2)))
+        break;
+  }
+  CK(cudaStreamSynchronize(g->stream));
+  cudaFree(dmap);
+  if (rc) return rc;
+  // current-slot uphi_bar and Y0 for every column (unchanged columns rewrite
+  // their own values)
+  if (g->p.scheme_type == FALCON_IMEX) {
+    CK(launch_extract_mode0(R, M, B, g->up, g->ubh[g->head], g->stream));
+  } else {
+    CK(launch_extract_mode0(R, M, B, g->up, g->u0, g->stream));
+    const size_t bytes2 = sizeof(double2);
+    // Y0 of column b from the state: gather/scatter through the staging path
+    double2* tmp = nullptr;
+    CK(cudaMalloc(&tmp, bytes2 * n));
+    CK(launch_gather_instance(R, M, B, b, g->T(), tmp, g->stream));
+    CK(launch_scatter_instance(R, M, B, b, tmp, g->t0, g->stream));
+    CK(launch_gather_instance(R, M, B, b, g->W(), tmp, g->stream));
+    CK(launch_scatter_instance(R, M, B, b, tmp, g->w0, g->stream));
+    CK(cudaStreamSynchronize(g->stream));
+    cudaFree(tmp);
+  }
+  CK(cudaStreamSynchronize(g->stream));
+  return 0;
+}
+
+// Seeded noise (host): splitmix64 keyed by (seed, m, i), Box-Muller in FP64.
+uint64_t splitmix64(uint64_t* x) {
+  uint64_t z = (*x += 0x9E3779B97F4A7C15ull);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+void noise_pair(uint64_t seed, int m, int i, double* a, double* b) {
+  uint64_t st = seed * 0xD1B54A32D192ED03ull ^ ((uint64_t)(unsigned)m << 32) ^ (uint64_t)(unsigned)i;
+  splitmix64(&st);
+  const double u1 = ((double)(splitmix64(&st) >> 11) + 1.0) * (1.0 / 9007199254740992.0);
+  const double u2 = (double)(splitmix64(&st) >> 11) * (1.0 / 9007199254740992.0);
+  const double rad = std::sqrt(-2.0 * std::log(u1));
+  const double ang = 2.0 * (4.0 * std::atan(1.0)) * u2;
+  *a = rad * std::cos(ang);
+  *b = rad * std::sin(ang);
+}
+
+// Host restatement of forfft (src/fourier_fftw.F90:39-57) by the direct sum,
+// used once for the reference-style initial perturbation.
+void host_forfft(int nm, int np, const double* ff, double* f) {
+  const double two_pi = 8.0 * std::atan(1.0);
+  for (int m = 0; m <= nm; ++m) {
+    double sr = 0.0, si = 0.0;
+    for (int j = 0; j < np; ++j) {
+      const long idx = ((long)m * j) % np;
+      const double a = two_pi * (double)idx / (double)np;
+      sr += ff[j] * std::cos(a);
+      si -= ff[j] * std::sin(a);
+    }
+    f[2 * m] = sr / (double)np;
+    f[2 * m + 1] = si / (double)np;
+  }
+}
+
+// Initial temperature of one instance in Fortran layout (M,R) complex.
+void initial_temperature(const falcon_params& p, int kind, double amp, uint64_t seed, std::vector<double>& tFR) {
+  const int R = p.nr_max, Nm = p.nm_max, M = Nm + 1, P = 3 * Nm;
+  Cheb c = make_cheb(R, p.eta);
+  tFR.assign((size_t)2 * M * R, 0.0);
+  const double lrr = std::log(c.rmin / c.rmax), lrmax = std::log(c.rmax);
+  const double pi = 4.0 * std::atan(1.0);
+  if (kind == 1) {
+    for (int r = 0; r < R; ++r) {
+      tFR[2 * ((size_t)M * r)] = std::log(c.radius[r]) / lrr - lrmax / lrr;
+      if (r == 0 || r == R - 1) continue;
+      for (int m = 1; m <= Nm; ++m) {
+        double a, b;
+        noise_pair(seed, m, r, &a, &b);
+        tFR[2 * ((size_t)m + (size_t)M * r)] = amp * a;
+        tFR[2 * ((size_t)m + (size_t)M * r) + 1] = amp * b;
+      }
+    }
+    return;
+  }
+  // init_perturbation (src/init.F90:277-399)
+  std::vector<double> tt(P), phi(P, 0.0);
+  for (int j = 1; j < P; ++j) phi[j] = phi[j - 1] + 2.0 * pi / (double)P;
+  std::vector<double> gasp(R, 0.0);
+  if (p.n_init == 0) {
+    auto gm = [&](double r, double cc, double L) {
+      return pi / 3.0 * L * r * (r + 3.0 * L) * std::exp(-r / L) +
+             (2.0 * pi * L * L * (cc + L) * (cc + L)) / r * std::exp(-2.0 * cc / L) *
+                 (1.0 - (1.0 - r / (cc + L)) * std::exp(r / L)) +
+             pi * L * L * L * (std::exp(-r / L) - std::exp((r - 2.0 * cc) / L));
+    };
+    auto ge = [&](double r, double cc, double L) {
+      return 2.0 * pi * L / r * std::exp(-r / L) *
+             (0.5 * (r * (r + L) * (2.0 * cc - r)) + 1.0 / 3.0 * ((r - cc) * (r - cc) * (r - cc) - cc * cc * cc) -
+              L * (cc + L) * (r - cc + L) + L * (cc + L) * (cc + L) * std::exp((r - 2.0 * cc) / L));
+    };
+    auto gc = [&](double cc, double L) {
+      return pi * L * L * L * (1.0 - std::exp(-2.0 * cc / L)) - 2.0 * pi * cc * L * (cc + L) * std::exp(-2.0 * cc / L);
+    };
+    const double sigma_r = 0.1 / std::sqrt(2.0), sigma_p = 0.2;
+    double rc = 0.5 * (c.rmax + c.rmin);
+    int ir = 0;
+    double best = std::fabs(c.radius[0] - rc);
+    for (int i = 1; i < R; ++i)
+      if (std::fabs(c.radius[i] - rc) < best) { best = std::fabs(c.radius[i] - rc); ir = i; }
+    rc = c.radius[ir];
+    const double c1 = 0.5 * (c.radius[R - 1] - rc), c2 = 0.5 * (rc - c.radius[0]), L = 0.5 * sigma_r;
+    for (int i = 0; i < R; ++i) {
+      const double rr = c.radius[i];
+      if (i == ir) gasp[i] = 1.0;
+      else if (rr < rc - c2) gasp[i] = ge(rc - rr, c2, L);
+      else if (rr >= rc - c2 && rr < rc) gasp[i] = gm(rc - rr, c2, L);
+      else if (rr > rc && rr <= rc + c1) gasp[i] = gm(rr - rc, c1, L);
+      else if (rr > rc + c1) gasp[i] = ge(rr - rc, c1, L);
+    }
+    for (int i = 0; i < R; ++i) {
+      if (i < ir) gasp[i] = gasp[i] / gc(c1, L);
+      else if (i > ir) gasp[i] = gasp[i] / gc(c2, L);
+    }
+    for (int r = 0; r < R; ++r) {
+      const double c_r = amp * gasp[r];
+      const double tcon = std::log(c.radius[r]) / lrr - lrmax / lrr;
+      for (int j = 0; j < P; ++j) {
+        const double ph = (double)j * 2.0 * pi / (double)P;
+        tt[j] = c_r * std::exp(-(ph - pi) * (ph - pi) / (sigma_p * sigma_p)) + tcon;
+      }
+      host_forfft(Nm, P, tt.data(), &tFR[(size_t)2 * M * r]);
+    }
+  } else {
+    for (int r = 0; r < R; ++r) {
+      const double tcon = std::log(c.radius[r]) / lrr - lrmax / lrr;
+      const double rad = c.radius[r];
+      for (int j = 0; j < P; ++j) {
+        if (p.n_init < 0) {
+          const double sp = 0.25, sr = 0.25, rmid = c.rmax - (c.rmax - c.rmin) / 2.0;
+          if (phi[j] > 1.0 && phi[j] < 3.0)
+            tt[j] = -1.0 * (c.rmax - rad) * (c.rmin - rad) * amp * (1.0 / (2.0 * pi * sp * sr)) *
+                        std::exp(-1.0 * ((rad - rmid) * (rad - rmid) / (sr * sr) + (phi[j] - 2.0) * (phi[j] - 2.0) / (sp * sp))) +
+                    tcon;
+          else
+            tt[j] = tcon;
+        } else {
+          tt[j] = amp * (c.rmax - rad) * (c.rmin - rad) * std::cos((double)p.n_init * phi[j]) + tcon;
+        }
+      }
+      host_forfft(Nm, P, tt.data(), &tFR[(size_t)2 * M * r]);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// writeKE_spectral (src/output.F90:122-324) evaluated on the host from the
+// downloaded state of one instance.
+// ---------------------------------------------------------------------------
+double radint(const Cheb& c, const std::vector<double>& f) {
+  // radInt (src/integ.F90:36-76): chebtransform of f*r, Clenshaw-Curtis weights
+  const int R = c.R;
+  std::vector<double> ff(R), ft(R);
+  for (int i = 0; i < R; ++i) ff[i] = f[i] * c.radius[i];
+  const double fac = std::sqrt(2.0 / (double)(R - 1));
+  for (int k = 0; k < R; ++k) {
+    double s = 0.0;
+    for (int i = 0; i < R; ++i) {
+      const double cp = (i == 0 || i == R - 1) ? 1.0 : 2.0;
+      s += cp * ff[i] * c.t[i + (size_t)R * k];
+    }
+    ft[k] = s / ((double)(R - 1) * fac);
+  }
+  double tot = 0.0;
+  for (int i = 0; i < R; ++i) {
+    const double Qm = (i % 2 == 0) ? -1.0 / (double)(i * i - 1) : 0.0;
+    tot += ((i == 0 || i == R - 1) ? 0.5 : 1.0) * ft[i] * Qm;
+  }
+  return fac * tot;
+}
+
+void diagnostics_host(const falcon_params& p, double time, const double* t, const double* w,
+                      const double* up, const double* ur, const std::vector<double>* tgrid_mean_urt,
+                      falcon_diag* out) {
+  const int R = p.nr_max, M = p.nm_max + 1;
+  Cheb c = make_cheb(R, p.eta);
+  const double pi = 4.0 * std::atan(1.0);
+  std::vector<double> ur2(R), up2(R), upb2(R), w2(R), urt(R, 0.0);
+  for (int j = 0; j < R; ++j) {
+    double a = 0.0, b = 0.0, ww = 0.0;
+    for (int m = 0; m < M; ++m) {
+      const double* u = &ur[2 * ((size_t)m + (size_t)M * j)];
+      const double* v = &up[2 * ((size_t)m + (size_t)M * j)];
+      const double* o = &w[2 * ((size_t)m + (size_t)M * j)];
+      a += u[0] * u[0] + u[1] * u[1];
+      b += v[0] * v[0] + v[1] * v[1];
+      if (m == 0) ww += o[0] * o[0] - o[1] * o[1];
+      else ww += 2.0 * (o[0] * o[0] + o[1] * o[1]);
+    }
+    ur2[j] = a; up2[j] = b; w2[j] = ww;
+    const double upavg = up[2 * ((size_t)M * j)];
+    upb2[j] = upavg * upavg;
+    if (tgrid_mean_urt) urt[j] = (*tgrid_mean_urt)[j];
+  }
+  const double urk = radint(c, ur2), upk = radint(c, up2), upbk = radint(c, upb2);
+  out->time = time;
+  out->dt = p.dt;
+  out->ke = 2.0 * pi * (urk + upk);
+  out->ke_r = 2.0 * pi * urk;
+  out->ke_phi = 2.0 * pi * upk;
+  out->ke_upbar = 2.0 * pi * upbk;
+  // Nusselt from dT0/dr at the walls (src/output.F90:259-265)
+  std::vector<double> d1p, lp;
+  phys_deriv(c, d1p, lp);
+  double d0 = 0.0, dR = 0.0;
+  for (int k = 0; k < R; ++k) {
+    const double T0 = t[2 * ((size_t)M * k)];
+    d0 += d1p[0 + (size_t)R * k] * T0;
+    dR += d1p[R - 1 + (size_t)R * k] * T0;
+  }
+  const double eta = p.eta;
+  out->nu_bot = d0 / ((1.0 - eta) / (eta * std::log(eta)));
+  out->nu_top = dR / ((1.0 - eta) / (std::log(eta)));
+  const double vis1 = radint(c, w2);
+  if (p.mbc == 1) out->vis = 2.0 * pi * vis1 - (4.0 * pi * 2.0 * up2[R - 1] - 4.0 * pi * 2.0 * up2[0]);
+  else out->vis = 2.0 * pi * vis1;
+  out->buo = 2.0 * pi * p.ra / p.pr * radint(c, urt);
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Batches
+// ---------------------------------------------------------------------------
+struct falcon_batch {
+  std::vector<falcon_params> params;
+  std::vector<std::unique_ptr<Group>> groups;
+  std::vector<std::pair<int, int>> where;  // instance -> (group, slot)
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  ~falcon_batch() {
+    groups.clear();
+    if (own_stream && stream) cudaStreamDestroy(stream);
+  }
+};
+
+struct falcon_handle {
+  falcon_batch* b = nullptr;
+};
+
+static int batch_create(const falcon_params* ps, int n, falcon_batch** out) {
+  if (!ps || n <= 0 || !out) return fail(FALCON_EINVAL, "invalid batch arguments");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+    return fail(FALCON_ECUDA, "no CUDA device: the GB300 library has no CPU fallback");
+  CK(init_dft_tables());
+  std::unique_ptr<falcon_batch> b(new falcon_batch());
+  b->params.assign(ps, ps + n);
+  for (int i = 0; i < n; ++i) {
+    int rc = validate(ps[i]);
+    if (rc) return rc;
+  }
+  CK(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+  b->own_stream = true;
+  std::map<OpKey, std::vector<int>> byk;
+  for (int i = 0; i < n; ++i) {
+    Scheme s;
+    scheme_weights(ps[i].scheme_type, ps[i].scheme_imp, ps[i].scheme_exp, &s);
+    OpKey k = key_of(ps[i], s);
+    k.wt = k.wt;  // operators shared whenever the key matches (Ra may differ)
+    byk[k].push_back(i);
+  }
+  b->where.resize(n);
+  for (auto& kv : byk) {
+    auto g = std::make_unique<Group>();
+    g->stream = b->stream;
+    int rc = group_init(g.get(), b->params, kv.second);
+    if (rc) return rc;
+    for (size_t j = 0; j < kv.second.size(); ++j) b->where[kv.second[j]] = {(int)b->groups.size(), (int)j};
+    b->groups.push_back(std::move(g));
+  }
+  *out = b.release();
+  return 0;
+}
+
+extern "C" {
+
+const char* falcon_last_error(void) { return g_err.c_str(); }
+const char* falcon_version(void) { return "falcon-gb300 0.1 (sm_103a, FP64)"; }
+
+int falcon_params_default(falcon_params* p) {
+  if (!p) return fail(FALCON_EINVAL, "null params");
+  std::memset(p, 0, sizeof(*p));
+  p->nr_max = 20; p->nm_max = 20;
+  p->eta = 0.35; p->ra = 1000.0; p->pr = 1.0; p->mbc = 1; p->ampT = 0.00001;
+  p->l_add_pert = 0; p->lagpts = 14; p->buo_imp = 1; p->n_init = 0;
+  p->n_time_steps = 100; p->dt = 0.01; p->totaltime = 100.0;
+  p->l_vartimestep = 0; p->l_optimizedt = 0;
+  p->scheme_type = FALCON_IMEXRK; p->scheme_imp = FALCON_IMP_ARS222; p->scheme_exp = FALCON_EXP_ARS222;
+  p->l_imexrk_started = 1; p->dt_coef = 2.0; p->dt_max = 3.e-5; p->cfl = 0.9;
+  p->l_restart = 0; p->n_restart = 0; p->n_restart_point = 0; p->n_snapshot_point = 0;
+  std::strcpy(p->tag, "");
+  p->n_checkpoint = 500000; p->n_snapshot = 300000; p->n_KE = 1; p->n_KEspec = 100000;
+  return 0;
+}
+
+int falcon_params_set_scheme(falcon_params* p, const char* type, const char* imp, const char* exp) {
+  if (!p || !type || !imp || !exp) return fail(FALCON_EINVAL, "null argument");
+  auto up = [](std::string s) {
+    for (auto& ch : s) ch = (char)std::toupper((unsigned char)ch);
+    return s;
+  };
+  const std::string t = up(type), i = up(imp), e = up(exp);
+  if (t == "IMEX") p->scheme_type = FALCON_IMEX;
+  else if (t == "IMEXRK") p->scheme_type = FALCON_IMEXRK;
+  else if (t == "RK") p->scheme_type = FALCON_RK;
+  else return fail(FALCON_EINVAL, "unknown time_scheme_type " + t);
+  static const std::map<std::string, int> imps = {
+      {"CN", FALCON_IMP_CN}, {"BDF2", FALCON_IMP_BDF2}, {"BDF3", FALCON_IMP_BDF3}, {"BDF4", FALCON_IMP_BDF4},
+      {"ARS443", FALCON_IMP_ARS443}, {"ARS343", FALCON_IMP_ARS343}, {"BPR353", FALCON_IMP_BPR353},
+      {"ARS222", FALCON_IMP_ARS222}, {"NONE", FALCON_IMP_NONE}};
+  static const std::map<std::string, int> exps = {
+      {"AB2", FALCON_EXP_AB2}, {"AB3", FALCON_EXP_AB3}, {"AB4", FALCON_EXP_AB4},
+      {"EXPARS443", FALCON_EXP_ARS443}, {"EXPARS343", FALCON_EXP_ARS343}, {"EXPBPR353", FALCON_EXP_BPR353},
+      {"EXPARS222", FALCON_EXP_ARS222}, {"RK2", FALCON_EXP_RK2}, {"RK4", FALCON_EXP_RK4}};
+  auto a = imps.find(i);
+  auto b = exps.find(e);
+  if (a == imps.end()) return fail(FALCON_EINVAL, "unknown time_scheme_imp " + i);
+  if (b == exps.end()) return fail(FALCON_EINVAL, "unknown time_scheme_exp " + e);
+  p->scheme_imp = a->second;
+  p->scheme_exp = b->second;
+  return 0;
+}
+
+// Namelist reader: groups `&name ... /`, entries `key = value` separated by
+// commas or newlines, `!` comments, Fortran logicals and quoted strings.
+int falcon_params_read_namelist(const char* path, falcon_params* p) {
+  if (!path || !p) return fail(FALCON_EINVAL, "null argument");
+  std::ifstream in(path);
+  if (!in) return fail(FALCON_EIO, std::string("Input namelist file not found: ") + path);
+  falcon_params_default(p);
+  std::string text, line;
+  while (std::getline(in, line)) {
+    bool inq = false;
+    char q = 0;
+    for (size_t i = 0; i < line.size(); ++i) {
+      const char ch = line[i];
+      if (inq) { if (ch == q) inq = false; }
+      else if (ch == '"' || ch == '\'') { inq = true; q = ch; }
+      else if (ch == '!') { line = line.substr(0, i); break; }
+    }
+    text += line + "\n";
+  }
+  std::string typ = "IMEXRK", imp = "ARS222", exp = "expARS222";
+  auto lower = [](std::string s) {
+    for (auto& ch : s) ch = (char)std::tolower((unsigned char)ch);
+    return s;
+  };
+  auto trim = [](std::string s) {
+    size_t a = s.find_first_not_of(" \t\r\n,");
+    size_t b = s.find_last_not_of(" \t\r\n,");
+    return a == std::string::npos ? std::string() : s.substr(a, b - a + 1);
+  };
+  auto as_bool = [&](const std::string& v) {
+    std::string s = lower(v);
+    return s == ".true." || s == "t" || s == ".t." || s == "true";
+  };
+  auto as_str = [&](std::string v) {
+    v = trim(v);
+    if (v.size() >= 2 && (v[0] == '"' || v[0] == '\'')) v = v.substr(1, v.size() - 2);
+    return v;
+  };
+  auto as_num = [&](std::string v) {
+    v = trim(v);
+    for (auto& ch : v) if (ch == 'd' || ch == 'D') ch = 'e';
+    return std::strtod(v.c_str(), nullptr);
+  };
+  size_t pos = 0;
+  while ((pos = text.find('&', pos)) != std::string::npos) {
+    size_t end = pos + 1;
+    bool inq = false;
+    char qc = 0;
+    for (; end < text.size(); ++end) {
+      const char ch = text[end];
+      if (inq) { if (ch == qc) inq = false; }
+      else if (ch == '"' || ch == '\'') { inq = true; qc = ch; }
+      else if (ch == '/') break;
+    }
+    std::string body = text.substr(pos + 1, end - pos - 1);
+    pos = end;
+    size_t sp = body.find_first_of(" \t\r\n");
+    body = (sp == std::string::npos) ? std::string() : body.substr(sp);
+    // split into key = value pairs: a key is an identifier followed by '='
+    std::vector<std::pair<std::string, std::string>> kv;
+    size_t i = 0;
+    while (i < body.size()) {
+      size_t eq = body.find('=', i);
+      if (eq == std::string::npos) break;
+      std::string key = lower(trim(body.substr(i, eq - i)));
+      size_t ks = key.find_last_of(" \t\r\n,");
+      if (ks != std::string::npos) key = key.substr(ks + 1);
+      // value runs to the start of the next "ident =" outside quotes
+      size_t j = eq + 1;
+      bool q2 = false;
+      char qq = 0;
+      size_t val_end = body.size();
+      for (; j < body.size(); ++j) {
+        const char ch = body[j];
+        if (q2) { if (ch == qq) q2 = false; continue; }
+        if (ch == '"' || ch == '\'') { q2 = true; qq = ch; continue; }
+        if (ch == '=') {
+          size_t k = j;
+          while (k > eq + 1 && std::isspace((unsigned char)body[k - 1])) --k;
+          while (k > eq + 1 && (std::isalnum((unsigned char)body[k - 1]) || body[k - 1] == '_')) --k;
+          val_end = k;
+          break;
+        }
+      }
+      kv.emplace_back(key, trim(body.substr(eq + 1, val_end - eq - 1)));
+      i = val_end;
+    }
+    for (auto& e : kv) {
+      const std::string& k = e.first;
+      const std::string& v = e.second;
+      if (k == "nr_max") p->nr_max = (int)as_num(v);
+      else if (k == "nm_max") p->nm_max = (int)as_num(v);
+      else if (k == "eta") p->eta = as_num(v);
+      else if (k == "ra") p->ra = as_num(v);
+      else if (k == "pr") p->pr = as_num(v);
+      else if (k == "mbc") p->mbc = (lower(as_str(v)) == "sf") ? 1 : 0;
+      else if (k == "ampt") p->ampT = as_num(v);
+      else if (k == "l_add_pert") p->l_add_pert = as_bool(v);
+      else if (k == "lagpts") p->lagpts = (int)as_num(v);
+      else if (k == "n_init") p->n_init = (int)as_num(v);
+      else if (k == "buo_tscheme") p->buo_imp = (lower(as_str(v)) == "imp") ? 1 : 0;
+      else if (k == "n_time_steps") p->n_time_steps = (int)as_num(v);
+      else if (k == "dt") p->dt = as_num(v);
+      else if (k == "totaltime") p->totaltime = as_num(v);
+      else if (k == "l_vartimestep") p->l_vartimestep = as_bool(v);
+      else if (k == "l_optimizedt") p->l_optimizedt = as_bool(v);
+      else if (k == "time_scheme_type") typ = as_str(v);
+      else if (k == "time_scheme_imp") imp = as_str(v);
+      else if (k == "time_scheme_exp") exp = as_str(v);
+      else if (k == "l_imexrk_started") p->l_imexrk_started = as_bool(v);
+      else if (k == "dt_coef") p->dt_coef = as_num(v);
+      else if (k == "dt_max") p->dt_max = as_num(v);
+      else if (k == "cfl") p->cfl = as_num(v);
+      else if (k == "l_restart") p->l_restart = as_bool(v);
+      else if (k == "n_restart") p->n_restart = (int)as_num(v);
+      else if (k == "n_restart_point") p->n_restart_point = (int)as_num(v);
+      else if (k == "n_snapshot_point") p->n_snapshot_point = (int)as_num(v);
+      else if (k == "tag") std::snprintf(p->tag, sizeof(p->tag), "%s", as_str(v).c_str());
+      else if (k == "n_checkpoint") p->n_checkpoint = (int)as_num(v);
+      else if (k == "n_snapshot") p->n_snapshot = (int)as_num(v);
+      else if (k == "n_ke") p->n_KE = (int)as_num(v);
+      else if (k == "n_kespec") p->n_KEspec = (int)as_num(v);
+    }
+  }
+  return falcon_params_set_scheme(p, typ.c_str(), imp.c_str(), exp.c_str());
+}
+
+int falcon_batch_create(const falcon_params* params, int n, falcon_batch** out) {
+  return batch_create(params, n, out);
+}
+
+void falcon_batch_destroy(falcon_batch* b) {
+  if (b) { cudaStreamSynchronize(b->stream); delete b; }
+}
+
+int falcon_batch_size(const falcon_batch* b) { return b ? (int)b->params.size() : 0; }
+int falcon_batch_ngroups(const falcon_batch* b) { return b ? (int)b->groups.size() : 0; }
+
+size_t falcon_batch_device_bytes(const falcon_batch* b) {
+  if (!b) return 0;
+  size_t s = 0;
+  std::vector<const OpSet*> seen;
+  for (auto& g : b->groups) {
+    s += g->bytes;
+    if (std::find(seen.begin(), seen.end(), g->ops.get()) == seen.end()) {
+      seen.push_back(g->ops.get());
+      s += g->ops->bytes;
+    }
+  }
+  return s;
+}
+
+int falcon_batch_set_stream(falcon_batch* b, void* stream) {
+  if (!b) return fail(FALCON_EINVAL, "null batch");
+  cudaStreamSynchronize(b->stream);
+  if (b->own_stream) cudaStreamDestroy(b->stream);
+  b->own_stream = false;
+  b->stream = (cudaStream_t)stream;
+  for (auto& g : b->groups) g->stream = b->stream;
+  return 0;
+}
+
+int falcon_batch_set_state(falcon_batch* b, int i, const double* tFR, const double* omgFR, const double* upFR,
+                           const double* urFR) {
+  if (!b || i < 0 || i >= (int)b->params.size()) return fail(FALCON_EINVAL, "instance index out of range");
+  Group* g = b->groups[b->where[i].first].get();
+  int rc = group_set_instance(g, b->where[i].second, tFR, omgFR, upFR, urFR);
+  if (rc) return rc;
+  return group_reset(g);
+}
+
+int falcon_batch_init_state(falcon_batch* b, int kind, double amp, const uint64_t* seeds) {
+  if (!b) return fail(FALCON_EINVAL, "null batch");
+  for (size_t i = 0; i < b->params.size(); ++i) {
+    std::vector<double> t;
+    initial_temperature(b->params[i], kind, kind == 1 ? amp : b->params[i].ampT, seeds ? seeds[i] : (uint64_t)i, t);
+    Group* g = b->groups[b->where[i].first].get();
+    int rc = group_set_instance(g, b->where[i].second, t.data(), nullptr, nullptr, nullptr);
+    if (rc) return rc;
+  }
+  for (auto& g : b->groups) {
+    int rc = group_reset(g.get());
+    if (rc) return rc;
+  }
+  CK(cudaStreamSynchronize(b->stream));
+  return 0;
+}
+
+int falcon_batch_get_state(falcon_batch* b, int i, double* tFR, double* omgFR, double* upFR, double* urFR,
+                           double* psi) {
+  if (!b || i < 0 || i >= (int)b->params.size()) return fail(FALCON_EINVAL, "instance index out of range");
+  Group* g = b->groups[b->where[i].first].get();
+  return group_get_instance(g, b->where[i].second, tFR, omgFR, upFR, urFR, psi);
+}
+
+int falcon_batch_step(falcon_batch* b, int nsteps) {
+  if (!b || nsteps < 0) return fail(FALCON_EINVAL, "invalid step arguments");
+  for (int k = 0; k < nsteps; ++k)
+    for (auto& g : b->groups) {
+      int rc = group_step(g.get());
+      if (rc) return rc;
+    }
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(FALCON_ECUDA, cudaGetErrorString(e));
+  return 0;
+}
+
+int falcon_batch_diagnostics(falcon_batch* b, falcon_diag* out) {
+  if (!b || !out) return fail(FALCON_EINVAL, "null argument");
+  CK(cudaStreamSynchronize(b->stream));
+  for (size_t i = 0; i < b->params.size(); ++i) {
+    const falcon_params& p = b->params[i];
+    const size_t n = (size_t)2 * (p.nm_max + 1) * p.nr_max;
+    std::vector<double> t(n), w(n), up(n), ur(n);
+    int rc = falcon_batch_get_state(b, (int)i, t.data(), w.data(), up.data(), ur.data(), nullptr);
+    if (rc) return rc;
+    for (double v : t)
+      if (!std::isfinite(v)) return fail(FALCON_ENONFINITE, "non-finite temperature in instance " + std::to_string(i));
+    Group* g = b->groups[b->where[i].first].get();
+    diagnostics_host(p, g->tot_time, t.data(), w.data(), up.data(), ur.data(), nullptr, &out[i]);
+  }
+  return 0;
+}
+
+int falcon_create(const falcon_params* p, falcon_handle** out) {
+  if (!p || !out) return fail(FALCON_EINVAL, "null argument");
+  falcon_batch* b = nullptr;
+  int rc = batch_create(p, 1, &b);
+  if (rc) return rc;
+  auto* h = new falcon_handle();
+  h->b = b;
+  *out = h;
+  return 0;
+}
+
+void falcon_destroy(falcon_handle* h) {
+  if (!h) return;
+  falcon_batch_destroy(h->b);
+  delete h;
+}
+
+int falcon_init_state(falcon_handle* h, int kind, double amp, uint64_t seed) {
+  if (!h) return fail(FALCON_EINVAL, "null handle");
+  return falcon_batch_init_state(h->b, kind, amp, &seed);
+}
+
+int falcon_set_state(falcon_handle* h, const double* tFR, const double* omgFR, const double* upFR,
+                     const double* urFR) {
+  if (!h) return fail(FALCON_EINVAL, "null handle");
+  return falcon_batch_set_state(h->b, 0, tFR, omgFR, upFR, urFR);
+}
+
+int falcon_get_state(falcon_handle* h, double* tFR, double* omgFR, double* upFR, double* urFR, double* psi) {
+  if (!h) return fail(FALCON_EINVAL, "null handle");
+  return falcon_batch_get_state(h->b, 0, tFR, omgFR, upFR, urFR, psi);
+}
+
+int falcon_step(falcon_handle* h, int nsteps) {
+  if (!h) return fail(FALCON_EINVAL, "null handle");
+  return falcon_batch_step(h->b, nsteps);
+}
+
+int falcon_diagnostics(falcon_handle* h, falcon_diag* out) {
+  if (!h) return fail(FALCON_EINVAL, "null handle");
+  return falcon_batch_diagnostics(h->b, out);
+}
+
+// ---- kernel-level entry points ----
+int falcon_nonlin_dev(int nr, int nm, int nb, const double* t_dev, const double* omg_dev, const double* up_dev,
+                      const double* ur_dev, double* uphi_t_dev, double* ur_t_dev, double* uphi_omg_dev,
+                      double* ur_omg_dev, void* stream) {
+  if (nr < 1 || nm < 1 || nb < 1) return fail(FALCON_EINVAL, "invalid sizes");
+  CK(init_dft_tables());
+  std::unique_ptr<FftTables> f;
+  int rc = make_fft(3 * nm, &f);
+  if (rc) return rc;
+  NonlinArgs a{};
+  a.R = nr; a.M = nm + 1; a.B = nb; a.Nm = nm;
+  a.plan = f->plan; a.tw = f->tw; a.pos = f->pos;
+  a.t = reinterpret_cast<const double2*>(t_dev); a.w = reinterpret_cast<const double2*>(omg_dev);
+  a.up = reinterpret_cast<const double2*>(up_dev); a.ur = reinterpret_cast<const double2*>(ur_dev);
+  a.ntp = reinterpret_cast<double2*>(uphi_t_dev); a.ntr = reinterpret_cast<double2*>(ur_t_dev);
+  a.nwp = reinterpret_cast<double2*>(uphi_omg_dev); a.nwr = reinterpret_cast<double2*>(ur_omg_dev);
+  CK(launch_nonlin(a, (cudaStream_t)stream));
+  CK(cudaStreamSynchronize((cudaStream_t)stream));
+  return 0;
+}
+
+int falcon_nonlin(int nr, int nm, const double* tFR, const double* omgFR, const double* upFR, const double* urFR,
+                  double* o1, double* o2, double* o3, double* o4) {
+  if (!tFR || !omgFR || !upFR || !urFR || !o1 || !o2 || !o3 || !o4) return fail(FALCON_EINVAL, "null argument");
+  const size_t nb = sizeof(double2) * (size_t)(nm + 1) * nr;
+  double* d = nullptr;
+  CK(cudaMalloc(&d, nb * 8));
+  const double* in[4] = {tFR, omgFR, upFR, urFR};
+  for (int f = 0; f < 4; ++f) CK(cudaMemcpy((char*)d + f * nb, in[f], nb, cudaMemcpyHostToDevice));
+  double* q[8];
+  for (int f = 0; f < 8; ++f) q[f] = (double*)((char*)d + f * nb);
+  int rc = falcon_nonlin_dev(nr, nm, 1, q[0], q[1], q[2], q[3], q[4], q[5], q[6], q[7], nullptr);
+  if (rc) { cudaFree(d); return rc; }
+  double* out[4] = {o1, o2, o3, o4};
+  for (int f = 0; f < 4; ++f) CK(cudaMemcpy(out[f], q[4 + f], nb, cudaMemcpyDeviceToHost));
+  cudaFree(d);
+  return 0;
+}
+
+int falcon_getrs_batched_dev(int n, int nsys, int nrhs, const double* lu_dev, const int* ipiv_dev, double* b_dev,
+                             void* stream) {
+  if (n < 1 || nsys < 1 || nrhs < 1) return fail(FALCON_EINVAL, "invalid sizes");
+  CK(launch_getrs_batched(n, nsys, nrhs, lu_dev, ipiv_dev, b_dev, (cudaStream_t)stream));
+  return 0;
+}
+
+double falcon_fp64_peak_gflops(void) { return measure_fp64_peak(); }
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Chebyshev transforms as dense operators (chebtransform / chebinvtran /
+// chebinvtranD1 / chebinvtranD2 of src/chebyshev_fftw.F90:124-352).  Their
+// matrices, row-major n x n: inv = C t H, d1 = C D H, d2 = C D2 H,
+// fwd = t^T diag(c') / ((n-1) C) (C = sqrt(2/(n-1))).
+// ---------------------------------------------------------------------------
+namespace {
+struct ChebMats {
+  int n = 0;
+  double *fwd = nullptr, *inv = nullptr, *d1 = nullptr, *d2 = nullptr;
+};
+std::mutex g_cheb_mu;
+std::map<int, ChebMats> g_cheb;
+
+int cheb_mats(int n, ChebMats** out) {
+  std::lock_guard<std::mutex> lk(g_cheb_mu);
+  auto it = g_cheb.find(n);
+  if (it != g_cheb.end()) { *out = &it->second; return 0; }
+  Cheb c = make_cheb(n, 0.35);
+  const double C = std::sqrt(2.0 / (double)(n - 1));
+  std::vector<double> fwd((size_t)n * n), inv((size_t)n * n), d1((size_t)n * n), d2((size_t)n * n);
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) {
+      const double h = (j == 0 || j == n - 1) ? 0.5 : 1.0;
+      inv[(size_t)i * n + j] = C * c.t[i + (size_t)n * j] * h;
+      d1[(size_t)i * n + j] = C * c.D[i + (size_t)n * j] * h;
+      d2[(size_t)i * n + j] = C * c.D2[i + (size_t)n * j] * h;
+      const double cp = (j == 0 || j == n - 1) ? 1.0 : 2.0;  // row i = coefficient, column j = point
+      fwd[(size_t)i * n + j] = c.t[j + (size_t)n * i] * cp / ((double)(n - 1) * C);
+    }
+  ChebMats m;
+  m.n = n;
+  int rc;
+  if ((rc = upload(&m.fwd, fwd, nullptr)) || (rc = upload(&m.inv, inv, nullptr)) ||
+      (rc = upload(&m.d1, d1, nullptr)) || (rc = upload(&m.d2, d2, nullptr)))
+    return rc;
+  auto res = g_cheb.emplace(n, m);
+  *out = &res.first->second;
+  return 0;
+}
+
+int cheb_apply(int which, int nr, int ncol, const double* in, double* out, void* stream) {
+  if (nr < 3 || ncol < 1 || !in || !out) return fail(FALCON_EINVAL, "invalid Chebyshev transform arguments");
+  ChebMats* m = nullptr;
+  int rc = cheb_mats(nr, &m);
+  if (rc) return rc;
+  const double* A = which == 0 ? m->fwd : which == 1 ? m->inv : which == 2 ? m->d1 : m->d2;
+  CK(launch_apply_cols(nr, ncol, A, reinterpret_cast<const double2*>(in), reinterpret_cast<double2*>(out),
+                       (cudaStream_t)stream));
+  return 0;
+}
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Serving loop: requests admitted by device-memory footprint into groups
+// that share operators, stepped together one step per iteration, retired at
+// their horizon.  Groups are repacked when members join or leave.
+// ---------------------------------------------------------------------------
+struct ServerRequest {
+  int64_t id = 0;
+  falcon_params p{};
+  uint64_t seed = 0;
+  int horizon = 0;
+  int steps = 0;
+  int state = 0;  // 0 queued, 1 active, 2 done
+  size_t foot = 0;
+  falcon_diag diag{};
+  std::vector<double> tfr;
+  OpKey key{};
+};
+
+struct ServerGroup {
+  std::unique_ptr<Group> g;
+  std::vector<int64_t> ids;  // request id per slot
+  std::vector<int64_t> pending;
+  falcon_params rep{};       // parameters of the operator key
+};
+
+struct falcon_server {
+  size_t budget = 0;
+  int max_active = 0;
+  size_t used = 0;
+  int64_t next_id = 1;
+  std::deque<int64_t> queue;
+  std::map<int64_t, ServerRequest> reqs;
+  std::map<OpKey, ServerGroup> groups;
+  cudaStream_t stream = nullptr;
+  int active = 0;
+  ~falcon_server() {
+    groups.clear();
+    if (stream) cudaStreamDestroy(stream);
+  }
+};
+
+namespace {
+
+// Device bytes of one resident instance (state, histories, stage stores,
+// products and scratch), from the same allocation list as group_init.
+size_t instance_bytes(const falcon_params& p) {
+  Scheme s;
+  scheme_weights(p.scheme_type, p.scheme_imp, p.scheme_exp, &s);
+  const size_t R = p.nr_max, M = p.nm_max + 1, f = 16 * R * M;
+  size_t n = 0;
+  if (p.scheme_type == FALCON_IMEX) n += (2 * s.n_imp + 2 * s.n_exp) * f + (s.n_imp + s.n_exp) * 8 * R;
+  else n += (2 + 5 * s.n_exp) * f + 8 * R;
+  n += 13 * f + 16 * R + 32 * R + 8;
+  return n;
+}
+
+size_t opset_bytes(const falcon_params& p) {
+  const size_t R = p.nr_max, M = p.nm_max + 1;
+  return 8 * (2 * R * R + M * R * R + M * 3 * R * R + 2 * R * R + 2 * R);
+}
+
+int server_admit_group(falcon_server* s, const OpKey& key, ServerGroup& sg) {
+  // repack: keep current ids (minus retired), append pending
+  std::vector<int64_t> new_ids;
+  std::vector<int> map;
+  for (size_t j = 0; j < sg.ids.size(); ++j) {
+    auto it = s->reqs.find(sg.ids[j]);
+    if (it != s->reqs.end() && it->second.state == 1) { new_ids.push_back(sg.ids[j]); map.push_back((int)j); }
+  }
+  for (int64_t id : sg.pending) { new_ids.push_back(id); map.push_back(-1); }
+  sg.pending.clear();
+  if (new_ids.empty()) { sg.g.reset(); sg.ids.clear(); return 0; }
+  int rc;
+  if (!sg.g) {
+    std::vector<falcon_params> ps;
+    std::vector<int> mem;
+    for (size_t j = 0; j < new_ids.size(); ++j) { ps.push_back(s->reqs[new_ids[j]].p); mem.push_back((int)j); }
+    sg.g = std::make_unique<Group>();
+    sg.g->stream = s->stream;
+    if ((rc = group_init(sg.g.get(), ps, mem))) return rc;
+    sg.ids = new_ids;
+    for (size_t j = 0; j < new_ids.size(); ++j) {
+      ServerRequest& r = s->reqs[new_ids[j]];
+      std::vector<double> t;
+      initial_temperature(r.p, 1, 1e-3, r.seed, t);
+      if ((rc = group_set_instance(sg.g.get(), (int)j, t.data(), nullptr, nullptr, nullptr))) return rc;
+    }
+    return group_reset(sg.g.get());
+  }
+  if ((rc = group_resize(sg.g.get(), map))) return rc;
+  sg.ids = new_ids;
+  std::vector<double> ra(new_ids.size());
+  for (size_t j = 0; j < new_ids.size(); ++j) ra[j] = s->reqs[new_ids[j]].p.ra / s->reqs[new_ids[j]].p.pr;
+  sg.g->ra_pr_h = ra;
+  CK(cudaMemcpy(sg.g->ra_pr, ra.data(), sizeof(double) * ra.size(), cudaMemcpyHostToDevice));
+  for (size_t j = 0; j < new_ids.size(); ++j) {
+    if (map[j] >= 0) continue;
+    ServerRequest& r = s->reqs[new_ids[j]];
+    std::vector<double> t;
+    initial_temperature(r.p, 1, 1e-3, r.seed, t);
+    if ((rc = group_set_instance(sg.g.get(), (int)j, t.data(), nullptr, nullptr, nullptr))) return rc;
+    if ((rc = group_reset_instance(sg.g.get(), (int)j))) return rc;
+  }
+  (void)key;
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int falcon_cheb_fwd_dev(int nr, int ncol, const double* in_dev, double* out_dev, void* stream) {
+  return cheb_apply(0, nr, ncol, in_dev, out_dev, stream);
+}
+int falcon_cheb_inv_dev(int nr, int ncol, const double* in_dev, double* out_dev, void* stream) {
+  return cheb_apply(1, nr, ncol, in_dev, out_dev, stream);
+}
+int falcon_cheb_d1_dev(int nr, int ncol, const double* in_dev, double* out_dev, void* stream) {
+  return cheb_apply(2, nr, ncol, in_dev, out_dev, stream);
+}
+int falcon_cheb_d2_dev(int nr, int ncol, const double* in_dev, double* out_dev, void* stream) {
+  return cheb_apply(3, nr, ncol, in_dev, out_dev, stream);
+}
+
+int falcon_server_create(size_t hbm_budget_bytes, int max_active, falcon_server** out) {
+  if (!out || hbm_budget_bytes == 0) return fail(FALCON_EINVAL, "invalid server arguments");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+    return fail(FALCON_ECUDA, "no CUDA device: the GB300 library has no CPU fallback");
+  CK(init_dft_tables());
+  auto* s = new falcon_server();
+  s->budget = hbm_budget_bytes;
+  s->max_active = max_active > 0 ? max_active : (1 << 30);
+  if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete s;
+    return fail(FALCON_ECUDA, "stream creation failed");
+  }
+  *out = s;
+  return 0;
+}
+
+void falcon_server_destroy(falcon_server* s) {
+  if (!s) return;
+  cudaStreamSynchronize(s->stream);
+  delete s;
+}
+
+int falcon_server_submit(falcon_server* s, const falcon_params* p, uint64_t seed, int horizon, int64_t* id) {
+  if (!s || !p || horizon <= 0) return fail(FALCON_EINVAL, "invalid request");
+  int rc = validate(*p);
+  if (rc) return rc;
+  ServerRequest r;
+  r.id = s->next_id++;
+  r.p = *p;
+  r.seed = seed;
+  r.horizon = horizon;
+  r.foot = instance_bytes(*p);
+  Scheme sc;
+  scheme_weights(p->scheme_type, p->scheme_imp, p->scheme_exp, &sc);
+  r.key = key_of(*p, sc);
+  if (r.foot + opset_bytes(*p) > s->budget) return fail(FALCON_EBUSY, "request larger than the device budget");
+  s->reqs[r.id] = r;
+  s->queue.push_back(r.id);
+  if (id) *id = r.id;
+  return 0;
+}
+
+int falcon_server_iterate(falcon_server* s, int* n_active, int* n_queued) {
+  if (!s) return fail(FALCON_EINVAL, "null server");
+  // 1. admission, first come first served, by device footprint
+  std::map<OpKey, bool> touched;
+  while (!s->queue.empty() && s->active < s->max_active) {
+    ServerRequest& r = s->reqs[s->queue.front()];
+    auto git = s->groups.find(r.key);
+    const bool resident = (git != s->groups.end() && (git->second.g || !git->second.pending.empty()));
+    const size_t need = r.foot + (resident ? 0 : opset_bytes(r.p));
+    if (s->used + need > s->budget) break;
+    s->used += need;
+    r.state = 1;
+    s->groups[r.key].pending.push_back(r.id);
+    s->groups[r.key].rep = r.p;
+    touched[r.key] = true;
+    s->active++;
+    s->queue.pop_front();
+  }
+  // 2. repack groups whose membership changed
+  for (auto& kv : s->groups) {
+    if (!touched.count(kv.first)) continue;
+    int rc = server_admit_group(s, kv.first, kv.second);
+    if (rc) return rc;
+  }
+  // 3. one step of every active group
+  for (auto& kv : s->groups) {
+    if (!kv.second.g) continue;
+    int rc = group_step(kv.second.g.get());
+    if (rc) return rc;
+  }
+  CK(cudaStreamSynchronize(s->stream));
+  // 4. retire finished requests
+  for (auto& kv : s->groups) {
+    ServerGroup& sg = kv.second;
+    if (!sg.g) continue;
+    bool changed = false;
+    for (size_t j = 0; j < sg.ids.size(); ++j) {
+      ServerRequest& r = s->reqs[sg.ids[j]];
+      if (r.state != 1) continue;
+      r.steps++;
+      if (r.steps >= r.horizon) {
+        const size_t n = (size_t)2 * (r.p.nm_max + 1) * r.p.nr_max;
+        std::vector<double> t(n), w(n), up(n), ur(n);
+        int rc = group_get_instance(sg.g.get(), (int)j, t.data(), w.data(), up.data(), ur.data(), nullptr);
+        if (rc) return rc;
+        diagnostics_host(r.p, r.steps * r.p.dt, t.data(), w.data(), up.data(), ur.data(), nullptr, &r.diag);
+        r.tfr = std::move(t);
+        r.state = 2;
+        s->active--;
+        s->used -= r.foot;
+        changed = true;
+      }
+    }
+    if (changed) {
+      int rc = server_admit_group(s, kv.first, sg);
+      if (rc) return rc;
+      if (!sg.g) s->used -= std::min(s->used, opset_bytes(sg.rep));
+    }
+  }
+  if (n_active) *n_active = s->active;
+  if (n_queued) *n_queued = (int)s->queue.size();
+  return 0;
+}
+
+int falcon_server_poll(falcon_server* s, int64_t id, int* done, falcon_diag* out, double* tFR) {
+  if (!s || !done) return fail(FALCON_EINVAL, "null argument");
+  auto it = s->reqs.find(id);
+  if (it == s->reqs.end()) return fail(FALCON_EINVAL, "unknown request id");
+  *done = it->second.state == 2;
+  if (*done) {
+    if (out) *out = it->second.diag;
+    if (tFR) std::memcpy(tFR, it->second.tfr.data(), sizeof(double) * it->second.tfr.size());
+  }
+  return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,130 @@
+// Internal interfaces between the host runtime (falcon_host.cpp) and the
+// sm_103a kernels (falcon_kernels.cu).  Not part of the C ABI.
+//
+// Device layout of every complex field of a group of B instances that share
+// (Nr, Nm): X[r][m][b] (instance fastest), one double2 per element, so that
+//  - a radial operator (R x R) applied to all modes and instances is one
+//    GEMM with K = R and N = 2*M*B contiguous columns, and
+//  - a per-mode operator applied to all instances of a mode is a GEMM whose
+//    2*B columns are contiguous.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace falcon {
+
+constexpr int kMaxRadix = 16;     // stages of a mixed-radix FFT plan
+constexpr int kMaxStages = 6;     // IMEXRK stages supported
+
+// Mixed-radix plan of the azimuthal transform of length P = 3*Nm.
+struct FftPlan {
+  int P;
+  int nrad;
+  int rad[kMaxRadix];   // radices, outermost first (DIT processes them last)
+};
+
+// Arguments of the nonlinear-pass kernel (Nr_maxLOOP, src/nonlin.F90:35-91).
+struct NonlinArgs {
+  int R, M, B, Nm;
+  FftPlan plan;
+  const double2* tw;    // exp(-2 pi i k/P), k < P
+  const int* pos;       // digit-reversal positions, P entries
+  const double2 *t, *w, *up, *ur;        // inputs  [r][m][b]
+  double2 *ntp, *ntr, *nwp, *nwr;        // outputs [r][m][b]
+  double* umax;                          // optional [r][b][2]: max|ur|, max|uphi|
+};
+
+// Y[row][n] = alpha * sum_k A[k*lda + row] * X[k*ldx + n] for
+// row < rows, n < N, with a batch index z applying the strides sA, sX, sY.
+struct GemmArgs {
+  const double* A; long lda;
+  const double* X; long ldx;
+  double* Y; long ldy;
+  int K, rows, N;
+  long sA, sX, sY;
+  int batch;
+  double alpha;
+};
+
+// Elementwise arguments shared by the right-hand-side kernels.
+struct RhsArgs {
+  int R, M, B;
+  const double* inv_r;      // R
+  const double* inv_r2;     // R
+  const double* ra_pr;      // B: Ra/Pr per instance
+  double dt, inv_pr;
+  // IMEX multistep
+  int scheme_cn;            // 1: Crank-Nicolson implicit part, 0: BDF
+  int n_imp, n_exp;
+  double w_imp[4], w_exp[4], wt_lhs;
+  const double2* th[4];     // T history, th[0] = current state
+  const double2* wh[4];     // omega history
+  double2* nt_new;          // explicit term of T written for this step
+  double2* nw_new;
+  const double2* nth[4];    // explicit history, nth[0] aliases nt_new
+  const double2* nwh[4];
+  const double* ubh[4];     // uphi_bar history [r][b]
+  double* urom_new;         // mean(ur*omg) written for this step
+  const double* uromh[4];
+  const double2 *ntp, *ntr, *dntr, *nwp, *nwr, *dnwr;
+  const double2 *lt, *lw;   // L T and L omega (CN)
+  const double2* lu0;       // L applied to uphi_bar, [r][b] complex (CN)
+  double2 *rhs_t, *rhs_w;
+};
+
+// IMEXRK stage arguments (src/fourierloop_imexrk.F90).
+struct StageArgs {
+  int R, M, B, st;
+  const double* inv_r;
+  const double* inv_r2;
+  const double* ra_pr;
+  double dt, inv_pr;
+  double aD[kMaxStages], aA[kMaxStages];   // row `st` of the Butcher tables
+  double aD_ss;
+  int buo_imp;
+  const double2* t0; const double2* w0; const double* u0;
+  const double2* fat[kMaxStages]; const double2* fdt[kMaxStages];
+  const double2* faw[kMaxStages]; const double2* fdw[kMaxStages];
+  const double2* buo[kMaxStages];
+  double2 *rhs_t, *rhs_w;
+  // stage derivatives (RHS_construct_stage)
+  const double2 *ntp, *ntr, *dntr, *nwp, *nwr, *dnwr, *lt, *lw, *lu0, *t, *w, *up;
+  double2 *fat_out, *fdt_out, *faw_out, *fdw_out, *buo_out;
+};
+
+// ---- launchers (falcon_kernels.cu) ----
+cudaError_t launch_nonlin(const NonlinArgs& a, cudaStream_t s);
+cudaError_t launch_gemm(const GemmArgs& g, cudaStream_t s);
+cudaError_t launch_imex_rhs(const RhsArgs& a, cudaStream_t s);
+// rhs_w(m>=1) += coef_b * (i m / r) * t_new, coef_b = scale * ra_pr[b]
+cudaError_t launch_add_buoyancy(int R, int M, int B, const double* inv_r, const double* ra_pr,
+                                double scale, const double2* t_new, double2* rhs_w,
+                                double2* buo_out, cudaStream_t s);
+// u_r = i m psi / r for m >= 1; m = 0 from the uphi_bar solve output
+// ub (rows 0..R-1: uphi_bar, rows R..2R-1: d uphi_bar/dr, columns 2*b+{0,1}).
+cudaError_t launch_post_w(int R, int M, int B, const double* inv_r, const double2* psi,
+                          double2* ur, double2* up, double2* w, const double* ub,
+                          double* ubar_new, cudaStream_t s);
+cudaError_t launch_stage_rhs(const StageArgs& a, cudaStream_t s);
+cudaError_t launch_stage_deriv(const StageArgs& a, cudaStream_t s);
+// Fortran (M,R) complex of instance b <-> device [r][m][b]
+cudaError_t launch_scatter_instance(int R, int M, int B, int b, const double2* src, double2* dst,
+                                    cudaStream_t s);
+cudaError_t launch_gather_instance(int R, int M, int B, int b, const double2* src, double2* dst,
+                                   cudaStream_t s);
+// dst[r][b] = src[r][0][b].x  (mode-0 real part)
+cudaError_t launch_extract_mode0(int R, int M, int B, const double2* src, double* dst, cudaStream_t s);
+cudaError_t launch_getrs_batched(int n, int nsys, int nrhs, const double* lu, const int* ipiv,
+                                 double* b, cudaStream_t s);
+// out[c] = A in[c] for ncol complex columns of length n (A real row-major).
+cudaError_t launch_apply_cols(int n, int ncol, const double* A, const double2* in, double2* out, cudaStream_t s);
+// Instance-column remap of a [rows][B] array (ew doubles per element).
+cudaError_t launch_remap_cols(const double* src, double* dst, size_t rows, int bs, int bd, int ew, const int* map,
+                              cudaStream_t s);
+// Self-timed FP64 FMA throughput kernel (returns GFLOP/s, or < 0 on error).
+double measure_fp64_peak();
+// Set the odd-prime DFT coefficient tables (constant memory); idempotent.
+cudaError_t init_dft_tables();
+
+}  // namespace falcon

@@ -1,0 +1,921 @@
+// sm_103a kernels of the FAlCon-DNS time step (FP64 throughout).
+//
+// On GB300 the FP64 FMA pipe (~1.2 TFLOP/s measured) is ~30x slower than
+// HBM relative to the bytes these kernels move, so every kernel here is
+// bound by FP64 issue, not memory: the code minimises FP64 instructions
+// (two-for-one real transforms, symmetric odd-prime butterflies with
+// constant-bank coefficients, register-tiled DFMA GEMMs) and keeps the
+// non-FP64 instruction count per FMA below one.
+#include <math.h>
+#include <stdio.h>
+
+#include "falcon_internal.h"
+
+namespace falcon {
+
+// ---------------------------------------------------------------------------
+// complex helpers
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ double2 cmul(double2 a, double2 w) {
+  return make_double2(fma(a.x, w.x, -a.y * w.y), fma(a.x, w.y, a.y * w.x));
+}
+
+// ---------------------------------------------------------------------------
+// Odd-prime DFT coefficient tables: kC<p>[i] = cos(2 pi i/p), kS<p>[i] =
+// sin(2 pi i/p), filled from the host once per process.
+// ---------------------------------------------------------------------------
+template <int p> struct DftTab;
+#define FALCON_DEF_TAB(p)                                                    \
+  __constant__ double kC##p[p];                                              \
+  __constant__ double kS##p[p];                                              \
+  template <> struct DftTab<p> {                                             \
+    __device__ static __forceinline__ double c(int i) { return kC##p[i]; }   \
+    __device__ static __forceinline__ double s(int i) { return kS##p[i]; }   \
+  };
+FALCON_DEF_TAB(3)
+FALCON_DEF_TAB(5)
+FALCON_DEF_TAB(7)
+FALCON_DEF_TAB(11)
+FALCON_DEF_TAB(13)
+FALCON_DEF_TAB(17)
+FALCON_DEF_TAB(19)
+FALCON_DEF_TAB(23)
+FALCON_DEF_TAB(29)
+FALCON_DEF_TAB(31)
+
+template <int p>
+static cudaError_t set_tab(const void* csym, const void* ssym) {
+  double c[p], s[p];
+  const double two_pi = 8.0 * atan(1.0);
+  for (int i = 0; i < p; ++i) {
+    c[i] = cos(two_pi * i / p);
+    s[i] = sin(two_pi * i / p);
+  }
+  cudaError_t e = cudaMemcpyToSymbol(csym, c, sizeof(c));
+  if (e != cudaSuccess) return e;
+  return cudaMemcpyToSymbol(ssym, s, sizeof(s));
+}
+
+cudaError_t init_dft_tables() {
+  static bool done = false;
+  static int done_dev = -1;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (done && done_dev == dev) return cudaSuccess;
+  cudaError_t e = cudaSuccess;
+#define FALCON_SET(p) if (e == cudaSuccess) e = set_tab<p>(kC##p, kS##p);
+  FALCON_SET(3) FALCON_SET(5) FALCON_SET(7) FALCON_SET(11) FALCON_SET(13)
+  FALCON_SET(17) FALCON_SET(19) FALCON_SET(23) FALCON_SET(29) FALCON_SET(31)
+#undef FALCON_SET
+  if (e == cudaSuccess) { done = true; done_dev = dev; }
+  return e;
+}
+
+// Forward DFT of length p in registers: v_j <- sum_q v_q exp(-2 pi i j q/p).
+template <int p>
+__device__ __forceinline__ void dft(double2 (&v)[p]) {
+  if constexpr (p == 2) {
+    double2 a = v[0], b = v[1];
+    v[0] = cadd(a, b); v[1] = csub(a, b);
+  } else if constexpr (p == 4) {
+    double2 t0 = cadd(v[0], v[2]), t1 = csub(v[0], v[2]);
+    double2 t2 = cadd(v[1], v[3]), t3 = csub(v[1], v[3]);
+    v[0] = cadd(t0, t2); v[2] = csub(t0, t2);
+    v[1] = make_double2(t1.x + t3.y, t1.y - t3.x);
+    v[3] = make_double2(t1.x - t3.y, t1.y + t3.x);
+  } else {
+    constexpr int h = (p - 1) / 2;
+    double2 a[h], b[h];
+#pragma unroll
+    for (int q = 1; q <= h; ++q) { a[q - 1] = cadd(v[q], v[p - q]); b[q - 1] = csub(v[q], v[p - q]); }
+    double2 y0 = v[0];
+#pragma unroll
+    for (int q = 0; q < h; ++q) y0 = cadd(y0, a[q]);
+#pragma unroll
+    for (int j = 1; j <= h; ++j) {
+      double2 A = v[0];
+      double2 Bv = make_double2(0.0, 0.0);
+#pragma unroll
+      for (int q = 1; q <= h; ++q) {
+        const int idx = (j * q) % p;
+        const double c = DftTab<p>::c(idx), s = DftTab<p>::s(idx);
+        A.x = fma(a[q - 1].x, c, A.x); A.y = fma(a[q - 1].y, c, A.y);
+        Bv.x = fma(b[q - 1].x, s, Bv.x); Bv.y = fma(b[q - 1].y, s, Bv.y);
+      }
+      v[j] = make_double2(A.x + Bv.y, A.y - Bv.x);
+      v[p - j] = make_double2(A.x - Bv.y, A.y + Bv.x);
+    }
+    v[0] = y0;
+  }
+}
+
+// One in-place decimation-in-time stage (radix p, current span m) applied to
+// two buffers at once.  tw[k] = exp(-2 pi i k / P); stride = P / (m p).
+template <int p>
+__device__ __forceinline__ void dit_stage(double2* __restrict__ A, double2* __restrict__ Bf, int P,
+                                          int m, int stride, const double2* __restrict__ tw, int lane) {
+  const int mp = m * p, nb = P / p;
+  const float inv_m = 1.0f / (float)m;
+  for (int t = lane; t < nb; t += 32) {
+    const int g = (int)(((float)t + 0.5f) * inv_m);
+    const int k = t - g * m;
+    const int base = g * mp + k;
+    double2 va[p], vb[p];
+#pragma unroll
+    for (int q = 0; q < p; ++q) { va[q] = A[base + q * m]; vb[q] = Bf[base + q * m]; }
+    if (k > 0) {
+      const int ks = k * stride;
+#pragma unroll
+      for (int q = 1; q < p; ++q) {
+        const double2 w = tw[q * ks];
+        va[q] = cmul(va[q], w); vb[q] = cmul(vb[q], w);
+      }
+    }
+    dft<p>(va);
+    dft<p>(vb);
+#pragma unroll
+    for (int q = 0; q < p; ++q) { A[base + q * m] = va[q]; Bf[base + q * m] = vb[q]; }
+  }
+}
+
+// One in-place decimation-in-frequency stage (radix p, span m after it).
+template <int p>
+__device__ __forceinline__ void dif_stage(double2* __restrict__ A, double2* __restrict__ Bf, int P,
+                                          int m, int stride, const double2* __restrict__ tw, int lane) {
+  const int mp = m * p, nb = P / p;
+  const float inv_m = 1.0f / (float)m;
+  for (int t = lane; t < nb; t += 32) {
+    const int g = (int)(((float)t + 0.5f) * inv_m);
+    const int k = t - g * m;
+    const int base = g * mp + k;
+    double2 va[p], vb[p];
+#pragma unroll
+    for (int q = 0; q < p; ++q) { va[q] = A[base + q * m]; vb[q] = Bf[base + q * m]; }
+    dft<p>(va);
+    dft<p>(vb);
+    if (k > 0) {
+      const int ks = k * stride;
+#pragma unroll
+      for (int q = 1; q < p; ++q) {
+        const double2 w = tw[q * ks];
+        va[q] = cmul(va[q], w); vb[q] = cmul(vb[q], w);
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < p; ++q) { A[base + q * m] = va[q]; Bf[base + q * m] = vb[q]; }
+  }
+}
+
+// Generic prime radix (p <= 64) with coefficients read from the P-point
+// twiddle table: exp(-2 pi i j/p) = tw[j * P/p].
+__device__ void generic_stage(double2* A, double2* Bf, int P, int p, int m, int stride,
+                              const double2* tw, int lane, bool dif) {
+  const int mp = m * p, nb = P / p, tp = P / p;
+  for (int t = lane; t < nb; t += 32) {
+    const int g = t / m, k = t - g * m, base = g * mp + k;
+    double2 va[64], vb[64], ya[64], yb[64];
+    for (int q = 0; q < p; ++q) { va[q] = A[base + q * m]; vb[q] = Bf[base + q * m]; }
+    if (!dif && k > 0)
+      for (int q = 1; q < p; ++q) { double2 w = tw[q * k * stride]; va[q] = cmul(va[q], w); vb[q] = cmul(vb[q], w); }
+    for (int j = 0; j < p; ++j) {
+      double2 sa = make_double2(0, 0), sb = make_double2(0, 0);
+      for (int q = 0; q < p; ++q) {
+        double2 w = tw[((j * q) % p) * tp];
+        sa = cadd(sa, cmul(va[q], w)); sb = cadd(sb, cmul(vb[q], w));
+      }
+      ya[j] = sa; yb[j] = sb;
+    }
+    if (dif && k > 0)
+      for (int q = 1; q < p; ++q) { double2 w = tw[q * k * stride]; ya[q] = cmul(ya[q], w); yb[q] = cmul(yb[q], w); }
+    for (int q = 0; q < p; ++q) { A[base + q * m] = ya[q]; Bf[base + q * m] = yb[q]; }
+  }
+}
+
+__device__ __forceinline__ void run_stage(int p, bool dif, double2* A, double2* Bf, int P, int m,
+                                          int stride, const double2* tw, int lane) {
+#define FALCON_CASE(q)                                                  \
+  case q:                                                               \
+    if (dif) dif_stage<q>(A, Bf, P, m, stride, tw, lane);               \
+    else dit_stage<q>(A, Bf, P, m, stride, tw, lane);                   \
+    break;
+  switch (p) {
+    FALCON_CASE(2) FALCON_CASE(3) FALCON_CASE(4) FALCON_CASE(5) FALCON_CASE(7)
+    FALCON_CASE(11) FALCON_CASE(13) FALCON_CASE(17) FALCON_CASE(19) FALCON_CASE(23)
+    FALCON_CASE(29) FALCON_CASE(31)
+    default: generic_stage(A, Bf, P, p, m, stride, tw, lane, dif); break;
+  }
+#undef FALCON_CASE
+}
+
+// ---------------------------------------------------------------------------
+// Nonlinear pass (Nr_maxLOOP, src/nonlin.F90:55-86): one warp per radial
+// line (r, b).  invfft of T, omega, u_phi, u_r (two complex inverse FFTs of
+// length P, each carrying two real fields), the four grid products, and the
+// two forward FFTs that return u_phi*T, u_r*T, u_phi*omega, u_r*omega
+// truncated to modes 0..Nm and divided by P.
+// ---------------------------------------------------------------------------
+__global__ void nonlin_kernel(NonlinArgs a) {
+  extern __shared__ double2 smem[];
+  const int P = a.plan.P;
+  double2* tw = smem;
+  int* pos = reinterpret_cast<int*>(smem + P);
+  const int pos_pad = (P + 3) / 4;  // ints rounded up to double2 units (16 B)
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nwarp = blockDim.x >> 5;
+  double2* bufA = smem + P + pos_pad + (size_t)warp * 2 * P;
+  double2* bufB = bufA + P;
+  for (int i = threadIdx.x; i < P; i += blockDim.x) { tw[i] = a.tw[i]; pos[i] = a.pos[i]; }
+  __syncthreads();
+  const int nlines = a.R * a.B;
+  const int line = blockIdx.x * nwarp + warp;
+  if (line >= nlines) return;
+  const int r = line / a.B, b = line - r * a.B;
+  const int M = a.M, B = a.B, Nm = a.Nm;
+  for (int j = lane; j < P; j += 32) { bufA[j] = make_double2(0, 0); bufB[j] = make_double2(0, 0); }
+  __syncwarp();
+  // Scatter conj(Z) at digit-reversed positions, Z_k = X_k + i Y_k for the
+  // Hermitian spectra X, Y of two real lines (only Re of mode 0 counts, as
+  // in a c2r transform).  IFFT(Z) = conj(FFT(conj(Z))).
+  const size_t row = (size_t)r * M * B + b;
+  for (int k = lane; k <= Nm; k += 32) {
+    const size_t e = row + (size_t)k * B;
+    const double2 T = a.t[e], W = a.w[e], U = a.up[e], V = a.ur[e];
+    if (k == 0) {
+      bufA[pos[0]] = make_double2(T.x, -W.x);
+      bufB[pos[0]] = make_double2(U.x, -V.x);
+    } else {
+      // conj(Z_k) = (T.x - W.y, -(T.y + W.x)); conj(Z_{P-k}) = (T.x + W.y, T.y - W.x)
+      bufA[pos[k]] = make_double2(T.x - W.y, -(T.y + W.x));
+      bufA[pos[P - k]] = make_double2(T.x + W.y, T.y - W.x);
+      bufB[pos[k]] = make_double2(U.x - V.y, -(U.y + V.x));
+      bufB[pos[P - k]] = make_double2(U.x + V.y, U.y - V.x);
+    }
+  }
+  __syncwarp();
+  {  // DIT: radices processed innermost first
+    int m = 1;
+    for (int s = a.plan.nrad - 1; s >= 0; --s) {
+      const int p = a.plan.rad[s];
+      run_stage(p, false, bufA, bufB, P, m, P / (m * p), tw, lane);
+      m *= p;
+      __syncwarp();
+    }
+  }
+  // Grid values: bufA = conj(t + i omg) -> t = A.x, omg = -A.y; likewise for
+  // (u_phi, u_r) in bufB.  Products, in natural order for the DIF.
+  double urmax = 0.0, upmax = 0.0;
+  for (int j = lane; j < P; j += 32) {
+    const double2 za = bufA[j], zb = bufB[j];
+    const double tt = za.x, om = -za.y, up = zb.x, ur = -zb.y;
+    bufA[j] = make_double2(up * tt, ur * tt);
+    bufB[j] = make_double2(up * om, ur * om);
+    urmax = fmax(urmax, fabs(ur));
+    upmax = fmax(upmax, fabs(up));
+  }
+  __syncwarp();
+  {  // DIF: outermost radix first
+    int m = P;
+    for (int s = 0; s < a.plan.nrad; ++s) {
+      const int p = a.plan.rad[s];
+      m /= p;
+      run_stage(p, true, bufA, bufB, P, m, P / (m * p), tw, lane);
+      __syncwarp();
+    }
+  }
+  // Split the two-for-one spectra: X_k = (Z_k + conj Z_{P-k})/2,
+  // Y_k = (Z_k - conj Z_{P-k})/(2i), then divide by P.
+  const double s = 0.5 / (double)P;
+  for (int k = lane; k <= Nm; k += 32) {
+    const size_t e = row + (size_t)k * B;
+    const double2 za = bufA[pos[k]], ca = bufA[pos[k == 0 ? 0 : P - k]];
+    const double2 zb = bufB[pos[k]], cb = bufB[pos[k == 0 ? 0 : P - k]];
+    a.ntp[e] = make_double2((za.x + ca.x) * s, (za.y - ca.y) * s);
+    a.ntr[e] = make_double2((za.y + ca.y) * s, (ca.x - za.x) * s);
+    a.nwp[e] = make_double2((zb.x + cb.x) * s, (zb.y - cb.y) * s);
+    a.nwr[e] = make_double2((zb.y + cb.y) * s, (cb.x - zb.x) * s);
+  }
+  if (a.umax) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      urmax = fmax(urmax, __shfl_xor_sync(0xffffffffu, urmax, o));
+      upmax = fmax(upmax, __shfl_xor_sync(0xffffffffu, upmax, o));
+    }
+    if (lane == 0) {
+      a.umax[2 * ((size_t)r * B + b)] = urmax;
+      a.umax[2 * ((size_t)r * B + b) + 1] = upmax;
+    }
+  }
+}
+
+static int nonlin_warps(int P, int* smem_bytes) {
+  int dev = 0, maxsm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  const int fixed = (P + (P + 3) / 4) * 16;
+  int w = 4;
+  while (w > 1 && fixed + w * 2 * P * 16 > maxsm) --w;
+  *smem_bytes = fixed + w * 2 * P * 16;
+  return w;
+}
+
+cudaError_t launch_nonlin(const NonlinArgs& a, cudaStream_t s) {
+  int smem = 0;
+  const int w = nonlin_warps(a.plan.P, &smem);
+  cudaError_t e = cudaFuncSetAttribute(nonlin_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return e;
+  const int nlines = a.R * a.B;
+  const int grid = (nlines + w - 1) / w;
+  nonlin_kernel<<<grid, 32 * w, smem, s>>>(a);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Register-tiled FP64 GEMM, Y = alpha * A * X (A column-major, rows x K).
+// 256 threads: warp w owns rows [row0 + w*RPT, +RPT), lane owns columns
+// n0 + 2*lane + {0,1}; K is staged in chunks of 16 through shared memory.
+// ---------------------------------------------------------------------------
+constexpr int kKC = 16;
+
+template <int RPT>
+__global__ void __launch_bounds__(256) gemm_tile_kernel(GemmArgs g) {
+  constexpr int ROWS = 8 * RPT;
+  __shared__ __align__(16) double As[kKC][ROWS + 2];
+  __shared__ __align__(16) double Xs[kKC][64];
+  const int z = blockIdx.z;
+  const double* A = g.A + (size_t)z * g.sA;
+  const double* X = g.X + (size_t)z * g.sX;
+  double* Y = g.Y + (size_t)z * g.sY;
+  const int n0 = blockIdx.x * 64;
+  const int row0 = blockIdx.y * ROWS;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  double acc[RPT][2];
+#pragma unroll
+  for (int i = 0; i < RPT; ++i) { acc[i][0] = 0.0; acc[i][1] = 0.0; }
+  for (int k0 = 0; k0 < g.K; k0 += kKC) {
+    for (int idx = threadIdx.x; idx < kKC * ROWS; idx += 256) {
+      const int kk = idx / ROWS, rr = idx - kk * ROWS;
+      const int k = k0 + kk, row = row0 + rr;
+      As[kk][rr] = (k < g.K && row < g.rows) ? A[(size_t)k * g.lda + row] : 0.0;
+    }
+    for (int idx = threadIdx.x; idx < kKC * 64; idx += 256) {
+      const int kk = idx >> 6, c = idx & 63;
+      const int k = k0 + kk, n = n0 + c;
+      Xs[kk][c] = (k < g.K && n < g.N) ? X[(size_t)k * g.ldx + n] : 0.0;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < kKC; ++kk) {
+      const double2 xv = *reinterpret_cast<const double2*>(&Xs[kk][2 * lane]);
+#pragma unroll
+      for (int i = 0; i < RPT; ++i) {
+        const double av = As[kk][warp * RPT + i];
+        acc[i][0] = fma(av, xv.x, acc[i][0]);
+        acc[i][1] = fma(av, xv.y, acc[i][1]);
+      }
+    }
+    __syncthreads();
+  }
+  const int n = n0 + 2 * lane;
+#pragma unroll
+  for (int i = 0; i < RPT; ++i) {
+    const int row = row0 + warp * RPT + i;
+    if (row < g.rows) {
+      if (n + 1 < g.N) {
+        *reinterpret_cast<double2*>(&Y[(size_t)row * g.ldy + n]) =
+            make_double2(g.alpha * acc[i][0], g.alpha * acc[i][1]);
+      } else if (n < g.N) {
+        Y[(size_t)row * g.ldy + n] = g.alpha * acc[i][0];
+      }
+    }
+  }
+}
+
+// Small-N form (N <= 8 columns per batch entry): one thread per output row.
+template <int NC>
+__global__ void __launch_bounds__(128) gemv_kernel(GemmArgs g) {
+  extern __shared__ double xs[];  // K x NC
+  const int z = blockIdx.y;
+  const double* A = g.A + (size_t)z * g.sA;
+  const double* X = g.X + (size_t)z * g.sX;
+  double* Y = g.Y + (size_t)z * g.sY;
+  for (int idx = threadIdx.x; idx < g.K * NC; idx += blockDim.x) {
+    const int k = idx / NC, c = idx - k * NC;
+    xs[idx] = (c < g.N) ? X[(size_t)k * g.ldx + c] : 0.0;
+  }
+  __syncthreads();
+  const int row = blockIdx.x * blockDim.x + threadIdx.x;
+  if (row >= g.rows) return;
+  double acc[NC];
+#pragma unroll
+  for (int c = 0; c < NC; ++c) acc[c] = 0.0;
+  for (int k = 0; k < g.K; ++k) {
+    const double av = A[(size_t)k * g.lda + row];
+#pragma unroll
+    for (int c = 0; c < NC; ++c) acc[c] = fma(av, xs[k * NC + c], acc[c]);
+  }
+#pragma unroll
+  for (int c = 0; c < NC; ++c)
+    if (c < g.N) Y[(size_t)row * g.ldy + c] = g.alpha * acc[c];
+}
+
+template <int RPT>
+static cudaError_t launch_tile(const GemmArgs& g, int row_blocks, cudaStream_t s) {
+  dim3 grid((g.N + 63) / 64, row_blocks, g.batch);
+  gemm_tile_kernel<RPT><<<grid, 256, 0, s>>>(g);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gemm(const GemmArgs& g, cudaStream_t s) {
+  if (g.rows <= 0 || g.N <= 0 || g.batch <= 0) return cudaSuccess;
+  if (g.N <= 8) {
+    dim3 grid((g.rows + 127) / 128, g.batch);
+    const size_t sm = (size_t)g.K * 8 * sizeof(double);
+    if (g.N <= 2) gemv_kernel<2><<<grid, 128, (size_t)g.K * 2 * sizeof(double), s>>>(g);
+    else if (g.N <= 4) gemv_kernel<4><<<grid, 128, (size_t)g.K * 4 * sizeof(double), s>>>(g);
+    else gemv_kernel<8><<<grid, 128, sm, s>>>(g);
+    return cudaGetLastError();
+  }
+  // Choose rows per thread: cover all rows in one block when there is
+  // enough column parallelism, otherwise split the rows across blocks.
+  int dev = 0, nsm = 152;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  const long col_blocks = (long)((g.N + 63) / 64) * g.batch;
+  int rpt = (g.rows + 7) / 8;
+  if (rpt > 16) rpt = 16;
+  while (rpt > 1 && col_blocks * ((g.rows + 8 * rpt - 1) / (8 * rpt)) < 2L * nsm) rpt = (rpt + 1) / 2;
+  const int rb = (g.rows + 8 * rpt - 1) / (8 * rpt);
+  switch (rpt) {
+    case 1: return launch_tile<1>(g, rb, s);
+    case 2: return launch_tile<2>(g, rb, s);
+    case 3: return launch_tile<3>(g, rb, s);
+    case 4: return launch_tile<4>(g, rb, s);
+    case 5: return launch_tile<5>(g, rb, s);
+    case 6: return launch_tile<6>(g, rb, s);
+    case 7: return launch_tile<7>(g, rb, s);
+    case 8: return launch_tile<8>(g, rb, s);
+    case 9: return launch_tile<9>(g, rb, s);
+    case 10: return launch_tile<10>(g, rb, s);
+    case 11: return launch_tile<11>(g, rb, s);
+    case 12: return launch_tile<12>(g, rb, s);
+    case 13: return launch_tile<13>(g, rb, s);
+    case 14: return launch_tile<14>(g, rb, s);
+    case 15: return launch_tile<15>(g, rb, s);
+    default: return launch_tile<16>(g, rb, s);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// IMEX right-hand sides (rhs_construct_temp / _vort / _uphi_bar,
+// src/rhs_create.F90:24-385), one thread per (r, m, b).
+// ---------------------------------------------------------------------------
+__global__ void imex_rhs_kernel(RhsArgs a) {
+  const size_t total = (size_t)a.R * a.M * a.B;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total;
+       e += (size_t)gridDim.x * blockDim.x) {
+    const int b = (int)(e % a.B);
+    const size_t rm = e / a.B;
+    const int m = (int)(rm % a.M);
+    const int r = (int)(rm / a.M);
+    const double ir = a.inv_r[r], ir2 = a.inv_r2[r];
+    const double dm = (double)m, mm = dm * dm;
+    const double dt = a.dt;
+    // explicit (advective) term of T: i m r^-1 (uphi T) + d(ur T)/dr + r^-1 (ur T)
+    {
+      const double2 p = a.ntp[e], q = a.ntr[e], dq = a.dntr[e];
+      const double2 nt = make_double2(-dm * ir * p.y + dq.x + ir * q.x, dm * ir * p.x + dq.y + ir * q.y);
+      a.nt_new[e] = nt;
+      double2 rhs;
+      if (a.scheme_cn) {
+        const double2 T = a.th[0][e], L = a.lt[e];
+        const double c = (1.0 - a.w_imp[0]) * dt * a.inv_pr;
+        rhs = make_double2(T.x + c * (L.x - mm * ir2 * T.x), T.y + c * (L.y - mm * ir2 * T.y));
+      } else {
+        rhs = make_double2(0.0, 0.0);
+        for (int i = 0; i < a.n_imp; ++i) {
+          const double2 h = a.th[i][e];
+          rhs.x += a.w_imp[i] * h.x; rhs.y += a.w_imp[i] * h.y;
+        }
+      }
+      for (int i = 0; i < a.n_exp; ++i) {
+        const double2 h = (i == 0) ? nt : a.nth[i][e];
+        rhs.x -= dt * (a.w_exp[i] * h.x); rhs.y -= dt * (a.w_exp[i] * h.y);
+      }
+      if (r == 0) rhs = make_double2(m == 0 ? 1.0 : 0.0, 0.0);
+      if (r == a.R - 1) rhs = make_double2(0.0, 0.0);
+      a.rhs_t[e] = rhs;
+    }
+    if (m > 0) {
+      const double2 p = a.nwp[e], q = a.nwr[e], dq = a.dnwr[e];
+      const double2 nw = make_double2(-dm * ir * p.y + dq.x + ir * q.x, dm * ir * p.x + dq.y + ir * q.y);
+      a.nw_new[e] = nw;
+      double2 rhs;
+      if (a.scheme_cn) {
+        const double2 W = a.wh[0][e], L = a.lw[e], To = a.th[0][e];
+        const double c = (1.0 - a.w_imp[0]) * dt;
+        const double bc = a.ra_pr[b] * dt * 0.5 * dm * ir;  // old-T half of the CN buoyancy
+        rhs = make_double2(W.x + c * (L.x - mm * ir2 * W.x) + bc * To.y,
+                           W.y + c * (L.y - mm * ir2 * W.y) - bc * To.x);
+      } else {
+        rhs = make_double2(0.0, 0.0);
+        for (int i = 0; i < a.n_imp; ++i) {
+          const double2 h = a.wh[i][e];
+          rhs.x += a.w_imp[i] * h.x; rhs.y += a.w_imp[i] * h.y;
+        }
+      }
+      for (int i = 0; i < a.n_exp; ++i) {
+        const double2 h = (i == 0) ? nw : a.nwh[i][e];
+        rhs.x -= dt * (a.w_exp[i] * h.x); rhs.y -= dt * (a.w_exp[i] * h.y);
+      }
+      if (r == 0 || r == a.R - 1) rhs = make_double2(0.0, 0.0);
+      a.rhs_w[e] = rhs;
+    } else {
+      // mean azimuthal flow: rhs_construct_uphi_bar
+      const size_t rb = (size_t)r * a.B + b;
+      const double urom = a.nwr[e].x;  // mode-0 coefficient of ur*omg = its azimuthal mean
+      a.urom_new[rb] = urom;
+      double rhs;
+      if (a.scheme_cn) {
+        const double u = a.ubh[0][rb];
+        const double lu = a.lu0[rb].x;
+        rhs = u + (1.0 - a.w_imp[0]) * dt * (lu - ir2 * u);
+      } else {
+        rhs = 0.0;
+        for (int i = 0; i < a.n_imp; ++i) rhs += a.w_imp[i] * a.ubh[i][rb];
+      }
+      for (int i = 0; i < a.n_exp; ++i) {
+        const double h = (i == 0) ? urom : a.uromh[i][rb];
+        rhs -= dt * (a.w_exp[i] * h);
+      }
+      if (r == 0 || r == a.R - 1) rhs = 0.0;
+      a.rhs_w[e] = make_double2(rhs, 0.0);
+    }
+  }
+}
+
+static int ew_grid(size_t n) {
+  size_t g = (n + 255) / 256;
+  if (g > 152 * 32) g = 152 * 32;
+  return (int)(g ? g : 1);
+}
+
+cudaError_t launch_imex_rhs(const RhsArgs& a, cudaStream_t s) {
+  imex_rhs_kernel<<<ew_grid((size_t)a.R * a.M * a.B), 256, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+__global__ void add_buoyancy_kernel(int R, int M, int B, const double* inv_r, const double* ra_pr,
+                                    double scale, const double2* t_new, double2* rhs_w, double2* buo_out) {
+  const size_t total = (size_t)R * M * B;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total;
+       e += (size_t)gridDim.x * blockDim.x) {
+    const int b = (int)(e % B);
+    const size_t rm = e / B;
+    const int m = (int)(rm % M);
+    const int r = (int)(rm / M);
+    if (m == 0) continue;
+    const double2 T = t_new[e];
+    const double f = (double)m * inv_r[r];
+    // buoyancy term -(Ra/Pr) i m r^-1 T
+    const double2 bu = make_double2(ra_pr[b] * f * T.y, -ra_pr[b] * f * T.x);
+    if (buo_out) buo_out[e] = bu;
+    if (rhs_w && r > 0 && r < R - 1) {
+      double2 v = rhs_w[e];
+      v.x += scale * bu.x; v.y += scale * bu.y;
+      rhs_w[e] = v;
+    }
+  }
+}
+
+cudaError_t launch_add_buoyancy(int R, int M, int B, const double* inv_r, const double* ra_pr,
+                                double scale, const double2* t_new, double2* rhs_w, double2* buo_out,
+                                cudaStream_t s) {
+  add_buoyancy_kernel<<<ew_grid((size_t)R * M * B), 256, 0, s>>>(R, M, B, inv_r, ra_pr, scale, t_new,
+                                                                  rhs_w, buo_out);
+  return cudaGetLastError();
+}
+
+// u_r = i m r^-1 psi (m >= 1); mode 0: u_phi = uphi_bar, omega = uphi_bar/r +
+// d uphi_bar/dr, u_r = 0 (src/fourierloop.F90:267-315).
+__global__ void post_w_kernel(int R, int M, int B, const double* inv_r, const double2* psi, double2* ur,
+                              double2* up, double2* w, const double* ub, double* ubar_new) {
+  const size_t total = (size_t)R * M * B;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total;
+       e += (size_t)gridDim.x * blockDim.x) {
+    const int b = (int)(e % B);
+    const size_t rm = e / B;
+    const int m = (int)(rm % M);
+    const int r = (int)(rm / M);
+    if (m > 0) {
+      const double2 ps = psi[e];
+      const double f = (double)m * inv_r[r];
+      ur[e] = make_double2(-f * ps.y, f * ps.x);
+    } else {
+      const double u = ub[(size_t)r * 2 * B + 2 * b];
+      const double du = ub[(size_t)(R + r) * 2 * B + 2 * b];
+      up[e] = make_double2(u, 0.0);
+      ur[e] = make_double2(0.0, 0.0);
+      w[e] = make_double2(u * inv_r[r] + du, 0.0);
+      if (ubar_new) ubar_new[(size_t)r * B + b] = u;
+    }
+  }
+}
+
+cudaError_t launch_post_w(int R, int M, int B, const double* inv_r, const double2* psi, double2* ur,
+                          double2* up, double2* w, const double* ub, double* ubar_new, cudaStream_t s) {
+  post_w_kernel<<<ew_grid((size_t)R * M * B), 256, 0, s>>>(R, M, B, inv_r, psi, ur, up, w, ub, ubar_new);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// IMEXRK stage right-hand side (Get_stage_var, src/fourierloop_imexrk.F90:
+// 214-354): Y0 + dt * (sum_i aD(s,i) F_d(i) + aA(s,i) F_a(i)) [+ buoyancy].
+// The buoyancy of the current stage is added after the temperature solve.
+// ---------------------------------------------------------------------------
+__global__ void stage_rhs_kernel(StageArgs a) {
+  const size_t total = (size_t)a.R * a.M * a.B;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total;
+       e += (size_t)gridDim.x * blockDim.x) {
+    const int b = (int)(e % a.B);
+    const size_t rm = e / a.B;
+    const int m = (int)(rm % a.M);
+    const int r = (int)(rm / a.M);
+    const double dt = a.dt;
+    {
+      double2 fd = make_double2(0, 0), fa = make_double2(0, 0);
+      for (int i = 0; i < a.st; ++i) {
+        const double2 q = a.fdt[i][e];
+        fd.x += a.aD[i] * q.x; fd.y += a.aD[i] * q.y;
+      }
+      for (int i = 0; i < a.st; ++i) {
+        const double2 q = a.fat[i][e];
+        fa.x += a.aA[i] * q.x; fa.y += a.aA[i] * q.y;
+      }
+      const double2 y0 = a.t0[e];
+      double2 rhs = make_double2(y0.x + dt * (fd.x + fa.x), y0.y + dt * (fd.y + fa.y));
+      if (r == 0) rhs = make_double2(m == 0 ? 1.0 : 0.0, 0.0);
+      if (r == a.R - 1) rhs = make_double2(0.0, 0.0);
+      a.rhs_t[e] = rhs;
+    }
+    double2 fd = make_double2(0, 0), fa = make_double2(0, 0), fb = make_double2(0, 0);
+    for (int i = 0; i < a.st; ++i) {
+      const double2 q = a.fdw[i][e];
+      fd.x += a.aD[i] * q.x; fd.y += a.aD[i] * q.y;
+    }
+    for (int i = 0; i < a.st; ++i) {
+      const double2 q = a.faw[i][e];
+      fa.x += a.aA[i] * q.x; fa.y += a.aA[i] * q.y;
+    }
+    if (m == 0) {
+      const double y0 = a.u0[(size_t)r * a.B + b];
+      double rhs = y0 + dt * (fd.x + fa.x);
+      if (r == 0 || r == a.R - 1) rhs = 0.0;
+      a.rhs_w[e] = make_double2(rhs, 0.0);
+    } else {
+      for (int i = 0; i < a.st; ++i) {
+        const double2 q = a.buo[i][e];
+        const double c = a.buo_imp ? a.aD[i] : a.aA[i];
+        fb.x += c * q.x; fb.y += c * q.y;
+      }
+      const double2 y0 = a.w0[e];
+      double2 rhs = make_double2(y0.x + dt * (fd.x + fa.x + fb.x), y0.y + dt * (fd.y + fa.y + fb.y));
+      if (r == 0 || r == a.R - 1) rhs = make_double2(0.0, 0.0);
+      a.rhs_w[e] = rhs;
+    }
+  }
+}
+
+cudaError_t launch_stage_rhs(const StageArgs& a, cudaStream_t s) {
+  stage_rhs_kernel<<<ew_grid((size_t)a.R * a.M * a.B), 256, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+// Stage derivatives (RHS_construct_stage, src/fourierloop_imexrk.F90:403-497
+// with src/rhs_create_imexrk.F90): advective -N, diffusive L f, and the
+// stage-1 buoyancy.
+__global__ void stage_deriv_kernel(StageArgs a) {
+  const size_t total = (size_t)a.R * a.M * a.B;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total;
+       e += (size_t)gridDim.x * blockDim.x) {
+    const int b = (int)(e % a.B);
+    const size_t rm = e / a.B;
+    const int m = (int)(rm % a.M);
+    const int r = (int)(rm / a.M);
+    const double ir = a.inv_r[r], ir2 = a.inv_r2[r];
+    const double dm = (double)m, mm = dm * dm;
+    {
+      const double2 p = a.ntp[e], q = a.ntr[e], dq = a.dntr[e];
+      a.fat_out[e] = make_double2(-(-dm * ir * p.y + dq.x + ir * q.x), -(dm * ir * p.x + dq.y + ir * q.y));
+      const double2 T = a.t[e], L = a.lt[e];
+      a.fdt_out[e] = make_double2(a.inv_pr * (L.x - mm * ir2 * T.x), a.inv_pr * (L.y - mm * ir2 * T.y));
+    }
+    if (m == 0) {
+      const size_t rb = (size_t)r * a.B + b;
+      a.faw_out[e] = make_double2(-a.nwr[e].x, 0.0);
+      const double u = a.up[e].x;
+      a.fdw_out[e] = make_double2(a.lu0[rb].x - ir2 * u, 0.0);
+    } else {
+      const double2 p = a.nwp[e], q = a.nwr[e], dq = a.dnwr[e];
+      a.faw_out[e] = make_double2(-(-dm * ir * p.y + dq.x + ir * q.x), -(dm * ir * p.x + dq.y + ir * q.y));
+      const double2 W = a.w[e], L = a.lw[e];
+      a.fdw_out[e] = make_double2(L.x - mm * ir2 * W.x, L.y - mm * ir2 * W.y);
+      if (a.buo_out) {
+        const double2 T = a.t[e];
+        const double f = dm * ir;
+        a.buo_out[e] = make_double2(a.ra_pr[b] * f * T.y, -a.ra_pr[b] * f * T.x);
+      }
+    }
+  }
+}
+
+cudaError_t launch_stage_deriv(const StageArgs& a, cudaStream_t s) {
+  stage_deriv_kernel<<<ew_grid((size_t)a.R * a.M * a.B), 256, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Layout transforms and small helpers
+// ---------------------------------------------------------------------------
+__global__ void scatter_instance_kernel(int R, int M, int B, int b, const double2* src, double2* dst) {
+  const int n = R * M;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int r = i / M, m = i - r * M;  // src index m + M r (Fortran (M,R))
+    dst[((size_t)r * M + m) * B + b] = src[i];
+  }
+}
+__global__ void gather_instance_kernel(int R, int M, int B, int b, const double2* src, double2* dst) {
+  const int n = R * M;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int r = i / M, m = i - r * M;
+    dst[i] = src[((size_t)r * M + m) * B + b];
+  }
+}
+cudaError_t launch_scatter_instance(int R, int M, int B, int b, const double2* src, double2* dst,
+                                    cudaStream_t s) {
+  scatter_instance_kernel<<<ew_grid((size_t)R * M), 256, 0, s>>>(R, M, B, b, src, dst);
+  return cudaGetLastError();
+}
+cudaError_t launch_gather_instance(int R, int M, int B, int b, const double2* src, double2* dst,
+                                   cudaStream_t s) {
+  gather_instance_kernel<<<ew_grid((size_t)R * M), 256, 0, s>>>(R, M, B, b, src, dst);
+  return cudaGetLastError();
+}
+__global__ void extract_mode0_kernel(int R, int M, int B, const double2* src, double* dst) {
+  const int n = R * B;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int r = i / B, b = i - r * B;
+    dst[i] = src[(size_t)r * M * B + b].x;
+  }
+}
+cudaError_t launch_extract_mode0(int R, int M, int B, const double2* src, double* dst, cudaStream_t s) {
+  extract_mode0_kernel<<<ew_grid((size_t)R * B), 256, 0, s>>>(R, M, B, src, dst);
+  return cudaGetLastError();
+}
+
+// dgetrs 'N' (src/algebra_lapack.F90:36-37) for many systems: row
+// interchanges, unit-lower forward substitution, upper back substitution,
+// in the column order of the reference BLAS dtrsm.  One warp per right-hand
+// side; the column updates are spread over the lanes.
+__global__ void getrs_kernel(int n, int nsys, int nrhs, const double* lu, const int* ipiv, double* b) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp >= nsys * nrhs) return;
+  const int sys = warp / nrhs;
+  const double* A = lu + (size_t)sys * n * n;
+  const int* pv = ipiv + (size_t)sys * n;
+  double* x = b + (size_t)warp * n;
+  if (lane == 0)
+    for (int i = 0; i < n; ++i) {
+      const int p = pv[i] - 1;
+      if (p != i) { const double t = x[i]; x[i] = x[p]; x[p] = t; }
+    }
+  __syncwarp();
+  for (int j = 0; j < n; ++j) {
+    const double xj = x[j];
+    __syncwarp();
+    if (xj != 0.0)
+      for (int i = j + 1 + lane; i < n; i += 32) x[i] -= xj * A[(size_t)j * n + i];
+    __syncwarp();
+  }
+  for (int j = n - 1; j >= 0; --j) {
+    double xj = x[j];
+    __syncwarp();
+    if (xj != 0.0) {
+      xj = xj / A[(size_t)j * n + j];
+      __syncwarp();
+      if (lane == 0) x[j] = xj;
+      for (int i = lane; i < j; i += 32) x[i] -= xj * A[(size_t)j * n + i];
+    }
+    __syncwarp();
+  }
+}
+
+cudaError_t launch_getrs_batched(int n, int nsys, int nrhs, const double* lu, const int* ipiv,
+                                 double* b, cudaStream_t s) {
+  const int warps = nsys * nrhs;
+  const int threads = 128;
+  const int grid = (warps * 32 + threads - 1) / threads;
+  getrs_kernel<<<grid, threads, 0, s>>>(n, nsys, nrhs, lu, ipiv, b);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// FP64 FMA throughput (the roofline denominator of every kernel above).
+// ---------------------------------------------------------------------------
+__global__ void fp64_peak_kernel(double* out, int iters, double a, double c) {
+  double x0 = threadIdx.x * 1e-3, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3;
+  double x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+      x0 = fma(x0, a, c); x1 = fma(x1, a, c); x2 = fma(x2, a, c); x3 = fma(x3, a, c);
+      x4 = fma(x4, a, c); x5 = fma(x5, a, c); x6 = fma(x6, a, c); x7 = fma(x7, a, c);
+    }
+  }
+  out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+}
+
+double measure_fp64_peak() {
+  int dev = 0, nsm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return -1.0;
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  const int blocks = nsm * 4, threads = 256, iters = 200;
+  double* out = nullptr;
+  if (cudaMalloc(&out, sizeof(double) * blocks * threads) != cudaSuccess) return -1.0;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  fp64_peak_kernel<<<blocks, threads>>>(out, 20, 1.0000001, 1e-9);
+  float best = 1e30f;
+  for (int rep = 0; rep < 3; ++rep) {
+    cudaEventRecord(e0);
+    fp64_peak_kernel<<<blocks, threads>>>(out, iters, 1.0000001, 1e-9);
+    cudaEventRecord(e1);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (ms < best) best = ms;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  if (cudaGetLastError() != cudaSuccess) return -1.0;
+  const double flops = 2.0 * 8 * 16 * (double)iters * blocks * threads;
+  return flops / (best * 1e-3) / 1e9;
+}
+
+}  // namespace falcon
+
+namespace falcon {
+
+// out[c][i] = sum_k A[i*n + k] * in[c][k] for complex columns (A real,
+// row-major n x n): the Chebyshev transforms as dense operators.
+__global__ void apply_cols_kernel(int n, int ncol, const double* A, const double2* in, double2* out) {
+  const int c = blockIdx.y;
+  const double2* x = in + (size_t)c * n;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    double sr = 0.0, si = 0.0;
+    for (int k = 0; k < n; ++k) {
+      const double a = A[(size_t)i * n + k];
+      const double2 v = x[k];
+      sr = fma(a, v.x, sr);
+      si = fma(a, v.y, si);
+    }
+    out[(size_t)c * n + i] = make_double2(sr, si);
+  }
+}
+
+cudaError_t launch_apply_cols(int n, int ncol, const double* A, const double2* in, double2* out, cudaStream_t s) {
+  dim3 grid((n + 127) / 128, ncol);
+  apply_cols_kernel<<<grid, 128, 0, s>>>(n, ncol, A, in, out);
+  return cudaGetLastError();
+}
+
+// dst[row][j] = map[j] >= 0 ? src[row][map[j]] : 0 (instance-column remap of
+// a [rows][B] array, elements of `ew` doubles).
+__global__ void remap_cols_kernel(const double* src, double* dst, size_t rows, int bs, int bd, int ew,
+                                  const int* map) {
+  const size_t total = rows * (size_t)bd * ew;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+    const int q = (int)(i % ew);
+    const size_t rj = i / ew;
+    const int j = (int)(rj % bd);
+    const size_t row = rj / bd;
+    const int sj = map[j];
+    dst[i] = (sj >= 0 && src) ? src[(row * bs + sj) * ew + q] : 0.0;
+  }
+}
+
+cudaError_t launch_remap_cols(const double* src, double* dst, size_t rows, int bs, int bd, int ew, const int* map,
+                              cudaStream_t s) {
+  const size_t total = rows * (size_t)bd * ew;
+  size_t g = (total + 255) / 256;
+  if (g > 152 * 64) g = 152 * 64;
+  if (g == 0) g = 1;
+  remap_cols_kernel<<<(int)g, 256, 0, s>>>(src, dst, rows, bs, bd, ew, map);
+  return cudaGetLastError();
+}
+
+}  // namespace falcon

@@ -1,0 +1,269 @@
+"""Python binding of libfalcon_gpu (the C ABI declared in include/falcon_gpu.h).
+
+Mirrors the reference's driver interface for the time-step path:
+``solver_init`` (src/solver.F90:38-66) -> :class:`Instance` / :class:`Batch`
+construction, ``timeloop_*`` step bodies -> :meth:`step`, and
+``writeKE_spectral`` (src/output.F90:122-324) -> :meth:`diagnostics`.  Fields
+are numpy complex128 arrays of shape (Nr_max, Nm_max+1), i.e. the Fortran
+(Nm_max+1, Nr_max) layout, mode fastest.
+
+There is no CPU fallback: importing works anywhere, but creating an instance
+raises if the CUDA library or a GPU is missing.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libfalcon_gpu.so")
+
+FALCON_IMEX, FALCON_IMEXRK, FALCON_RK = 0, 1, 2
+IMP = {"CN": 0, "BDF2": 1, "BDF3": 2, "BDF4": 3, "ARS443": 10, "ARS343": 11, "BPR353": 12,
+       "ARS222": 13, "NONE": 20}
+EXP = {"AB2": 0, "AB3": 1, "AB4": 2, "expARS443": 10, "expARS343": 11, "expBPR353": 12,
+       "expARS222": 13, "RK2": 20, "RK4": 21}
+TYPE = {"IMEX": 0, "IMEXRK": 1, "RK": 2}
+SCHEMES = {
+    "CNAB2": ("IMEX", "CN", "AB2"),
+    "CNAB3": ("IMEX", "CN", "AB3"),
+    "SBDF2": ("IMEX", "BDF2", "AB2"),
+    "SBDF3": ("IMEX", "BDF3", "AB3"),
+    "SBDF4": ("IMEX", "BDF4", "AB4"),
+    "ARS443": ("IMEXRK", "ARS443", "expARS443"),
+    "ARS343": ("IMEXRK", "ARS343", "expARS343"),
+    "BPR353": ("IMEXRK", "BPR353", "expBPR353"),
+    "ARS222": ("IMEXRK", "ARS222", "expARS222"),
+}
+
+
+class FalconParams(ctypes.Structure):
+    _fields_ = [
+        ("nr_max", ctypes.c_int), ("nm_max", ctypes.c_int),
+        ("eta", ctypes.c_double), ("ra", ctypes.c_double), ("pr", ctypes.c_double),
+        ("mbc", ctypes.c_int), ("ampT", ctypes.c_double),
+        ("l_add_pert", ctypes.c_int), ("lagpts", ctypes.c_int), ("n_init", ctypes.c_int),
+        ("buo_imp", ctypes.c_int), ("n_time_steps", ctypes.c_int),
+        ("dt", ctypes.c_double), ("totaltime", ctypes.c_double),
+        ("l_vartimestep", ctypes.c_int), ("l_optimizedt", ctypes.c_int),
+        ("scheme_type", ctypes.c_int), ("scheme_imp", ctypes.c_int), ("scheme_exp", ctypes.c_int),
+        ("l_imexrk_started", ctypes.c_int),
+        ("dt_coef", ctypes.c_double), ("dt_max", ctypes.c_double), ("cfl", ctypes.c_double),
+        ("l_restart", ctypes.c_int), ("n_restart", ctypes.c_int), ("n_restart_point", ctypes.c_int),
+        ("n_snapshot_point", ctypes.c_int), ("tag", ctypes.c_char * 100),
+        ("n_checkpoint", ctypes.c_int), ("n_snapshot", ctypes.c_int), ("n_KE", ctypes.c_int),
+        ("n_KEspec", ctypes.c_int),
+    ]
+
+
+class FalconDiag(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_double) for n in
+                ("time", "dt", "ke", "ke_r", "ke_phi", "ke_upbar", "nu_top", "nu_bot", "vis", "buo")]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
+class FalconError(RuntimeError):
+    pass
+
+
+_lib = None
+EXPORTS = (
+    "falcon_params_default", "falcon_params_read_namelist", "falcon_params_set_scheme",
+    "falcon_create", "falcon_destroy", "falcon_init_state", "falcon_set_state", "falcon_get_state",
+    "falcon_step", "falcon_diagnostics", "falcon_batch_create", "falcon_batch_destroy",
+    "falcon_batch_size", "falcon_batch_ngroups", "falcon_batch_init_state", "falcon_batch_set_state",
+    "falcon_batch_get_state", "falcon_batch_step", "falcon_batch_diagnostics", "falcon_batch_set_stream",
+    "falcon_batch_device_bytes", "falcon_nonlin_dev", "falcon_nonlin", "falcon_getrs_batched_dev",
+    "falcon_cheb_fwd_dev", "falcon_cheb_inv_dev", "falcon_cheb_d1_dev", "falcon_cheb_d2_dev",
+    "falcon_server_create", "falcon_server_destroy", "falcon_server_submit", "falcon_server_iterate",
+    "falcon_server_poll", "falcon_last_error", "falcon_version", "falcon_fp64_peak_gflops",
+)
+
+
+def lib():
+    """Load libfalcon_gpu.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise FalconError("libfalcon_gpu.so is not built: run falcon-dns_gb300/build.py")
+    L = ctypes.CDLL(LIB_PATH)
+    P = ctypes.POINTER
+    dp, vp, ip = P(ctypes.c_double), ctypes.c_void_p, ctypes.c_int
+    pp = P(FalconParams)
+    L.falcon_last_error.restype = ctypes.c_char_p
+    L.falcon_version.restype = ctypes.c_char_p
+    L.falcon_params_default.argtypes = [pp]
+    L.falcon_params_read_namelist.argtypes = [ctypes.c_char_p, pp]
+    L.falcon_params_set_scheme.argtypes = [pp, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p]
+    L.falcon_create.argtypes = [pp, P(vp)]
+    L.falcon_destroy.argtypes = [vp]
+    L.falcon_destroy.restype = None
+    L.falcon_init_state.argtypes = [vp, ip, ctypes.c_double, ctypes.c_uint64]
+    L.falcon_set_state.argtypes = [vp, dp, dp, dp, dp]
+    L.falcon_get_state.argtypes = [vp, dp, dp, dp, dp, dp]
+    L.falcon_step.argtypes = [vp, ip]
+    L.falcon_diagnostics.argtypes = [vp, P(FalconDiag)]
+    L.falcon_batch_create.argtypes = [pp, ip, P(vp)]
+    L.falcon_batch_destroy.argtypes = [vp]
+    L.falcon_batch_destroy.restype = None
+    L.falcon_batch_size.argtypes = [vp]
+    L.falcon_batch_ngroups.argtypes = [vp]
+    L.falcon_batch_init_state.argtypes = [vp, ip, ctypes.c_double, P(ctypes.c_uint64)]
+    L.falcon_batch_set_state.argtypes = [vp, ip, dp, dp, dp, dp]
+    L.falcon_batch_get_state.argtypes = [vp, ip, dp, dp, dp, dp, dp]
+    L.falcon_batch_step.argtypes = [vp, ip]
+    L.falcon_batch_diagnostics.argtypes = [vp, P(FalconDiag)]
+    L.falcon_batch_set_stream.argtypes = [vp, vp]
+    L.falcon_batch_device_bytes.argtypes = [vp]
+    L.falcon_batch_device_bytes.restype = ctypes.c_size_t
+    L.falcon_nonlin_dev.argtypes = [ip, ip, ip] + [ctypes.c_void_p] * 8 + [vp]
+    L.falcon_nonlin.argtypes = [ip, ip] + [dp] * 8
+    L.falcon_getrs_batched_dev.argtypes = [ip, ip, ip, vp, vp, vp, vp]
+    for f in ("falcon_cheb_fwd_dev", "falcon_cheb_inv_dev", "falcon_cheb_d1_dev", "falcon_cheb_d2_dev"):
+        getattr(L, f).argtypes = [ip, ip, vp, vp, vp]
+    L.falcon_server_create.argtypes = [ctypes.c_size_t, ip, P(vp)]
+    L.falcon_server_destroy.argtypes = [vp]
+    L.falcon_server_destroy.restype = None
+    L.falcon_server_submit.argtypes = [vp, pp, ctypes.c_uint64, ip, P(ctypes.c_int64)]
+    L.falcon_server_iterate.argtypes = [vp, P(ctypes.c_int), P(ctypes.c_int)]
+    L.falcon_server_poll.argtypes = [vp, ctypes.c_int64, P(ctypes.c_int), P(FalconDiag), dp]
+    L.falcon_fp64_peak_gflops.restype = ctypes.c_double
+    _lib = L
+    return L
+
+
+def check(rc):
+    if rc != 0:
+        msg = lib().falcon_last_error().decode()
+        raise FalconError(f"falcon error {rc}: {msg}")
+    return rc
+
+
+def _dp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double)) if a is not None else None
+
+
+def default_params():
+    p = FalconParams()
+    check(lib().falcon_params_default(ctypes.byref(p)))
+    return p
+
+
+def read_namelist(path):
+    """readNamelists (src/namelists.F90:49-110) through the C ABI."""
+    p = FalconParams()
+    check(lib().falcon_params_read_namelist(str(path).encode(), ctypes.byref(p)))
+    return p
+
+
+def make_params(nr, nm, scheme="CNAB2", eta=0.35, ra=1e5, pr=1.0, dt=1e-5, mbc="NS", lagpts=16,
+                buo="IMP"):
+    p = default_params()
+    p.nr_max, p.nm_max, p.eta, p.ra, p.pr, p.dt = nr, nm, eta, ra, pr, dt
+    p.mbc = 0 if mbc == "NS" else 1
+    p.lagpts = lagpts
+    p.buo_imp = 1 if buo == "IMP" else 0
+    p.l_vartimestep = 0
+    p.l_imexrk_started = 0
+    typ, imp, exp = SCHEMES[scheme]
+    check(lib().falcon_params_set_scheme(ctypes.byref(p), typ.encode(), imp.encode(), exp.encode()))
+    return p
+
+
+def _field(shape):
+    return np.empty(shape, np.complex128)
+
+
+class Batch:
+    """Independent annulus instances stepped together on the GPU."""
+
+    def __init__(self, params):
+        params = list(params)
+        arr = (FalconParams * len(params))(*params)
+        h = ctypes.c_void_p()
+        check(lib().falcon_batch_create(arr, len(params), ctypes.byref(h)))
+        self.h = h
+        self.params = params
+        self.n = len(params)
+
+    def close(self):
+        if getattr(self, "h", None) is not None and self.h.value:
+            lib().falcon_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def ngroups(self):
+        return lib().falcon_batch_ngroups(self.h)
+
+    @property
+    def device_bytes(self):
+        return lib().falcon_batch_device_bytes(self.h)
+
+    def init_noise(self, seeds, amp=1e-3):
+        s = (ctypes.c_uint64 * self.n)(*[int(x) for x in seeds])
+        check(lib().falcon_batch_init_state(self.h, 1, amp, s))
+
+    def init_reference(self):
+        check(lib().falcon_batch_init_state(self.h, 0, 0.0, None))
+
+    def set_state(self, i, t, om=None, up=None, ur=None):
+        arrs = [None if a is None else np.ascontiguousarray(a, np.complex128) for a in (t, om, up, ur)]
+        check(lib().falcon_batch_set_state(self.h, i, *[_dp(a) for a in arrs]))
+
+    def get_state(self, i):
+        p = self.params[i]
+        shape = (p.nr_max, p.nm_max + 1)
+        arrs = [_field(shape) for _ in range(5)]
+        check(lib().falcon_batch_get_state(self.h, i, *[_dp(a) for a in arrs]))
+        return dict(zip(("T", "omg", "up", "ur", "psi"), arrs))
+
+    def step(self, n=1):
+        check(lib().falcon_batch_step(self.h, n))
+
+    def set_stream(self, stream_ptr):
+        check(lib().falcon_batch_set_stream(self.h, ctypes.c_void_p(stream_ptr)))
+
+    def diagnostics(self):
+        out = (FalconDiag * self.n)()
+        check(lib().falcon_batch_diagnostics(self.h, out))
+        return [d.as_dict() for d in out]
+
+
+class Instance(Batch):
+    """One annulus instance (a batch of one)."""
+
+    def __init__(self, params):
+        super().__init__([params])
+
+    def init_noise(self, seed, amp=1e-3):
+        super().init_noise([seed], amp)
+
+    def get_state(self, i=0):
+        return super().get_state(0)
+
+    def set_state(self, t, om=None, up=None, ur=None):
+        super().set_state(0, t, om, up, ur)
+
+    def diagnostics(self):
+        return super().diagnostics()[0]
+
+
+def nonlin(nm, t, om, up, ur):
+    """Nr_maxLOOP for one instance through the host-array C entry point."""
+    ins = [np.ascontiguousarray(a, np.complex128) for a in (t, om, up, ur)]
+    outs = [np.empty_like(ins[0]) for _ in range(4)]
+    check(lib().falcon_nonlin(ins[0].shape[0], nm, *[_dp(a) for a in ins], *[_dp(o) for o in outs]))
+    return outs
+
+
+def fp64_peak_gflops():
+    return lib().falcon_fp64_peak_gflops()

@@ -1,0 +1,193 @@
+/*
+ * falcon_gpu.h -- C ABI of the GB300 (sm_103a) implementation of the
+ * FAlCon-DNS per-time-step hot path.
+ *
+ * The reference (FAlCon-DNS, Fortran) advances one annulus instance with
+ * `timeloop_imex` / `timeloop_imexrk` (src/steptime.F90:52,
+ * src/steptime_imexrk.F90:50), whose per-step body is the nonlinear pass
+ * `Nr_maxLOOP` (src/nonlin.F90:35) followed by the per-mode implicit solves
+ * (`Nm_maxLOOP`, src/fourierloop.F90:156; `Get_stage_var`,
+ * src/fourierloop_imexrk.F90:75).  This header is the drop-in boundary a
+ * Fortran host binds through ISO_C_BINDING and the C++
+ * driver and Python harness bind directly.
+ *
+ * Conventions
+ *  - Every call returns 0 on success or a negative FALCON_E* code; the text
+ *    of the last error of the calling thread is in falcon_last_error().
+ *  - Complex fields use the reference's Fortran layout X(Nm_max+1, Nr_max):
+ *    mode fastest, element (m, r) at index m + (Nm_max+1)*r, each complex
+ *    value two doubles (re, im) -- i.e. `complex(c_double_complex)` arrays.
+ *  - Host pointers unless a name ends in _dev; _dev entry points take device
+ *    pointers and a cudaStream_t passed as void*.
+ *  - All arithmetic is IEEE FP64.  Ownership: the caller owns every array it
+ *    passes; a handle owns all device memory it allocates.
+ */
+#ifndef FALCON_GPU_H
+#define FALCON_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- error codes ---- */
+#define FALCON_OK 0
+#define FALCON_EINVAL (-1)     /* bad argument / size / unsupported option */
+#define FALCON_ECUDA (-2)      /* CUDA runtime error */
+#define FALCON_ENOMEM (-3)     /* device or host allocation failed */
+#define FALCON_ESINGULAR (-4)  /* dgetrf reported INFO != 0 on an operator */
+#define FALCON_ENONFINITE (-5) /* non-finite value found in the state */
+#define FALCON_EBLOWUP (-6)    /* kinetic energy above 1e10 (src/output.F90:321) */
+#define FALCON_EIO (-7)        /* namelist file missing or unreadable */
+#define FALCON_EBUSY (-8)      /* server queue full / admission refused */
+
+/* ---- scheme identifiers (namelist strings, src/timeschemes.F90:42-962) ---- */
+enum falcon_scheme_type { FALCON_IMEX = 0, FALCON_IMEXRK = 1, FALCON_RK = 2 };
+enum falcon_scheme_imp {
+  FALCON_IMP_CN = 0, FALCON_IMP_BDF2 = 1, FALCON_IMP_BDF3 = 2, FALCON_IMP_BDF4 = 3,
+  FALCON_IMP_ARS443 = 10, FALCON_IMP_ARS343 = 11, FALCON_IMP_BPR353 = 12,
+  FALCON_IMP_ARS222 = 13, FALCON_IMP_NONE = 20
+};
+enum falcon_scheme_exp {
+  FALCON_EXP_AB2 = 0, FALCON_EXP_AB3 = 1, FALCON_EXP_AB4 = 2,
+  FALCON_EXP_ARS443 = 10, FALCON_EXP_ARS343 = 11, FALCON_EXP_BPR353 = 12,
+  FALCON_EXP_ARS222 = 13, FALCON_EXP_RK2 = 20, FALCON_EXP_RK4 = 21
+};
+
+/* Namelist scalars of src/namelists.F90:52-58 (&grid, &physics,
+ * &timecontrol, &output).  Np_max = 3*Nm_max, rmin = eta/(1-eta) and
+ * rmax = 1/(1-eta) are derived (src/namelists.F90:105-107). */
+typedef struct falcon_params {
+  int nr_max, nm_max;                 /* &grid */
+  double eta, ra, pr;                 /* &physics */
+  int mbc;                            /* 0 = "NS", 1 = "SF" */
+  double ampT;
+  int l_add_pert, lagpts, n_init;
+  int buo_imp;                        /* buo_tscheme: 1 = "IMP", 0 = "EXP" */
+  int n_time_steps;                   /* &timecontrol */
+  double dt, totaltime;
+  int l_vartimestep, l_optimizedt;
+  int scheme_type, scheme_imp, scheme_exp;
+  int l_imexrk_started;
+  double dt_coef, dt_max, cfl;
+  int l_restart, n_restart, n_restart_point, n_snapshot_point;
+  char tag[100];                      /* &output */
+  int n_checkpoint, n_snapshot, n_KE, n_KEspec;
+} falcon_params;
+
+/* writeKE_spectral quantities (src/output.F90:122-324) of one instance. */
+typedef struct falcon_diag {
+  double time, dt;
+  double ke, ke_r, ke_phi, ke_upbar;  /* KE_<tag> columns 3-6 */
+  double nu_top, nu_bot;              /* Nusselt_<tag> */
+  double vis, buo;                    /* power_<tag> */
+} falcon_diag;
+
+typedef struct falcon_handle falcon_handle;
+typedef struct falcon_batch falcon_batch;
+typedef struct falcon_server falcon_server;
+
+/* ---- parameters ---- */
+/* defaultNamelists, src/namelists.F90:112-146 */
+int falcon_params_default(falcon_params* p);
+/* readNamelists, src/namelists.F90:49-110: reads &grid, &physics,
+ * &timecontrol and &output from a namelist file into *p (defaults first). */
+int falcon_params_read_namelist(const char* path, falcon_params* p);
+/* Maps the namelist strings time_scheme_type/_imp/_exp onto the enums. */
+int falcon_params_set_scheme(falcon_params* p, const char* type, const char* imp, const char* exp);
+
+/* ---- one instance (a batch of one) ---- */
+/* solver_init, src/solver.F90:38-66: grid, operators (mat_build* +
+ * dgetrf, src/mat_assembly.F90), device state. */
+int falcon_create(const falcon_params* p, falcon_handle** out);
+void falcon_destroy(falcon_handle* h);
+/* Initial state.  kind 0: reference perturbation (init_perturbation,
+ * src/init.F90:277-399, n_init and ampT of the params).  kind 1: conductive
+ * profile tcon (src/init.F90:209) plus complex Gaussian noise of amplitude
+ * `amp` on modes 1..Nm_max at interior radii, seeded by `seed`. */
+int falcon_init_state(falcon_handle* h, int kind, double amp, uint64_t seed);
+/* Fortran-layout host arrays (M,R) complex; any of them may be NULL in
+ * get_state.  set_state restarts the step counter (fresh start). */
+int falcon_set_state(falcon_handle* h, const double* tFR, const double* omgFR,
+                     const double* upFR, const double* urFR);
+int falcon_get_state(falcon_handle* h, double* tFR, double* omgFR, double* upFR,
+                     double* urFR, double* psi);
+/* Advances nsteps time steps (the loop bodies of src/steptime.F90:196-251 /
+ * src/steptime_imexrk.F90:96-190). */
+int falcon_step(falcon_handle* h, int nsteps);
+int falcon_diagnostics(falcon_handle* h, falcon_diag* out);
+
+/* ---- batches of independent instances ---- */
+/* Instances are grouped by operator key (Nr, Nm, mBC, scheme, dt, Pr);
+ * each group shares its implicit operators. */
+int falcon_batch_create(const falcon_params* params, int n, falcon_batch** out);
+void falcon_batch_destroy(falcon_batch* b);
+int falcon_batch_size(const falcon_batch* b);
+int falcon_batch_ngroups(const falcon_batch* b);
+int falcon_batch_init_state(falcon_batch* b, int kind, double amp, const uint64_t* seeds);
+int falcon_batch_set_state(falcon_batch* b, int i, const double* tFR, const double* omgFR,
+                           const double* upFR, const double* urFR);
+int falcon_batch_get_state(falcon_batch* b, int i, double* tFR, double* omgFR, double* upFR,
+                           double* urFR, double* psi);
+int falcon_batch_step(falcon_batch* b, int nsteps);
+int falcon_batch_diagnostics(falcon_batch* b, falcon_diag* out /* n entries */);
+/* Optional: run every step of the batch on this stream (cudaStream_t). */
+int falcon_batch_set_stream(falcon_batch* b, void* stream);
+/* Device bytes held by the batch (state, history, operators, scratch). */
+size_t falcon_batch_device_bytes(const falcon_batch* b);
+
+/* ---- kernel-level entry points (device pointers) ---- */
+/* Nr_maxLOOP (src/nonlin.F90:35-91) for `nb` instances that share
+ * (Nr, Nm).  Device layout X[r][m][b] (instance fastest), double2 per
+ * element, for the four inputs and the four products. */
+int falcon_nonlin_dev(int nr, int nm, int nb, const double* t_dev, const double* omg_dev,
+                      const double* up_dev, const double* ur_dev, double* uphi_t_dev,
+                      double* ur_t_dev, double* uphi_omg_dev, double* ur_omg_dev, void* stream);
+/* Host-array form of falcon_nonlin_dev for one instance, Fortran layout;
+ * copies in and out inside the call. */
+int falcon_nonlin(int nr, int nm, const double* tFR, const double* omgFR, const double* upFR,
+                  const double* urFR, double* uphi_temp_FR, double* ur_temp_FR,
+                  double* uphi_omg_FR, double* ur_omg_FR);
+/* matsolve (src/algebra_lapack.F90:26-38): for each of `nsys` systems,
+ * solves A x = b with the LU factors and pivots of dgetrf (column-major
+ * n x n, 1-based pivots), `nrhs` real right-hand sides per system.
+ * lu: nsys*n*n, ipiv: nsys*n, b: nsys*nrhs*n (solved in place). */
+int falcon_getrs_batched_dev(int n, int nsys, int nrhs, const double* lu_dev,
+                             const int* ipiv_dev, double* b_dev, void* stream);
+/* chebtransform / chebinvtran / chebinvtranD1 / chebinvtranD2
+ * (src/chebyshev_fftw.F90:124-352) applied to `ncol` complex columns of
+ * length nr stored contiguously (column-major, nr x ncol). */
+int falcon_cheb_fwd_dev(int nr, int ncol, const double* in_dev, double* out_dev, void* stream);
+int falcon_cheb_inv_dev(int nr, int ncol, const double* in_dev, double* out_dev, void* stream);
+int falcon_cheb_d1_dev(int nr, int ncol, const double* in_dev, double* out_dev, void* stream);
+int falcon_cheb_d2_dev(int nr, int ncol, const double* in_dev, double* out_dev, void* stream);
+
+/* ---- serving ---- */
+/* A request loop that admits simulation requests by device-memory
+ * footprint, keeps their state resident, steps every admitted request
+ * together each iteration, and retires each one at its horizon. */
+int falcon_server_create(size_t hbm_budget_bytes, int max_active, falcon_server** out);
+void falcon_server_destroy(falcon_server* s);
+/* Queues a request; *id receives its identifier. */
+int falcon_server_submit(falcon_server* s, const falcon_params* p, uint64_t seed, int horizon,
+                         int64_t* id);
+/* One serving iteration: admit what fits, step the active set once,
+ * retire finished requests.  *n_active / *n_queued report the sizes. */
+int falcon_server_iterate(falcon_server* s, int* n_active, int* n_queued);
+/* 1 when request `id` has finished; its final diagnostics in *out and, if
+ * tFR is not NULL, its final temperature field (Fortran layout). */
+int falcon_server_poll(falcon_server* s, int64_t id, int* done, falcon_diag* out, double* tFR);
+
+/* ---- misc ---- */
+const char* falcon_last_error(void);
+const char* falcon_version(void);
+/* Measured FP64 FMA throughput of the current device in GFLOP/s (a short
+ * self-timed kernel), used as the roofline denominator. */
+double falcon_fp64_peak_gflops(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FALCON_GPU_H */
