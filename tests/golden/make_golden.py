@@ -31,9 +31,12 @@ def load_cheblib():
 
 def fourier_gg_forfft(nm, np_, ff):
     # src/fourier_GG.F90:14-38: f(m) = (1/Np) sum_j ff(j) exp(-2 pi i m (j-1)/Np)
+    # the phase index m*(j-1) is reduced modulo Np exactly before the angle is
+    # formed, so the sums carry no argument-rounding error
     j = np.arange(np_)
     m = np.arange(nm + 1)[:, None]
-    return (ff[None, :] * np.exp(-2j * np.pi * m * j[None, :] / np_)).sum(axis=1) / np_
+    k = (m * j[None, :]) % np_
+    return (ff[None, :] * np.exp(-2j * np.pi * k / np_)).sum(axis=1) / np_
 
 
 def fourier_gg_invfft(nm, np_, f):
@@ -42,7 +45,7 @@ def fourier_gg_invfft(nm, np_, f):
     out = np.zeros(np_)
     for m in range(nm + 1):
         c = 0.5 if m == 0 else 1.0
-        out += c * np.real(f[m] * np.exp(2j * np.pi * m * j / np_))
+        out += c * np.real(f[m] * np.exp(2j * np.pi * ((m * j) % np_) / np_))
     return 2.0 * out
 
 
