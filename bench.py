@@ -1,0 +1,348 @@
+"""Benchmark of the GB300 FAlCon-DNS time step.
+
+Workload (one GPU): the uniform batch of 256 annulus instances sharing the
+grid Nr=65, Ntheta=512 (Nm_max=170, Np_max=510), scheme SBDF3 (BDF3/AB3),
+dt=1e-6, Pr=1, Ra log-uniform in [1e6, 1e8] (seed 3), noise seeds 1000+k,
+amplitude 1e-3, FP64.  A step is one time step of every instance of the
+batch.  Metric: instance-steps/s.
+
+Printed as one JSON line by rank 0:
+  value        device-resident batched throughput (CUDA events on the
+               batch's stream, state resident in HBM; the working set,
+               ~1.1 GB, is larger than L2)
+  e2e          the same work through the C ABI from host arrays: initial
+               state uploaded from pinned host memory, per-step diagnostics
+               (writeKE_spectral) read back to the host
+  one_at_a_time  the plain path: instances stepped one at a time
+  roofline     dominant kernel class against the measured FP64 FMA peak
+  cpu_baseline the CPU oracle (OpenMP over modes, as the reference) on a
+               bounded sample of the same workload
+`--impl reference` times the CPU implementation alone (the reference arm).
+Under torchrun each rank runs its own 256-instance shard (weak scaling).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "falcon-dns_gb300"))
+
+WORKLOAD = dict(nr=65, nm=170, scheme="SBDF3", dt=1e-6, pr=1.0, n=256, ra_lo=1e6, ra_hi=1e8, ra_seed=3,
+                noise_seed0=1000, amp=1e-3)
+WORKLOAD_NAME = ("uniform batch of 256 instances, Nr=65, Ntheta=512 (Nm_max=170, Np_max=510), SBDF3, "
+                 "dt=1e-6, Pr=1, Ra log-uniform [1e6,1e8], FP64")
+METRIC = "instance-steps/s batched+served vs one-at-a-time on same GB300; p50/p99 latency"
+
+
+def workload_ras(n, rank=0):
+    rng = np.random.default_rng(WORKLOAD["ra_seed"] + 7919 * rank)
+    u = rng.random(n)
+    return [10 ** (6.0 + 2.0 * x) for x in u]
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.path or not os.path.exists(self.path):
+            return None
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_port_rate(budget_s=10.0, threads=0, rank=0):
+    """The CPU oracle on one instance of the workload, all host threads."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    oracle.build()
+    if threads:
+        oracle.set_threads(threads)
+    ra = workload_ras(1, rank)[0]
+    s = oracle.Sim(oracle.make_params(WORKLOAD["nr"], WORKLOAD["nm"], WORKLOAD["scheme"], ra=ra,
+                                      dt=WORKLOAD["dt"], pr=WORKLOAD["pr"]))
+    s.init_noise(WORKLOAD["noise_seed0"], WORKLOAD["amp"])
+    s.step(2)  # past the first step, which skips the nonlinear pass
+    n = 0
+    t0 = time.perf_counter()
+    while time.perf_counter() - t0 < budget_s:
+        s.step(1)
+        n += 1
+    dt = time.perf_counter() - t0
+    return n / dt, n, dt
+
+
+def run_reference(args):
+    rank, world, _ = dist_info()
+    if world > 1 and rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    oracle.build()
+    cores = os.cpu_count()
+    ras = workload_ras(4)
+    sims = []
+    for k, ra in enumerate(ras):
+        s = oracle.Sim(oracle.make_params(WORKLOAD["nr"], WORKLOAD["nm"], WORKLOAD["scheme"], ra=ra,
+                                          dt=WORKLOAD["dt"], pr=WORKLOAD["pr"]))
+        s.init_noise(WORKLOAD["noise_seed0"] + k, WORKLOAD["amp"])
+        sims.append(s)
+    for k in range(args.warmup):
+        sims[k % len(sims)].step(1)
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        sims[k % len(sims)].step(1)
+    dt = time.perf_counter() - t0
+    v = args.steps / dt
+    line = {
+        "metric": METRIC, "value": v, "unit": "instance-steps/s", "impl": "reference", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD_NAME, "nr": WORKLOAD["nr"], "nm": WORKLOAD["nm"],
+                   "scheme": WORKLOAD["scheme"], "sample": "4 instances of the workload, one time step each per step"},
+        "cpu_baseline": {"value": v, "unit": "instance-steps/s", "cores": cores, "kind": "port",
+                         "sample": f"{args.steps} single-instance steps over 4 instances (Nr=65, Nm=170, SBDF3), "
+                                   "OpenMP over modes with all host threads"},
+        "e2e": {"value": v, "unit": "instance-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def load_traffic(kernel):
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        d = json.load(open(path))
+        return d.get(kernel)
+    except (OSError, ValueError):
+        return None
+
+
+def run_gpu(args):
+    import torch
+    import falcon_gpu as fg
+    import build as falcon_build
+
+    rank, world, local = dist_info()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    falcon_build.build()
+    fg.lib()
+    stream = torch.cuda.Stream()
+    W = WORKLOAD
+    n = args.instances or W["n"]
+    ras = workload_ras(n, rank)
+    params = [fg.make_params(W["nr"], W["nm"], W["scheme"], ra=ra, dt=W["dt"], pr=W["pr"]) for ra in ras]
+    seeds = [W["noise_seed0"] + rank * n + k for k in range(n)]
+    peak = fg.fp64_peak_gflops()
+
+    # ---- device-resident batched throughput ----
+    b = fg.Batch(params)
+    b.set_stream(stream.cuda_stream)
+    b.init_noise(seeds, W["amp"])
+    with torch.cuda.stream(stream):
+        b.step(args.warmup)
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    launches0 = fg.launch_count()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        ev0.record(stream)
+        b.step(args.steps)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    launches = fg.launch_count() - launches0
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * n * args.steps / (ms / 1e3)
+    finite = all(np.isfinite(b.get_state(i)["T"]).all() for i in (0, n - 1))
+
+    # ---- kernel classes (CUDA events per launch on the same stream) ----
+    prof = b.profile(3)
+    tot = sum(v["ms"] for v in prof.values())
+    dom = max(prof, key=lambda k: prof[k]["ms"])
+    d = prof[dom]
+    achieved = d["flops"] / (d["ms"] / 1e3) / 1e12
+    traffic = load_traffic(dom)
+    roofline = {"bound": "fp64", "achieved": achieved, "peak": peak / 1e3, "unit": "TFLOP/s",
+                "frac": achieved / (peak / 1e3), "traffic": traffic, "kernel": dom,
+                "share": d["ms"] / tot,
+                "peak_source": "FP64 FMA throughput measured live by the library's DFMA kernel "
+                               "(no FP64 figure in MEASURED_PEAKS.json)",
+                "classes": {k: {"ms_per_step": v["ms"] / 3, "tflops": v["flops"] / (v["ms"] / 1e3) / 1e12,
+                                "share": v["ms"] / tot, "launches_per_step": v["launches"] / 3}
+                            for k, v in prof.items()}}
+    b.close()
+
+    # ---- end to end through the C ABI from host arrays ----
+    e2e = None
+    if rank == 0 or True:
+        b2 = fg.Batch(params)
+        b2.set_stream(stream.cuda_stream)
+        # host initial conditions (Fortran layout), pinned
+        b2.init_noise(seeds, W["amp"])
+        init_T = [b2.get_state(i)["T"] for i in range(n)]
+        init_T = [torch.from_numpy(t).pin_memory().numpy() for t in init_T]
+        zero = np.zeros_like(init_T[0])
+        torch.cuda.synchronize()
+        k_e2e = max(10, args.steps // 2)
+        n_ke = 10
+        h2d = d2h = 0
+        t0 = time.perf_counter()
+        for i in range(n):
+            b2.set_state(i, init_T[i], zero, zero, zero)
+            h2d += 4 * init_T[i].nbytes
+        for k in range(k_e2e):
+            b2.step(1)
+            if (k + 1) % n_ke == 0:
+                diag = b2.diagnostics()  # writeKE_spectral cadence n_KE = 10
+                d2h += n * 4 * init_T[0].nbytes
+        torch.cuda.synchronize()
+        e2e_s = time.perf_counter() - t0
+        e2e = {"value": world * n * k_e2e / e2e_s, "unit": "instance-steps/s",
+               "h2d_bytes_per_step": h2d // k_e2e, "d2h_bytes_per_step": d2h // k_e2e,
+               "steps": k_e2e, "diagnostics_every": n_ke,
+               "note": "initial fields uploaded from host arrays inside the timed region; diagnostics "
+                       "(KE, Nusselt, power) read back every n_KE steps"}
+        b2.close()
+
+    # ---- plain one-instance-at-a-time GPU path ----
+    n1 = min(args.one_at_a_time, n)
+    insts = []
+    for k in range(n1):
+        it = fg.Instance(params[k])
+        it.set_stream(stream.cuda_stream)
+        it.init_noise(seeds[k], W["amp"])
+        insts.append(it)
+    for it in insts:
+        it.step(2)
+    torch.cuda.synchronize()
+    k1 = max(5, args.steps // 4)
+    ev0.record(stream)
+    for k in range(k1):
+        for it in insts:
+            it.step(1)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    one_rate = n1 * k1 / (ev0.elapsed_time(ev1) / 1e3)
+    for it in insts:
+        it.close()
+
+    if rank != 0:
+        if world > 1:
+            torch.distributed.barrier()
+        return
+    cpu = None
+    if not args.no_cpu:
+        rate, nst, secs = cpu_port_rate(args.cpu_seconds)
+        cpu = {"value": rate, "unit": "instance-steps/s", "cores": os.cpu_count(), "kind": "port",
+               "sample": f"{nst} time steps of one workload instance (Nr=65, Nm=170, SBDF3) in {secs:.1f} s, "
+                         "CPU oracle with OpenMP over modes on all host threads"}
+    line = {
+        "metric": METRIC, "value": value, "unit": "instance-steps/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD_NAME, "instances_per_gpu": n, "nr": W["nr"], "nm": W["nm"],
+                   "np": 3 * W["nm"], "scheme": W["scheme"], "dt": W["dt"],
+                   "l2": "working set ~1.1 GB per GPU, larger than L2 (129 MB); no flush needed",
+                   "parallelism": f"replicas x{world}"},
+        "one_at_a_time": {"value": one_rate, "unit": "instance-steps/s", "instances": n1, "steps": k1,
+                          "batched_over_one_at_a_time": value / world / one_rate},
+        "e2e": e2e,
+        "roofline": roofline,
+        "cpu_baseline": cpu,
+        "clocks": clk.summary(),
+        "gpu_launches": launches,
+        "device_bytes_per_batch": None,
+        "state_finite": bool(finite),
+    }
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.barrier()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--instances", type=int, default=0, help="instances per GPU (default 256)")
+    ap.add_argument("--one-at-a-time", dest="one_at_a_time", type=int, default=16)
+    ap.add_argument("--cpu-seconds", dest="cpu_seconds", type=float, default=10.0)
+    ap.add_argument("--no-cpu", dest="no_cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -11,6 +11,7 @@
 #include <cstring>
 #include <deque>
 #include <fstream>
+#include <functional>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -40,6 +41,16 @@ int fail(int code, const std::string& msg) {
     if (e_ != cudaSuccess)                                                        \
       return fail(FALCON_ECUDA, std::string(#call ": ") + cudaGetErrorString(e_)); \
   } while (0)
+
+std::atomic<long long> g_launches(0);
+
+// Optional per-launch CUDA-event timing (falcon_batch_profile).
+enum KernelClass { KC_NONLIN = 0, KC_GEMM_RADIAL, KC_GEMM_MODE, KC_ELEMENTWISE, KC_COUNT };
+const char* kClassNames[KC_COUNT] = {"nonlin_fft", "gemm_radial", "gemm_mode_solve", "elementwise"};
+struct Prof {
+  struct Rec { int cls; cudaEvent_t a, b; double flops; };
+  std::vector<Rec> recs;
+};
 
 // ---------------------------------------------------------------------------
 // Dense algebra on the host (operator construction only).  dgetrf/dgetrs
@@ -615,7 +626,9 @@ struct Group {
           *buo[kMaxStages] = {};
   double2 *t0 = nullptr, *w0 = nullptr;
   double* u0 = nullptr;
+  double2* t_grid = nullptr;   // temperature seen by the last nonlinear pass (IMEXRK)
   double2* stage_buf = nullptr;  // host staging (pinned) for one instance
+  Prof* prof = nullptr;
   int head = 0, head_e = 0;
   int n_step = 0;
   double tot_time = 0.0;
@@ -703,7 +716,8 @@ int group_init(Group* g, const std::vector<falcon_params>& ps, const std::vector
           (rc = g->alloc(&g->fdw[i], n)) || (rc = g->alloc(&g->buo[i], n)))
         return rc;
     }
-    if ((rc = g->alloc(&g->t0, n)) || (rc = g->alloc(&g->w0, n)) || (rc = g->alloc(&g->u0, (size_t)R * B)))
+    if ((rc = g->alloc(&g->t0, n)) || (rc = g->alloc(&g->w0, n)) || (rc = g->alloc(&g->u0, (size_t)R * B)) ||
+        (rc = g->alloc(&g->t_grid, n)))
       return rc;
   }
   if ((rc = g->alloc(&g->up, n)) || (rc = g->alloc(&g->ur, n)) || (rc = g->alloc(&g->psi, n)) ||
@@ -742,6 +756,36 @@ GemmArgs per_mode(const double* A, long lda, long sA, const double2* X, double2*
   return g;
 }
 
+// Every kernel launch of a step goes through here: counted, and timed with
+// events on the group's stream when profiling.
+template <class F>
+int launch(Group* g, int cls, double flops, F f) {
+  cudaEvent_t a = nullptr, b = nullptr;
+  if (g->prof) {
+    CK(cudaEventCreate(&a));
+    CK(cudaEventCreate(&b));
+    CK(cudaEventRecord(a, g->stream));
+  }
+  cudaError_t e = f();
+  if (e != cudaSuccess) return fail(FALCON_ECUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
+  g_launches++;
+  if (g->prof) {
+    CK(cudaEventRecord(b, g->stream));
+    g->prof->recs.push_back({cls, a, b, flops});
+  }
+  return 0;
+}
+
+double gemm_flops(const GemmArgs& q) { return 2.0 * q.rows * (double)q.K * q.N * q.batch; }
+
+int gemm(Group* g, int cls, const GemmArgs& q) {
+  return launch(g, cls, gemm_flops(q), [&]() { return launch_gemm(q, g->stream); });
+}
+
+int elementwise(Group* g, double flops_per_el, std::function<cudaError_t()> f) {
+  return launch(g, KC_ELEMENTWISE, flops_per_el * (double)g->nel(), f);
+}
+
 int run_nonlin(Group* g) {
   NonlinArgs a{};
   a.R = g->R; a.M = g->M; a.B = g->B; a.Nm = g->Nm;
@@ -749,8 +793,9 @@ int run_nonlin(Group* g) {
   a.t = g->T(); a.w = g->W(); a.up = g->up; a.ur = g->ur;
   a.ntp = g->ntp; a.ntr = g->ntr; a.nwp = g->nwp; a.nwr = g->nwr;
   a.umax = nullptr;
-  CK(launch_nonlin(a, g->stream));
-  return 0;
+  const double P = g->P;
+  const double flops = (double)g->R * g->B * (4.0 * 5.0 * P * std::log2(P) + 6.0 * P);
+  return launch(g, KC_NONLIN, flops, [&]() { return launch_nonlin(a, g->stream); });
 }
 
 // The implicit solves shared by IMEX and IMEXRK: temperature, then
@@ -760,22 +805,28 @@ int solve_all(Group* g, double2* t_out, double2* w_out, double buo_scale, double
   const int R = g->R, M = g->M, B = g->B;
   OpSet* o = g->ops.get();
   cudaStream_t s = g->stream;
-  CK(launch_gemm(per_mode(o->ST, R, (long)R * R, g->rhs_t, t_out, R, M, B, 0, M, R), s));
-  CK(launch_add_buoyancy(R, M, B, o->inv_r, g->ra_pr, buo_scale, t_out, g->rhs_w, buo_store, s));
+  int rc;
+  if ((rc = gemm(g, KC_GEMM_MODE, per_mode(o->ST, R, (long)R * R, g->rhs_t, t_out, R, M, B, 0, M, R)))) return rc;
+  if ((rc = elementwise(g, 6.0, [&]() {
+         return launch_add_buoyancy(R, M, B, o->inv_r, g->ra_pr, buo_scale, t_out, g->rhs_w, buo_store, s);
+       })))
+    return rc;
   if (M > 1) {
     const long sG = 3L * R * R;
-    CK(launch_gemm(per_mode(o->G, 3 * R, sG, g->rhs_w, w_out, R, M, B, 1, M - 1, R), s));
-    CK(launch_gemm(per_mode(o->G + R, 3 * R, sG, g->rhs_w, g->psi, R, M, B, 1, M - 1, R), s));
-    CK(launch_gemm(per_mode(o->G + 2 * R, 3 * R, sG, g->rhs_w, g->up, R, M, B, 1, M - 1, R), s));
+    if ((rc = gemm(g, KC_GEMM_MODE, per_mode(o->G, 3 * R, sG, g->rhs_w, w_out, R, M, B, 1, M - 1, R))) ||
+        (rc = gemm(g, KC_GEMM_MODE, per_mode(o->G + R, 3 * R, sG, g->rhs_w, g->psi, R, M, B, 1, M - 1, R))) ||
+        (rc = gemm(g, KC_GEMM_MODE, per_mode(o->G + 2 * R, 3 * R, sG, g->rhs_w, g->up, R, M, B, 1, M - 1, R))))
+      return rc;
   }
   GemmArgs gu{};
   gu.A = o->U; gu.lda = 2 * R;
   gu.X = reinterpret_cast<const double*>(g->rhs_w); gu.ldx = 2L * M * B;
   gu.Y = g->ub; gu.ldy = 2L * B;
   gu.K = R; gu.rows = 2 * R; gu.N = 2 * B; gu.batch = 1; gu.alpha = 1.0;
-  CK(launch_gemm(gu, s));
-  CK(launch_post_w(R, M, B, o->inv_r, g->psi, g->ur, g->up, w_out, g->ub, ubar_store, s));
-  return 0;
+  if ((rc = gemm(g, KC_GEMM_MODE, gu))) return rc;
+  return elementwise(g, 3.0, [&]() {
+    return launch_post_w(R, M, B, o->inv_r, g->psi, g->ur, g->up, w_out, g->ub, ubar_store, s);
+  });
 }
 
 int step_imex(Group* g) {
@@ -794,15 +845,17 @@ int step_imex(Group* g) {
     CK(cudaMemsetAsync(g->nwp, 0, sizeof(double2) * n, s));
     CK(cudaMemsetAsync(g->nwr, 0, sizeof(double2) * n, s));
   }
-  CK(launch_gemm(radial(o->D1p, g->ntr, g->dntr, R, M, B), s));
-  CK(launch_gemm(radial(o->D1p, g->nwr, g->dnwr, R, M, B), s));
+  if ((rc = gemm(g, KC_GEMM_RADIAL, radial(o->D1p, g->ntr, g->dntr, R, M, B))) ||
+      (rc = gemm(g, KC_GEMM_RADIAL, radial(o->D1p, g->nwr, g->dnwr, R, M, B))))
+    return rc;
   const bool cn = (sc.imp == FALCON_IMP_CN);
   if (cn) {
-    CK(launch_gemm(radial(o->Lp, g->T(), g->lt, R, M, B), s));
-    CK(launch_gemm(radial(o->Lp, g->W(), g->lw, R, M, B), s));
     GemmArgs gl = radial(o->Lp, g->up, g->lu0, R, M, B);
     gl.N = 2 * B; gl.ldy = 2L * B;
-    CK(launch_gemm(gl, s));
+    if ((rc = gemm(g, KC_GEMM_RADIAL, radial(o->Lp, g->T(), g->lt, R, M, B))) ||
+        (rc = gemm(g, KC_GEMM_RADIAL, radial(o->Lp, g->W(), g->lw, R, M, B))) ||
+        (rc = gemm(g, KC_GEMM_RADIAL, gl)))
+      return rc;
   }
   const int ni = sc.n_imp, ne = sc.n_exp;
   const int he_new = (g->head_e + ne - 1) % ne;
@@ -828,7 +881,7 @@ int step_imex(Group* g) {
   a.ntp = g->ntp; a.ntr = g->ntr; a.dntr = g->dntr; a.nwp = g->nwp; a.nwr = g->nwr; a.dnwr = g->dnwr;
   a.lt = g->lt; a.lw = g->lw; a.lu0 = g->lu0;
   a.rhs_t = g->rhs_t; a.rhs_w = g->rhs_w;
-  CK(launch_imex_rhs(a, s));
+  if ((rc = elementwise(g, 10.0 + 8.0 * (ni + ne), [&]() { return launch_imex_rhs(a, s); }))) return rc;
   const double buo_scale = g->p.dt * (cn ? 0.5 : sc.wt_lhs);
   if ((rc = solve_all(g, g->th[h_new], g->wh[h_new], buo_scale, nullptr, g->ubh[h_new]))) return rc;
   g->head = h_new;
@@ -864,7 +917,7 @@ int step_imexrk(Group* g) {
     for (int i = 0; i < kMaxStages; ++i) { a.aD[i] = sc.aD[st][i]; a.aA[i] = sc.aA[st][i]; }
     a.aD_ss = sc.aD[st][st];
     if (st > 0) {
-      CK(launch_stage_rhs(a, s));
+      if ((rc = elementwise(g, 12.0 * st + 8.0, [&]() { return launch_stage_rhs(a, s); }))) return rc;
       const double scale = g->p.buo_imp ? g->p.dt * sc.aD[st][st] : 0.0;
       if ((rc = solve_all(g, g->T(), g->W(), scale, g->buo[st], nullptr))) return rc;
     }
@@ -872,6 +925,7 @@ int step_imexrk(Group* g) {
     for (int i = 0; i < ns; ++i) colsum += sc.aA[i][st];
     if ((nstep > 1 || st > 0) && (colsum + sc.bA[st] != 0.0)) {
       if ((rc = run_nonlin(g))) return rc;
+      CK(cudaMemcpyAsync(g->t_grid, g->T(), sizeof(double2) * n, cudaMemcpyDeviceToDevice, s));
     } else if (nstep == 1 && st == 0) {
       CK(cudaMemsetAsync(g->ntp, 0, sizeof(double2) * n, s));
       CK(cudaMemsetAsync(g->ntr, 0, sizeof(double2) * n, s));
@@ -879,21 +933,22 @@ int step_imexrk(Group* g) {
       CK(cudaMemsetAsync(g->nwr, 0, sizeof(double2) * n, s));
     }
     if (sa && st == ns - 1) break;  // last-stage derivatives are unused by the SA assembly
-    CK(launch_gemm(radial(o->D1p, g->ntr, g->dntr, R, M, B), s));
-    CK(launch_gemm(radial(o->D1p, g->nwr, g->dnwr, R, M, B), s));
-    CK(launch_gemm(radial(o->Lp, g->T(), g->lt, R, M, B), s));
-    CK(launch_gemm(radial(o->Lp, g->W(), g->lw, R, M, B), s));
     GemmArgs gl = radial(o->Lp, g->up, g->lu0, R, M, B);
     gl.N = 2 * B; gl.ldy = 2L * B;
-    CK(launch_gemm(gl, s));
+    if ((rc = gemm(g, KC_GEMM_RADIAL, radial(o->D1p, g->ntr, g->dntr, R, M, B))) ||
+        (rc = gemm(g, KC_GEMM_RADIAL, radial(o->D1p, g->nwr, g->dnwr, R, M, B))) ||
+        (rc = gemm(g, KC_GEMM_RADIAL, radial(o->Lp, g->T(), g->lt, R, M, B))) ||
+        (rc = gemm(g, KC_GEMM_RADIAL, radial(o->Lp, g->W(), g->lw, R, M, B))) ||
+        (rc = gemm(g, KC_GEMM_RADIAL, gl)))
+      return rc;
     a.fat_out = g->fat[st]; a.fdt_out = g->fdt[st]; a.faw_out = g->faw[st]; a.fdw_out = g->fdw[st];
     a.buo_out = (st == 0) ? g->buo[0] : nullptr;
-    CK(launch_stage_deriv(a, s));
+    if ((rc = elementwise(g, 20.0, [&]() { return launch_stage_deriv(a, s); }))) return rc;
   }
   // Assembly_stage_SA (src/fourierloop_imexrk.F90:653-665)
   CK(cudaMemcpyAsync(g->t0, g->T(), sizeof(double2) * n, cudaMemcpyDeviceToDevice, s));
   CK(cudaMemcpyAsync(g->w0, g->W(), sizeof(double2) * n, cudaMemcpyDeviceToDevice, s));
-  CK(launch_extract_mode0(R, M, B, g->up, g->u0, s));
+  if ((rc = launch(g, KC_ELEMENTWISE, 0.0, [&]() { return launch_extract_mode0(R, M, B, g->up, g->u0, s); }))) return rc;
   g->n_step = nstep;
   g->tot_time += g->p.dt;
   return 0;
@@ -928,6 +983,7 @@ int group_reset(Group* g) {
   } else {
     CK(cudaMemcpyAsync(g->t0, g->T(), sizeof(double2) * n, cudaMemcpyDeviceToDevice, s));
     CK(cudaMemcpyAsync(g->w0, g->W(), sizeof(double2) * n, cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(g->t_grid, g->T(), sizeof(double2) * n, cudaMemcpyDeviceToDevice, s));
     CK(launch_extract_mode0(R, M, B, g->up, g->u0, s));
     for (int i = 0; i < g->sch.n_exp; ++i) {
       CK(cudaMemsetAsync(g->fat[i], 0, sizeof(double2) * n, s));
@@ -1013,58 +1069,39 @@ int group_resize(Group* g, const std::vector<int>& map) {
   return 0;
 }
 
-// Per-instance fresh start (the column of `b`): histories zeroed, current
-// slot and Y0 from the state (the group-wide counterpart is group_reset).
+// Per-instance fresh start (the column of `b`): its histories and stage
+// stores zeroed, its current-slot uphi_bar and Y0 taken from its state.
 int group_reset_instance(Group* g, int b) {
   const int R = g->R, M = g->M, B = g->B;
-  std::vector<int> keep(B);
-  for (int j = 0; j < B; ++j) keep[j] = (j == b) ? -1 : j;
-  int* dmap = nullptr;
-  CK(cudaMalloc(&dmap, sizeof(int) * B));
-  CK(cudaMemcpy(dmap, keep.data(), sizeof(int) * B, cudaMemcpyHostToDevice));
-  auto zero_col = [&](void* q, size_t rows, int ew) -> int {
-    // in-place remap keeps other columns and zeroes column b
-    CK(launch_remap_cols(reinterpret_cast<double*>(q), reinterpret_cast<double*>(q), rows, B, B, ew, dmap, g->stream));
-    return 0;
-  };
   const size_t n = (size_t)R * M;
-  int rc = 0;
+  cudaStream_t s = g->stream;
+  auto zero = [&](void* q, size_t rows, int ew) {
+    return launch_col_op(nullptr, reinterpret_cast<double*>(q), rows, B, b, ew, s);
+  };
+  auto copy = [&](const void* src, void* dst, size_t rows, int ew) {
+    return launch_col_op(reinterpret_cast<const double*>(src), reinterpret_cast<double*>(dst), rows, B, b, ew, s);
+  };
   if (g->p.scheme_type == FALCON_IMEX) {
     for (int i = 0; i < g->sch.n_imp; ++i)
       if (i != g->head) {
-        if ((rc = zero_col(g->th[i], n, 2)) || (rc = zero_col(g->wh[i], n, 2)) || (rc = zero_col(g->ubh[i], R, 1)))
-          break;
+        CK(zero(g->th[i], n, 2)); CK(zero(g->wh[i], n, 2)); CK(zero(g->ubh[i], R, 1));
       }
-    for (int i = 0; !rc && i < g->sch.n_exp; ++i)
-      if ((rc = zero_col(g->nth[i], n, 2)) || (rc = zero_col(g->nwh[i], n, 2)) || (rc = zero_col(g->uromh[i], R, 1)))
-        break;
+    for (int i = 0; i < g->sch.n_exp; ++i) {
+      CK(zero(g->nth[i], n, 2)); CK(zero(g->nwh[i], n, 2)); CK(zero(g->uromh[i], R, 1));
+    }
+    CK(launch_extract_mode0(R, M, B, g->up, g->ubh[g->head], s));
   } else {
-    for (int i = 0; !rc && i < g->sch.n_exp; ++i)
-      if ((rc = zero_col(g->fat[i], n, 2)) || (rc = zero_col(g->fdt[i], n, 2)) || (rc = zero_col(g->faw[i], n, 2)) ||
-          (rc = zero_col(g->fdw[i], n, 2)) || (rc = zero_col(g->buo[i], n, 2)))
-        break;
+    for (int i = 0; i < g->sch.n_exp; ++i) {
+      CK(zero(g->fat[i], n, 2)); CK(zero(g->fdt[i], n, 2)); CK(zero(g->faw[i], n, 2));
+      CK(zero(g->fdw[i], n, 2)); CK(zero(g->buo[i], n, 2));
+    }
+    CK(copy(g->T(), g->t0, n, 2));
+    CK(copy(g->W(), g->w0, n, 2));
+    CK(copy(g->T(), g->t_grid, n, 2));
+    CK(launch_extract_mode0(R, M, B, g->up, g->u0, s));
   }
-  CK(cudaStreamSynchronize(g->stream));
-  cudaFree(dmap);
-  if (rc) return rc;
-  // current-slot uphi_bar and Y0 for every column (unchanged columns rewrite
-  // their own values)
-  if (g->p.scheme_type == FALCON_IMEX) {
-    CK(launch_extract_mode0(R, M, B, g->up, g->ubh[g->head], g->stream));
-  } else {
-    CK(launch_extract_mode0(R, M, B, g->up, g->u0, g->stream));
-    const size_t bytes2 = sizeof(double2);
-    // Y0 of column b from the state: gather/scatter through the staging path
-    double2* tmp = nullptr;
-    CK(cudaMalloc(&tmp, bytes2 * n));
-    CK(launch_gather_instance(R, M, B, b, g->T(), tmp, g->stream));
-    CK(launch_scatter_instance(R, M, B, b, tmp, g->t0, g->stream));
-    CK(launch_gather_instance(R, M, B, b, g->W(), tmp, g->stream));
-    CK(launch_scatter_instance(R, M, B, b, tmp, g->w0, g->stream));
-    CK(cudaStreamSynchronize(g->stream));
-    cudaFree(tmp);
-  }
-  CK(cudaStreamSynchronize(g->stream));
+  CK(zero(g->psi, n, 2));
+  CK(cudaStreamSynchronize(s));
   return 0;
 }
 
@@ -1219,9 +1256,12 @@ double radint(const Cheb& c, const std::vector<double>& f) {
   return fac * tot;
 }
 
+// tprev: the temperature the last nonlinear pass saw (the module grid `tt`
+// that src/output.F90:211 multiplies with the current u_r); the azimuthal
+// mean of the product of two dealiased lines is Re X0 Re Y0 + 2 sum Re(X_m
+// conj Y_m).  NULL uses the current temperature.
 void diagnostics_host(const falcon_params& p, double time, const double* t, const double* w,
-                      const double* up, const double* ur, const std::vector<double>* tgrid_mean_urt,
-                      falcon_diag* out) {
+                      const double* up, const double* ur, const double* tprev, falcon_diag* out) {
   const int R = p.nr_max, M = p.nm_max + 1;
   Cheb c = make_cheb(R, p.eta);
   const double pi = 4.0 * std::atan(1.0);
@@ -1240,7 +1280,14 @@ void diagnostics_host(const falcon_params& p, double time, const double* t, cons
     ur2[j] = a; up2[j] = b; w2[j] = ww;
     const double upavg = up[2 * ((size_t)M * j)];
     upb2[j] = upavg * upavg;
-    if (tgrid_mean_urt) urt[j] = (*tgrid_mean_urt)[j];
+    const double* tp = tprev ? tprev : t;
+    double acc = ur[2 * ((size_t)M * j)] * tp[2 * ((size_t)M * j)];
+    for (int m = 1; m < M; ++m) {
+      const double* u = &ur[2 * ((size_t)m + (size_t)M * j)];
+      const double* q = &tp[2 * ((size_t)m + (size_t)M * j)];
+      acc += 2.0 * (u[0] * q[0] + u[1] * q[1]);
+    }
+    urt[j] = acc;
   }
   const double urk = radint(c, ur2), upk = radint(c, up2), upbk = radint(c, upb2);
   out->time = time;
@@ -1540,7 +1587,8 @@ int falcon_batch_set_state(falcon_batch* b, int i, const double* tFR, const doub
   Group* g = b->groups[b->where[i].first].get();
   int rc = group_set_instance(g, b->where[i].second, tFR, omgFR, upFR, urFR);
   if (rc) return rc;
-  return group_reset(g);
+  if (g->n_step == 0) g->tot_time = 0.0;
+  return group_reset_instance(g, b->where[i].second);
 }
 
 int falcon_batch_init_state(falcon_batch* b, int kind, double amp, const uint64_t* seeds) {
@@ -1591,7 +1639,20 @@ int falcon_batch_diagnostics(falcon_batch* b, falcon_diag* out) {
     for (double v : t)
       if (!std::isfinite(v)) return fail(FALCON_ENONFINITE, "non-finite temperature in instance " + std::to_string(i));
     Group* g = b->groups[b->where[i].first].get();
-    diagnostics_host(p, g->tot_time, t.data(), w.data(), up.data(), ur.data(), nullptr, &out[i]);
+    std::vector<double> tp(n);
+    {
+      const double2* src = nullptr;
+      if (g->p.scheme_type == FALCON_IMEX) src = (g->n_step > 0) ? g->th[(g->head + 1) % g->sch.n_imp] : g->T();
+      else src = g->t_grid;
+      const int R = g->R, M = g->M;
+      double2* d = nullptr;
+      CK(cudaMalloc(&d, sizeof(double2) * (size_t)R * M));
+      CK(launch_gather_instance(R, M, g->B, b->where[i].second, src, d, g->stream));
+      CK(cudaStreamSynchronize(g->stream));
+      CK(cudaMemcpy(tp.data(), d, sizeof(double2) * (size_t)R * M, cudaMemcpyDeviceToHost));
+      cudaFree(d);
+    }
+    diagnostics_host(p, g->tot_time, t.data(), w.data(), up.data(), ur.data(), tp.data(), &out[i]);
   }
   return 0;
 }
@@ -1982,6 +2043,49 @@ int falcon_server_poll(falcon_server* s, int64_t id, int* done, falcon_diag* out
     if (out) *out = it->second.diag;
     if (tFR) std::memcpy(tFR, it->second.tfr.data(), sizeof(double) * it->second.tfr.size());
   }
+  return 0;
+}
+
+}  // extern "C"
+
+extern "C" {
+
+long long falcon_launch_count(void) { return g_launches.load(); }
+
+int falcon_batch_profile(falcon_batch* b, int nsteps, falcon_kernel_stat* stats, int max_stats, int* nstats) {
+  if (!b || nsteps <= 0 || !stats || !nstats) return fail(FALCON_EINVAL, "invalid profile arguments");
+  Prof prof;
+  for (auto& g : b->groups) g->prof = &prof;
+  int rc = 0;
+  for (int k = 0; k < nsteps && !rc; ++k)
+    for (auto& g : b->groups) {
+      rc = group_step(g.get());
+      if (rc) break;
+    }
+  for (auto& g : b->groups) g->prof = nullptr;
+  cudaStreamSynchronize(b->stream);
+  double ms[KC_COUNT] = {0}, fl[KC_COUNT] = {0};
+  int nl[KC_COUNT] = {0};
+  for (auto& r : prof.recs) {
+    float t = 0.f;
+    cudaEventElapsedTime(&t, r.a, r.b);
+    ms[r.cls] += t;
+    fl[r.cls] += r.flops;
+    nl[r.cls] += 1;
+    cudaEventDestroy(r.a);
+    cudaEventDestroy(r.b);
+  }
+  if (rc) return rc;
+  int n = 0;
+  for (int c = 0; c < KC_COUNT && n < max_stats; ++c) {
+    if (!nl[c]) continue;
+    std::snprintf(stats[n].name, sizeof(stats[n].name), "%s", kClassNames[c]);
+    stats[n].launches = nl[c];
+    stats[n].ms = ms[c];
+    stats[n].flops = fl[c];
+    ++n;
+  }
+  *nstats = n;
   return 0;
 }
 

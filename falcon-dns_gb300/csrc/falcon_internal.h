@@ -122,6 +122,8 @@ cudaError_t launch_apply_cols(int n, int ncol, const double* A, const double2* i
 // Instance-column remap of a [rows][B] array (ew doubles per element).
 cudaError_t launch_remap_cols(const double* src, double* dst, size_t rows, int bs, int bd, int ew, const int* map,
                               cudaStream_t s);
+// Column b of a [rows][B] array: dst = src (or zero when src is null).
+cudaError_t launch_col_op(const double* src, double* dst, size_t rows, int B, int b, int ew, cudaStream_t s);
 // Self-timed FP64 FMA throughput kernel (returns GFLOP/s, or < 0 on error).
 double measure_fp64_peak();
 // Set the odd-prime DFT coefficient tables (constant memory); idempotent.

@@ -919,3 +919,27 @@ cudaError_t launch_remap_cols(const double* src, double* dst, size_t rows, int b
 }
 
 }  // namespace falcon
+
+namespace falcon {
+
+// Column b of a [rows][B] array (ew doubles per element): dst = src, or 0
+// when src is null.  Touches only that column.
+__global__ void col_op_kernel(const double* src, double* dst, size_t rows, int B, int b, int ew) {
+  const size_t total = rows * ew;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+    const size_t row = i / ew;
+    const int q = (int)(i % ew);
+    const size_t e = (row * B + b) * ew + q;
+    dst[e] = src ? src[e] : 0.0;
+  }
+}
+
+cudaError_t launch_col_op(const double* src, double* dst, size_t rows, int B, int b, int ew, cudaStream_t s) {
+  size_t g = (rows * ew + 255) / 256;
+  if (g > 152 * 16) g = 152 * 16;
+  if (g == 0) g = 1;
+  col_op_kernel<<<(int)g, 256, 0, s>>>(src, dst, rows, B, b, ew);
+  return cudaGetLastError();
+}
+
+}  // namespace falcon

@@ -64,6 +64,11 @@ class FalconDiag(ctypes.Structure):
         return {n: getattr(self, n) for n, _ in self._fields_}
 
 
+class KernelStat(ctypes.Structure):
+    _fields_ = [("name", ctypes.c_char * 32), ("launches", ctypes.c_int), ("ms", ctypes.c_double),
+                ("flops", ctypes.c_double)]
+
+
 class FalconError(RuntimeError):
     pass
 
@@ -79,6 +84,7 @@ EXPORTS = (
     "falcon_cheb_fwd_dev", "falcon_cheb_inv_dev", "falcon_cheb_d1_dev", "falcon_cheb_d2_dev",
     "falcon_server_create", "falcon_server_destroy", "falcon_server_submit", "falcon_server_iterate",
     "falcon_server_poll", "falcon_last_error", "falcon_version", "falcon_fp64_peak_gflops",
+    "falcon_batch_profile", "falcon_launch_count",
 )
 
 
@@ -131,6 +137,8 @@ def lib():
     L.falcon_server_iterate.argtypes = [vp, P(ctypes.c_int), P(ctypes.c_int)]
     L.falcon_server_poll.argtypes = [vp, ctypes.c_int64, P(ctypes.c_int), P(FalconDiag), dp]
     L.falcon_fp64_peak_gflops.restype = ctypes.c_double
+    L.falcon_batch_profile.argtypes = [vp, ip, P(KernelStat), ip, P(ctypes.c_int)]
+    L.falcon_launch_count.restype = ctypes.c_longlong
     _lib = L
     return L
 
@@ -237,6 +245,14 @@ class Batch:
         check(lib().falcon_batch_diagnostics(self.h, out))
         return [d.as_dict() for d in out]
 
+    def profile(self, nsteps):
+        """Per-kernel-class CUDA-event times of `nsteps` steps (advances the state)."""
+        stats = (KernelStat * 8)()
+        n = ctypes.c_int()
+        check(lib().falcon_batch_profile(self.h, nsteps, stats, 8, ctypes.byref(n)))
+        return {stats[i].name.decode(): {"launches": stats[i].launches, "ms": stats[i].ms,
+                                         "flops": stats[i].flops} for i in range(n.value)}
+
 
 class Instance(Batch):
     """One annulus instance (a batch of one)."""
@@ -267,3 +283,7 @@ def nonlin(nm, t, om, up, ur):
 
 def fp64_peak_gflops():
     return lib().falcon_fp64_peak_gflops()
+
+
+def launch_count():
+    return lib().falcon_launch_count()

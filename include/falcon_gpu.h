@@ -180,6 +180,22 @@ int falcon_server_iterate(falcon_server* s, int* n_active, int* n_queued);
  * tFR is not NULL, its final temperature field (Fortran layout). */
 int falcon_server_poll(falcon_server* s, int64_t id, int* done, falcon_diag* out, double* tFR);
 
+/* ---- measurement hooks ---- */
+/* Per-kernel-class statistics of `nsteps` steps of a batch, timed with CUDA
+ * events around every launch on the batch's stream (the steps advance the
+ * state like falcon_batch_step).  flops is the algorithmic FP64 operation
+ * count of the launches: 2*rows*K*N per GEMM, 5 P log2 P per complex FFT of
+ * length P (four per radial line) plus the grid products. */
+typedef struct falcon_kernel_stat {
+  char name[32];
+  int launches;
+  double ms;
+  double flops;
+} falcon_kernel_stat;
+int falcon_batch_profile(falcon_batch* b, int nsteps, falcon_kernel_stat* stats, int max_stats, int* nstats);
+/* Number of kernels this library has launched in the calling process. */
+long long falcon_launch_count(void);
+
 /* ---- misc ---- */
 const char* falcon_last_error(void);
 const char* falcon_version(void);
