@@ -194,6 +194,7 @@ def run_gpu(args):
     params = [fg.make_params(W["nr"], W["nm"], W["scheme"], ra=ra, dt=W["dt"], pr=W["pr"]) for ra in ras]
     seeds = [W["noise_seed0"] + rank * n + k for k in range(n)]
     peak = fg.fp64_peak_gflops()
+    mma_peak = fg.fp64_mma_peak_gflops()
 
     # ---- device-resident batched throughput ----
     b = fg.Batch(params)
@@ -233,6 +234,7 @@ def run_gpu(args):
                 "share": d["ms"] / tot,
                 "peak_source": "FP64 FMA throughput measured live by the library's DFMA kernel "
                                "(no FP64 figure in MEASURED_PEAKS.json)",
+                "fp64_mma_peak_tflops": mma_peak / 1e3,
                 "classes": {k: {"ms_per_step": v["ms"] / 3, "tflops": v["flops"] / (v["ms"] / 1e3) / 1e12,
                                 "share": v["ms"] / tot, "launches_per_step": v["launches"] / 3}
                             for k, v in prof.items()}}

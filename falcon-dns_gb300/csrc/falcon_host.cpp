@@ -1747,6 +1747,7 @@ int falcon_getrs_batched_dev(int n, int nsys, int nrhs, const double* lu_dev, co
 }
 
 double falcon_fp64_peak_gflops(void) { return measure_fp64_peak(); }
+double falcon_fp64_mma_peak_gflops(void) { return measure_fp64_mma_peak(); }
 
 }  // extern "C"
 

@@ -126,6 +126,8 @@ cudaError_t launch_remap_cols(const double* src, double* dst, size_t rows, int b
 cudaError_t launch_col_op(const double* src, double* dst, size_t rows, int B, int b, int ew, cudaStream_t s);
 // Self-timed FP64 FMA throughput kernel (returns GFLOP/s, or < 0 on error).
 double measure_fp64_peak();
+// Same for the FP64 tensor-core MMA (mma.sync m8n8k4 f64).
+double measure_fp64_mma_peak();
 // Set the odd-prime DFT coefficient tables (constant memory); idempotent.
 cudaError_t init_dft_tables();
 

@@ -943,3 +943,58 @@ cudaError_t launch_col_op(const double* src, double* dst, size_t rows, int B, in
 }
 
 }  // namespace falcon
+
+namespace falcon {
+
+// FP64 tensor-core (mma.sync m8n8k4 f64) throughput, measured to decide
+// between DMMA and DFMA for the per-mode contractions.
+__global__ void dmma_peak_kernel(double* out, int iters) {
+  const double a = threadIdx.x * 1e-3, b = 1.0 - a;
+  double c[4][2];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) { c[j][0] = 0.0; c[j][1] = 0.0; }
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+        asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0,%1}, {%2}, {%3}, {%0,%1};\n"
+                     : "+d"(c[j][0]), "+d"(c[j][1]) : "d"(a), "d"(b));
+    }
+  }
+  double s = 0.0;
+#pragma unroll
+  for (int j = 0; j < 4; ++j) s += c[j][0] + c[j][1];
+  out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+double measure_fp64_mma_peak() {
+  int dev = 0, nsm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return -1.0;
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  const int blocks = nsm * 4, threads = 128, iters = 100;
+  double* out = nullptr;
+  if (cudaMalloc(&out, sizeof(double) * blocks * threads) != cudaSuccess) return -1.0;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  dmma_peak_kernel<<<blocks, threads>>>(out, 10);
+  float best = 1e30f;
+  for (int rep = 0; rep < 3; ++rep) {
+    cudaEventRecord(e0);
+    dmma_peak_kernel<<<blocks, threads>>>(out, iters);
+    cudaEventRecord(e1);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (ms < best) best = ms;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  if (cudaGetLastError() != cudaSuccess) return -1.0;
+  const double flops = 2.0 * 8 * 8 * 4 * 16 * 4 * (double)iters * blocks * (threads / 32);
+  return flops / (best * 1e-3) / 1e9;
+}
+
+}  // namespace falcon

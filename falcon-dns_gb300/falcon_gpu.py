@@ -84,7 +84,7 @@ EXPORTS = (
     "falcon_cheb_fwd_dev", "falcon_cheb_inv_dev", "falcon_cheb_d1_dev", "falcon_cheb_d2_dev",
     "falcon_server_create", "falcon_server_destroy", "falcon_server_submit", "falcon_server_iterate",
     "falcon_server_poll", "falcon_last_error", "falcon_version", "falcon_fp64_peak_gflops",
-    "falcon_batch_profile", "falcon_launch_count",
+    "falcon_batch_profile", "falcon_launch_count", "falcon_fp64_mma_peak_gflops",
 )
 
 
@@ -137,6 +137,7 @@ def lib():
     L.falcon_server_iterate.argtypes = [vp, P(ctypes.c_int), P(ctypes.c_int)]
     L.falcon_server_poll.argtypes = [vp, ctypes.c_int64, P(ctypes.c_int), P(FalconDiag), dp]
     L.falcon_fp64_peak_gflops.restype = ctypes.c_double
+    L.falcon_fp64_mma_peak_gflops.restype = ctypes.c_double
     L.falcon_batch_profile.argtypes = [vp, ip, P(KernelStat), ip, P(ctypes.c_int)]
     L.falcon_launch_count.restype = ctypes.c_longlong
     _lib = L
@@ -283,6 +284,10 @@ def nonlin(nm, t, om, up, ur):
 
 def fp64_peak_gflops():
     return lib().falcon_fp64_peak_gflops()
+
+
+def fp64_mma_peak_gflops():
+    return lib().falcon_fp64_mma_peak_gflops()
 
 
 def launch_count():

@@ -202,6 +202,8 @@ const char* falcon_version(void);
 /* Measured FP64 FMA throughput of the current device in GFLOP/s (a short
  * self-timed kernel), used as the roofline denominator. */
 double falcon_fp64_peak_gflops(void);
+/* Same for the FP64 tensor-core path (mma.sync f64), for comparison. */
+double falcon_fp64_mma_peak_gflops(void);
 
 #ifdef __cplusplus
 }
