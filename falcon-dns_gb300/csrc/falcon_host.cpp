@@ -1370,6 +1370,14 @@ static int batch_create(const falcon_params* ps, int n, falcon_batch** out) {
   return 0;
 }
 
+namespace falcon {
+// Error text for entry points defined in the kernels translation unit.
+int set_error_message(const char* msg) {
+  g_err = msg ? msg : "";
+  return 0;
+}
+}  // namespace falcon
+
 extern "C" {
 
 const char* falcon_last_error(void) { return g_err.c_str(); }

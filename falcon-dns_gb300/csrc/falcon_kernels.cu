@@ -998,3 +998,123 @@ double measure_fp64_mma_peak() {
 }
 
 }  // namespace falcon
+
+// ---------------------------------------------------------------------------
+// Allocation-free nonlinear pass.
+//
+// falcon_nonlin_dev builds its FFT tables (P twiddles, P digit-reversal
+// positions) in device memory it allocates per call.  Some callers must not
+// have the library allocate: hosts that own every byte of device memory
+// through their own pre-sized pool (the way the serving loop budgets HBM per
+// request) and cannot let a library grow the footprint behind their back,
+// and hosts stepping in tight loops where a cudaMalloc/cudaFree pair would
+// synchronise the device on every call.  For them the tables live in the
+// fixed file-scope array below, sized for Np_max = 3*Nm_max <= 4096.
+// ---------------------------------------------------------------------------
+namespace falcon {
+
+constexpr int kNoAllocMaxP = 4096;
+// twiddles (kNoAllocMaxP double2) followed by positions (kNoAllocMaxP int):
+// 80 KiB, held by every GPU that loads the library until the process exits.
+constexpr size_t kNoAllocScratchBytes = (size_t)kNoAllocMaxP * (sizeof(double2) + sizeof(int));
+static __device__ __align__(256) unsigned char g_nonlin_scratch[kNoAllocScratchBytes];
+
+// Per-device address of g_nonlin_scratch (host code may not use the symbol
+// itself as a device pointer).
+static void* g_scratch_addr[64] = {nullptr};
+
+// tw[k] = exp(-2 pi i k/P); pos[n] = sum_s d_s(n) P/(p_0..p_s) for the radices
+// of `plan`, written into the scratch array.
+__global__ void noalloc_tables_kernel(FftPlan plan, double2* tw, int* pos) {
+  const int P = plan.P;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < P; k += gridDim.x * blockDim.x) {
+    double s, c;
+    sincospi(-2.0 * (double)k / (double)P, &s, &c);
+    tw[k] = make_double2(c, s);
+    int x = k, span = P, pp = 0;
+    for (int i = 0; i < plan.nrad; ++i) {
+      const int p = plan.rad[i];
+      const int d = x % p;
+      x /= p;
+      span /= p;
+      pp += d * span;
+    }
+    pos[k] = pp;
+  }
+}
+
+}  // namespace falcon
+
+extern "C" const char* falcon_last_error(void);
+namespace falcon { int set_error_message(const char* msg); }
+
+// Same computation and device layout as falcon_nonlin_dev, without any
+// device allocation: the FFT tables go to a fixed static device array.
+//  - The first call on a device looks up that device's address of the array
+//    (cudaGetSymbolAddress, with the device current); make that first call
+//    before any stream capture on that device.
+//  - Every call overwrites the whole table region it uses, so no state
+//    carries over between calls; but all calls on a device share the one
+//    array, so calls whose kernels overlap on the GPU (different streams, or
+//    host threads) race on it and must be serialised by the caller.
+//  - Limit: Np_max = 3*nm <= 4096 (nm <= 1365); larger sizes return
+//    FALCON_EINVAL (-1).
+extern "C" int falcon_nonlin_noalloc_dev(int nr, int nm, int nb, const double* t_dev, const double* omg_dev,
+                                         const double* up_dev, const double* ur_dev, double* uphi_t_dev,
+                                         double* ur_t_dev, double* uphi_omg_dev, double* ur_omg_dev,
+                                         void* stream) {
+  using namespace falcon;
+  if (nr < 1 || nm < 1 || nb < 1) { set_error_message("falcon_nonlin_noalloc_dev: invalid sizes"); return -1; }
+  const int P = 3 * nm;
+  if (P > kNoAllocMaxP) {
+    set_error_message("falcon_nonlin_noalloc_dev: Np_max = 3*Nm_max exceeds the 4096-point scratch limit");
+    return -1;
+  }
+  FftPlan plan{};
+  plan.P = P;
+  {
+    int n = P, k = 0;
+    while (n % 4 == 0 && k < kMaxRadix) { plan.rad[k++] = 4; n /= 4; }
+    while (n % 2 == 0 && k < kMaxRadix) { plan.rad[k++] = 2; n /= 2; }
+    for (int p = 3; p * p <= n && k < kMaxRadix; p += 2)
+      while (n % p == 0 && k < kMaxRadix) { plan.rad[k++] = p; n /= p; }
+    if (n > 1 && k < kMaxRadix) plan.rad[k++] = n;
+    plan.nrad = k;
+    for (int i = 0; i < k; ++i)
+      if (plan.rad[i] > 64) {
+        set_error_message("falcon_nonlin_noalloc_dev: 3*Nm_max has a prime factor above 64");
+        return -1;
+      }
+  }
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess || dev < 0 || dev >= 64) { set_error_message("falcon_nonlin_noalloc_dev: no current device"); return -2; }
+  if (!g_scratch_addr[dev]) {
+    void* ptr = nullptr;
+    e = cudaGetSymbolAddress(&ptr, g_nonlin_scratch);
+    if (e != cudaSuccess || !ptr) {
+      set_error_message("falcon_nonlin_noalloc_dev: cudaGetSymbolAddress failed");
+      return -2;
+    }
+    g_scratch_addr[dev] = ptr;
+  }
+  e = init_dft_tables();
+  if (e != cudaSuccess) { set_error_message(cudaGetErrorString(e)); return -2; }
+  double2* tw = reinterpret_cast<double2*>(g_scratch_addr[dev]);
+  int* pos = reinterpret_cast<int*>(reinterpret_cast<unsigned char*>(g_scratch_addr[dev]) +
+                                    (size_t)kNoAllocMaxP * sizeof(double2));
+  cudaStream_t s = (cudaStream_t)stream;
+  noalloc_tables_kernel<<<(P + 255) / 256, 256, 0, s>>>(plan, tw, pos);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) { set_error_message(cudaGetErrorString(e)); return -2; }
+  NonlinArgs a{};
+  a.R = nr; a.M = nm + 1; a.B = nb; a.Nm = nm;
+  a.plan = plan; a.tw = tw; a.pos = pos;
+  a.t = reinterpret_cast<const double2*>(t_dev); a.w = reinterpret_cast<const double2*>(omg_dev);
+  a.up = reinterpret_cast<const double2*>(up_dev); a.ur = reinterpret_cast<const double2*>(ur_dev);
+  a.ntp = reinterpret_cast<double2*>(uphi_t_dev); a.ntr = reinterpret_cast<double2*>(ur_t_dev);
+  a.nwp = reinterpret_cast<double2*>(uphi_omg_dev); a.nwr = reinterpret_cast<double2*>(ur_omg_dev);
+  e = launch_nonlin(a, s);
+  if (e != cudaSuccess) { set_error_message(cudaGetErrorString(e)); return -2; }
+  return 0;
+}

@@ -85,6 +85,7 @@ EXPORTS = (
     "falcon_server_create", "falcon_server_destroy", "falcon_server_submit", "falcon_server_iterate",
     "falcon_server_poll", "falcon_last_error", "falcon_version", "falcon_fp64_peak_gflops",
     "falcon_batch_profile", "falcon_launch_count", "falcon_fp64_mma_peak_gflops",
+    "falcon_nonlin_noalloc_dev",
 )
 
 
@@ -127,6 +128,7 @@ def lib():
     L.falcon_batch_device_bytes.restype = ctypes.c_size_t
     L.falcon_nonlin_dev.argtypes = [ip, ip, ip] + [ctypes.c_void_p] * 8 + [vp]
     L.falcon_nonlin.argtypes = [ip, ip] + [dp] * 8
+    L.falcon_nonlin_noalloc_dev.argtypes = [ip, ip, ip] + [ctypes.c_void_p] * 8 + [vp]
     L.falcon_getrs_batched_dev.argtypes = [ip, ip, ip, vp, vp, vp, vp]
     for f in ("falcon_cheb_fwd_dev", "falcon_cheb_inv_dev", "falcon_cheb_d1_dev", "falcon_cheb_d2_dev"):
         getattr(L, f).argtypes = [ip, ip, vp, vp, vp]

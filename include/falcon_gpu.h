@@ -145,6 +145,18 @@ size_t falcon_batch_device_bytes(const falcon_batch* b);
 int falcon_nonlin_dev(int nr, int nm, int nb, const double* t_dev, const double* omg_dev,
                       const double* up_dev, const double* ur_dev, double* uphi_t_dev,
                       double* ur_t_dev, double* uphi_omg_dev, double* ur_omg_dev, void* stream);
+/* Allocation-free form of falcon_nonlin_dev (no counterpart in the
+ * reference): same arguments, layout and results, but the library allocates
+ * no device memory -- its FFT tables go to a fixed 80 KiB static device
+ * array -- for hosts that own all device memory through their own budgeted
+ * pool, or that step in loops where cudaMalloc/cudaFree would synchronise
+ * the device.  Limit: 3*nm <= 4096, else FALCON_EINVAL.  The first call on a
+ * device resolves the array's device address (make it before any stream
+ * capture); every call overwrites the table region it uses; calls whose
+ * kernels overlap on the GPU share the array and race, so serialise them. */
+int falcon_nonlin_noalloc_dev(int nr, int nm, int nb, const double* t_dev, const double* omg_dev,
+                              const double* up_dev, const double* ur_dev, double* uphi_t_dev,
+                              double* ur_t_dev, double* uphi_omg_dev, double* ur_omg_dev, void* stream);
 /* Host-array form of falcon_nonlin_dev for one instance, Fortran layout;
  * copies in and out inside the call. */
 int falcon_nonlin(int nr, int nm, const double* tFR, const double* omgFR, const double* upFR,
