@@ -565,26 +565,10 @@ struct FftTables {
 
 int make_fft(int P, std::unique_ptr<FftTables>* out) {
   auto f = std::make_unique<FftTables>();
-  f->plan.P = P;
-  int n = P, k = 0;
-  std::vector<int> rad;
-  while (n % 4 == 0) { rad.push_back(4); n /= 4; }
-  while (n % 2 == 0) { rad.push_back(2); n /= 2; }
-  for (int p = 3; p * p <= n; p += 2)
-    while (n % p == 0) { rad.push_back(p); n /= p; }
-  if (n > 1) rad.push_back(n);
-  for (int p : rad)
-    if (p > 64) return fail(FALCON_EINVAL, "azimuthal length 3*Nm has a prime factor above 64");
-  if ((int)rad.size() > kMaxRadix) return fail(FALCON_EINVAL, "too many FFT stages");
-  f->plan.nrad = (int)rad.size();
-  for (int p : rad) f->plan.rad[k++] = p;
-  // digit-reversal positions: pos(n) = sum_s d_s(n) * P/(p_0..p_s)
+  if (make_fft_plan(P, &f->plan) != 0)
+    return fail(FALCON_EINVAL, "azimuthal length 3*Nm has a prime factor above 64 or too many factors");
   std::vector<int> pos(P);
-  for (int i = 0; i < P; ++i) {
-    int x = i, span = P, pp = 0;
-    for (int p : rad) { int d = x % p; x /= p; span /= p; pp += d * span; }
-    pos[i] = pp;
-  }
+  for (int i = 0; i < P; ++i) pos[i] = fft_position(f->plan, i);
   std::vector<double2> tw(P);
   const double two_pi = 8.0 * std::atan(1.0);
   for (int i = 0; i < P; ++i) {

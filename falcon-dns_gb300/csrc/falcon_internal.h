@@ -17,12 +17,87 @@ namespace falcon {
 constexpr int kMaxRadix = 16;     // stages of a mixed-radix FFT plan
 constexpr int kMaxStages = 6;     // IMEXRK stages supported
 
-// Mixed-radix plan of the azimuthal transform of length P = 3*Nm.
+// Plan of the azimuthal transform of length P = 3*Nm.  Two forms:
+//  - pfa = 1 (P square-free, prime factors <= 31): Good-Thomas prime-factor
+//    mapping; the stages are twiddle-free DFTs along the axes of a
+//    rad[0] x rad[1] x ... array (row-major, last axis contiguous) and the
+//    spectrum sits at pos[k] = sum_d ((k cinv[d]) mod rad[d]) stride[d],
+//    cinv[d] = (P/rad[d])^-1 mod rad[d];
+//  - pfa = 0: mixed-radix Cooley-Tukey, in-place DIT/DIF with twiddles and
+//    the spectrum at the digit-reversed positions pos[k].
 struct FftPlan {
   int P;
   int nrad;
-  int rad[kMaxRadix];   // radices, outermost first (DIT processes them last)
+  int pfa;
+  int rad[kMaxRadix];   // radices / axis sizes, outermost first
+  int cinv[kMaxRadix];
 };
+
+// Builds the plan for length P (host).  Returns 0, or -1 when P has a prime
+// factor above 64 or more than kMaxRadix factors.
+inline int make_fft_plan(int P, FftPlan* plan) {
+  FftPlan f{};
+  f.P = P;
+  int primes[64], np = 0, n = P;
+  for (int q = 2; q * q <= n; ++q)
+    while (n % q == 0) { if (np < 64) primes[np++] = q; n /= q; }
+  if (n > 1 && np < 64) primes[np++] = n;
+  bool squarefree = true, small = true;
+  for (int i = 0; i < np; ++i) {
+    if (i > 0 && primes[i] == primes[i - 1]) squarefree = false;
+    if (primes[i] > 31) small = false;
+    if (primes[i] > 64) return -1;
+  }
+  if (squarefree && small && np <= kMaxRadix) {
+    f.pfa = 1;
+    f.nrad = np;
+    for (int i = 0; i < np; ++i) {
+      const int Nd = primes[i], a = (P / Nd) % Nd;
+      int c = 1;
+      while ((a * c) % Nd != 1 % Nd) ++c;  // modular inverse, Nd <= 31
+      f.rad[i] = Nd;
+      f.cinv[i] = (Nd == 1) ? 0 : c;
+    }
+  } else {
+    int k = 0;
+    n = P;
+    while (n % 4 == 0 && k < kMaxRadix) { f.rad[k++] = 4; n /= 4; }
+    while (n % 2 == 0 && k < kMaxRadix) { f.rad[k++] = 2; n /= 2; }
+    for (int q = 3; q * q <= n && k < kMaxRadix; q += 2)
+      while (n % q == 0 && k < kMaxRadix) { f.rad[k++] = q; n /= q; }
+    if (n > 1) {
+      if (k >= kMaxRadix) return -1;
+      f.rad[k++] = n;
+    }
+    if (n > 1 && n > 64) return -1;
+    f.nrad = k;
+  }
+  *plan = f;
+  return 0;
+}
+
+// Position of spectral index k in the transform's work array.
+#ifdef __CUDACC__
+__host__ __device__
+#endif
+inline int fft_position(const FftPlan& f, int k) {
+  int span = f.P, pp = 0;
+  if (f.pfa) {
+    for (int i = 0; i < f.nrad; ++i) {
+      span /= f.rad[i];
+      pp += ((int)(((long long)k * f.cinv[i]) % f.rad[i])) * span;
+    }
+  } else {
+    int x = k;
+    for (int i = 0; i < f.nrad; ++i) {
+      const int d = x % f.rad[i];
+      x /= f.rad[i];
+      span /= f.rad[i];
+      pp += d * span;
+    }
+  }
+  return pp;
+}
 
 // Arguments of the nonlinear-pass kernel (Nr_maxLOOP, src/nonlin.F90:35-91).
 struct NonlinArgs {

@@ -73,111 +73,125 @@ cudaError_t init_dft_tables() {
   return e;
 }
 
-// Forward DFT of length p in registers: v_j <- sum_q v_q exp(-2 pi i j q/p).
+// Forward DFT of length p in registers: v_j <- sum_q v_q exp(-2 pi i j q/p)
+// (radix 2 and 4; odd primes go through dft_odd_store below).
 template <int p>
-__device__ __forceinline__ void dft(double2 (&v)[p]) {
+__device__ __forceinline__ void dft_small(double2 (&v)[p]) {
   if constexpr (p == 2) {
     double2 a = v[0], b = v[1];
     v[0] = cadd(a, b); v[1] = csub(a, b);
-  } else if constexpr (p == 4) {
+  } else {
     double2 t0 = cadd(v[0], v[2]), t1 = csub(v[0], v[2]);
     double2 t2 = cadd(v[1], v[3]), t3 = csub(v[1], v[3]);
     v[0] = cadd(t0, t2); v[2] = csub(t0, t2);
     v[1] = make_double2(t1.x + t3.y, t1.y - t3.x);
     v[3] = make_double2(t1.x - t3.y, t1.y + t3.x);
-  } else {
-    constexpr int h = (p - 1) / 2;
-    double2 a[h], b[h];
-#pragma unroll
-    for (int q = 1; q <= h; ++q) { a[q - 1] = cadd(v[q], v[p - q]); b[q - 1] = csub(v[q], v[p - q]); }
-    double2 y0 = v[0];
-#pragma unroll
-    for (int q = 0; q < h; ++q) y0 = cadd(y0, a[q]);
-#pragma unroll
-    for (int j = 1; j <= h; ++j) {
-      double2 A = v[0];
-      double2 Bv = make_double2(0.0, 0.0);
-#pragma unroll
-      for (int q = 1; q <= h; ++q) {
-        const int idx = (j * q) % p;
-        const double c = DftTab<p>::c(idx), s = DftTab<p>::s(idx);
-        A.x = fma(a[q - 1].x, c, A.x); A.y = fma(a[q - 1].y, c, A.y);
-        Bv.x = fma(b[q - 1].x, s, Bv.x); Bv.y = fma(b[q - 1].y, s, Bv.y);
-      }
-      v[j] = make_double2(A.x + Bv.y, A.y - Bv.x);
-      v[p - j] = make_double2(A.x - Bv.y, A.y + Bv.x);
-    }
-    v[0] = y0;
   }
 }
 
-// One in-place decimation-in-time stage (radix p, current span m) applied to
-// two buffers at once.  tw[k] = exp(-2 pi i k / P); stride = P / (m p).
+// Odd-prime forward DFT in the symmetric form
+//   y_0 = v_0 + sum a_q,  y_j = A_j - i B_j,  y_{p-j} = A_j + i B_j,
+//   a_q = v_q + v_{p-q}, b_q = v_q - v_{p-q}, A_j = v_0 + sum a_q cos(2 pi jq/p),
+//   B_j = sum b_q sin(2 pi jq/p),
+// with each output pair multiplied by its twiddle (DIF) and stored as soon
+// as it is formed, so only a, b stay live.
 template <int p>
-__device__ __forceinline__ void dit_stage(double2* __restrict__ A, double2* __restrict__ Bf, int P,
-                                          int m, int stride, const double2* __restrict__ tw, int lane) {
+__device__ __forceinline__ void dft_odd_store(double2 (&v)[p], double2* __restrict__ dst, int base, int m,
+                                              const double2* __restrict__ tw, int ks, bool post_tw) {
+  constexpr int h = (p - 1) / 2;
+  double2 a[h], b[h];
+#pragma unroll
+  for (int q = 1; q <= h; ++q) { a[q - 1] = cadd(v[q], v[p - q]); b[q - 1] = csub(v[q], v[p - q]); }
+  const double2 v0 = v[0];
+  double2 y0 = v0;
+#pragma unroll
+  for (int q = 0; q < h; ++q) y0 = cadd(y0, a[q]);
+  dst[base] = y0;
+#pragma unroll
+  for (int j = 1; j <= h; ++j) {
+    double2 A = v0;
+    double2 Bv = make_double2(0.0, 0.0);
+#pragma unroll
+    for (int q = 1; q <= h; ++q) {
+      const int idx = (j * q) % p;
+      const double c = DftTab<p>::c(idx), s = DftTab<p>::s(idx);
+      A.x = fma(a[q - 1].x, c, A.x); A.y = fma(a[q - 1].y, c, A.y);
+      Bv.x = fma(b[q - 1].x, s, Bv.x); Bv.y = fma(b[q - 1].y, s, Bv.y);
+    }
+    double2 yj = make_double2(A.x + Bv.y, A.y - Bv.x);
+    double2 yk = make_double2(A.x - Bv.y, A.y + Bv.x);
+    if (post_tw) {
+      yj = cmul(yj, tw[j * ks]);
+      yk = cmul(yk, tw[(p - j) * ks]);
+    }
+    dst[base + j * m] = yj;
+    dst[base + (p - j) * m] = yk;
+  }
+}
+
+// One in-place stage of radix p and span m on NB (1 or 2) buffers.
+// DIT (dif = false): twiddles exp(-2 pi i q k / (m p)) on the inputs; DIF:
+// on the outputs; none for the prime-factor plan (twid = false).
+// tw[k] = exp(-2 pi i k / P); stride = P / (m p).
+template <int p, int NB>
+__device__ __forceinline__ void fft_stage(double2* __restrict__ A, double2* __restrict__ Bf, int P, int m,
+                                          int stride, const double2* __restrict__ tw, int lane, bool dif,
+                                          bool twid) {
   const int mp = m * p, nb = P / p;
   const float inv_m = 1.0f / (float)m;
   for (int t = lane; t < nb; t += 32) {
     const int g = (int)(((float)t + 0.5f) * inv_m);
     const int k = t - g * m;
     const int base = g * mp + k;
+    const bool tk = twid && k > 0;
+    const int ks = k * stride;
     double2 va[p], vb[p];
 #pragma unroll
-    for (int q = 0; q < p; ++q) { va[q] = A[base + q * m]; vb[q] = Bf[base + q * m]; }
-    if (k > 0) {
-      const int ks = k * stride;
+    for (int q = 0; q < p; ++q) {
+      va[q] = A[base + q * m];
+      if (NB == 2) vb[q] = Bf[base + q * m];
+    }
+    if (tk && !dif) {
 #pragma unroll
       for (int q = 1; q < p; ++q) {
         const double2 w = tw[q * ks];
-        va[q] = cmul(va[q], w); vb[q] = cmul(vb[q], w);
+        va[q] = cmul(va[q], w);
+        if (NB == 2) vb[q] = cmul(vb[q], w);
       }
     }
-    dft<p>(va);
-    dft<p>(vb);
+    if constexpr (p == 2 || p == 4) {
+      dft_small<p>(va);
+      if (NB == 2) dft_small<p>(vb);
+      if (tk && dif) {
 #pragma unroll
-    for (int q = 0; q < p; ++q) { A[base + q * m] = va[q]; Bf[base + q * m] = vb[q]; }
-  }
-}
-
-// One in-place decimation-in-frequency stage (radix p, span m after it).
-template <int p>
-__device__ __forceinline__ void dif_stage(double2* __restrict__ A, double2* __restrict__ Bf, int P,
-                                          int m, int stride, const double2* __restrict__ tw, int lane) {
-  const int mp = m * p, nb = P / p;
-  const float inv_m = 1.0f / (float)m;
-  for (int t = lane; t < nb; t += 32) {
-    const int g = (int)(((float)t + 0.5f) * inv_m);
-    const int k = t - g * m;
-    const int base = g * mp + k;
-    double2 va[p], vb[p];
-#pragma unroll
-    for (int q = 0; q < p; ++q) { va[q] = A[base + q * m]; vb[q] = Bf[base + q * m]; }
-    dft<p>(va);
-    dft<p>(vb);
-    if (k > 0) {
-      const int ks = k * stride;
-#pragma unroll
-      for (int q = 1; q < p; ++q) {
-        const double2 w = tw[q * ks];
-        va[q] = cmul(va[q], w); vb[q] = cmul(vb[q], w);
+        for (int q = 1; q < p; ++q) {
+          const double2 w = tw[q * ks];
+          va[q] = cmul(va[q], w);
+          if (NB == 2) vb[q] = cmul(vb[q], w);
+        }
       }
-    }
 #pragma unroll
-    for (int q = 0; q < p; ++q) { A[base + q * m] = va[q]; Bf[base + q * m] = vb[q]; }
+      for (int q = 0; q < p; ++q) {
+        A[base + q * m] = va[q];
+        if (NB == 2) Bf[base + q * m] = vb[q];
+      }
+    } else {
+      dft_odd_store<p>(va, A, base, m, tw, ks, tk && dif);
+      if (NB == 2) dft_odd_store<p>(vb, Bf, base, m, tw, ks, tk && dif);
+    }
   }
 }
 
 // Generic prime radix (p <= 64) with coefficients read from the P-point
 // twiddle table: exp(-2 pi i j/p) = tw[j * P/p].
 __device__ void generic_stage(double2* A, double2* Bf, int P, int p, int m, int stride,
-                              const double2* tw, int lane, bool dif) {
+                              const double2* tw, int lane, bool dif, bool twid) {
   const int mp = m * p, nb = P / p, tp = P / p;
   for (int t = lane; t < nb; t += 32) {
     const int g = t / m, k = t - g * m, base = g * mp + k;
     double2 va[64], vb[64], ya[64], yb[64];
     for (int q = 0; q < p; ++q) { va[q] = A[base + q * m]; vb[q] = Bf[base + q * m]; }
-    if (!dif && k > 0)
+    if (twid && !dif && k > 0)
       for (int q = 1; q < p; ++q) { double2 w = tw[q * k * stride]; va[q] = cmul(va[q], w); vb[q] = cmul(vb[q], w); }
     for (int j = 0; j < p; ++j) {
       double2 sa = make_double2(0, 0), sb = make_double2(0, 0);
@@ -187,26 +201,37 @@ __device__ void generic_stage(double2* A, double2* Bf, int P, int p, int m, int 
       }
       ya[j] = sa; yb[j] = sb;
     }
-    if (dif && k > 0)
+    if (twid && dif && k > 0)
       for (int q = 1; q < p; ++q) { double2 w = tw[q * k * stride]; ya[q] = cmul(ya[q], w); yb[q] = cmul(yb[q], w); }
     for (int q = 0; q < p; ++q) { A[base + q * m] = ya[q]; Bf[base + q * m] = yb[q]; }
   }
 }
 
-__device__ __forceinline__ void run_stage(int p, bool dif, double2* A, double2* Bf, int P, int m,
+// MAXP bounds the radices compiled into one kernel instance, so a plan
+// with small radices is not held to the register budget of radix 31.
+template <int MAXP>
+__device__ __forceinline__ void run_stage(int p, bool dif, bool twid, double2* A, double2* Bf, int P, int m,
                                           int stride, const double2* tw, int lane) {
-#define FALCON_CASE(q)                                                  \
-  case q:                                                               \
-    if (dif) dif_stage<q>(A, Bf, P, m, stride, tw, lane);               \
-    else dit_stage<q>(A, Bf, P, m, stride, tw, lane);                   \
+  // two buffers interleaved up to radix 7; one at a time above, to bound
+  // the live registers of the butterfly
+#define FALCON_CASE2(q) case q: fft_stage<q, 2>(A, Bf, P, m, stride, tw, lane, dif, twid); return;
+#define FALCON_CASE1(q)                                                  \
+  case q:                                                                \
+    if constexpr (q <= MAXP) {                                           \
+      fft_stage<q, 1>(A, nullptr, P, m, stride, tw, lane, dif, twid);    \
+      fft_stage<q, 1>(Bf, nullptr, P, m, stride, tw, lane, dif, twid);   \
+      return;                                                            \
+    }                                                                    \
     break;
   switch (p) {
-    FALCON_CASE(2) FALCON_CASE(3) FALCON_CASE(4) FALCON_CASE(5) FALCON_CASE(7)
-    FALCON_CASE(11) FALCON_CASE(13) FALCON_CASE(17) FALCON_CASE(19) FALCON_CASE(23)
-    FALCON_CASE(29) FALCON_CASE(31)
-    default: generic_stage(A, Bf, P, p, m, stride, tw, lane, dif); break;
+    FALCON_CASE2(2) FALCON_CASE2(3) FALCON_CASE2(4) FALCON_CASE2(5) FALCON_CASE2(7)
+    FALCON_CASE1(11) FALCON_CASE1(13) FALCON_CASE1(17)
+    FALCON_CASE1(19) FALCON_CASE1(23) FALCON_CASE1(29) FALCON_CASE1(31)
+    default: break;
   }
-#undef FALCON_CASE
+#undef FALCON_CASE1
+#undef FALCON_CASE2
+  generic_stage(A, Bf, P, p, m, stride, tw, lane, dif, twid);
 }
 
 // ---------------------------------------------------------------------------
@@ -216,7 +241,8 @@ __device__ __forceinline__ void run_stage(int p, bool dif, double2* A, double2* 
 // two forward FFTs that return u_phi*T, u_r*T, u_phi*omega, u_r*omega
 // truncated to modes 0..Nm and divided by P.
 // ---------------------------------------------------------------------------
-__global__ void nonlin_kernel(NonlinArgs a) {
+template <int MAXP>
+__global__ void __launch_bounds__(128) nonlin_kernel(NonlinArgs a) {
   extern __shared__ double2 smem[];
   const int P = a.plan.P;
   double2* tw = smem;
@@ -258,7 +284,7 @@ __global__ void nonlin_kernel(NonlinArgs a) {
     int m = 1;
     for (int s = a.plan.nrad - 1; s >= 0; --s) {
       const int p = a.plan.rad[s];
-      run_stage(p, false, bufA, bufB, P, m, P / (m * p), tw, lane);
+      run_stage<MAXP>(p, false, !a.plan.pfa, bufA, bufB, P, m, P / (m * p), tw, lane);
       m *= p;
       __syncwarp();
     }
@@ -280,7 +306,7 @@ __global__ void nonlin_kernel(NonlinArgs a) {
     for (int s = 0; s < a.plan.nrad; ++s) {
       const int p = a.plan.rad[s];
       m /= p;
-      run_stage(p, true, bufA, bufB, P, m, P / (m * p), tw, lane);
+      run_stage<MAXP>(p, true, !a.plan.pfa, bufA, bufB, P, m, P / (m * p), tw, lane);
       __syncwarp();
     }
   }
@@ -320,59 +346,89 @@ static int nonlin_warps(int P, int* smem_bytes) {
   return w;
 }
 
-cudaError_t launch_nonlin(const NonlinArgs& a, cudaStream_t s) {
+template <int MAXP>
+static cudaError_t launch_nonlin_t(const NonlinArgs& a, cudaStream_t s) {
   int smem = 0;
   const int w = nonlin_warps(a.plan.P, &smem);
-  cudaError_t e = cudaFuncSetAttribute(nonlin_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  cudaError_t e = cudaFuncSetAttribute(nonlin_kernel<MAXP>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return e;
   const int nlines = a.R * a.B;
   const int grid = (nlines + w - 1) / w;
-  nonlin_kernel<<<grid, 32 * w, smem, s>>>(a);
+  nonlin_kernel<MAXP><<<grid, 32 * w, smem, s>>>(a);
   return cudaGetLastError();
+}
+
+cudaError_t launch_nonlin(const NonlinArgs& a, cudaStream_t s) {
+  int maxp = 0;
+  for (int i = 0; i < a.plan.nrad; ++i) maxp = a.plan.rad[i] > maxp ? a.plan.rad[i] : maxp;
+  if (maxp <= 7) return launch_nonlin_t<7>(a, s);
+  if (maxp <= 17) return launch_nonlin_t<17>(a, s);
+  return launch_nonlin_t<31>(a, s);
 }
 
 // ---------------------------------------------------------------------------
 // Register-tiled FP64 GEMM, Y = alpha * A * X (A column-major, rows x K).
-// 256 threads: warp w owns rows [row0 + w*RPT, +RPT), lane owns columns
-// n0 + 2*lane + {0,1}; K is staged in chunks of 16 through shared memory.
+// nw warps per block (runtime); warp w owns RPT consecutive rows
+// [row0 + w*RPT, +RPT), lane owns columns n0 + 2*lane + {0,1}.  K is staged
+// in chunks of 16 through shared memory; the last chunk runs only its valid
+// length, and nw*RPT is chosen on the host to cover the rows with little
+// padding, so the FP64 pipe does almost no wasted FMAs.
 // ---------------------------------------------------------------------------
 constexpr int kKC = 16;
 
 template <int RPT>
-__global__ void __launch_bounds__(256) gemm_tile_kernel(GemmArgs g) {
-  constexpr int ROWS = 8 * RPT;
-  __shared__ __align__(16) double As[kKC][ROWS + 2];
-  __shared__ __align__(16) double Xs[kKC][64];
+__global__ void __launch_bounds__(512) gemm_tile_kernel(GemmArgs g) {
+  extern __shared__ __align__(16) double gsm[];
+  const int nw = blockDim.x >> 5;
+  const int rows_blk = nw * RPT;
+  double* As = gsm;                    // [kKC][rows_blk]
+  double* Xs = gsm + kKC * rows_blk;   // [kKC][64]
   const int z = blockIdx.z;
   const double* A = g.A + (size_t)z * g.sA;
   const double* X = g.X + (size_t)z * g.sX;
   double* Y = g.Y + (size_t)z * g.sY;
   const int n0 = blockIdx.x * 64;
-  const int row0 = blockIdx.y * ROWS;
+  const int row0 = blockIdx.y * rows_blk;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   double acc[RPT][2];
 #pragma unroll
   for (int i = 0; i < RPT; ++i) { acc[i][0] = 0.0; acc[i][1] = 0.0; }
   for (int k0 = 0; k0 < g.K; k0 += kKC) {
-    for (int idx = threadIdx.x; idx < kKC * ROWS; idx += 256) {
-      const int kk = idx / ROWS, rr = idx - kk * ROWS;
-      const int k = k0 + kk, row = row0 + rr;
-      As[kk][rr] = (k < g.K && row < g.rows) ? A[(size_t)k * g.lda + row] : 0.0;
+    const int kc = min(kKC, g.K - k0);
+    for (int kk = 0; kk < kc; ++kk) {
+      const double* Ak = A + (size_t)(k0 + kk) * g.lda;
+      for (int rr = threadIdx.x; rr < rows_blk; rr += blockDim.x) {
+        const int row = row0 + rr;
+        As[kk * rows_blk + rr] = (row < g.rows) ? Ak[row] : 0.0;
+      }
     }
-    for (int idx = threadIdx.x; idx < kKC * 64; idx += 256) {
+    for (int idx = threadIdx.x; idx < kc * 64; idx += blockDim.x) {
       const int kk = idx >> 6, c = idx & 63;
-      const int k = k0 + kk, n = n0 + c;
-      Xs[kk][c] = (k < g.K && n < g.N) ? X[(size_t)k * g.ldx + n] : 0.0;
+      const int n = n0 + c;
+      Xs[kk * 64 + c] = (n < g.N) ? X[(size_t)(k0 + kk) * g.ldx + n] : 0.0;
     }
     __syncthreads();
+    const double* Aw = As + warp * RPT;
+    if (kc == kKC) {
 #pragma unroll
-    for (int kk = 0; kk < kKC; ++kk) {
-      const double2 xv = *reinterpret_cast<const double2*>(&Xs[kk][2 * lane]);
+      for (int kk = 0; kk < kKC; ++kk) {
+        const double2 xv = *reinterpret_cast<const double2*>(&Xs[kk * 64 + 2 * lane]);
 #pragma unroll
-      for (int i = 0; i < RPT; ++i) {
-        const double av = As[kk][warp * RPT + i];
-        acc[i][0] = fma(av, xv.x, acc[i][0]);
-        acc[i][1] = fma(av, xv.y, acc[i][1]);
+        for (int i = 0; i < RPT; ++i) {
+          const double av = Aw[kk * rows_blk + i];
+          acc[i][0] = fma(av, xv.x, acc[i][0]);
+          acc[i][1] = fma(av, xv.y, acc[i][1]);
+        }
+      }
+    } else {
+      for (int kk = 0; kk < kc; ++kk) {
+        const double2 xv = *reinterpret_cast<const double2*>(&Xs[kk * 64 + 2 * lane]);
+#pragma unroll
+        for (int i = 0; i < RPT; ++i) {
+          const double av = Aw[kk * rows_blk + i];
+          acc[i][0] = fma(av, xv.x, acc[i][0]);
+          acc[i][1] = fma(av, xv.y, acc[i][1]);
+        }
       }
     }
     __syncthreads();
@@ -421,10 +477,26 @@ __global__ void __launch_bounds__(128) gemv_kernel(GemmArgs g) {
 }
 
 template <int RPT>
-static cudaError_t launch_tile(const GemmArgs& g, int row_blocks, cudaStream_t s) {
+static cudaError_t launch_tile(const GemmArgs& g, int nw, int row_blocks, cudaStream_t s) {
   dim3 grid((g.N + 63) / 64, row_blocks, g.batch);
-  gemm_tile_kernel<RPT><<<grid, 256, 0, s>>>(g);
+  const size_t smem = (size_t)kKC * (nw * RPT + 64) * sizeof(double);
+  gemm_tile_kernel<RPT><<<grid, 32 * nw, smem, s>>>(g);
   return cudaGetLastError();
+}
+
+// Smallest nw*rpt >= rows with 2 <= nw <= 16 warps and rpt <= 16.
+static void pick_tile(int rows, int* nw_out, int* rpt_out) {
+  int best = 1 << 30, bnw = 8, brpt = 16;
+  for (int rpt = 1; rpt <= 16; ++rpt)
+    for (int nw = 2; nw <= 16; ++nw) {
+      const int cover = nw * rpt;
+      if (cover < rows) continue;
+      // prefer little padding, then 4..12 warps
+      const int score = (cover - rows) * 64 + ((nw < 4 || nw > 12) ? 8 : 0) + nw;
+      if (score < best) { best = score; bnw = nw; brpt = rpt; }
+    }
+  *nw_out = bnw;
+  *rpt_out = brpt;
 }
 
 cudaError_t launch_gemm(const GemmArgs& g, cudaStream_t s) {
@@ -437,33 +509,35 @@ cudaError_t launch_gemm(const GemmArgs& g, cudaStream_t s) {
     else gemv_kernel<8><<<grid, 128, sm, s>>>(g);
     return cudaGetLastError();
   }
-  // Choose rows per thread: cover all rows in one block when there is
-  // enough column parallelism, otherwise split the rows across blocks.
+  // One block row tile covers all rows when the column blocks alone fill
+  // the GPU; otherwise the rows are split into up to 16 tiles.
   int dev = 0, nsm = 152;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   const long col_blocks = (long)((g.N + 63) / 64) * g.batch;
-  int rpt = (g.rows + 7) / 8;
-  if (rpt > 16) rpt = 16;
-  while (rpt > 1 && col_blocks * ((g.rows + 8 * rpt - 1) / (8 * rpt)) < 2L * nsm) rpt = (rpt + 1) / 2;
-  const int rb = (g.rows + 8 * rpt - 1) / (8 * rpt);
+  int rb = 1;
+  while (rb < 16 && col_blocks * rb < 2L * nsm && (g.rows + rb) / (rb + 1) >= 4) ++rb;
+  const int rows_per = (g.rows + rb - 1) / rb;
+  int nw, rpt;
+  pick_tile(rows_per, &nw, &rpt);
+  rb = (g.rows + nw * rpt - 1) / (nw * rpt);
   switch (rpt) {
-    case 1: return launch_tile<1>(g, rb, s);
-    case 2: return launch_tile<2>(g, rb, s);
-    case 3: return launch_tile<3>(g, rb, s);
-    case 4: return launch_tile<4>(g, rb, s);
-    case 5: return launch_tile<5>(g, rb, s);
-    case 6: return launch_tile<6>(g, rb, s);
-    case 7: return launch_tile<7>(g, rb, s);
-    case 8: return launch_tile<8>(g, rb, s);
-    case 9: return launch_tile<9>(g, rb, s);
-    case 10: return launch_tile<10>(g, rb, s);
-    case 11: return launch_tile<11>(g, rb, s);
-    case 12: return launch_tile<12>(g, rb, s);
-    case 13: return launch_tile<13>(g, rb, s);
-    case 14: return launch_tile<14>(g, rb, s);
-    case 15: return launch_tile<15>(g, rb, s);
-    default: return launch_tile<16>(g, rb, s);
+    case 1: return launch_tile<1>(g, nw, rb, s);
+    case 2: return launch_tile<2>(g, nw, rb, s);
+    case 3: return launch_tile<3>(g, nw, rb, s);
+    case 4: return launch_tile<4>(g, nw, rb, s);
+    case 5: return launch_tile<5>(g, nw, rb, s);
+    case 6: return launch_tile<6>(g, nw, rb, s);
+    case 7: return launch_tile<7>(g, nw, rb, s);
+    case 8: return launch_tile<8>(g, nw, rb, s);
+    case 9: return launch_tile<9>(g, nw, rb, s);
+    case 10: return launch_tile<10>(g, nw, rb, s);
+    case 11: return launch_tile<11>(g, nw, rb, s);
+    case 12: return launch_tile<12>(g, nw, rb, s);
+    case 13: return launch_tile<13>(g, nw, rb, s);
+    case 14: return launch_tile<14>(g, nw, rb, s);
+    case 15: return launch_tile<15>(g, nw, rb, s);
+    default: return launch_tile<16>(g, nw, rb, s);
   }
 }
 
@@ -1031,15 +1105,7 @@ __global__ void noalloc_tables_kernel(FftPlan plan, double2* tw, int* pos) {
     double s, c;
     sincospi(-2.0 * (double)k / (double)P, &s, &c);
     tw[k] = make_double2(c, s);
-    int x = k, span = P, pp = 0;
-    for (int i = 0; i < plan.nrad; ++i) {
-      const int p = plan.rad[i];
-      const int d = x % p;
-      x /= p;
-      span /= p;
-      pp += d * span;
-    }
-    pos[k] = pp;
+    pos[k] = fft_position(plan, k);
   }
 }
 
@@ -1071,20 +1137,9 @@ extern "C" int falcon_nonlin_noalloc_dev(int nr, int nm, int nb, const double* t
     return -1;
   }
   FftPlan plan{};
-  plan.P = P;
-  {
-    int n = P, k = 0;
-    while (n % 4 == 0 && k < kMaxRadix) { plan.rad[k++] = 4; n /= 4; }
-    while (n % 2 == 0 && k < kMaxRadix) { plan.rad[k++] = 2; n /= 2; }
-    for (int p = 3; p * p <= n && k < kMaxRadix; p += 2)
-      while (n % p == 0 && k < kMaxRadix) { plan.rad[k++] = p; n /= p; }
-    if (n > 1 && k < kMaxRadix) plan.rad[k++] = n;
-    plan.nrad = k;
-    for (int i = 0; i < k; ++i)
-      if (plan.rad[i] > 64) {
-        set_error_message("falcon_nonlin_noalloc_dev: 3*Nm_max has a prime factor above 64");
-        return -1;
-      }
+  if (make_fft_plan(P, &plan) != 0) {
+    set_error_message("falcon_nonlin_noalloc_dev: 3*Nm_max has a prime factor above 64");
+    return -1;
   }
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
