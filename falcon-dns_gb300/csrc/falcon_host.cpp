@@ -192,10 +192,13 @@ struct OpSet {
   double* U = nullptr;     // 2R x R: [Tinv A_u^-1; D1inv A_u^-1]
   double* inv_r = nullptr;
   double* inv_r2 = nullptr;
+  double* wq = nullptr;     // radInt weights (src/integ.F90:36-76) on values
+  double* d1_0 = nullptr;   // rows 0 and R-1 of D1p
+  double* d1_R = nullptr;
   size_t bytes = 0;
   ~OpSet() {
     cudaFree(D1p); cudaFree(Lp); cudaFree(ST); cudaFree(G); cudaFree(U);
-    cudaFree(inv_r); cudaFree(inv_r2);
+    cudaFree(inv_r); cudaFree(inv_r2); cudaFree(wq); cudaFree(d1_0); cudaFree(d1_R);
   }
 };
 
@@ -401,6 +404,30 @@ int build_opset(const OpKey& k, std::shared_ptr<OpSet>* out) {
   if ((rc = upload(&ops->U, U, &ops->bytes))) return rc;
   if ((rc = upload(&ops->inv_r, c.inv_r, &ops->bytes))) return rc;
   if ((rc = upload(&ops->inv_r2, c.inv_r2, &ops->bytes))) return rc;
+  {
+    // radInt(f) = fac * sum_k w_k Re(chebtransform(f r))_k with w_k = -1/(k^2-1)
+    // for even k (halved at k = 0, R-1), 0 for odd k; chebtransform is
+    // t^T diag(c') / ((R-1) fac) on the values.
+    const double fac = std::sqrt(2.0 / (double)(R - 1));
+    std::vector<double> wq(R, 0.0), d10(R), d1R(R);
+    for (int k = 0; k < R; ++k) {
+      if (k % 2 != 0) continue;
+      double qk = -1.0 / (double)(k * k - 1);
+      if (k == 0 || k == R - 1) qk *= 0.5;
+      for (int j = 0; j < R; ++j) {
+        const double cp = (j == 0 || j == R - 1) ? 1.0 : 2.0;
+        wq[j] += qk * cp * c.t[j + (size_t)R * k] / ((double)(R - 1) * fac);
+      }
+    }
+    for (int j = 0; j < R; ++j) {
+      wq[j] *= fac * c.radius[j];
+      d10[j] = D1p[0 + (size_t)R * j];
+      d1R[j] = D1p[(R - 1) + (size_t)R * j];
+    }
+    if ((rc = upload(&ops->wq, wq, &ops->bytes))) return rc;
+    if ((rc = upload(&ops->d1_0, d10, &ops->bytes))) return rc;
+    if ((rc = upload(&ops->d1_R, d1R, &ops->bytes))) return rc;
+  }
   {
     std::lock_guard<std::mutex> lk(g_ops_mu);
     g_ops[k] = ops;
@@ -611,6 +638,8 @@ struct Group {
   double2 *t0 = nullptr, *w0 = nullptr;
   double* u0 = nullptr;
   double2* t_grid = nullptr;   // temperature seen by the last nonlinear pass (IMEXRK)
+  double* diag_dev = nullptr;  // 8 per instance
+  std::vector<double> diag_host;
   double2* stage_buf = nullptr;  // host staging (pinned) for one instance
   Prof* prof = nullptr;
   int head = 0, head_e = 0;
@@ -709,7 +738,8 @@ int group_init(Group* g, const std::vector<falcon_params>& ps, const std::vector
       (rc = g->alloc(&g->nwr, n)) || (rc = g->alloc(&g->dntr, n)) || (rc = g->alloc(&g->dnwr, n)) ||
       (rc = g->alloc(&g->lt, n)) || (rc = g->alloc(&g->lw, n)) || (rc = g->alloc(&g->lu0, (size_t)R * B)) ||
       (rc = g->alloc(&g->rhs_t, n)) || (rc = g->alloc(&g->rhs_w, n)) ||
-      (rc = g->alloc(&g->ub2, (size_t)2 * R * B)) || (rc = g->alloc(&g->ra_pr, (size_t)B)))
+      (rc = g->alloc(&g->ub2, (size_t)2 * R * B)) || (rc = g->alloc(&g->ra_pr, (size_t)B)) ||
+      (rc = g->alloc(&g->diag_dev, (size_t)8 * B)))
     return rc;
   g->ub = reinterpret_cast<double*>(g->ub2);
   g->ra_pr_h.resize(B);
@@ -1089,6 +1119,35 @@ int group_reset_instance(Group* g, int b) {
   return 0;
 }
 
+// writeKE_spectral of every instance of the group on the device; fills
+// g->diag_host (8 doubles per instance).
+int group_diagnostics(Group* g) {
+  OpSet* o = g->ops.get();
+  DiagArgs a{};
+  a.R = g->R; a.M = g->M; a.B = g->B; a.mbc_sf = g->p.mbc == 1;
+  a.t = g->T(); a.w = g->W(); a.up = g->up; a.ur = g->ur;
+  if (g->p.scheme_type == FALCON_IMEX) a.tprev = (g->n_step > 0) ? g->th[(g->head + 1) % g->sch.n_imp] : g->T();
+  else a.tprev = g->t_grid;
+  a.wq = o->wq; a.d1_0 = o->d1_0; a.d1_R = o->d1_R; a.ra_pr = g->ra_pr;
+  const double eta = g->p.eta;
+  a.nu_bot_den = (1.0 - eta) / (eta * std::log(eta));
+  a.nu_top_den = (1.0 - eta) / std::log(eta);
+  a.pi = 4.0 * std::atan(1.0);
+  a.out = g->diag_dev;
+  CK(launch_diagnostics(a, g->stream));
+  g->diag_host.resize((size_t)8 * g->B);
+  CK(cudaMemcpyAsync(g->diag_host.data(), g->diag_dev, sizeof(double) * 8 * g->B, cudaMemcpyDeviceToHost, g->stream));
+  CK(cudaStreamSynchronize(g->stream));
+  return 0;
+}
+
+void fill_diag(const Group* g, int b, double time, falcon_diag* d) {
+  const double* v = &g->diag_host[(size_t)8 * b];
+  d->time = time; d->dt = g->p.dt;
+  d->ke = v[0]; d->ke_r = v[1]; d->ke_phi = v[2]; d->ke_upbar = v[3];
+  d->nu_top = v[4]; d->nu_bot = v[5]; d->vis = v[6]; d->buo = v[7];
+}
+
 // Seeded noise (host): splitmix64 keyed by (seed, m, i), Box-Muller in FP64.
 uint64_t splitmix64(uint64_t* x) {
   uint64_t z = (*x += 0x9E3779B97F4A7C15ull);
@@ -1212,90 +1271,6 @@ void initial_temperature(const falcon_params& p, int kind, double amp, uint64_t 
       host_forfft(Nm, P, tt.data(), &tFR[(size_t)2 * M * r]);
     }
   }
-}
-
-// ---------------------------------------------------------------------------
-// writeKE_spectral (src/output.F90:122-324) evaluated on the host from the
-// downloaded state of one instance.
-// ---------------------------------------------------------------------------
-double radint(const Cheb& c, const std::vector<double>& f) {
-  // radInt (src/integ.F90:36-76): chebtransform of f*r, Clenshaw-Curtis weights
-  const int R = c.R;
-  std::vector<double> ff(R), ft(R);
-  for (int i = 0; i < R; ++i) ff[i] = f[i] * c.radius[i];
-  const double fac = std::sqrt(2.0 / (double)(R - 1));
-  for (int k = 0; k < R; ++k) {
-    double s = 0.0;
-    for (int i = 0; i < R; ++i) {
-      const double cp = (i == 0 || i == R - 1) ? 1.0 : 2.0;
-      s += cp * ff[i] * c.t[i + (size_t)R * k];
-    }
-    ft[k] = s / ((double)(R - 1) * fac);
-  }
-  double tot = 0.0;
-  for (int i = 0; i < R; ++i) {
-    const double Qm = (i % 2 == 0) ? -1.0 / (double)(i * i - 1) : 0.0;
-    tot += ((i == 0 || i == R - 1) ? 0.5 : 1.0) * ft[i] * Qm;
-  }
-  return fac * tot;
-}
-
-// tprev: the temperature the last nonlinear pass saw (the module grid `tt`
-// that src/output.F90:211 multiplies with the current u_r); the azimuthal
-// mean of the product of two dealiased lines is Re X0 Re Y0 + 2 sum Re(X_m
-// conj Y_m).  NULL uses the current temperature.
-void diagnostics_host(const falcon_params& p, double time, const double* t, const double* w,
-                      const double* up, const double* ur, const double* tprev, falcon_diag* out) {
-  const int R = p.nr_max, M = p.nm_max + 1;
-  Cheb c = make_cheb(R, p.eta);
-  const double pi = 4.0 * std::atan(1.0);
-  std::vector<double> ur2(R), up2(R), upb2(R), w2(R), urt(R, 0.0);
-  for (int j = 0; j < R; ++j) {
-    double a = 0.0, b = 0.0, ww = 0.0;
-    for (int m = 0; m < M; ++m) {
-      const double* u = &ur[2 * ((size_t)m + (size_t)M * j)];
-      const double* v = &up[2 * ((size_t)m + (size_t)M * j)];
-      const double* o = &w[2 * ((size_t)m + (size_t)M * j)];
-      a += u[0] * u[0] + u[1] * u[1];
-      b += v[0] * v[0] + v[1] * v[1];
-      if (m == 0) ww += o[0] * o[0] - o[1] * o[1];
-      else ww += 2.0 * (o[0] * o[0] + o[1] * o[1]);
-    }
-    ur2[j] = a; up2[j] = b; w2[j] = ww;
-    const double upavg = up[2 * ((size_t)M * j)];
-    upb2[j] = upavg * upavg;
-    const double* tp = tprev ? tprev : t;
-    double acc = ur[2 * ((size_t)M * j)] * tp[2 * ((size_t)M * j)];
-    for (int m = 1; m < M; ++m) {
-      const double* u = &ur[2 * ((size_t)m + (size_t)M * j)];
-      const double* q = &tp[2 * ((size_t)m + (size_t)M * j)];
-      acc += 2.0 * (u[0] * q[0] + u[1] * q[1]);
-    }
-    urt[j] = acc;
-  }
-  const double urk = radint(c, ur2), upk = radint(c, up2), upbk = radint(c, upb2);
-  out->time = time;
-  out->dt = p.dt;
-  out->ke = 2.0 * pi * (urk + upk);
-  out->ke_r = 2.0 * pi * urk;
-  out->ke_phi = 2.0 * pi * upk;
-  out->ke_upbar = 2.0 * pi * upbk;
-  // Nusselt from dT0/dr at the walls (src/output.F90:259-265)
-  std::vector<double> d1p, lp;
-  phys_deriv(c, d1p, lp);
-  double d0 = 0.0, dR = 0.0;
-  for (int k = 0; k < R; ++k) {
-    const double T0 = t[2 * ((size_t)M * k)];
-    d0 += d1p[0 + (size_t)R * k] * T0;
-    dR += d1p[R - 1 + (size_t)R * k] * T0;
-  }
-  const double eta = p.eta;
-  out->nu_bot = d0 / ((1.0 - eta) / (eta * std::log(eta)));
-  out->nu_top = dR / ((1.0 - eta) / (std::log(eta)));
-  const double vis1 = radint(c, w2);
-  if (p.mbc == 1) out->vis = 2.0 * pi * vis1 - (4.0 * pi * 2.0 * up2[R - 1] - 4.0 * pi * 2.0 * up2[0]);
-  else out->vis = 2.0 * pi * vis1;
-  out->buo = 2.0 * pi * p.ra / p.pr * radint(c, urt);
 }
 
 }  // namespace
@@ -1621,32 +1596,22 @@ int falcon_batch_step(falcon_batch* b, int nsteps) {
 
 int falcon_batch_diagnostics(falcon_batch* b, falcon_diag* out) {
   if (!b || !out) return fail(FALCON_EINVAL, "null argument");
-  CK(cudaStreamSynchronize(b->stream));
-  for (size_t i = 0; i < b->params.size(); ++i) {
-    const falcon_params& p = b->params[i];
-    const size_t n = (size_t)2 * (p.nm_max + 1) * p.nr_max;
-    std::vector<double> t(n), w(n), up(n), ur(n);
-    int rc = falcon_batch_get_state(b, (int)i, t.data(), w.data(), up.data(), ur.data(), nullptr);
+  for (auto& g : b->groups) {
+    int rc = group_diagnostics(g.get());
     if (rc) return rc;
-    for (double v : t)
-      if (!std::isfinite(v)) return fail(FALCON_ENONFINITE, "non-finite temperature in instance " + std::to_string(i));
-    Group* g = b->groups[b->where[i].first].get();
-    std::vector<double> tp(n);
-    {
-      const double2* src = nullptr;
-      if (g->p.scheme_type == FALCON_IMEX) src = (g->n_step > 0) ? g->th[(g->head + 1) % g->sch.n_imp] : g->T();
-      else src = g->t_grid;
-      const int R = g->R, M = g->M;
-      double2* d = nullptr;
-      CK(cudaMalloc(&d, sizeof(double2) * (size_t)R * M));
-      CK(launch_gather_instance(R, M, g->B, b->where[i].second, src, d, g->stream));
-      CK(cudaStreamSynchronize(g->stream));
-      CK(cudaMemcpy(tp.data(), d, sizeof(double2) * (size_t)R * M, cudaMemcpyDeviceToHost));
-      cudaFree(d);
-    }
-    diagnostics_host(p, g->tot_time, t.data(), w.data(), up.data(), ur.data(), tp.data(), &out[i]);
   }
-  return 0;
+  int status = 0;
+  for (size_t i = 0; i < b->params.size(); ++i) {
+    const Group* g = b->groups[b->where[i].first].get();
+    fill_diag(g, b->where[i].second, g->tot_time, &out[i]);
+    if (!std::isfinite(out[i].ke) || !std::isfinite(out[i].nu_top) || !std::isfinite(out[i].nu_bot)) {
+      status = fail(FALCON_ENONFINITE, "non-finite state in instance " + std::to_string(i));
+    } else if (out[i].ke > 1e10 && status == 0) {
+      // the reference stops the run here (src/output.F90:321-323)
+      status = fail(FALCON_EBLOWUP, "kinetic energy above 1e10 in instance " + std::to_string(i));
+    }
+  }
+  return status;
 }
 
 int falcon_create(const falcon_params* p, falcon_handle** out) {
@@ -1999,6 +1964,7 @@ int falcon_server_iterate(falcon_server* s, int* n_active, int* n_queued) {
     ServerGroup& sg = kv.second;
     if (!sg.g) continue;
     bool changed = false;
+    sg.g->diag_host.clear();
     for (size_t j = 0; j < sg.ids.size(); ++j) {
       ServerRequest& r = s->reqs[sg.ids[j]];
       if (r.state != 1) continue;
@@ -2006,9 +1972,12 @@ int falcon_server_iterate(falcon_server* s, int* n_active, int* n_queued) {
       if (r.steps >= r.horizon) {
         const size_t n = (size_t)2 * (r.p.nm_max + 1) * r.p.nr_max;
         std::vector<double> t(n), w(n), up(n), ur(n);
-        int rc = group_get_instance(sg.g.get(), (int)j, t.data(), w.data(), up.data(), ur.data(), nullptr);
+        int rc = group_get_instance(sg.g.get(), (int)j, t.data(), nullptr, nullptr, nullptr, nullptr);
         if (rc) return rc;
-        diagnostics_host(r.p, r.steps * r.p.dt, t.data(), w.data(), up.data(), ur.data(), nullptr, &r.diag);
+        if (sg.g->diag_host.size() != (size_t)8 * sg.g->B) {
+          if ((rc = group_diagnostics(sg.g.get()))) return rc;
+        }
+        fill_diag(sg.g.get(), (int)j, r.steps * r.p.dt, &r.diag);
         r.tfr = std::move(t);
         r.state = 2;
         s->active--;

@@ -168,6 +168,15 @@ struct StageArgs {
   double2 *fat_out, *fdt_out, *faw_out, *fdw_out, *buo_out;
 };
 
+// Diagnostics of every instance of a group (writeKE_spectral).
+struct DiagArgs {
+  int R, M, B, mbc_sf;
+  const double2 *t, *w, *up, *ur, *tprev;
+  const double *wq, *d1_0, *d1_R, *ra_pr;
+  double nu_top_den, nu_bot_den, pi;
+  double* out;  // 8 per instance
+};
+
 // ---- launchers (falcon_kernels.cu) ----
 cudaError_t launch_nonlin(const NonlinArgs& a, cudaStream_t s);
 cudaError_t launch_gemm(const GemmArgs& g, cudaStream_t s);
@@ -199,6 +208,7 @@ cudaError_t launch_remap_cols(const double* src, double* dst, size_t rows, int b
                               cudaStream_t s);
 // Column b of a [rows][B] array: dst = src (or zero when src is null).
 cudaError_t launch_col_op(const double* src, double* dst, size_t rows, int B, int b, int ew, cudaStream_t s);
+cudaError_t launch_diagnostics(const DiagArgs& a, cudaStream_t s);
 // Self-timed FP64 FMA throughput kernel (returns GFLOP/s, or < 0 on error).
 double measure_fp64_peak();
 // Same for the FP64 tensor-core MMA (mma.sync m8n8k4 f64).

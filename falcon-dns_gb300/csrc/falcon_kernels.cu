@@ -1173,3 +1173,83 @@ extern "C" int falcon_nonlin_noalloc_dev(int nr, int nm, int nb, const double* t
   if (e != cudaSuccess) { set_error_message(cudaGetErrorString(e)); return -2; }
   return 0;
 }
+
+namespace falcon {
+
+// writeKE_spectral (src/output.F90:122-324) for every instance of a group,
+// one block per instance.  wq[r] is the radInt functional (src/integ.F90:
+// 36-76) written as weights on the values: radInt(f) = sum_r wq[r] f(r).
+// d1_0 / d1_R are rows 0 and R-1 of the physical d/dr matrix (Nusselt from
+// dT0/dr at the walls, src/output.F90:259-263).  tprev is the temperature of
+// the last nonlinear pass, which the reference multiplies with the current
+// u_r for the buoyancy power (src/output.F90:211, :302).  Output per
+// instance (8 doubles): ke, ke_r, ke_phi, ke_upbar, nu_top, nu_bot, vis, buo.
+__global__ void diagnostics_kernel(DiagArgs a) {
+  const int b = blockIdx.x;
+  const int R = a.R, M = a.M, B = a.B;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  __shared__ double part[32][9];
+  double k_r = 0.0, k_p = 0.0, k_b = 0.0, vw = 0.0, bu = 0.0, d0 = 0.0, dR = 0.0, s_in = 0.0, s_out = 0.0;
+  for (int r = warp; r < R; r += nw) {
+    double ur2 = 0.0, up2 = 0.0, w2 = 0.0, urt = 0.0;
+    for (int m = lane; m < M; m += 32) {
+      const size_t e = ((size_t)r * M + m) * B + b;
+      const double2 u = a.ur[e], v = a.up[e], o = a.w[e], tp = a.tprev[e];
+      ur2 += u.x * u.x + u.y * u.y;
+      up2 += v.x * v.x + v.y * v.y;
+      if (m == 0) {
+        w2 += o.x * o.x - o.y * o.y;
+        urt += u.x * tp.x;
+      } else {
+        w2 += 2.0 * (o.x * o.x + o.y * o.y);
+        urt += 2.0 * (u.x * tp.x + u.y * tp.y);
+      }
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      ur2 += __shfl_xor_sync(0xffffffffu, ur2, off);
+      up2 += __shfl_xor_sync(0xffffffffu, up2, off);
+      w2 += __shfl_xor_sync(0xffffffffu, w2, off);
+      urt += __shfl_xor_sync(0xffffffffu, urt, off);
+    }
+    const double q = a.wq[r];
+    const size_t e0 = ((size_t)r * M) * B + b;
+    const double u0 = a.up[e0].x, t0 = a.t[e0].x;
+    k_r += q * ur2;
+    k_p += q * up2;
+    k_b += q * u0 * u0;
+    vw += q * w2;
+    bu += q * urt;
+    d0 += a.d1_0[r] * t0;
+    dR += a.d1_R[r] * t0;
+    if (r == 0) s_in = up2;
+    if (r == R - 1) s_out = up2;
+  }
+  if (lane == 0) {
+    part[warp][0] = k_r; part[warp][1] = k_p; part[warp][2] = k_b; part[warp][3] = vw;
+    part[warp][4] = bu; part[warp][5] = d0; part[warp][6] = dR; part[warp][7] = s_in; part[warp][8] = s_out;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (int w = 0; w < nw; ++w)
+      for (int i = 0; i < 9; ++i) t[i] += part[w][i];
+    const double two_pi = 2.0 * a.pi;
+    double* o = a.out + (size_t)b * 8;
+    o[0] = two_pi * (t[0] + t[1]);
+    o[1] = two_pi * t[0];
+    o[2] = two_pi * t[1];
+    o[3] = two_pi * t[2];
+    o[4] = t[6] / a.nu_top_den;
+    o[5] = t[5] / a.nu_bot_den;
+    o[6] = two_pi * t[3] - (a.mbc_sf ? (4.0 * a.pi * 2.0 * t[8] - 4.0 * a.pi * 2.0 * t[7]) : 0.0);
+    o[7] = two_pi * a.ra_pr[b] * t[4];
+  }
+}
+
+cudaError_t launch_diagnostics(const DiagArgs& a, cudaStream_t s) {
+  diagnostics_kernel<<<a.B, 256, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+}  // namespace falcon
