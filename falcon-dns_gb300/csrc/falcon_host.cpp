@@ -175,9 +175,10 @@ Cheb make_cheb(int R, double eta) {
 struct OpKey {
   int R, Nm, mbc, type, imp, exp;
   double dt, pr, eta, wt;
+  int needs_lap, lagpts;
   bool operator<(const OpKey& o) const {
-    return std::tie(R, Nm, mbc, type, imp, exp, dt, pr, eta, wt) <
-           std::tie(o.R, o.Nm, o.mbc, o.type, o.imp, o.exp, o.dt, o.pr, o.eta, o.wt);
+    return std::tie(R, Nm, mbc, type, imp, exp, dt, pr, eta, wt, needs_lap, lagpts) <
+           std::tie(o.R, o.Nm, o.mbc, o.type, o.imp, o.exp, o.dt, o.pr, o.eta, o.wt, o.needs_lap, o.lagpts);
   }
 };
 
@@ -189,7 +190,8 @@ struct OpSet {
   double* Lp = nullptr;    // R x R physical d2/dr2 + r^-1 d/dr
   double* ST = nullptr;    // M blocks of R x R: chebinvtran o AT_m^-1
   double* G = nullptr;     // M blocks of 3R x R: [Tinv X_w; Tinv X_psi; -D1inv X_psi]
-  double* U = nullptr;     // 2R x R: [Tinv A_u^-1; D1inv A_u^-1]
+  double* U = nullptr;      // 2R x R: [Tinv A_u^-1; D1inv A_u^-1]
+  double* LAP = nullptr;    // M blocks of (2R+2) x R: [Tinv; -D1inv; wall omega rows] o LAPpsi_m^-1
   double* inv_r = nullptr;
   double* inv_r2 = nullptr;
   double* wq = nullptr;     // radInt weights (src/integ.F90:36-76) on values
@@ -197,7 +199,7 @@ struct OpSet {
   double* d1_R = nullptr;
   size_t bytes = 0;
   ~OpSet() {
-    cudaFree(D1p); cudaFree(Lp); cudaFree(ST); cudaFree(G); cudaFree(U);
+    cudaFree(D1p); cudaFree(Lp); cudaFree(ST); cudaFree(G); cudaFree(U); cudaFree(LAP);
     cudaFree(inv_r); cudaFree(inv_r2); cudaFree(wq); cudaFree(d1_0); cudaFree(d1_R);
   }
 };
@@ -321,6 +323,87 @@ void apply_inv(const Cheb& c, const double* coef, double* val, double* dval) {
   }
 }
 
+// dlagrange / d2lagrange (src/chebyshev_fftw.F90:449-517): derivatives at x
+// of the Lagrange basis on the points xp.
+void dlagrange(int n, const double* xp, double x, double* dw) {
+  std::vector<double> w(n, 1.0), ww(n, 0.0);
+  for (int i = 0; i < n; ++i) dw[i] = 0.0;
+  for (int j = 0; j < n; ++j)
+    for (int i = 0; i < n; ++i) {
+      w[i] = 1.0;
+      if (i != j) {
+        for (int m = 0; m < n; ++m)
+          if (m != i && m != j) w[i] = w[i] * (x - xp[m]) / (xp[j] - xp[m]);
+        ww[i] = w[i] / (xp[j] - xp[i]);
+        dw[j] = dw[j] + ww[i];
+      }
+    }
+}
+
+void d2lagrange(int n, const double* xp, double x, double* d2w) {
+  std::vector<double> w(n, 1.0), ww(n, 0.0), mw(n, 0.0);
+  for (int i = 0; i < n; ++i) d2w[i] = 0.0;
+  for (int j = 0; j < n; ++j)
+    for (int i = 0; i < n; ++i)
+      if (i != j) {
+        mw[i] = 0.0;
+        for (int m = 0; m < n; ++m)
+          if (m != i && m != j) {
+            w[i] = 1.0;
+            for (int l = 0; l < n; ++l)
+              if (l != j && l != i && l != m) w[i] = w[i] * (x - xp[l]) / (xp[j] - xp[l]);
+            ww[i] = w[i] / (xp[j] - xp[m]);
+            mw[i] = mw[i] + ww[i];
+          }
+        d2w[j] = d2w[j] + mw[i] / (xp[j] - xp[i]);
+      }
+}
+
+// mat_build_rk (src/mat_assembly.F90:415-462): the psi Poisson operator with
+// psi = 0 boundary rows, end columns halved, times C.
+void assemble_lap(const Cheb& c, int n, std::vector<double>& L) {
+  const int R = c.R;
+  const double C = std::pow(2.0 / (double)(R - 1), 0.5);
+  const double nn = (double)n * (double)n;
+  L.assign((size_t)R * R, 0.0);
+  for (int j = 0; j < R; ++j) {
+    for (int i = 0; i < R; ++i)
+      L[i + (size_t)R * j] = c.inv_r[i] * c.D[i + (size_t)R * j] + c.D2[i + (size_t)R * j] -
+                             nn * c.inv_r2[i] * c.t[i + (size_t)R * j];
+    L[0 + (size_t)R * j] = 1.0 * c.t[0 + (size_t)R * j];
+    L[R - 1 + (size_t)R * j] = 1.0 * c.t[R - 1 + (size_t)R * j];
+  }
+  for (int i = 0; i < R; ++i) { L[i] *= 0.5; L[i + (size_t)R * (R - 1)] *= 0.5; }
+  for (auto& v : L) v = 1.0 * C * v;
+}
+
+// Wall vorticity of the Johnston strategy (src/fourierloop_imexrk.F90:
+// 586-637) as weights on the physical psi values: omega(wall) = sum_i
+// win[i] psi(i), over the lm interior points next to each wall.
+void johnston_weights(const Cheb& c, int lagpts, int mbc, std::vector<double>& win, std::vector<double>& wout) {
+  const int R = c.R;
+  int lm = std::min(lagpts, R - 2);
+  if (lm < 1) lm = 1;
+  std::vector<double> pts(lm), dwmin(lm), d2wmin(lm), dwmax(lm), d2wmax(lm);
+  for (int i = 0; i < lm; ++i) pts[i] = c.radius[1 + i];
+  dlagrange(lm, pts.data(), c.rmin, dwmin.data());
+  d2lagrange(lm, pts.data(), c.rmin, d2wmin.data());
+  for (int i = 0; i < lm; ++i) pts[i] = c.radius[R - 2 - i];
+  dlagrange(lm, pts.data(), c.rmax, dwmax.data());
+  d2lagrange(lm, pts.data(), c.rmax, d2wmax.data());
+  win.assign(R, 0.0);
+  wout.assign(R, 0.0);
+  for (int i = 0; i < lm; ++i) {
+    if (mbc == 0) {
+      win[1 + i] += -1.0 * (d2wmin[i] - 2.0 * dwmin[0] * dwmin[i]);
+      wout[R - 2 - i] += -1.0 * (d2wmax[i] - 2.0 * dwmax[0] * dwmax[i]);
+    } else {
+      win[1 + i] += -2.0 / c.radius[0] * dwmin[i];
+      wout[R - 2 - i] += -2.0 / c.radius[R - 1] * dwmax[i];
+    }
+  }
+}
+
 template <class T>
 int upload(T** dst, const std::vector<T>& v, size_t* acc) {
   CK(cudaMalloc(dst, sizeof(T) * v.size()));
@@ -379,6 +462,39 @@ int build_opset(const OpKey& k, std::shared_ptr<OpSet>* out) {
     }
   });
   if (bad) return fail(FALCON_ESINGULAR, "dgetrf: singular operator for mode " + std::to_string(bad - 1));
+  std::vector<double> LAP;
+  if (k.needs_lap) {
+    std::vector<double> win, wout;
+    johnston_weights(c, k.lagpts, k.mbc, win, wout);
+    const int rows = 2 * R + 2;
+    LAP.assign((size_t)M * rows * R, 0.0);
+    parallel_for(M, [&](int m) {
+      if (m == 0) return;
+      std::vector<double> L;
+      assemble_lap(c, m, L);
+      std::vector<int> pv(R);
+      if (host_dgetrf(R, L.data(), pv.data()) != 0) bad = m + 1;
+      std::vector<double> x(R), v(R), dv(R);
+      double* Lm = &LAP[(size_t)m * rows * R];
+      for (int j = 0; j < R; ++j) {
+        std::fill(x.begin(), x.end(), 0.0);
+        x[j] = 1.0;
+        host_dgetrs(R, L.data(), pv.data(), x.data());
+        apply_inv(c, x.data(), v.data(), dv.data());
+        double oin = 0.0, oout = 0.0;
+        for (int i = 0; i < R; ++i) {
+          Lm[i + (size_t)rows * j] = v[i];
+          Lm[R + i + (size_t)rows * j] = -dv[i];
+          oin += win[i] * v[i];
+          oout += wout[i] * v[i];
+        }
+        Lm[2 * R + (size_t)rows * j] = oin;
+        Lm[2 * R + 1 + (size_t)rows * j] = oout;
+      }
+    });
+    if (bad) return fail(FALCON_ESINGULAR, "dgetrf: singular psi Poisson operator for mode " + std::to_string(bad - 1));
+  }
+
   {
     std::vector<double> Au;
     assemble_Au(c, k.mbc, k.dt, k.wt, Au);
@@ -402,6 +518,7 @@ int build_opset(const OpKey& k, std::shared_ptr<OpSet>* out) {
   if ((rc = upload(&ops->ST, ST, &ops->bytes))) return rc;
   if ((rc = upload(&ops->G, G, &ops->bytes))) return rc;
   if ((rc = upload(&ops->U, U, &ops->bytes))) return rc;
+  if (!LAP.empty() && (rc = upload(&ops->LAP, LAP, &ops->bytes))) return rc;
   if ((rc = upload(&ops->inv_r, c.inv_r, &ops->bytes))) return rc;
   if ((rc = upload(&ops->inv_r2, c.inv_r2, &ops->bytes))) return rc;
   {
@@ -678,6 +795,8 @@ OpKey key_of(const falcon_params& p, const Scheme& s) {
   k.R = p.nr_max; k.Nm = p.nm_max; k.mbc = p.mbc; k.type = p.scheme_type;
   k.imp = p.scheme_imp; k.exp = p.scheme_exp; k.dt = p.dt; k.pr = p.pr; k.eta = p.eta;
   k.wt = (p.scheme_type == FALCON_IMEX) ? s.wt_lhs : s.aD[s.diag][s.diag];
+  k.needs_lap = (p.scheme_type == FALCON_IMEXRK && !(s.check_A && s.check_D)) ? 1 : 0;
+  k.lagpts = k.needs_lap ? p.lagpts : 0;
   return k;
 }
 
@@ -694,8 +813,6 @@ int validate(const falcon_params& p) {
   Scheme s;
   if (scheme_weights(p.scheme_type, p.scheme_imp, p.scheme_exp, &s) != 0)
     return fail(FALCON_EINVAL, "unsupported time scheme combination");
-  if (p.scheme_type == FALCON_IMEXRK && !(s.check_A && s.check_D))
-    return fail(FALCON_EINVAL, "IMEXRK schemes that are not stiffly accurate (e.g. ARS343) are not supported yet");
   return 0;
 }
 
@@ -959,10 +1076,46 @@ int step_imexrk(Group* g) {
     a.buo_out = (st == 0) ? g->buo[0] : nullptr;
     if ((rc = elementwise(g, 20.0, [&]() { return launch_stage_deriv(a, s); }))) return rc;
   }
-  // Assembly_stage_SA (src/fourierloop_imexrk.F90:653-665)
-  CK(cudaMemcpyAsync(g->t0, g->T(), sizeof(double2) * n, cudaMemcpyDeviceToDevice, s));
-  CK(cudaMemcpyAsync(g->w0, g->W(), sizeof(double2) * n, cudaMemcpyDeviceToDevice, s));
-  if ((rc = launch(g, KC_ELEMENTWISE, 0.0, [&]() { return launch_extract_mode0(R, M, B, g->up, g->u0, s); }))) return rc;
+  if (sa) {
+    // Assembly_stage_SA (src/fourierloop_imexrk.F90:653-665)
+    CK(cudaMemcpyAsync(g->t0, g->T(), sizeof(double2) * n, cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(g->w0, g->W(), sizeof(double2) * n, cudaMemcpyDeviceToDevice, s));
+    if ((rc = launch(g, KC_ELEMENTWISE, 0.0, [&]() { return launch_extract_mode0(R, M, B, g->up, g->u0, s); }))) return rc;
+  } else {
+    // Assembly_stage (src/fourierloop_imexrk.F90:499-651)
+    AsmArgs q{};
+    q.R = R; q.M = M; q.B = B; q.ns = ns; q.dt = g->p.dt;
+    for (int i = 0; i < ns; ++i) {
+      q.bA[i] = sc.bA[i]; q.bD[i] = sc.bD[i];
+      q.fat[i] = g->fat[i]; q.fdt[i] = g->fdt[i]; q.faw[i] = g->faw[i]; q.fdw[i] = g->fdw[i]; q.buo[i] = g->buo[i];
+    }
+    q.t0 = g->t0; q.w0 = g->w0; q.rhs_w = g->rhs_w; q.u0 = g->u0;
+    if ((rc = elementwise(g, 8.0 * ns + 6.0, [&]() { return launch_assembly(q, s); }))) return rc;
+    if (M > 1) {
+      const int rows = 2 * R + 2;
+      const long sL = (long)rows * R;
+      double2* psi_tmp = g->rhs_t;  // the reference leaves psii at its last-stage value
+      if ((rc = gemm(g, KC_GEMM_MODE, per_mode(o->LAP, rows, sL, g->rhs_w, psi_tmp, R, M, B, 1, M - 1, R))) ||
+          (rc = gemm(g, KC_GEMM_MODE, per_mode(o->LAP + R, rows, sL, g->rhs_w, g->up, R, M, B, 1, M - 1, R))) ||
+          (rc = gemm(g, KC_GEMM_MODE, per_mode(o->LAP + 2 * R, rows, sL, g->rhs_w, g->w0, R, M, B, 1, M - 1, 1))) ||
+          (rc = gemm(g, KC_GEMM_MODE, per_mode(o->LAP + 2 * R + 1, rows, sL, g->rhs_w, g->w0 + (size_t)(R - 1) * M * B,
+                                               R, M, B, 1, M - 1, 1))))
+        return rc;
+    }
+    GemmArgs gd{};
+    gd.A = o->D1p; gd.lda = R;
+    gd.X = g->u0; gd.ldx = B;
+    gd.Y = reinterpret_cast<double*>(g->lu0); gd.ldy = B;
+    gd.K = R; gd.rows = R; gd.N = B; gd.batch = 1; gd.alpha = 1.0;
+    if ((rc = gemm(g, KC_GEMM_RADIAL, gd))) return rc;
+    if ((rc = elementwise(g, 3.0, [&]() {
+           return launch_assembly_post(R, M, B, o->inv_r, g->rhs_t, g->u0, reinterpret_cast<const double*>(g->lu0),
+                                       g->ur, g->up, g->w0, s);
+         })))
+      return rc;
+    CK(cudaMemcpyAsync(g->T(), g->t0, sizeof(double2) * n, cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(g->W(), g->w0, sizeof(double2) * n, cudaMemcpyDeviceToDevice, s));
+  }
   g->n_step = nstep;
   g->tot_time += g->p.dt;
   return 0;

@@ -177,6 +177,18 @@ struct DiagArgs {
   double* out;  // 8 per instance
 };
 
+// Non-stiffly-accurate IMEXRK assembly (elementwise part).
+struct AsmArgs {
+  int R, M, B, ns;
+  double dt;
+  double bA[kMaxStages], bD[kMaxStages];
+  const double2* fat[kMaxStages]; const double2* fdt[kMaxStages];
+  const double2* faw[kMaxStages]; const double2* fdw[kMaxStages];
+  const double2* buo[kMaxStages];
+  double2 *t0, *w0, *rhs_w;
+  double* u0;
+};
+
 // ---- launchers (falcon_kernels.cu) ----
 cudaError_t launch_nonlin(const NonlinArgs& a, cudaStream_t s);
 cudaError_t launch_gemm(const GemmArgs& g, cudaStream_t s);
@@ -209,6 +221,9 @@ cudaError_t launch_remap_cols(const double* src, double* dst, size_t rows, int b
 // Column b of a [rows][B] array: dst = src (or zero when src is null).
 cudaError_t launch_col_op(const double* src, double* dst, size_t rows, int B, int b, int ew, cudaStream_t s);
 cudaError_t launch_diagnostics(const DiagArgs& a, cudaStream_t s);
+cudaError_t launch_assembly(const AsmArgs& a, cudaStream_t s);
+cudaError_t launch_assembly_post(int R, int M, int B, const double* inv_r, const double2* psi, const double* u0,
+                                 const double* du0, double2* ur, double2* up, double2* w0, cudaStream_t s);
 // Self-timed FP64 FMA throughput kernel (returns GFLOP/s, or < 0 on error).
 double measure_fp64_peak();
 // Same for the FP64 tensor-core MMA (mma.sync m8n8k4 f64).

@@ -1253,3 +1253,100 @@ cudaError_t launch_diagnostics(const DiagArgs& a, cudaStream_t s) {
 }
 
 }  // namespace falcon
+
+namespace falcon {
+
+// Assembly_stage for schemes that are not stiffly accurate
+// (src/fourierloop_imexrk.F90:499-651), elementwise part: y_n = y_0 +
+// dt sum_i (bA_i F_a(i) + bD_i F_d(i)) for T, uphi_bar (m = 0) and the
+// interior vorticity (m >= 1, with the buoyancy under bD), then the psi
+// Poisson right-hand side -omega (zero boundary rows) into rhs_w.
+__global__ void assembly_kernel(AsmArgs a) {
+  const size_t total = (size_t)a.R * a.M * a.B;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+    const int b = (int)(e % a.B);
+    const size_t rm = e / a.B;
+    const int m = (int)(rm % a.M);
+    const int r = (int)(rm / a.M);
+    double2 f = make_double2(0.0, 0.0);
+    for (int i = 0; i < a.ns; ++i) {
+      const double2 qa = a.fat[i][e], qd = a.fdt[i][e];
+      f.x = f.x + a.bA[i] * qa.x + a.bD[i] * qd.x;
+      f.y = f.y + a.bA[i] * qa.y + a.bD[i] * qd.y;
+    }
+    double2 t = a.t0[e];
+    t.x = t.x + a.dt * f.x;
+    t.y = t.y + a.dt * f.y;
+    if (r == 0) t = make_double2(m == 0 ? 1.0 : 0.0, 0.0);
+    if (r == a.R - 1) t = make_double2(0.0, 0.0);
+    a.t0[e] = t;
+    if (m == 0) {
+      double fu = 0.0;
+      for (int i = 0; i < a.ns; ++i) fu = fu + a.bA[i] * a.faw[i][e].x + a.bD[i] * a.fdw[i][e].x;
+      const size_t rb = (size_t)r * a.B + b;
+      double u = a.u0[rb] + a.dt * fu;
+      if (r == 0 || r == a.R - 1) u = 0.0;
+      a.u0[rb] = u;
+      a.rhs_w[e] = make_double2(0.0, 0.0);
+    } else {
+      double2 w = a.w0[e];
+      if (r > 0 && r < a.R - 1) {
+        double2 g = make_double2(0.0, 0.0);
+        for (int i = 0; i < a.ns; ++i) {
+          const double2 qa = a.faw[i][e], qd = a.fdw[i][e], qb = a.buo[i][e];
+          g.x = g.x + a.bA[i] * qa.x + a.bD[i] * qd.x + a.bD[i] * qb.x;
+          g.y = g.y + a.bA[i] * qa.y + a.bD[i] * qd.y + a.bD[i] * qb.y;
+        }
+        w.x = w.x + a.dt * g.x;
+        w.y = w.y + a.dt * g.y;
+        a.w0[e] = w;
+        a.rhs_w[e] = make_double2(-1.0 * w.x, -1.0 * w.y);
+      } else {
+        a.rhs_w[e] = make_double2(0.0, 0.0);
+      }
+    }
+  }
+}
+
+// After the psi solve: u_r = i m psi/r (m >= 1); mode 0: omega = ubar/r +
+// d ubar/dr, u_phi = ubar, u_r = 0 (src/fourierloop_imexrk.F90:556-572).
+__global__ void assembly_post_kernel(int R, int M, int B, const double* inv_r, const double2* psi,
+                                     const double* u0, const double* du0, double2* ur, double2* up, double2* w0) {
+  const size_t total = (size_t)R * M * B;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+    const int b = (int)(e % B);
+    const size_t rm = e / B;
+    const int m = (int)(rm % M);
+    const int r = (int)(rm / M);
+    if (m > 0) {
+      const double2 ps = psi[e];
+      const double f = 1.0 * (double)m * inv_r[r];
+      ur[e] = make_double2(-f * ps.y, f * ps.x);
+    } else {
+      const size_t rb = (size_t)r * B + b;
+      const double u = u0[rb];
+      up[e] = make_double2(u, 0.0);
+      ur[e] = make_double2(0.0, 0.0);
+      w0[e] = make_double2(u * inv_r[r] + du0[rb], 0.0);
+    }
+  }
+}
+
+cudaError_t launch_assembly(const AsmArgs& a, cudaStream_t s) {
+  size_t n = (size_t)a.R * a.M * a.B;
+  size_t g = (n + 255) / 256;
+  if (g > 152 * 32) g = 152 * 32;
+  assembly_kernel<<<(int)(g ? g : 1), 256, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_assembly_post(int R, int M, int B, const double* inv_r, const double2* psi, const double* u0,
+                                 const double* du0, double2* ur, double2* up, double2* w0, cudaStream_t s) {
+  size_t n = (size_t)R * M * B;
+  size_t g = (n + 255) / 256;
+  if (g > 152 * 32) g = 152 * 32;
+  assembly_post_kernel<<<(int)(g ? g : 1), 256, 0, s>>>(R, M, B, inv_r, psi, u0, du0, ur, up, w0);
+  return cudaGetLastError();
+}
+
+}  // namespace falcon

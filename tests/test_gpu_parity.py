@@ -118,6 +118,7 @@ def compare_run(orc, fg, scheme, R, Nm, ra, dt, nsteps, seed=1, mbc="NS", pr=1.0
     ("SBDF2", 17, 8, 1e4, 1e-4),
     ("SBDF4", 17, 8, 1e4, 1e-4),
     ("ARS222", 17, 8, 1e4, 1e-4),
+    ("ARS343", 33, 42, 1e5, 1e-5),     # not stiffly accurate: psi Poisson + Johnston walls
 ])
 def test_time_step_parity_after_100_steps(orc, fg, scheme, R, Nm, ra, dt):
     errs, _, _ = compare_run(orc, fg, scheme, R, Nm, ra, dt, 100)
@@ -126,6 +127,11 @@ def test_time_step_parity_after_100_steps(orc, fg, scheme, R, Nm, ra, dt):
 
 def test_stress_free_boundaries(orc, fg):
     errs, _, _ = compare_run(orc, fg, "CNAB2", 17, 10, 1e4, 1e-4, 100, mbc="SF")
+    assert max(errs.values()) < STEP_TOL, errs
+
+
+def test_stress_free_non_sa_imexrk(orc, fg):
+    errs, _, _ = compare_run(orc, fg, "ARS343", 17, 10, 1e4, 1e-4, 100, mbc="SF")
     assert max(errs.values()) < STEP_TOL, errs
 
 
