@@ -48,20 +48,19 @@ def build(force=False, verbose=False):
         return LIB
     os.makedirs(OUT, exist_ok=True)
     home, nvcc = _cuda_home()
-    kern_o = os.path.join(OUT, "falcon_kernels.o")
+    cu_srcs = sorted(f for f in os.listdir(SRC) if f.endswith(".cu"))
+    objs = [os.path.join(OUT, f[:-3] + ".o") for f in cu_srcs]
     host_o = os.path.join(OUT, "falcon_host.o")
-    cmds = [
-        [nvcc] + ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xptxas", "-v",
-                         "-c", os.path.join(SRC, "falcon_kernels.cu"), "-o", kern_o],
-        ["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-pthread",
-         "-I" + os.path.join(home, "include"), "-c", os.path.join(SRC, "falcon_host.cpp"), "-o", host_o],
-    ]
-    with ThreadPoolExecutor(2) as ex:
+    cmds = [[nvcc] + ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xptxas", "-v",
+                             "-c", os.path.join(SRC, f), "-o", o] for f, o in zip(cu_srcs, objs)]
+    cmds.append(["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-pthread",
+                 "-I" + os.path.join(home, "include"), "-c", os.path.join(SRC, "falcon_host.cpp"), "-o", host_o])
+    with ThreadPoolExecutor(len(cmds)) as ex:
         logs = list(ex.map(_run, cmds))
     if verbose:
         print(logs[0])
     tmp = LIB + ".tmp"
-    _run([nvcc] + ARCH + ["-shared", "-o", tmp, kern_o, host_o, "-lcudart", "-lpthread"])
+    _run([nvcc] + ARCH + ["-shared", "-o", tmp] + objs + [host_o, "-lcudart", "-lpthread"])
     os.replace(tmp, LIB)
     return LIB
 

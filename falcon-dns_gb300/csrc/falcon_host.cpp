@@ -236,54 +236,6 @@ void phys_deriv(const Cheb& c, std::vector<double>& D1p, std::vector<double>& Lp
     }
 }
 
-// mat_build / mat_build_IRK (src/mat_assembly.F90:68-187, :242-359) for one
-// mode: AT (R x R) and AF (2R x 2R), before factorisation.
-void assemble_AT_AF(const Cheb& c, int mbc, double dt, int n, double wt, double pr, bool irk,
-                    std::vector<double>& AT, std::vector<double>& AF) {
-  const int R = c.R, R2 = 2 * R;
-  const double C = std::pow(2.0 / (double)(R - 1), 0.5);
-  const double nn = (double)n * (double)n;
-  AT.assign((size_t)R * R, 0.0);
-  AF.assign((size_t)R2 * R2, 0.0);
-  auto t = [&](int i, int j) { return c.t[i + (size_t)R * j]; };
-  auto D = [&](int i, int j) { return c.D[i + (size_t)R * j]; };
-  auto D2 = [&](int i, int j) { return c.D2[i + (size_t)R * j]; };
-  auto at = [&](int i, int j) -> double& { return AT[i + (size_t)R * j]; };
-  auto af = [&](int i, int j) -> double& { return AF[i + (size_t)R2 * j]; };
-  auto bcp2 = [&](int side, int j) {
-    const int i = side ? R - 1 : 0;
-    return mbc == 0 ? D(i, j) : D2(i, j) - c.inv_r[i] * D(i, j);
-  };
-  for (int j = 0; j < R; ++j) {
-    for (int i = 0; i < R; ++i)
-      at(i, j) = t(i, j) - wt * dt * (1.0 / pr) * (c.inv_r[i] * D(i, j) + D2(i, j) - nn * c.inv_r2[i] * t(i, j));
-    at(0, j) = t(0, j);
-    at(R - 1, j) = t(R - 1, j);
-  }
-  for (int i = 0; i < R; ++i) { at(i, 0) *= 0.5; at(i, R - 1) *= 0.5; }
-  for (auto& v : AT) v = C * v;
-  for (int j = 0; j < R; ++j) {
-    for (int i = 0; i < R; ++i) {
-      const double L = c.inv_r[i] * D(i, j) + D2(i, j) - nn * c.inv_r2[i] * t(i, j);
-      af(i, j) = L;
-      af(i, R + j) = t(i, j);
-      af(R + i, j) = 0.0;
-      af(R + i, R + j) = t(i, j) - wt * dt * L;
-    }
-    if (irk) { af(0, j) = bcp2(0, j); af(R - 1, j) = bcp2(1, j); }
-    else { af(0, j) = t(0, j); af(R - 1, j) = t(R - 1, j); }
-    af(0, R + j) = 0.0; af(R - 1, R + j) = 0.0;
-    if (irk) { af(R, j) = t(0, j); af(R2 - 1, j) = t(R - 1, j); }
-    else { af(R, j) = bcp2(0, j); af(R2 - 1, j) = bcp2(1, j); }
-    af(R, R + j) = 0.0; af(R2 - 1, R + j) = 0.0;
-  }
-  for (int i = 0; i < R; ++i) {
-    af(i, 0) *= 0.5; af(i, R - 1) *= 0.5; af(i, R) *= 0.5; af(i, R2 - 1) *= 0.5;
-    af(R + i, 0) *= 0.5; af(R + i, R - 1) *= 0.5; af(R + i, R) *= 0.5; af(R + i, R2 - 1) *= 0.5;
-  }
-  for (auto& v : AF) v = C * v;
-}
-
 // mat_build_uphibar(_IRK) (src/mat_assembly.F90:189-240, :361-413)
 void assemble_Au(const Cheb& c, int mbc, double dt, double wt, std::vector<double>& A) {
   const int R = c.R;
@@ -359,24 +311,6 @@ void d2lagrange(int n, const double* xp, double x, double* d2w) {
       }
 }
 
-// mat_build_rk (src/mat_assembly.F90:415-462): the psi Poisson operator with
-// psi = 0 boundary rows, end columns halved, times C.
-void assemble_lap(const Cheb& c, int n, std::vector<double>& L) {
-  const int R = c.R;
-  const double C = std::pow(2.0 / (double)(R - 1), 0.5);
-  const double nn = (double)n * (double)n;
-  L.assign((size_t)R * R, 0.0);
-  for (int j = 0; j < R; ++j) {
-    for (int i = 0; i < R; ++i)
-      L[i + (size_t)R * j] = c.inv_r[i] * c.D[i + (size_t)R * j] + c.D2[i + (size_t)R * j] -
-                             nn * c.inv_r2[i] * c.t[i + (size_t)R * j];
-    L[0 + (size_t)R * j] = 1.0 * c.t[0 + (size_t)R * j];
-    L[R - 1 + (size_t)R * j] = 1.0 * c.t[R - 1 + (size_t)R * j];
-  }
-  for (int i = 0; i < R; ++i) { L[i] *= 0.5; L[i + (size_t)R * (R - 1)] *= 0.5; }
-  for (auto& v : L) v = 1.0 * C * v;
-}
-
 // Wall vorticity of the Johnston strategy (src/fourierloop_imexrk.F90:
 // 586-637) as weights on the physical psi values: omega(wall) = sum_i
 // win[i] psi(i), over the lm interior points next to each wall.
@@ -412,6 +346,134 @@ int upload(T** dst, const std::vector<T>& v, size_t* acc) {
   return 0;
 }
 
+// The per-mode combined operators of one key, built on the device:
+//   ST[m] = chebinvtran o AT_m^-1                          (R x R)
+//   G[m]  = [chebinvtran; chebinvtran; -chebinvtranD1] o the omega, psi and
+//           psi rows of AF_m^-1 on the vorticity right-hand side (3R x R)
+//   LAP[m] = [chebinvtran; -chebinvtranD1; wall omega] o LAPpsi_m^-1
+// Factorisations: batched dgetf2/dgetrs (falcon_ops.cu) on modes in chunks
+// that keep the workspace near 256 MB.  Products: the DFMA GEMM.  G[0] and
+// LAP[0] stay zero (the m = 0 flow is the u_phi_bar equation).
+int build_mode_operators(const OpKey& k, const Cheb& c, OpSet* ops) {
+  const int R = c.R, M = k.Nm + 1;
+  const size_t RR = (size_t)R * R;
+  cudaStream_t s = nullptr;
+  const double C = std::pow(2.0 / (double)(R - 1), 0.5);
+  // chebinvtran / chebinvtranD1 on scaled coefficients as column-major
+  // matrices: Tinv = C t H, D1inv = C D H (negated for u_phi = -dpsi/dr).
+  std::vector<double> tinv(RR), mdinv(RR);
+  for (int j = 0; j < R; ++j) {
+    const double h = (j == 0 || j == R - 1) ? 0.5 : 1.0;
+    for (int i = 0; i < R; ++i) {
+      tinv[i + (size_t)R * j] = C * c.t[i + (size_t)R * j] * h;
+      mdinv[i + (size_t)R * j] = -(C * c.D[i + (size_t)R * j] * h);
+    }
+  }
+  std::vector<double> win, wout, pin(R, 0.0), pout(R, 0.0);
+  if (k.needs_lap) {
+    johnston_weights(c, k.lagpts, k.mbc, win, wout);
+    for (int kk = 0; kk < R; ++kk)
+      for (int i = 0; i < R; ++i) {
+        pin[kk] += win[i] * tinv[i + (size_t)R * kk];
+        pout[kk] += wout[i] * tinv[i + (size_t)R * kk];
+      }
+  }
+  const size_t per_mode = 6 * RR;  // AF (4 RR) + its right-hand sides (2 RR)
+  const int mc = (int)std::max<size_t>(1, std::min<size_t>((size_t)M, ((size_t)256 << 20) / (per_mode * 8)));
+  double *d_t = nullptr, *d_D = nullptr, *d_D2 = nullptr, *d_ir = nullptr, *d_ir2 = nullptr, *d_tinv = nullptr,
+         *d_mdinv = nullptr, *d_pin = nullptr, *d_pout = nullptr, *Wm = nullptr, *Wr = nullptr;
+  int* d_info = nullptr;
+  auto cleanup = [&]() {
+    for (void* q : {(void*)d_t, (void*)d_D, (void*)d_D2, (void*)d_ir, (void*)d_ir2, (void*)d_tinv, (void*)d_mdinv,
+                    (void*)d_pin, (void*)d_pout, (void*)Wm, (void*)Wr, (void*)d_info})
+      cudaFree(q);
+  };
+  int rc = 0;
+  if ((rc = upload(&d_t, c.t, nullptr)) || (rc = upload(&d_D, c.D, nullptr)) || (rc = upload(&d_D2, c.D2, nullptr)) ||
+      (rc = upload(&d_ir, c.inv_r, nullptr)) || (rc = upload(&d_ir2, c.inv_r2, nullptr)) ||
+      (rc = upload(&d_tinv, tinv, nullptr)) || (rc = upload(&d_mdinv, mdinv, nullptr)) ||
+      (rc = upload(&d_pin, pin, nullptr)) || (rc = upload(&d_pout, pout, nullptr))) {
+    cleanup();
+    return rc;
+  }
+  auto dev_alloc = [&](double** q, size_t n) -> int {
+    if (cudaMalloc(q, sizeof(double) * n) != cudaSuccess) return fail(FALCON_ENOMEM, "operator workspace");
+    if (cudaMemset(*q, 0, sizeof(double) * n) != cudaSuccess) return fail(FALCON_ECUDA, "operator workspace");
+    return 0;
+  };
+  const long lap_rows = 2L * R + 2;
+  if ((rc = dev_alloc(&Wm, 4 * RR * mc)) || (rc = dev_alloc(&Wr, 2 * RR * mc)) ||
+      (rc = dev_alloc(&ops->ST, RR * M)) || (rc = dev_alloc(&ops->G, 3 * RR * M)) ||
+      (k.needs_lap && (rc = dev_alloc(&ops->LAP, (size_t)lap_rows * R * M)))) {
+    cleanup();
+    return rc;
+  }
+  ops->bytes += sizeof(double) * 4 * RR * M + (k.needs_lap ? sizeof(double) * lap_rows * R * M : 0);
+  if (cudaMalloc(&d_info, sizeof(int) * mc) != cudaSuccess) { cleanup(); return fail(FALCON_ENOMEM, "info"); }
+  auto ck = [&](cudaError_t e, const char* what) -> int {
+    if (e != cudaSuccess) return fail(FALCON_ECUDA, std::string(what) + ": " + cudaGetErrorString(e));
+    return 0;
+  };
+  auto check_info = [&](int nb, int m_first, const char* what) -> int {
+    std::vector<int> info(nb);
+    const cudaError_t e = cudaMemcpy(info.data(), d_info, sizeof(int) * nb, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return fail(FALCON_ECUDA, std::string("operator build (") + what + "): " + cudaGetErrorString(e));
+    for (int m = 0; m < nb; ++m)
+      if (info[m] != 0)
+        return fail(FALCON_ESINGULAR, std::string("dgetrf: singular ") + what + " for mode " + std::to_string(m_first + m));
+    return 0;
+  };
+  // out (column-major, leading dimension ldy) = P X for each mode, with X the
+  // row-major solutions (stride sA) and P column-major (nrows_p x R).
+  auto prod = [&](const double* Xrm, long sA, const double* Pcm, double* out, long ldy, int nrows_p, int nb) {
+    GemmArgs g{};
+    g.A = Xrm; g.lda = R; g.sA = sA;
+    g.X = Pcm; g.ldx = nrows_p; g.sX = 0;
+    g.Y = out; g.ldy = ldy; g.sY = ldy * R;
+    g.K = R; g.rows = R; g.N = nrows_p; g.batch = nb; g.alpha = 1.0;
+    return launch_gemm(g, s);
+  };
+  const double wdt = k.wt * k.dt;
+  const int irk = (k.type == FALCON_IMEXRK) ? 1 : 0;
+  const long L2 = (long)2 * RR, L3 = (long)3 * RR;
+  for (int m0 = 0; m0 < M && rc == 0; m0 += mc) {
+    const int nm = std::min(mc, M - m0);
+    // temperature: ST[m] = Tinv AT_m^-1
+    if ((rc = ck(launch_assemble(0, R, m0, nm, d_t, d_D, d_D2, d_ir, d_ir2, wdt, 1.0 / k.pr, C, Wm, s), "assemble AT")) ||
+        (rc = ck(launch_unit_rhs(R, R, 0, nm, Wr, s), "unit rhs")) ||
+        (rc = ck(launch_lu_solve(R, nm, Wm, RR, Wr, RR, R, d_info, s), "lu AT")) ||
+        (rc = check_info(nm, m0, "AT")) ||
+        (rc = ck(prod(Wr, (long)RR, d_tinv, ops->ST + (size_t)m0 * RR, R, R, nm), "ST product")))
+      break;
+    const int a0 = std::max(m0, 1), na = m0 + nm - a0;
+    if (na <= 0) continue;
+    // psi-omega: AF_m^-1 on [0; e_j], unknowns [psi; omega]
+    double* Gm = ops->G + (size_t)a0 * L3;
+    if ((rc = ck(launch_assemble_af(R, a0, na, k.mbc, irk, d_t, d_D, d_D2, d_ir, d_ir2, wdt, C, Wm, s), "assemble AF")) ||
+        (rc = ck(launch_unit_rhs(2 * R, R, R, na, Wr, s), "unit rhs")) ||
+        (rc = ck(launch_lu_solve(2 * R, na, Wm, 4 * RR, Wr, L2, R, d_info, s), "lu AF")) ||
+        (rc = check_info(na, a0, "psi-omega operator")) ||
+        (rc = ck(prod(Wr + RR, L2, d_tinv, Gm, 3L * R, R, na), "G omega")) ||
+        (rc = ck(prod(Wr, L2, d_tinv, Gm + R, 3L * R, R, na), "G psi")) ||
+        (rc = ck(prod(Wr, L2, d_mdinv, Gm + 2 * R, 3L * R, R, na), "G uphi")))
+      break;
+    if (!k.needs_lap) continue;
+    double* Lm = ops->LAP + (size_t)a0 * lap_rows * R;
+    if ((rc = ck(launch_assemble(4, R, a0, na, d_t, d_D, d_D2, d_ir, d_ir2, 0.0, 1.0, C, Wm, s), "assemble LAPpsi")) ||
+        (rc = ck(launch_unit_rhs(R, R, 0, na, Wr, s), "unit rhs")) ||
+        (rc = ck(launch_lu_solve(R, na, Wm, RR, Wr, RR, R, d_info, s), "lu LAPpsi")) ||
+        (rc = check_info(na, a0, "psi Poisson operator")) ||
+        (rc = ck(prod(Wr, (long)RR, d_tinv, Lm, lap_rows, R, na), "LAP psi")) ||
+        (rc = ck(prod(Wr, (long)RR, d_mdinv, Lm + R, lap_rows, R, na), "LAP uphi")) ||
+        (rc = ck(prod(Wr, (long)RR, d_pin, Lm + 2 * R, lap_rows, 1, na), "LAP wall in")) ||
+        (rc = ck(prod(Wr, (long)RR, d_pout, Lm + 2 * R + 1, lap_rows, 1, na), "LAP wall out")))
+      break;
+  }
+  if (rc == 0) rc = ck(cudaDeviceSynchronize(), "operator build");
+  cleanup();
+  return rc;
+}
+
 int build_opset(const OpKey& k, std::shared_ptr<OpSet>* out) {
   {
     std::lock_guard<std::mutex> lk(g_ops_mu);
@@ -424,77 +486,12 @@ int build_opset(const OpKey& k, std::shared_ptr<OpSet>* out) {
   ops->key = k;
   const int R = k.R, M = k.Nm + 1;
   ops->R = R; ops->M = M;
-  const bool irk = (k.type == FALCON_IMEXRK);
   Cheb c = make_cheb(R, k.eta);
   std::vector<double> D1p, Lp;
   phys_deriv(c, D1p, Lp);
-  std::vector<double> ST((size_t)M * R * R), G((size_t)M * 3 * R * R), U((size_t)2 * R * R);
-  std::atomic<int> bad(0);
-  parallel_for(M, [&](int m) {
-    std::vector<double> AT, AF;
-    assemble_AT_AF(c, k.mbc, k.dt, m, k.wt, k.pr, irk, AT, AF);
-    std::vector<int> p1(R), p2(2 * R);
-    if (host_dgetrf(R, AT.data(), p1.data()) != 0) bad = m + 1;
-    if (host_dgetrf(2 * R, AF.data(), p2.data()) != 0 && m > 0) bad = m + 1;
-    std::vector<double> x(2 * R), v(R), dv(R);
-    double* S = &ST[(size_t)m * R * R];
-    for (int j = 0; j < R; ++j) {
-      std::fill(x.begin(), x.end(), 0.0);
-      x[j] = 1.0;
-      host_dgetrs(R, AT.data(), p1.data(), x.data());
-      apply_inv(c, x.data(), v.data(), nullptr);
-      for (int i = 0; i < R; ++i) S[i + (size_t)R * j] = v[i];
-    }
-    if (m > 0) {
-      double* Gm = &G[(size_t)m * 3 * R * R];
-      for (int j = 0; j < R; ++j) {
-        std::fill(x.begin(), x.end(), 0.0);
-        x[R + j] = 1.0;
-        host_dgetrs(2 * R, AF.data(), p2.data(), x.data());
-        apply_inv(c, x.data() + R, v.data(), nullptr);  // omega coefficients
-        for (int i = 0; i < R; ++i) Gm[i + (size_t)3 * R * j] = v[i];
-        apply_inv(c, x.data(), v.data(), dv.data());    // psi coefficients
-        for (int i = 0; i < R; ++i) {
-          Gm[R + i + (size_t)3 * R * j] = v[i];
-          Gm[2 * R + i + (size_t)3 * R * j] = -dv[i];
-        }
-      }
-    }
-  });
-  if (bad) return fail(FALCON_ESINGULAR, "dgetrf: singular operator for mode " + std::to_string(bad - 1));
-  std::vector<double> LAP;
-  if (k.needs_lap) {
-    std::vector<double> win, wout;
-    johnston_weights(c, k.lagpts, k.mbc, win, wout);
-    const int rows = 2 * R + 2;
-    LAP.assign((size_t)M * rows * R, 0.0);
-    parallel_for(M, [&](int m) {
-      if (m == 0) return;
-      std::vector<double> L;
-      assemble_lap(c, m, L);
-      std::vector<int> pv(R);
-      if (host_dgetrf(R, L.data(), pv.data()) != 0) bad = m + 1;
-      std::vector<double> x(R), v(R), dv(R);
-      double* Lm = &LAP[(size_t)m * rows * R];
-      for (int j = 0; j < R; ++j) {
-        std::fill(x.begin(), x.end(), 0.0);
-        x[j] = 1.0;
-        host_dgetrs(R, L.data(), pv.data(), x.data());
-        apply_inv(c, x.data(), v.data(), dv.data());
-        double oin = 0.0, oout = 0.0;
-        for (int i = 0; i < R; ++i) {
-          Lm[i + (size_t)rows * j] = v[i];
-          Lm[R + i + (size_t)rows * j] = -dv[i];
-          oin += win[i] * v[i];
-          oout += wout[i] * v[i];
-        }
-        Lm[2 * R + (size_t)rows * j] = oin;
-        Lm[2 * R + 1 + (size_t)rows * j] = oout;
-      }
-    });
-    if (bad) return fail(FALCON_ESINGULAR, "dgetrf: singular psi Poisson operator for mode " + std::to_string(bad - 1));
-  }
-
+  std::vector<double> U((size_t)2 * R * R);
+  int rc;
+  if ((rc = build_mode_operators(k, c, ops.get()))) return rc;
   {
     std::vector<double> Au;
     assemble_Au(c, k.mbc, k.dt, k.wt, Au);
@@ -512,13 +509,9 @@ int build_opset(const OpKey& k, std::shared_ptr<OpSet>* out) {
       }
     }
   }
-  int rc;
   if ((rc = upload(&ops->D1p, D1p, &ops->bytes))) return rc;
   if ((rc = upload(&ops->Lp, Lp, &ops->bytes))) return rc;
-  if ((rc = upload(&ops->ST, ST, &ops->bytes))) return rc;
-  if ((rc = upload(&ops->G, G, &ops->bytes))) return rc;
   if ((rc = upload(&ops->U, U, &ops->bytes))) return rc;
-  if (!LAP.empty() && (rc = upload(&ops->LAP, LAP, &ops->bytes))) return rc;
   if ((rc = upload(&ops->inv_r, c.inv_r, &ops->bytes))) return rc;
   if ((rc = upload(&ops->inv_r2, c.inv_r2, &ops->bytes))) return rc;
   {

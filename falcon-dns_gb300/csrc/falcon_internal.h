@@ -224,6 +224,19 @@ cudaError_t launch_diagnostics(const DiagArgs& a, cudaStream_t s);
 cudaError_t launch_assembly(const AsmArgs& a, cudaStream_t s);
 cudaError_t launch_assembly_post(int R, int M, int B, const double* inv_r, const double2* psi, const double* u0,
                                  const double* du0, double2* ur, double2* up, double2* w0, cudaStream_t s);
+// ---- operator construction (falcon_ops.cu) ----
+// kind 0: AT, kind 4: LAPpsi (R x R column-major per mode, modes m0..)
+cudaError_t launch_assemble(int kind, int R, int m0, int nmodes, const double* t, const double* D, const double* D2,
+                            const double* inv_r, const double* inv_r2, double wdt, double inv_pr, double C,
+                            double* out, cudaStream_t s);
+// AF (2R x 2R column-major per mode), irk selects the IMEXRK boundary-row order
+cudaError_t launch_assemble_af(int R, int m0, int nmodes, int mbc, int irk, const double* t, const double* D,
+                               const double* D2, const double* inv_r, const double* inv_r2, double wdt, double C,
+                               double* out, cudaStream_t s);
+// dgetrf + dgetrs per matrix; rhs row-major (n x nrhs); mats may be overwritten
+cudaError_t launch_lu_solve(int n, int nb, double* mats, size_t mstride, double* rhs, size_t rstride, int nrhs,
+                            int* info, cudaStream_t s);
+cudaError_t launch_unit_rhs(int n, int nrhs, int off, int nb, double* out, cudaStream_t s);
 // Self-timed FP64 FMA throughput kernel (returns GFLOP/s, or < 0 on error).
 double measure_fp64_peak();
 // Same for the FP64 tensor-core MMA (mma.sync m8n8k4 f64).

@@ -438,9 +438,13 @@ __global__ void __launch_bounds__(512) gemm_tile_kernel(GemmArgs g) {
   for (int i = 0; i < RPT; ++i) {
     const int row = row0 + warp * RPT + i;
     if (row < g.rows) {
-      if (n + 1 < g.N) {
-        *reinterpret_cast<double2*>(&Y[(size_t)row * g.ldy + n]) =
-            make_double2(g.alpha * acc[i][0], g.alpha * acc[i][1]);
+      double* yp = &Y[(size_t)row * g.ldy + n];
+      if (n + 1 < g.N && (reinterpret_cast<uintptr_t>(yp) & 15) == 0) {
+        *reinterpret_cast<double2*>(yp) = make_double2(g.alpha * acc[i][0], g.alpha * acc[i][1]);
+      } else if (n + 1 < g.N) {
+        // odd leading dimension or offset: two 8-byte stores
+        yp[0] = g.alpha * acc[i][0];
+        yp[1] = g.alpha * acc[i][1];
       } else if (n < g.N) {
         Y[(size_t)row * g.ldy + n] = g.alpha * acc[i][0];
       }
