@@ -166,6 +166,131 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+MIXED_NR = (33, 65, 97, 129)
+MIXED_NTHETA = (128, 256, 512, 1024, 1536)
+MIXED_SCHEMES = ("CNAB2", "SBDF3", "ARS343", "BPR353")
+MIXED_PR = (0.1, 1.0, 10.0)
+
+
+def cfl_dt(nr, nm, eta=0.35):
+    """0.2 x the t=0 CFL estimate: the diffusive bounds of get_dtvals
+    (src/nonlin.F90:102-104), dr^2 and (r dphi)^2 with dphi = (2/3) pi / Nm,
+    times compute_new_dt's Pr factor (src/steptime_rk.F90:194-199), which is
+    1 for every Pr."""
+    i = np.arange(nr)
+    rmin = eta / (1.0 - eta)
+    r = rmin + 0.5 * (1.0 + np.cos((nr - 1 - i) * np.pi / (nr - 1)))
+    dr = np.empty(nr)
+    dr[1:] = r[1:] - r[:-1]
+    dr[0] = dr[1]
+    rdphi = (2.0 / 3.0) * (r * np.pi) / nm
+    return 0.2 * min(float(np.min(dr * dr)), float(np.min(rdphi * rdphi)))
+
+
+def mixed_requests(fg, n, seed):
+    """Instances of the uneven batch / serving stream: Nr from {33,65,97,129},
+    Ntheta from {128,...,1536} (Nm = Ntheta // 3), scheme from {CNAB2, SBDF3,
+    ARS343, BPR353}, Ra log-uniform in [1e5, 1e8], Pr from {0.1, 1, 10},
+    dt = 0.2 x CFL estimate; noise seed per instance."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(n):
+        nr = int(rng.choice(MIXED_NR))
+        nm = int(rng.choice(MIXED_NTHETA)) // 3
+        scheme = str(rng.choice(MIXED_SCHEMES))
+        ra = 10.0 ** rng.uniform(5.0, 8.0)
+        pr = float(rng.choice(MIXED_PR))
+        p = fg.make_params(nr, nm, scheme, ra=ra, dt=cfl_dt(nr, nm), pr=pr)
+        out.append((p, 100000 * seed + k))
+    return out
+
+
+def run_uneven(args, fg, stream, torch):
+    """The uneven batch: 512 mixed instances stepped together (one group per
+    operator key, groups on concurrent streams, steady steps replayed from
+    CUDA graphs)."""
+    reqs = mixed_requests(fg, args.uneven_instances, 4)
+    t0 = time.perf_counter()
+    b = fg.Batch([p for p, _ in reqs])
+    setup_s = time.perf_counter() - t0
+    b.set_stream(stream.cuda_stream)
+    b.init_noise([s for _, s in reqs], 1e-3)
+    with torch.cuda.stream(stream):
+        b.step(args.warmup)
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    l0 = fg.launch_count()
+    ev0.record(stream)
+    b.step(args.uneven_steps)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    launches = fg.launch_count() - l0
+    n = len(reqs)
+    finite = sum(bool(np.isfinite(b.get_state(i)["T"]).all()) for i in range(n))
+    out = {"value": n * args.uneven_steps / (ms / 1e3), "unit": "instance-steps/s", "instances": n,
+           "steps": args.uneven_steps, "warmup": args.warmup, "ms_per_step": ms / args.uneven_steps,
+           "operator_groups": b.ngroups, "device_bytes": b.device_bytes, "setup_s": setup_s,
+           "gpu_launches": launches, "instances_finite": finite,
+           "workload": "512 instances (seed 4): Nr {33,65,97,129}, Ntheta {128,256,512,1024,1536} (Nm=Ntheta//3), "
+                       "scheme {CNAB2,SBDF3,ARS343,BPR353}, Ra log-uniform [1e5,1e8], Pr {0.1,1,10}, "
+                       "dt = 0.2 x CFL estimate, FP64"}
+    b.close()
+    return out
+
+
+def run_serving(args, fg, torch):
+    """The served stream: Poisson arrivals (50/s, seed 5) of mixed requests,
+    admitted by device footprint, stepped by continuous batching; latency is
+    submit -> result."""
+    rng = np.random.default_rng(5)
+    arrivals = []
+    t = 0.0
+    while True:
+        t += rng.exponential(1.0 / args.serve_rate)
+        if t > args.serve_seconds:
+            break
+        arrivals.append(t)
+    reqs = mixed_requests(fg, len(arrivals), 5)
+    lo, hi = 100 * args.serve_horizon_scale, 20000 * args.serve_horizon_scale
+    horizons = [max(1, int(round(np.exp(rng.uniform(np.log(lo), np.log(hi)))))) for _ in reqs]
+    srv = fg.Server(args.serve_budget_gb << 30)
+    submitted, done_at, ids = 0, {}, {}
+    pending = set()
+    steps_total = 0
+    iters = 0
+    t0 = time.perf_counter()
+    while len(done_at) < len(reqs):
+        now = time.perf_counter() - t0
+        while submitted < len(reqs) and arrivals[submitted] <= now:
+            p, seed = reqs[submitted]
+            ids[srv.submit(p, seed, horizons[submitted])] = submitted
+            pending.add(submitted)
+            submitted += 1
+        if not pending:
+            time.sleep(max(0.0, min(arrivals[submitted] - now, 0.01)))
+            continue
+        srv.iterate()
+        iters += 1
+        for rid, k in list(ids.items()):
+            if k in pending:
+                fin, _, _ = srv.poll(rid)
+                if fin:
+                    done_at[k] = time.perf_counter() - t0
+                    pending.discard(k)
+                    steps_total += horizons[k]
+    wall = time.perf_counter() - t0
+    srv.close()
+    lat = np.array([done_at[k] - arrivals[k] for k in range(len(reqs))])
+    return {"value": steps_total / wall, "unit": "instance-steps/s", "requests": len(reqs),
+            "p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
+            "mean_latency_s": float(lat.mean()), "wall_s": wall, "iterations": iters,
+            "instance_steps": steps_total,
+            "stream": f"Poisson arrivals {args.serve_rate:g}/s for {args.serve_seconds:g} s (seed 5), requests drawn "
+                      f"as the uneven batch, horizons log-uniform [{lo:g}, {hi:g}] steps "
+                      f"({args.serve_horizon_scale:g} x [100, 20000]), device budget {args.serve_budget_gb} GB"}
+
+
 def load_traffic(kernel):
     path = os.path.join(ROOT, "profiles", "traffic.json")
     try:
@@ -293,6 +418,11 @@ def run_gpu(args):
     for it in insts:
         it.close()
 
+    uneven = serving = None
+    if not args.no_mixed:
+        uneven = run_uneven(args, fg, stream, torch)
+        serving = run_serving(args, fg, torch)
+
     if rank != 0:
         if world > 1:
             torch.distributed.barrier()
@@ -314,6 +444,8 @@ def run_gpu(args):
         "one_at_a_time": {"value": one_rate, "unit": "instance-steps/s", "instances": n1, "steps": k1,
                           "batched_over_one_at_a_time": value / world / one_rate},
         "e2e": e2e,
+        "uneven_batch": uneven,
+        "serving": serving,
         "roofline": roofline,
         "cpu_baseline": cpu,
         "clocks": clk.summary(),
@@ -336,6 +468,13 @@ def main():
     ap.add_argument("--one-at-a-time", dest="one_at_a_time", type=int, default=16)
     ap.add_argument("--cpu-seconds", dest="cpu_seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", dest="no_cpu", action="store_true")
+    ap.add_argument("--no-mixed", dest="no_mixed", action="store_true", help="skip the uneven batch and serving")
+    ap.add_argument("--uneven-instances", dest="uneven_instances", type=int, default=512)
+    ap.add_argument("--uneven-steps", dest="uneven_steps", type=int, default=100)
+    ap.add_argument("--serve-rate", dest="serve_rate", type=float, default=50.0)
+    ap.add_argument("--serve-seconds", dest="serve_seconds", type=float, default=10.0)
+    ap.add_argument("--serve-horizon-scale", dest="serve_horizon_scale", type=float, default=0.1)
+    ap.add_argument("--serve-budget-gb", dest="serve_budget_gb", type=int, default=64)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -43,6 +43,7 @@ int fail(int code, const std::string& msg) {
   } while (0)
 
 std::atomic<long long> g_launches(0);
+std::atomic<int> g_graphs(1);  // replay steady-state steps as CUDA graphs
 
 // Optional per-launch CUDA-event timing (falcon_batch_profile).
 enum KernelClass { KC_NONLIN = 0, KC_GEMM_RADIAL, KC_GEMM_MODE, KC_ELEMENTWISE, KC_COUNT };
@@ -756,10 +757,23 @@ struct Group {
   int n_step = 0;
   double tot_time = 0.0;
   size_t bytes = 0;
+  // Steady-state steps replayed as CUDA graphs, one per ring-buffer phase
+  // (the kernel arguments of a step depend only on the history heads).
+  struct StepGraph { int phase; cudaGraphExec_t exec; long long kernels; };
+  std::vector<StepGraph> graphs;
+  bool own_stream = false;
+  cudaEvent_t done = nullptr;  // joins the group's stream back to its batch's stream
 
+  void drop_graphs() {
+    for (auto& sg : graphs) cudaGraphExecDestroy(sg.exec);
+    graphs.clear();
+  }
   ~Group() {
+    drop_graphs();
     for (void* q : allocs) cudaFree(q);
     if (stage_buf) cudaFreeHost(stage_buf);
+    if (done) cudaEventDestroy(done);
+    if (own_stream && stream) cudaStreamDestroy(stream);
   }
   size_t nel() const { return (size_t)R * M * B; }
   // Every per-instance array is [rows][B] elements of `ew` doubles; the
@@ -1114,8 +1128,51 @@ int step_imexrk(Group* g) {
   return 0;
 }
 
-int group_step(Group* g) {
+int group_step_direct(Group* g) {
   return g->p.scheme_type == FALCON_IMEX ? step_imex(g) : step_imexrk(g);
+}
+
+// Host-side bookkeeping of one step (what step_imex / step_imexrk update).
+void group_advance(Group* g) {
+  if (g->p.scheme_type == FALCON_IMEX) {
+    g->head = (g->head + g->sch.n_imp - 1) % g->sch.n_imp;
+    g->head_e = (g->head_e + g->sch.n_exp - 1) % g->sch.n_exp;
+  }
+  g->n_step += 1;
+  g->tot_time += g->p.dt;
+}
+
+// One time step.  From the second step on, the launch sequence of a step is
+// fixed up to the ring-buffer phase, so each phase is captured once into a
+// CUDA graph and replayed: one launch instead of 11 (IMEX) to ~60 (IMEXRK)
+// kernel launches, which lets many small groups keep the GPU busy.
+int group_step(Group* g) {
+  if (!g_graphs.load() || g->prof || g->n_step < 1) return group_step_direct(g);
+  const int phase = g->head * 8 + g->head_e;
+  for (auto& sg : g->graphs)
+    if (sg.phase == phase) {
+      CK(cudaGraphLaunch(sg.exec, g->stream));
+      g_launches += sg.kernels;
+      group_advance(g);
+      return 0;
+    }
+  const long long before = g_launches.load();
+  CK(cudaStreamBeginCapture(g->stream, cudaStreamCaptureModeThreadLocal));
+  const int rc = group_step_direct(g);  // advances the host state once
+  cudaGraph_t graph = nullptr;
+  const cudaError_t e = cudaStreamEndCapture(g->stream, &graph);
+  if (rc) {
+    if (graph) cudaGraphDestroy(graph);
+    return rc;
+  }
+  if (e != cudaSuccess) return fail(FALCON_ECUDA, std::string("step capture: ") + cudaGetErrorString(e));
+  cudaGraphExec_t exec = nullptr;
+  const cudaError_t ei = cudaGraphInstantiate(&exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (ei != cudaSuccess) return fail(FALCON_ECUDA, std::string("step graph: ") + cudaGetErrorString(ei));
+  g->graphs.push_back({phase, exec, g_launches.load() - before});
+  CK(cudaGraphLaunch(exec, g->stream));
+  return 0;
 }
 
 // After a state is loaded: histories zeroed, current slot = state,
@@ -1202,6 +1259,7 @@ int group_get_instance(Group* g, int b, double* t, double* w, double* up, double
 // new layout takes old slot map[j] (or zeros when map[j] < 0).
 int group_resize(Group* g, const std::vector<int>& map) {
   const int Bn = (int)map.size();
+  g->drop_graphs();  // the arrays move
   int* dmap = nullptr;
   CK(cudaMalloc(&dmap, sizeof(int) * std::max(Bn, 1)));
   CK(cudaMemcpy(dmap, map.data(), sizeof(int) * Bn, cudaMemcpyHostToDevice));
@@ -1430,9 +1488,18 @@ struct falcon_batch {
   std::vector<std::pair<int, int>> where;  // instance -> (group, slot)
   cudaStream_t stream = nullptr;
   bool own_stream = false;
+  cudaEvent_t start = nullptr;  // fans the batch's stream out to the group streams
   ~falcon_batch() {
     groups.clear();
+    if (start) cudaEventDestroy(start);
     if (own_stream && stream) cudaStreamDestroy(stream);
+  }
+  // Work of every group done and visible to the host.
+  int sync() {
+    for (auto& g : groups)
+      if (g->own_stream) CK(cudaStreamSynchronize(g->stream));
+    CK(cudaStreamSynchronize(stream));
+    return 0;
   }
 };
 
@@ -1470,6 +1537,17 @@ static int batch_create(const falcon_params* ps, int n, falcon_batch** out) {
     if (rc) return rc;
     for (size_t j = 0; j < kv.second.size(); ++j) b->where[kv.second[j]] = {(int)b->groups.size(), (int)j};
     b->groups.push_back(std::move(g));
+  }
+  if (b->groups.size() > 1) {
+    // groups of different operator keys run concurrently, one stream each,
+    // ordered after (and joined back into) the batch's stream in every step call
+    CK(cudaEventCreateWithFlags(&b->start, cudaEventDisableTiming));
+    for (auto& g : b->groups) {
+      CK(cudaStreamSynchronize(g->stream));
+      CK(cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking));
+      g->own_stream = true;
+      CK(cudaEventCreateWithFlags(&g->done, cudaEventDisableTiming));
+    }
   }
   *out = b.release();
   return 0;
@@ -1664,7 +1742,7 @@ int falcon_batch_create(const falcon_params* params, int n, falcon_batch** out) 
 }
 
 void falcon_batch_destroy(falcon_batch* b) {
-  if (b) { cudaStreamSynchronize(b->stream); delete b; }
+  if (b) { b->sync(); delete b; }
 }
 
 int falcon_batch_size(const falcon_batch* b) { return b ? (int)b->params.size() : 0; }
@@ -1690,7 +1768,8 @@ int falcon_batch_set_stream(falcon_batch* b, void* stream) {
   if (b->own_stream) cudaStreamDestroy(b->stream);
   b->own_stream = false;
   b->stream = (cudaStream_t)stream;
-  for (auto& g : b->groups) g->stream = b->stream;
+  for (auto& g : b->groups)
+    if (!g->own_stream) g->stream = b->stream;
   return 0;
 }
 
@@ -1717,8 +1796,7 @@ int falcon_batch_init_state(falcon_batch* b, int kind, double amp, const uint64_
     int rc = group_reset(g.get());
     if (rc) return rc;
   }
-  CK(cudaStreamSynchronize(b->stream));
-  return 0;
+  return b->sync();
 }
 
 int falcon_batch_get_state(falcon_batch* b, int i, double* tFR, double* omgFR, double* upFR, double* urFR,
@@ -1730,11 +1808,24 @@ int falcon_batch_get_state(falcon_batch* b, int i, double* tFR, double* omgFR, d
 
 int falcon_batch_step(falcon_batch* b, int nsteps) {
   if (!b || nsteps < 0) return fail(FALCON_EINVAL, "invalid step arguments");
-  for (int k = 0; k < nsteps; ++k)
+  const bool fan = b->start != nullptr;
+  if (fan) {
+    CK(cudaEventRecord(b->start, b->stream));
+    for (auto& g : b->groups) CK(cudaStreamWaitEvent(g->stream, b->start, 0));
+  }
+  int rc = 0;
+  for (int k = 0; k < nsteps && !rc; ++k)
     for (auto& g : b->groups) {
-      int rc = group_step(g.get());
-      if (rc) return rc;
+      rc = group_step(g.get());
+      if (rc) break;
     }
+  if (fan) {
+    for (auto& g : b->groups) {
+      CK(cudaEventRecord(g->done, g->stream));
+      CK(cudaStreamWaitEvent(b->stream, g->done, 0));
+    }
+  }
+  if (rc) return rc;
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return fail(FALCON_ECUDA, cudaGetErrorString(e));
   return 0;
@@ -1940,13 +2031,21 @@ struct falcon_server {
   std::deque<int64_t> queue;
   std::map<int64_t, ServerRequest> reqs;
   std::map<OpKey, ServerGroup> groups;
-  cudaStream_t stream = nullptr;
+  // groups are spread over a pool of streams so that their steps overlap
+  std::vector<cudaStream_t> streams;
+  int next_stream = 0;
   int active = 0;
   ~falcon_server() {
     groups.clear();
-    if (stream) cudaStreamDestroy(stream);
+    for (cudaStream_t q : streams) cudaStreamDestroy(q);
+  }
+  int sync() {
+    for (cudaStream_t q : streams) CK(cudaStreamSynchronize(q));
+    return 0;
   }
 };
+
+constexpr int kServerStreams = 16;
 
 namespace {
 
@@ -1985,7 +2084,7 @@ int server_admit_group(falcon_server* s, const OpKey& key, ServerGroup& sg) {
     std::vector<int> mem;
     for (size_t j = 0; j < new_ids.size(); ++j) { ps.push_back(s->reqs[new_ids[j]].p); mem.push_back((int)j); }
     sg.g = std::make_unique<Group>();
-    sg.g->stream = s->stream;
+    sg.g->stream = s->streams[s->next_stream++ % s->streams.size()];
     if ((rc = group_init(sg.g.get(), ps, mem))) return rc;
     sg.ids = new_ids;
     for (size_t j = 0; j < new_ids.size(); ++j) {
@@ -2040,9 +2139,13 @@ int falcon_server_create(size_t hbm_budget_bytes, int max_active, falcon_server*
   auto* s = new falcon_server();
   s->budget = hbm_budget_bytes;
   s->max_active = max_active > 0 ? max_active : (1 << 30);
-  if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) {
-    delete s;
-    return fail(FALCON_ECUDA, "stream creation failed");
+  for (int i = 0; i < kServerStreams; ++i) {
+    cudaStream_t q = nullptr;
+    if (cudaStreamCreateWithFlags(&q, cudaStreamNonBlocking) != cudaSuccess) {
+      delete s;
+      return fail(FALCON_ECUDA, "stream creation failed");
+    }
+    s->streams.push_back(q);
   }
   *out = s;
   return 0;
@@ -2050,7 +2153,7 @@ int falcon_server_create(size_t hbm_budget_bytes, int max_active, falcon_server*
 
 void falcon_server_destroy(falcon_server* s) {
   if (!s) return;
-  cudaStreamSynchronize(s->stream);
+  s->sync();
   delete s;
 }
 
@@ -2104,7 +2207,7 @@ int falcon_server_iterate(falcon_server* s, int* n_active, int* n_queued) {
     int rc = group_step(kv.second.g.get());
     if (rc) return rc;
   }
-  CK(cudaStreamSynchronize(s->stream));
+  if (int rc = s->sync()) return rc;
   // 4. retire finished requests
   for (auto& kv : s->groups) {
     ServerGroup& sg = kv.second;
@@ -2160,6 +2263,8 @@ extern "C" {
 
 long long falcon_launch_count(void) { return g_launches.load(); }
 
+int falcon_set_step_graphs(int enable) { return g_graphs.exchange(enable ? 1 : 0); }
+
 int falcon_batch_profile(falcon_batch* b, int nsteps, falcon_kernel_stat* stats, int max_stats, int* nstats) {
   if (!b || nsteps <= 0 || !stats || !nstats) return fail(FALCON_EINVAL, "invalid profile arguments");
   Prof prof;
@@ -2171,7 +2276,7 @@ int falcon_batch_profile(falcon_batch* b, int nsteps, falcon_kernel_stat* stats,
       if (rc) break;
     }
   for (auto& g : b->groups) g->prof = nullptr;
-  cudaStreamSynchronize(b->stream);
+  b->sync();
   double ms[KC_COUNT] = {0}, fl[KC_COUNT] = {0};
   int nl[KC_COUNT] = {0};
   for (auto& r : prof.recs) {

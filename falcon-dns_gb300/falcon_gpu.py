@@ -85,7 +85,7 @@ EXPORTS = (
     "falcon_server_create", "falcon_server_destroy", "falcon_server_submit", "falcon_server_iterate",
     "falcon_server_poll", "falcon_last_error", "falcon_version", "falcon_fp64_peak_gflops",
     "falcon_batch_profile", "falcon_launch_count", "falcon_fp64_mma_peak_gflops",
-    "falcon_nonlin_noalloc_dev",
+    "falcon_nonlin_noalloc_dev", "falcon_set_step_graphs",
 )
 
 
@@ -142,6 +142,7 @@ def lib():
     L.falcon_fp64_mma_peak_gflops.restype = ctypes.c_double
     L.falcon_batch_profile.argtypes = [vp, ip, P(KernelStat), ip, P(ctypes.c_int)]
     L.falcon_launch_count.restype = ctypes.c_longlong
+    L.falcon_set_step_graphs.argtypes = [ip]
     _lib = L
     return L
 
@@ -276,6 +277,52 @@ class Instance(Batch):
         return super().diagnostics()[0]
 
 
+class Server:
+    """Continuous-batching request loop (falcon_server_*).
+
+    submit() queues a simulation request (seeded noise initial state, a
+    horizon in steps); iterate() admits queued requests by device footprint,
+    steps every admitted request once and retires finished ones; poll()
+    returns (done, diagnostics, final temperature spectrum)."""
+
+    def __init__(self, hbm_budget_bytes, max_active=0):
+        self.h = ctypes.c_void_p()
+        check(lib().falcon_server_create(int(hbm_budget_bytes), int(max_active), ctypes.byref(self.h)))
+        self.shape = {}
+
+    def submit(self, params, seed, horizon):
+        i = ctypes.c_int64()
+        check(lib().falcon_server_submit(self.h, ctypes.byref(params), int(seed), int(horizon), ctypes.byref(i)))
+        self.shape[i.value] = (params.nr_max, params.nm_max + 1)
+        return i.value
+
+    def iterate(self):
+        na, nq = ctypes.c_int(), ctypes.c_int()
+        check(lib().falcon_server_iterate(self.h, ctypes.byref(na), ctypes.byref(nq)))
+        return na.value, nq.value
+
+    def poll(self, rid, want_state=False):
+        done = ctypes.c_int()
+        diag = FalconDiag()
+        t = None
+        if want_state:
+            t = np.empty(self.shape[rid], np.complex128)
+        check(lib().falcon_server_poll(self.h, rid, ctypes.byref(done), ctypes.byref(diag),
+                                       _dp(t) if t is not None else None))
+        return bool(done.value), (diag.as_dict() if done.value else None), (t if done.value else None)
+
+    def close(self):
+        if self.h:
+            lib().falcon_server_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def nonlin(nm, t, om, up, ur):
     """Nr_maxLOOP for one instance through the host-array C entry point."""
     ins = [np.ascontiguousarray(a, np.complex128) for a in (t, om, up, ur)]
@@ -294,3 +341,8 @@ def fp64_mma_peak_gflops():
 
 def launch_count():
     return lib().falcon_launch_count()
+
+
+def set_step_graphs(enable):
+    """Replay steady-state steps as CUDA graphs (default on); returns the previous setting."""
+    return lib().falcon_set_step_graphs(1 if enable else 0)

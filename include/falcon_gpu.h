@@ -205,8 +205,15 @@ typedef struct falcon_kernel_stat {
   double flops;
 } falcon_kernel_stat;
 int falcon_batch_profile(falcon_batch* b, int nsteps, falcon_kernel_stat* stats, int max_stats, int* nstats);
-/* Number of kernels this library has launched in the calling process. */
+/* Number of kernels this library has launched in the calling process
+ * (kernels inside a replayed step graph count once per replay). */
 long long falcon_launch_count(void);
+/* Steady-state steps (from the second step of a run on) are captured once
+ * per history phase into CUDA graphs and replayed; 0 turns this off for the
+ * whole process (every kernel launched directly), 1 turns it back on.
+ * Returns the previous setting.  Results are identical either way.
+ * No reference counterpart (launch mechanics of the GPU step). */
+int falcon_set_step_graphs(int enable);
 
 /* ---- misc ---- */
 const char* falcon_last_error(void);
