@@ -198,10 +198,17 @@ struct OpSet {
   double* wq = nullptr;     // radInt weights (src/integ.F90:36-76) on values
   double* d1_0 = nullptr;   // rows 0 and R-1 of D1p
   double* d1_R = nullptr;
+  // Explicit RK only: chebinvtranD1 and chebinvtranD2 + r^-1 chebinvtranD1
+  // applied to values taken as scaled coefficients (C D H, C (D2 + r^-1 D) H),
+  // for the first stage of a run, where the reference's upFC holds upFR
+  // (src/init.F90:252, used by src/rhs_create_rk.F90:158-161).
+  double* D1c = nullptr;
+  double* Lc = nullptr;
   size_t bytes = 0;
   ~OpSet() {
     cudaFree(D1p); cudaFree(Lp); cudaFree(ST); cudaFree(G); cudaFree(U); cudaFree(LAP);
     cudaFree(inv_r); cudaFree(inv_r2); cudaFree(wq); cudaFree(d1_0); cudaFree(d1_R);
+    cudaFree(D1c); cudaFree(Lc);
   }
 };
 
@@ -403,13 +410,14 @@ int build_mode_operators(const OpKey& k, const Cheb& c, OpSet* ops) {
     return 0;
   };
   const long lap_rows = 2L * R + 2;
+  const bool implicit = (k.type != FALCON_RK);  // explicit RK needs only LAPpsi
   if ((rc = dev_alloc(&Wm, 4 * RR * mc)) || (rc = dev_alloc(&Wr, 2 * RR * mc)) ||
-      (rc = dev_alloc(&ops->ST, RR * M)) || (rc = dev_alloc(&ops->G, 3 * RR * M)) ||
+      (implicit && (rc = dev_alloc(&ops->ST, RR * M))) || (implicit && (rc = dev_alloc(&ops->G, 3 * RR * M))) ||
       (k.needs_lap && (rc = dev_alloc(&ops->LAP, (size_t)lap_rows * R * M)))) {
     cleanup();
     return rc;
   }
-  ops->bytes += sizeof(double) * 4 * RR * M + (k.needs_lap ? sizeof(double) * lap_rows * R * M : 0);
+  ops->bytes += (implicit ? sizeof(double) * 4 * RR * M : 0) + (k.needs_lap ? sizeof(double) * lap_rows * R * M : 0);
   if (cudaMalloc(&d_info, sizeof(int) * mc) != cudaSuccess) { cleanup(); return fail(FALCON_ENOMEM, "info"); }
   auto ck = [&](cudaError_t e, const char* what) -> int {
     if (e != cudaSuccess) return fail(FALCON_ECUDA, std::string(what) + ": " + cudaGetErrorString(e));
@@ -439,24 +447,24 @@ int build_mode_operators(const OpKey& k, const Cheb& c, OpSet* ops) {
   const long L2 = (long)2 * RR, L3 = (long)3 * RR;
   for (int m0 = 0; m0 < M && rc == 0; m0 += mc) {
     const int nm = std::min(mc, M - m0);
+    const int a0 = std::max(m0, 1), na = m0 + nm - a0;
     // temperature: ST[m] = Tinv AT_m^-1
-    if ((rc = ck(launch_assemble(0, R, m0, nm, d_t, d_D, d_D2, d_ir, d_ir2, wdt, 1.0 / k.pr, C, Wm, s), "assemble AT")) ||
+    if (implicit && ((rc = ck(launch_assemble(0, R, m0, nm, d_t, d_D, d_D2, d_ir, d_ir2, wdt, 1.0 / k.pr, C, Wm, s), "assemble AT")) ||
         (rc = ck(launch_unit_rhs(R, R, 0, nm, Wr, s), "unit rhs")) ||
         (rc = ck(launch_lu_solve(R, nm, Wm, RR, Wr, RR, R, d_info, s), "lu AT")) ||
         (rc = check_info(nm, m0, "AT")) ||
-        (rc = ck(prod(Wr, (long)RR, d_tinv, ops->ST + (size_t)m0 * RR, R, R, nm), "ST product")))
+        (rc = ck(prod(Wr, (long)RR, d_tinv, ops->ST + (size_t)m0 * RR, R, R, nm), "ST product"))))
       break;
-    const int a0 = std::max(m0, 1), na = m0 + nm - a0;
     if (na <= 0) continue;
     // psi-omega: AF_m^-1 on [0; e_j], unknowns [psi; omega]
-    double* Gm = ops->G + (size_t)a0 * L3;
-    if ((rc = ck(launch_assemble_af(R, a0, na, k.mbc, irk, d_t, d_D, d_D2, d_ir, d_ir2, wdt, C, Wm, s), "assemble AF")) ||
+    double* Gm = implicit ? ops->G + (size_t)a0 * L3 : nullptr;
+    if (implicit && ((rc = ck(launch_assemble_af(R, a0, na, k.mbc, irk, d_t, d_D, d_D2, d_ir, d_ir2, wdt, C, Wm, s), "assemble AF")) ||
         (rc = ck(launch_unit_rhs(2 * R, R, R, na, Wr, s), "unit rhs")) ||
         (rc = ck(launch_lu_solve(2 * R, na, Wm, 4 * RR, Wr, L2, R, d_info, s), "lu AF")) ||
         (rc = check_info(na, a0, "psi-omega operator")) ||
         (rc = ck(prod(Wr + RR, L2, d_tinv, Gm, 3L * R, R, na), "G omega")) ||
         (rc = ck(prod(Wr, L2, d_tinv, Gm + R, 3L * R, R, na), "G psi")) ||
-        (rc = ck(prod(Wr, L2, d_mdinv, Gm + 2 * R, 3L * R, R, na), "G uphi")))
+        (rc = ck(prod(Wr, L2, d_mdinv, Gm + 2 * R, 3L * R, R, na), "G uphi"))))
       break;
     if (!k.needs_lap) continue;
     double* Lm = ops->LAP + (size_t)a0 * lap_rows * R;
@@ -515,6 +523,20 @@ int build_opset(const OpKey& k, std::shared_ptr<OpSet>* out) {
   if ((rc = upload(&ops->U, U, &ops->bytes))) return rc;
   if ((rc = upload(&ops->inv_r, c.inv_r, &ops->bytes))) return rc;
   if ((rc = upload(&ops->inv_r2, c.inv_r2, &ops->bytes))) return rc;
+  if (k.type == FALCON_RK) {
+    const double C = std::pow(2.0 / (double)(R - 1), 0.5);
+    std::vector<double> D1c((size_t)R * R), Lc((size_t)R * R);
+    for (int j = 0; j < R; ++j) {
+      const double h = (j == 0 || j == R - 1) ? 0.5 : 1.0;
+      for (int i = 0; i < R; ++i) {
+        const size_t q = i + (size_t)R * j;
+        D1c[q] = C * c.D[q] * h;
+        Lc[q] = C * c.D2[q] * h + c.inv_r[i] * D1c[q];
+      }
+    }
+    if ((rc = upload(&ops->D1c, D1c, &ops->bytes))) return rc;
+    if ((rc = upload(&ops->Lc, Lc, &ops->bytes))) return rc;
+  }
   {
     // radInt(f) = fac * sum_k w_k Re(chebtransform(f r))_k with w_k = -1/(k^2-1)
     // for even k (halved at k = 0, R-1), 0 for odd k; chebtransform is
@@ -626,6 +648,24 @@ int scheme_weights(int type, int imp, int exp, Scheme* s) {
       }
       default: return -1;
     }
+  }
+  if (type == FALCON_RK) {
+    // butcher_a / butcher_b (src/timeschemes.F90:1701-1720); the implicit
+    // tables stay zero.  RK4's a(2,3) = 1/2 of the reference is never read
+    // (stage 2 sums i < 2) and is left out.
+    if (imp != FALCON_IMP_NONE) return -1;
+    if (exp == FALCON_EXP_RK2) {
+      s->n_imp = s->n_exp = 2;
+      s->aA[1][0] = 0.5;
+      s->bA[0] = 0.0; s->bA[1] = 1.0;
+    } else if (exp == FALCON_EXP_RK4) {
+      s->n_imp = s->n_exp = 4;
+      s->aA[1][0] = 0.5; s->aA[2][1] = 0.5; s->aA[3][2] = 1.0;
+      s->bA[0] = 1.0 / 6.0; s->bA[1] = 1.0 / 3.0; s->bA[2] = 1.0 / 3.0; s->bA[3] = 1.0 / 6.0;
+    } else {
+      return -1;
+    }
+    return 0;
   }
   if (type == FALCON_IMEXRK) {
     auto set = [&](int n, const double* aD, const double* bD, const double* aA, const double* bA) {
@@ -748,6 +788,7 @@ struct Group {
           *buo[kMaxStages] = {};
   double2 *t0 = nullptr, *w0 = nullptr;
   double* u0 = nullptr;
+  double* us = nullptr;        // explicit RK: stage uphi_bar (R x B)
   double2* t_grid = nullptr;   // temperature seen by the last nonlinear pass (IMEXRK)
   double* diag_dev = nullptr;  // 8 per instance
   std::vector<double> diag_host;
@@ -802,7 +843,7 @@ OpKey key_of(const falcon_params& p, const Scheme& s) {
   k.R = p.nr_max; k.Nm = p.nm_max; k.mbc = p.mbc; k.type = p.scheme_type;
   k.imp = p.scheme_imp; k.exp = p.scheme_exp; k.dt = p.dt; k.pr = p.pr; k.eta = p.eta;
   k.wt = (p.scheme_type == FALCON_IMEX) ? s.wt_lhs : s.aD[s.diag][s.diag];
-  k.needs_lap = (p.scheme_type == FALCON_IMEXRK && !(s.check_A && s.check_D)) ? 1 : 0;
+  k.needs_lap = (p.scheme_type == FALCON_RK || (p.scheme_type == FALCON_IMEXRK && !(s.check_A && s.check_D))) ? 1 : 0;
   k.lagpts = k.needs_lap ? p.lagpts : 0;
   return k;
 }
@@ -814,7 +855,6 @@ int validate(const falcon_params& p) {
   if (!(p.dt > 0.0) || !std::isfinite(p.dt)) return fail(FALCON_EINVAL, "dt must be positive");
   if (!(p.pr > 0.0)) return fail(FALCON_EINVAL, "Pr must be positive");
   if (p.mbc != 0 && p.mbc != 1) return fail(FALCON_EINVAL, "mBC must be NS or SF");
-  if (p.scheme_type == FALCON_RK) return fail(FALCON_EINVAL, "time_scheme_type RK is not supported by this build");
   if (p.l_vartimestep) return fail(FALCON_EINVAL, "l_vartimestep=.TRUE. is not supported by this build");
   if (p.l_restart) return fail(FALCON_EINVAL, "l_restart=.TRUE. is not supported by this build");
   Scheme s;
@@ -846,6 +886,16 @@ int group_init(Group* g, const std::vector<falcon_params>& ps, const std::vector
           (rc = g->alloc(&g->uromh[i], (size_t)R * B)))
         return rc;
     }
+  } else if (g->p.scheme_type == FALCON_RK) {
+    // explicit RK: one right-hand side per stage for T and for omega (with
+    // uphi_bar in the m = 0 column), the stage uphi_bar
+    if ((rc = g->alloc(&g->th[0], n)) || (rc = g->alloc(&g->wh[0], n)) || (rc = g->alloc(&g->us, (size_t)R * B)))
+      return rc;
+    for (int i = 0; i < g->sch.n_exp; ++i)
+      if ((rc = g->alloc(&g->fat[i], n)) || (rc = g->alloc(&g->faw[i], n))) return rc;
+    if ((rc = g->alloc(&g->t0, n)) || (rc = g->alloc(&g->w0, n)) || (rc = g->alloc(&g->u0, (size_t)R * B)) ||
+        (rc = g->alloc(&g->t_grid, n)))
+      return rc;
   } else {
     if ((rc = g->alloc(&g->th[0], n)) || (rc = g->alloc(&g->wh[0], n))) return rc;
     for (int i = 0; i < g->sch.n_exp; ++i) {
@@ -1128,8 +1178,102 @@ int step_imexrk(Group* g) {
   return 0;
 }
 
+// Explicit RK (timeloop_rk, src/steptime_rk.F90:103-141): per stage the
+// stage values (Get_stage_var: psi through LAPpsi, Johnston wall vorticity,
+// mode 0 from uphi_bar), the nonlinear pass, and the explicit right-hand
+// sides; then Assembly_stage with the b weights.
+int step_rk(Group* g) {
+  const int R = g->R, M = g->M, B = g->B;
+  const size_t n = g->nel();
+  OpSet* o = g->ops.get();
+  cudaStream_t s = g->stream;
+  const Scheme& sc = g->sch;
+  const int ns = sc.n_exp;
+  const int nstep = g->n_step + 1;
+  int rc;
+  double2* dup = g->rhs_t;  // d(u_phi)/dr of every mode (rhs_t is unused by RK)
+  auto combine = [&](int nf, const double* coef, double2* t_out, double2* w_out, double* u_out) {
+    RkCombineArgs a{};
+    a.R = R; a.M = M; a.B = B; a.nf = nf; a.dt = g->p.dt;
+    for (int i = 0; i < nf; ++i) { a.c[i] = coef[i]; a.ft[i] = g->fat[i]; a.fw[i] = g->faw[i]; }
+    a.t0 = g->t0; a.w0 = g->w0; a.u0 = g->u0;
+    a.t_out = t_out; a.w_out = w_out; a.u_out = u_out; a.rhs_w = g->rhs_w;
+    return elementwise(g, 8.0 * nf + 4.0, [&]() { return launch_rk_combine(a, s); });
+  };
+  // psi, u_phi, u_r and the wall vorticity of modes >= 1 from rhs_w; mode 0
+  // from uphi_bar (omega_0 = u/r + du/dr, u_phi = u, u_r = 0)
+  auto psi_update = [&](double2* w_out, double* u_in) -> int {
+    if (M > 1) {
+      const int rows = 2 * R + 2;
+      const long sL = (long)rows * R;
+      if ((rc = gemm(g, KC_GEMM_MODE, per_mode(o->LAP, rows, sL, g->rhs_w, g->psi, R, M, B, 1, M - 1, R))) ||
+          (rc = gemm(g, KC_GEMM_MODE, per_mode(o->LAP + R, rows, sL, g->rhs_w, g->up, R, M, B, 1, M - 1, R))) ||
+          (rc = gemm(g, KC_GEMM_MODE, per_mode(o->LAP + 2 * R, rows, sL, g->rhs_w, w_out, R, M, B, 1, M - 1, 1))) ||
+          (rc = gemm(g, KC_GEMM_MODE, per_mode(o->LAP + 2 * R + 1, rows, sL, g->rhs_w, w_out + (size_t)(R - 1) * M * B,
+                                               R, M, B, 1, M - 1, 1))))
+        return rc;
+    }
+    GemmArgs gd{};
+    gd.A = o->D1p; gd.lda = R;
+    gd.X = u_in; gd.ldx = B;
+    gd.Y = reinterpret_cast<double*>(g->lu0); gd.ldy = B;
+    gd.K = R; gd.rows = R; gd.N = B; gd.batch = 1; gd.alpha = 1.0;
+    if ((rc = gemm(g, KC_GEMM_RADIAL, gd))) return rc;
+    return elementwise(g, 3.0, [&]() {
+      return launch_assembly_post(R, M, B, o->inv_r, g->psi, u_in, reinterpret_cast<const double*>(g->lu0), g->ur,
+                                  g->up, w_out, s);
+    });
+  };
+  for (int st = 0; st < ns; ++st) {
+    if (st > 0) {
+      if ((rc = combine(st, sc.aA[st], g->T(), g->W(), g->us)) || (rc = psi_update(g->W(), g->us))) return rc;
+    }
+    if (nstep > 1 || st > 0) {
+      if ((rc = run_nonlin(g))) return rc;
+      CK(cudaMemcpyAsync(g->t_grid, g->T(), sizeof(double2) * n, cudaMemcpyDeviceToDevice, s));
+    } else {
+      CK(cudaMemsetAsync(g->ntp, 0, sizeof(double2) * n, s));
+      CK(cudaMemsetAsync(g->ntr, 0, sizeof(double2) * n, s));
+      CK(cudaMemsetAsync(g->nwp, 0, sizeof(double2) * n, s));
+      CK(cudaMemsetAsync(g->nwr, 0, sizeof(double2) * n, s));
+    }
+    // the first stage of a run reads upFC as initialised (= upFR)
+    const bool coef = (nstep == 1 && st == 0);
+    GemmArgs gl = radial(coef ? o->Lc : o->Lp, g->up, g->lu0, R, M, B);
+    gl.N = 2 * B; gl.ldy = 2L * B;
+    if ((rc = gemm(g, KC_GEMM_RADIAL, radial(o->D1p, g->ntr, g->dntr, R, M, B))) ||
+        (rc = gemm(g, KC_GEMM_RADIAL, radial(o->D1p, g->nwr, g->dnwr, R, M, B))) ||
+        (rc = gemm(g, KC_GEMM_RADIAL, radial(o->Lp, g->T(), g->lt, R, M, B))) ||
+        (rc = gemm(g, KC_GEMM_RADIAL, radial(o->Lp, g->W(), g->lw, R, M, B))) ||
+        (rc = gemm(g, KC_GEMM_RADIAL, radial(coef ? o->D1c : o->D1p, g->up, dup, R, M, B))) ||
+        (rc = gemm(g, KC_GEMM_RADIAL, gl)))
+      return rc;
+    RkRhsArgs a{};
+    a.R = R; a.M = M; a.B = B; a.inv_pr = 1.0 / g->p.pr;
+    a.inv_r = o->inv_r; a.inv_r2 = o->inv_r2; a.ra_pr = g->ra_pr;
+    a.t = g->T(); a.w = g->W(); a.lt = g->lt; a.lw = g->lw;
+    a.ntp = g->ntp; a.ntr = g->ntr; a.dntr = g->dntr; a.nwp = g->nwp; a.nwr = g->nwr; a.dnwr = g->dnwr;
+    a.up = g->up; a.ur = g->ur; a.dup = dup; a.lub = g->lu0;
+    a.ft = g->fat[st]; a.fw = g->faw[st];
+    if ((rc = elementwise(g, 30.0, [&]() { return launch_rk_rhs(a, s); })) ||
+        (rc = launch(g, KC_ELEMENTWISE, 8.0 * M * R * B, [&]() { return launch_rk_ubar(a, s); })))
+      return rc;
+  }
+  // Assembly_stage: y_n = y_0 + dt sum_i b_i F_i, in place
+  if ((rc = combine(ns, sc.bA, g->t0, g->w0, g->u0)) || (rc = psi_update(g->w0, g->u0))) return rc;
+  CK(cudaMemcpyAsync(g->T(), g->t0, sizeof(double2) * n, cudaMemcpyDeviceToDevice, s));
+  CK(cudaMemcpyAsync(g->W(), g->w0, sizeof(double2) * n, cudaMemcpyDeviceToDevice, s));
+  g->n_step = nstep;
+  g->tot_time += g->p.dt;
+  return 0;
+}
+
 int group_step_direct(Group* g) {
-  return g->p.scheme_type == FALCON_IMEX ? step_imex(g) : step_imexrk(g);
+  switch (g->p.scheme_type) {
+    case FALCON_IMEX: return step_imex(g);
+    case FALCON_IMEXRK: return step_imexrk(g);
+    default: return step_rk(g);
+  }
 }
 
 // Host-side bookkeeping of one step (what step_imex / step_imexrk update).
@@ -1202,13 +1346,9 @@ int group_reset(Group* g) {
     CK(cudaMemcpyAsync(g->w0, g->W(), sizeof(double2) * n, cudaMemcpyDeviceToDevice, s));
     CK(cudaMemcpyAsync(g->t_grid, g->T(), sizeof(double2) * n, cudaMemcpyDeviceToDevice, s));
     CK(launch_extract_mode0(R, M, B, g->up, g->u0, s));
-    for (int i = 0; i < g->sch.n_exp; ++i) {
-      CK(cudaMemsetAsync(g->fat[i], 0, sizeof(double2) * n, s));
-      CK(cudaMemsetAsync(g->fdt[i], 0, sizeof(double2) * n, s));
-      CK(cudaMemsetAsync(g->faw[i], 0, sizeof(double2) * n, s));
-      CK(cudaMemsetAsync(g->fdw[i], 0, sizeof(double2) * n, s));
-      CK(cudaMemsetAsync(g->buo[i], 0, sizeof(double2) * n, s));
-    }
+    for (int i = 0; i < g->sch.n_exp; ++i)
+      for (double2* q : {g->fat[i], g->fdt[i], g->faw[i], g->fdw[i], g->buo[i]})
+        if (q) CK(cudaMemsetAsync(q, 0, sizeof(double2) * n, s));
   }
   CK(cudaMemsetAsync(g->psi, 0, sizeof(double2) * n, s));
   return 0;
@@ -1309,10 +1449,9 @@ int group_reset_instance(Group* g, int b) {
     }
     CK(launch_extract_mode0(R, M, B, g->up, g->ubh[g->head], s));
   } else {
-    for (int i = 0; i < g->sch.n_exp; ++i) {
-      CK(zero(g->fat[i], n, 2)); CK(zero(g->fdt[i], n, 2)); CK(zero(g->faw[i], n, 2));
-      CK(zero(g->fdw[i], n, 2)); CK(zero(g->buo[i], n, 2));
-    }
+    for (int i = 0; i < g->sch.n_exp; ++i)
+      for (double2* q : {g->fat[i], g->fdt[i], g->faw[i], g->fdw[i], g->buo[i]})
+        if (q) CK(zero(q, n, 2));
     CK(copy(g->T(), g->t0, n, 2));
     CK(copy(g->W(), g->w0, n, 2));
     CK(copy(g->T(), g->t_grid, n, 2));
@@ -2057,6 +2196,7 @@ size_t instance_bytes(const falcon_params& p) {
   const size_t R = p.nr_max, M = p.nm_max + 1, f = 16 * R * M;
   size_t n = 0;
   if (p.scheme_type == FALCON_IMEX) n += (2 * s.n_imp + 2 * s.n_exp) * f + (s.n_imp + s.n_exp) * 8 * R;
+  else if (p.scheme_type == FALCON_RK) n += (2 + 2 * s.n_exp) * f + 16 * R;
   else n += (2 + 5 * s.n_exp) * f + 8 * R;
   n += 13 * f + 16 * R + 32 * R + 8;
   return n;

@@ -224,6 +224,32 @@ cudaError_t launch_diagnostics(const DiagArgs& a, cudaStream_t s);
 cudaError_t launch_assembly(const AsmArgs& a, cudaStream_t s);
 cudaError_t launch_assembly_post(int R, int M, int B, const double* inv_r, const double2* psi, const double* u0,
                                  const double* du0, double2* ur, double2* up, double2* w0, cudaStream_t s);
+// ---- explicit RK (falcon_rk.cu) ----
+// y_out = y0 + dt sum_i c_i F_i for T (with its boundary values), the
+// vorticity of modes m >= 1 (all rows) and uphi_bar (held in the m = 0
+// column of the vorticity stage arrays); rhs_w = -omega with zero boundary
+// rows (m >= 1), 0 for m = 0.  Outputs may alias the y0 inputs.
+struct RkCombineArgs {
+  int R, M, B, nf;
+  double dt;
+  double c[kMaxStages];
+  const double2* ft[kMaxStages]; const double2* fw[kMaxStages];
+  const double2 *t0, *w0; const double* u0;
+  double2 *t_out, *w_out, *rhs_w; double* u_out;
+};
+// Explicit right-hand sides of one stage (rhs_create_rk): temperature for
+// every mode, vorticity for m >= 1, and uphi_bar into fw[(r, 0, b)].
+struct RkRhsArgs {
+  int R, M, B;
+  double inv_pr;
+  const double *inv_r, *inv_r2, *ra_pr;
+  const double2 *t, *w, *lt, *lw, *ntp, *ntr, *dntr, *nwp, *nwr, *dnwr;
+  const double2 *up, *ur, *dup, *lub;  // lub: radial Laplacian of the m = 0 column, R x B
+  double2 *ft, *fw;
+};
+cudaError_t launch_rk_combine(const RkCombineArgs& a, cudaStream_t s);
+cudaError_t launch_rk_rhs(const RkRhsArgs& a, cudaStream_t s);
+cudaError_t launch_rk_ubar(const RkRhsArgs& a, cudaStream_t s);
 // ---- operator construction (falcon_ops.cu) ----
 // kind 0: AT, kind 4: LAPpsi (R x R column-major per mode, modes m0..)
 cudaError_t launch_assemble(int kind, int R, int m0, int nmodes, const double* t, const double* D, const double* D2,

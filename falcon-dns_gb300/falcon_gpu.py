@@ -34,6 +34,8 @@ SCHEMES = {
     "ARS343": ("IMEXRK", "ARS343", "expARS343"),
     "BPR353": ("IMEXRK", "BPR353", "expBPR353"),
     "ARS222": ("IMEXRK", "ARS222", "expARS222"),
+    "RK2": ("RK", "NONE", "RK2"),
+    "RK4": ("RK", "NONE", "RK4"),
 }
 
 

@@ -611,6 +611,28 @@ orc_sim* orc_sim_create(const orc_params* p) {
     s->ipiv1 = (int*)calloc((size_t)R * M, sizeof(int));
     s->ipiv2 = (int*)calloc((size_t)2 * R * M, sizeof(int));
     s->ipiv_uphi = (int*)calloc((size_t)R, sizeof(int));
+  } else if (p->scheme_type == ORC_TYPE_RK) {
+    /* butcher_a / butcher_b of RK2 (midpoint) and RK4 (classical),
+     * src/timeschemes.F90:1701-1720 */
+    memset(&s->sch, 0, sizeof(s->sch));
+    if (p->scheme_exp == ORC_EXP_RK2) {
+      s->sch.n_exp = 2;
+      s->sch.aA[1][0] = 0.5;
+      s->sch.bA[0] = 0.0; s->sch.bA[1] = 1.0;
+    } else if (p->scheme_exp == ORC_EXP_RK4) {
+      s->sch.n_exp = 4;
+      s->sch.aA[1][0] = 0.5; s->sch.aA[1][2] = 0.5; /* a(2,3) is never read: stage 2 sums i < 2 */
+      s->sch.aA[2][1] = 0.5;
+      s->sch.aA[3][2] = 1.0;
+      s->sch.bA[0] = 1.0 / 6.0; s->sch.bA[1] = 1.0 / 3.0; s->sch.bA[2] = 1.0 / 3.0; s->sch.bA[3] = 1.0 / 6.0;
+    } else {
+      orc_sim_destroy(s);
+      return NULL;
+    }
+    s->sch.n_imp = s->sch.n_exp;
+    int ns = s->sch.n_exp;
+    s->dtemp_a = zalloc(cf * ns); s->dtemp_d = zalloc(cf * ns);
+    s->domg_a = zalloc(cf * ns); s->domg_d = zalloc(cf * ns); s->rhs_buo = zalloc(cf * ns);
   } else {
     orc_sim_destroy(s);
     return NULL;
@@ -1680,10 +1702,287 @@ static void imexrk_step(orc_sim* s) {
   s->n_step = n_step;
 }
 
+/* ------------------------------------------------------------------------ */
+/* Explicit RK (RK2, RK4): src/steptime_rk.F90:52-180,                       */
+/* src/fourierloop_rk.F90, src/rhs_create_rk.F90                             */
+/* ------------------------------------------------------------------------ */
+
+/* psi from the vorticity of mode m >= 1 through LAPpsi (rhs = -omega with
+ * zero boundary rows), then psii, u_phi = -dpsi/dr, u_r = i m psi / r, the
+ * Johnston wall vorticity written into w[0], w[R-1], and upFC(m)
+ * (src/fourierloop_rk.F90:168-212, :373-413). */
+static void rk_psi_update(orc_sim* s, int m, double* w, double* v) {
+  int R = s->R, M = s->M, lm = s->p.lagpts;
+  const double* rr = s->r_radius;
+  double* rhs = v; double* psr = v + 2 * R; double* dps = v + 4 * R; double* ut = v + 6 * R;
+  double* solw = v + 8 * R;
+  for (int r = 0; r < R; ++r) { rhs[2 * r] = -1.0 * w[2 * r]; rhs[2 * r + 1] = -1.0 * w[2 * r + 1]; }
+  rhs[0] = 0.0; rhs[1] = 0.0; rhs[2 * (R - 1)] = 0.0; rhs[2 * (R - 1) + 1] = 0.0;
+  matsolve_cplx(R, s->LAPpsi_all + (size_t)R * R * m, s->ipiv_lap + (size_t)R * m, rhs, solw);
+  orc_chebinvtran(R, rhs, psr);
+  orc_chebinvtranD1(R, rhs, dps);
+  double d2min[2] = {0, 0}, dmin[2] = {0, 0}, d2max[2] = {0, 0}, dmax[2] = {0, 0};
+  for (int i = 0; i < lm; ++i)
+    for (int q = 0; q < 2; ++q) {
+      d2min[q] = d2min[q] + s->d2w_rmin[i] * psr[2 * (i + 1) + q];
+      dmin[q] = dmin[q] + s->dw_rmin[i] * psr[2 * (i + 1) + q];
+    }
+  for (int i = 0; i < lm; ++i)
+    for (int q = 0; q < 2; ++q) {
+      d2max[q] = d2max[q] + s->d2w_rmax[i] * psr[2 * (R - 2 - i) + q];
+      dmax[q] = dmax[q] + s->dw_rmax[i] * psr[2 * (R - 2 - i) + q];
+    }
+  for (int r = 0; r < R; ++r) {
+    CX(s->psii, m, r)[0] = psr[2 * r]; CX(s->psii, m, r)[1] = psr[2 * r + 1];
+    CX(s->upFR, m, r)[0] = -1.0 * dps[2 * r]; CX(s->upFR, m, r)[1] = -1.0 * dps[2 * r + 1];
+    double ar, ai;
+    cmul(0.0, (double)m * rr[r], psr[2 * r], psr[2 * r + 1], &ar, &ai);
+    CX(s->urFR, m, r)[0] = ar; CX(s->urFR, m, r)[1] = ai;
+  }
+  for (int q = 0; q < 2; ++q) {
+    if (s->p.mbc == 0) {
+      w[q] = -1.0 * (d2min[q] - 2.0 * s->dw_rmin[0] * dmin[q]);
+      w[2 * (R - 1) + q] = -1.0 * (d2max[q] - 2.0 * s->dw_rmax[0] * dmax[q]);
+    } else {
+      w[q] = -2.0 * rr[0] * dmin[q];
+      w[2 * (R - 1) + q] = -2.0 * rr[R - 1] * dmax[q];
+    }
+  }
+  get_mode(s, s->upFR, m, ut);
+  orc_chebtransform(R, ut, ut + 2 * R);
+  put_mode(s, s->upFC, m, ut + 2 * R);
+}
+
+/* Mode 0 from uphi_bar: upFC(0), omega_0 = ubar/r + d ubar/dr, u_r = 0. */
+static void rk_mode0_update(orc_sim* s, const double* u, double* w0, double* v) {
+  int R = s->R, M = s->M;
+  double* c = v; double* du = v + 2 * R;
+  orc_chebtransform(R, u, c);
+  put_mode(s, s->upFC, 0, c);
+  orc_chebinvtranD1(R, c, du);
+  for (int r = 0; r < R; ++r) {
+    CX(s->urFR, 0, r)[0] = 0.0; CX(s->urFR, 0, r)[1] = 0.0;
+    w0[2 * r] = u[2 * r] * s->r_radius[r] + du[2 * r];
+    w0[2 * r + 1] = u[2 * r + 1] * s->r_radius[r] + du[2 * r + 1];
+  }
+}
+
+/* Get_stage_var, src/fourierloop_rk.F90:75-222: Y_s = Y_0 + dt sum_i a(s,i) F_i */
+static void rk_get_stage_var(orc_sim* s, int st) {
+  int R = s->R, M = s->M, ns = s->sch.n_exp;
+  double dt = s->dt_array[0];
+#pragma omp parallel
+  {
+    double* v = zalloc(24 * (size_t)R);
+#pragma omp for schedule(static)
+    for (int m = 0; m < M; ++m) {
+      double* F = v; double* y = v + 2 * R; double* wk = v + 4 * R;
+      for (int i = 0; i < 2 * R; ++i) F[i] = 0.0;
+      for (int i = 0; i < st; ++i)
+        for (int r = 0; r < R; ++r) {
+          const double* q = stg(s->dtemp_a, ns, i, M, m, r);
+          F[2 * r] = F[2 * r] + s->sch.aA[st][i] * q[0];
+          F[2 * r + 1] = F[2 * r + 1] + s->sch.aA[st][i] * q[1];
+        }
+      for (int r = 0; r < R; ++r) {
+        const double* y0 = CX(s->temp_spec, m, r);
+        CX(s->tFR, m, r)[0] = y0[0] + dt * F[2 * r];
+        CX(s->tFR, m, r)[1] = y0[1] + dt * F[2 * r + 1];
+      }
+      CX(s->tFR, m, 0)[0] = (m == 0) ? 1.0 : 0.0; CX(s->tFR, m, 0)[1] = 0.0;
+      CX(s->tFR, m, R - 1)[0] = 0.0; CX(s->tFR, m, R - 1)[1] = 0.0;
+      for (int i = 0; i < 2 * R; ++i) F[i] = 0.0;
+      for (int i = 0; i < st; ++i)
+        for (int r = 0; r < R; ++r) {
+          const double* q = stg(s->domg_a, ns, i, M, m, r);
+          F[2 * r] = F[2 * r] + s->sch.aA[st][i] * q[0];
+          F[2 * r + 1] = F[2 * r + 1] + s->sch.aA[st][i] * q[1];
+        }
+      if (m == 0) {
+        for (int r = 0; r < R; ++r) {
+          y[2 * r] = s->uphi_bar_spec[2 * r] + dt * F[2 * r];
+          y[2 * r + 1] = s->uphi_bar_spec[2 * r + 1] + dt * F[2 * r + 1];
+        }
+        y[0] = 0.0; y[1] = 0.0; y[2 * (R - 1)] = 0.0; y[2 * (R - 1) + 1] = 0.0;
+        put_mode(s, s->upFR, 0, y);
+        rk_mode0_update(s, y, F, wk);
+        put_mode(s, s->omgFR, 0, F);
+      } else {
+        for (int r = 0; r < R; ++r) {
+          const double* y0 = CX(s->omg_spec, m, r);
+          y[2 * r] = y0[0] + dt * F[2 * r];
+          y[2 * r + 1] = y0[1] + dt * F[2 * r + 1];
+        }
+        rk_psi_update(s, m, y, wk);
+        put_mode(s, s->omgFR, m, y);
+      }
+    }
+    free(v);
+  }
+}
+
+/* RHS_construct_stage with rhs_create_rk (src/fourierloop_rk.F90:224-279,
+ * src/rhs_create_rk.F90:19-224): the full explicit right-hand sides. */
+static void rk_rhs_construct_stage(orc_sim* s, int st) {
+  int R = s->R, M = s->M, ns = s->sch.n_exp;
+  const double* rr = s->r_radius;
+  const double* rr2 = s->r_radius2;
+  double rp = s->p.ra / s->p.pr;
+#pragma omp parallel
+  {
+    double* wk = zalloc(24 * (size_t)R);
+    double* a = wk + 12 * R; double* b = wk + 14 * R; double* o = wk + 16 * R; double* l = wk + 18 * R;
+#pragma omp for schedule(static)
+    for (int m = 0; m < M; ++m) {
+      get_mode(s, s->uphi_temp_FR, m, a);
+      get_mode(s, s->ur_temp_FR, m, b);
+      advect_term(s, m, a, b, o, wk);
+      get_mode(s, s->tFR, m, a);
+      lap_phys(s, m, a, l, wk);
+      for (int r = 0; r < R; ++r) {
+        double* d = stg(s->dtemp_a, ns, st, M, m, r);
+        d[0] = (1.0 / s->p.pr) * l[2 * r] + o[2 * r];
+        d[1] = (1.0 / s->p.pr) * l[2 * r + 1] + o[2 * r + 1];
+      }
+      if (m == 0) continue;
+      get_mode(s, s->uphi_omg_FR, m, a);
+      get_mode(s, s->ur_omg_FR, m, b);
+      advect_term(s, m, a, b, o, wk);
+      get_mode(s, s->omgFR, m, a);
+      lap_phys(s, m, a, l, wk);
+      get_mode(s, s->tFR, m, a);
+      for (int r = 0; r < R; ++r) {
+        double br, bi;
+        cmul(0.0, (double)m * rr[r], a[2 * r], a[2 * r + 1], &br, &bi);
+        double* d = stg(s->domg_a, ns, st, M, m, r);
+        d[0] = (l[2 * r] + o[2 * r]) - rp * br;
+        d[1] = (l[2 * r + 1] + o[2 * r + 1]) - rp * bi;
+      }
+    }
+    free(wk);
+  }
+  /* rhs_construct_uphi_bar (src/rhs_create_rk.F90:135-224): diffusion of
+   * ubar minus the Fourier-space means of ur d(u_phi)/dr + ur u_phi / r,
+   * with d(u_phi)/dr from upFC of every mode. */
+  double* d1 = zalloc(2 * (size_t)M * R);
+  double* d2u = zalloc(2 * (size_t)R);
+  double* c = zalloc(2 * (size_t)R); double* tmp = zalloc(2 * (size_t)R);
+  for (int m = 0; m < M; ++m) {
+    get_mode(s, s->upFC, m, c);
+    orc_chebinvtranD1(R, c, tmp);
+    for (int r = 0; r < R; ++r) { d1[2 * ((size_t)M * r + m)] = tmp[2 * r]; d1[2 * ((size_t)M * r + m) + 1] = tmp[2 * r + 1]; }
+    if (m == 0) orc_chebinvtranD2(R, c, d2u);
+  }
+  for (int r = 0; r < R; ++r) {
+    double uu = 0.0, ud = 0.0;
+    for (int m = 0; m < M; ++m) {
+      const double* ur = CX(s->urFR, m, r);
+      const double* up = CX(s->upFR, m, r);
+      const double* du = d1 + 2 * ((size_t)M * r + m);
+      if (m == 0) {
+        uu = uu + (ur[0] * up[0] - ur[1] * up[1]);
+        ud = ud + (ur[0] * du[0] - ur[1] * du[1]);
+      } else {
+        /* real(ur conj(up) + conj(ur) up) */
+        uu = uu + ((ur[0] * up[0] - ur[1] * (-up[1])) + (ur[0] * up[0] - (-ur[1]) * up[1]));
+        ud = ud + ((ur[0] * du[0] - ur[1] * (-du[1])) + (ur[0] * du[0] - (-ur[1]) * du[1]));
+      }
+    }
+    const double* u0 = CX(s->upFR, 0, r);
+    const double diff = (d2u[2 * r] - rr2[r] * u0[0]) + rr[r] * d1[2 * ((size_t)M * r)];
+    double* d = stg(s->domg_a, ns, st, M, 0, r);
+    d[0] = diff - (ud + rr[r] * uu);
+    d[1] = 0.0;
+  }
+  free(d1); free(d2u); free(c); free(tmp);
+}
+
+/* Assembly_stage, src/fourierloop_rk.F90:281-424: Y_n = Y_0 + dt sum b_i F_i */
+static void rk_assembly_stage(orc_sim* s) {
+  int R = s->R, M = s->M, ns = s->sch.n_exp;
+  double dt = s->dt_new;
+#pragma omp parallel
+  {
+    double* v = zalloc(24 * (size_t)R);
+#pragma omp for schedule(static)
+    for (int m = 0; m < M; ++m) {
+      double* F = v; double* y = v + 2 * R; double* wk = v + 4 * R;
+      for (int i = 0; i < 2 * R; ++i) F[i] = 0.0;
+      for (int i = 0; i < ns; ++i)
+        for (int r = 0; r < R; ++r) {
+          const double* q = stg(s->dtemp_a, ns, i, M, m, r);
+          F[2 * r] = F[2 * r] + s->sch.bA[i] * q[0];
+          F[2 * r + 1] = F[2 * r + 1] + s->sch.bA[i] * q[1];
+        }
+      for (int r = 0; r < R; ++r) {
+        double* t = CX(s->temp_spec, m, r);
+        t[0] = t[0] + dt * F[2 * r]; t[1] = t[1] + dt * F[2 * r + 1];
+      }
+      CX(s->temp_spec, m, 0)[0] = (m == 0) ? 1.0 : 0.0; CX(s->temp_spec, m, 0)[1] = 0.0;
+      CX(s->temp_spec, m, R - 1)[0] = 0.0; CX(s->temp_spec, m, R - 1)[1] = 0.0;
+      for (int i = 0; i < 2 * R; ++i) F[i] = 0.0;
+      for (int i = 0; i < ns; ++i)
+        for (int r = 0; r < R; ++r) {
+          const double* q = stg(s->domg_a, ns, i, M, m, r);
+          F[2 * r] = F[2 * r] + s->sch.bA[i] * q[0];
+          F[2 * r + 1] = F[2 * r + 1] + s->sch.bA[i] * q[1];
+        }
+      if (m == 0) {
+        for (int r = 0; r < R; ++r) {
+          s->uphi_bar_spec[2 * r] = s->uphi_bar_spec[2 * r] + dt * F[2 * r];
+          s->uphi_bar_spec[2 * r + 1] = s->uphi_bar_spec[2 * r + 1] + dt * F[2 * r + 1];
+        }
+        s->uphi_bar_spec[0] = 0.0; s->uphi_bar_spec[1] = 0.0;
+        s->uphi_bar_spec[2 * (R - 1)] = 0.0; s->uphi_bar_spec[2 * (R - 1) + 1] = 0.0;
+        rk_mode0_update(s, s->uphi_bar_spec, y, wk);
+        put_mode(s, s->omg_spec, 0, y);
+      } else {
+        for (int r = 0; r < R; ++r) {
+          const double* y0 = CX(s->omg_spec, m, r);
+          y[2 * r] = y0[0] + dt * F[2 * r];
+          y[2 * r + 1] = y0[1] + dt * F[2 * r + 1];
+        }
+        rk_psi_update(s, m, y, wk);
+        put_mode(s, s->omg_spec, m, y);
+      }
+    }
+    free(v);
+  }
+  size_t cf = 2 * (size_t)M * R;
+  memcpy(s->tFR, s->temp_spec, cf * sizeof(double));
+  memcpy(s->omgFR, s->omg_spec, cf * sizeof(double));
+  put_mode(s, s->upFR, 0, s->uphi_bar_spec);
+}
+
+static void rk_step(orc_sim* s) {
+  int R = s->R, M = s->M, ns = s->sch.n_exp;
+  int n_step = s->n_step + 1;
+  if (n_step == 1 && !s->mats_built) {
+    /* mat_build_rk for every mode before the loop (src/steptime_rk.F90:92-94) */
+    for (int m = 0; m < M; ++m) mat_build_rk(s, m, s->LAPpsi_all + (size_t)R * R * m, s->ipiv_lap + (size_t)R * m);
+    s->mats_built = 1;
+  }
+  s->dt_new = s->p.dt;
+  for (int i = 0; i < 4; ++i) s->dt_array[i] = s->p.dt;
+  for (int st = 0; st < ns; ++st) {
+    if (st > 0) rk_get_stage_var(s, st);
+    if (n_step > 1 || st > 0) nr_maxloop(s);
+    rk_rhs_construct_stage(s, st);
+  }
+  rk_assembly_stage(s);
+  s->tot_time = s->tot_time + s->dt_new;
+  double* v = zalloc(2 * (size_t)R);
+  get_mode(s, s->tFR, 0, v);
+  orc_chebtransform(R, v, s->TFC);
+  free(v);
+  s->n_step = n_step;
+}
+
 int orc_sim_step(orc_sim* s, int nsteps) {
   for (int k = 0; k < nsteps; ++k) {
     if (s->p.scheme_type == ORC_TYPE_IMEX) imex_step(s);
     else if (s->p.scheme_type == ORC_TYPE_IMEXRK) imexrk_step(s);
+    else if (s->p.scheme_type == ORC_TYPE_RK) rk_step(s);
     else return -1;
   }
   return 0;
