@@ -177,9 +177,12 @@ struct OpKey {
   int R, Nm, mbc, type, imp, exp;
   double dt, pr, eta, wt;
   int needs_lap, lagpts;
+  // Grouping only (0 for operator sets): a variable-dt instance carries a
+  // unique tag so that it never shares a group (its dt is its own).
+  long long tag;
   bool operator<(const OpKey& o) const {
-    return std::tie(R, Nm, mbc, type, imp, exp, dt, pr, eta, wt, needs_lap, lagpts) <
-           std::tie(o.R, o.Nm, o.mbc, o.type, o.imp, o.exp, o.dt, o.pr, o.eta, o.wt, o.needs_lap, o.lagpts);
+    return std::tie(R, Nm, mbc, type, imp, exp, dt, pr, eta, wt, needs_lap, lagpts, tag) <
+           std::tie(o.R, o.Nm, o.mbc, o.type, o.imp, o.exp, o.dt, o.pr, o.eta, o.wt, o.needs_lap, o.lagpts, o.tag);
   }
 };
 
@@ -582,12 +585,12 @@ struct Scheme {
   int diag = 1;
 };
 
-// Constant-dt weights of rhs_update_wts_imp/_exp (src/timeschemes.F90:
-// 1004-1052, 1621-1701) with dt_array(:) = dt.
-int scheme_weights(int type, int imp, int exp, Scheme* s) {
-  s->type = type; s->imp = imp; s->exp = exp;
-  if (type == FALCON_IMEX) {
-    const double d[4] = {1, 1, 1, 1};
+// Multistep weights of rhs_update_wts_imp/_exp (src/timeschemes.F90:
+// 1004-1052, 1621-1701) for the time-step history dta = dt_array(1..4)
+// (dta[0] the newest); all-equal entries give the constant-dt weights.
+int imex_weights(int imp, int exp, const double* dta, Scheme* s) {
+  {
+    const double* d = dta;
     switch (imp) {
       case FALCON_IMP_CN:
         s->n_imp = 2; s->w_imp[0] = 0.5; s->wt_lhs = 0.5;
@@ -604,7 +607,7 @@ int scheme_weights(int type, int imp, int exp, Scheme* s) {
         return 0;
       case FALCON_IMP_BDF2: {
         if (exp != FALCON_EXP_AB2) return -1;
-        const double r1 = 1.0, a0 = (2.0 + r1) / (1.0 + r1), a1 = 1.0 + 1.0 / r1;
+        const double r1 = d[1] / d[0], a0 = (2.0 + r1) / (1.0 + r1), a1 = 1.0 + 1.0 / r1;
         const double a2 = -1.0 * (1.0 / r1 / (1.0 + r1));
         s->n_imp = 2; s->n_exp = 2;
         s->wt_lhs = 1.0 / a0; s->w_imp[0] = a1 / a0; s->w_imp[1] = a2 / a0;
@@ -613,7 +616,7 @@ int scheme_weights(int type, int imp, int exp, Scheme* s) {
       }
       case FALCON_IMP_BDF3: {
         if (exp != FALCON_EXP_AB3) return -1;
-        const double r1 = 1.0, r2 = 1.0;
+        const double r1 = d[1] / d[0], r2 = d[2] / d[0];
         const double a0 = (1.0 + 1.0 / (1.0 + r1) + 1.0 / (1.0 + r1 + r2));
         const double a1 = (((1.0 + r1) * (1.0 + r1 + r2)) / (r1 * (r1 + r2)));
         const double a2 = (-1.0 * (1.0 + r1 + r2) / (r1 * r2 * (1.0 + r1)));
@@ -629,7 +632,7 @@ int scheme_weights(int type, int imp, int exp, Scheme* s) {
       }
       case FALCON_IMP_BDF4: {
         if (exp != FALCON_EXP_AB4) return -1;
-        const double r1 = 1.0, r2 = 1.0, r3 = 1.0;
+        const double r1 = d[0] / d[1], r2 = d[1] / d[2], r3 = d[2] / d[3];
         const double c1 = 1.0 + r3 * (1.0 + r2), c2 = 1.0 + r2 * (1.0 + r1), c3 = 1.0 + r3 * c2;
         const double a0 = 1.0 + r1 / (1.0 + r1) + r2 * r1 / c2 + r3 * r2 * r1 / c3;
         const double a1 = -1.0 - r1 * (1.0 + r2 * (1.0 + r1) * (1.0 + r3 * c2 / c1) / (1.0 + r2));
@@ -648,6 +651,15 @@ int scheme_weights(int type, int imp, int exp, Scheme* s) {
       }
       default: return -1;
     }
+  }
+}
+
+// Scheme tables with dt_array(:) = dt (constant time step).
+int scheme_weights(int type, int imp, int exp, Scheme* s) {
+  s->type = type; s->imp = imp; s->exp = exp;
+  if (type == FALCON_IMEX) {
+    const double ones[4] = {1, 1, 1, 1};
+    return imex_weights(imp, exp, ones, s);
   }
   if (type == FALCON_RK) {
     // butcher_a / butcher_b (src/timeschemes.F90:1701-1720); the implicit
@@ -804,6 +816,15 @@ struct Group {
   std::vector<StepGraph> graphs;
   bool own_stream = false;
   cudaEvent_t done = nullptr;  // joins the group's stream back to its batch's stream
+  // Variable time step (l_vartimestep, one instance per group): the dt
+  // history dt_array(1..4), the current dt, the per-line velocity maxima of
+  // the last nonlinear pass, and the grid spacing for get_dtvals.
+  bool vardt = false;
+  double dt_array[4] = {0, 0, 0, 0};
+  double dt_new = 0.0;
+  double* umax = nullptr;
+  std::vector<double> umax_h, dr_h, radius_h;
+  double cur_dt() const { return vardt ? dt_new : p.dt; }
 
   void drop_graphs() {
     for (auto& sg : graphs) cudaGraphExecDestroy(sg.exec);
@@ -855,7 +876,10 @@ int validate(const falcon_params& p) {
   if (!(p.dt > 0.0) || !std::isfinite(p.dt)) return fail(FALCON_EINVAL, "dt must be positive");
   if (!(p.pr > 0.0)) return fail(FALCON_EINVAL, "Pr must be positive");
   if (p.mbc != 0 && p.mbc != 1) return fail(FALCON_EINVAL, "mBC must be NS or SF");
-  if (p.l_vartimestep) return fail(FALCON_EINVAL, "l_vartimestep=.TRUE. is not supported by this build");
+  if (p.l_vartimestep && p.scheme_type != FALCON_IMEX)
+    return fail(FALCON_EINVAL, "l_vartimestep=.TRUE. is supported for IMEX multistep schemes only by this build");
+  if (p.l_vartimestep && !(p.cfl > 0.0 && p.dt_coef > 0.0 && p.dt_max > 0.0))
+    return fail(FALCON_EINVAL, "l_vartimestep needs CFL, dt_coef and dt_max > 0");
   if (p.l_restart) return fail(FALCON_EINVAL, "l_restart=.TRUE. is not supported by this build");
   Scheme s;
   if (scheme_weights(p.scheme_type, p.scheme_imp, p.scheme_exp, &s) != 0)
@@ -916,6 +940,17 @@ int group_init(Group* g, const std::vector<falcon_params>& ps, const std::vector
       (rc = g->alloc(&g->diag_dev, (size_t)8 * B)))
     return rc;
   g->ub = reinterpret_cast<double*>(g->ub2);
+  if (g->p.l_vartimestep) {
+    if (B != 1) return fail(FALCON_EINVAL, "a variable-dt group holds one instance");
+    g->vardt = true;
+    if ((rc = g->alloc(&g->umax, (size_t)2 * R * B))) return rc;
+    g->umax_h.resize((size_t)2 * R);
+    Cheb c = make_cheb(R, g->p.eta);
+    g->dr_h = c.dr;
+    g->radius_h = c.radius;
+    for (int i = 0; i < 4; ++i) g->dt_array[i] = g->p.dt;
+    g->dt_new = g->p.dt;
+  }
   g->ra_pr_h.resize(B);
   for (int i = 0; i < B; ++i) g->ra_pr_h[i] = ps[members[i]].ra / ps[members[i]].pr;
   CK(cudaMemcpy(g->ra_pr, g->ra_pr_h.data(), sizeof(double) * B, cudaMemcpyHostToDevice));
@@ -980,7 +1015,7 @@ int run_nonlin(Group* g) {
   a.plan = g->fft->plan; a.tw = g->fft->tw; a.pos = g->fft->pos;
   a.t = g->T(); a.w = g->W(); a.up = g->up; a.ur = g->ur;
   a.ntp = g->ntp; a.ntr = g->ntr; a.nwp = g->nwp; a.nwr = g->nwr;
-  a.umax = nullptr;
+  a.umax = g->vardt ? g->umax : nullptr;
   const double P = g->P;
   const double flops = (double)g->R * g->B * (4.0 * 5.0 * P * std::log2(P) + 6.0 * P);
   return launch(g, KC_NONLIN, flops, [&]() { return launch_nonlin(a, g->stream); });
@@ -1017,12 +1052,53 @@ int solve_all(Group* g, double2* t_out, double2* w_out, double buo_scale, double
   });
 }
 
+// compute_new_dt of the multistep loop (src/steptime.F90:313-370) from the
+// get_dtvals time scales (src/nonlin.F90:93-106) of the last nonlinear
+// pass: the CFL step, optionally changed only when needed (l_optimizedt),
+// and the dt_array history shifted.  Before the second step, dt = the
+// namelist dt.
+int vardt_update(Group* g, int nstep) {
+  const falcon_params& p = g->p;
+  if (nstep <= 1) {
+    g->dt_new = p.dt;
+    for (int i = 0; i < 4; ++i) g->dt_array[i] = p.dt;
+    return 0;
+  }
+  const int R = g->R;
+  CK(cudaMemcpyAsync(g->umax_h.data(), g->umax, sizeof(double) * 2 * R, cudaMemcpyDeviceToHost, g->stream));
+  CK(cudaStreamSynchronize(g->stream));
+  const double pi = 4.0 * std::atan(1.0);
+  double mr = 0.0, mp = 0.0;
+  for (int r = 0; r < R; ++r) {
+    const double dtr = g->dr_h[r] / g->umax_h[2 * r];
+    const double dtp = (2.0 / 3.0) * (g->radius_h[r] * pi) / ((double)g->Nm * g->umax_h[2 * r + 1]);
+    mr = (r == 0) ? dtr : std::fmin(mr, dtr);
+    mp = (r == 0) ? dtp : std::fmin(mp, dtp);
+  }
+  const double dt_cal = std::fmin(mr, mp);
+  double dt_n;
+  if (p.pr == 1.0 || p.pr > 1.0) dt_n = std::fmax(1.0 / p.pr, 1.0) * p.cfl * dt_cal;
+  else dt_n = std::fmin(1.0 / p.pr, 1.0) * p.cfl * dt_cal;
+  const double dt2 = std::fmin(0.5 * (1.0 / p.dt_coef + 1.0) * dt_n, p.dt_max);
+  if (p.l_optimizedt) {
+    // dt keeps its previous value when no branch applies
+    if (g->dt_array[1] > p.dt_max) g->dt_new = p.dt_max;
+    else if (g->dt_array[1] >= dt_cal) g->dt_new = dt2;
+    else if (p.dt_coef * g->dt_array[1] < dt_cal && g->dt_array[1] < p.dt_max)
+      g->dt_new = (g->dt_array[0] < dt2) ? dt2 : g->dt_array[0];
+  } else {
+    g->dt_new = dt2;
+  }
+  const int nmax = std::max(g->sch.n_imp, g->sch.n_exp);
+  for (int i = nmax - 1; i >= 1; --i) g->dt_array[i] = g->dt_array[i - 1];
+  g->dt_array[0] = g->dt_new;
+  return 0;
+}
+
 int step_imex(Group* g) {
   const int R = g->R, M = g->M, B = g->B;
   const size_t n = g->nel();
-  OpSet* o = g->ops.get();
   cudaStream_t s = g->stream;
-  const Scheme& sc = g->sch;
   const int nstep = g->n_step + 1;
   int rc;
   if (nstep > 1) {
@@ -1033,6 +1109,26 @@ int step_imex(Group* g) {
     CK(cudaMemsetAsync(g->nwp, 0, sizeof(double2) * n, s));
     CK(cudaMemsetAsync(g->nwr, 0, sizeof(double2) * n, s));
   }
+  // Variable time step: new dt, weights of the dt history, and the
+  // operators rebuilt when dt_array(1) /= dt_array(2) (src/fourierloop.F90:
+  // 74-91; the matrices keep their previous weight otherwise, as there).
+  Scheme vs = g->sch;
+  if (g->vardt) {
+    if ((rc = vardt_update(g, nstep))) return rc;
+    if (imex_weights(vs.imp, vs.exp, g->dt_array, &vs) != 0) return fail(FALCON_EINVAL, "unsupported time scheme");
+    if (nstep == 1 || g->dt_array[0] != g->dt_array[1]) {
+      OpKey k = key_of(g->p, vs);
+      k.dt = g->dt_array[0];
+      k.wt = vs.wt_lhs;
+      if (k < g->ops->key || g->ops->key < k) {
+        std::shared_ptr<OpSet> fresh;
+        if ((rc = build_opset(k, &fresh))) return rc;
+        g->ops = fresh;
+      }
+    }
+  }
+  const Scheme& sc = vs;
+  OpSet* o = g->ops.get();
   if ((rc = gemm(g, KC_GEMM_RADIAL, radial(o->D1p, g->ntr, g->dntr, R, M, B))) ||
       (rc = gemm(g, KC_GEMM_RADIAL, radial(o->D1p, g->nwr, g->dnwr, R, M, B))))
     return rc;
@@ -1051,7 +1147,7 @@ int step_imex(Group* g) {
   RhsArgs a{};
   a.R = R; a.M = M; a.B = B;
   a.inv_r = o->inv_r; a.inv_r2 = o->inv_r2; a.ra_pr = g->ra_pr;
-  a.dt = g->p.dt; a.inv_pr = 1.0 / g->p.pr;
+  a.dt = g->cur_dt(); a.inv_pr = 1.0 / g->p.pr;
   a.scheme_cn = cn ? 1 : 0;
   a.n_imp = ni; a.n_exp = ne; a.wt_lhs = sc.wt_lhs;
   for (int i = 0; i < 4; ++i) { a.w_imp[i] = sc.w_imp[i]; a.w_exp[i] = sc.w_exp[i]; }
@@ -1070,12 +1166,12 @@ int step_imex(Group* g) {
   a.lt = g->lt; a.lw = g->lw; a.lu0 = g->lu0;
   a.rhs_t = g->rhs_t; a.rhs_w = g->rhs_w;
   if ((rc = elementwise(g, 10.0 + 8.0 * (ni + ne), [&]() { return launch_imex_rhs(a, s); }))) return rc;
-  const double buo_scale = g->p.dt * (cn ? 0.5 : sc.wt_lhs);
+  const double buo_scale = g->cur_dt() * (cn ? 0.5 : sc.wt_lhs);
   if ((rc = solve_all(g, g->th[h_new], g->wh[h_new], buo_scale, nullptr, g->ubh[h_new]))) return rc;
   g->head = h_new;
   g->head_e = he_new;
   g->n_step = nstep;
-  g->tot_time += g->p.dt;
+  g->tot_time += g->cur_dt();
   return 0;
 }
 
@@ -1291,7 +1387,7 @@ void group_advance(Group* g) {
 // CUDA graph and replayed: one launch instead of 11 (IMEX) to ~60 (IMEXRK)
 // kernel launches, which lets many small groups keep the GPU busy.
 int group_step(Group* g) {
-  if (!g_graphs.load() || g->prof || g->n_step < 1) return group_step_direct(g);
+  if (!g_graphs.load() || g->prof || g->n_step < 1 || g->vardt) return group_step_direct(g);
   const int phase = g->head * 8 + g->head_e;
   for (auto& sg : g->graphs)
     if (sg.phase == phase) {
@@ -1486,7 +1582,7 @@ int group_diagnostics(Group* g) {
 
 void fill_diag(const Group* g, int b, double time, falcon_diag* d) {
   const double* v = &g->diag_host[(size_t)8 * b];
-  d->time = time; d->dt = g->p.dt;
+  d->time = time; d->dt = g->cur_dt();
   d->ke = v[0]; d->ke_r = v[1]; d->ke_phi = v[2]; d->ke_upbar = v[3];
   d->nu_top = v[4]; d->nu_bot = v[5]; d->vis = v[6]; d->buo = v[7];
 }
@@ -1664,8 +1760,8 @@ static int batch_create(const falcon_params* ps, int n, falcon_batch** out) {
   for (int i = 0; i < n; ++i) {
     Scheme s;
     scheme_weights(ps[i].scheme_type, ps[i].scheme_imp, ps[i].scheme_exp, &s);
-    OpKey k = key_of(ps[i], s);
-    k.wt = k.wt;  // operators shared whenever the key matches (Ra may differ)
+    OpKey k = key_of(ps[i], s);  // operators shared whenever the key matches (Ra may differ)
+    if (ps[i].l_vartimestep) k.tag = i + 1;
     byk[k].push_back(i);
   }
   b->where.resize(n);
@@ -2310,6 +2406,7 @@ int falcon_server_submit(falcon_server* s, const falcon_params* p, uint64_t seed
   Scheme sc;
   scheme_weights(p->scheme_type, p->scheme_imp, p->scheme_exp, &sc);
   r.key = key_of(*p, sc);
+  if (p->l_vartimestep) r.key.tag = r.id;
   if (r.foot + opset_bytes(*p) > s->budget) return fail(FALCON_EBUSY, "request larger than the device budget");
   s->reqs[r.id] = r;
   s->queue.push_back(r.id);

@@ -174,13 +174,15 @@ def read_namelist(path):
 
 
 def make_params(nr, nm, scheme="CNAB2", eta=0.35, ra=1e5, pr=1.0, dt=1e-5, mbc="NS", lagpts=16,
-                buo="IMP"):
+                buo="IMP", vartimestep=False, optimizedt=False, cfl=0.9, dt_coef=2.0, dt_max=3e-5):
     p = default_params()
     p.nr_max, p.nm_max, p.eta, p.ra, p.pr, p.dt = nr, nm, eta, ra, pr, dt
     p.mbc = 0 if mbc == "NS" else 1
     p.lagpts = lagpts
     p.buo_imp = 1 if buo == "IMP" else 0
-    p.l_vartimestep = 0
+    p.l_vartimestep = 1 if vartimestep else 0
+    p.l_optimizedt = 1 if optimizedt else 0
+    p.cfl, p.dt_coef, p.dt_max = cfl, dt_coef, dt_max
     p.l_imexrk_started = 0
     typ, imp, exp = SCHEMES[scheme]
     check(lib().falcon_params_set_scheme(ctypes.byref(p), typ.encode(), imp.encode(), exp.encode()))

@@ -55,6 +55,9 @@ typedef struct orc_params {
   int scheme_imp;        /* ORC_IMP_* */
   int scheme_exp;        /* ORC_EXP_* */
   int l_imexrk_started;  /* l_imexrk_started */
+  int l_vartimestep;     /* &timecontrol l_vartimestep: dt from the CFL condition */
+  int l_optimizedt;      /* l_optimizedt: change dt only when needed */
+  double cfl, dt_coef, dt_max;  /* CFL, dt_coef, dt_max */
 } orc_params;
 
 /* ---- transforms (reference: src/fourier_fftw.F90, src/chebyshev_fftw.F90) ---- */
@@ -95,6 +98,8 @@ int orc_sim_step(orc_sim* s, int nsteps);
  * out[5]=Nu_bot out[6]=viscous dissipation out[7]=buoyancy power out[8]=time */
 int orc_sim_diagnostics(orc_sim* s, double* out);
 int orc_sim_nstep(const orc_sim* s);
+/* Current time step (dt_new; changes with l_vartimestep). */
+double orc_sim_dt(const orc_sim* s);
 /* Host seeded-noise generator shared by the kind-1 initial state. */
 void orc_noise_pair(uint64_t seed, int m, int i, double* a, double* b);
 /* Number of OpenMP threads the oracle uses (0 = runtime default). */

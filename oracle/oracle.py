@@ -42,7 +42,9 @@ class OrcParams(ctypes.Structure):
                 ("mbc", ctypes.c_int), ("lagpts", ctypes.c_int), ("buo_imp", ctypes.c_int),
                 ("dt", ctypes.c_double), ("scheme_type", ctypes.c_int),
                 ("scheme_imp", ctypes.c_int), ("scheme_exp", ctypes.c_int),
-                ("l_imexrk_started", ctypes.c_int)]
+                ("l_imexrk_started", ctypes.c_int), ("l_vartimestep", ctypes.c_int),
+                ("l_optimizedt", ctypes.c_int), ("cfl", ctypes.c_double), ("dt_coef", ctypes.c_double),
+                ("dt_max", ctypes.c_double)]
 
 
 def build():
@@ -82,6 +84,8 @@ def lib():
         L.orc_sim_step.argtypes = [ctypes.c_void_p, ctypes.c_int]
         L.orc_sim_diagnostics.argtypes = [ctypes.c_void_p, dp]
         L.orc_sim_nstep.argtypes = [ctypes.c_void_p]
+        L.orc_sim_dt.argtypes = [ctypes.c_void_p]
+        L.orc_sim_dt.restype = ctypes.c_double
         L.orc_noise_pair.argtypes = [ctypes.c_uint64, ctypes.c_int, ctypes.c_int, dp, dp]
         L.orc_set_threads.argtypes = [ctypes.c_int]
         _lib = L
@@ -174,11 +178,13 @@ def nonlin(nm, t, om, up, ur):
 
 
 def make_params(nr, nm, scheme="CNAB2", eta=0.35, ra=1e5, pr=1.0, dt=1e-5, mbc="NS",
-                lagpts=16, buo="IMP", imexrk_started=False):
+                lagpts=16, buo="IMP", imexrk_started=False, vartimestep=False, optimizedt=False,
+                cfl=0.9, dt_coef=2.0, dt_max=3e-5):
     typ, imp, exp = SCHEMES[scheme]
     return OrcParams(nr, nm, eta, ra, pr, 0 if mbc == "NS" else 1, lagpts,
                      1 if buo == "IMP" else 0, dt, TYPE[typ], IMP[imp], EXP[exp],
-                     1 if imexrk_started else 0)
+                     1 if imexrk_started else 0, 1 if vartimestep else 0, 1 if optimizedt else 0,
+                     cfl, dt_coef, dt_max)
 
 
 class Sim:
@@ -211,6 +217,11 @@ class Sim:
         arrs = [np.empty((self.R, self.M), np.complex128) for _ in range(5)]
         lib().orc_sim_get_state(self.h, *[_dp(a) for a in arrs])
         return dict(zip(("T", "omg", "up", "ur", "psi"), arrs))
+
+    @property
+    def dt(self):
+        """Current time step (dt_new)."""
+        return lib().orc_sim_dt(self.h)
 
     def step(self, n=1):
         rc = lib().orc_sim_step(self.h, n)

@@ -532,6 +532,7 @@ struct orc_sim {
   double *AT_all, *AF_all, *A_uphi; int *ipiv1, *ipiv2, *ipiv_uphi;
   double *LAPpsi_all; int *ipiv_lap;
   double *dw_rmin, *d2w_rmin, *dw_rmax, *d2w_rmax;
+  double *dtval_r, *dtval_p;  /* get_dtvals of the last nonlinear pass */
   scheme_t sch;
   double dt_array[4];
   double dt_new, tot_time;
@@ -645,6 +646,7 @@ orc_sim* orc_sim_create(const orc_params* p) {
   if (lm > R - 2) lm = R - 2;
   s->p.lagpts = lm;
   s->dw_rmin = zalloc(lm); s->d2w_rmin = zalloc(lm); s->dw_rmax = zalloc(lm); s->d2w_rmax = zalloc(lm);
+  s->dtval_r = zalloc(R); s->dtval_p = zalloc(R);
   {
     double* pts = zalloc(lm);
     for (int i = 0; i < lm; ++i) pts[i] = s->radius[1 + i];
@@ -670,12 +672,13 @@ void orc_sim_destroy(orc_sim* s) {
                   s->tmp_imp_uphi, s->tmp_exp_uphi, s->dtemp_a, s->dtemp_d, s->domg_a,
                   s->domg_d, s->rhs_buo, s->AT_all, s->AF_all, s->A_uphi, s->ipiv1, s->ipiv2,
                   s->ipiv_uphi, s->LAPpsi_all, s->ipiv_lap, s->dw_rmin, s->d2w_rmin,
-                  s->dw_rmax, s->d2w_rmax};
+                  s->dw_rmax, s->d2w_rmax, s->dtval_r, s->dtval_p};
   for (size_t i = 0; i < sizeof(ptrs) / sizeof(ptrs[0]); ++i) free(ptrs[i]);
   free(s);
 }
 
 int orc_sim_nstep(const orc_sim* s) { return s->n_step; }
+double orc_sim_dt(const orc_sim* s) { return s->dt_new; }
 
 /* splitmix64 stream keyed by (seed, m, i) -> two standard normals (Box-Muller). */
 static uint64_t splitmix64(uint64_t* x) {
@@ -991,6 +994,16 @@ static void nr_maxloop(orc_sim* s) {
                 s->ur + (size_t)P * r, CX(s->uphi_temp_FR, 0, r), CX(s->ur_temp_FR, 0, r),
                 CX(s->uphi_omg_FR, 0, r), CX(s->ur_omg_FR, 0, r), work);
   free(work);
+  /* get_dtvals (src/nonlin.F90:93-106): advective time scales per radius */
+  for (int r = 0; r < R; ++r) {
+    double mr = 0.0, mp = 0.0;
+    for (int j = 0; j < P; ++j) {
+      mr = fmax(mr, fabs(s->ur[j + (size_t)P * r]));
+      mp = fmax(mp, fabs(s->up[j + (size_t)P * r]));
+    }
+    s->dtval_r[r] = s->dr[r] / mr;
+    s->dtval_p[r] = (2.0 / 3.0) * (s->radius[r] * PI_) / ((double)Nm * mp);
+  }
 }
 
 /* gather / scatter one mode's radial vector */
@@ -1215,6 +1228,34 @@ static void rhs_construct_uphi_bar(orc_sim* s, int n_step, double dt, double* rh
   rhs_uphi[0] = 0.0; rhs_uphi[R - 1] = 0.0;
 }
 
+/* compute_new_dt of the multistep loop (src/steptime.F90:313-370), called
+ * from the second step on: the CFL time step from the last nonlinear pass,
+ * optionally changed only when needed (l_optimizedt), and the dt_array
+ * history shifted (n_order_tscheme_max = max(n_imp, n_exp)). */
+static void compute_new_dt_imex(orc_sim* s) {
+  const orc_params* p = &s->p;
+  int R = s->R;
+  double mr = s->dtval_r[0], mp = s->dtval_p[0];
+  for (int r = 1; r < R; ++r) { mr = fmin(mr, s->dtval_r[r]); mp = fmin(mp, s->dtval_p[r]); }
+  double dt_cal = fmin(mr, mp);
+  double dt_n;
+  if (p->pr == 1.0 || p->pr > 1.0) dt_n = fmax(1.0 / p->pr, 1.0) * p->cfl * dt_cal;
+  else dt_n = fmin(1.0 / p->pr, 1.0) * p->cfl * dt_cal;
+  double dt2 = fmin(0.5 * (1.0 / p->dt_coef + 1.0) * dt_n, p->dt_max);
+  if (p->l_optimizedt) {
+    /* dt_new keeps its previous value when no branch applies */
+    if (s->dt_array[1] > p->dt_max) s->dt_new = p->dt_max;
+    else if (s->dt_array[1] >= dt_cal) s->dt_new = dt2;
+    else if (p->dt_coef * s->dt_array[1] < dt_cal && s->dt_array[1] < p->dt_max)
+      s->dt_new = (s->dt_array[0] < dt2) ? dt2 : s->dt_array[0];
+  } else {
+    s->dt_new = dt2;
+  }
+  int nmax = s->sch.n_imp > s->sch.n_exp ? s->sch.n_imp : s->sch.n_exp;
+  for (int i = nmax - 1; i >= 1; --i) s->dt_array[i] = s->dt_array[i - 1];
+  s->dt_array[0] = s->dt_new;
+}
+
 static void imex_step(orc_sim* s) {
   int R = s->R, M = s->M;
   int n_step = s->n_step + 1;
@@ -1225,8 +1266,12 @@ static void imex_step(orc_sim* s) {
     memcpy(s->upFR_prev, s->upFR, cf * sizeof(double));
     memcpy(s->urFR_prev, s->urFR, cf * sizeof(double));
   }
-  s->dt_new = s->p.dt;
-  for (int i = 0; i < 4; ++i) s->dt_array[i] = s->p.dt;
+  if (s->p.l_vartimestep && n_step > 1) {
+    compute_new_dt_imex(s);
+  } else {
+    s->dt_new = s->p.dt;
+    for (int i = 0; i < 4; ++i) s->dt_array[i] = s->p.dt;
+  }
   if (n_step > 1) {
     int ni = s->sch.n_imp, ne = s->sch.n_exp;
     memcpy(s->tmp_imp_temp, s->rhs_imp_temp, cf * ni * sizeof(double));
