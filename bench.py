@@ -216,7 +216,7 @@ def run_uneven(args, fg, stream, torch):
     b.set_stream(stream.cuda_stream)
     b.init_noise([s for _, s in reqs], 1e-3)
     with torch.cuda.stream(stream):
-        b.step(args.warmup)
+        b.step(gpu_warmup(args))
     torch.cuda.synchronize()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     l0 = fg.launch_count()
@@ -229,7 +229,7 @@ def run_uneven(args, fg, stream, torch):
     n = len(reqs)
     finite = sum(bool(np.isfinite(b.get_state(i)["T"]).all()) for i in range(n))
     out = {"value": n * args.uneven_steps / (ms / 1e3), "unit": "instance-steps/s", "instances": n,
-           "steps": args.uneven_steps, "warmup": args.warmup, "ms_per_step": ms / args.uneven_steps,
+           "steps": args.uneven_steps, "warmup": gpu_warmup(args), "ms_per_step": ms / args.uneven_steps,
            "operator_groups": b.ngroups, "device_bytes": b.device_bytes, "setup_s": setup_s,
            "gpu_launches": launches, "instances_finite": finite,
            "workload": "512 instances (seed 4): Nr {33,65,97,129}, Ntheta {128,256,512,1024,1536} (Nm=Ntheta//3), "
@@ -291,6 +291,13 @@ def run_serving(args, fg, torch):
                       f"({args.serve_horizon_scale:g} x [100, 20000]), device budget {args.serve_budget_gb} GB"}
 
 
+def gpu_warmup(args):
+    """Untimed steps before a GPU timing: at least W, and at least 5 so that
+    the step graph of every history phase (period <= 4) is captured before
+    the timed steps."""
+    return max(args.warmup, 5)
+
+
 def load_traffic(kernel):
     path = os.path.join(ROOT, "profiles", "traffic.json")
     try:
@@ -326,7 +333,7 @@ def run_gpu(args):
     b.set_stream(stream.cuda_stream)
     b.init_noise(seeds, W["amp"])
     with torch.cuda.stream(stream):
-        b.step(args.warmup)
+        b.step(gpu_warmup(args))
     torch.cuda.synchronize()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     launches0 = fg.launch_count()
@@ -405,7 +412,7 @@ def run_gpu(args):
         it.init_noise(seeds[k], W["amp"])
         insts.append(it)
     for it in insts:
-        it.step(2)
+        it.step(gpu_warmup(args))
     torch.cuda.synchronize()
     k1 = max(5, args.steps // 4)
     ev0.record(stream)
@@ -435,7 +442,7 @@ def run_gpu(args):
                          "CPU oracle with OpenMP over modes on all host threads"}
     line = {
         "metric": METRIC, "value": value, "unit": "instance-steps/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "warmup": gpu_warmup(args), "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": WORKLOAD_NAME, "instances_per_gpu": n, "nr": W["nr"], "nm": W["nm"],
                    "np": 3 * W["nm"], "scheme": W["scheme"], "dt": W["dt"],
