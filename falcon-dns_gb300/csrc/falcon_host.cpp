@@ -23,6 +23,7 @@
 
 #include "../../include/falcon_gpu.h"
 #include "falcon_internal.h"
+#include "imexrk_tables.h"
 
 using namespace falcon;
 
@@ -680,65 +681,19 @@ int scheme_weights(int type, int imp, int exp, Scheme* s) {
     return 0;
   }
   if (type == FALCON_IMEXRK) {
-    auto set = [&](int n, const double* aD, const double* bD, const double* aA, const double* bA) {
-      s->n_imp = n; s->n_exp = n;
-      for (int i = 0; i < n; ++i) {
-        for (int j = 0; j < n; ++j) { s->aD[i][j] = aD[i * n + j]; s->aA[i][j] = aA[i * n + j]; }
-        s->bD[i] = bD[i]; s->bA[i] = bA[i];
-      }
-      s->check_D = false; s->check_A = false;
-      for (int i = 0; i < n; ++i) if (s->aD[n - 1][i] == s->bD[i]) s->check_D = true;
-      for (int i = 0; i < n; ++i) if (s->aA[n - 1][i] == s->bA[i]) s->check_A = true;
-    };
-    switch (imp) {
-      case FALCON_IMP_ARS443: {  // src/timeschemes.F90:1215-1233, :1919-1940
-        if (exp != FALCON_EXP_ARS443) return -1;
-        const double aD[25] = {0, 0, 0, 0, 0, 0, 0.5, 0, 0, 0, 0, 1.0 / 6.0, 0.5, 0, 0,
-                               0, -0.5, 0.5, 0.5, 0, 0, 1.5, -1.5, 0.5, 0.5};
-        const double bD[5] = {0, 1.5, -1.5, 0.5, 0.5};
-        const double aA[25] = {0, 0, 0, 0, 0, 0.5, 0, 0, 0, 0, 11.0 / 18.0, 1.0 / 18.0, 0, 0, 0,
-                               5.0 / 6.0, -5.0 / 6.0, 0.5, 0, 0, 0.25, 7.0 / 4.0, 0.75, -7.0 / 4.0, 0};
-        const double bA[5] = {0.25, 7.0 / 4.0, 0.75, -7.0 / 4.0, 0};
-        set(5, aD, bD, aA, bA);
-        return 0;
-      }
-      case FALCON_IMP_BPR353: {  // :1277-1295, :1995-2015
-        if (exp != FALCON_EXP_BPR353) return -1;
-        const double aD[25] = {0, 0, 0, 0, 0, 0.5, 0.5, 0, 0, 0, 5.0 / 18.0, -1.0 / 9.0, 0.5, 0, 0,
-                               0.5, 0, 0, 0.5, 0, 0.25, 0, 0.75, -0.5, 0.5};
-        const double bD[5] = {0.25, 0, 0.75, -0.5, 0.5};
-        const double aA[25] = {0, 0, 0, 0, 0, 1.0, 0, 0, 0, 0, 4.0 / 9.0, 2.0 / 9.0, 0, 0, 0,
-                               0.25, 0, 0.75, 0, 0, 0.25, 0, 0.75, 0, 0};
-        const double bA[5] = {0.25, 0, 0.75, 0, 0};
-        set(5, aD, bD, aA, bA);
-        return 0;
-      }
-      case FALCON_IMP_ARS343: {  // :1107-1120, :1788-1804
-        if (exp != FALCON_EXP_ARS343) return -1;
-        const double g = 0.435866521508459;
-        const double bb1 = -1.5 * g * g + 4.0 * g - 0.25, bb2 = 1.5 * g * g - 5.0 * g + 1.25;
-        const double aD[16] = {0, 0, 0, 0, 0, g, 0, 0, 0, 0.5 * (1.0 - g), g, 0, 0, bb1, bb2, g};
-        const double bD[4] = {0, bb1, bb2, g};
-        const double aA[16] = {0, 0, 0, 0, g, 0, 0, 0, 0.3212788860286278, 0.3966543747256017, 0, 0,
-                               -0.1058582960718797, 0.5529291480359398, 0.5529291480359398, 0};
-        const double bA[4] = {0, bb1, bb2, g};
-        set(4, aD, bD, aA, bA);
-        s->check_D = true; s->check_A = false;  // set explicitly by the reference (:1117, :1802)
-        return 0;
-      }
-      case FALCON_IMP_ARS222: {  // :1065-1078, :1737-1751
-        if (exp != FALCON_EXP_ARS222) return -1;
-        const double g = (2.0 - std::sqrt(2.0)) / 2.0, dl = 1.0 - 1.0 / g / 2.0;
-        const double aD[9] = {0, 0, 0, 0, g, 0, 0, 1.0 - g, g};
-        const double bD[3] = {0, 1.0 - g, g};
-        const double aA[9] = {0, 0, 0, g, 0, 0, dl, 1.0 - dl, 0};
-        const double bA[3] = {dl, 1.0 - dl, 0};
-        set(3, aD, bD, aA, bA);
-        s->check_D = true; s->check_A = true;
-        return 0;
-      }
-      default: return -1;
+    // Butcher tables and the reference's ars_eqn_check / diag_index flags
+    // (imexrk_tables.h); stage-dependent implicit diagonals (diag_diff) and
+    // schemes with more than kMaxStages stages are not built.
+    imexrk_table t;
+    if (imexrk_table_get(imp, exp, &t) != 0 || t.diag_diff || t.n > kMaxStages) return -1;
+    s->n_imp = s->n_exp = t.n;
+    for (int i = 0; i < t.n; ++i) {
+      for (int j = 0; j < t.n; ++j) { s->aD[i][j] = t.aD[i][j]; s->aA[i][j] = t.aA[i][j]; }
+      s->bD[i] = t.bD[i]; s->bA[i] = t.bA[i];
     }
+    s->check_D = t.check_D != 0; s->check_A = t.check_A != 0;
+    s->diag = t.diag_index - 1;
+    return 0;
   }
   return -1;
 }
@@ -883,7 +838,12 @@ int validate(const falcon_params& p) {
   if (p.l_restart) return fail(FALCON_EINVAL, "l_restart=.TRUE. is not supported by this build");
   Scheme s;
   if (scheme_weights(p.scheme_type, p.scheme_imp, p.scheme_exp, &s) != 0)
+  {
+    if (p.scheme_type == FALCON_IMEXRK && p.scheme_imp >= FALCON_IMP_KC774 && p.scheme_imp <= FALCON_IMP_LZ4A1)
+      return fail(FALCON_EINVAL, "IMEXRK schemes with 7-8 stages (KC774, KC885) or a stage-dependent implicit "
+                                 "diagonal (SMR333, CB3e, CB3f, CB4, LZ3L1, LZ3A4a, LZ4A1) are not supported by this build");
     return fail(FALCON_EINVAL, "unsupported time scheme combination");
+  }
   return 0;
 }
 
@@ -1744,16 +1704,16 @@ struct falcon_handle {
 
 static int batch_create(const falcon_params* ps, int n, falcon_batch** out) {
   if (!ps || n <= 0 || !out) return fail(FALCON_EINVAL, "invalid batch arguments");
+  for (int i = 0; i < n; ++i) {
+    int rc = validate(ps[i]);
+    if (rc) return rc;
+  }
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
     return fail(FALCON_ECUDA, "no CUDA device: the GB300 library has no CPU fallback");
   CK(init_dft_tables());
   std::unique_ptr<falcon_batch> b(new falcon_batch());
   b->params.assign(ps, ps + n);
-  for (int i = 0; i < n; ++i) {
-    int rc = validate(ps[i]);
-    if (rc) return rc;
-  }
   CK(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
   b->own_stream = true;
   std::map<OpKey, std::vector<int>> byk;
@@ -1830,18 +1790,22 @@ int falcon_params_set_scheme(falcon_params* p, const char* type, const char* imp
   else return fail(FALCON_EINVAL, "unknown time_scheme_type " + t);
   static const std::map<std::string, int> imps = {
       {"CN", FALCON_IMP_CN}, {"BDF2", FALCON_IMP_BDF2}, {"BDF3", FALCON_IMP_BDF3}, {"BDF4", FALCON_IMP_BDF4},
-      {"ARS443", FALCON_IMP_ARS443}, {"ARS343", FALCON_IMP_ARS343}, {"BPR353", FALCON_IMP_BPR353},
-      {"ARS222", FALCON_IMP_ARS222}, {"NONE", FALCON_IMP_NONE}};
+      {"NONE", FALCON_IMP_NONE}};
   static const std::map<std::string, int> exps = {
       {"AB2", FALCON_EXP_AB2}, {"AB3", FALCON_EXP_AB3}, {"AB4", FALCON_EXP_AB4},
-      {"EXPARS443", FALCON_EXP_ARS443}, {"EXPARS343", FALCON_EXP_ARS343}, {"EXPBPR353", FALCON_EXP_BPR353},
-      {"EXPARS222", FALCON_EXP_ARS222}, {"RK2", FALCON_EXP_RK2}, {"RK4", FALCON_EXP_RK4}};
+      {"RK2", FALCON_EXP_RK2}, {"RK4", FALCON_EXP_RK4}};
+  // IMEXRK pairs: "XXX" / "expXXX" (src/timeschemes.F90:186-962)
+  int ii = -1, ie = -1;
   auto a = imps.find(i);
   auto b = exps.find(e);
-  if (a == imps.end()) return fail(FALCON_EINVAL, "unknown time_scheme_imp " + i);
-  if (b == exps.end()) return fail(FALCON_EINVAL, "unknown time_scheme_exp " + e);
-  p->scheme_imp = a->second;
-  p->scheme_exp = b->second;
+  if (a != imps.end()) ii = a->second;
+  else ii = imexrk_scheme_id(i.c_str());
+  if (b != exps.end()) ie = b->second;
+  else if (e.compare(0, 3, "EXP") == 0) ie = imexrk_scheme_id(e.c_str() + 3);
+  if (ii < 0) return fail(FALCON_EINVAL, "unknown time_scheme_imp " + i);
+  if (ie < 0) return fail(FALCON_EINVAL, "unknown time_scheme_exp " + e);
+  p->scheme_imp = ii;
+  p->scheme_exp = ie;
   return 0;
 }
 

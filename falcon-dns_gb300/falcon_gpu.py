@@ -37,6 +37,14 @@ SCHEMES = {
     "RK2": ("RK", "NONE", "RK2"),
     "RK4": ("RK", "NONE", "RK4"),
 }
+# IMEXRK pairs "XXX" / "expXXX" (same number for both halves)
+IMEXRK_IDS = {"ARS232": 14, "ARS233": 15, "EUL111": 30, "MARS343": 31, "IJ3": 32, "PC2": 33, "SSP332": 34,
+              "SSP543": 35, "PR433": 36, "DBM453": 37, "KC343": 38, "KC564": 39, "FW53": 40, "CK222": 41,
+              "BPR442": 42, "CFN343": 43, "BHR553": 44, "CFN564": 45}
+for _n, _i in IMEXRK_IDS.items():
+    IMP[_n] = _i
+    EXP["exp" + _n] = _i
+    SCHEMES[_n] = ("IMEXRK", _n, "exp" + _n)
 
 
 class FalconParams(ctypes.Structure):

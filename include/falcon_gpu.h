@@ -45,15 +45,34 @@ extern "C" {
 
 /* ---- scheme identifiers (namelist strings, src/timeschemes.F90:42-962) ---- */
 enum falcon_scheme_type { FALCON_IMEX = 0, FALCON_IMEXRK = 1, FALCON_RK = 2 };
+/* IMEXRK pairs use the same number for "XXX" (implicit) and "expXXX"
+ * (explicit).  KC774, KC885 and the schemes whose implicit diagonal changes
+ * by stage (SMR333, CB3e, CB3f, CB4, LZ3L1, LZ3A4a, LZ4A1) are recognised
+ * and rejected at creation. */
 enum falcon_scheme_imp {
   FALCON_IMP_CN = 0, FALCON_IMP_BDF2 = 1, FALCON_IMP_BDF3 = 2, FALCON_IMP_BDF4 = 3,
   FALCON_IMP_ARS443 = 10, FALCON_IMP_ARS343 = 11, FALCON_IMP_BPR353 = 12,
-  FALCON_IMP_ARS222 = 13, FALCON_IMP_NONE = 20
+  FALCON_IMP_ARS222 = 13, FALCON_IMP_ARS232 = 14, FALCON_IMP_ARS233 = 15, FALCON_IMP_NONE = 20,
+  FALCON_IMP_EUL111 = 30, FALCON_IMP_MARS343 = 31, FALCON_IMP_IJ3 = 32, FALCON_IMP_PC2 = 33,
+  FALCON_IMP_SSP332 = 34, FALCON_IMP_SSP543 = 35, FALCON_IMP_PR433 = 36, FALCON_IMP_DBM453 = 37,
+  FALCON_IMP_KC343 = 38, FALCON_IMP_KC564 = 39, FALCON_IMP_FW53 = 40, FALCON_IMP_CK222 = 41,
+  FALCON_IMP_BPR442 = 42, FALCON_IMP_CFN343 = 43, FALCON_IMP_BHR553 = 44, FALCON_IMP_CFN564 = 45,
+  FALCON_IMP_KC774 = 46, FALCON_IMP_KC885 = 47, FALCON_IMP_SMR333 = 48, FALCON_IMP_CB3E = 49,
+  FALCON_IMP_CB3F = 50, FALCON_IMP_CB4 = 51, FALCON_IMP_LZ3L1 = 52, FALCON_IMP_LZ3A4A = 53,
+  FALCON_IMP_LZ4A1 = 54
 };
 enum falcon_scheme_exp {
   FALCON_EXP_AB2 = 0, FALCON_EXP_AB3 = 1, FALCON_EXP_AB4 = 2,
   FALCON_EXP_ARS443 = 10, FALCON_EXP_ARS343 = 11, FALCON_EXP_BPR353 = 12,
-  FALCON_EXP_ARS222 = 13, FALCON_EXP_RK2 = 20, FALCON_EXP_RK4 = 21
+  FALCON_EXP_ARS222 = 13, FALCON_EXP_ARS232 = 14, FALCON_EXP_ARS233 = 15,
+  FALCON_EXP_RK2 = 20, FALCON_EXP_RK4 = 21,
+  FALCON_EXP_EUL111 = 30, FALCON_EXP_MARS343 = 31, FALCON_EXP_IJ3 = 32, FALCON_EXP_PC2 = 33,
+  FALCON_EXP_SSP332 = 34, FALCON_EXP_SSP543 = 35, FALCON_EXP_PR433 = 36, FALCON_EXP_DBM453 = 37,
+  FALCON_EXP_KC343 = 38, FALCON_EXP_KC564 = 39, FALCON_EXP_FW53 = 40, FALCON_EXP_CK222 = 41,
+  FALCON_EXP_BPR442 = 42, FALCON_EXP_CFN343 = 43, FALCON_EXP_BHR553 = 44, FALCON_EXP_CFN564 = 45,
+  FALCON_EXP_KC774 = 46, FALCON_EXP_KC885 = 47, FALCON_EXP_SMR333 = 48, FALCON_EXP_CB3E = 49,
+  FALCON_EXP_CB3F = 50, FALCON_EXP_CB4 = 51, FALCON_EXP_LZ3L1 = 52, FALCON_EXP_LZ3A4A = 53,
+  FALCON_EXP_LZ4A1 = 54
 };
 
 /* Namelist scalars of src/namelists.F90:52-58 (&grid, &physics,

@@ -102,6 +102,9 @@ int orc_sim_nstep(const orc_sim* s);
 double orc_sim_dt(const orc_sim* s);
 /* Host seeded-noise generator shared by the kind-1 initial state. */
 void orc_noise_pair(uint64_t seed, int m, int i, double* a, double* b);
+/* IMEXRK table of scheme number `scheme` (see imexrk_tables.h): out = n,
+ * aD (n x n, row-major), bD, aA, bA, check_D, check_A, diag_index. */
+int orc_imexrk_table(int scheme, double* out);
 /* Number of OpenMP threads the oracle uses (0 = runtime default). */
 void orc_set_threads(int n);
 

@@ -18,6 +18,7 @@
 #endif
 
 #include "oracle.h"
+#include "imexrk_tables.h"
 
 #define PI_ (4.0 * atan(1.0))
 
@@ -440,66 +441,35 @@ static int set_rows(double a[6][6], int n, const double* v) {
 
 /* Butcher pairs: init_time_schemes src/timeschemes.F90:37-973 (stage counts),
  * rhs_update_wts_imp :1053-1612 and rhs_update_wts_exp :1733-2388. */
+/* IMEXRK Butcher tables (src/timeschemes.F90) from the shared table of
+ * published coefficients; schemes with a stage-dependent implicit diagonal
+ * (diag_diff) or more than 6 stages are not supported. */
 static int butcher_tables(const orc_params* p, scheme_t* s) {
+  imexrk_table t;
   memset(s->aD, 0, sizeof(s->aD)); memset(s->aA, 0, sizeof(s->aA));
   memset(s->bD, 0, sizeof(s->bD)); memset(s->bA, 0, sizeof(s->bA));
-  s->check_A = 0; s->check_D = 0; s->diag_index = 1;
-  int n = 0;
-  switch (p->scheme_imp) {
-    case ORC_IMP_ARS222: { /* :1078-1091, exp :1752-1769 */
-      double g = (2.0 - sqrt(2.0)) / 2.0, d = 1.0 - 1.0 / g / 2.0;
-      n = 3;
-      double aD[9] = {0, 0, 0, 0, g, 0, 0, 1.0 - g, g};
-      double bD[3] = {0, 1.0 - g, g};
-      double aA[9] = {0, 0, 0, g, 0, 0, d, 1.0 - d, 0};
-      double bA[3] = {d, 1.0 - d, 0};
-      set_rows(s->aD, 3, aD); set_rows(s->aA, 3, aA);
-      memcpy(s->bD, bD, sizeof(bD)); memcpy(s->bA, bA, sizeof(bA));
-      s->check_D = 1; s->check_A = 1;
-    } break;
-    case ORC_IMP_ARS343: { /* :1107-1120, exp :1788-1804 */
-      double g = 0.435866521508459;
-      double bb1 = -1.5 * g * g + 4.0 * g - 0.25, bb2 = 1.5 * g * g - 5.0 * g + 1.25;
-      n = 4;
-      double aD[16] = {0, 0, 0, 0, 0, g, 0, 0, 0, 0.5 * (1.0 - g), g, 0, 0, bb1, bb2, g};
-      double bD[4] = {0, bb1, bb2, g};
-      double aA[16] = {0, 0, 0, 0, g, 0, 0, 0, 0.3212788860286278, 0.3966543747256017, 0, 0,
-                       -0.1058582960718797, 0.5529291480359398, 0.5529291480359398, 0};
-      double bA[4] = {0, bb1, bb2, g};
-      set_rows(s->aD, 4, aD); set_rows(s->aA, 4, aA);
-      memcpy(s->bD, bD, sizeof(bD)); memcpy(s->bA, bA, sizeof(bA));
-      s->check_D = 1; s->check_A = 0;
-    } break;
-    case ORC_IMP_ARS443: { /* :1215-1233, exp :1919-1940 */
-      n = 5;
-      double aD[25] = {0, 0, 0, 0, 0, 0, 0.5, 0, 0, 0, 0, 1.0 / 6.0, 0.5, 0, 0,
-                       0, -0.5, 0.5, 0.5, 0, 0, 1.5, -1.5, 0.5, 0.5};
-      double bD[5] = {0, 1.5, -1.5, 0.5, 0.5};
-      double aA[25] = {0, 0, 0, 0, 0, 0.5, 0, 0, 0, 0, 11.0 / 18.0, 1.0 / 18.0, 0, 0, 0,
-                       5.0 / 6.0, -5.0 / 6.0, 0.5, 0, 0, 0.25, 7.0 / 4.0, 0.75, -7.0 / 4.0, 0};
-      double bA[5] = {0.25, 7.0 / 4.0, 0.75, -7.0 / 4.0, 0};
-      set_rows(s->aD, 5, aD); set_rows(s->aA, 5, aA);
-      memcpy(s->bD, bD, sizeof(bD)); memcpy(s->bA, bA, sizeof(bA));
-      for (int i = 0; i < 5; ++i) if (s->aD[4][i] == s->bD[i]) s->check_D = 1;
-      for (int i = 0; i < 5; ++i) if (s->aA[4][i] == s->bA[i]) s->check_A = 1;
-    } break;
-    case ORC_IMP_BPR353: { /* :1277-1295, exp :1995-2015 */
-      n = 5;
-      double aD[25] = {0, 0, 0, 0, 0, 0.5, 0.5, 0, 0, 0, 5.0 / 18.0, -1.0 / 9.0, 0.5, 0, 0,
-                       0.5, 0, 0, 0.5, 0, 0.25, 0, 0.75, -0.5, 0.5};
-      double bD[5] = {0.25, 0, 0.75, -0.5, 0.5};
-      double aA[25] = {0, 0, 0, 0, 0, 1.0, 0, 0, 0, 0, 4.0 / 9.0, 2.0 / 9.0, 0, 0, 0,
-                       0.25, 0, 0.75, 0, 0, 0.25, 0, 0.75, 0, 0};
-      double bA[5] = {0.25, 0, 0.75, 0, 0};
-      set_rows(s->aD, 5, aD); set_rows(s->aA, 5, aA);
-      memcpy(s->bD, bD, sizeof(bD)); memcpy(s->bA, bA, sizeof(bA));
-      for (int i = 0; i < 5; ++i) if (s->aD[4][i] == s->bD[i]) s->check_D = 1;
-      for (int i = 0; i < 5; ++i) if (s->aA[4][i] == s->bA[i]) s->check_A = 1;
-    } break;
-    default:
-      return -1;
+  if (imexrk_table_get(p->scheme_imp, p->scheme_exp, &t) != 0 || t.diag_diff || t.n > 6) return -1;
+  for (int i = 0; i < t.n; ++i) {
+    for (int j = 0; j < t.n; ++j) { s->aD[i][j] = t.aD[i][j]; s->aA[i][j] = t.aA[i][j]; }
+    s->bD[i] = t.bD[i]; s->bA[i] = t.bA[i];
   }
-  s->n_imp = n; s->n_exp = n;
+  s->check_A = t.check_A; s->check_D = t.check_D; s->diag_index = t.diag_index - 1;
+  s->n_imp = t.n; s->n_exp = t.n;
+  return 0;
+}
+
+/* Exported for the table tests: n, then aD (n x n), bD, aA, bA, then
+ * check_D, check_A, diag_index (1-based); returns -1 if not built. */
+int orc_imexrk_table(int scheme, double* out) {
+  imexrk_table t;
+  if (imexrk_table_get(scheme, scheme, &t) != 0) return -1;
+  int n = t.n, k = 0;
+  out[k++] = n;
+  for (int i = 0; i < n; ++i) for (int j = 0; j < n; ++j) out[k++] = t.aD[i][j];
+  for (int i = 0; i < n; ++i) out[k++] = t.bD[i];
+  for (int i = 0; i < n; ++i) for (int j = 0; j < n; ++j) out[k++] = t.aA[i][j];
+  for (int i = 0; i < n; ++i) out[k++] = t.bA[i];
+  out[k++] = t.check_D; out[k++] = t.check_A; out[k++] = t.diag_index;
   return 0;
 }
 
