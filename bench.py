@@ -228,14 +228,46 @@ def run_uneven(args, fg, stream, torch):
     launches = fg.launch_count() - l0
     n = len(reqs)
     finite = sum(bool(np.isfinite(b.get_state(i)["T"]).all()) for i in range(n))
+    # FLOP of one step of every group from the launch-level model (GEMM,
+    # FFT and elementwise counts of each launch), against the step time
+    prof = b.profile(1)
+    step_flops = sum(v["flops"] for v in prof.values())
     out = {"value": n * args.uneven_steps / (ms / 1e3), "unit": "instance-steps/s", "instances": n,
            "steps": args.uneven_steps, "warmup": gpu_warmup(args), "ms_per_step": ms / args.uneven_steps,
            "operator_groups": b.ngroups, "device_bytes": b.device_bytes, "setup_s": setup_s,
            "gpu_launches": launches, "instances_finite": finite,
+           "gflop_per_step": step_flops / 1e9, "tflops": step_flops / (ms / args.uneven_steps / 1e3) / 1e12,
            "workload": "512 instances (seed 4): Nr {33,65,97,129}, Ntheta {128,256,512,1024,1536} (Nm=Ntheta//3), "
                        "scheme {CNAB2,SBDF3,ARS343,BPR353}, Ra log-uniform [1e5,1e8], Pr {0.1,1,10}, "
                        "dt = 0.2 x CFL estimate, FP64"}
     b.close()
+    return out
+
+
+def run_single(args, fg, stream, torch):
+    """The single larger instance: Nr=97, Ntheta=1024 (Nm=341, Np=1023),
+    ARS443, dt=2e-7, Ra=1e8, Pr=1, seed 2; steps of one instance (latency)."""
+    p = fg.make_params(97, 341, "ARS443", ra=1e8, dt=2e-7, pr=1.0)
+    it = fg.Instance(p)
+    it.set_stream(stream.cuda_stream)
+    it.init_noise(2, 1e-3)
+    with torch.cuda.stream(stream):
+        it.step(gpu_warmup(args))
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    k = args.single_steps
+    ev0.record(stream)
+    it.step(k)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    prof = it.profile(1)
+    flops = sum(v["flops"] for v in prof.values())
+    out = {"value": k / (ms / 1e3), "unit": "instance-steps/s", "steps": k, "ms_per_step": ms / k,
+           "tflops": flops / (ms / k / 1e3) / 1e12, "state_finite": bool(np.isfinite(it.get_state()["T"]).all()),
+           "classes": {c: {"ms_per_step": v["ms"], "launches_per_step": v["launches"]} for c, v in prof.items()},
+           "workload": "single instance Nr=97, Ntheta=1024 (Nm=341, Np=1023), ARS443, dt=2e-7, Ra=1e8, Pr=1, seed 2"}
+    it.close()
     return out
 
 
@@ -426,6 +458,7 @@ def run_gpu(args):
         it.close()
 
     uneven = serving = None
+    single = run_single(args, fg, stream, torch)
     if not args.no_mixed:
         uneven = run_uneven(args, fg, stream, torch)
         serving = run_serving(args, fg, torch)
@@ -451,6 +484,7 @@ def run_gpu(args):
         "one_at_a_time": {"value": one_rate, "unit": "instance-steps/s", "instances": n1, "steps": k1,
                           "batched_over_one_at_a_time": value / world / one_rate},
         "e2e": e2e,
+        "single_instance": single,
         "uneven_batch": uneven,
         "serving": serving,
         "roofline": roofline,
@@ -476,6 +510,7 @@ def main():
     ap.add_argument("--cpu-seconds", dest="cpu_seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", dest="no_cpu", action="store_true")
     ap.add_argument("--no-mixed", dest="no_mixed", action="store_true", help="skip the uneven batch and serving")
+    ap.add_argument("--single-steps", dest="single_steps", type=int, default=200)
     ap.add_argument("--uneven-instances", dest="uneven_instances", type=int, default=512)
     ap.add_argument("--uneven-steps", dest="uneven_steps", type=int, default=100)
     ap.add_argument("--serve-rate", dest="serve_rate", type=float, default=50.0)

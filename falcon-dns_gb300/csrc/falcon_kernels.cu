@@ -129,17 +129,18 @@ __device__ __forceinline__ void dft_odd_store(double2 (&v)[p], double2* __restri
   }
 }
 
-// One in-place stage of radix p and span m on NB (1 or 2) buffers.
+// One in-place stage of radix p and span m on NB (1 or 2) buffers, its
+// butterflies shared by nl cooperating lanes (lane < nl).
 // DIT (dif = false): twiddles exp(-2 pi i q k / (m p)) on the inputs; DIF:
 // on the outputs; none for the prime-factor plan (twid = false).
 // tw[k] = exp(-2 pi i k / P); stride = P / (m p).
 template <int p, int NB>
 __device__ __forceinline__ void fft_stage(double2* __restrict__ A, double2* __restrict__ Bf, int P, int m,
-                                          int stride, const double2* __restrict__ tw, int lane, bool dif,
+                                          int stride, const double2* __restrict__ tw, int lane, int nl, bool dif,
                                           bool twid) {
   const int mp = m * p, nb = P / p;
   const float inv_m = 1.0f / (float)m;
-  for (int t = lane; t < nb; t += 32) {
+  for (int t = lane; t < nb; t += nl) {
     const int g = (int)(((float)t + 0.5f) * inv_m);
     const int k = t - g * m;
     const int base = g * mp + k;
@@ -183,14 +184,15 @@ __device__ __forceinline__ void fft_stage(double2* __restrict__ A, double2* __re
 }
 
 // Generic prime radix (p <= 64) with coefficients read from the P-point
-// twiddle table: exp(-2 pi i j/p) = tw[j * P/p].
+// twiddle table: exp(-2 pi i j/p) = tw[j * P/p].  Bf may be null (one buffer).
 __device__ void generic_stage(double2* A, double2* Bf, int P, int p, int m, int stride,
-                              const double2* tw, int lane, bool dif, bool twid) {
+                              const double2* tw, int lane, int nl, bool dif, bool twid) {
   const int mp = m * p, nb = P / p, tp = P / p;
-  for (int t = lane; t < nb; t += 32) {
+  double2* B2 = Bf ? Bf : A;  // with one buffer the second transform is a repeat, not stored
+  for (int t = lane; t < nb; t += nl) {
     const int g = t / m, k = t - g * m, base = g * mp + k;
     double2 va[64], vb[64], ya[64], yb[64];
-    for (int q = 0; q < p; ++q) { va[q] = A[base + q * m]; vb[q] = Bf[base + q * m]; }
+    for (int q = 0; q < p; ++q) { va[q] = A[base + q * m]; vb[q] = B2[base + q * m]; }
     if (twid && !dif && k > 0)
       for (int q = 1; q < p; ++q) { double2 w = tw[q * k * stride]; va[q] = cmul(va[q], w); vb[q] = cmul(vb[q], w); }
     for (int j = 0; j < p; ++j) {
@@ -203,7 +205,10 @@ __device__ void generic_stage(double2* A, double2* Bf, int P, int p, int m, int 
     }
     if (twid && dif && k > 0)
       for (int q = 1; q < p; ++q) { double2 w = tw[q * k * stride]; ya[q] = cmul(ya[q], w); yb[q] = cmul(yb[q], w); }
-    for (int q = 0; q < p; ++q) { A[base + q * m] = ya[q]; Bf[base + q * m] = yb[q]; }
+    for (int q = 0; q < p; ++q) {
+      A[base + q * m] = ya[q];
+      if (Bf) Bf[base + q * m] = yb[q];
+    }
   }
 }
 
@@ -214,14 +219,14 @@ __device__ __forceinline__ void run_stage(int p, bool dif, bool twid, double2* A
                                           int stride, const double2* tw, int lane) {
   // two buffers interleaved up to radix 7; one at a time above, to bound
   // the live registers of the butterfly
-#define FALCON_CASE2(q) case q: fft_stage<q, 2>(A, Bf, P, m, stride, tw, lane, dif, twid); return;
-#define FALCON_CASE1(q)                                                  \
-  case q:                                                                \
-    if constexpr (q <= MAXP) {                                           \
-      fft_stage<q, 1>(A, nullptr, P, m, stride, tw, lane, dif, twid);    \
-      fft_stage<q, 1>(Bf, nullptr, P, m, stride, tw, lane, dif, twid);   \
-      return;                                                            \
-    }                                                                    \
+#define FALCON_CASE2(q) case q: fft_stage<q, 2>(A, Bf, P, m, stride, tw, lane, 32, dif, twid); return;
+#define FALCON_CASE1(q)                                                      \
+  case q:                                                                    \
+    if constexpr (q <= MAXP) {                                               \
+      fft_stage<q, 1>(A, nullptr, P, m, stride, tw, lane, 32, dif, twid);    \
+      fft_stage<q, 1>(Bf, nullptr, P, m, stride, tw, lane, 32, dif, twid);   \
+      return;                                                                \
+    }                                                                        \
     break;
   switch (p) {
     FALCON_CASE2(2) FALCON_CASE2(3) FALCON_CASE2(4) FALCON_CASE2(5) FALCON_CASE2(7)
@@ -231,7 +236,28 @@ __device__ __forceinline__ void run_stage(int p, bool dif, bool twid, double2* A
   }
 #undef FALCON_CASE1
 #undef FALCON_CASE2
-  generic_stage(A, Bf, P, p, m, stride, tw, lane, dif, twid);
+  generic_stage(A, Bf, P, p, m, stride, tw, lane, 32, dif, twid);
+}
+
+// One buffer, its butterflies shared by nl lanes (the block-per-line form).
+template <int MAXP>
+__device__ __forceinline__ void run_stage1(int p, bool dif, bool twid, double2* A, int P, int m, int stride,
+                                           const double2* tw, int lane, int nl) {
+#define FALCON_CASE(q)                                                   \
+  case q:                                                                \
+    if constexpr (q <= MAXP) {                                           \
+      fft_stage<q, 1>(A, nullptr, P, m, stride, tw, lane, nl, dif, twid); \
+      return;                                                            \
+    }                                                                    \
+    break;
+  switch (p) {
+    FALCON_CASE(2) FALCON_CASE(3) FALCON_CASE(4) FALCON_CASE(5) FALCON_CASE(7)
+    FALCON_CASE(11) FALCON_CASE(13) FALCON_CASE(17) FALCON_CASE(19) FALCON_CASE(23)
+    FALCON_CASE(29) FALCON_CASE(31)
+    default: break;
+  }
+#undef FALCON_CASE
+  generic_stage(A, nullptr, P, p, m, stride, tw, lane, nl, dif, twid);
 }
 
 // ---------------------------------------------------------------------------
@@ -335,6 +361,104 @@ __global__ void __launch_bounds__(128) nonlin_kernel(NonlinArgs a) {
   }
 }
 
+// Block-per-line form of the same pass, for launches with too few radial
+// lines to fill the GPU at one warp per line (one instance, or a small
+// group): the (T, omega) and (u_phi, u_r) transforms run on the two halves of
+// the block, each spread over S warps, with block barriers between stages.
+// Same arithmetic per element as nonlin_kernel (bit-identical results).
+template <int MAXP, int S>
+__global__ void __launch_bounds__(64 * S) nonlin_line_kernel(NonlinArgs a) {
+  extern __shared__ double2 smem[];
+  __shared__ double red[2][2 * S];
+  const int P = a.plan.P;
+  double2* tw = smem;
+  int* pos = reinterpret_cast<int*>(smem + P);
+  const int pos_pad = (P + 3) / 4;
+  double2* bufA = smem + P + pos_pad;
+  double2* bufB = bufA + P;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int nl = 32 * S, half = tid / nl, hl = tid - half * nl;
+  double2* mine = half ? bufB : bufA;
+  for (int i = tid; i < P; i += nt) {
+    tw[i] = a.tw[i];
+    pos[i] = a.pos[i];
+    bufA[i] = make_double2(0, 0);
+    bufB[i] = make_double2(0, 0);
+  }
+  __syncthreads();
+  const int line = blockIdx.x;
+  const int r = line / a.B, b = line - r * a.B;
+  const int M = a.M, B = a.B, Nm = a.Nm;
+  const size_t row = (size_t)r * M * B + b;
+  for (int k = tid; k <= Nm; k += nt) {
+    const size_t e = row + (size_t)k * B;
+    const double2 T = a.t[e], W = a.w[e], U = a.up[e], V = a.ur[e];
+    if (k == 0) {
+      bufA[pos[0]] = make_double2(T.x, -W.x);
+      bufB[pos[0]] = make_double2(U.x, -V.x);
+    } else {
+      bufA[pos[k]] = make_double2(T.x - W.y, -(T.y + W.x));
+      bufA[pos[P - k]] = make_double2(T.x + W.y, T.y - W.x);
+      bufB[pos[k]] = make_double2(U.x - V.y, -(U.y + V.x));
+      bufB[pos[P - k]] = make_double2(U.x + V.y, U.y - V.x);
+    }
+  }
+  __syncthreads();
+  {
+    int m = 1;
+    for (int s = a.plan.nrad - 1; s >= 0; --s) {
+      const int p = a.plan.rad[s];
+      run_stage1<MAXP>(p, false, !a.plan.pfa, mine, P, m, P / (m * p), tw, hl, nl);
+      m *= p;
+      __syncthreads();
+    }
+  }
+  double urmax = 0.0, upmax = 0.0;
+  for (int j = tid; j < P; j += nt) {
+    const double2 za = bufA[j], zb = bufB[j];
+    const double tt = za.x, om = -za.y, up = zb.x, ur = -zb.y;
+    bufA[j] = make_double2(up * tt, ur * tt);
+    bufB[j] = make_double2(up * om, ur * om);
+    urmax = fmax(urmax, fabs(ur));
+    upmax = fmax(upmax, fabs(up));
+  }
+  __syncthreads();
+  {
+    int m = P;
+    for (int s = 0; s < a.plan.nrad; ++s) {
+      const int p = a.plan.rad[s];
+      m /= p;
+      run_stage1<MAXP>(p, true, !a.plan.pfa, mine, P, m, P / (m * p), tw, hl, nl);
+      __syncthreads();
+    }
+  }
+  const double sc = 0.5 / (double)P;
+  for (int k = tid; k <= Nm; k += nt) {
+    const size_t e = row + (size_t)k * B;
+    const double2 za = bufA[pos[k]], ca = bufA[pos[k == 0 ? 0 : P - k]];
+    const double2 zb = bufB[pos[k]], cb = bufB[pos[k == 0 ? 0 : P - k]];
+    a.ntp[e] = make_double2((za.x + ca.x) * sc, (za.y - ca.y) * sc);
+    a.ntr[e] = make_double2((za.y + ca.y) * sc, (ca.x - za.x) * sc);
+    a.nwp[e] = make_double2((zb.x + cb.x) * sc, (zb.y - cb.y) * sc);
+    a.nwr[e] = make_double2((zb.y + cb.y) * sc, (cb.x - zb.x) * sc);
+  }
+  if (a.umax) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      urmax = fmax(urmax, __shfl_xor_sync(0xffffffffu, urmax, o));
+      upmax = fmax(upmax, __shfl_xor_sync(0xffffffffu, upmax, o));
+    }
+    const int w = tid >> 5;
+    if ((tid & 31) == 0) { red[0][w] = urmax; red[1][w] = upmax; }
+    __syncthreads();
+    if (tid == 0) {
+      for (int i = 1; i < 2 * S; ++i) { urmax = fmax(urmax, red[0][i]); upmax = fmax(upmax, red[1][i]); }
+      a.umax[2 * ((size_t)r * B + b)] = urmax;
+      a.umax[2 * ((size_t)r * B + b) + 1] = upmax;
+    }
+  }
+}
+
 static int nonlin_warps(int P, int* smem_bytes) {
   int dev = 0, maxsm = 0;
   cudaGetDevice(&dev);
@@ -346,13 +470,31 @@ static int nonlin_warps(int P, int* smem_bytes) {
   return w;
 }
 
+template <int MAXP, int S>
+static cudaError_t launch_nonlin_line(const NonlinArgs& a, cudaStream_t s) {
+  const int P = a.plan.P;
+  const int smem = (P + (P + 3) / 4 + 2 * P) * 16;
+  cudaError_t e = cudaFuncSetAttribute(nonlin_line_kernel<MAXP, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return e;
+  nonlin_line_kernel<MAXP, S><<<a.R * a.B, 64 * S, smem, s>>>(a);
+  return cudaGetLastError();
+}
+
+// Lines that one warp each cannot spread over the GPU (fewer than two per
+// SM) go to the block-per-line form: 8 warps per line up to one line per
+// SM, 4 up to two.
 template <int MAXP>
 static cudaError_t launch_nonlin_t(const NonlinArgs& a, cudaStream_t s) {
+  int dev = 0, nsm = 152;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  const int nlines = a.R * a.B;
+  if (nlines <= nsm) return launch_nonlin_line<MAXP, 4>(a, s);
+  if (nlines <= 2 * nsm) return launch_nonlin_line<MAXP, 2>(a, s);
   int smem = 0;
   const int w = nonlin_warps(a.plan.P, &smem);
   cudaError_t e = cudaFuncSetAttribute(nonlin_kernel<MAXP>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return e;
-  const int nlines = a.R * a.B;
   const int grid = (nlines + w - 1) / w;
   nonlin_kernel<MAXP><<<grid, 32 * w, smem, s>>>(a);
   return cudaGetLastError();
