@@ -831,8 +831,6 @@ int validate(const falcon_params& p) {
   if (!(p.dt > 0.0) || !std::isfinite(p.dt)) return fail(FALCON_EINVAL, "dt must be positive");
   if (!(p.pr > 0.0)) return fail(FALCON_EINVAL, "Pr must be positive");
   if (p.mbc != 0 && p.mbc != 1) return fail(FALCON_EINVAL, "mBC must be NS or SF");
-  if (p.l_vartimestep && p.scheme_type != FALCON_IMEX)
-    return fail(FALCON_EINVAL, "l_vartimestep=.TRUE. is supported for IMEX multistep schemes only by this build");
   if (p.l_vartimestep && !(p.cfl > 0.0 && p.dt_coef > 0.0 && p.dt_max > 0.0))
     return fail(FALCON_EINVAL, "l_vartimestep needs CFL, dt_coef and dt_max > 0");
   if (p.l_restart) return fail(FALCON_EINVAL, "l_restart=.TRUE. is not supported by this build");
@@ -1012,35 +1010,46 @@ int solve_all(Group* g, double2* t_out, double2* w_out, double buo_scale, double
   });
 }
 
-// compute_new_dt of the multistep loop (src/steptime.F90:313-370) from the
-// get_dtvals time scales (src/nonlin.F90:93-106) of the last nonlinear
-// pass: the CFL step, optionally changed only when needed (l_optimizedt),
-// and the dt_array history shifted.  Before the second step, dt = the
-// namelist dt.
+// compute_new_dt from the get_dtvals time scales (src/nonlin.F90:93-106) of
+// the last nonlinear pass: the CFL step, bounded by dt_max, changed only
+// when needed with l_optimizedt, and the dt_array history shifted.
+//   multistep (src/steptime.F90:313-370): the whole history shifts;
+//   IMEXRK (src/steptime_imexrk.F90:248-308): only dt_array(2);
+//   RK (src/steptime_rk.F90:180-238): dt and dt_array reset to the namelist
+//   dt first, the diffusive scales dr^2, (r dphi)^2 included, and the
+//   "optimize" branch always taken.
+// Before the second step of a run, dt = the namelist dt.
 int vardt_update(Group* g, int nstep) {
   const falcon_params& p = g->p;
-  if (nstep <= 1) {
+  const bool rk = (p.scheme_type == FALCON_RK);
+  if (rk || nstep <= 1) {
     g->dt_new = p.dt;
     for (int i = 0; i < 4; ++i) g->dt_array[i] = p.dt;
-    return 0;
   }
+  if (nstep <= 1) return 0;
   const int R = g->R;
   CK(cudaMemcpyAsync(g->umax_h.data(), g->umax, sizeof(double) * 2 * R, cudaMemcpyDeviceToHost, g->stream));
   CK(cudaStreamSynchronize(g->stream));
   const double pi = 4.0 * std::atan(1.0);
-  double mr = 0.0, mp = 0.0;
+  double mr = 0.0, mp = 0.0, mrr = 0.0, mpp = 0.0;
   for (int r = 0; r < R; ++r) {
+    const double rp = g->radius_h[r] * pi;
     const double dtr = g->dr_h[r] / g->umax_h[2 * r];
-    const double dtp = (2.0 / 3.0) * (g->radius_h[r] * pi) / ((double)g->Nm * g->umax_h[2 * r + 1]);
+    const double dtp = (2.0 / 3.0) * rp / ((double)g->Nm * g->umax_h[2 * r + 1]);
+    const double dtrr = g->dr_h[r] * g->dr_h[r];
+    const double dtpp = (2.0 / 3.0) * rp / (double)g->Nm * (2.0 / 3.0) * rp / (double)g->Nm;
     mr = (r == 0) ? dtr : std::fmin(mr, dtr);
     mp = (r == 0) ? dtp : std::fmin(mp, dtp);
+    mrr = (r == 0) ? dtrr : std::fmin(mrr, dtrr);
+    mpp = (r == 0) ? dtpp : std::fmin(mpp, dtpp);
   }
-  const double dt_cal = std::fmin(mr, mp);
+  double dt_cal = std::fmin(mr, mp);
+  if (rk) dt_cal = std::fmin(dt_cal, std::fmin(mrr, mpp));
   double dt_n;
   if (p.pr == 1.0 || p.pr > 1.0) dt_n = std::fmax(1.0 / p.pr, 1.0) * p.cfl * dt_cal;
   else dt_n = std::fmin(1.0 / p.pr, 1.0) * p.cfl * dt_cal;
   const double dt2 = std::fmin(0.5 * (1.0 / p.dt_coef + 1.0) * dt_n, p.dt_max);
-  if (p.l_optimizedt) {
+  if (rk || p.l_optimizedt) {
     // dt keeps its previous value when no branch applies
     if (g->dt_array[1] > p.dt_max) g->dt_new = p.dt_max;
     else if (g->dt_array[1] >= dt_cal) g->dt_new = dt2;
@@ -1049,7 +1058,7 @@ int vardt_update(Group* g, int nstep) {
   } else {
     g->dt_new = dt2;
   }
-  const int nmax = std::max(g->sch.n_imp, g->sch.n_exp);
+  const int nmax = (p.scheme_type == FALCON_IMEX) ? std::max(g->sch.n_imp, g->sch.n_exp) : 2;
   for (int i = nmax - 1; i >= 1; --i) g->dt_array[i] = g->dt_array[i - 1];
   g->dt_array[0] = g->dt_new;
   return 0;
@@ -1138,17 +1147,37 @@ int step_imex(Group* g) {
 int step_imexrk(Group* g) {
   const int R = g->R, M = g->M, B = g->B;
   const size_t n = g->nel();
-  OpSet* o = g->ops.get();
   cudaStream_t s = g->stream;
   const Scheme& sc = g->sch;
   const int ns = sc.n_exp;
   const int nstep = g->n_step + 1;
   const bool sa = sc.check_A && sc.check_D;
   int rc;
+  // Variable time step (src/steptime_imexrk.F90:102-137): the CFL step from
+  // a nonlinear pass on the assembled state (not stiffly accurate) or from
+  // the last stage pass (stiffly accurate); operators rebuilt when dt
+  // changed (src/fourierloop_imexrk.F90:117-125).
+  if (g->vardt) {
+    if (nstep > 1 && !sa) {
+      if ((rc = run_nonlin(g))) return rc;
+      CK(cudaMemcpyAsync(g->t_grid, g->T(), sizeof(double2) * n, cudaMemcpyDeviceToDevice, s));
+    }
+    if ((rc = vardt_update(g, nstep))) return rc;
+    if (nstep == 1 || g->dt_array[0] != g->dt_array[1]) {
+      OpKey k = key_of(g->p, sc);
+      k.dt = g->dt_array[0];
+      if (k < g->ops->key || g->ops->key < k) {
+        std::shared_ptr<OpSet> fresh;
+        if ((rc = build_opset(k, &fresh))) return rc;
+        g->ops = fresh;
+      }
+    }
+  }
+  OpSet* o = g->ops.get();
   StageArgs a{};
   a.R = R; a.M = M; a.B = B;
   a.inv_r = o->inv_r; a.inv_r2 = o->inv_r2; a.ra_pr = g->ra_pr;
-  a.dt = g->p.dt; a.inv_pr = 1.0 / g->p.pr; a.buo_imp = g->p.buo_imp;
+  a.dt = g->cur_dt(); a.inv_pr = 1.0 / g->p.pr; a.buo_imp = g->p.buo_imp;
   a.t0 = g->t0; a.w0 = g->w0; a.u0 = g->u0;
   for (int i = 0; i < ns; ++i) {
     a.fat[i] = g->fat[i]; a.fdt[i] = g->fdt[i]; a.faw[i] = g->faw[i]; a.fdw[i] = g->fdw[i]; a.buo[i] = g->buo[i];
@@ -1162,7 +1191,7 @@ int step_imexrk(Group* g) {
     a.aD_ss = sc.aD[st][st];
     if (st > 0) {
       if ((rc = elementwise(g, 12.0 * st + 8.0, [&]() { return launch_stage_rhs(a, s); }))) return rc;
-      const double scale = g->p.buo_imp ? g->p.dt * sc.aD[st][st] : 0.0;
+      const double scale = g->p.buo_imp ? g->cur_dt() * sc.aD[st][st] : 0.0;
       if ((rc = solve_all(g, g->T(), g->W(), scale, g->buo[st], nullptr))) return rc;
     }
     double colsum = 0.0;
@@ -1197,7 +1226,7 @@ int step_imexrk(Group* g) {
   } else {
     // Assembly_stage (src/fourierloop_imexrk.F90:499-651)
     AsmArgs q{};
-    q.R = R; q.M = M; q.B = B; q.ns = ns; q.dt = g->p.dt;
+    q.R = R; q.M = M; q.B = B; q.ns = ns; q.dt = g->cur_dt();
     for (int i = 0; i < ns; ++i) {
       q.bA[i] = sc.bA[i]; q.bD[i] = sc.bD[i];
       q.fat[i] = g->fat[i]; q.fdt[i] = g->fdt[i]; q.faw[i] = g->faw[i]; q.fdw[i] = g->fdw[i]; q.buo[i] = g->buo[i];
@@ -1230,7 +1259,7 @@ int step_imexrk(Group* g) {
     CK(cudaMemcpyAsync(g->W(), g->w0, sizeof(double2) * n, cudaMemcpyDeviceToDevice, s));
   }
   g->n_step = nstep;
-  g->tot_time += g->p.dt;
+  g->tot_time += g->cur_dt();
   return 0;
 }
 
@@ -1247,10 +1276,12 @@ int step_rk(Group* g) {
   const int ns = sc.n_exp;
   const int nstep = g->n_step + 1;
   int rc;
+  // variable time step (src/steptime_rk.F90:103-115); LAPpsi does not depend on dt
+  if (g->vardt && (rc = vardt_update(g, nstep))) return rc;
   double2* dup = g->rhs_t;  // d(u_phi)/dr of every mode (rhs_t is unused by RK)
   auto combine = [&](int nf, const double* coef, double2* t_out, double2* w_out, double* u_out) {
     RkCombineArgs a{};
-    a.R = R; a.M = M; a.B = B; a.nf = nf; a.dt = g->p.dt;
+    a.R = R; a.M = M; a.B = B; a.nf = nf; a.dt = g->cur_dt();
     for (int i = 0; i < nf; ++i) { a.c[i] = coef[i]; a.ft[i] = g->fat[i]; a.fw[i] = g->faw[i]; }
     a.t0 = g->t0; a.w0 = g->w0; a.u0 = g->u0;
     a.t_out = t_out; a.w_out = w_out; a.u_out = u_out; a.rhs_w = g->rhs_w;
@@ -1320,7 +1351,7 @@ int step_rk(Group* g) {
   CK(cudaMemcpyAsync(g->T(), g->t0, sizeof(double2) * n, cudaMemcpyDeviceToDevice, s));
   CK(cudaMemcpyAsync(g->W(), g->w0, sizeof(double2) * n, cudaMemcpyDeviceToDevice, s));
   g->n_step = nstep;
-  g->tot_time += g->p.dt;
+  g->tot_time += g->cur_dt();
   return 0;
 }
 
@@ -1339,7 +1370,7 @@ void group_advance(Group* g) {
     g->head_e = (g->head_e + g->sch.n_exp - 1) % g->sch.n_exp;
   }
   g->n_step += 1;
-  g->tot_time += g->p.dt;
+  g->tot_time += g->cur_dt();
 }
 
 // One time step.  From the second step on, the launch sequence of a step is

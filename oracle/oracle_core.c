@@ -502,7 +502,7 @@ struct orc_sim {
   double *AT_all, *AF_all, *A_uphi; int *ipiv1, *ipiv2, *ipiv_uphi;
   double *LAPpsi_all; int *ipiv_lap;
   double *dw_rmin, *d2w_rmin, *dw_rmax, *d2w_rmax;
-  double *dtval_r, *dtval_p;  /* get_dtvals of the last nonlinear pass */
+  double *dtval_r, *dtval_p, *dtval_rkr, *dtval_rkp;  /* get_dtvals of the last nonlinear pass */
   scheme_t sch;
   double dt_array[4];
   double dt_new, tot_time;
@@ -616,7 +616,7 @@ orc_sim* orc_sim_create(const orc_params* p) {
   if (lm > R - 2) lm = R - 2;
   s->p.lagpts = lm;
   s->dw_rmin = zalloc(lm); s->d2w_rmin = zalloc(lm); s->dw_rmax = zalloc(lm); s->d2w_rmax = zalloc(lm);
-  s->dtval_r = zalloc(R); s->dtval_p = zalloc(R);
+  s->dtval_r = zalloc(R); s->dtval_p = zalloc(R); s->dtval_rkr = zalloc(R); s->dtval_rkp = zalloc(R);
   {
     double* pts = zalloc(lm);
     for (int i = 0; i < lm; ++i) pts[i] = s->radius[1 + i];
@@ -642,7 +642,7 @@ void orc_sim_destroy(orc_sim* s) {
                   s->tmp_imp_uphi, s->tmp_exp_uphi, s->dtemp_a, s->dtemp_d, s->domg_a,
                   s->domg_d, s->rhs_buo, s->AT_all, s->AF_all, s->A_uphi, s->ipiv1, s->ipiv2,
                   s->ipiv_uphi, s->LAPpsi_all, s->ipiv_lap, s->dw_rmin, s->d2w_rmin,
-                  s->dw_rmax, s->d2w_rmax, s->dtval_r, s->dtval_p};
+                  s->dw_rmax, s->d2w_rmax, s->dtval_r, s->dtval_p, s->dtval_rkr, s->dtval_rkp};
   for (size_t i = 0; i < sizeof(ptrs) / sizeof(ptrs[0]); ++i) free(ptrs[i]);
   free(s);
 }
@@ -973,6 +973,8 @@ static void nr_maxloop(orc_sim* s) {
     }
     s->dtval_r[r] = s->dr[r] / mr;
     s->dtval_p[r] = (2.0 / 3.0) * (s->radius[r] * PI_) / ((double)Nm * mp);
+    s->dtval_rkr[r] = s->dr[r] * s->dr[r];
+    s->dtval_rkp[r] = (2.0 / 3.0) * (s->radius[r] * PI_) / (double)Nm * (2.0 / 3.0) * (s->radius[r] * PI_) / (double)Nm;
   }
 }
 
@@ -1202,6 +1204,37 @@ static void rhs_construct_uphi_bar(orc_sim* s, int n_step, double dt, double* rh
  * from the second step on: the CFL time step from the last nonlinear pass,
  * optionally changed only when needed (l_optimizedt), and the dt_array
  * history shifted (n_order_tscheme_max = max(n_imp, n_exp)). */
+static double minval(const double* v, int n) {
+  double m = v[0];
+  for (int i = 1; i < n; ++i) m = fmin(m, v[i]);
+  return m;
+}
+
+/* compute_new_dt of the IMEXRK loop (src/steptime_imexrk.F90:248-308) and of
+ * the RK loop (src/steptime_rk.F90:180-238): as the multistep one, but only
+ * dt_array(2) is shifted; RK adds the diffusive scales to dt_cal and always
+ * takes the "optimize" branch, after dt_array(:) was reset to dt. */
+static void compute_new_dt_rk(orc_sim* s, int rk) {
+  const orc_params* p = &s->p;
+  int R = s->R;
+  double dt_cal = fmin(minval(s->dtval_r, R), minval(s->dtval_p, R));
+  if (rk) dt_cal = fmin(dt_cal, fmin(minval(s->dtval_rkr, R), minval(s->dtval_rkp, R)));
+  double dt_n;
+  if (p->pr == 1.0 || p->pr > 1.0) dt_n = fmax(1.0 / p->pr, 1.0) * p->cfl * dt_cal;
+  else dt_n = fmin(1.0 / p->pr, 1.0) * p->cfl * dt_cal;
+  double dt2 = fmin(0.5 * (1.0 / p->dt_coef + 1.0) * dt_n, p->dt_max);
+  if (rk || p->l_optimizedt) {
+    if (s->dt_array[1] > p->dt_max) s->dt_new = p->dt_max;
+    else if (s->dt_array[1] >= dt_cal) s->dt_new = dt2;
+    else if (p->dt_coef * s->dt_array[1] < dt_cal && s->dt_array[1] < p->dt_max)
+      s->dt_new = (s->dt_array[0] < dt2) ? dt2 : s->dt_array[0];
+  } else {
+    s->dt_new = dt2;
+  }
+  s->dt_array[1] = s->dt_array[0];
+  s->dt_array[0] = s->dt_new;
+}
+
 static void compute_new_dt_imex(orc_sim* s) {
   const orc_params* p = &s->p;
   int R = s->R;
@@ -1428,7 +1461,9 @@ static void rhs_construct_stage(orc_sim* s, int st) {
 /* Get_stage_var, src/fourierloop_imexrk.F90:75-401 (diag_diff = .FALSE.) */
 static void get_stage_var(orc_sim* s, int st, int n_step) {
   int R = s->R, M = s->M, ns = s->sch.n_exp;
-  if (n_step == 1 && st == 1 && !s->mats_built) {
+  /* matrices at stage 2 of the first step, and again whenever dt changed
+   * (src/fourierloop_imexrk.F90:108-125) */
+  if ((n_step == 1 && st == 1 && !s->mats_built) || (n_step > 1 && st == 1 && s->dt_array[0] != s->dt_array[1])) {
     double w = s->sch.aD[s->sch.diag_index][s->sch.diag_index];
     for (int m = 0; m < M; ++m) {
       mat_build(s, s->dt_array[0], m, w, 1, s->AT_all + (size_t)R * R * m, s->ipiv1 + (size_t)R * m,
@@ -1698,8 +1733,22 @@ static void imexrk_step(orc_sim* s) {
     /* mat_build_rk for every mode before the loop (src/steptime_imexrk.F90:93-95) */
     for (int m = 0; m < M; ++m) mat_build_rk(s, m, s->LAPpsi_all + (size_t)R * R * m, s->ipiv_lap + (size_t)R * m);
   }
-  s->dt_new = s->p.dt;
-  for (int i = 0; i < 4; ++i) s->dt_array[i] = s->p.dt;
+  /* src/steptime_imexrk.F90:102-137: with a variable dt, the CFL step comes
+   * from a nonlinear pass on the assembled state (non stiffly accurate
+   * schemes) or from the last stage pass (stiffly accurate ones) */
+  if (n_step == 1) {
+    s->dt_new = s->p.dt;
+    for (int i = 0; i < 4; ++i) s->dt_array[i] = s->p.dt;
+  }
+  if (s->p.l_vartimestep) {
+    if (n_step > 1) {
+      if (!s->sch.check_A || !s->sch.check_D) nr_maxloop(s);
+      compute_new_dt_rk(s, 0);
+    }
+  } else {
+    s->dt_new = s->p.dt;
+    for (int i = 0; i < 4; ++i) s->dt_array[i] = s->p.dt;
+  }
   for (int st = 0; st < ns; ++st) {
     if (st > 0) get_stage_var(s, st, n_step);
     double colsum = 0.0;
@@ -1977,8 +2026,11 @@ static void rk_step(orc_sim* s) {
     for (int m = 0; m < M; ++m) mat_build_rk(s, m, s->LAPpsi_all + (size_t)R * R * m, s->ipiv_lap + (size_t)R * m);
     s->mats_built = 1;
   }
+  /* src/steptime_rk.F90:103-115: dt and dt_array reset every step, then
+   * compute_new_dt from the last nonlinear pass */
   s->dt_new = s->p.dt;
   for (int i = 0; i < 4; ++i) s->dt_array[i] = s->p.dt;
+  if (s->p.l_vartimestep && n_step > 1) compute_new_dt_rk(s, 1);
   for (int st = 0; st < ns; ++st) {
     if (st > 0) rk_get_stage_var(s, st);
     if (n_step > 1 || st > 0) nr_maxloop(s);
