@@ -775,6 +775,11 @@ struct Group {
   // history dt_array(1..4), the current dt, the per-line velocity maxima of
   // the last nonlinear pass, and the grid spacing for get_dtvals.
   bool vardt = false;
+  // restored from a checkpoint: the operators are rebuilt for the restored
+  // dt at the next step, and (IMEXRK, RK) the velocity maxima of the restored
+  // state are taken by an extra nonlinear pass before compute_new_dt
+  bool force_rebuild = false;
+  bool need_cfl_pass = false;
   double dt_array[4] = {0, 0, 0, 0};
   double dt_new = 0.0;
   double* umax = nullptr;
@@ -1085,7 +1090,9 @@ int step_imex(Group* g) {
   if (g->vardt) {
     if ((rc = vardt_update(g, nstep))) return rc;
     if (imex_weights(vs.imp, vs.exp, g->dt_array, &vs) != 0) return fail(FALCON_EINVAL, "unsupported time scheme");
-    if (nstep == 1 || g->dt_array[0] != g->dt_array[1]) {
+    const bool rebuild = nstep == 1 || g->dt_array[0] != g->dt_array[1] || g->force_rebuild;
+    g->force_rebuild = false;
+    if (rebuild) {
       OpKey k = key_of(g->p, vs);
       k.dt = g->dt_array[0];
       k.wt = vs.wt_lhs;
@@ -1158,12 +1165,15 @@ int step_imexrk(Group* g) {
   // the last stage pass (stiffly accurate); operators rebuilt when dt
   // changed (src/fourierloop_imexrk.F90:117-125).
   if (g->vardt) {
-    if (nstep > 1 && !sa) {
+    if (nstep > 1 && (!sa || g->need_cfl_pass)) {
       if ((rc = run_nonlin(g))) return rc;
       CK(cudaMemcpyAsync(g->t_grid, g->T(), sizeof(double2) * n, cudaMemcpyDeviceToDevice, s));
     }
+    g->need_cfl_pass = false;
     if ((rc = vardt_update(g, nstep))) return rc;
-    if (nstep == 1 || g->dt_array[0] != g->dt_array[1]) {
+    const bool rebuild = nstep == 1 || g->dt_array[0] != g->dt_array[1] || g->force_rebuild;
+    g->force_rebuild = false;
+    if (rebuild) {
       OpKey k = key_of(g->p, sc);
       k.dt = g->dt_array[0];
       if (k < g->ops->key || g->ops->key < k) {
@@ -1277,7 +1287,11 @@ int step_rk(Group* g) {
   const int nstep = g->n_step + 1;
   int rc;
   // variable time step (src/steptime_rk.F90:103-115); LAPpsi does not depend on dt
-  if (g->vardt && (rc = vardt_update(g, nstep))) return rc;
+  if (g->vardt) {
+    if (g->need_cfl_pass && nstep > 1 && (rc = run_nonlin(g))) return rc;
+    g->need_cfl_pass = false;
+    if ((rc = vardt_update(g, nstep))) return rc;
+  }
   double2* dup = g->rhs_t;  // d(u_phi)/dr of every mode (rhs_t is unused by RK)
   auto combine = [&](int nf, const double* coef, double2* t_out, double2* w_out, double* u_out) {
     RkCombineArgs a{};
@@ -1546,6 +1560,305 @@ int group_reset_instance(Group* g, int b) {
   }
   CK(zero(g->psi, n, 2));
   CK(cudaStreamSynchronize(s));
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// Checkpoint and snapshot files (store_checkpoint, store_snapshot of
+// src/output.F90:359-516): Fortran unformatted sequential records, each
+// framed by its byte length as a 4-byte integer before and after.
+// ---------------------------------------------------------------------------
+struct RecordWriter {
+  std::FILE* f = nullptr;
+  std::vector<char> buf;
+  template <class T>
+  void put(const T& v) {
+    const char* p = reinterpret_cast<const char*>(&v);
+    buf.insert(buf.end(), p, p + sizeof(T));
+  }
+  void put_array(const double* v, size_t n) {
+    const char* p = reinterpret_cast<const char*>(v);
+    buf.insert(buf.end(), p, p + n * sizeof(double));
+  }
+  bool end_record() {
+    const int32_t len = (int32_t)buf.size();
+    const bool ok = std::fwrite(&len, 4, 1, f) == 1 && std::fwrite(buf.data(), 1, buf.size(), f) == buf.size() &&
+                    std::fwrite(&len, 4, 1, f) == 1;
+    buf.clear();
+    return ok;
+  }
+};
+
+int read_record(std::FILE* f, std::vector<char>* out) {
+  int32_t a = 0, b = 0;
+  if (std::fread(&a, 4, 1, f) != 1 || a < 0) return fail(FALCON_EIO, "checkpoint: truncated record header");
+  out->resize((size_t)a);
+  if (a > 0 && std::fread(out->data(), 1, (size_t)a, f) != (size_t)a) return fail(FALCON_EIO, "checkpoint: truncated record");
+  if (std::fread(&b, 4, 1, f) != 1 || b != a) return fail(FALCON_EIO, "checkpoint: corrupt record marker");
+  return 0;
+}
+
+// One instance's (M, R) complex field, Fortran layout (mode fastest).
+int gather_field(Group* g, int b, const double2* src, std::vector<double>* out) {
+  const size_t nb = sizeof(double2) * (size_t)g->M * g->R;
+  out->assign((size_t)2 * g->M * g->R, 0.0);
+  if (!src) return 0;
+  double2* d = nullptr;
+  CK(cudaMallocAsync(&d, nb, g->stream));
+  CK(launch_gather_instance(g->R, g->M, g->B, b, src, d, g->stream));
+  CK(cudaMemcpyAsync(g->stage_buf, d, nb, cudaMemcpyDeviceToHost, g->stream));
+  CK(cudaFreeAsync(d, g->stream));
+  CK(cudaStreamSynchronize(g->stream));
+  std::memcpy(out->data(), g->stage_buf, nb);
+  return 0;
+}
+
+int scatter_field(Group* g, int b, const double* in, double2* dst) {
+  const size_t nb = sizeof(double2) * (size_t)g->M * g->R;
+  double2* d = nullptr;
+  CK(cudaMallocAsync(&d, nb, g->stream));
+  std::memcpy(g->stage_buf, in, nb);
+  CK(cudaMemcpyAsync(d, g->stage_buf, nb, cudaMemcpyHostToDevice, g->stream));
+  CK(launch_scatter_instance(g->R, g->M, g->B, b, d, dst, g->stream));
+  CK(cudaFreeAsync(d, g->stream));
+  CK(cudaStreamSynchronize(g->stream));
+  return 0;
+}
+
+// One instance's column of an R x B real array, as R complex values.
+int gather_real(Group* g, int b, const double* src, std::vector<double>* out) {
+  const int R = g->R, B = g->B;
+  out->assign((size_t)2 * R, 0.0);
+  if (!src) return 0;
+  std::vector<double> all((size_t)R * B);
+  CK(cudaMemcpyAsync(all.data(), src, sizeof(double) * all.size(), cudaMemcpyDeviceToHost, g->stream));
+  CK(cudaStreamSynchronize(g->stream));
+  for (int r = 0; r < R; ++r) (*out)[2 * r] = all[(size_t)r * B + b];
+  return 0;
+}
+
+int scatter_real(Group* g, int b, const double* in /* R complex */, double* dst) {
+  const int R = g->R, B = g->B;
+  for (int r = 0; r < R; ++r)
+    CK(cudaMemcpyAsync(dst + (size_t)r * B + b, in + 2 * r, sizeof(double), cudaMemcpyHostToDevice, g->stream));
+  CK(cudaStreamSynchronize(g->stream));
+  return 0;
+}
+
+// Orders written in the header (n_order_tscheme_imp / _exp / _max) and the
+// number of levels of the rhs_imp_* / rhs_exp_* records: the multistep
+// orders; for IMEXRK the stage count in the header and single-level arrays
+// (store_checkpoint_imexrk, src/output.F90:404-447); for RK the stage count
+// for both (store_checkpoint with the RK orders).
+struct CkptShape { int ni, ne, nmax, li, le; };
+CkptShape checkpoint_shape(const Group* g) {
+  if (g->p.scheme_type == FALCON_IMEX) {
+    const int ni = g->sch.n_imp, ne = g->sch.n_exp;
+    return {ni, ne, std::max(ni, ne), ni, ne};
+  }
+  const int ns = g->sch.n_exp;
+  if (g->p.scheme_type == FALCON_IMEXRK) return {ns, ns, ns, 1, 1};
+  return {ns, ns, ns, ns, ns};
+}
+
+// store_checkpoint (src/output.F90:359-402) for instance b.  Multistep runs
+// write the history arrays rhs_imp_* (T, omega, uphi_bar at the previous
+// steps) and rhs_exp_* (the explicit terms): entry i of rhs_imp is the
+// state i steps before the current one, except that the oldest entry, which
+// the next step shifts out before any use, is not kept on the device and is
+// written as zero; the Runge-Kutta loops write their arrays as zero (they
+// carry no history between steps).
+int group_store_checkpoint(Group* g, int b, const char* path) {
+  const int R = g->R, M = g->M;
+  const CkptShape sh = checkpoint_shape(g);
+  const int ni = sh.li, ne = sh.le, nmax = sh.nmax;
+  std::FILE* f = std::fopen(path, "wb");
+  if (!f) return fail(FALCON_EIO, std::string("cannot write checkpoint ") + path);
+  RecordWriter w;
+  w.f = f;
+  int rc = 0;
+  auto done = [&](int e) { std::fclose(f); return e; };
+  w.put(g->cur_dt()); w.put(g->tot_time);
+  w.put((int32_t)g->Nm); w.put((int32_t)R); w.put((int32_t)sh.ni); w.put((int32_t)sh.ne); w.put((int32_t)nmax);
+  if (!w.end_record()) return done(fail(FALCON_EIO, "checkpoint write failed"));
+  for (int i = 0; i < nmax; ++i) w.put((g->vardt && i < 4) ? g->dt_array[i] : g->p.dt);
+  if (!w.end_record()) return done(fail(FALCON_EIO, "checkpoint write failed"));
+  std::vector<double> v;
+  for (const double2* fld : std::initializer_list<const double2*>{g->T(), g->W(), g->ur, g->up}) {
+    if ((rc = gather_field(g, b, fld, &v))) return done(rc);
+    w.put_array(v.data(), v.size());
+    if (!w.end_record()) return done(fail(FALCON_EIO, "checkpoint write failed"));
+  }
+  const bool ms = (g->p.scheme_type == FALCON_IMEX);
+  // (order, M, R) complex arrays, the order index fastest; the vorticity
+  // histories hold modes m >= 1 (mode 0 is the uphi_bar equation and the
+  // reference leaves its entries zero)
+  auto hist3 = [&](int n, std::function<const double2*(int)> level, bool modes1) -> int {
+    std::vector<std::vector<double>> lv(n);
+    for (int io = 0; io < n; ++io) {
+      if ((rc = gather_field(g, b, ms ? level(io) : nullptr, &lv[io]))) return rc;
+      if (modes1)
+        for (int r = 0; r < R; ++r) lv[io][2 * ((size_t)r * M)] = lv[io][2 * ((size_t)r * M) + 1] = 0.0;
+    }
+    std::vector<double> out((size_t)2 * n * M * R);
+    for (size_t rm = 0; rm < (size_t)M * R; ++rm)
+      for (int io = 0; io < n; ++io) {
+        out[2 * (io + (size_t)n * rm)] = lv[io][2 * rm];
+        out[2 * (io + (size_t)n * rm) + 1] = lv[io][2 * rm + 1];
+      }
+    w.put_array(out.data(), out.size());
+    return w.end_record() ? 0 : fail(FALCON_EIO, "checkpoint write failed");
+  };
+  auto hist2 = [&](int n, std::function<const double*(int)> level) -> int {
+    std::vector<std::vector<double>> lv(n);
+    for (int io = 0; io < n; ++io)
+      if ((rc = gather_real(g, b, ms ? level(io) : nullptr, &lv[io]))) return rc;
+    std::vector<double> out((size_t)2 * n * R);
+    for (int r = 0; r < R; ++r)
+      for (int io = 0; io < n; ++io) out[2 * (io + (size_t)n * r)] = lv[io][2 * r];
+    w.put_array(out.data(), out.size());
+    return w.end_record() ? 0 : fail(FALCON_EIO, "checkpoint write failed");
+  };
+  auto imp_slot = [&](int io) { return io + 1 < ni ? (g->head + io + 1) % ni : -1; };
+  auto exp_slot = [&](int io) { return (g->head_e + io) % ne; };
+  if ((rc = hist3(ni, [&](int io) -> const double2* { int k = imp_slot(io); return k < 0 ? nullptr : g->th[k]; },
+                  false)) ||
+      (rc = hist3(ne, [&](int io) -> const double2* { return g->nth[exp_slot(io)]; }, false)) ||
+      (rc = hist3(ni, [&](int io) -> const double2* { int k = imp_slot(io); return k < 0 ? nullptr : g->wh[k]; },
+                  true)) ||
+      (rc = hist3(ne, [&](int io) -> const double2* { return g->nwh[exp_slot(io)]; }, true)) ||
+      (rc = hist2(ni, [&](int io) -> const double* { int k = imp_slot(io); return k < 0 ? nullptr : g->ubh[k]; })) ||
+      (rc = hist2(ne, [&](int io) -> const double* { return g->uromh[exp_slot(io)]; })))
+    return done(rc);
+  if (std::fclose(f) != 0) return fail(FALCON_EIO, "checkpoint close failed");
+  return 0;
+}
+
+// Restores instance b from a checkpoint of the same grid and scheme: the
+// state, the time, the time-step history and, for multistep runs, the
+// history arrays, so that a constant-dt run continues bit for bit.  With a
+// variable dt the operators are rebuilt for the restored dt at the next step
+// (the reference's restart does the same, src/fourierloop.F90:87).  (The
+// reference's read_checkpoint, src/init.F90:865-935, reads the state and dt
+// only and rebuilds the histories from earlier checkpoints.)  The time and
+// the step count are the group's: instances of one group are restored from
+// checkpoints of the same run time.
+int group_load_checkpoint(Group* g, int b, const char* path) {
+  const int R = g->R, M = g->M;
+  const CkptShape sh = checkpoint_shape(g);
+  const int ni = sh.li, ne = sh.le, nmax = sh.nmax;
+  std::FILE* f = std::fopen(path, "rb");
+  if (!f) return fail(FALCON_EIO, std::string("checkpoint not found: ") + path);
+  auto done = [&](int e) { std::fclose(f); return e; };
+  std::vector<char> rec;
+  int rc;
+  if ((rc = read_record(f, &rec))) return done(rc);
+  if (rec.size() != 36) return done(fail(FALCON_EIO, "checkpoint: unexpected header record"));
+  double dt_new, tot_time;
+  int32_t hd[5];
+  std::memcpy(&dt_new, rec.data(), 8);
+  std::memcpy(&tot_time, rec.data() + 8, 8);
+  std::memcpy(hd, rec.data() + 16, 20);
+  if (hd[0] != g->Nm || hd[1] != R)
+    return done(fail(FALCON_EINVAL, "checkpoint grid differs from the instance's (resolution change is not supported)"));
+  if (hd[2] != sh.ni || hd[3] != sh.ne || hd[4] != nmax)
+    return done(fail(FALCON_EINVAL, "checkpoint time-scheme orders differ from the instance's"));
+  if ((rc = read_record(f, &rec))) return done(rc);
+  if (rec.size() != sizeof(double) * nmax) return done(fail(FALCON_EIO, "checkpoint: dt_array size"));
+  double dta[4] = {g->p.dt, g->p.dt, g->p.dt, g->p.dt};
+  std::memcpy(dta, rec.data(), sizeof(double) * std::min(nmax, 4));
+  const size_t fb = sizeof(double2) * (size_t)M * R;
+  std::vector<std::vector<double>> fld(4);
+  for (int k = 0; k < 4; ++k) {
+    if ((rc = read_record(f, &rec))) return done(rc);
+    if (rec.size() != fb) return done(fail(FALCON_EIO, "checkpoint: field size"));
+    fld[k].resize((size_t)2 * M * R);
+    std::memcpy(fld[k].data(), rec.data(), fb);
+  }
+  std::vector<std::vector<double>> hist(6);
+  const int nh[6] = {ni, ne, ni, ne, ni, ne};
+  for (int k = 0; k < 6; ++k) {
+    if ((rc = read_record(f, &rec))) return done(rc);
+    const size_t want = sizeof(double2) * (size_t)nh[k] * (k < 4 ? (size_t)M * R : (size_t)R);
+    if (rec.size() != want) return done(fail(FALCON_EIO, "checkpoint: history size"));
+    hist[k].resize(want / sizeof(double));
+    std::memcpy(hist[k].data(), rec.data(), want);
+  }
+  std::fclose(f);
+  // state (tFR, omgFR, urFR, upFR)
+  if ((rc = scatter_field(g, b, fld[0].data(), g->T())) || (rc = scatter_field(g, b, fld[1].data(), g->W())) ||
+      (rc = scatter_field(g, b, fld[2].data(), g->ur)) || (rc = scatter_field(g, b, fld[3].data(), g->up)))
+    return rc;
+  if ((rc = group_reset_instance(g, b))) return rc;  // Y0, uphi_bar slot, stage stores
+  if (g->p.scheme_type == FALCON_IMEX) {
+    auto level3 = [&](const std::vector<double>& h, int n, int io, std::vector<double>* out) {
+      out->resize((size_t)2 * M * R);
+      for (size_t rm = 0; rm < (size_t)M * R; ++rm) {
+        (*out)[2 * rm] = h[2 * (io + (size_t)n * rm)];
+        (*out)[2 * rm + 1] = h[2 * (io + (size_t)n * rm) + 1];
+      }
+    };
+    auto level2 = [&](const std::vector<double>& h, int n, int io, std::vector<double>* out) {
+      out->assign((size_t)2 * R, 0.0);
+      for (int r = 0; r < R; ++r) (*out)[2 * r] = h[2 * (io + (size_t)n * r)];
+    };
+    std::vector<double> v;
+    for (int io = 0; io + 1 < ni; ++io) {
+      const int k = (g->head + io + 1) % ni;
+      level3(hist[0], ni, io, &v);
+      if ((rc = scatter_field(g, b, v.data(), g->th[k]))) return rc;
+      level3(hist[2], ni, io, &v);
+      if ((rc = scatter_field(g, b, v.data(), g->wh[k]))) return rc;
+      level2(hist[4], ni, io, &v);
+      if ((rc = scatter_real(g, b, v.data(), g->ubh[k]))) return rc;
+    }
+    for (int io = 0; io < ne; ++io) {
+      const int k = (g->head_e + io) % ne;
+      level3(hist[1], ne, io, &v);
+      if ((rc = scatter_field(g, b, v.data(), g->nth[k]))) return rc;
+      level3(hist[3], ne, io, &v);
+      if ((rc = scatter_field(g, b, v.data(), g->nwh[k]))) return rc;
+      level2(hist[5], ne, io, &v);
+      if ((rc = scatter_real(g, b, v.data(), g->uromh[k]))) return rc;
+    }
+  }
+  // continue as a running step sequence (the first step after a restart
+  // takes the nonlinear pass, src/steptime.F90:205)
+  g->n_step = std::max(g->n_step, 1);
+  g->tot_time = tot_time;
+  if (g->vardt) {
+    for (int i = 0; i < 4; ++i) g->dt_array[i] = dta[i];
+    g->dt_new = dt_new;
+    g->force_rebuild = true;
+    g->need_cfl_pass = (g->p.scheme_type != FALCON_IMEX);
+  }
+  return 0;
+}
+
+// store_snapshot (src/output.F90:487-516) for instance b.
+int group_store_snapshot(Group* g, int b, const char* path) {
+  std::FILE* f = std::fopen(path, "wb");
+  if (!f) return fail(FALCON_EIO, std::string("cannot write snapshot ") + path);
+  auto done = [&](int e) { std::fclose(f); return e; };
+  RecordWriter w;
+  w.f = f;
+  w.put(g->ra_pr_h[b] * g->p.pr); w.put(g->p.pr); w.put(g->p.eta);
+  if (!w.end_record()) return done(fail(FALCON_EIO, "snapshot write failed"));
+  w.put(g->cur_dt()); w.put(g->tot_time);
+  if (!w.end_record()) return done(fail(FALCON_EIO, "snapshot write failed"));
+  w.put((int32_t)g->Nm); w.put((int32_t)g->R);
+  if (!w.end_record()) return done(fail(FALCON_EIO, "snapshot write failed"));
+  Cheb c = make_cheb(g->R, g->p.eta);
+  w.put_array(c.radius.data(), c.radius.size());
+  if (!w.end_record()) return done(fail(FALCON_EIO, "snapshot write failed"));
+  std::vector<double> v;
+  int rc;
+  for (const double2* fld : std::initializer_list<const double2*>{g->T(), g->W(), g->ur, g->up}) {
+    if ((rc = gather_field(g, b, fld, &v))) return done(rc);
+    w.put_array(v.data(), v.size());
+    if (!w.end_record()) return done(fail(FALCON_EIO, "snapshot write failed"));
+  }
+  if (std::fclose(f) != 0) return fail(FALCON_EIO, "snapshot close failed");
   return 0;
 }
 
@@ -2122,6 +2435,42 @@ int falcon_step(falcon_handle* h, int nsteps) {
 int falcon_diagnostics(falcon_handle* h, falcon_diag* out) {
   if (!h) return fail(FALCON_EINVAL, "null handle");
   return falcon_batch_diagnostics(h->b, out);
+}
+
+int falcon_batch_store_checkpoint(falcon_batch* b, int i, const char* path) {
+  if (!b || !path || i < 0 || i >= (int)b->params.size()) return fail(FALCON_EINVAL, "invalid checkpoint arguments");
+  int rc = b->sync();
+  if (rc) return rc;
+  return group_store_checkpoint(b->groups[b->where[i].first].get(), b->where[i].second, path);
+}
+
+int falcon_batch_load_checkpoint(falcon_batch* b, int i, const char* path) {
+  if (!b || !path || i < 0 || i >= (int)b->params.size()) return fail(FALCON_EINVAL, "invalid checkpoint arguments");
+  int rc = b->sync();
+  if (rc) return rc;
+  return group_load_checkpoint(b->groups[b->where[i].first].get(), b->where[i].second, path);
+}
+
+int falcon_batch_store_snapshot(falcon_batch* b, int i, const char* path) {
+  if (!b || !path || i < 0 || i >= (int)b->params.size()) return fail(FALCON_EINVAL, "invalid snapshot arguments");
+  int rc = b->sync();
+  if (rc) return rc;
+  return group_store_snapshot(b->groups[b->where[i].first].get(), b->where[i].second, path);
+}
+
+int falcon_store_checkpoint(falcon_handle* h, const char* path) {
+  if (!h) return fail(FALCON_EINVAL, "null handle");
+  return falcon_batch_store_checkpoint(h->b, 0, path);
+}
+
+int falcon_load_checkpoint(falcon_handle* h, const char* path) {
+  if (!h) return fail(FALCON_EINVAL, "null handle");
+  return falcon_batch_load_checkpoint(h->b, 0, path);
+}
+
+int falcon_store_snapshot(falcon_handle* h, const char* path) {
+  if (!h) return fail(FALCON_EINVAL, "null handle");
+  return falcon_batch_store_snapshot(h->b, 0, path);
 }
 
 // ---- kernel-level entry points ----

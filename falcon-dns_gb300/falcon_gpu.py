@@ -95,7 +95,9 @@ EXPORTS = (
     "falcon_server_create", "falcon_server_destroy", "falcon_server_submit", "falcon_server_iterate",
     "falcon_server_poll", "falcon_last_error", "falcon_version", "falcon_fp64_peak_gflops",
     "falcon_batch_profile", "falcon_launch_count", "falcon_fp64_mma_peak_gflops",
-    "falcon_nonlin_noalloc_dev", "falcon_set_step_graphs",
+    "falcon_nonlin_noalloc_dev", "falcon_set_step_graphs", "falcon_store_checkpoint", "falcon_load_checkpoint",
+    "falcon_store_snapshot", "falcon_batch_store_checkpoint", "falcon_batch_load_checkpoint",
+    "falcon_batch_store_snapshot",
 )
 
 
@@ -153,6 +155,10 @@ def lib():
     L.falcon_batch_profile.argtypes = [vp, ip, P(KernelStat), ip, P(ctypes.c_int)]
     L.falcon_launch_count.restype = ctypes.c_longlong
     L.falcon_set_step_graphs.argtypes = [ip]
+    for f in ("falcon_store_checkpoint", "falcon_load_checkpoint", "falcon_store_snapshot"):
+        getattr(L, f).argtypes = [vp, ctypes.c_char_p]
+    for f in ("falcon_batch_store_checkpoint", "falcon_batch_load_checkpoint", "falcon_batch_store_snapshot"):
+        getattr(L, f).argtypes = [vp, ip, ctypes.c_char_p]
     _lib = L
     return L
 
@@ -261,6 +267,18 @@ class Batch:
         check(lib().falcon_batch_diagnostics(self.h, out))
         return [d.as_dict() for d in out]
 
+    def store_checkpoint(self, i, path):
+        """store_checkpoint layout (Fortran unformatted records) of instance i."""
+        check(lib().falcon_batch_store_checkpoint(self.h, i, os.fsencode(path)))
+
+    def load_checkpoint(self, i, path):
+        """Restore instance i (state, time, dt and multistep histories)."""
+        check(lib().falcon_batch_load_checkpoint(self.h, i, os.fsencode(path)))
+
+    def store_snapshot(self, i, path):
+        """store_snapshot layout of instance i."""
+        check(lib().falcon_batch_store_snapshot(self.h, i, os.fsencode(path)))
+
     def profile(self, nsteps):
         """Per-kernel-class CUDA-event times of `nsteps` steps (advances the state)."""
         stats = (KernelStat * 8)()
@@ -287,6 +305,15 @@ class Instance(Batch):
 
     def diagnostics(self):
         return super().diagnostics()[0]
+
+    def store_checkpoint(self, path):
+        super().store_checkpoint(0, path)
+
+    def load_checkpoint(self, path):
+        super().load_checkpoint(0, path)
+
+    def store_snapshot(self, path):
+        super().store_snapshot(0, path)
 
 
 class Server:

@@ -137,6 +137,22 @@ int falcon_get_state(falcon_handle* h, double* tFR, double* omgFR, double* upFR,
  * src/steptime_imexrk.F90:96-190). */
 int falcon_step(falcon_handle* h, int nsteps);
 int falcon_diagnostics(falcon_handle* h, falcon_diag* out);
+/* Checkpoint file in the layout of store_checkpoint (src/output.F90:359-447,
+ * Fortran unformatted sequential records): dt_new, tot_time, Nm_max, Nr_max
+ * and the time-scheme orders; dt_array; tFR, omgFR, urFR, upFR; the history
+ * arrays rhs_imp_* / rhs_exp_* of the multistep schemes (the oldest implicit
+ * level, which the next step shifts out unused, is written as zero; the
+ * Runge-Kutta loops write zero arrays).  Replaces the call at
+ * src/steptime.F90:269-277 (and its IMEXRK and RK twins). */
+int falcon_store_checkpoint(falcon_handle* h, const char* path);
+/* Restores a checkpoint written by falcon_store_checkpoint (same grid and
+ * scheme): state, time, dt history and the multistep histories; a
+ * constant-dt run continues bit for bit.  Counterpart of read_checkpoint
+ * (src/init.F90:865-935), which reads the state and dt only. */
+int falcon_load_checkpoint(falcon_handle* h, const char* path);
+/* Snapshot file in the layout of store_snapshot (src/output.F90:487-516):
+ * Ra, Pr, eta; dt, time; Nm_max, Nr_max; radius; tFR, omgFR, urFR, upFR. */
+int falcon_store_snapshot(falcon_handle* h, const char* path);
 
 /* ---- batches of independent instances ---- */
 /* Instances are grouped by operator key (Nr, Nm, mBC, scheme, dt, Pr);
@@ -152,6 +168,12 @@ int falcon_batch_get_state(falcon_batch* b, int i, double* tFR, double* omgFR, d
                            double* urFR, double* psi);
 int falcon_batch_step(falcon_batch* b, int nsteps);
 int falcon_batch_diagnostics(falcon_batch* b, falcon_diag* out /* n entries */);
+/* Checkpoint / snapshot of instance i (as the falcon_handle forms).  A load
+ * sets the time and step count of instance i's group: load every instance
+ * of a group from checkpoints of the same run time. */
+int falcon_batch_store_checkpoint(falcon_batch* b, int i, const char* path);
+int falcon_batch_load_checkpoint(falcon_batch* b, int i, const char* path);
+int falcon_batch_store_snapshot(falcon_batch* b, int i, const char* path);
 /* Optional: run every step of the batch on this stream (cudaStream_t). */
 int falcon_batch_set_stream(falcon_batch* b, void* stream);
 /* Device bytes held by the batch (state, history, operators, scratch). */

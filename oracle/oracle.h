@@ -105,6 +105,9 @@ void orc_noise_pair(uint64_t seed, int m, int i, double* a, double* b);
 /* IMEXRK table of scheme number `scheme` (see imexrk_tables.h): out = n,
  * aD (n x n, row-major), bD, aA, bA, check_D, check_A, diag_index. */
 int orc_imexrk_table(int scheme, double* out);
+/* store_checkpoint / store_snapshot files (src/output.F90:359-516). */
+int orc_sim_store_checkpoint(const orc_sim* s, const char* path);
+int orc_sim_store_snapshot(const orc_sim* s, const char* path);
 /* Number of OpenMP threads the oracle uses (0 = runtime default). */
 void orc_set_threads(int n);
 

@@ -93,6 +93,8 @@ def lib():
         L.orc_sim_diagnostics.argtypes = [ctypes.c_void_p, dp]
         L.orc_sim_nstep.argtypes = [ctypes.c_void_p]
         L.orc_sim_dt.argtypes = [ctypes.c_void_p]
+        L.orc_sim_store_checkpoint.argtypes = [ctypes.c_void_p, ctypes.c_char_p]
+        L.orc_sim_store_snapshot.argtypes = [ctypes.c_void_p, ctypes.c_char_p]
         L.orc_sim_dt.restype = ctypes.c_double
         L.orc_noise_pair.argtypes = [ctypes.c_uint64, ctypes.c_int, ctypes.c_int, dp, dp]
         L.orc_set_threads.argtypes = [ctypes.c_int]
@@ -225,6 +227,14 @@ class Sim:
         arrs = [np.empty((self.R, self.M), np.complex128) for _ in range(5)]
         lib().orc_sim_get_state(self.h, *[_dp(a) for a in arrs])
         return dict(zip(("T", "omg", "up", "ur", "psi"), arrs))
+
+    def store_checkpoint(self, path):
+        if lib().orc_sim_store_checkpoint(self.h, os.fsencode(path)) != 0:
+            raise RuntimeError("oracle: checkpoint write failed")
+
+    def store_snapshot(self, path):
+        if lib().orc_sim_store_snapshot(self.h, os.fsencode(path)) != 0:
+            raise RuntimeError("oracle: snapshot write failed")
 
     @property
     def dt(self):

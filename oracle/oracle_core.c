@@ -11,6 +11,8 @@
  * nonlinear pass stays serial as in src/nonlin.F90:52-54.
  */
 #include <math.h>
+#include <stdint.h>
+#include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 #ifdef _OPENMP
@@ -2138,4 +2140,78 @@ int orc_sim_diagnostics(orc_sim* s, double* out) {
   out[4] = nus_t; out[5] = nus_b; out[6] = vis; out[7] = buo; out[8] = s->tot_time;
   free(ur2); free(up2); free(upb2); free(w2); free(urt); free(upg); free(urg); free(dT);
   return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Checkpoint and snapshot files: store_checkpoint / store_checkpoint_imexrk */
+/* and store_snapshot (src/output.F90:359-516), Fortran unformatted          */
+/* sequential records framed by their byte length (4-byte integers).          */
+/* ------------------------------------------------------------------------ */
+static int rec_write(FILE* f, const void* data, size_t bytes) {
+  int32_t n = (int32_t)bytes;
+  return fwrite(&n, 4, 1, f) == 1 && (bytes == 0 || fwrite(data, 1, bytes, f) == bytes) && fwrite(&n, 4, 1, f) == 1;
+}
+
+int orc_sim_store_checkpoint(const orc_sim* s, const char* path) {
+  int R = s->R, M = s->M, type = s->p.scheme_type;
+  int ni, ne, nmax, li, le; /* header orders, and levels of the rhs records */
+  if (type == ORC_TYPE_IMEX) {
+    ni = s->sch.n_imp; ne = s->sch.n_exp; nmax = ni > ne ? ni : ne; li = ni; le = ne;
+  } else {
+    ni = ne = nmax = s->sch.n_exp;
+    li = le = (type == ORC_TYPE_IMEXRK) ? 1 : ni;
+  }
+  FILE* f = fopen(path, "wb");
+  if (!f) return -1;
+  unsigned char hdr[36];
+  int32_t iv[5] = {s->Nm, R, ni, ne, nmax};
+  memcpy(hdr, &s->dt_new, 8); memcpy(hdr + 8, &s->tot_time, 8); memcpy(hdr + 16, iv, 20);
+  int ok = rec_write(f, hdr, 36);
+  double dta[8];
+  for (int i = 0; i < nmax; ++i) dta[i] = (i < 4) ? s->dt_array[i] : s->dt_array[3];
+  ok = ok && rec_write(f, dta, sizeof(double) * nmax);
+  size_t cf = 2 * (size_t)M * R;
+  ok = ok && rec_write(f, s->tFR, cf * sizeof(double)) && rec_write(f, s->omgFR, cf * sizeof(double)) &&
+       rec_write(f, s->urFR, cf * sizeof(double)) && rec_write(f, s->upFR, cf * sizeof(double));
+  int ms = (type == ORC_TYPE_IMEX);
+  /* (order, M, R) arrays are held in that layout; the uphi_bar ones are (R, order) and transposed */
+  const double* h3[4] = {ms ? s->rhs_imp_temp : NULL, ms ? s->rhs_exp_temp : NULL,
+                         ms ? s->rhs_imp_vort : NULL, ms ? s->rhs_exp_vort : NULL};
+  const int lv3[4] = {li, le, li, le};
+  for (int k = 0; k < 4 && ok; ++k) {
+    size_t n = cf * lv3[k];
+    double* z = zalloc(n);
+    if (h3[k]) memcpy(z, h3[k], n * sizeof(double));
+    ok = rec_write(f, z, n * sizeof(double));
+    free(z);
+  }
+  const double* h2[2] = {ms ? s->rhs_imp_uphi : NULL, ms ? s->rhs_exp_uphi : NULL};
+  const int lv2[2] = {li, le};
+  for (int k = 0; k < 2 && ok; ++k) {
+    int n = lv2[k];
+    double* z = zalloc(2 * (size_t)n * R);
+    if (h2[k])
+      for (int r = 0; r < R; ++r)
+        for (int io = 0; io < n; ++io) {
+          z[2 * (io + (size_t)n * r)] = h2[k][2 * ((size_t)R * io + r)];
+          z[2 * (io + (size_t)n * r) + 1] = h2[k][2 * ((size_t)R * io + r) + 1];
+        }
+    ok = rec_write(f, z, 2 * (size_t)n * R * sizeof(double));
+    free(z);
+  }
+  return (fclose(f) == 0 && ok) ? 0 : -1;
+}
+
+int orc_sim_store_snapshot(const orc_sim* s, const char* path) {
+  int R = s->R, M = s->M;
+  FILE* f = fopen(path, "wb");
+  if (!f) return -1;
+  double a[3] = {s->p.ra, s->p.pr, s->p.eta}, b[2] = {s->dt_new, s->tot_time};
+  int32_t nn[2] = {s->Nm, R};
+  size_t cf = 2 * (size_t)M * R;
+  int ok = rec_write(f, a, sizeof(a)) && rec_write(f, b, sizeof(b)) && rec_write(f, nn, sizeof(nn)) &&
+           rec_write(f, s->radius, sizeof(double) * R) && rec_write(f, s->tFR, cf * sizeof(double)) &&
+           rec_write(f, s->omgFR, cf * sizeof(double)) && rec_write(f, s->urFR, cf * sizeof(double)) &&
+           rec_write(f, s->upFR, cf * sizeof(double));
+  return (fclose(f) == 0 && ok) ? 0 : -1;
 }
