@@ -583,6 +583,7 @@ struct Scheme {
   double aD[kMaxStages][kMaxStages] = {{0}}, aA[kMaxStages][kMaxStages] = {{0}};
   double bD[kMaxStages] = {0}, bA[kMaxStages] = {0};
   bool check_A = false, check_D = false;
+  bool diag_diff = false;         // implicit diagonal varies by stage
   int diag = 1;
 };
 
@@ -681,17 +682,17 @@ int scheme_weights(int type, int imp, int exp, Scheme* s) {
     return 0;
   }
   if (type == FALCON_IMEXRK) {
-    // Butcher tables and the reference's ars_eqn_check / diag_index flags
-    // (imexrk_tables.h); stage-dependent implicit diagonals (diag_diff) and
-    // schemes with more than kMaxStages stages are not built.
+    // Butcher tables and the reference's ars_eqn_check / diag_diff /
+    // diag_index flags (imexrk_tables.h).
     imexrk_table t;
-    if (imexrk_table_get(imp, exp, &t) != 0 || t.diag_diff || t.n > kMaxStages) return -1;
+    if (imexrk_table_get(imp, exp, &t) != 0 || t.n > kMaxStages) return -1;
     s->n_imp = s->n_exp = t.n;
     for (int i = 0; i < t.n; ++i) {
       for (int j = 0; j < t.n; ++j) { s->aD[i][j] = t.aD[i][j]; s->aA[i][j] = t.aA[i][j]; }
       s->bD[i] = t.bD[i]; s->bA[i] = t.bA[i];
     }
     s->check_D = t.check_D != 0; s->check_A = t.check_A != 0;
+    s->diag_diff = t.diag_diff != 0;
     s->diag = t.diag_index - 1;
     return 0;
   }
@@ -737,6 +738,9 @@ struct Group {
   Scheme sch;
   int R = 0, M = 0, Nm = 0, P = 0, B = 0;
   std::shared_ptr<OpSet> ops;
+  // IMEXRK with a stage-dependent implicit diagonal: the operators of each
+  // stage whose diagonal differs from that of stage diag_index (null: ops)
+  std::shared_ptr<OpSet> stage_ops[kMaxStages];
   std::unique_ptr<FftTables> fft;
   std::vector<int> members;    // batch indices
   std::vector<double> ra_pr_h; // per instance Ra/Pr
@@ -841,11 +845,35 @@ int validate(const falcon_params& p) {
   if (p.l_restart) return fail(FALCON_EINVAL, "l_restart=.TRUE. is not supported by this build");
   Scheme s;
   if (scheme_weights(p.scheme_type, p.scheme_imp, p.scheme_exp, &s) != 0)
-  {
-    if (p.scheme_type == FALCON_IMEXRK && p.scheme_imp >= FALCON_IMP_KC774 && p.scheme_imp <= FALCON_IMP_LZ4A1)
-      return fail(FALCON_EINVAL, "IMEXRK schemes with 7-8 stages (KC774, KC885) or a stage-dependent implicit "
-                                 "diagonal (SMR333, CB3e, CB3f, CB4, LZ3L1, LZ3A4a, LZ4A1) are not supported by this build");
     return fail(FALCON_EINVAL, "unsupported time scheme combination");
+  // With diag_diff a stage solves with its own weight butcher_aD(st,st).  A
+  // zero weight leaves the coupled omega-psi operator of mat_build_IRK
+  // (src/mat_assembly.F90:131-160) singular: the omega wall coefficients
+  // enter no row.  The reference factorises it regardless and its run
+  // diverges in the first step (LZ3A4a, stages 2 and 4); refused here.
+  if (p.scheme_type == FALCON_IMEXRK && s.diag_diff)
+    for (int st = 1; st < s.n_exp; ++st)
+      if (s.aD[st][st] == 0.0)
+        return fail(FALCON_EINVAL, "IMEXRK scheme with a zero implicit diagonal at a stage (LZ3A4a): the reference's "
+                                   "coupled omega-psi operator for that stage is singular");
+  return 0;
+}
+
+// Operators of the IMEXRK stages whose implicit diagonal differs from that
+// of stage diag_index (diag_diff, src/fourierloop_imexrk.F90:134-160),
+// built with the weight butcher_aD(rk_stage,rk_stage) at time step dt.
+// Stages with equal diagonals share one set through the operator cache;
+// LAPpsi comes from the main set.
+int build_stage_ops(Group* g, double dt) {
+  const Scheme& sc = g->sch;
+  for (auto& so : g->stage_ops) so.reset();
+  if (g->p.scheme_type != FALCON_IMEXRK || !sc.diag_diff) return 0;
+  for (int st = 1; st < sc.n_exp; ++st) {
+    if (sc.aD[st][st] == sc.aD[sc.diag][sc.diag]) continue;
+    OpKey k = key_of(g->p, sc);
+    k.dt = dt; k.wt = sc.aD[st][st]; k.needs_lap = 0; k.lagpts = 0;
+    const int rc = build_opset(k, &g->stage_ops[st]);
+    if (rc) return rc;
   }
   return 0;
 }
@@ -859,6 +887,7 @@ int group_init(Group* g, const std::vector<falcon_params>& ps, const std::vector
     return fail(FALCON_EINVAL, "unsupported scheme");
   int rc;
   if ((rc = build_opset(key_of(g->p, g->sch), &g->ops))) return rc;
+  if ((rc = build_stage_ops(g, g->p.dt))) return rc;
   if ((rc = make_fft(g->P, &g->fft))) return rc;
   const size_t n = g->nel();
   const int R = g->R, B = g->B;
@@ -987,9 +1016,9 @@ int run_nonlin(Group* g) {
 // The implicit solves shared by IMEX and IMEXRK: temperature, then
 // buoyancy, then (omega, psi, u_phi) for m >= 1 and uphi_bar for m = 0.
 int solve_all(Group* g, double2* t_out, double2* w_out, double buo_scale, double2* buo_store,
-              double* ubar_store) {
+              double* ubar_store, const OpSet* o = nullptr) {
   const int R = g->R, M = g->M, B = g->B;
-  OpSet* o = g->ops.get();
+  if (!o) o = g->ops.get();
   cudaStream_t s = g->stream;
   int rc;
   if ((rc = gemm(g, KC_GEMM_MODE, per_mode(o->ST, R, (long)R * R, g->rhs_t, t_out, R, M, B, 0, M, R)))) return rc;
@@ -1180,6 +1209,7 @@ int step_imexrk(Group* g) {
         std::shared_ptr<OpSet> fresh;
         if ((rc = build_opset(k, &fresh))) return rc;
         g->ops = fresh;
+        if ((rc = build_stage_ops(g, k.dt))) return rc;
       }
     }
   }
@@ -1202,7 +1232,8 @@ int step_imexrk(Group* g) {
     if (st > 0) {
       if ((rc = elementwise(g, 12.0 * st + 8.0, [&]() { return launch_stage_rhs(a, s); }))) return rc;
       const double scale = g->p.buo_imp ? g->cur_dt() * sc.aD[st][st] : 0.0;
-      if ((rc = solve_all(g, g->T(), g->W(), scale, g->buo[st], nullptr))) return rc;
+      const OpSet* so = g->stage_ops[st] ? g->stage_ops[st].get() : o;
+      if ((rc = solve_all(g, g->T(), g->W(), scale, g->buo[st], nullptr, so))) return rc;
     }
     double colsum = 0.0;
     for (int i = 0; i < ns; ++i) colsum += sc.aA[i][st];
@@ -2297,10 +2328,14 @@ size_t falcon_batch_device_bytes(const falcon_batch* b) {
   std::vector<const OpSet*> seen;
   for (auto& g : b->groups) {
     s += g->bytes;
-    if (std::find(seen.begin(), seen.end(), g->ops.get()) == seen.end()) {
-      seen.push_back(g->ops.get());
-      s += g->ops->bytes;
-    }
+    std::vector<const OpSet*> sets{g->ops.get()};
+    for (auto& so : g->stage_ops)
+      if (so) sets.push_back(so.get());
+    for (const OpSet* o : sets)
+      if (std::find(seen.begin(), seen.end(), o) == seen.end()) {
+        seen.push_back(o);
+        s += o->bytes;
+      }
   }
   return s;
 }

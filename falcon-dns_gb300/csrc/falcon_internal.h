@@ -15,7 +15,7 @@
 namespace falcon {
 
 constexpr int kMaxRadix = 16;     // stages of a mixed-radix FFT plan
-constexpr int kMaxStages = 6;     // IMEXRK stages supported
+constexpr int kMaxStages = 8;     // IMEXRK stages supported (KC885 has 8)
 
 // Plan of the azimuthal transform of length P = 3*Nm.  Two forms:
 //  - pfa = 1 (P square-free, prime factors <= 31): Good-Thomas prime-factor

@@ -46,9 +46,13 @@ extern "C" {
 /* ---- scheme identifiers (namelist strings, src/timeschemes.F90:42-962) ---- */
 enum falcon_scheme_type { FALCON_IMEX = 0, FALCON_IMEXRK = 1, FALCON_RK = 2 };
 /* IMEXRK pairs use the same number for "XXX" (implicit) and "expXXX"
- * (explicit).  KC774, KC885 and the schemes whose implicit diagonal changes
- * by stage (SMR333, CB3e, CB3f, CB4, LZ3L1, LZ3A4a, LZ4A1) are recognised
- * and rejected at creation. */
+ * (explicit); all 31 pairs of the reference are built, up to 8 stages
+ * (KC885).  The schemes whose implicit diagonal changes by stage (diag_diff:
+ * SMR333, CB3e, CB3f, CB4, LZ3L1, LZ3A4a, LZ4A1) solve each stage with the
+ * operators of its own weight (src/fourierloop_imexrk.F90:134-160).
+ * LZ3A4a is rejected at creation: its stages 2 and 4 have a zero implicit
+ * weight, for which the reference's coupled omega-psi operator is singular
+ * (its runs diverge in the first step). */
 enum falcon_scheme_imp {
   FALCON_IMP_CN = 0, FALCON_IMP_BDF2 = 1, FALCON_IMP_BDF3 = 2, FALCON_IMP_BDF4 = 3,
   FALCON_IMP_ARS443 = 10, FALCON_IMP_ARS343 = 11, FALCON_IMP_BPR353 = 12,

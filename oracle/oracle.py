@@ -37,7 +37,8 @@ SCHEMES = {
 # IMEXRK pairs "XXX" / "expXXX" (same number for both halves)
 IMEXRK_IDS = {"ARS232": 14, "ARS233": 15, "EUL111": 30, "MARS343": 31, "IJ3": 32, "PC2": 33, "SSP332": 34,
               "SSP543": 35, "PR433": 36, "DBM453": 37, "KC343": 38, "KC564": 39, "FW53": 40, "CK222": 41,
-              "BPR442": 42, "CFN343": 43, "BHR553": 44, "CFN564": 45}
+              "BPR442": 42, "CFN343": 43, "BHR553": 44, "CFN564": 45, "KC774": 46, "KC885": 47,
+              "SMR333": 48, "CB3e": 49, "CB3f": 50, "CB4": 51, "LZ3L1": 52, "LZ3A4a": 53, "LZ4A1": 54}
 for _n, _i in IMEXRK_IDS.items():
     IMP[_n] = _i
     EXP["exp" + _n] = _i

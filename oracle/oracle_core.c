@@ -359,8 +359,9 @@ typedef struct {
   int n_imp, n_exp;          /* n_order_tscheme_imp / _exp (stages for RK) */
   double wt_lhs;
   double w_imp[4], w_exp[4];
-  double aD[6][6], bD[6], aA[6][6], bA[6];
+  double aD[8][8], bD[8], aA[8][8], bA[8];
   int check_A, check_D, diag_index; /* diag_index 0-based */
+  int diag_diff;             /* implicit diagonal varies by stage */
 } scheme_t;
 
 /* Variable-dt multistep weights with dt_array(1..4); constant dt reduces them
@@ -435,27 +436,21 @@ static void multistep_weights(const orc_params* p, const double* dta, scheme_t* 
   }
 }
 
-static int set_rows(double a[6][6], int n, const double* v) {
-  for (int i = 0; i < n; ++i)
-    for (int j = 0; j < n; ++j) a[i][j] = v[i * n + j];
-  return 0;
-}
-
 /* Butcher pairs: init_time_schemes src/timeschemes.F90:37-973 (stage counts),
  * rhs_update_wts_imp :1053-1612 and rhs_update_wts_exp :1733-2388. */
 /* IMEXRK Butcher tables (src/timeschemes.F90) from the shared table of
- * published coefficients; schemes with a stage-dependent implicit diagonal
- * (diag_diff) or more than 6 stages are not supported. */
+ * published coefficients (up to 8 stages). */
 static int butcher_tables(const orc_params* p, scheme_t* s) {
   imexrk_table t;
   memset(s->aD, 0, sizeof(s->aD)); memset(s->aA, 0, sizeof(s->aA));
   memset(s->bD, 0, sizeof(s->bD)); memset(s->bA, 0, sizeof(s->bA));
-  if (imexrk_table_get(p->scheme_imp, p->scheme_exp, &t) != 0 || t.diag_diff || t.n > 6) return -1;
+  if (imexrk_table_get(p->scheme_imp, p->scheme_exp, &t) != 0 || t.n > 8) return -1;
   for (int i = 0; i < t.n; ++i) {
     for (int j = 0; j < t.n; ++j) { s->aD[i][j] = t.aD[i][j]; s->aA[i][j] = t.aA[i][j]; }
     s->bD[i] = t.bD[i]; s->bA[i] = t.bA[i];
   }
   s->check_A = t.check_A; s->check_D = t.check_D; s->diag_index = t.diag_index - 1;
+  s->diag_diff = t.diag_diff;
   s->n_imp = t.n; s->n_exp = t.n;
   return 0;
 }
@@ -471,7 +466,7 @@ int orc_imexrk_table(int scheme, double* out) {
   for (int i = 0; i < n; ++i) out[k++] = t.bD[i];
   for (int i = 0; i < n; ++i) for (int j = 0; j < n; ++j) out[k++] = t.aA[i][j];
   for (int i = 0; i < n; ++i) out[k++] = t.bA[i];
-  out[k++] = t.check_D; out[k++] = t.check_A; out[k++] = t.diag_index;
+  out[k++] = t.check_D; out[k++] = t.check_A; out[k++] = t.diag_index; out[k++] = t.diag_diff;
   return 0;
 }
 
@@ -502,6 +497,9 @@ struct orc_sim {
   double *dtemp_a, *dtemp_d, *domg_a, *domg_d, *rhs_buo;
   /* operators */
   double *AT_all, *AF_all, *A_uphi; int *ipiv1, *ipiv2, *ipiv_uphi;
+  /* diag_diff: the operators of stages whose diagonal differs from that of
+   * stage diag_index (AT_all_IRK(:,:,:,rk_stage), ...), else NULL */
+  double *AT_st[8], *AF_st[8], *Au_st[8]; int *p1_st[8], *p2_st[8], *pu_st[8];
   double *LAPpsi_all; int *ipiv_lap;
   double *dw_rmin, *d2w_rmin, *dw_rmax, *d2w_rmax;
   double *dtval_r, *dtval_p, *dtval_rkr, *dtval_rkp;  /* get_dtvals of the last nonlinear pass */
@@ -584,6 +582,15 @@ orc_sim* orc_sim_create(const orc_params* p) {
     s->ipiv1 = (int*)calloc((size_t)R * M, sizeof(int));
     s->ipiv2 = (int*)calloc((size_t)2 * R * M, sizeof(int));
     s->ipiv_uphi = (int*)calloc((size_t)R, sizeof(int));
+    const int di = s->sch.diag_index;
+    for (int st = 1; st < ns && s->sch.diag_diff; ++st) {
+      if (s->sch.aD[st][st] == s->sch.aD[di][di]) continue;
+      s->AT_st[st] = zalloc((size_t)R * R * M); s->AF_st[st] = zalloc((size_t)4 * R * R * M);
+      s->Au_st[st] = zalloc((size_t)R * R);
+      s->p1_st[st] = (int*)calloc((size_t)R * M, sizeof(int));
+      s->p2_st[st] = (int*)calloc((size_t)2 * R * M, sizeof(int));
+      s->pu_st[st] = (int*)calloc((size_t)R, sizeof(int));
+    }
   } else if (p->scheme_type == ORC_TYPE_RK) {
     /* butcher_a / butcher_b of RK2 (midpoint) and RK4 (classical),
      * src/timeschemes.F90:1701-1720 */
@@ -646,6 +653,10 @@ void orc_sim_destroy(orc_sim* s) {
                   s->ipiv_uphi, s->LAPpsi_all, s->ipiv_lap, s->dw_rmin, s->d2w_rmin,
                   s->dw_rmax, s->d2w_rmax, s->dtval_r, s->dtval_p, s->dtval_rkr, s->dtval_rkp};
   for (size_t i = 0; i < sizeof(ptrs) / sizeof(ptrs[0]); ++i) free(ptrs[i]);
+  for (int st = 0; st < 8; ++st) {
+    free(s->AT_st[st]); free(s->AF_st[st]); free(s->Au_st[st]);
+    free(s->p1_st[st]); free(s->p2_st[st]); free(s->pu_st[st]);
+  }
   free(s);
 }
 
@@ -1460,11 +1471,15 @@ static void rhs_construct_stage(orc_sim* s, int st) {
   free(wk);
 }
 
-/* Get_stage_var, src/fourierloop_imexrk.F90:75-401 (diag_diff = .FALSE.) */
+/* Get_stage_var, src/fourierloop_imexrk.F90:75-401 */
 static void get_stage_var(orc_sim* s, int st, int n_step) {
   int R = s->R, M = s->M, ns = s->sch.n_exp;
   /* matrices at stage 2 of the first step, and again whenever dt changed
-   * (src/fourierloop_imexrk.F90:108-125) */
+   * (src/fourierloop_imexrk.F90:108-125).  With diag_diff (:134-160) the
+   * reference rebuilds under the same conditions at every stage, each stage
+   * whose diagonal differs from that of stage diag_index into a set of its
+   * own; the values do not change within a step, so they are built here
+   * together at stage 2. */
   if ((n_step == 1 && st == 1 && !s->mats_built) || (n_step > 1 && st == 1 && s->dt_array[0] != s->dt_array[1])) {
     double w = s->sch.aD[s->sch.diag_index][s->sch.diag_index];
     for (int m = 0; m < M; ++m) {
@@ -1472,8 +1487,22 @@ static void get_stage_var(orc_sim* s, int st, int n_step) {
                 s->AF_all + (size_t)4 * R * R * m, s->ipiv2 + (size_t)2 * R * m);
       mat_build_uphibar(s, s->dt_array[0], w, s->A_uphi, s->ipiv_uphi);
     }
+    for (int k = 1; k < ns; ++k) {
+      if (!s->AT_st[k]) continue;
+      double wk = s->sch.aD[k][k];
+      for (int m = 0; m < M; ++m)
+        mat_build(s, s->dt_array[0], m, wk, 1, s->AT_st[k] + (size_t)R * R * m, s->p1_st[k] + (size_t)R * m,
+                  s->AF_st[k] + (size_t)4 * R * R * m, s->p2_st[k] + (size_t)2 * R * m);
+      mat_build_uphibar(s, s->dt_array[0], wk, s->Au_st[k], s->pu_st[k]);
+    }
     s->mats_built = 1;
   }
+  const double* AT = s->AT_st[st] ? s->AT_st[st] : s->AT_all;
+  const double* AF = s->AT_st[st] ? s->AF_st[st] : s->AF_all;
+  const double* Au = s->AT_st[st] ? s->Au_st[st] : s->A_uphi;
+  const int* p1 = s->AT_st[st] ? s->p1_st[st] : s->ipiv1;
+  const int* p2 = s->AT_st[st] ? s->p2_st[st] : s->ipiv2;
+  const int* pu = s->AT_st[st] ? s->pu_st[st] : s->ipiv_uphi;
   double dt = s->dt_array[0];
   double rp = s->p.ra / s->p.pr;
   const double* rr = s->r_radius;
@@ -1504,7 +1533,7 @@ static void get_stage_var(orc_sim* s, int st, int n_step) {
       }
       rhs[0] = (m == 0) ? 1.0 : 0.0; rhs[1] = 0.0;
       rhs[2 * (R - 1)] = 0.0; rhs[2 * (R - 1) + 1] = 0.0;
-      matsolve_cplx(R, s->AT_all + (size_t)R * R * m, s->ipiv1 + (size_t)R * m, rhs, solw);
+      matsolve_cplx(R, AT + (size_t)R * R * m, p1 + (size_t)R * m, rhs, solw);
       orc_chebinvtran(R, rhs, tr);
       put_mode(s, s->tFR, m, tr);
       if (m == 0) {
@@ -1524,7 +1553,7 @@ static void get_stage_var(orc_sim* s, int st, int n_step) {
           }
         for (int r = 0; r < R; ++r) ru[r] = s->uphi_bar_spec[2 * r] + dt * (Fud[2 * r] + Fua[2 * r]);
         ru[0] = 0.0; ru[R - 1] = 0.0;
-        orc_dgetrs(R, s->A_uphi, s->ipiv_uphi, ru);
+        orc_dgetrs(R, Au, pu, ru);
         double* c = v + 14 * R; double* u = v + 16 * R; double* du = v + 18 * R;
         for (int r = 0; r < R; ++r) { c[2 * r] = ru[r]; c[2 * r + 1] = 0.0; }
         put_mode(s, s->upFC, 0, c);
@@ -1579,7 +1608,7 @@ static void get_stage_var(orc_sim* s, int st, int n_step) {
         }
         rf[2 * R] = 0.0; rf[2 * R + 1] = 0.0; rf[2 * (2 * R - 1)] = 0.0; rf[2 * (2 * R - 1) + 1] = 0.0;
         double* sw = zalloc(4 * (size_t)R);
-        matsolve_cplx(2 * R, s->AF_all + (size_t)4 * R * R * m, s->ipiv2 + (size_t)2 * R * m, rf, sw);
+        matsolve_cplx(2 * R, AF + (size_t)4 * R * R * m, p2 + (size_t)2 * R * m, rf, sw);
         free(sw);
         double* omr = v + 18 * R; double* psr = v + 20 * R; double* dps = v + 22 * R; double* ut = v + 24 * R;
         orc_chebinvtran(R, rf + 2 * R, omr);

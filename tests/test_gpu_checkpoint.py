@@ -48,13 +48,19 @@ def test_checkpoint_file_matches_oracle(orc, fg, tmp_path, scheme):
 
 
 # variable dt: settings under which dt changes every step (operators rebuilt
-# every step), so that the restored run and the uninterrupted one rebuild alike
+# every step), so that the restored run and the uninterrupted one rebuild alike.
+# Not stiffly accurate IMEXRK schemes take the CFL step from a nonlinear pass
+# on the assembled state in both runs.  Stiffly accurate ones take it from
+# the last nonlinear pass of the previous step, which the restored run does
+# not have; like the reference (src/steptime_imexrk.F90:109-117) it runs a
+# pass on the restored state instead, so those runs are not compared here.
 VARDT = dict(ra=1e6, vartimestep=True, cfl=0.02, dt_coef=1.5, dt_max=1e-4)
 
 
 @pytest.mark.parametrize("scheme,vardt", [("SBDF3", False), ("CNAB2", False), ("CNAB3", False), ("SBDF4", False),
                                           ("ARS443", False), ("ARS343", False), ("RK4", False),
-                                          ("SBDF3", True), ("ARS343", True)])
+                                          ("SBDF3", True), ("ARS343", True), ("CB4", False), ("SMR333", False),
+                                          ("CB3f", True)])
 def test_restart_continues_bit_for_bit(fg, tmp_path, scheme, vardt):
     R, Nm = 17, 8
     kw = dict(ra=1e5, dt=1e-6 if scheme.startswith("RK") else 1e-5)

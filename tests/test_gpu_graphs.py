@@ -14,7 +14,8 @@ FIELDS = ("T", "omg", "up", "ur", "psi")
 
 CASES = [("CNAB2", 17, 8, 1e4, 1e-4, 11), ("SBDF3", 33, 20, 1e5, 1e-5, 12),
          ("SBDF4", 17, 10, 1e4, 1e-5, 13), ("ARS443", 17, 10, 1e4, 1e-5, 14),
-         ("ARS343", 17, 10, 1e4, 1e-5, 15), ("SBDF3", 33, 20, 3e5, 1e-5, 16)]
+         ("ARS343", 17, 10, 1e4, 1e-5, 15), ("SBDF3", 33, 20, 3e5, 1e-5, 16),
+         ("CB4", 17, 10, 1e4, 1e-5, 17), ("KC885", 17, 8, 1e4, 1e-5, 18)]
 
 
 def run(fg, graphs, nsteps):

@@ -56,7 +56,8 @@ def test_variable_dt_instances_keep_their_own_step_in_a_batch(orc, fg):
 
 
 @pytest.mark.parametrize("scheme,optimize", [("ARS443", False), ("ARS343", False), ("BHR553", False),
-                                             ("BPR353", True), ("PC2", False)])
+                                             ("BPR353", True), ("PC2", False), ("SMR333", False),
+                                             ("CB3f", False), ("LZ4A1", True), ("KC885", False)])
 def test_variable_dt_imexrk_matches_oracle(orc, fg, scheme, optimize):
     # IMEXRK compute_new_dt (src/steptime_imexrk.F90:248-308), operators
     # rebuilt whenever dt changes
