@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <atomic>
 #include <cctype>
 #include <cmath>
@@ -784,6 +785,7 @@ struct Group {
   // state are taken by an extra nonlinear pass before compute_new_dt
   bool force_rebuild = false;
   bool need_cfl_pass = false;
+  bool restart_first = false;  // the next step is the first after a restart (l_restart)
   double dt_array[4] = {0, 0, 0, 0};
   double dt_new = 0.0;
   double* umax = nullptr;
@@ -842,7 +844,6 @@ int validate(const falcon_params& p) {
   if (p.mbc != 0 && p.mbc != 1) return fail(FALCON_EINVAL, "mBC must be NS or SF");
   if (p.l_vartimestep && !(p.cfl > 0.0 && p.dt_coef > 0.0 && p.dt_max > 0.0))
     return fail(FALCON_EINVAL, "l_vartimestep needs CFL, dt_coef and dt_max > 0");
-  if (p.l_restart) return fail(FALCON_EINVAL, "l_restart=.TRUE. is not supported by this build");
   Scheme s;
   if (scheme_weights(p.scheme_type, p.scheme_imp, p.scheme_exp, &s) != 0)
     return fail(FALCON_EINVAL, "unsupported time scheme combination");
@@ -1056,11 +1057,19 @@ int solve_all(Group* g, double2* t_out, double2* w_out, double buo_scale, double
 int vardt_update(Group* g, int nstep) {
   const falcon_params& p = g->p;
   const bool rk = (p.scheme_type == FALCON_RK);
-  if (rk || nstep <= 1) {
+  // First step after a restart (l_restart, n_step-n_restart == 1): dt_new
+  // starts from the namelist dt; the IMEXRK and RK loops also reset
+  // dt_array(:) (src/steptime_imexrk.F90:102-106, src/steptime_rk.F90:92-98)
+  // while the multistep loop keeps the restored history; compute_new_dt
+  // then sets dt_array(1) only, none of the "optimize" branches applying.
+  const bool first = g->restart_first;
+  g->restart_first = false;
+  if (rk || nstep <= 1 || (first && p.scheme_type == FALCON_IMEXRK)) {
     g->dt_new = p.dt;
     for (int i = 0; i < 4; ++i) g->dt_array[i] = p.dt;
   }
-  if (nstep <= 1) return 0;
+  if (first) g->dt_new = p.dt;
+  if (nstep <= 1 || (first && rk)) return 0;
   const int R = g->R;
   CK(cudaMemcpyAsync(g->umax_h.data(), g->umax, sizeof(double) * 2 * R, cudaMemcpyDeviceToHost, g->stream));
   CK(cudaStreamSynchronize(g->stream));
@@ -1085,12 +1094,17 @@ int vardt_update(Group* g, int nstep) {
   const double dt2 = std::fmin(0.5 * (1.0 / p.dt_coef + 1.0) * dt_n, p.dt_max);
   if (rk || p.l_optimizedt) {
     // dt keeps its previous value when no branch applies
-    if (g->dt_array[1] > p.dt_max) g->dt_new = p.dt_max;
+    if (first) {
+    } else if (g->dt_array[1] > p.dt_max) g->dt_new = p.dt_max;
     else if (g->dt_array[1] >= dt_cal) g->dt_new = dt2;
     else if (p.dt_coef * g->dt_array[1] < dt_cal && g->dt_array[1] < p.dt_max)
       g->dt_new = (g->dt_array[0] < dt2) ? dt2 : g->dt_array[0];
   } else {
     g->dt_new = dt2;
+  }
+  if (first) {
+    g->dt_array[0] = g->dt_new;
+    return 0;
   }
   const int nmax = (p.scheme_type == FALCON_IMEX) ? std::max(g->sch.n_imp, g->sch.n_exp) : 2;
   for (int i = nmax - 1; i >= 1; --i) g->dt_array[i] = g->dt_array[i - 1];
@@ -1867,6 +1881,328 @@ int group_load_checkpoint(Group* g, int b, const char* path) {
 }
 
 // store_snapshot (src/output.F90:487-516) for instance b.
+// ---------------------------------------------------------------------------
+// Restart (l_restart): get_checkpoint_data and read_checkpoint
+// (src/init.F90:447-935), the restart branch of init_fields (:183-204) and
+// the multistep bootstrap of timeloop_imex (src/steptime.F90:87-193 with
+// rhs_*_from_restart, src/rhs_create.F90:387-573).
+// ---------------------------------------------------------------------------
+struct CkptData {
+  double dt_new = 0.0, tot_time = 0.0;
+  int nm = 0, nr = 0, ni = 0, ne = 0, nmax = 0;
+  double dta[8] = {0};
+  std::vector<double> fld[4];        // tFR, omgFR, urFR, upFR: complex (nm+1, nr)
+  std::vector<double> h3[4], h2[2];  // rhs_imp/exp_temp, _vort (order, M, R); _uphi_bar (order, R)
+};
+
+// One record, or false at the end of the file or on a malformed frame.
+bool try_record(std::FILE* f, std::vector<char>* out) {
+  int32_t a = 0, b = 0;
+  if (std::fread(&a, 4, 1, f) != 1 || a < 0) return false;
+  out->resize((size_t)a);
+  if (a > 0 && std::fread(out->data(), 1, (size_t)a, f) != (size_t)a) return false;
+  return std::fread(&b, 4, 1, f) == 1 && b == a;
+}
+
+// read_checkpoint reads the header, dt_array and the four fields; the
+// history records after them are kept when they hold ni / ne levels (files
+// of the multistep loop) and left empty otherwise.
+int read_checkpoint_file(const std::string& path, CkptData* c) {
+  std::FILE* f = std::fopen(path.c_str(), "rb");
+  if (!f) return fail(FALCON_EIO, "checkpoint not found: " + path);
+  auto bad = [&](const char* what) {
+    std::fclose(f);
+    return fail(FALCON_EIO, std::string("checkpoint ") + path + ": " + what);
+  };
+  std::vector<char> rec;
+  if (!try_record(f, &rec) || rec.size() != 36) return bad("unexpected header record");
+  int32_t hd[5];
+  std::memcpy(&c->dt_new, rec.data(), 8);
+  std::memcpy(&c->tot_time, rec.data() + 8, 8);
+  std::memcpy(hd, rec.data() + 16, 20);
+  c->nm = hd[0]; c->nr = hd[1]; c->ni = hd[2]; c->ne = hd[3]; c->nmax = hd[4];
+  if (c->nm < 1 || c->nm > 4096 || c->nr < 4 || c->nr > 257 || c->ni < 1 || c->ne < 1 || c->ni > 8 ||
+      c->ne > 8 || c->nmax < 1 || c->nmax > 8)
+    return bad("invalid header");
+  if (!try_record(f, &rec) || rec.size() != sizeof(double) * c->nmax) return bad("dt_array size");
+  std::memcpy(c->dta, rec.data(), rec.size());
+  const size_t cf = (size_t)2 * (c->nm + 1) * c->nr;
+  for (int k = 0; k < 4; ++k) {
+    if (!try_record(f, &rec) || rec.size() != sizeof(double) * cf) return bad("field size");
+    c->fld[k].resize(cf);
+    std::memcpy(c->fld[k].data(), rec.data(), rec.size());
+  }
+  const int lv[6] = {c->ni, c->ne, c->ni, c->ne, c->ni, c->ne};
+  for (int k = 0; k < 6; ++k) {
+    if (!try_record(f, &rec)) break;
+    const size_t want = sizeof(double) * 2 * (size_t)lv[k] * (k < 4 ? (size_t)(c->nm + 1) * c->nr : (size_t)c->nr);
+    if (rec.size() != want) continue;
+    std::vector<double>& h = (k < 4) ? c->h3[k] : c->h2[k - 4];
+    h.resize(want / sizeof(double));
+    std::memcpy(h.data(), rec.data(), want);
+  }
+  std::fclose(f);
+  return 0;
+}
+
+// Fields of a checkpoint on a smaller grid (src/init.F90:726-861): per
+// radial line the unnormalised DCT-I of the old values, zero padding, the
+// DCT-I at the new length divided by 2(Nr-1), times (Nr-1)/(Nr_old-1); the
+// three steps are one Nr x Nr_old matrix, applied on the device to the four
+// fields at once.  Modes above the old Nm are zero.
+int resample_fields(Group* g, const CkptData& c, std::vector<double> out[4]) {
+  const int R = g->R, M = g->M, Ro = c.nr, Mo = c.nm + 1;
+  const double pi = 4.0 * std::atan(1.0);
+  auto cosn = [&](long a, long n) { return std::cos(pi * (double)(a % (2 * n)) / (double)n); };
+  std::vector<double> Q((size_t)R * Ro);
+  for (int i = 0; i < Ro; ++i)
+    for (int j = 0; j < R; ++j) {
+      double acc = 0.0;
+      for (int k = 0; k < Ro; ++k) {
+        const double wo = (i == 0) ? 1.0 : (i == Ro - 1) ? ((k & 1) ? -1.0 : 1.0) : 2.0 * cosn((long)i * k, Ro - 1);
+        const double wn = (k == 0) ? 1.0 : (k == R - 1) ? ((j & 1) ? -1.0 : 1.0) : 2.0 * cosn((long)k * j, R - 1);
+        acc += wn * wo;
+      }
+      Q[j + (size_t)R * i] = acc / (2.0 * (double)(R - 1)) * ((2.0 * (double)(R - 1)) / (2.0 * (double)(Ro - 1)));
+    }
+  const size_t nx = (size_t)2 * Ro * M * 4, ny = (size_t)2 * R * M * 4;
+  std::vector<double> X(nx, 0.0), Y(ny);
+  for (int r = 0; r < Ro; ++r)
+    for (int m = 0; m < Mo; ++m)
+      for (int f = 0; f < 4; ++f) {
+        X[2 * (((size_t)r * M + m) * 4 + f)] = c.fld[f][2 * (m + (size_t)Mo * r)];
+        X[2 * (((size_t)r * M + m) * 4 + f) + 1] = c.fld[f][2 * (m + (size_t)Mo * r) + 1];
+      }
+  double *dQ = nullptr, *dX = nullptr, *dY = nullptr;
+  cudaStream_t s = g->stream;
+  CK(cudaMallocAsync(&dQ, sizeof(double) * Q.size(), s));
+  CK(cudaMallocAsync(&dX, sizeof(double) * nx, s));
+  CK(cudaMallocAsync(&dY, sizeof(double) * ny, s));
+  CK(cudaMemcpyAsync(dQ, Q.data(), sizeof(double) * Q.size(), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(dX, X.data(), sizeof(double) * nx, cudaMemcpyHostToDevice, s));
+  GemmArgs q{};
+  q.A = dQ; q.lda = R;
+  q.X = dX; q.ldx = 2L * M * 4;
+  q.Y = dY; q.ldy = 2L * M * 4;
+  q.K = Ro; q.rows = R; q.N = 2 * M * 4; q.batch = 1; q.alpha = 1.0;
+  int rc = gemm(g, KC_GEMM_RADIAL, q);
+  if (rc == 0) {
+    CK(cudaMemcpyAsync(Y.data(), dY, sizeof(double) * ny, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+  }
+  CK(cudaFreeAsync(dQ, s)); CK(cudaFreeAsync(dX, s)); CK(cudaFreeAsync(dY, s));
+  CK(cudaStreamSynchronize(s));
+  if (rc) return rc;
+  for (int f = 0; f < 4; ++f) {
+    out[f].assign((size_t)2 * M * R, 0.0);
+    for (int r = 0; r < R; ++r)
+      for (int m = 0; m < M; ++m) {
+        out[f][2 * (m + (size_t)M * r)] = Y[2 * (((size_t)r * M + m) * 4 + f)];
+        out[f][2 * (m + (size_t)M * r) + 1] = Y[2 * (((size_t)r * M + m) * 4 + f) + 1];
+      }
+  }
+  return 0;
+}
+
+// Restart of every instance of group g, member b from the checkpoint files
+// "<dirs[b]>/checkpoint_%05d" with the member's n_restart_point:
+//  - a multistep scheme with l_imexrk_started (CN, BDF2, BDF3, BDF4) reads
+//    the last n_imp checkpoints and builds its histories from them: for each,
+//    oldest first, a nonlinear pass on that state, then its values as
+//    implicit entry n_imp-j and its explicit terms as explicit entry
+//    n_exp-j (1-based; j = 0 the oldest), so that for CN/AB3 the two
+//    explicit entries used by the first step both come from the last two
+//    states shifted by one, as in the reference;
+//  - another multistep restart takes the histories of the file (the
+//    reference's own reads of these records are commented out) with the
+//    order rules of src/init.F90:593-716;
+//  - IMEXRK and RK restart from one file, which may hold a smaller grid
+//    (Chebyshev resampling, zero Fourier modes above the old Nm).
+// The time step history follows src/init.F90:566-580; l_add_pert adds ampT
+// to every temperature entry.  Members of one group must restart to the same
+// time and dt history (they step together).
+int group_restart(Group* g, const std::vector<std::string>& dirs, const std::vector<const falcon_params*>& mp) {
+  const int R = g->R, M = g->M, B = g->B, Nm = g->Nm, type = g->p.scheme_type;
+  const int ni = g->sch.n_imp, ne = g->sch.n_exp;
+  const CkptShape sh = checkpoint_shape(g);
+  const bool started = type == FALCON_IMEX && g->p.l_imexrk_started;
+  const int nfiles = started ? ni : 1;
+  cudaStream_t s = g->stream;
+  int rc;
+  std::vector<std::vector<CkptData>> cd(B, std::vector<CkptData>(nfiles));
+  std::vector<std::array<double, 4>> dts(B);
+  for (int b = 0; b < B; ++b) {
+    if ((type == FALCON_IMEX) && ((mp[b]->l_imexrk_started != 0) != started))
+      return fail(FALCON_EINVAL, "restart: l_imexrk_started differs between instances of one operator group");
+    const int np = mp[b]->n_restart_point;
+    if (np - nfiles + 1 < 0) return fail(FALCON_EINVAL, "restart: n_restart_point too small for the scheme");
+    for (int j = 0; j < nfiles; ++j) {
+      char name[64];
+      std::snprintf(name, sizeof(name), "checkpoint_%05d", np - (nfiles - 1) + j);
+      const std::string path = (dirs[b].empty() ? std::string(".") : dirs[b]) + "/" + name;
+      if ((rc = read_checkpoint_file(path, &cd[b][j]))) return rc;
+    }
+    const CkptData& nw = cd[b][nfiles - 1];
+    const bool same = nw.nm == Nm && nw.nr == R;
+    if (!same && !(nw.nm <= Nm && nw.nr <= R))
+      return fail(FALCON_EINVAL, "restart: the checkpoint's grid is larger than the instance's");
+    if (!same && type == FALCON_IMEX)
+      return fail(FALCON_EINVAL, "restart: a multistep scheme cannot change grid (its histories are per grid point)");
+    for (int j = 0; j < nfiles; ++j)
+      if (started && (cd[b][j].nm != Nm || cd[b][j].nr != R))
+        return fail(FALCON_EINVAL, "restart: l_imexrk_started needs checkpoints of the instance's grid");
+    if (type == FALCON_IMEX && !started) {
+      for (int k = 0; k < 4; ++k)
+        if (nw.h3[k].empty()) return fail(FALCON_EINVAL, "restart: the checkpoint holds no multistep histories");
+      for (int k = 0; k < 2; ++k)
+        if (nw.h2[k].empty()) return fail(FALCON_EINVAL, "restart: the checkpoint holds no multistep histories");
+      if (ne > nw.ne && nw.ne > ni)
+        return fail(FALCON_EINVAL, "restart: explicit order extension reads beyond the implicit history");
+    }
+    // dt_array
+    std::array<double, 8> d;
+    d.fill(g->p.dt);
+    if (started) {
+      for (int j = 0; j < nfiles; ++j) d[nfiles - 1 - j] = cd[b][j].dta[0];
+    } else {
+      const int mo = nw.nmax;
+      for (int i = 0; i < std::min(sh.nmax, mo); ++i) d[i] = nw.dta[i];
+      for (int i = mo; i < sh.nmax; ++i) d[i] = d[mo - 1];
+    }
+    for (int i = 0; i < 4; ++i) dts[b][i] = d[i];
+    if (b > 0 && (dts[b] != dts[0] || nw.tot_time != cd[0][nfiles - 1].tot_time ||
+                  nw.dt_new != cd[0][nfiles - 1].dt_new))
+      return fail(FALCON_EINVAL, "restart: instances of one operator group must restart to the same time and dt");
+  }
+  g->drop_graphs();
+  if (type == FALCON_IMEX) { g->head = 0; g->head_e = 1 % ne; }
+  auto newest_fields = [&](int b, std::vector<double> f[4]) -> int {
+    const CkptData& nw = cd[b][nfiles - 1];
+    if (nw.nm == Nm && nw.nr == R) {
+      for (int k = 0; k < 4; ++k) f[k] = nw.fld[k];
+      return 0;
+    }
+    return resample_fields(g, nw, f);
+  };
+  auto put_state = [&](int b, std::vector<double> f[4]) -> int {
+    int e;
+    if ((e = scatter_field(g, b, f[0].data(), g->T())) || (e = scatter_field(g, b, f[1].data(), g->W())) ||
+        (e = scatter_field(g, b, f[2].data(), g->ur)) || (e = scatter_field(g, b, f[3].data(), g->up)))
+      return e;
+    return 0;
+  };
+  auto add_pert = [&](int b, std::vector<double>& t) {
+    if (!mp[b]->l_add_pert) return;
+    for (size_t e = 0; e < t.size() / 2; ++e) t[2 * e] = mp[b]->ampT + t[2 * e];
+  };
+  for (int b = 0; b < B; ++b) {
+    std::vector<double> f[4];
+    if ((rc = newest_fields(b, f))) return rc;
+    if (!started) add_pert(b, f[0]);
+    if ((rc = put_state(b, f)) || (rc = group_reset_instance(g, b))) return rc;
+  }
+  if (started) {
+    OpSet* o = g->ops.get();
+    const bool cn = (g->sch.imp == FALCON_IMP_CN);
+    for (int j = 0; j < nfiles; ++j) {
+      const int si = ni - 1 - j, se = ne - 1 - j;
+      for (int b = 0; b < B; ++b) {
+        std::vector<double> f[4];
+        for (int k = 0; k < 4; ++k) f[k] = cd[b][j].fld[k];
+        if ((rc = put_state(b, f))) return rc;
+      }
+      if ((rc = run_nonlin(g)) || (rc = gemm(g, KC_GEMM_RADIAL, radial(o->D1p, g->ntr, g->dntr, R, M, B))) ||
+          (rc = gemm(g, KC_GEMM_RADIAL, radial(o->D1p, g->nwr, g->dnwr, R, M, B))))
+        return rc;
+      // the explicit terms of this state, written by the right-hand-side
+      // kernel into explicit entry se (its right-hand sides are discarded)
+      RhsArgs a{};
+      a.R = R; a.M = M; a.B = B;
+      a.inv_r = o->inv_r; a.inv_r2 = o->inv_r2; a.ra_pr = g->ra_pr;
+      a.dt = g->cur_dt(); a.inv_pr = 1.0 / g->p.pr;
+      a.scheme_cn = cn ? 1 : 0;
+      a.n_imp = ni; a.n_exp = ne; a.wt_lhs = g->sch.wt_lhs;
+      for (int i = 0; i < ni; ++i) { a.th[i] = g->th[i]; a.wh[i] = g->wh[i]; a.ubh[i] = g->ubh[i]; }
+      for (int i = 0; i < ne; ++i) { a.nth[i] = g->nth[i]; a.nwh[i] = g->nwh[i]; a.uromh[i] = g->uromh[i]; }
+      a.nt_new = g->nth[se]; a.nw_new = g->nwh[se]; a.urom_new = g->uromh[se];
+      a.ntp = g->ntp; a.ntr = g->ntr; a.dntr = g->dntr; a.nwp = g->nwp; a.nwr = g->nwr; a.dnwr = g->dnwr;
+      a.lt = g->lt; a.lw = g->lw; a.lu0 = g->lu0;
+      a.rhs_t = g->rhs_t; a.rhs_w = g->rhs_w;
+      if ((rc = launch(g, KC_ELEMENTWISE, 0.0, [&]() { return launch_imex_rhs(a, s); }))) return rc;
+      // its values as implicit entry si (entry 0 is the current state itself)
+      const size_t n = g->nel();
+      if (si != 0) {
+        CK(cudaMemcpyAsync(g->th[si], g->th[0], sizeof(double2) * n, cudaMemcpyDeviceToDevice, s));
+        CK(cudaMemcpyAsync(g->wh[si], g->wh[0], sizeof(double2) * n, cudaMemcpyDeviceToDevice, s));
+      }
+      if ((rc = launch(g, KC_ELEMENTWISE, 0.0, [&]() { return launch_extract_mode0(R, M, B, g->up, g->ubh[si], s); })))
+        return rc;
+      CK(cudaStreamSynchronize(s));
+    }
+    for (int b = 0; b < B; ++b) {
+      if (!mp[b]->l_add_pert) continue;
+      std::vector<double> t = cd[b][nfiles - 1].fld[0];
+      add_pert(b, t);
+      if ((rc = scatter_field(g, b, t.data(), g->T()))) return rc;
+    }
+  } else if (type == FALCON_IMEX) {
+    // histories of the file, with the order rules of src/init.F90:593-716
+    for (int b = 0; b < B; ++b) {
+      const CkptData& nw = cd[b][nfiles - 1];
+      const int io_ = nw.ni, eo = nw.ne;
+      auto level3 = [&](const std::vector<double>& h, int n, int io, std::vector<double>* out) {
+        out->resize((size_t)2 * M * R);
+        for (size_t rm = 0; rm < (size_t)M * R; ++rm) {
+          (*out)[2 * rm] = h[2 * (io + (size_t)n * rm)];
+          (*out)[2 * rm + 1] = h[2 * (io + (size_t)n * rm) + 1];
+        }
+      };
+      auto level2 = [&](const std::vector<double>& h, int n, int io, std::vector<double>* out) {
+        out->assign((size_t)2 * R, 0.0);
+        for (int r = 0; r < R; ++r) (*out)[2 * r] = h[2 * (io + (size_t)n * r)];
+      };
+      std::vector<double> v;
+      // implicit entry io (0-based) becomes entry io+1 of the first step;
+      // the oldest is shifted out before any use
+      for (int io = 0; io + 1 < ni; ++io) {
+        const int src = std::min(io, io_ - 1);
+        const int k = (g->head + io + 1) % ni;
+        level3(nw.h3[0], io_, src, &v);
+        if ((rc = scatter_field(g, b, v.data(), g->th[k]))) return rc;
+        level3(nw.h3[2], io_, src, &v);
+        if ((rc = scatter_field(g, b, v.data(), g->wh[k]))) return rc;
+        level2(nw.h2[0], io_, src, &v);
+        if ((rc = scatter_real(g, b, v.data(), g->ubh[k]))) return rc;
+      }
+      // explicit entries; beyond the file's order they are the implicit entry
+      // n_exp_old (src/init.F90:673-679)
+      for (int io = 0; io < ne; ++io) {
+        const int k = (g->head_e + io) % ne;
+        const bool have = io < eo;
+        const int src = have ? io : std::min(eo - 1, io_ - 1);
+        level3(have ? nw.h3[1] : nw.h3[0], have ? eo : io_, src, &v);
+        if ((rc = scatter_field(g, b, v.data(), g->nth[k]))) return rc;
+        level3(have ? nw.h3[3] : nw.h3[2], have ? eo : io_, src, &v);
+        if ((rc = scatter_field(g, b, v.data(), g->nwh[k]))) return rc;
+        level2(have ? nw.h2[1] : nw.h2[0], have ? eo : io_, src, &v);
+        if ((rc = scatter_real(g, b, v.data(), g->uromh[k]))) return rc;
+      }
+    }
+  }
+  const CkptData& n0 = cd[0][nfiles - 1];
+  g->n_step = 1;  // the first step after a restart takes the nonlinear pass
+  g->tot_time = n0.tot_time;
+  if (g->vardt) {
+    for (int i = 0; i < 4; ++i) g->dt_array[i] = dts[0][i];
+    g->dt_new = n0.dt_new;
+    g->force_rebuild = true;
+    g->need_cfl_pass = (type == FALCON_IMEXRK);
+    g->restart_first = true;
+  }
+  CK(cudaStreamSynchronize(s));
+  return 0;
+}
+
 int group_store_snapshot(Group* g, int b, const char* path) {
   std::FILE* f = std::fopen(path, "wb");
   if (!f) return fail(FALCON_EIO, std::string("cannot write snapshot ") + path);
@@ -2054,6 +2390,7 @@ void initial_temperature(const falcon_params& p, int kind, double amp, uint64_t 
 // ---------------------------------------------------------------------------
 struct falcon_batch {
   std::vector<falcon_params> params;
+  bool restart_pending = false;  // l_restart set: falcon_batch_restart comes before the first step
   std::vector<std::unique_ptr<Group>> groups;
   std::vector<std::pair<int, int>> where;  // instance -> (group, slot)
   cudaStream_t stream = nullptr;
@@ -2108,6 +2445,8 @@ static int batch_create(const falcon_params* ps, int n, falcon_batch** out) {
     for (size_t j = 0; j < kv.second.size(); ++j) b->where[kv.second[j]] = {(int)b->groups.size(), (int)j};
     b->groups.push_back(std::move(g));
   }
+  for (int i = 0; i < n; ++i)
+    if (b->params[i].l_restart) b->restart_pending = true;
   if (b->groups.size() > 1) {
     // groups of different operator keys run concurrently, one stream each,
     // ordered after (and joined back into) the batch's stream in every step call
@@ -2357,6 +2696,7 @@ int falcon_batch_set_state(falcon_batch* b, int i, const double* tFR, const doub
   Group* g = b->groups[b->where[i].first].get();
   int rc = group_set_instance(g, b->where[i].second, tFR, omgFR, upFR, urFR);
   if (rc) return rc;
+  b->restart_pending = false;
   if (g->n_step == 0) g->tot_time = 0.0;
   return group_reset_instance(g, b->where[i].second);
 }
@@ -2374,6 +2714,7 @@ int falcon_batch_init_state(falcon_batch* b, int kind, double amp, const uint64_
     int rc = group_reset(g.get());
     if (rc) return rc;
   }
+  b->restart_pending = false;
   return b->sync();
 }
 
@@ -2386,6 +2727,8 @@ int falcon_batch_get_state(falcon_batch* b, int i, double* tFR, double* omgFR, d
 
 int falcon_batch_step(falcon_batch* b, int nsteps) {
   if (!b || nsteps < 0) return fail(FALCON_EINVAL, "invalid step arguments");
+  if (b->restart_pending)
+    return fail(FALCON_EINVAL, "l_restart is set: restore the state with falcon_restart before stepping");
   const bool fan = b->start != nullptr;
   if (fan) {
     CK(cudaEventRecord(b->start, b->stream));
@@ -2491,6 +2834,29 @@ int falcon_batch_store_snapshot(falcon_batch* b, int i, const char* path) {
   int rc = b->sync();
   if (rc) return rc;
   return group_store_snapshot(b->groups[b->where[i].first].get(), b->where[i].second, path);
+}
+
+int falcon_batch_restart(falcon_batch* b, const char* const* dirs) {
+  if (!b) return fail(FALCON_EINVAL, "null batch");
+  int rc = b->sync();
+  if (rc) return rc;
+  for (auto& g : b->groups) {
+    std::vector<std::string> d;
+    std::vector<const falcon_params*> mp;
+    for (int i : g->members) {
+      d.push_back((dirs && dirs[i]) ? std::string(dirs[i]) : std::string("."));
+      mp.push_back(&b->params[i]);
+    }
+    if ((rc = group_restart(g.get(), d, mp))) return rc;
+  }
+  b->restart_pending = false;
+  return b->sync();
+}
+
+int falcon_restart(falcon_handle* h, const char* dir) {
+  if (!h) return fail(FALCON_EINVAL, "null handle");
+  const char* d[1] = {dir};
+  return falcon_batch_restart(h->b, d);
 }
 
 int falcon_store_checkpoint(falcon_handle* h, const char* path) {

@@ -98,7 +98,7 @@ EXPORTS = (
     "falcon_batch_profile", "falcon_launch_count", "falcon_fp64_mma_peak_gflops",
     "falcon_nonlin_noalloc_dev", "falcon_set_step_graphs", "falcon_store_checkpoint", "falcon_load_checkpoint",
     "falcon_store_snapshot", "falcon_batch_store_checkpoint", "falcon_batch_load_checkpoint",
-    "falcon_batch_store_snapshot",
+    "falcon_batch_store_snapshot", "falcon_restart", "falcon_batch_restart",
 )
 
 
@@ -160,6 +160,8 @@ def lib():
         getattr(L, f).argtypes = [vp, ctypes.c_char_p]
     for f in ("falcon_batch_store_checkpoint", "falcon_batch_load_checkpoint", "falcon_batch_store_snapshot"):
         getattr(L, f).argtypes = [vp, ip, ctypes.c_char_p]
+    L.falcon_restart.argtypes = [vp, ctypes.c_char_p]
+    L.falcon_batch_restart.argtypes = [vp, P(ctypes.c_char_p)]
     _lib = L
     return L
 
@@ -189,7 +191,8 @@ def read_namelist(path):
 
 
 def make_params(nr, nm, scheme="CNAB2", eta=0.35, ra=1e5, pr=1.0, dt=1e-5, mbc="NS", lagpts=16,
-                buo="IMP", vartimestep=False, optimizedt=False, cfl=0.9, dt_coef=2.0, dt_max=3e-5):
+                buo="IMP", vartimestep=False, optimizedt=False, cfl=0.9, dt_coef=2.0, dt_max=3e-5,
+                imexrk_started=False, restart=False, restart_point=0, add_pert=False, ampT=None):
     p = default_params()
     p.nr_max, p.nm_max, p.eta, p.ra, p.pr, p.dt = nr, nm, eta, ra, pr, dt
     p.mbc = 0 if mbc == "NS" else 1
@@ -198,7 +201,12 @@ def make_params(nr, nm, scheme="CNAB2", eta=0.35, ra=1e5, pr=1.0, dt=1e-5, mbc="
     p.l_vartimestep = 1 if vartimestep else 0
     p.l_optimizedt = 1 if optimizedt else 0
     p.cfl, p.dt_coef, p.dt_max = cfl, dt_coef, dt_max
-    p.l_imexrk_started = 0
+    p.l_imexrk_started = 1 if imexrk_started else 0
+    p.l_restart = 1 if restart else 0
+    p.n_restart_point = restart_point
+    p.l_add_pert = 1 if add_pert else 0
+    if ampT is not None:
+        p.ampT = ampT
     typ, imp, exp = SCHEMES[scheme]
     check(lib().falcon_params_set_scheme(ctypes.byref(p), typ.encode(), imp.encode(), exp.encode()))
     return p
@@ -280,6 +288,11 @@ class Batch:
         """store_snapshot layout of instance i."""
         check(lib().falcon_batch_store_snapshot(self.h, i, os.fsencode(path)))
 
+    def restart(self, dirs):
+        """l_restart: every instance from "<dirs[i]>/checkpoint_%05d" (its n_restart_point)."""
+        arr = (ctypes.c_char_p * self.n)(*[os.fsencode(str(d)) for d in dirs])
+        check(lib().falcon_batch_restart(self.h, arr))
+
     def profile(self, nsteps):
         """Per-kernel-class CUDA-event times of `nsteps` steps (advances the state)."""
         stats = (KernelStat * 8)()
@@ -312,6 +325,9 @@ class Instance(Batch):
 
     def load_checkpoint(self, path):
         super().load_checkpoint(0, path)
+
+    def restart(self, directory):
+        super().restart([directory])
 
     def store_snapshot(self, path):
         super().store_snapshot(0, path)

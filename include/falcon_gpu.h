@@ -154,6 +154,25 @@ int falcon_store_checkpoint(falcon_handle* h, const char* path);
  * constant-dt run continues bit for bit.  Counterpart of read_checkpoint
  * (src/init.F90:865-935), which reads the state and dt only. */
 int falcon_load_checkpoint(falcon_handle* h, const char* path);
+/* l_restart = .TRUE.: restores the instance from the checkpoint files
+ * "<dir>/checkpoint_%05d" (dir NULL: the working directory) the way the
+ * reference starts a restarted run, replacing init_fields' restart branch
+ * (src/init.F90:183-204) with get_checkpoint_data / read_checkpoint
+ * (:447-935) and the restart block of timeloop_imex (src/steptime.F90:87-193):
+ *  - n_restart_point names the file; a multistep scheme (CN, BDF2, BDF3,
+ *    BDF4) with l_imexrk_started reads the last n_imp checkpoints (e.g. of
+ *    an IMEXRK run) and builds its histories from those states
+ *    (rhs_*_from_restart, src/rhs_create.F90:387-573);
+ *  - another multistep restart takes the histories stored in the file, with
+ *    the reference's rules for a change of order (src/init.F90:593-716);
+ *  - IMEXRK and RK may restart on a larger grid (Chebyshev resampling,
+ *    src/init.F90:726-861);
+ *  - dt_array follows src/init.F90:566-580; l_add_pert adds ampT to tFR.
+ * The first step after it follows the reference's restart step (nonlinear
+ * pass first, restart rules of compute_new_dt).  With l_restart set,
+ * falcon_step fails until this (or falcon_set_state / falcon_init_state)
+ * has given the state. */
+int falcon_restart(falcon_handle* h, const char* dir);
 /* Snapshot file in the layout of store_snapshot (src/output.F90:487-516):
  * Ra, Pr, eta; dt, time; Nm_max, Nr_max; radius; tFR, omgFR, urFR, upFR. */
 int falcon_store_snapshot(falcon_handle* h, const char* path);
@@ -178,6 +197,11 @@ int falcon_batch_diagnostics(falcon_batch* b, falcon_diag* out /* n entries */);
 int falcon_batch_store_checkpoint(falcon_batch* b, int i, const char* path);
 int falcon_batch_load_checkpoint(falcon_batch* b, int i, const char* path);
 int falcon_batch_store_snapshot(falcon_batch* b, int i, const char* path);
+/* falcon_restart for every instance, instance i from directory dirs[i]
+ * (dirs or dirs[i] NULL: the working directory) with its own
+ * n_restart_point.  Instances of one operator group step together, so
+ * they must restart to the same time and dt history. */
+int falcon_batch_restart(falcon_batch* b, const char* const* dirs);
 /* Optional: run every step of the batch on this stream (cudaStream_t). */
 int falcon_batch_set_stream(falcon_batch* b, void* stream);
 /* Device bytes held by the batch (state, history, operators, scratch). */

@@ -108,6 +108,12 @@ int orc_imexrk_table(int scheme, double* out);
 /* store_checkpoint / store_snapshot files (src/output.F90:359-516). */
 int orc_sim_store_checkpoint(const orc_sim* s, const char* path);
 int orc_sim_store_snapshot(const orc_sim* s, const char* path);
+/* l_restart: restore from "<dir>/checkpoint_%05d" files (get_checkpoint_data,
+ * src/init.F90:447-935, and the multistep bootstrap of src/steptime.F90:87-193
+ * when l_imexrk_started is set for CN/BDF2/BDF3/BDF4).  Returns 0, -2 (file
+ * missing or malformed), -3 (smaller grid), -4 (grid change with multistep
+ * histories), -5 (no usable multistep histories in the file). */
+int orc_sim_restart(orc_sim* s, const char* dir, int npoint, int add_pert, double ampT);
 /* Number of OpenMP threads the oracle uses (0 = runtime default). */
 void orc_set_threads(int n);
 

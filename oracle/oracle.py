@@ -96,6 +96,8 @@ def lib():
         L.orc_sim_dt.argtypes = [ctypes.c_void_p]
         L.orc_sim_store_checkpoint.argtypes = [ctypes.c_void_p, ctypes.c_char_p]
         L.orc_sim_store_snapshot.argtypes = [ctypes.c_void_p, ctypes.c_char_p]
+        L.orc_sim_restart.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int, ctypes.c_int,
+                                      ctypes.c_double]
         L.orc_sim_dt.restype = ctypes.c_double
         L.orc_noise_pair.argtypes = [ctypes.c_uint64, ctypes.c_int, ctypes.c_int, dp, dp]
         L.orc_set_threads.argtypes = [ctypes.c_int]
@@ -236,6 +238,12 @@ class Sim:
     def store_snapshot(self, path):
         if lib().orc_sim_store_snapshot(self.h, os.fsencode(path)) != 0:
             raise RuntimeError("oracle: snapshot write failed")
+
+    def restart(self, directory, npoint, add_pert=False, ampT=0.0):
+        """l_restart from "<directory>/checkpoint_%05d" files (see orc_sim_restart)."""
+        rc = lib().orc_sim_restart(self.h, os.fsencode(str(directory)), npoint, 1 if add_pert else 0, ampT)
+        if rc != 0:
+            raise RuntimeError("oracle: restart failed (%d)" % rc)
 
     @property
     def dt(self):

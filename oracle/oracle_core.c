@@ -506,8 +506,9 @@ struct orc_sim {
   scheme_t sch;
   double dt_array[4];
   double dt_new, tot_time;
-  int n_step;      /* steps completed */
+  int n_step;      /* steps completed (since the start or the restart) */
   int mats_built;
+  int restarted;   /* l_restart: the run continues from checkpoint files */
 };
 
 #define CX(a, m, r) ((a) + 2 * ((size_t)(m) + (size_t)M * (r)))
@@ -703,7 +704,7 @@ static double gasp_center(double c, double L) {
 static void reset_after_state(orc_sim* s) {
   int M = s->M, R = s->R;
   size_t cf = 2 * (size_t)M * R;
-  s->n_step = 0; s->tot_time = 0.0; s->mats_built = 0;
+  s->n_step = 0; s->tot_time = 0.0; s->mats_built = 0; s->restarted = 0;
   for (int i = 0; i < 4; ++i) s->dt_array[i] = s->p.dt;
   /* temp_spec = tFR, omg_spec = omgFR, upFC = upFR (src/init.F90:393-395) */
   memcpy(s->temp_spec, s->tFR, cf * sizeof(double));
@@ -1035,8 +1036,9 @@ static void shift_hist(orc_sim* s, double* rhs, const double* tmp, int nord, int
     }
 }
 
+/* n_step-n_restart>1 .or. l_restart .and. (.not. l_imexrk_started) */
 static int shift_condition(const orc_sim* s, int n_step) {
-  return (n_step > 1);  /* n_step-n_restart>1 .or. l_restart.and..not.started, no restart */
+  return (n_step > 1) || (s->restarted && !s->p.l_imexrk_started);
 }
 
 /* rhs_construct_temp, src/rhs_create.F90:24-140 */
@@ -1227,7 +1229,7 @@ static double minval(const double* v, int n) {
  * the RK loop (src/steptime_rk.F90:180-238): as the multistep one, but only
  * dt_array(2) is shifted; RK adds the diffusive scales to dt_cal and always
  * takes the "optimize" branch, after dt_array(:) was reset to dt. */
-static void compute_new_dt_rk(orc_sim* s, int rk) {
+static void compute_new_dt_rk(orc_sim* s, int rk, int n_step) {
   const orc_params* p = &s->p;
   int R = s->R;
   double dt_cal = fmin(minval(s->dtval_r, R), minval(s->dtval_p, R));
@@ -1237,18 +1239,24 @@ static void compute_new_dt_rk(orc_sim* s, int rk) {
   else dt_n = fmin(1.0 / p->pr, 1.0) * p->cfl * dt_cal;
   double dt2 = fmin(0.5 * (1.0 / p->dt_coef + 1.0) * dt_n, p->dt_max);
   if (rk || p->l_optimizedt) {
-    if (s->dt_array[1] > p->dt_max) s->dt_new = p->dt_max;
-    else if (s->dt_array[1] >= dt_cal) s->dt_new = dt2;
-    else if (p->dt_coef * s->dt_array[1] < dt_cal && s->dt_array[1] < p->dt_max)
-      s->dt_new = (s->dt_array[0] < dt2) ? dt2 : s->dt_array[0];
+    if (n_step > 1) {
+      if (s->dt_array[1] > p->dt_max) s->dt_new = p->dt_max;
+      else if (s->dt_array[1] >= dt_cal) s->dt_new = dt2;
+      else if (p->dt_coef * s->dt_array[1] < dt_cal && s->dt_array[1] < p->dt_max)
+        s->dt_new = (s->dt_array[0] < dt2) ? dt2 : s->dt_array[0];
+    }
   } else {
     s->dt_new = dt2;
+  }
+  if (n_step == 1) {  /* first step after a restart */
+    s->dt_array[0] = s->dt_new;
+    return;
   }
   s->dt_array[1] = s->dt_array[0];
   s->dt_array[0] = s->dt_new;
 }
 
-static void compute_new_dt_imex(orc_sim* s) {
+static void compute_new_dt_imex(orc_sim* s, int n_step) {
   const orc_params* p = &s->p;
   int R = s->R;
   double mr = s->dtval_r[0], mp = s->dtval_p[0];
@@ -1259,13 +1267,20 @@ static void compute_new_dt_imex(orc_sim* s) {
   else dt_n = fmin(1.0 / p->pr, 1.0) * p->cfl * dt_cal;
   double dt2 = fmin(0.5 * (1.0 / p->dt_coef + 1.0) * dt_n, p->dt_max);
   if (p->l_optimizedt) {
-    /* dt_new keeps its previous value when no branch applies */
-    if (s->dt_array[1] > p->dt_max) s->dt_new = p->dt_max;
-    else if (s->dt_array[1] >= dt_cal) s->dt_new = dt2;
-    else if (p->dt_coef * s->dt_array[1] < dt_cal && s->dt_array[1] < p->dt_max)
-      s->dt_new = (s->dt_array[0] < dt2) ? dt2 : s->dt_array[0];
+    /* dt_new keeps its previous value when no branch applies (all of them
+     * need n_step > 1 + n_restart) */
+    if (n_step > 1) {
+      if (s->dt_array[1] > p->dt_max) s->dt_new = p->dt_max;
+      else if (s->dt_array[1] >= dt_cal) s->dt_new = dt2;
+      else if (p->dt_coef * s->dt_array[1] < dt_cal && s->dt_array[1] < p->dt_max)
+        s->dt_new = (s->dt_array[0] < dt2) ? dt2 : s->dt_array[0];
+    }
   } else {
     s->dt_new = dt2;
+  }
+  if (n_step == 1) {  /* first step after a restart: the restored history stays */
+    s->dt_array[0] = s->dt_new;
+    return;
   }
   int nmax = s->sch.n_imp > s->sch.n_exp ? s->sch.n_imp : s->sch.n_exp;
   for (int i = nmax - 1; i >= 1; --i) s->dt_array[i] = s->dt_array[i - 1];
@@ -1277,13 +1292,13 @@ static void imex_step(orc_sim* s) {
   int n_step = s->n_step + 1;
   size_t cf = 2 * (size_t)M * R;
   if (n_step == 1) s->dt_new = s->p.dt;
-  if (n_step > 1) {
+  if (n_step > 1 || s->restarted) {
     nr_maxloop(s);
     memcpy(s->upFR_prev, s->upFR, cf * sizeof(double));
     memcpy(s->urFR_prev, s->urFR, cf * sizeof(double));
   }
-  if (s->p.l_vartimestep && n_step > 1) {
-    compute_new_dt_imex(s);
+  if (s->p.l_vartimestep && (n_step > 1 || s->restarted)) {
+    compute_new_dt_imex(s, n_step);
   } else {
     s->dt_new = s->p.dt;
     for (int i = 0; i < 4; ++i) s->dt_array[i] = s->p.dt;
@@ -1772,9 +1787,13 @@ static void imexrk_step(orc_sim* s) {
     for (int i = 0; i < 4; ++i) s->dt_array[i] = s->p.dt;
   }
   if (s->p.l_vartimestep) {
+    if (n_step == 1 && s->restarted) {
+      nr_maxloop(s);
+      compute_new_dt_rk(s, 0, n_step);
+    }
     if (n_step > 1) {
       if (!s->sch.check_A || !s->sch.check_D) nr_maxloop(s);
-      compute_new_dt_rk(s, 0);
+      compute_new_dt_rk(s, 0, n_step);
     }
   } else {
     s->dt_new = s->p.dt;
@@ -1784,7 +1803,7 @@ static void imexrk_step(orc_sim* s) {
     if (st > 0) get_stage_var(s, st, n_step);
     double colsum = 0.0;
     for (int i = 0; i < ns; ++i) colsum += s->sch.aA[i][st];
-    if ((n_step > 1 || st > 0) && (colsum + s->sch.bA[st] != 0.0)) nr_maxloop(s);
+    if ((n_step > 1 || st > 0 || s->restarted) && (colsum + s->sch.bA[st] != 0.0)) nr_maxloop(s);
     rhs_construct_stage(s, st);
   }
   if (!s->sch.check_A || !s->sch.check_D) assembly_stage(s);
@@ -2061,10 +2080,10 @@ static void rk_step(orc_sim* s) {
    * compute_new_dt from the last nonlinear pass */
   s->dt_new = s->p.dt;
   for (int i = 0; i < 4; ++i) s->dt_array[i] = s->p.dt;
-  if (s->p.l_vartimestep && n_step > 1) compute_new_dt_rk(s, 1);
+  if (s->p.l_vartimestep && n_step > 1) compute_new_dt_rk(s, 1, n_step);
   for (int st = 0; st < ns; ++st) {
     if (st > 0) rk_get_stage_var(s, st);
-    if (n_step > 1 || st > 0) nr_maxloop(s);
+    if (n_step > 1 || st > 0 || s->restarted) nr_maxloop(s);
     rk_rhs_construct_stage(s, st);
   }
   rk_assembly_stage(s);
@@ -2243,4 +2262,291 @@ int orc_sim_store_snapshot(const orc_sim* s, const char* path) {
            rec_write(f, s->omgFR, cf * sizeof(double)) && rec_write(f, s->urFR, cf * sizeof(double)) &&
            rec_write(f, s->upFR, cf * sizeof(double));
   return (fclose(f) == 0 && ok) ? 0 : -1;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Restart (l_restart): read_checkpoint and get_checkpoint_data             */
+/* (src/init.F90:447-935), the restart branch of init_fields (:183-204) and  */
+/* the multistep bootstrap of timeloop_imex (src/steptime.F90:87-193) with   */
+/* rhs_*_from_restart (src/rhs_create.F90:387-573).                          */
+/* ------------------------------------------------------------------------ */
+static int rec_read(FILE* f, double** buf, size_t* bytes) {
+  int32_t n1, n2;
+  *buf = NULL;
+  if (fread(&n1, 4, 1, f) != 1 || n1 < 0) return -1;
+  *buf = (double*)malloc(n1 ? (size_t)n1 : 8);
+  if (n1 && fread(*buf, 1, (size_t)n1, f) != (size_t)n1) return -1;
+  if (fread(&n2, 4, 1, f) != 1 || n2 != n1) return -1;
+  *bytes = (size_t)n1;
+  return 0;
+}
+
+typedef struct {
+  double dt_new, tot_time;
+  int nm, nr, ni, ne, nmax;
+  double dta[8];
+  double* fld[4];  /* tFR, omgFR, urFR, upFR: complex (nm+1, nr) */
+  double* h3[4];   /* rhs_imp_temp, rhs_exp_temp, rhs_imp_vort, rhs_exp_vort (order, M, R) */
+  double* h2[2];   /* rhs_imp_uphi_bar, rhs_exp_uphi_bar (order, R) */
+} ckpt_t;
+
+static void ckpt_free(ckpt_t* c) {
+  for (int k = 0; k < 4; ++k) { free(c->fld[k]); free(c->h3[k]); }
+  for (int k = 0; k < 2; ++k) free(c->h2[k]);
+}
+
+/* read_checkpoint (src/init.F90:865-935) reads the header, dt_array and the
+ * four fields; the history records that follow are read here as well when
+ * they hold ni / ne levels (files of the multistep loop), else left NULL. */
+static int ckpt_read(const char* path, ckpt_t* c) {
+  memset(c, 0, sizeof(*c));
+  FILE* f = fopen(path, "rb");
+  if (!f) return -1;
+  double* b = NULL;
+  size_t n = 0;
+  int ok = rec_read(f, &b, &n) == 0 && n == 36;
+  if (ok) {
+    int32_t iv[5];
+    memcpy(&c->dt_new, b, 8); memcpy(&c->tot_time, (char*)b + 8, 8); memcpy(iv, (char*)b + 16, 20);
+    c->nm = iv[0]; c->nr = iv[1]; c->ni = iv[2]; c->ne = iv[3]; c->nmax = iv[4];
+    ok = c->nm >= 1 && c->nr >= 4 && c->ni >= 1 && c->ne >= 1 && c->nmax >= 1 && c->nmax <= 8;
+  }
+  free(b);
+  ok = ok && rec_read(f, &b, &n) == 0 && n == sizeof(double) * (size_t)c->nmax;
+  if (ok) memcpy(c->dta, b, n);
+  free(b);
+  size_t cf = 2 * (size_t)(c->nm + 1) * c->nr;
+  for (int k = 0; k < 4 && ok; ++k) {
+    ok = rec_read(f, &c->fld[k], &n) == 0 && n == cf * sizeof(double);
+  }
+  const int lv[6] = {c->ni, c->ne, c->ni, c->ne, c->ni, c->ne};
+  for (int k = 0; k < 6 && ok; ++k) {
+    double* h = NULL;
+    if (rec_read(f, &h, &n) != 0) { free(h); break; }
+    size_t want = sizeof(double) * 2 * (size_t)lv[k] * (k < 4 ? (size_t)(c->nm + 1) * c->nr : (size_t)c->nr);
+    if (n != want) { free(h); continue; }
+    if (k < 4) c->h3[k] = h; else c->h2[k - 4] = h;
+  }
+  fclose(f);
+  if (!ok) { ckpt_free(c); return -1; }
+  return 0;
+}
+
+/* Grid change at restart (src/init.F90:726-861): per radial line, the
+ * unnormalised DCT-I of the old values (chebtransform_redft), zero padding
+ * to the new length, the DCT-I at the new length divided by 2(Nr-1)
+ * (chebinvtran_redft), then the factor (Nr-1)/(Nr_old-1). */
+static void cheb_resample(int ro, int rn, const double* x, double* y) {
+  double* c = zalloc(2 * (size_t)rn);
+  redft00_cplx(ro, x, c);
+  for (int k = ro; k < rn; ++k) { c[2 * k] = 0.0; c[2 * k + 1] = 0.0; }
+  redft00_cplx(rn, c, y);
+  double fac = (2.0 * (double)(rn - 1)) / (2.0 * (double)(ro - 1));
+  for (int i = 0; i < 2 * rn; ++i) y[i] = y[i] / (2.0 * (double)(rn - 1));
+  for (int i = 0; i < 2 * rn; ++i) y[i] = y[i] * fac;
+  free(c);
+}
+
+/* rhs_temp/vort/uphibar_from_restart for the state held in tFR..upFR after
+ * a nonlinear pass on it: implicit slot si, explicit slot se (0-based). */
+static void history_from_state(orc_sim* s, int si, int se) {
+  int R = s->R, M = s->M, ni = s->sch.n_imp, ne = s->sch.n_exp;
+  const double* rr = s->r_radius;
+  double rp = s->p.ra / s->p.pr;
+  double* wk = zalloc(8 * (size_t)R);
+  double* a = wk; double* b = wk + 2 * R; double* bs = wk + 4 * R; double* db = wk + 6 * R;
+  for (int m = 0; m < M; ++m) {
+    double dm = (double)m;
+    for (int f = 0; f < 2; ++f) {
+      get_mode(s, f == 0 ? s->uphi_temp_FR : s->uphi_omg_FR, m, a);
+      get_mode(s, f == 0 ? s->ur_temp_FR : s->ur_omg_FR, m, b);
+      orc_chebtransform(R, b, bs);
+      orc_chebinvtranD1(R, bs, db);
+      double* imp = f == 0 ? s->rhs_imp_temp : s->rhs_imp_vort;
+      double* ex = f == 0 ? s->rhs_exp_temp : s->rhs_exp_vort;
+      const double* st = f == 0 ? s->tFR : s->omgFR;
+      for (int i = 0; i < R; ++i) {
+        double* hi = hist(imp, ni, si, M, m, i);
+        double* he = hist(ex, ne, se, M, m, i);
+        hi[0] = CX(st, m, i)[0]; hi[1] = CX(st, m, i)[1];
+        double ar, ai;
+        cmul(0.0, dm * rr[i], a[2 * i], a[2 * i + 1], &ar, &ai);
+        he[0] = ar + db[2 * i] + rr[i] * b[2 * i];
+        he[1] = ai + db[2 * i + 1] + rr[i] * b[2 * i + 1];
+        if (f == 1) {
+          double* bu = hist(s->rhs_buo_term, ni, si, M, m, i);
+          double br, bi;
+          cmul(0.0, dm * rr[i], CX(s->tFR, m, i)[0], CX(s->tFR, m, i)[1], &br, &bi);
+          bu[0] = -rp * br; bu[1] = -rp * bi;
+        }
+      }
+    }
+  }
+  mean_ur_omg(s, wk);
+  for (int i = 0; i < R; ++i) {
+    s->rhs_imp_uphi[2 * ((size_t)R * si + i)] = CX(s->upFR, 0, i)[0];
+    s->rhs_imp_uphi[2 * ((size_t)R * si + i) + 1] = CX(s->upFR, 0, i)[1];
+    s->rhs_exp_uphi[2 * ((size_t)R * se + i)] = wk[i];
+    s->rhs_exp_uphi[2 * ((size_t)R * se + i) + 1] = 0.0;
+  }
+  free(wk);
+}
+
+int orc_sim_restart(orc_sim* s, const char* dir, int npoint, int add_pert, double ampT) {
+  const int type = s->p.scheme_type, R = s->R, M = s->M, Nm = s->Nm;
+  const int ni = s->sch.n_imp, ne = s->sch.n_exp;
+  const int started = (type == ORC_TYPE_IMEX) && s->p.l_imexrk_started;
+  const int nfiles = started ? ni : 1;  /* CN, BDF2: 2 files; BDF3: 3; BDF4: 4 */
+  const size_t cf = 2 * (size_t)M * R;
+  if (npoint - nfiles + 1 < 0) return -1;
+  ckpt_t c[4];
+  memset(c, 0, sizeof(c));
+  int rc = 0;
+  for (int j = 0; j < nfiles && rc == 0; ++j) {
+    char path[4096];
+    snprintf(path, sizeof(path), "%s/checkpoint_%05d", dir, npoint - (nfiles - 1) + j);
+    if (ckpt_read(path, &c[j]) != 0) rc = -2;
+  }
+  const ckpt_t* nw = &c[nfiles - 1];
+  if (rc == 0) {
+    int same = nw->nm == Nm && nw->nr == R;
+    int grow = nw->nm <= Nm && nw->nr <= R && !same;
+    if (!same && !grow) rc = -3;                       /* a smaller grid is not restored */
+    if (!same && type == ORC_TYPE_IMEX) rc = -4;       /* histories cannot change grid */
+    for (int j = 0; j < nfiles && rc == 0 && started; ++j)
+      if (c[j].nm != Nm || c[j].nr != R) rc = -4;
+    if (rc == 0 && type == ORC_TYPE_IMEX && !started && !(nw->h3[0] && nw->h3[1] && nw->h2[0] && nw->h2[1]))
+      rc = -5;                                         /* no multistep histories in the file */
+    if (rc == 0 && type == ORC_TYPE_IMEX && !started && nw->ne > ni && ne > nw->ne) rc = -5;
+  }
+  if (rc != 0) {
+    for (int j = 0; j < nfiles; ++j) ckpt_free(&c[j]);
+    return rc;
+  }
+  /* dt_array */
+  int nmax = ni > ne ? ni : ne;
+  double dta[8];
+  for (int i = 0; i < 8; ++i) dta[i] = s->p.dt;
+  if (started) {
+    for (int j = 0; j < nfiles; ++j) dta[nfiles - 1 - j] = c[j].dta[0];
+  } else {
+    int mo = nw->nmax;
+    for (int i = 0; i < (nmax < mo ? nmax : mo); ++i) dta[i] = nw->dta[i];
+    for (int i = mo; i < nmax; ++i) dta[i] = dta[mo - 1];
+  }
+  for (int i = 0; i < 4; ++i) s->dt_array[i] = dta[i];
+  /* zero every history and stage store, as allocated */
+  if (s->rhs_imp_temp) {
+    memset(s->rhs_imp_temp, 0, cf * ni * sizeof(double)); memset(s->rhs_imp_vort, 0, cf * ni * sizeof(double));
+    memset(s->rhs_buo_term, 0, cf * ni * sizeof(double)); memset(s->rhs_exp_temp, 0, cf * ne * sizeof(double));
+    memset(s->rhs_exp_vort, 0, cf * ne * sizeof(double));
+    memset(s->rhs_imp_uphi, 0, 2 * (size_t)R * ni * sizeof(double));
+    memset(s->rhs_exp_uphi, 0, 2 * (size_t)R * ne * sizeof(double));
+  }
+  if (s->dtemp_a) {
+    memset(s->dtemp_a, 0, cf * ne * sizeof(double)); memset(s->dtemp_d, 0, cf * ne * sizeof(double));
+    memset(s->domg_a, 0, cf * ne * sizeof(double)); memset(s->domg_d, 0, cf * ne * sizeof(double));
+    memset(s->rhs_buo, 0, cf * ne * sizeof(double));
+  }
+  double* dst[4] = {s->tFR, s->omgFR, s->urFR, s->upFR};
+  if (started) {
+    /* timeloop_imex restart branch: for each stored step, oldest first, a
+     * nonlinear pass on it and its history entries; implicit slot
+     * n_imp - j, explicit slot n_exp - j (0-based, j = 0 the oldest) */
+    for (int j = 0; j < nfiles; ++j) {
+      for (int k = 0; k < 4; ++k) memcpy(dst[k], c[j].fld[k], cf * sizeof(double));
+      nr_maxloop(s);
+      history_from_state(s, ni - 1 - j, ne - 1 - j);
+    }
+  } else if (nw->nm == Nm && nw->nr == R) {
+    for (int k = 0; k < 4; ++k) memcpy(dst[k], nw->fld[k], cf * sizeof(double));
+    if (type == ORC_TYPE_IMEX) {
+      /* the file's histories with the order rules of src/init.F90:593-716
+       * (the reference's own read of these records is commented out) */
+      int io_ = nw->ni, eo = nw->ne;
+      for (int i = 0; i < ni; ++i) {
+        int src = i < io_ ? i : io_ - 1;
+        for (size_t mr = 0; mr < (size_t)M * R; ++mr)
+          for (int q = 0; q < 2; ++q) {
+            s->rhs_imp_temp[2 * (i + (size_t)ni * mr) + q] = nw->h3[0][2 * (src + (size_t)io_ * mr) + q];
+            s->rhs_imp_vort[2 * (i + (size_t)ni * mr) + q] = nw->h3[2][2 * (src + (size_t)io_ * mr) + q];
+          }
+        for (int r = 0; r < R; ++r)
+          for (int q = 0; q < 2; ++q)
+            s->rhs_imp_uphi[2 * ((size_t)R * i + r) + q] = nw->h2[0][2 * (src + (size_t)io_ * r) + q];
+      }
+      for (int i = 0; i < ne; ++i) {
+        for (size_t mr = 0; mr < (size_t)M * R; ++mr)
+          for (int q = 0; q < 2; ++q) {
+            if (i < eo) {
+              s->rhs_exp_temp[2 * (i + (size_t)ne * mr) + q] = nw->h3[1][2 * (i + (size_t)eo * mr) + q];
+              s->rhs_exp_vort[2 * (i + (size_t)ne * mr) + q] = nw->h3[3][2 * (i + (size_t)eo * mr) + q];
+            } else {  /* rhs_exp(j) = rhs_imp(n_exp_old), src/init.F90:673-679 */
+              s->rhs_exp_temp[2 * (i + (size_t)ne * mr) + q] = s->rhs_imp_temp[2 * ((eo - 1) + (size_t)ni * mr) + q];
+              s->rhs_exp_vort[2 * (i + (size_t)ne * mr) + q] = s->rhs_imp_vort[2 * ((eo - 1) + (size_t)ni * mr) + q];
+            }
+          }
+        for (int r = 0; r < R; ++r)
+          for (int q = 0; q < 2; ++q)
+            s->rhs_exp_uphi[2 * ((size_t)R * i + r) + q] =
+                i < eo ? nw->h2[1][2 * (i + (size_t)eo * r) + q] : s->rhs_imp_uphi[2 * ((size_t)R * (eo - 1) + r) + q];
+      }
+    }
+  } else {
+    /* larger grid (IMEXRK, RK): modes above the old Nm are zero */
+    int mo = nw->nm + 1, ro = nw->nr;
+    double* x = zalloc(2 * (size_t)ro);
+    double* y = zalloc(2 * (size_t)R);
+    for (int k = 0; k < 4; ++k) {
+      memset(dst[k], 0, cf * sizeof(double));
+      for (int m = 0; m < M; ++m) {
+        for (int r = 0; r < ro; ++r) {
+          x[2 * r] = m < mo ? nw->fld[k][2 * (m + (size_t)mo * r)] : 0.0;
+          x[2 * r + 1] = m < mo ? nw->fld[k][2 * (m + (size_t)mo * r) + 1] : 0.0;
+        }
+        cheb_resample(ro, R, x, y);
+        put_mode(s, dst[k], m, y);
+      }
+    }
+    free(x); free(y);
+  }
+  if (s->rhs_imp_temp) {
+    memcpy(s->tmp_imp_temp, s->rhs_imp_temp, cf * ni * sizeof(double));
+    memcpy(s->tmp_exp_temp, s->rhs_exp_temp, cf * ne * sizeof(double));
+    memcpy(s->tmp_imp_vort, s->rhs_imp_vort, cf * ni * sizeof(double));
+    memcpy(s->tmp_exp_vort, s->rhs_exp_vort, cf * ne * sizeof(double));
+    memcpy(s->tmp_buo_term, s->rhs_buo_term, cf * ni * sizeof(double));
+    memcpy(s->tmp_imp_uphi, s->rhs_imp_uphi, 2 * (size_t)R * ni * sizeof(double));
+    memcpy(s->tmp_exp_uphi, s->rhs_exp_uphi, 2 * (size_t)R * ne * sizeof(double));
+  }
+  /* init_fields, restart branch */
+  if (add_pert)
+    for (size_t e = 0; e < (size_t)M * R; ++e) s->tFR[2 * e] = ampT + s->tFR[2 * e];
+  memcpy(s->temp_spec, s->tFR, cf * sizeof(double));
+  memcpy(s->omg_spec, s->omgFR, cf * sizeof(double));
+  for (int r = 0; r < R; ++r) {
+    s->uphi_bar_spec[2 * r] = CX(s->upFR, 0, r)[0];
+    s->uphi_bar_spec[2 * r + 1] = CX(s->upFR, 0, r)[1];
+  }
+  /* upFC is not assigned by the reference's restart; the Chebyshev transform
+   * of u_phi is what a continuing run holds */
+  {
+    double* v = zalloc(4 * (size_t)R);
+    for (int m = 0; m < M; ++m) {
+      get_mode(s, s->upFR, m, v);
+      orc_chebtransform(R, v, v + 2 * R);
+      put_mode(s, s->upFC, m, v + 2 * R);
+    }
+    free(v);
+  }
+  memcpy(s->upFR_prev, s->upFR, cf * sizeof(double));
+  memcpy(s->urFR_prev, s->urFR, cf * sizeof(double));
+  memset(s->psii, 0, cf * sizeof(double));
+  s->tot_time = nw->tot_time;
+  s->dt_new = nw->dt_new;
+  s->n_step = 0;
+  s->mats_built = 0;
+  s->restarted = 1;
+  for (int j = 0; j < nfiles; ++j) ckpt_free(&c[j]);
+  return 0;
 }
