@@ -9,6 +9,9 @@
 #include <math.h>
 #include <stdio.h>
 
+#include <algorithm>
+#include <unordered_map>
+
 #include "falcon_internal.h"
 
 namespace falcon {
@@ -510,51 +513,71 @@ cudaError_t launch_nonlin(const NonlinArgs& a, cudaStream_t s) {
 
 // ---------------------------------------------------------------------------
 // Register-tiled FP64 GEMM, Y = alpha * A * X (A column-major, rows x K).
-// nw warps per block (runtime); warp w owns RPT consecutive rows
-// [row0 + w*RPT, +RPT), lane owns columns n0 + 2*lane + {0,1}.  K is staged
-// in chunks of 16 through shared memory; the last chunk runs only its valid
-// length, and nw*RPT is chosen on the host to cover the rows with little
-// padding, so the FP64 pipe does almost no wasted FMAs.
+// A block covers NCOL columns (64, 32 or 16) and nw * RG * RPT rows, RG =
+// 64 / NCOL: lane = (row group rg, column pair cp) with NCOL / 2 column
+// pairs, so warp w owns rows [row0 + (w*RG + rg)*RPT, +RPT) and columns
+// n0 + 2*cp + {0,1}.  Narrow tiles keep the lanes busy when a batch entry
+// has few columns (per-mode solves of small groups).  K is staged in chunks
+// of 16 through shared memory; the last chunk runs only its valid length.
+// Every output accumulates over k in ascending order with FMAs, whatever
+// the tile, so results do not depend on the launch shape.
 // ---------------------------------------------------------------------------
 constexpr int kKC = 16;
 
-template <int RPT>
+template <int RPT, int NCOL>
 __global__ void __launch_bounds__(512) gemm_tile_kernel(GemmArgs g) {
+  constexpr int RG = 64 / NCOL, CP = NCOL / 2;
   extern __shared__ __align__(16) double gsm[];
   const int nw = blockDim.x >> 5;
-  const int rows_blk = nw * RPT;
+  const int rows_blk = nw * RG * RPT;
   double* As = gsm;                    // [kKC][rows_blk]
-  double* Xs = gsm + kKC * rows_blk;   // [kKC][64]
+  double* Xs = gsm + kKC * rows_blk;   // [kKC][NCOL]
   const int z = blockIdx.z;
   const double* A = g.A + (size_t)z * g.sA;
   const double* X = g.X + (size_t)z * g.sX;
   double* Y = g.Y + (size_t)z * g.sY;
-  const int n0 = blockIdx.x * 64;
+  const int n0 = blockIdx.x * NCOL;
   const int row0 = blockIdx.y * rows_blk;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int rg = lane / CP, cp = lane - rg * CP;
+  const int rw = (warp * RG + rg) * RPT;  // first row of this thread within the block
   double acc[RPT][2];
 #pragma unroll
   for (int i = 0; i < RPT; ++i) { acc[i][0] = 0.0; acc[i][1] = 0.0; }
+  const int nthr = blockDim.x;
   for (int k0 = 0; k0 < g.K; k0 += kKC) {
     const int kc = min(kKC, g.K - k0);
-    for (int kk = 0; kk < kc; ++kk) {
-      const double* Ak = A + (size_t)(k0 + kk) * g.lda;
-      for (int rr = threadIdx.x; rr < rows_blk; rr += blockDim.x) {
-        const int row = row0 + rr;
-        As[kk * rows_blk + rr] = (row < g.rows) ? Ak[row] : 0.0;
+    // stage the A and X panels of this chunk: each thread issues up to four
+    // loads before its first shared store, so the memory latency is paid
+    // once per chunk even when few threads share the panel
+    const int na = kc * rows_blk, nx = kc * NCOL;
+    for (int b0 = 0; b0 < na + nx; b0 += 4 * nthr) {
+      double v[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int idx = b0 + u * nthr + (int)threadIdx.x;
+        v[u] = 0.0;
+        if (idx < na) {
+          const int kk = idx / rows_blk, rr = idx - kk * rows_blk, row = row0 + rr;
+          if (row < g.rows) v[u] = A[(size_t)(k0 + kk) * g.lda + row];
+        } else if (idx < na + nx) {
+          const int j = idx - na, kk = j / NCOL, c = j - kk * NCOL, n = n0 + c;
+          if (n < g.N) v[u] = X[(size_t)(k0 + kk) * g.ldx + n];
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int idx = b0 + u * nthr + (int)threadIdx.x;
+        if (idx < na) As[idx] = v[u];
+        else if (idx < na + nx) Xs[idx - na] = v[u];
       }
     }
-    for (int idx = threadIdx.x; idx < kc * 64; idx += blockDim.x) {
-      const int kk = idx >> 6, c = idx & 63;
-      const int n = n0 + c;
-      Xs[kk * 64 + c] = (n < g.N) ? X[(size_t)(k0 + kk) * g.ldx + n] : 0.0;
-    }
     __syncthreads();
-    const double* Aw = As + warp * RPT;
+    const double* Aw = As + rw;
     if (kc == kKC) {
 #pragma unroll
       for (int kk = 0; kk < kKC; ++kk) {
-        const double2 xv = *reinterpret_cast<const double2*>(&Xs[kk * 64 + 2 * lane]);
+        const double2 xv = *reinterpret_cast<const double2*>(&Xs[kk * NCOL + 2 * cp]);
 #pragma unroll
         for (int i = 0; i < RPT; ++i) {
           const double av = Aw[kk * rows_blk + i];
@@ -564,7 +587,7 @@ __global__ void __launch_bounds__(512) gemm_tile_kernel(GemmArgs g) {
       }
     } else {
       for (int kk = 0; kk < kc; ++kk) {
-        const double2 xv = *reinterpret_cast<const double2*>(&Xs[kk * 64 + 2 * lane]);
+        const double2 xv = *reinterpret_cast<const double2*>(&Xs[kk * NCOL + 2 * cp]);
 #pragma unroll
         for (int i = 0; i < RPT; ++i) {
           const double av = Aw[kk * rows_blk + i];
@@ -575,10 +598,10 @@ __global__ void __launch_bounds__(512) gemm_tile_kernel(GemmArgs g) {
     }
     __syncthreads();
   }
-  const int n = n0 + 2 * lane;
+  const int n = n0 + 2 * cp;
 #pragma unroll
   for (int i = 0; i < RPT; ++i) {
-    const int row = row0 + warp * RPT + i;
+    const int row = row0 + rw + i;
     if (row < g.rows) {
       double* yp = &Y[(size_t)row * g.ldy + n];
       if (n + 1 < g.N && (reinterpret_cast<uintptr_t>(yp) & 15) == 0) {
@@ -596,15 +619,27 @@ __global__ void __launch_bounds__(512) gemm_tile_kernel(GemmArgs g) {
 
 // Small-N form (N <= 8 columns per batch entry): one thread per output row.
 template <int NC>
-__global__ void __launch_bounds__(128) gemv_kernel(GemmArgs g) {
+__global__ void __launch_bounds__(32) gemv_kernel(GemmArgs g) {
   extern __shared__ double xs[];  // K x NC
   const int z = blockIdx.y;
   const double* A = g.A + (size_t)z * g.sA;
   const double* X = g.X + (size_t)z * g.sX;
   double* Y = g.Y + (size_t)z * g.sY;
-  for (int idx = threadIdx.x; idx < g.K * NC; idx += blockDim.x) {
-    const int k = idx / NC, c = idx - k * NC;
-    xs[idx] = (c < g.N) ? X[(size_t)k * g.ldx + c] : 0.0;
+  // the block's X panel, eight loads in flight per thread
+  const int nthr = blockDim.x, nx = g.K * NC;
+  for (int b0 = 0; b0 < nx; b0 += 8 * nthr) {
+    double v[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int idx = b0 + u * nthr + (int)threadIdx.x;
+      const int k = idx / NC, c = idx - k * NC;
+      v[u] = (idx < nx && c < g.N) ? X[(size_t)k * g.ldx + c] : 0.0;
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int idx = b0 + u * nthr + (int)threadIdx.x;
+      if (idx < nx) xs[idx] = v[u];
+    }
   }
   __syncthreads();
   const int row = blockIdx.x * blockDim.x + threadIdx.x;
@@ -612,7 +647,18 @@ __global__ void __launch_bounds__(128) gemv_kernel(GemmArgs g) {
   double acc[NC];
 #pragma unroll
   for (int c = 0; c < NC; ++c) acc[c] = 0.0;
-  for (int k = 0; k < g.K; ++k) {
+  // A loads issued eight at a time ahead of their FMAs (k order kept)
+  int k = 0;
+  for (; k + 8 <= g.K; k += 8) {
+    double av[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) av[u] = A[(size_t)(k + u) * g.lda + row];
+#pragma unroll
+    for (int u = 0; u < 8; ++u)
+#pragma unroll
+      for (int c = 0; c < NC; ++c) acc[c] = fma(av[u], xs[(k + u) * NC + c], acc[c]);
+  }
+  for (; k < g.K; ++k) {
     const double av = A[(size_t)k * g.lda + row];
 #pragma unroll
     for (int c = 0; c < NC; ++c) acc[c] = fma(av, xs[k * NC + c], acc[c]);
@@ -622,69 +668,119 @@ __global__ void __launch_bounds__(128) gemv_kernel(GemmArgs g) {
     if (c < g.N) Y[(size_t)row * g.ldy + c] = g.alpha * acc[c];
 }
 
-template <int RPT>
+template <int RPT, int NCOL>
 static cudaError_t launch_tile(const GemmArgs& g, int nw, int row_blocks, cudaStream_t s) {
-  dim3 grid((g.N + 63) / 64, row_blocks, g.batch);
-  const size_t smem = (size_t)kKC * (nw * RPT + 64) * sizeof(double);
-  gemm_tile_kernel<RPT><<<grid, 32 * nw, smem, s>>>(g);
+  dim3 grid((g.N + NCOL - 1) / NCOL, row_blocks, g.batch);
+  const size_t smem = (size_t)kKC * (nw * (64 / NCOL) * RPT + NCOL) * sizeof(double);
+  gemm_tile_kernel<RPT, NCOL><<<grid, 32 * nw, smem, s>>>(g);
   return cudaGetLastError();
 }
 
-// Smallest nw*rpt >= rows with 2 <= nw <= 16 warps and rpt <= 16.
-static void pick_tile(int rows, int* nw_out, int* rpt_out) {
-  int best = 1 << 30, bnw = 8, brpt = 16;
-  for (int rpt = 1; rpt <= 16; ++rpt)
-    for (int nw = 2; nw <= 16; ++nw) {
-      const int cover = nw * rpt;
-      if (cover < rows) continue;
-      // prefer little padding, then 4..12 warps
-      const int score = (cover - rows) * 64 + ((nw < 4 || nw > 12) ? 8 : 0) + nw;
-      if (score < best) { best = score; bnw = nw; brpt = rpt; }
+// Launch shape from a cost model of the FP64 pipe: a block's work is
+// rows_blk x NCOL per k; blocks spread evenly over the SMs, so an SM runs
+// ceil(blocks / nsm) of them; an SM with fewer than 4 resident warps leaves
+// FP64 units of its sub-partitions idle.  The cheapest (NCOL, row blocks
+// rb, warps nw, rows per thread rpt) wins, ties going to deeper register
+// tiles; extra row blocks (each re-stages the X panel) and single-row
+// threads carry a small penalty.
+struct TileShape { int ncol, rb, nw, rpt; };
+static TileShape pick_shape(const GemmArgs& g, int nsm) {
+  TileShape best{64, 1, 8, 1};
+  double bcost = 1e300;
+  int brpt = 0;
+  for (int ncol = 16; ncol <= 64; ncol *= 2) {
+    const int rg = 64 / ncol, maxr = (ncol == 64) ? 16 : 8;
+    const long cb = (long)((g.N + ncol - 1) / ncol) * g.batch;
+    for (int rb = 1; rb <= 16; ++rb)
+      for (int nw = 2; nw <= 16; ++nw)
+        for (int rpt = 1; rpt <= maxr; ++rpt) {
+          const int rows_blk = nw * rg * rpt;
+          if ((long)rb * rows_blk < g.rows) continue;
+          if ((long)(rb - 1) * rows_blk >= g.rows) continue;   // no empty row block
+          if (rows_blk > 256) continue;                         // shared memory <= 40 KB
+          const long blocks = cb * rb;
+          const long waves = (blocks + nsm - 1) / nsm;
+          const long occ = std::max(1, std::min(48 / nw, 5));
+          const double wps = (double)nw * (double)std::min(waves, occ);
+          const double eff = std::min(1.0, wps / 4.0);
+          const double cost = (double)waves * rows_blk * ncol / eff * (1.0 + 0.02 * (rb - 1)) *
+                              (rpt == 1 ? 1.1 : 1.0);
+          if (cost < bcost * (1.0 - 1e-12) || (cost <= bcost * (1.0 + 1e-12) && rpt > brpt)) {
+            bcost = cost; brpt = rpt; best = {ncol, rb, nw, rpt};
+          }
+        }
+  }
+  return best;
+}
+
+template <int NCOL>
+static cudaError_t launch_ncol(const GemmArgs& g, const TileShape& t, cudaStream_t s) {
+  switch (t.rpt) {
+    case 1: return launch_tile<1, NCOL>(g, t.nw, t.rb, s);
+    case 2: return launch_tile<2, NCOL>(g, t.nw, t.rb, s);
+    case 3: return launch_tile<3, NCOL>(g, t.nw, t.rb, s);
+    case 4: return launch_tile<4, NCOL>(g, t.nw, t.rb, s);
+    case 5: return launch_tile<5, NCOL>(g, t.nw, t.rb, s);
+    case 6: return launch_tile<6, NCOL>(g, t.nw, t.rb, s);
+    case 7: return launch_tile<7, NCOL>(g, t.nw, t.rb, s);
+    case 8: return launch_tile<8, NCOL>(g, t.nw, t.rb, s);
+    default: break;
+  }
+  if constexpr (NCOL == 64) {
+    switch (t.rpt) {
+      case 9: return launch_tile<9, 64>(g, t.nw, t.rb, s);
+      case 10: return launch_tile<10, 64>(g, t.nw, t.rb, s);
+      case 11: return launch_tile<11, 64>(g, t.nw, t.rb, s);
+      case 12: return launch_tile<12, 64>(g, t.nw, t.rb, s);
+      case 13: return launch_tile<13, 64>(g, t.nw, t.rb, s);
+      case 14: return launch_tile<14, 64>(g, t.nw, t.rb, s);
+      case 15: return launch_tile<15, 64>(g, t.nw, t.rb, s);
+      default: return launch_tile<16, 64>(g, t.nw, t.rb, s);
     }
-  *nw_out = bnw;
-  *rpt_out = brpt;
+  }
+  return cudaErrorInvalidValue;
 }
 
 cudaError_t launch_gemm(const GemmArgs& g, cudaStream_t s) {
   if (g.rows <= 0 || g.N <= 0 || g.batch <= 0) return cudaSuccess;
   if (g.N <= 8) {
-    dim3 grid((g.rows + 127) / 128, g.batch);
+    // one warp of rows per block, so small problems spread over the SMs
+    dim3 grid((g.rows + 31) / 32, g.batch);
     const size_t sm = (size_t)g.K * 8 * sizeof(double);
-    if (g.N <= 2) gemv_kernel<2><<<grid, 128, (size_t)g.K * 2 * sizeof(double), s>>>(g);
-    else if (g.N <= 4) gemv_kernel<4><<<grid, 128, (size_t)g.K * 4 * sizeof(double), s>>>(g);
-    else gemv_kernel<8><<<grid, 128, sm, s>>>(g);
+    if (g.N <= 2) gemv_kernel<2><<<grid, 32, (size_t)g.K * 2 * sizeof(double), s>>>(g);
+    else if (g.N <= 4) gemv_kernel<4><<<grid, 32, (size_t)g.K * 4 * sizeof(double), s>>>(g);
+    else gemv_kernel<8><<<grid, 32, sm, s>>>(g);
     return cudaGetLastError();
   }
-  // One block row tile covers all rows when the column blocks alone fill
-  // the GPU; otherwise the rows are split into up to 16 tiles.
-  int dev = 0, nsm = 152;
+  static int nsm_dev[64] = {0};
+  int dev = 0;
   cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  const long col_blocks = (long)((g.N + 63) / 64) * g.batch;
-  int rb = 1;
-  while (rb < 16 && col_blocks * rb < 2L * nsm && (g.rows + rb) / (rb + 1) >= 4) ++rb;
-  const int rows_per = (g.rows + rb - 1) / rb;
-  int nw, rpt;
-  pick_tile(rows_per, &nw, &rpt);
-  rb = (g.rows + nw * rpt - 1) / (nw * rpt);
-  switch (rpt) {
-    case 1: return launch_tile<1>(g, nw, rb, s);
-    case 2: return launch_tile<2>(g, nw, rb, s);
-    case 3: return launch_tile<3>(g, nw, rb, s);
-    case 4: return launch_tile<4>(g, nw, rb, s);
-    case 5: return launch_tile<5>(g, nw, rb, s);
-    case 6: return launch_tile<6>(g, nw, rb, s);
-    case 7: return launch_tile<7>(g, nw, rb, s);
-    case 8: return launch_tile<8>(g, nw, rb, s);
-    case 9: return launch_tile<9>(g, nw, rb, s);
-    case 10: return launch_tile<10>(g, nw, rb, s);
-    case 11: return launch_tile<11>(g, nw, rb, s);
-    case 12: return launch_tile<12>(g, nw, rb, s);
-    case 13: return launch_tile<13>(g, nw, rb, s);
-    case 14: return launch_tile<14>(g, nw, rb, s);
-    case 15: return launch_tile<15>(g, nw, rb, s);
-    default: return launch_tile<16>(g, nw, rb, s);
+  int nsm = (dev >= 0 && dev < 64) ? nsm_dev[dev] : 0;
+  if (nsm == 0) {
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    if (nsm <= 0) nsm = 152;
+    if (dev >= 0 && dev < 64) nsm_dev[dev] = nsm;
   }
+  // shapes are memoised per (rows, N, batch, SM count): the search runs on
+  // the host once per problem size
+  struct Memo { int rows, N, batch, nsm; TileShape t; };
+  thread_local std::unordered_map<unsigned long long, Memo> memo;
+  // (a hash; the entry is checked against the full sizes)
+  const unsigned long long key = (unsigned long long)(g.rows & 0xfff) | ((unsigned long long)(g.N & 0xffffff) << 12) |
+                                 ((unsigned long long)(g.batch & 0xffff) << 36) |
+                                 ((unsigned long long)(nsm & 0xfff) << 52);
+  auto it = memo.find(key);
+  TileShape t;
+  if (it != memo.end() && it->second.rows == g.rows && it->second.N == g.N && it->second.batch == g.batch &&
+      it->second.nsm == nsm) {
+    t = it->second.t;
+  } else {
+    t = pick_shape(g, nsm);
+    memo[key] = Memo{g.rows, g.N, g.batch, nsm, t};
+  }
+  if (t.ncol == 16) return launch_ncol<16>(g, t, s);
+  if (t.ncol == 32) return launch_ncol<32>(g, t, s);
+  return launch_ncol<64>(g, t, s);
 }
 
 // ---------------------------------------------------------------------------
