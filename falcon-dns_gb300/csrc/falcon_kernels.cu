@@ -524,14 +524,24 @@ cudaError_t launch_nonlin(const NonlinArgs& a, cudaStream_t s) {
 // ---------------------------------------------------------------------------
 constexpr int kKC = 16;
 
+// Asynchronous 8-byte global -> shared copy (cp.async); a masked element is
+// written as zero without reading global memory.
+__device__ __forceinline__ void cp_async8(double* dst, const double* src, bool valid) {
+  const unsigned saddr = (unsigned)__cvta_generic_to_shared(dst);
+  const int sz = valid ? 8 : 0;
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(saddr), "l"(src), "r"(sz) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
 template <int RPT, int NCOL>
 __global__ void __launch_bounds__(512) gemm_tile_kernel(GemmArgs g) {
   constexpr int RG = 64 / NCOL, CP = NCOL / 2;
   extern __shared__ __align__(16) double gsm[];
   const int nw = blockDim.x >> 5;
   const int rows_blk = nw * RG * RPT;
-  double* As = gsm;                    // [kKC][rows_blk]
-  double* Xs = gsm + kKC * rows_blk;   // [kKC][NCOL]
+  const int stage = kKC * (rows_blk + NCOL);   // one buffer: A [kKC][rows_blk], X [kKC][NCOL]
   const int z = blockIdx.z;
   const double* A = g.A + (size_t)z * g.sA;
   const double* X = g.X + (size_t)z * g.sX;
@@ -545,34 +555,39 @@ __global__ void __launch_bounds__(512) gemm_tile_kernel(GemmArgs g) {
 #pragma unroll
   for (int i = 0; i < RPT; ++i) { acc[i][0] = 0.0; acc[i][1] = 0.0; }
   const int nthr = blockDim.x;
-  for (int k0 = 0; k0 < g.K; k0 += kKC) {
+  // Double-buffered K chunks: the copies of chunk c+1 are in flight while
+  // chunk c is multiplied, so the memory latency is hidden even when a
+  // small grid leaves no other blocks to switch to.
+  auto issue = [&](int k0, double* buf) {
     const int kc = min(kKC, g.K - k0);
-    // stage the A and X panels of this chunk: each thread issues up to four
-    // loads before its first shared store, so the memory latency is paid
-    // once per chunk even when few threads share the panel
     const int na = kc * rows_blk, nx = kc * NCOL;
-    for (int b0 = 0; b0 < na + nx; b0 += 4 * nthr) {
-      double v[4];
-#pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        const int idx = b0 + u * nthr + (int)threadIdx.x;
-        v[u] = 0.0;
-        if (idx < na) {
-          const int kk = idx / rows_blk, rr = idx - kk * rows_blk, row = row0 + rr;
-          if (row < g.rows) v[u] = A[(size_t)(k0 + kk) * g.lda + row];
-        } else if (idx < na + nx) {
-          const int j = idx - na, kk = j / NCOL, c = j - kk * NCOL, n = n0 + c;
-          if (n < g.N) v[u] = X[(size_t)(k0 + kk) * g.ldx + n];
-        }
-      }
-#pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        const int idx = b0 + u * nthr + (int)threadIdx.x;
-        if (idx < na) As[idx] = v[u];
-        else if (idx < na + nx) Xs[idx - na] = v[u];
+    for (int idx = threadIdx.x; idx < na + nx; idx += nthr) {
+      if (idx < na) {
+        const int kk = idx / rows_blk, rr = idx - kk * rows_blk, row = row0 + rr;
+        const bool ok = row < g.rows;
+        cp_async8(buf + idx, ok ? A + (size_t)(k0 + kk) * g.lda + row : A, ok);
+      } else {
+        const int j = idx - na, kk = j / NCOL, c = j - kk * NCOL, n = n0 + c;
+        const bool ok = n < g.N;
+        cp_async8(buf + kKC * rows_blk + j, ok ? X + (size_t)(k0 + kk) * g.ldx + n : X, ok);
       }
     }
+    cp_async_commit();
+  };
+  issue(0, gsm);
+  int cur = 0;
+  for (int k0 = 0; k0 < g.K; k0 += kKC) {
+    const int kc = min(kKC, g.K - k0);
+    const bool more = k0 + kKC < g.K;
+    if (more) {
+      issue(k0 + kKC, gsm + (cur ^ 1) * stage);
+      cp_async_wait<1>();
+    } else {
+      cp_async_wait<0>();
+    }
     __syncthreads();
+    const double* As = gsm + cur * stage;
+    const double* Xs = As + kKC * rows_blk;
     const double* Aw = As + rw;
     if (kc == kKC) {
 #pragma unroll
@@ -596,7 +611,8 @@ __global__ void __launch_bounds__(512) gemm_tile_kernel(GemmArgs g) {
         }
       }
     }
-    __syncthreads();
+    __syncthreads();  // every thread is done with this buffer before it is refilled
+    cur ^= 1;
   }
   const int n = n0 + 2 * cp;
 #pragma unroll
@@ -670,8 +686,18 @@ __global__ void __launch_bounds__(32) gemv_kernel(GemmArgs g) {
 
 template <int RPT, int NCOL>
 static cudaError_t launch_tile(const GemmArgs& g, int nw, int row_blocks, cudaStream_t s) {
+  // two K-chunk buffers; above 48 KB the kernel is opted in once per device
+  static bool opted[64] = {false};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev >= 0 && dev < 64 && !opted[dev]) {
+    const cudaError_t e = cudaFuncSetAttribute(gemm_tile_kernel<RPT, NCOL>,
+                                               cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024);
+    if (e != cudaSuccess) return e;
+    opted[dev] = true;
+  }
   dim3 grid((g.N + NCOL - 1) / NCOL, row_blocks, g.batch);
-  const size_t smem = (size_t)kKC * (nw * (64 / NCOL) * RPT + NCOL) * sizeof(double);
+  const size_t smem = (size_t)2 * kKC * (nw * (64 / NCOL) * RPT + NCOL) * sizeof(double);
   gemm_tile_kernel<RPT, NCOL><<<grid, 32 * nw, smem, s>>>(g);
   return cudaGetLastError();
 }
@@ -697,7 +723,7 @@ static TileShape pick_shape(const GemmArgs& g, int nsm) {
           const int rows_blk = nw * rg * rpt;
           if ((long)rb * rows_blk < g.rows) continue;
           if ((long)(rb - 1) * rows_blk >= g.rows) continue;   // no empty row block
-          if (rows_blk > 256) continue;                         // shared memory <= 40 KB
+          if (rows_blk > 256) continue;                         // two K buffers <= 80 KB
           const long blocks = cb * rb;
           const long waves = (blocks + nsm - 1) / nsm;
           const long occ = std::max(1, std::min(48 / nw, 5));
