@@ -209,13 +209,47 @@ struct OpSet {
   // (src/init.F90:252, used by src/rhs_create_rk.F90:158-161).
   double* D1c = nullptr;
   double* Lc = nullptr;
+  // Exact bf16 slices of each operator for the tensor-core GEMM (one entry
+  // per operator array: its FP64 base, shape and slice arrays).
+  struct Oz {
+    const double* base = nullptr;
+    long lda = 0, sA = 0;
+    int rows = 0, K = 0, nb = 0, rowsP = 0, KP = 0;
+    uint16_t* s = nullptr;
+    int* ex = nullptr;
+  };
+  std::vector<Oz> oz;
   size_t bytes = 0;
   ~OpSet() {
     cudaFree(D1p); cudaFree(Lp); cudaFree(ST); cudaFree(G); cudaFree(U); cudaFree(LAP);
     cudaFree(inv_r); cudaFree(inv_r2); cudaFree(wq); cudaFree(d1_0); cudaFree(d1_R);
     cudaFree(D1c); cudaFree(Lc);
+    for (auto& o : oz) { cudaFree(o.s); cudaFree(o.ex); }
   }
 };
+
+// Contractions through the tensor-core slices (1, default) or the FP64 FMA
+// tiles (0); both are FP64-accurate, the first is several times faster.
+std::atomic<int> g_gemm_mode{1};
+
+// Slices of one column-major operator array (rows x K, lda = rows, nb
+// entries of stride sA) for the tensor-core GEMM.
+int add_oz(OpSet* ops, const double* base, int rows, int K, int nb, long sA) {
+  if (!base || K > 257) return 0;
+  OpSet::Oz o;
+  o.base = base; o.lda = rows; o.sA = sA; o.rows = rows; o.K = K; o.nb = nb;
+  o.rowsP = oz_rows_padded(rows);
+  o.KP = ((K + 15) / 16) * 16;
+  const size_t ns = (size_t)nb * kOzS * o.rowsP * o.KP, ne = (size_t)nb * o.rowsP;
+  CK(cudaMalloc(&o.s, ns * sizeof(uint16_t)));
+  CK(cudaMalloc(&o.ex, ne * sizeof(int)));
+  CK(cudaMemset(o.s, 0, ns * sizeof(uint16_t)));
+  CK(cudaMemset(o.ex, 0, ne * sizeof(int)));
+  CK(launch_oz_slice_rows(base, rows, sA, rows, K, nb, o.s, o.ex, o.rowsP, o.KP, 0));
+  ops->bytes += ns * sizeof(uint16_t) + ne * sizeof(int);
+  ops->oz.push_back(o);
+  return 0;
+}
 
 std::mutex g_ops_mu;
 std::map<OpKey, std::weak_ptr<OpSet>> g_ops;
@@ -567,6 +601,16 @@ int build_opset(const OpKey& k, std::shared_ptr<OpSet>* out) {
     if ((rc = upload(&ops->d1_R, d1R, &ops->bytes))) return rc;
   }
   {
+    const long RR = (long)R * R;
+    if ((rc = add_oz(ops.get(), ops->D1p, R, R, 1, RR)) || (rc = add_oz(ops.get(), ops->Lp, R, R, 1, RR)) ||
+        (rc = add_oz(ops.get(), ops->ST, R, R, M, RR)) || (rc = add_oz(ops.get(), ops->G, 3 * R, R, M, 3 * RR)) ||
+        (rc = add_oz(ops.get(), ops->U, 2 * R, R, 1, 2 * RR)) ||
+        (rc = add_oz(ops.get(), ops->LAP, 2 * R + 2, R, M, (long)(2 * R + 2) * R)) ||
+        (rc = add_oz(ops.get(), ops->D1c, R, R, 1, RR)) || (rc = add_oz(ops.get(), ops->Lc, R, R, 1, RR)))
+      return rc;
+    CK(cudaDeviceSynchronize());
+  }
+  {
     std::lock_guard<std::mutex> lk(g_ops_mu);
     g_ops[k] = ops;
   }
@@ -786,6 +830,12 @@ struct Group {
   bool force_rebuild = false;
   bool need_cfl_pass = false;
   bool restart_first = false;  // the next step is the first after a restart (l_restart)
+  // Slice planes of the X operand of the tensor-core contractions, and the
+  // operand they hold (reused while it is unchanged).
+  uint16_t* oz_xs = nullptr;
+  int* oz_cexp = nullptr;
+  size_t oz_xs_cap = 0, oz_cexp_cap = 0;
+  struct { const double* X = nullptr; long ldx = 0, sX = 0; int K = 0, N = 0, batch = 0; bool valid = false; } oz_key;
   double dt_array[4] = {0, 0, 0, 0};
   double dt_new = 0.0;
   double* umax = nullptr;
@@ -798,6 +848,8 @@ struct Group {
   }
   ~Group() {
     drop_graphs();
+    cudaFree(oz_xs);
+    cudaFree(oz_cexp);
     for (void* q : allocs) cudaFree(q);
     if (stage_buf) cudaFreeHost(stage_buf);
     if (done) cudaEventDestroy(done);
@@ -860,6 +912,21 @@ int validate(const falcon_params& p) {
   return 0;
 }
 
+// Scratch for the slice planes of the largest X operand of the group's
+// contractions (allocated when the group is set up, before any capture).
+int oz_scratch_init(Group* g) {
+  const int R = g->R, M = g->M, B = g->B;
+  const long KP = ((R + 15) / 16) * 16;
+  auto np = [](long n) { return ((n + 31) / 32) * 32; };
+  const long cols = std::max(np(2L * M * B), (long)M * np(2L * B));
+  g->oz_xs_cap = (size_t)kOzS * KP * cols;
+  g->oz_cexp_cap = (size_t)cols;
+  CK(cudaMalloc(&g->oz_xs, g->oz_xs_cap * sizeof(uint16_t)));
+  CK(cudaMalloc(&g->oz_cexp, g->oz_cexp_cap * sizeof(int)));
+  g->bytes += g->oz_xs_cap * sizeof(uint16_t) + g->oz_cexp_cap * sizeof(int);
+  return 0;
+}
+
 // Operators of the IMEXRK stages whose implicit diagonal differs from that
 // of stage diag_index (diag_diff, src/fourierloop_imexrk.F90:134-160),
 // built with the weight butcher_aD(rk_stage,rk_stage) at time step dt.
@@ -890,6 +957,7 @@ int group_init(Group* g, const std::vector<falcon_params>& ps, const std::vector
   if ((rc = build_opset(key_of(g->p, g->sch), &g->ops))) return rc;
   if ((rc = build_stage_ops(g, g->p.dt))) return rc;
   if ((rc = make_fft(g->P, &g->fft))) return rc;
+  if ((rc = oz_scratch_init(g))) return rc;
   const size_t n = g->nel();
   const int R = g->R, B = g->B;
   if (g->p.scheme_type == FALCON_IMEX) {
@@ -994,7 +1062,67 @@ int launch(Group* g, int cls, double flops, F f) {
 
 double gemm_flops(const GemmArgs& q) { return 2.0 * q.rows * (double)q.K * q.N * q.batch; }
 
-int gemm(Group* g, int cls, const GemmArgs& q) {
+// The slice view of q.A when it lies in an operator of the group's sets
+// and q walks that operator with its own leading dimension and stride.
+bool attach_oz(const OpSet* o, GemmArgs* q) {
+  if (!o) return false;
+  for (const auto& z : o->oz) {
+    const long span = (z.nb > 1) ? z.nb * z.sA : z.lda * z.K;
+    const long delta = q->A - z.base;
+    if (delta < 0 || delta >= span) continue;
+    const long z0 = (z.nb > 1) ? delta / z.sA : 0;
+    const long row0 = delta - z0 * z.sA;
+    if (q->lda != z.lda || q->K != z.K || row0 >= z.lda || row0 + q->rows > z.rows) return false;
+    if (q->batch > 1 && (q->sA != z.sA || z0 + q->batch > z.nb)) return false;
+    q->oz_s = z.s + (size_t)z0 * kOzS * z.rowsP * z.KP;
+    q->oz_ex = z.ex + (size_t)z0 * z.rowsP;
+    q->oz_sz = (long)kOzS * z.rowsP * z.KP;
+    q->oz_rowsP = z.rowsP;
+    q->oz_KP = z.KP;
+    q->oz_row0 = (int)row0;
+    return true;
+  }
+  return false;
+}
+
+// reuse: the call follows a contraction with the same X operand, unchanged
+// since (the blocks of one operator applied to one right-hand side); its
+// slice planes are reused when they match.
+int gemm(Group* g, int cls, const GemmArgs& q0, bool reuse = false) {
+  GemmArgs q = q0;
+  q.oz_s = nullptr;
+  q.oz_xs = nullptr;
+  // Contractions with at least 16 columns per batch entry take the tensor
+  // cores; narrower ones (the per-mode solves of groups of up to 7
+  // instances) stay on the FP64 FMA path, where the operator's FP64 bytes
+  // (fewer than its slices) bound the time.  Radial contractions cover all
+  // modes and always take the slices.
+  bool ok = false;
+  if (g_gemm_mode.load() && g->oz_xs && q.N >= 16) {
+    ok = attach_oz(g->ops.get(), &q);
+    for (int st = 0; !ok && st < kMaxStages; ++st) ok = attach_oz(g->stage_ops[st].get(), &q);
+  }
+  if (ok) {
+    const int KP = q.oz_KP, Np = (int)(((long)q.N + 31) / 32 * 32);
+    if ((size_t)kOzS * KP * Np * q.batch > g->oz_xs_cap || (size_t)Np * q.batch > g->oz_cexp_cap) {
+      ok = false;  // beyond the scratch sized for this group: FMA tiles
+      q.oz_s = nullptr;
+    } else {
+      auto& k = g->oz_key;
+      const bool same = reuse && k.valid && k.X == q.X && k.ldx == q.ldx && k.sX == q.sX && k.K == q.K &&
+                        k.N == q.N && k.batch == q.batch;
+      if (!same) {
+        int rc = launch(g, KC_ELEMENTWISE, 0.0, [&]() {
+          return launch_oz_slice_cols(q.X, q.ldx, q.sX, q.K, q.N, q.batch, g->oz_xs, g->oz_cexp, KP, Np, g->stream);
+        });
+        if (rc) return rc;
+        k.X = q.X; k.ldx = q.ldx; k.sX = q.sX; k.K = q.K; k.N = q.N; k.batch = q.batch; k.valid = true;
+      }
+      q.oz_xs = g->oz_xs;
+      q.oz_cexp = g->oz_cexp;
+      q.oz_Np = Np;
+    }
+  }
   return launch(g, cls, gemm_flops(q), [&]() { return launch_gemm(q, g->stream); });
 }
 
@@ -1030,8 +1158,8 @@ int solve_all(Group* g, double2* t_out, double2* w_out, double buo_scale, double
   if (M > 1) {
     const long sG = 3L * R * R;
     if ((rc = gemm(g, KC_GEMM_MODE, per_mode(o->G, 3 * R, sG, g->rhs_w, w_out, R, M, B, 1, M - 1, R))) ||
-        (rc = gemm(g, KC_GEMM_MODE, per_mode(o->G + R, 3 * R, sG, g->rhs_w, g->psi, R, M, B, 1, M - 1, R))) ||
-        (rc = gemm(g, KC_GEMM_MODE, per_mode(o->G + 2 * R, 3 * R, sG, g->rhs_w, g->up, R, M, B, 1, M - 1, R))))
+        (rc = gemm(g, KC_GEMM_MODE, per_mode(o->G + R, 3 * R, sG, g->rhs_w, g->psi, R, M, B, 1, M - 1, R), true)) ||
+        (rc = gemm(g, KC_GEMM_MODE, per_mode(o->G + 2 * R, 3 * R, sG, g->rhs_w, g->up, R, M, B, 1, M - 1, R), true)))
       return rc;
   }
   GemmArgs gu{};
@@ -1293,10 +1421,11 @@ int step_imexrk(Group* g) {
       const long sL = (long)rows * R;
       double2* psi_tmp = g->rhs_t;  // the reference leaves psii at its last-stage value
       if ((rc = gemm(g, KC_GEMM_MODE, per_mode(o->LAP, rows, sL, g->rhs_w, psi_tmp, R, M, B, 1, M - 1, R))) ||
-          (rc = gemm(g, KC_GEMM_MODE, per_mode(o->LAP + R, rows, sL, g->rhs_w, g->up, R, M, B, 1, M - 1, R))) ||
-          (rc = gemm(g, KC_GEMM_MODE, per_mode(o->LAP + 2 * R, rows, sL, g->rhs_w, g->w0, R, M, B, 1, M - 1, 1))) ||
+          (rc = gemm(g, KC_GEMM_MODE, per_mode(o->LAP + R, rows, sL, g->rhs_w, g->up, R, M, B, 1, M - 1, R), true)) ||
+          (rc = gemm(g, KC_GEMM_MODE, per_mode(o->LAP + 2 * R, rows, sL, g->rhs_w, g->w0, R, M, B, 1, M - 1, 1),
+                     true)) ||
           (rc = gemm(g, KC_GEMM_MODE, per_mode(o->LAP + 2 * R + 1, rows, sL, g->rhs_w, g->w0 + (size_t)(R - 1) * M * B,
-                                               R, M, B, 1, M - 1, 1))))
+                                               R, M, B, 1, M - 1, 1), true)))
         return rc;
     }
     GemmArgs gd{};
@@ -1353,10 +1482,11 @@ int step_rk(Group* g) {
       const int rows = 2 * R + 2;
       const long sL = (long)rows * R;
       if ((rc = gemm(g, KC_GEMM_MODE, per_mode(o->LAP, rows, sL, g->rhs_w, g->psi, R, M, B, 1, M - 1, R))) ||
-          (rc = gemm(g, KC_GEMM_MODE, per_mode(o->LAP + R, rows, sL, g->rhs_w, g->up, R, M, B, 1, M - 1, R))) ||
-          (rc = gemm(g, KC_GEMM_MODE, per_mode(o->LAP + 2 * R, rows, sL, g->rhs_w, w_out, R, M, B, 1, M - 1, 1))) ||
+          (rc = gemm(g, KC_GEMM_MODE, per_mode(o->LAP + R, rows, sL, g->rhs_w, g->up, R, M, B, 1, M - 1, R), true)) ||
+          (rc = gemm(g, KC_GEMM_MODE, per_mode(o->LAP + 2 * R, rows, sL, g->rhs_w, w_out, R, M, B, 1, M - 1, 1),
+                     w_out != g->rhs_w)) ||
           (rc = gemm(g, KC_GEMM_MODE, per_mode(o->LAP + 2 * R + 1, rows, sL, g->rhs_w, w_out + (size_t)(R - 1) * M * B,
-                                               R, M, B, 1, M - 1, 1))))
+                                               R, M, B, 1, M - 1, 1), w_out != g->rhs_w)))
         return rc;
     }
     GemmArgs gd{};
@@ -3246,6 +3376,7 @@ extern "C" {
 long long falcon_launch_count(void) { return g_launches.load(); }
 
 int falcon_set_step_graphs(int enable) { return g_graphs.exchange(enable ? 1 : 0); }
+int falcon_set_gemm_mode(int mode) { return g_gemm_mode.exchange(mode ? 1 : 0); }
 
 int falcon_batch_profile(falcon_batch* b, int nsteps, falcon_kernel_stat* stats, int max_stats, int* nstats) {
   if (!b || nsteps <= 0 || !stats || !nstats) return fail(FALCON_EINVAL, "invalid profile arguments");

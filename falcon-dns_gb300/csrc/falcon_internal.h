@@ -120,7 +120,42 @@ struct GemmArgs {
   long sA, sX, sY;
   int batch;
   double alpha;
+  // Optional exact-slice copy of A for the tensor-core path (launch_gemm
+  // uses it when set): slices of batch entry z at oz_s + z*oz_sz, row
+  // exponents at oz_ex + z*oz_rowsP, this GEMM's first operator row oz_row0.
+  const uint16_t* oz_s;
+  const int* oz_ex;
+  long oz_sz;
+  int oz_rowsP, oz_KP, oz_row0;
+  // slices of X made by launch_oz_slice_cols: [batch][kOzS][oz_KP][oz_Np]
+  // bf16 and column exponents [batch][oz_Np]
+  const uint16_t* oz_xs;
+  const int* oz_cexp;
+  int oz_Np;
 };
+
+// ---- FP64 GEMM on bf16 tensor cores by exact slicing (falcon_ozaki.cu) ----
+// An FP64 operand row (or column) with |a| < 2^e is cut into kOzS signed
+// integers of kOzW bits, a = 2^e sum_s q_s 2^(-kOzW (s+1)) up to 2^(e-60).
+// Slice products are exact in bf16 x bf16 -> FP32 and their sums stay
+// below 2^24 (exact) for K <= 257; the pairs s + t <= kOzD are summed per
+// s + t and recombined in 64-bit integers and one FP64 FMA.
+constexpr int kOzS = 10, kOzW = 6, kOzD = 9;
+// Slices of a column-major FP64 operator (rows x K, lda, nb entries of
+// stride sA) into S [nb][kOzS][rowsP][KP] (bf16 bits, zero padded) and row
+// exponents ex [nb][rowsP].
+cudaError_t launch_oz_slice_rows(const double* A, long lda, long sA, int rows, int K, int nb, uint16_t* S, int* ex,
+                                 int rowsP, int KP, cudaStream_t s);
+// Slices of the columns of X (K x N, row stride ldx, batch stride sX) into
+// Xs [batch][kOzS][KP][Np] (zero for k >= K, n >= N) and column exponents
+// cexp [batch][Np].  Np is a multiple of 32.
+cudaError_t launch_oz_slice_cols(const double* X, long ldx, long sX, int K, int N, int batch, uint16_t* Xs,
+                                 int* cexp, int KP, int Np, cudaStream_t s);
+// Y = alpha A X from the slices of A (oz_s, oz_ex) and of X (oz_xs, oz_cexp).
+cudaError_t launch_oz_gemm(const GemmArgs& g, cudaStream_t s);
+// Row padding of operator slices: rows_total rounded up to 16, plus 64
+// (the row blocks of the tensor-core kernel cover up to 64 rows).
+inline int oz_rows_padded(int rows) { return ((rows + 15) / 16) * 16 + 64; }
 
 // Elementwise arguments shared by the right-hand-side kernels.
 struct RhsArgs {

@@ -263,6 +263,92 @@ __device__ __forceinline__ void run_stage1(int p, bool dif, bool twid, double2* 
   generic_stage(A, nullptr, P, p, m, stride, tw, lane, nl, dif, twid);
 }
 
+// Odd prime p >= 17 of a prime-factor plan (no twiddles) on both buffers
+// of a block at once, the output pairs of each butterfly shared by G lanes:
+// with one thread per butterfly the stage would run a few dozen long
+// butterflies on a few warps.  Work items are ordered lane group first, so
+// a warp's lanes share their lane group (uniform coefficient loads).  Each
+// output is formed with exactly the operations of dft_odd_store, so the
+// results are bit for bit those of the one-thread form.  In place: every
+// item loads its inputs before any item of the round stores.
+template <int p, int G>
+__device__ void fft_stage_split(double2* A, double2* Bf, int P, int m, int tid, int nt) {
+  constexpr int h = (p - 1) / 2;
+  const int nb = P / p, mp = m * p, items = 2 * nb * G;
+  const int rounds = (items + nt - 1) / nt;
+  const float inv_m = 1.0f / (float)m;
+  for (int rd = 0; rd < rounds; ++rd) {
+    const int it = rd * nt + tid;
+    const bool act = it < items;
+    int jg = 0, base = 0;
+    double2* buf = A;
+    double2 v[p];
+    if (act) {
+      jg = it / (2 * nb);
+      const int rem = it - jg * 2 * nb;
+      const int bsel = rem >= nb;
+      const int t = rem - bsel * nb;
+      buf = bsel ? Bf : A;
+      const int g = (int)(((float)t + 0.5f) * inv_m);
+      base = g * mp + (t - g * m);
+#pragma unroll
+      for (int q = 0; q < p; ++q) v[q] = buf[base + q * m];
+    }
+    __syncthreads();
+    if (act) {
+      double2 a[h], b[h];
+#pragma unroll
+      for (int q = 1; q <= h; ++q) { a[q - 1] = cadd(v[q], v[p - q]); b[q - 1] = csub(v[q], v[p - q]); }
+      const double2 v0 = v[0];
+      if (jg == 0) {
+        double2 y0 = v0;
+#pragma unroll
+        for (int q = 0; q < h; ++q) y0 = cadd(y0, a[q]);
+        buf[base] = y0;
+      }
+      for (int j = 1 + jg; j <= h; j += G) {
+        double2 Av = v0;
+        double2 Bv = make_double2(0.0, 0.0);
+#pragma unroll
+        for (int q = 1; q <= h; ++q) {
+          const int idx = (j * q) % p;
+          const double c = DftTab<p>::c(idx), sn = DftTab<p>::s(idx);
+          Av.x = fma(a[q - 1].x, c, Av.x); Av.y = fma(a[q - 1].y, c, Av.y);
+          Bv.x = fma(b[q - 1].x, sn, Bv.x); Bv.y = fma(b[q - 1].y, sn, Bv.y);
+        }
+        buf[base + j * m] = make_double2(Av.x + Bv.y, Av.y - Bv.x);
+        buf[base + (p - j) * m] = make_double2(Av.x - Bv.y, Av.y + Bv.x);
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// One stage of the block-per-line form: large odd primes of a prime-factor
+// plan through fft_stage_split over the whole block, the rest per buffer
+// half (run_stage1).  Called by every thread of the block.
+template <int MAXP>
+__device__ __forceinline__ void run_stage_block(int p, bool dif, bool twid, double2* A, double2* Bf, double2* mine,
+                                                int P, int m, int stride, const double2* tw, int tid, int nt, int hl,
+                                                int nl) {
+  if (!twid) {
+    switch (p) {
+#define FALCON_SPLIT(q, g)                                  \
+  case q:                                                   \
+    if constexpr (q <= MAXP) {                              \
+      fft_stage_split<q, g>(A, Bf, P, m, tid, nt);          \
+      return;                                               \
+    }                                                       \
+    break;
+      FALCON_SPLIT(17, 2) FALCON_SPLIT(19, 2) FALCON_SPLIT(23, 3) FALCON_SPLIT(29, 3) FALCON_SPLIT(31, 3)
+#undef FALCON_SPLIT
+      default: break;
+    }
+  }
+  run_stage1<MAXP>(p, dif, twid, mine, P, m, stride, tw, hl, nl);
+  __syncthreads();
+}
+
 // ---------------------------------------------------------------------------
 // Nonlinear pass (Nr_maxLOOP, src/nonlin.F90:55-86): one warp per radial
 // line (r, b).  invfft of T, omega, u_phi, u_r (two complex inverse FFTs of
@@ -411,9 +497,8 @@ __global__ void __launch_bounds__(64 * S) nonlin_line_kernel(NonlinArgs a) {
     int m = 1;
     for (int s = a.plan.nrad - 1; s >= 0; --s) {
       const int p = a.plan.rad[s];
-      run_stage1<MAXP>(p, false, !a.plan.pfa, mine, P, m, P / (m * p), tw, hl, nl);
+      run_stage_block<MAXP>(p, false, !a.plan.pfa, bufA, bufB, mine, P, m, P / (m * p), tw, tid, nt, hl, nl);
       m *= p;
-      __syncthreads();
     }
   }
   double urmax = 0.0, upmax = 0.0;
@@ -431,8 +516,7 @@ __global__ void __launch_bounds__(64 * S) nonlin_line_kernel(NonlinArgs a) {
     for (int s = 0; s < a.plan.nrad; ++s) {
       const int p = a.plan.rad[s];
       m /= p;
-      run_stage1<MAXP>(p, true, !a.plan.pfa, mine, P, m, P / (m * p), tw, hl, nl);
-      __syncthreads();
+      run_stage_block<MAXP>(p, true, !a.plan.pfa, bufA, bufB, mine, P, m, P / (m * p), tw, tid, nt, hl, nl);
     }
   }
   const double sc = 0.5 / (double)P;
@@ -769,6 +853,7 @@ static cudaError_t launch_ncol(const GemmArgs& g, const TileShape& t, cudaStream
 
 cudaError_t launch_gemm(const GemmArgs& g, cudaStream_t s) {
   if (g.rows <= 0 || g.N <= 0 || g.batch <= 0) return cudaSuccess;
+  if (g.oz_s) return launch_oz_gemm(g, s);
   if (g.N <= 8) {
     // one warp of rows per block, so small problems spread over the SMs
     dim3 grid((g.rows + 31) / 32, g.batch);

@@ -1,0 +1,311 @@
+// FP64 GEMM Y = alpha * A * X on the bf16 tensor cores (mma.sync m16n8k16,
+// FP32 accumulation) by exact integer slicing (the Ozaki scheme).
+//
+// On GB300 the FP64 pipe (~1.2 TFLOP/s) is ~500x slower than bf16 MMA
+// (~600 TFLOP/s measured for mma.sync), and DMMA shares the FP64 rate.  So
+// the operator contractions of the time step run as integer products:
+//   - A row i with |a| < 2^e_i and an X column n with |x| < 2^f_n are cut
+//     into kOzS = 10 signed 6-bit integers (|q| <= 63, exact in bf16):
+//       a = 2^e_i sum_s alpha_s 2^(-6(s+1)),  x = 2^f_n sum_t beta_t 2^(-6(t+1)),
+//     dropping bits below 2^(e-60);
+//   - P_st = sum_k alpha_s beta_t is exact in FP32: |alpha beta| < 2^12, K <=
+//     257 and at most 10 pairs per s + t keep every partial sum below 2^24;
+//   - Q_d = sum_{s+t=d} P_st for d <= 9 accumulates in one FP32 register set
+//     per d (still exact), the pairs s + t > 9 are dropped (< K 2^(e+f-56));
+//   - Y = 2^(e_i + f_n - 36) (H + 2^-30 L), H = sum_{d<=4} Q_d 64^(4-d) and
+//     L = sum_{d>=5} Q_d 64^(9-d) formed exactly in 64-bit integers, one
+//     FP64 FMA and an exact power-of-two scale.
+// The error is of the order of K 2^-56 max_k|A_ik| max_k|X_kn|, the level of
+// an FP64 GEMM's rounding; each output depends only on its own row and
+// column, and every FP32 sum is exact, so results do not depend on the
+// launch shape or on the other columns of the batch.
+//
+// The operators are constant: their slices are made once (launch_oz_slice_rows)
+// when an operator set is built.  X is sliced per contraction into slice
+// planes (launch_oz_slice_cols); contractions sharing one X reuse them.
+#include <cuda_bf16.h>
+#include <stdint.h>
+
+#include "falcon_internal.h"
+
+namespace falcon {
+
+namespace {
+
+__device__ __forceinline__ int biased_exp(double a) {
+  return (int)((__double_as_longlong(a) >> 52) & 0x7ff);
+}
+
+// |a| * 2^(60 - e) truncated to an integer (< 2^60 when |a| < 2^e); zero and
+// subnormal inputs give 0.
+__device__ __forceinline__ unsigned long long oz_mag(double a, int e) {
+  const long long bits = __double_as_longlong(a);
+  const int eb = (int)((bits >> 52) & 0x7ff);
+  if (eb == 0) return 0ull;
+  const unsigned long long m = (unsigned long long)(bits & 0xfffffffffffffLL) | (1ull << 52);
+  const int sh = eb - 1015 - e;  // a = m 2^(eb-1075): T = m 2^(eb - 1075 + 60 - e)
+  if (sh >= 0) return m << sh;   // sh <= 7 because |a| < 2^e
+  if (sh <= -64) return 0ull;
+  return m >> (-sh);
+}
+
+__device__ __forceinline__ uint16_t bf16_bits_of_int(int q) {
+  return __bfloat16_as_ushort(__float2bfloat16_rn((float)q));
+}
+
+__device__ __forceinline__ void mma_bf16(float (&c)[4], unsigned a0, unsigned a1, unsigned a2, unsigned a3,
+                                         unsigned b0, unsigned b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
+// 2^k as a double for the normal range, else a scaled fallback
+__device__ __forceinline__ double scale2(double y, int k) {
+  if (k >= -1022 && k <= 1023) return y * __longlong_as_double((long long)(k + 1023) << 52);
+  return ldexp(y, k);
+}
+
+}  // namespace
+
+// One thread per (entry, row): the row exponent, then the slices of each
+// element.  The caller zeroes S (padding rows and K columns stay zero).
+__global__ void oz_slice_rows_kernel(const double* A, long lda, long sA, int rows, int K, int nb, uint16_t* S,
+                                     int* ex, int rowsP, int KP) {
+  const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (t >= (long)nb * rows) return;
+  const int z = (int)(t / rows), r = (int)(t - (long)z * rows);
+  const double* a = A + (size_t)z * sA + r;
+  int mx = 0;
+  for (int k = 0; k < K; ++k) mx = max(mx, biased_exp(a[(size_t)k * lda]));
+  const int e = mx - 1022;  // |a| < 2^e for every entry of the row
+  ex[(size_t)z * rowsP + r] = mx ? e : 0;
+  uint16_t* s0 = S + (size_t)z * kOzS * rowsP * KP + (size_t)r * KP;
+  const size_t sls = (size_t)rowsP * KP;
+  for (int k = 0; k < K; ++k) {
+    const double v = a[(size_t)k * lda];
+    const unsigned long long T = mx ? oz_mag(v, e) : 0ull;
+#pragma unroll
+    for (int s = 0; s < kOzS; ++s) {
+      const int q = (int)((T >> (kOzW * (kOzS - 1 - s))) & ((1u << kOzW) - 1));
+      s0[s * sls + k] = bf16_bits_of_int(v < 0 ? -q : q);
+    }
+  }
+}
+
+cudaError_t launch_oz_slice_rows(const double* A, long lda, long sA, int rows, int K, int nb, uint16_t* S, int* ex,
+                                 int rowsP, int KP, cudaStream_t s) {
+  const long n = (long)nb * rows;
+  if (n <= 0) return cudaSuccess;
+  oz_slice_rows_kernel<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(A, lda, sA, rows, K, nb, S, ex, rowsP, KP);
+  return cudaGetLastError();
+}
+
+// Column slices of X: block (64 columns, batch entry); the column
+// exponent from four strided partial maxima, then every (k, column) element
+// cut into its kOzS slices, written slice plane by slice plane (coalesced
+// along the columns).
+__global__ void __launch_bounds__(256) oz_slice_cols_kernel(const double* X, long ldx, long sX, int K, int N,
+                                                            uint16_t* Xs, int* cexp, int KP, int Np) {
+  __shared__ int ex[4][64];
+  const int c = threadIdx.x & 63, kq = threadIdx.x >> 6;
+  const int z = blockIdx.y, n = blockIdx.x * 64 + c;
+  const double* Xz = X + (size_t)z * sX;
+  int mx = 0;
+  if (n < N)
+    for (int k = kq; k < K; k += 4) mx = max(mx, biased_exp(Xz[(size_t)k * ldx + n]));
+  ex[kq][c] = mx;
+  __syncthreads();
+  const int fb = max(max(ex[0][c], ex[1][c]), max(ex[2][c], ex[3][c]));
+  if (kq == 0 && n < Np) cexp[(size_t)z * Np + n] = fb;
+  if (n >= Np) return;
+  uint16_t* xz = Xs + (size_t)z * kOzS * KP * Np;
+  for (int k = kq; k < KP; k += 4) {
+    unsigned long long T = 0ull;
+    bool neg = false;
+    if (k < K && n < N && fb > 0) {
+      const double v = Xz[(size_t)k * ldx + n];
+      T = oz_mag(v, fb - 1022);
+      neg = v < 0.0;
+    }
+#pragma unroll
+    for (int sl = 0; sl < kOzS; ++sl) {
+      const int q = (int)((T >> (kOzW * (kOzS - 1 - sl))) & ((1u << kOzW) - 1));
+      xz[((size_t)sl * KP + k) * Np + n] = bf16_bits_of_int(neg ? -q : q);
+    }
+  }
+}
+
+cudaError_t launch_oz_slice_cols(const double* X, long ldx, long sX, int K, int N, int batch, uint16_t* Xs,
+                                 int* cexp, int KP, int Np, cudaStream_t s) {
+  if (N <= 0 || batch <= 0) return cudaSuccess;
+  dim3 grid((Np + 63) / 64, batch);
+  oz_slice_cols_kernel<<<grid, 256, 0, s>>>(X, ldx, sX, K, N, Xs, cexp, KP, Np);
+  return cudaGetLastError();
+}
+
+namespace {
+
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+  const unsigned saddr = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(saddr), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+__device__ __forceinline__ void ldsm_x4(unsigned (&r)[4], const void* p) {
+  const unsigned a = (unsigned)__cvta_generic_to_shared(p);
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]) : "r"(a));
+}
+__device__ __forceinline__ void ldsm_x2t(unsigned (&r)[2], const void* p) {
+  const unsigned a = (unsigned)__cvta_generic_to_shared(p);
+  asm volatile("ldmatrix.sync.aligned.m8n8.x2.trans.shared.b16 {%0,%1}, [%2];\n" : "=r"(r[0]), "=r"(r[1]) : "r"(a));
+}
+
+}  // namespace
+
+// Tiled slice GEMM.  Block: MT row tiles (16 rows) x NQ column groups (16
+// columns), one warp per (row tile, column group), K in chunks of 16 staged
+// in shared memory by cp.async two chunks deep (slices of A and X for all
+// kOzS slices of the chunk); fragments by ldmatrix from padded rows (48 and
+// NQ*32+16 bytes: conflict-free).  Per chunk a warp does the 55 slice-pair
+// products s + t <= kOzD on its two 16x8 tiles.
+template <int MT, int NQ>
+__global__ void __launch_bounds__(32 * MT * NQ) oz_mma_kernel(GemmArgs q) {
+  constexpr int AROW = 24, XROW = NQ * 16 + 8;           // padded row lengths (bf16)
+  constexpr int ASTAGE = kOzS * MT * 16 * AROW, XSTAGE = kOzS * 16 * XROW;
+  extern __shared__ __align__(16) uint16_t oz_panel[];   // [2][ASTAGE + XSTAGE]
+  const int z = blockIdx.z;
+  const int col0 = blockIdx.x * NQ * 16, row0b = blockIdx.y * MT * 16;
+  const uint16_t* Az = q.oz_s + (size_t)z * q.oz_sz + (size_t)(q.oz_row0 + row0b) * q.oz_KP;
+  const size_t aslice = (size_t)q.oz_rowsP * q.oz_KP;
+  const uint16_t* Xz = q.oz_xs + (size_t)z * kOzS * q.oz_KP * q.oz_Np + col0;
+  const size_t xslice = (size_t)q.oz_KP * q.oz_Np;
+  const int tid = threadIdx.x, nthr = 32 * MT * NQ;
+  auto stage = [&](int k0, int buf) {
+    uint16_t* Ap = oz_panel + buf * (ASTAGE + XSTAGE);
+    uint16_t* Xp = Ap + ASTAGE;
+    for (int i = tid; i < kOzS * MT * 16 * 2; i += nthr) {        // A: (slice, row, half)
+      const int h = i & 1, rr = (i >> 1) % (MT * 16), sl = (i >> 1) / (MT * 16);
+      cp_async16(Ap + (sl * MT * 16 + rr) * AROW + 8 * h, Az + sl * aslice + (size_t)rr * q.oz_KP + k0 + 8 * h);
+    }
+    for (int i = tid; i < kOzS * 16 * 2 * NQ; i += nthr) {        // X: (slice, k, 8-column chunk)
+      const int cq = i % (2 * NQ), kk = (i / (2 * NQ)) % 16, sl = i / (2 * NQ * 16);
+      cp_async16(Xp + (sl * 16 + kk) * XROW + 8 * cq, Xz + sl * xslice + (size_t)(k0 + kk) * q.oz_Np + 8 * cq);
+    }
+    cp_commit();
+  };
+  const int warp = tid >> 5, lane = tid & 31, gid = lane >> 2, tig = lane & 3;
+  const int wm = warp % MT, wn = warp / MT;
+  float acc[kOzD + 1][2][4];
+#pragma unroll
+  for (int d = 0; d <= kOzD; ++d)
+#pragma unroll
+    for (int nt = 0; nt < 2; ++nt)
+#pragma unroll
+      for (int i = 0; i < 4; ++i) acc[d][nt][i] = 0.f;
+  const int nk = q.oz_KP / 16;
+  stage(0, 0);
+  for (int kc = 0; kc < nk; ++kc) {
+    if (kc + 1 < nk) {
+      stage((kc + 1) * 16, (kc + 1) & 1);
+      cp_wait<1>();
+    } else {
+      cp_wait<0>();
+    }
+    __syncthreads();
+    const uint16_t* Ap = oz_panel + (kc & 1) * (ASTAGE + XSTAGE);
+    const uint16_t* Xp = Ap + ASTAGE;
+    unsigned bf[kOzS][2][2];
+#pragma unroll
+    for (int t = 0; t < kOzS; ++t)
+#pragma unroll
+      for (int nt = 0; nt < 2; ++nt)
+        ldsm_x2t(bf[t][nt], Xp + (t * 16 + (lane & 15)) * XROW + wn * 16 + nt * 8);
+#pragma unroll
+    for (int sl = 0; sl < kOzS; ++sl) {
+      unsigned af[4];
+      ldsm_x4(af, Ap + (sl * MT * 16 + wm * 16 + (lane & 15)) * AROW + (lane >> 4) * 8);
+#pragma unroll
+      for (int t = 0; t < kOzS && sl + t <= kOzD; ++t)
+#pragma unroll
+        for (int nt = 0; nt < 2; ++nt) mma_bf16(acc[sl + t][nt], af[0], af[1], af[2], af[3], bf[t][nt][0], bf[t][nt][1]);
+    }
+    __syncthreads();  // every warp is done with this buffer before it is refilled
+  }
+  // recombination: Y = 2^(e_r + f_n - 36) (H + 2^-30 L)
+  const int* aex = q.oz_ex + (size_t)z * q.oz_rowsP + q.oz_row0;
+  const int* cex = q.oz_cexp + (size_t)z * q.oz_Np;
+  double* Y = q.Y + (size_t)z * q.sY;
+#pragma unroll
+  for (int nt = 0; nt < 2; ++nt) {
+    const int n = col0 + wn * 16 + nt * 8 + tig * 2;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int r = row0b + wm * 16 + gid + 8 * h;
+      if (r >= q.rows || n >= q.N) continue;
+      const int er = aex[r];
+      double out[2];
+#pragma unroll
+      for (int j = 0; j < 2; ++j) {
+        const int i = 2 * h + j;
+        long long H = 0, L = 0;
+#pragma unroll
+        for (int d = 0; d <= 4; ++d) H = H * 64 + (long long)__float2int_rn(acc[d][nt][i]);
+#pragma unroll
+        for (int d = 5; d <= kOzD; ++d) L = L * 64 + (long long)__float2int_rn(acc[d][nt][i]);
+        const int fb = cex[n + j];
+        const double y = fma((double)L, 0x1p-30, (double)H);
+        out[j] = (fb > 0 && (H != 0 || L != 0)) ? q.alpha * scale2(y, er + (fb - 1022) - 36) : 0.0;
+      }
+      double* yp = Y + (size_t)r * q.ldy + n;
+      if (n + 1 < q.N) {
+        if ((reinterpret_cast<uintptr_t>(yp) & 15) == 0) {
+          *reinterpret_cast<double2*>(yp) = make_double2(out[0], out[1]);
+        } else {
+          yp[0] = out[0];
+          yp[1] = out[1];
+        }
+      } else {
+        yp[0] = out[0];
+      }
+    }
+  }
+}
+
+template <int MT, int NQ>
+static cudaError_t launch_oz_mt(const GemmArgs& g, cudaStream_t s) {
+  constexpr size_t smem = 2 * ((size_t)kOzS * MT * 16 * 24 + (size_t)kOzS * 16 * (NQ * 16 + 8)) * sizeof(uint16_t);
+  static bool opted[64] = {false};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev >= 0 && dev < 64 && !opted[dev]) {
+    const cudaError_t e = cudaFuncSetAttribute(oz_mma_kernel<MT, NQ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               (int)smem);
+    if (e != cudaSuccess) return e;
+    opted[dev] = true;
+  }
+  dim3 grid((g.N + NQ * 16 - 1) / (NQ * 16), (g.rows + MT * 16 - 1) / (MT * 16), g.batch);
+  oz_mma_kernel<MT, NQ><<<grid, 32 * MT * NQ, smem, s>>>(g);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_oz_gemm(const GemmArgs& g, cudaStream_t s) {
+  if (g.rows <= 0 || g.N <= 0 || g.batch <= 0) return cudaSuccess;
+  if (g.K > 257 || g.oz_KP < g.K || !g.oz_xs || (g.oz_Np % 32) != 0) return cudaErrorInvalidValue;
+  // row tiles per block: the fewest blocks of at most four tiles, balanced
+  const int rt = (g.rows + 15) / 16, groups = (rt + 3) / 4, mt = (rt + groups - 1) / groups;
+  const bool wide = g.N > 16;
+  switch (mt) {
+    case 1: return wide ? launch_oz_mt<1, 2>(g, s) : launch_oz_mt<1, 1>(g, s);
+    case 2: return wide ? launch_oz_mt<2, 2>(g, s) : launch_oz_mt<2, 1>(g, s);
+    case 3: return wide ? launch_oz_mt<3, 2>(g, s) : launch_oz_mt<3, 1>(g, s);
+    default: return wide ? launch_oz_mt<4, 2>(g, s) : launch_oz_mt<4, 1>(g, s);
+  }
+}
+
+}  // namespace falcon

@@ -98,7 +98,7 @@ EXPORTS = (
     "falcon_batch_profile", "falcon_launch_count", "falcon_fp64_mma_peak_gflops",
     "falcon_nonlin_noalloc_dev", "falcon_set_step_graphs", "falcon_store_checkpoint", "falcon_load_checkpoint",
     "falcon_store_snapshot", "falcon_batch_store_checkpoint", "falcon_batch_load_checkpoint",
-    "falcon_batch_store_snapshot", "falcon_restart", "falcon_batch_restart",
+    "falcon_batch_store_snapshot", "falcon_restart", "falcon_batch_restart", "falcon_set_gemm_mode",
 )
 
 
@@ -397,6 +397,13 @@ def fp64_mma_peak_gflops():
 
 def launch_count():
     return lib().falcon_launch_count()
+
+
+def set_gemm_mode(mode):
+    """1: operator contractions on the tensor cores by exact slicing; 0: FP64 FMA tiles.
+    Returns the previous mode."""
+    lib().falcon_set_gemm_mode.argtypes = [ctypes.c_int]
+    return lib().falcon_set_gemm_mode(1 if mode else 0)
 
 
 def set_step_graphs(enable):

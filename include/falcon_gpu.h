@@ -283,6 +283,16 @@ long long falcon_launch_count(void);
  * Returns the previous setting.  Results are identical either way.
  * No reference counterpart (launch mechanics of the GPU step). */
 int falcon_set_step_graphs(int enable);
+/* Operator contractions (the radial derivative / Laplacian and per-mode
+ * solve products) on the bf16 tensor cores by exact integer slicing of the
+ * FP64 operands (mode 1, the default) or as FP64 FMA tiles (mode 0).  Both
+ * give FP64-accurate results (error of the order of K 2^-56 max|A_row|
+ * max|X_col| for the slices); the first is several times faster on GB300,
+ * whose FP64 pipe is ~500x slower than its bf16 tensor cores.  Applies to
+ * launches after the call (step graphs already captured keep their mode).
+ * Returns the previous mode.  No counterpart in the reference, which uses
+ * LAPACK dgetrs (src/algebra_lapack.F90). */
+int falcon_set_gemm_mode(int mode);
 
 /* ---- misc ---- */
 const char* falcon_last_error(void);

@@ -65,3 +65,18 @@ def test_graph_replay_after_reset_and_new_state(fg):
         fg.set_step_graphs(prev)
     for f in FIELDS:
         assert np.array_equal(s1[f], s2[f]), f
+
+
+def test_block_per_line_and_warp_per_line_transforms_agree_bitwise(fg):
+    # one instance of Nr=97, Np=1023 (radix 3, 11, 31) runs the block-per-line
+    # nonlinear pass, four of them the warp-per-line one: the same bits
+    p = fg.make_params(97, 341, "ARS443", ra=1e6, dt=1e-7)
+    alone = fg.Instance(p)
+    alone.init_noise(9)
+    alone.step(3)
+    b = fg.Batch([p] * 4)
+    b.init_noise([9, 10, 11, 12])
+    b.step(3)
+    sa, sb = alone.get_state(), b.get_state(0)
+    for f in FIELDS:
+        assert np.array_equal(sa[f], sb[f]), f

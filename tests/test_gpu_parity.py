@@ -187,6 +187,24 @@ def test_mixed_batch_each_instance_matches_oracle(orc, fg):
         assert max(rel(gs[k], os_[k]) for k in ("T", "omg", "up", "ur")) < STEP_TOL
 
 
+def test_instance_close_alone_and_in_large_batch(fg):
+    # in a batch of 12 the per-mode solves take the tensor-core slices (16+
+    # columns), alone the FP64 FMA path: equal to FP64 rounding
+    from conftest import rel
+    R, Nm, n = 33, 42, 12
+    ps = [fg.make_params(R, Nm, "SBDF3", ra=1e5 * (1 + k), dt=1e-5) for k in range(n)]
+    b = fg.Batch(ps)
+    b.init_noise([500 + k for k in range(n)])
+    b.step(20)
+    k = 5
+    alone = fg.Instance(ps[k])
+    alone.init_noise(500 + k)
+    alone.step(20)
+    sb, sa = b.get_state(k), alone.get_state()
+    for f in ("T", "omg", "up", "ur", "psi"):
+        assert rel(sb[f], sa[f]) < 1e-12, f
+
+
 def test_instance_identical_alone_and_in_batch(fg):
     R, Nm, n = 65, 170, 6
     ras = [10 ** (6 + 2 * u) for u in np.linspace(0.1, 0.9, n)]
