@@ -128,7 +128,7 @@ __global__ void __launch_bounds__(256) oz_slice_cols_kernel(const double* X, lon
     if (k < K && n < N && fb > 0) {
       const double v = Xz[(size_t)k * ldx + n];
       T = oz_mag(v, fb - 1022);
-      neg = v < 0.0;
+      neg = __double_as_longlong(v) < 0;
     }
 #pragma unroll
     for (int sl = 0; sl < kOzS; ++sl) {
@@ -297,8 +297,19 @@ static cudaError_t launch_oz_mt(const GemmArgs& g, cudaStream_t s) {
 cudaError_t launch_oz_gemm(const GemmArgs& g, cudaStream_t s) {
   if (g.rows <= 0 || g.N <= 0 || g.batch <= 0) return cudaSuccess;
   if (g.K > 257 || g.oz_KP < g.K || !g.oz_xs || (g.oz_Np % 32) != 0) return cudaErrorInvalidValue;
-  // row tiles per block: the fewest blocks of at most four tiles, balanced
-  const int rt = (g.rows + 15) / 16, groups = (rt + 3) / 4, mt = (rt + groups - 1) / groups;
+  // Row tiles per block: all of them up to 8 (one column group of 16, so
+  // the operator panel is staged once for every row of the block), else the
+  // fewest balanced blocks of at most 4 tiles with two column groups.
+  const int rt = (g.rows + 15) / 16;
+  if (rt >= 5 && rt <= 8) {
+    switch (rt) {
+      case 5: return launch_oz_mt<5, 1>(g, s);
+      case 6: return launch_oz_mt<6, 1>(g, s);
+      case 7: return launch_oz_mt<7, 1>(g, s);
+      default: return launch_oz_mt<8, 1>(g, s);
+    }
+  }
+  const int groups = (rt + 3) / 4, mt = (rt + groups - 1) / groups;
   const bool wide = g.N > 16;
   switch (mt) {
     case 1: return wide ? launch_oz_mt<1, 2>(g, s) : launch_oz_mt<1, 1>(g, s);
