@@ -1597,12 +1597,19 @@ int group_step(Group* g) {
 
 // After a state is loaded: histories zeroed, current slot = state,
 // Y0 = state (src/init.F90:393-395, src/timeschemes.F90:51-53).
+int group_reset_arrays(Group* g);
 int group_reset(Group* g) {
+  g->n_step = 0;
+  g->tot_time = 0.0;
+  return group_reset_arrays(g);
+}
+
+// The array part of group_reset: every column restarted from its state,
+// step count and time kept (group_reset_instance on all columns at once).
+int group_reset_arrays(Group* g) {
   const int R = g->R, M = g->M, B = g->B;
   const size_t n = g->nel();
   cudaStream_t s = g->stream;
-  g->n_step = 0;
-  g->tot_time = 0.0;
   if (g->p.scheme_type == FALCON_IMEX) {
     const int ni = g->sch.n_imp, ne = g->sch.n_exp;
     for (int i = 0; i < ni; ++i)
@@ -1630,23 +1637,48 @@ int group_reset(Group* g) {
   return 0;
 }
 
-// Upload one instance's Fortran-layout fields (host) into the group.
+// Upload one instance's Fortran-layout fields (host) into the group.  The
+// copies read the caller's arrays directly: from pageable memory the copy
+// has taken the data when the call returns, from pinned memory it is still
+// in flight, so callers synchronise the stream before they return (every
+// C-ABI caller does, through group_reset_instance or falcon_batch sync).
 int group_set_instance(Group* g, int b, const double* t, const double* w, const double* up, const double* ur) {
   const int R = g->R, M = g->M, B = g->B;
-  const size_t nb = sizeof(double2) * (size_t)M * R;
+  const size_t ne = (size_t)M * R, nb = sizeof(double2) * ne;
   double2* d = nullptr;
-  CK(cudaMallocAsync(&d, nb, g->stream));
+  CK(cudaMallocAsync(&d, 4 * nb, g->stream));
   const double* src[4] = {t, w, up, ur};
   double2* dst[4] = {g->T(), g->W(), g->up, g->ur};
   for (int f = 0; f < 4; ++f) {
-    if (src[f]) {
-      std::memcpy(g->stage_buf, src[f], nb);
-      CK(cudaMemcpyAsync(d, g->stage_buf, nb, cudaMemcpyHostToDevice, g->stream));
-    } else {
-      CK(cudaMemsetAsync(d, 0, nb, g->stream));
+    if (src[f]) CK(cudaMemcpyAsync(d + f * ne, src[f], nb, cudaMemcpyHostToDevice, g->stream));
+    else CK(cudaMemsetAsync(d + f * ne, 0, nb, g->stream));
+    CK(launch_scatter_instance(R, M, B, b, d + f * ne, dst[f], g->stream));
+  }
+  CK(cudaFreeAsync(d, g->stream));
+  return 0;
+}
+
+// Every column of the group from host arrays: each run gives `len`
+// consecutive slots from `slot0` on, its instances back to back in the host
+// arrays (2 M R doubles each; a null field is zeros).  One copy per run and
+// field, one scatter per field.
+struct HostRun {
+  int slot0, len;
+  const double* src[4];
+};
+int group_set_columns(Group* g, const std::vector<HostRun>& runs) {
+  const int R = g->R, M = g->M, B = g->B;
+  const size_t ne = (size_t)M * R, nb = sizeof(double2) * ne;
+  double2* d = nullptr;
+  CK(cudaMallocAsync(&d, nb * B, g->stream));
+  double2* dst[4] = {g->T(), g->W(), g->up, g->ur};
+  for (int f = 0; f < 4; ++f) {
+    for (const HostRun& k : runs) {
+      double2* to = d + (size_t)k.slot0 * ne;
+      if (k.src[f]) CK(cudaMemcpyAsync(to, k.src[f], nb * k.len, cudaMemcpyHostToDevice, g->stream));
+      else CK(cudaMemsetAsync(to, 0, nb * k.len, g->stream));
     }
-    CK(launch_scatter_instance(R, M, B, b, d, dst[f], g->stream));
-    CK(cudaStreamSynchronize(g->stream));
+    CK(launch_scatter_columns(R, M, B, d, dst[f], g->stream));
   }
   CK(cudaFreeAsync(d, g->stream));
   return 0;
@@ -2829,6 +2861,38 @@ int falcon_batch_set_state(falcon_batch* b, int i, const double* tFR, const doub
   b->restart_pending = false;
   if (g->n_step == 0) g->tot_time = 0.0;
   return group_reset_instance(g, b->where[i].second);
+}
+
+int falcon_batch_set_states(falcon_batch* b, const double* tFR, const double* omgFR, const double* upFR,
+                            const double* urFR) {
+  if (!b || !tFR) return fail(FALCON_EINVAL, "null argument");
+  const size_t n = b->params.size();
+  const double* src[4] = {tFR, omgFR, upFR, urFR};
+  std::vector<std::vector<HostRun>> runs(b->groups.size());
+  std::vector<int> last(b->groups.size(), -2);  // host instance that ends each group's last run
+  size_t off = 0;
+  for (size_t i = 0; i < n; ++i) {
+    const int gi = b->where[i].first, slot = b->where[i].second;
+    auto& rv = runs[gi];
+    if (!rv.empty() && last[gi] == (int)i - 1 && rv.back().slot0 + rv.back().len == slot) {
+      rv.back().len += 1;
+    } else {
+      HostRun k{slot, 1, {}};
+      for (int f = 0; f < 4; ++f) k.src[f] = src[f] ? src[f] + off : nullptr;
+      rv.push_back(k);
+    }
+    last[gi] = (int)i;
+    off += 2 * (size_t)b->params[i].nr_max * (b->params[i].nm_max + 1);
+  }
+  for (size_t gi = 0; gi < b->groups.size(); ++gi) {
+    Group* g = b->groups[gi].get();
+    int rc = group_set_columns(g, runs[gi]);
+    if (!rc) rc = group_reset_arrays(g);
+    if (rc) return rc;
+    if (g->n_step == 0) g->tot_time = 0.0;
+  }
+  b->restart_pending = false;
+  return b->sync();
 }
 
 int falcon_batch_init_state(falcon_batch* b, int kind, double amp, const uint64_t* seeds) {

@@ -242,6 +242,7 @@ cudaError_t launch_stage_deriv(const StageArgs& a, cudaStream_t s);
 // Fortran (M,R) complex of instance b <-> device [r][m][b]
 cudaError_t launch_scatter_instance(int R, int M, int B, int b, const double2* src, double2* dst,
                                     cudaStream_t s);
+cudaError_t launch_scatter_columns(int R, int M, int B, const double2* src, double2* dst, cudaStream_t s);
 cudaError_t launch_gather_instance(int R, int M, int B, int b, const double2* src, double2* dst,
                                    cudaStream_t s);
 // dst[r][b] = src[r][0][b].x  (mode-0 real part)

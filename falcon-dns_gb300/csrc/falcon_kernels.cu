@@ -1184,6 +1184,22 @@ cudaError_t launch_scatter_instance(int R, int M, int B, int b, const double2* s
   scatter_instance_kernel<<<ew_grid((size_t)R * M), 256, 0, s>>>(R, M, B, b, src, dst);
   return cudaGetLastError();
 }
+// All B columns at once: src holds the B instances' Fortran (M, R) arrays
+// back to back in slot order; the slot index runs fastest over the threads
+// so the stores to the batched (R, M, B) layout are coalesced.
+__global__ void scatter_columns_kernel(int R, int M, int B, const double2* __restrict__ src,
+                                      double2* __restrict__ dst) {
+  const size_t rm = (size_t)R * M, n = rm * B;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const size_t e = i / B;  // r * M + m
+    const int b = (int)(i - e * B);
+    dst[i] = src[(size_t)b * rm + e];
+  }
+}
+cudaError_t launch_scatter_columns(int R, int M, int B, const double2* src, double2* dst, cudaStream_t s) {
+  scatter_columns_kernel<<<ew_grid((size_t)R * M * B), 256, 0, s>>>(R, M, B, src, dst);
+  return cudaGetLastError();
+}
 cudaError_t launch_gather_instance(int R, int M, int B, int b, const double2* src, double2* dst,
                                    cudaStream_t s) {
   gather_instance_kernel<<<ew_grid((size_t)R * M), 256, 0, s>>>(R, M, B, b, src, dst);

@@ -90,6 +90,7 @@ EXPORTS = (
     "falcon_create", "falcon_destroy", "falcon_init_state", "falcon_set_state", "falcon_get_state",
     "falcon_step", "falcon_diagnostics", "falcon_batch_create", "falcon_batch_destroy",
     "falcon_batch_size", "falcon_batch_ngroups", "falcon_batch_init_state", "falcon_batch_set_state",
+    "falcon_batch_set_states",
     "falcon_batch_get_state", "falcon_batch_step", "falcon_batch_diagnostics", "falcon_batch_set_stream",
     "falcon_batch_device_bytes", "falcon_nonlin_dev", "falcon_nonlin", "falcon_getrs_batched_dev",
     "falcon_cheb_fwd_dev", "falcon_cheb_inv_dev", "falcon_cheb_d1_dev", "falcon_cheb_d2_dev",
@@ -133,6 +134,7 @@ def lib():
     L.falcon_batch_ngroups.argtypes = [vp]
     L.falcon_batch_init_state.argtypes = [vp, ip, ctypes.c_double, P(ctypes.c_uint64)]
     L.falcon_batch_set_state.argtypes = [vp, ip, dp, dp, dp, dp]
+    L.falcon_batch_set_states.argtypes = [vp, dp, dp, dp, dp]
     L.falcon_batch_get_state.argtypes = [vp, ip, dp, dp, dp, dp, dp]
     L.falcon_batch_step.argtypes = [vp, ip]
     L.falcon_batch_diagnostics.argtypes = [vp, P(FalconDiag)]
@@ -257,6 +259,29 @@ class Batch:
     def set_state(self, i, t, om=None, up=None, ur=None):
         arrs = [None if a is None else np.ascontiguousarray(a, np.complex128) for a in (t, om, up, ur)]
         check(lib().falcon_batch_set_state(self.h, i, *[_dp(a) for a in arrs]))
+
+    def set_states(self, t, om=None, up=None, ur=None):
+        """Every instance's state at once (falcon_batch_set_states).  Each
+        field is either one contiguous complex128 array holding the
+        instances' (Nr, Nm + 1) arrays back to back in instance order (used
+        in place, e.g. a view of pinned memory) or a list of n such arrays
+        (concatenated on the host first)."""
+        total = sum(p.nr_max * (p.nm_max + 1) for p in self.params)
+
+        def flat(a):
+            if a is None:
+                return None
+            if isinstance(a, (list, tuple)):
+                if len(a) != self.n:
+                    raise ValueError("expected %d arrays" % self.n)
+                a = np.concatenate([np.asarray(x, np.complex128).ravel() for x in a])
+            a = np.ascontiguousarray(a, np.complex128)
+            if a.size != total:
+                raise ValueError("expected %d complex values, got %d" % (total, a.size))
+            return a
+
+        arrs = [flat(a) for a in (t, om, up, ur)]
+        check(lib().falcon_batch_set_states(self.h, *[_dp(a) for a in arrs]))
 
     def get_state(self, i):
         p = self.params[i]

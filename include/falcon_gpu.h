@@ -187,6 +187,15 @@ int falcon_batch_ngroups(const falcon_batch* b);
 int falcon_batch_init_state(falcon_batch* b, int kind, double amp, const uint64_t* seeds);
 int falcon_batch_set_state(falcon_batch* b, int i, const double* tFR, const double* omgFR,
                            const double* upFR, const double* urFR);
+/* Bulk form of falcon_batch_set_state for every instance at once (no
+ * reference counterpart: the reference loads one run's state at a time).
+ * Each array holds the n instances' Fortran-layout fields back to back,
+ * instance i at offset sum_{j<i} 2 Nr_j (Nm_j + 1) doubles; omgFR, upFR,
+ * urFR may be null (zeros).  Same result as n falcon_batch_set_state
+ * calls, with one host-to-device copy per field and group and one
+ * synchronisation; the arrays may be reused when the call returns. */
+int falcon_batch_set_states(falcon_batch* b, const double* tFR, const double* omgFR,
+                            const double* upFR, const double* urFR);
 int falcon_batch_get_state(falcon_batch* b, int i, double* tFR, double* omgFR, double* upFR,
                            double* urFR, double* psi);
 int falcon_batch_step(falcon_batch* b, int nsteps);
