@@ -448,7 +448,7 @@ def run_gpu(args):
         h2d += sum(a.nbytes for a in host)
         for k in range(k_e2e):
             b2.step(1)
-            diag = b2.diagnostics()  # writeKE_spectral every step (n_KE = 1, the namelist default)
+            diag = b2.diagnostics_array()  # writeKE_spectral every step (n_KE = 1, the namelist default)
             d2h += n * 8 * 8
         torch.cuda.synchronize()
         e2e_s = time.perf_counter() - t0

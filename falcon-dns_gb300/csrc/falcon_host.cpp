@@ -807,6 +807,7 @@ struct Group {
   double* us = nullptr;        // explicit RK: stage uphi_bar (R x B)
   double2* t_grid = nullptr;   // temperature seen by the last nonlinear pass (IMEXRK)
   double* diag_dev = nullptr;  // 8 per instance
+  double* diag_part = nullptr;  // 8 R per instance: diagnostics partial sums
   std::vector<double> diag_host;
   double2* stage_buf = nullptr;  // host staging (pinned) for one instance
   Prof* prof = nullptr;
@@ -998,7 +999,7 @@ int group_init(Group* g, const std::vector<falcon_params>& ps, const std::vector
       (rc = g->alloc(&g->lt, n)) || (rc = g->alloc(&g->lw, n)) || (rc = g->alloc(&g->lu0, (size_t)R * B)) ||
       (rc = g->alloc(&g->rhs_t, n)) || (rc = g->alloc(&g->rhs_w, n)) ||
       (rc = g->alloc(&g->ub2, (size_t)2 * R * B)) || (rc = g->alloc(&g->ra_pr, (size_t)B)) ||
-      (rc = g->alloc(&g->diag_dev, (size_t)8 * B)))
+      (rc = g->alloc(&g->diag_dev, (size_t)8 * B)) || (rc = g->alloc(&g->diag_part, (size_t)8 * R * B)))
     return rc;
   g->ub = reinterpret_cast<double*>(g->ub2);
   if (g->p.l_vartimestep) {
@@ -2406,6 +2407,7 @@ int group_diagnostics(Group* g) {
   a.nu_top_den = (1.0 - eta) / std::log(eta);
   a.pi = 4.0 * std::atan(1.0);
   a.out = g->diag_dev;
+  a.part = g->diag_part;
   CK(launch_diagnostics(a, g->stream));
   g->diag_host.resize((size_t)8 * g->B);
   CK(cudaMemcpyAsync(g->diag_host.data(), g->diag_dev, sizeof(double) * 8 * g->B, cudaMemcpyDeviceToHost, g->stream));

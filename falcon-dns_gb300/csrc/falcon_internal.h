@@ -209,7 +209,8 @@ struct DiagArgs {
   const double2 *t, *w, *up, *ur, *tprev;
   const double *wq, *d1_0, *d1_R, *ra_pr;
   double nu_top_den, nu_bot_den, pi;
-  double* out;  // 8 per instance
+  double* out;   // 8 per instance
+  double* part;  // 8 R B partial sums (radial row, instance)
 };
 
 // Non-stiffly-accurate IMEXRK assembly (elementwise part).

@@ -1553,15 +1553,19 @@ namespace falcon {
 // the last nonlinear pass, which the reference multiplies with the current
 // u_r for the buoyancy power (src/output.F90:211, :302).  Output per
 // instance (8 doubles): ke, ke_r, ke_phi, ke_upbar, nu_top, nu_bot, vis, buo.
-__global__ void diagnostics_kernel(DiagArgs a) {
-  const int b = blockIdx.x;
+// Phase 1, one block per radial row r and 32 instance columns: threads
+// (tx, ty) take column tx and the modes m = ty (mod 8), so every load of a
+// warp is one coalesced run of 32 columns.  Per (r, b) it writes the
+// radially weighted sums (k = 0..6) and the unweighted u_phi power (k = 7)
+// to part[(k R + r) B + b].
+__global__ void __launch_bounds__(256) diag_rows_kernel(DiagArgs a) {
+  const int r = blockIdx.x, tx = threadIdx.x, ty = threadIdx.y;
   const int R = a.R, M = a.M, B = a.B;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-  __shared__ double part[32][9];
-  double k_r = 0.0, k_p = 0.0, k_b = 0.0, vw = 0.0, bu = 0.0, d0 = 0.0, dR = 0.0, s_in = 0.0, s_out = 0.0;
-  for (int r = warp; r < R; r += nw) {
-    double ur2 = 0.0, up2 = 0.0, w2 = 0.0, urt = 0.0;
-    for (int m = lane; m < M; m += 32) {
+  const int b = blockIdx.y * 32 + tx;
+  __shared__ double part[8][4][33];
+  double ur2 = 0.0, up2 = 0.0, w2 = 0.0, urt = 0.0;
+  if (b < B) {
+    for (int m = ty; m < M; m += 8) {
       const size_t e = ((size_t)r * M + m) * B + b;
       const double2 u = a.ur[e], v = a.up[e], o = a.w[e], tp = a.tprev[e];
       ur2 += u.x * u.x + u.y * u.y;
@@ -1574,50 +1578,55 @@ __global__ void diagnostics_kernel(DiagArgs a) {
         urt += 2.0 * (u.x * tp.x + u.y * tp.y);
       }
     }
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-      ur2 += __shfl_xor_sync(0xffffffffu, ur2, off);
-      up2 += __shfl_xor_sync(0xffffffffu, up2, off);
-      w2 += __shfl_xor_sync(0xffffffffu, w2, off);
-      urt += __shfl_xor_sync(0xffffffffu, urt, off);
-    }
-    const double q = a.wq[r];
-    const size_t e0 = ((size_t)r * M) * B + b;
-    const double u0 = a.up[e0].x, t0 = a.t[e0].x;
-    k_r += q * ur2;
-    k_p += q * up2;
-    k_b += q * u0 * u0;
-    vw += q * w2;
-    bu += q * urt;
-    d0 += a.d1_0[r] * t0;
-    dR += a.d1_R[r] * t0;
-    if (r == 0) s_in = up2;
-    if (r == R - 1) s_out = up2;
   }
-  if (lane == 0) {
-    part[warp][0] = k_r; part[warp][1] = k_p; part[warp][2] = k_b; part[warp][3] = vw;
-    part[warp][4] = bu; part[warp][5] = d0; part[warp][6] = dR; part[warp][7] = s_in; part[warp][8] = s_out;
-  }
+  part[ty][0][tx] = ur2; part[ty][1][tx] = up2; part[ty][2][tx] = w2; part[ty][3][tx] = urt;
   __syncthreads();
-  if (threadIdx.x == 0) {
-    double t[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-    for (int w = 0; w < nw; ++w)
-      for (int i = 0; i < 9; ++i) t[i] += part[w][i];
-    const double two_pi = 2.0 * a.pi;
-    double* o = a.out + (size_t)b * 8;
-    o[0] = two_pi * (t[0] + t[1]);
-    o[1] = two_pi * t[0];
-    o[2] = two_pi * t[1];
-    o[3] = two_pi * t[2];
-    o[4] = t[6] / a.nu_top_den;
-    o[5] = t[5] / a.nu_bot_den;
-    o[6] = two_pi * t[3] - (a.mbc_sf ? (4.0 * a.pi * 2.0 * t[8] - 4.0 * a.pi * 2.0 * t[7]) : 0.0);
-    o[7] = two_pi * a.ra_pr[b] * t[4];
+  if (ty != 0 || b >= B) return;
+  for (int y = 1; y < 8; ++y) {
+    ur2 += part[y][0][tx]; up2 += part[y][1][tx]; w2 += part[y][2][tx]; urt += part[y][3][tx];
   }
+  const double q = a.wq[r];
+  const size_t e0 = ((size_t)r * M) * B + b;
+  const double u0 = a.up[e0].x, t0 = a.t[e0].x;
+  double* P = a.part + (size_t)r * B + b;
+  const size_t ks = (size_t)R * B;
+  P[0 * ks] = q * ur2;
+  P[1 * ks] = q * up2;
+  P[2 * ks] = q * u0 * u0;
+  P[3 * ks] = q * w2;
+  P[4 * ks] = q * urt;
+  P[5 * ks] = a.d1_0[r] * t0;
+  P[6 * ks] = a.d1_R[r] * t0;
+  P[7 * ks] = up2;
+}
+
+// Phase 2, one thread per instance: the radial sums in row order and the
+// eight diagnostics of writeKE_spectral / Nusselt (8 doubles per instance).
+__global__ void diag_sum_kernel(DiagArgs a) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  const int R = a.R, B = a.B;
+  if (b >= B) return;
+  const size_t ks = (size_t)R * B;
+  double t[7] = {0, 0, 0, 0, 0, 0, 0};
+  for (int r = 0; r < R; ++r)
+#pragma unroll
+    for (int k = 0; k < 7; ++k) t[k] += a.part[k * ks + (size_t)r * B + b];
+  const double s_in = a.part[7 * ks + b], s_out = a.part[7 * ks + (size_t)(R - 1) * B + b];
+  const double two_pi = 2.0 * a.pi;
+  double* o = a.out + (size_t)b * 8;
+  o[0] = two_pi * (t[0] + t[1]);
+  o[1] = two_pi * t[0];
+  o[2] = two_pi * t[1];
+  o[3] = two_pi * t[2];
+  o[4] = t[6] / a.nu_top_den;
+  o[5] = t[5] / a.nu_bot_den;
+  o[6] = two_pi * t[3] - (a.mbc_sf ? (4.0 * a.pi * 2.0 * s_out - 4.0 * a.pi * 2.0 * s_in) : 0.0);
+  o[7] = two_pi * a.ra_pr[b] * t[4];
 }
 
 cudaError_t launch_diagnostics(const DiagArgs& a, cudaStream_t s) {
-  diagnostics_kernel<<<a.B, 256, 0, s>>>(a);
+  diag_rows_kernel<<<dim3(a.R, (a.B + 31) / 32), dim3(32, 8), 0, s>>>(a);
+  diag_sum_kernel<<<(a.B + 127) / 128, 128, 0, s>>>(a);
   return cudaGetLastError();
 }
 

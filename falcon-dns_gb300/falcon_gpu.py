@@ -75,6 +75,9 @@ class FalconDiag(ctypes.Structure):
         return {n: getattr(self, n) for n, _ in self._fields_}
 
 
+DIAG_DTYPE = np.dtype([(n, np.float64) for n, _ in FalconDiag._fields_])
+
+
 class KernelStat(ctypes.Structure):
     _fields_ = [("name", ctypes.c_char * 32), ("launches", ctypes.c_int), ("ms", ctypes.c_double),
                 ("flops", ctypes.c_double)]
@@ -300,6 +303,14 @@ class Batch:
         out = (FalconDiag * self.n)()
         check(lib().falcon_batch_diagnostics(self.h, out))
         return [d.as_dict() for d in out]
+
+    def diagnostics_array(self):
+        """The same values as diagnostics() in one numpy structured array
+        (fields time, dt, ke, ...; one record per instance), without the
+        per-instance Python objects."""
+        out = np.zeros(self.n, DIAG_DTYPE)
+        check(lib().falcon_batch_diagnostics(self.h, out.ctypes.data_as(ctypes.POINTER(FalconDiag))))
+        return out
 
     def store_checkpoint(self, i, path):
         """store_checkpoint layout (Fortran unformatted records) of instance i."""
