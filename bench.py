@@ -332,8 +332,22 @@ def gpu_warmup(args):
 
 
 # launch class -> kernel function
-KERNEL_OF_CLASS = {"gemm_radial": "gemm_tile_kernel", "gemm_mode_solve": "gemm_tile_kernel",
+KERNEL_OF_CLASS = {"gemm_radial": "oz_mma_kernel", "gemm_mode_solve": "oz_mma_kernel",
                    "nonlin_fft": "nonlin_kernel", "elementwise": "elementwise kernels"}
+# The operator GEMMs of this workload (N >= 16 columns each) run as products
+# of 6-bit integer slices on the bf16 tensor cores: 10 slices per operand and
+# the 55 slice pairs s + t <= 9, i.e. 55 bf16 products per FP64 product.
+OZ_SLICE_PAIRS = 55
+
+
+def tensor_peak():
+    """Measured bf16 dense peak (TFLOP/s) for a kernel timed inside a long
+    step (the sustained figure), with where it came from."""
+    try:
+        d = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        return float(d["bf16_tflops_sustained"]), "bf16_tflops_sustained of measured MEASURED_PEAKS.json"
+    except (OSError, ValueError, KeyError):
+        return 1700.0, "fallback 1.7 PFLOP/s sustained bf16"
 
 
 def load_traffic(kernel):
@@ -396,7 +410,7 @@ def run_gpu(args):
     prof = b.profile(3)
     tot = sum(v["ms"] for v in prof.values())
     # the launch classes by kernel function: both GEMM classes are launches
-    # of gemm_tile_kernel, which is therefore the dominant kernel
+    # of oz_mma_kernel (with the slicing of their X columns)
     kern = {}
     for c, v in prof.items():
         k = KERNEL_OF_CLASS.get(c, c)
@@ -409,20 +423,30 @@ def run_gpu(args):
             e["traffic_sum"] += t * v["launches"]
     dom = max(kern, key=lambda k: kern[k]["ms"])
 
+    tpeak, tpeak_src = tensor_peak()
+
     def kernel_roof(k):
         e = kern[k]
         ach = e["flops"] / (e["ms"] / 1e3) / 1e12
-        return {"achieved": ach, "frac": ach / (peak / 1e3), "share": e["ms"] / tot,
-                "launches_per_step": e["launches"] / 3,
-                "traffic": (e["traffic_sum"] / e["launches"]) if (e["traffic_ok"] and e["launches"]) else None}
+        r = {"bound": "fp64", "achieved": ach, "peak": peak / 1e3, "frac": ach / (peak / 1e3), "share": e["ms"] / tot,
+             "launches_per_step": e["launches"] / 3,
+             "traffic": (e["traffic_sum"] / e["launches"]) if (e["traffic_ok"] and e["launches"]) else None}
+        if k == "oz_mma_kernel":
+            # bf16 slice products executed per second against the tensor
+            # peak; the FP64-equivalent rate against the DFMA peak beside it
+            r.update({"bound": "tensor", "achieved": ach * OZ_SLICE_PAIRS, "peak": tpeak,
+                      "frac": ach * OZ_SLICE_PAIRS / tpeak, "peak_source": tpeak_src,
+                      "fp64_equivalent_tflops": ach, "fp64_equivalent_over_dfma_peak": ach / (peak / 1e3),
+                      "note": "time includes the per-call slicing of the X columns (oz_slice_cols_kernel)"})
+        return r
     d = kernel_roof(dom)
     achieved = d["achieved"]
-    roofline = {"bound": "fp64", "achieved": achieved, "peak": peak / 1e3, "unit": "TFLOP/s",
-                "frac": achieved / (peak / 1e3), "traffic": d["traffic"], "kernel": dom,
+    roofline = {"bound": d["bound"], "achieved": achieved, "peak": d["peak"], "unit": "TFLOP/s",
+                "frac": d["frac"], "traffic": d["traffic"], "kernel": dom,
                 "share": d["share"],
                 "kernels": {k: kernel_roof(k) for k in kern},
-                "peak_source": "FP64 FMA throughput measured live by the library's DFMA kernel "
-                               "(no FP64 figure in MEASURED_PEAKS.json)",
+                "peak_source": d.get("peak_source", "FP64 FMA throughput measured live by the library's DFMA "
+                                                    "kernel (no FP64 figure in MEASURED_PEAKS.json)"),
                 "fp64_mma_peak_tflops": mma_peak / 1e3,
                 "classes": {k: {"ms_per_step": v["ms"] / 3, "tflops": v["flops"] / (v["ms"] / 1e3) / 1e12,
                                 "share": v["ms"] / tot, "launches_per_step": v["launches"] / 3}

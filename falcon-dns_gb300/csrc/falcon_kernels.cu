@@ -407,13 +407,16 @@ __global__ void __launch_bounds__(128) nonlin_kernel(NonlinArgs a) {
   // Grid values: bufA = conj(t + i omg) -> t = A.x, omg = -A.y; likewise for
   // (u_phi, u_r) in bufB.  Products, in natural order for the DIF.
   double urmax = 0.0, upmax = 0.0;
+  const bool want_max = a.umax != nullptr;
   for (int j = lane; j < P; j += 32) {
     const double2 za = bufA[j], zb = bufB[j];
     const double tt = za.x, om = -za.y, up = zb.x, ur = -zb.y;
     bufA[j] = make_double2(up * tt, ur * tt);
     bufB[j] = make_double2(up * om, ur * om);
-    urmax = fmax(urmax, fabs(ur));
-    upmax = fmax(upmax, fabs(up));
+    if (want_max) {  // FP64 max instructions only when the CFL inputs are read
+      urmax = fmax(urmax, fabs(ur));
+      upmax = fmax(upmax, fabs(up));
+    }
   }
   __syncwarp();
   {  // DIF: outermost radix first
@@ -502,13 +505,16 @@ __global__ void __launch_bounds__(64 * S) nonlin_line_kernel(NonlinArgs a) {
     }
   }
   double urmax = 0.0, upmax = 0.0;
+  const bool want_max = a.umax != nullptr;
   for (int j = tid; j < P; j += nt) {
     const double2 za = bufA[j], zb = bufB[j];
     const double tt = za.x, om = -za.y, up = zb.x, ur = -zb.y;
     bufA[j] = make_double2(up * tt, ur * tt);
     bufB[j] = make_double2(up * om, ur * om);
-    urmax = fmax(urmax, fabs(ur));
-    upmax = fmax(upmax, fabs(up));
+    if (want_max) {  // FP64 max instructions only when the CFL inputs are read
+      urmax = fmax(urmax, fabs(ur));
+      upmax = fmax(upmax, fabs(up));
+    }
   }
   __syncthreads();
   {
@@ -898,85 +904,94 @@ cudaError_t launch_gemm(const GemmArgs& g, cudaStream_t s) {
 // IMEX right-hand sides (rhs_construct_temp / _vort / _uphi_bar,
 // src/rhs_create.F90:24-385), one thread per (r, m, b).
 // ---------------------------------------------------------------------------
+// The FP64 pipe bounds this kernel (~35 FP64 instructions per element
+// against ~20 bytes of HBM traffic per instruction's worth of time), so the
+// weights are folded once per thread (c_exp = dt w_exp) and every sum is a
+// chain of FMAs.
 __global__ void imex_rhs_kernel(RhsArgs a) {
-  const size_t total = (size_t)a.R * a.M * a.B;
-  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total;
-       e += (size_t)gridDim.x * blockDim.x) {
-    const int b = (int)(e % a.B);
-    const size_t rm = e / a.B;
-    const int m = (int)(rm % a.M);
-    const int r = (int)(rm / a.M);
-    const double ir = a.inv_r[r], ir2 = a.inv_r2[r];
-    const double dm = (double)m, mm = dm * dm;
-    const double dt = a.dt;
+  const unsigned B = (unsigned)a.B, M = (unsigned)a.M;
+  const size_t total = (size_t)a.R * M * B;
+  const double dt = a.dt;
+  double c_exp[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) c_exp[i] = dt * a.w_exp[i];
+  const double c_cn = (1.0 - a.w_imp[0]) * dt;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+    const size_t rm = e / B;
+    const unsigned b = (unsigned)(e - rm * B);
+    const unsigned r = (unsigned)(rm / M), m = (unsigned)(rm - (size_t)r * M);
+    const double ir = a.inv_r[r];
+    const double dm = (double)(int)m, dmir = dm * ir;
     // explicit (advective) term of T: i m r^-1 (uphi T) + d(ur T)/dr + r^-1 (ur T)
     {
       const double2 p = a.ntp[e], q = a.ntr[e], dq = a.dntr[e];
-      const double2 nt = make_double2(-dm * ir * p.y + dq.x + ir * q.x, dm * ir * p.x + dq.y + ir * q.y);
+      const double2 nt = make_double2(fma(-dmir, p.y, fma(ir, q.x, dq.x)), fma(dmir, p.x, fma(ir, q.y, dq.y)));
       a.nt_new[e] = nt;
       double2 rhs;
       if (a.scheme_cn) {
         const double2 T = a.th[0][e], L = a.lt[e];
-        const double c = (1.0 - a.w_imp[0]) * dt * a.inv_pr;
-        rhs = make_double2(T.x + c * (L.x - mm * ir2 * T.x), T.y + c * (L.y - mm * ir2 * T.y));
+        const double c = c_cn * a.inv_pr, k2 = dm * dm * a.inv_r2[r];
+        rhs = make_double2(fma(c, fma(-k2, T.x, L.x), T.x), fma(c, fma(-k2, T.y, L.y), T.y));
       } else {
-        rhs = make_double2(0.0, 0.0);
-        for (int i = 0; i < a.n_imp; ++i) {
+        const double2 h0 = a.th[0][e];
+        rhs = make_double2(a.w_imp[0] * h0.x, a.w_imp[0] * h0.y);
+        for (int i = 1; i < a.n_imp; ++i) {
           const double2 h = a.th[i][e];
-          rhs.x += a.w_imp[i] * h.x; rhs.y += a.w_imp[i] * h.y;
+          rhs.x = fma(a.w_imp[i], h.x, rhs.x); rhs.y = fma(a.w_imp[i], h.y, rhs.y);
         }
       }
-      for (int i = 0; i < a.n_exp; ++i) {
-        const double2 h = (i == 0) ? nt : a.nth[i][e];
-        rhs.x -= dt * (a.w_exp[i] * h.x); rhs.y -= dt * (a.w_exp[i] * h.y);
+      rhs.x = fma(-c_exp[0], nt.x, rhs.x); rhs.y = fma(-c_exp[0], nt.y, rhs.y);
+      for (int i = 1; i < a.n_exp; ++i) {
+        const double2 h = a.nth[i][e];
+        rhs.x = fma(-c_exp[i], h.x, rhs.x); rhs.y = fma(-c_exp[i], h.y, rhs.y);
       }
       if (r == 0) rhs = make_double2(m == 0 ? 1.0 : 0.0, 0.0);
-      if (r == a.R - 1) rhs = make_double2(0.0, 0.0);
+      if (r == (unsigned)a.R - 1) rhs = make_double2(0.0, 0.0);
       a.rhs_t[e] = rhs;
     }
     if (m > 0) {
       const double2 p = a.nwp[e], q = a.nwr[e], dq = a.dnwr[e];
-      const double2 nw = make_double2(-dm * ir * p.y + dq.x + ir * q.x, dm * ir * p.x + dq.y + ir * q.y);
+      const double2 nw = make_double2(fma(-dmir, p.y, fma(ir, q.x, dq.x)), fma(dmir, p.x, fma(ir, q.y, dq.y)));
       a.nw_new[e] = nw;
       double2 rhs;
       if (a.scheme_cn) {
         const double2 W = a.wh[0][e], L = a.lw[e], To = a.th[0][e];
-        const double c = (1.0 - a.w_imp[0]) * dt;
-        const double bc = a.ra_pr[b] * dt * 0.5 * dm * ir;  // old-T half of the CN buoyancy
-        rhs = make_double2(W.x + c * (L.x - mm * ir2 * W.x) + bc * To.y,
-                           W.y + c * (L.y - mm * ir2 * W.y) - bc * To.x);
+        const double k2 = dm * dm * a.inv_r2[r];
+        const double bc = a.ra_pr[b] * dt * 0.5 * dmir;  // old-T half of the CN buoyancy
+        rhs = make_double2(fma(bc, To.y, fma(c_cn, fma(-k2, W.x, L.x), W.x)),
+                           fma(-bc, To.x, fma(c_cn, fma(-k2, W.y, L.y), W.y)));
       } else {
-        rhs = make_double2(0.0, 0.0);
-        for (int i = 0; i < a.n_imp; ++i) {
+        const double2 h0 = a.wh[0][e];
+        rhs = make_double2(a.w_imp[0] * h0.x, a.w_imp[0] * h0.y);
+        for (int i = 1; i < a.n_imp; ++i) {
           const double2 h = a.wh[i][e];
-          rhs.x += a.w_imp[i] * h.x; rhs.y += a.w_imp[i] * h.y;
+          rhs.x = fma(a.w_imp[i], h.x, rhs.x); rhs.y = fma(a.w_imp[i], h.y, rhs.y);
         }
       }
-      for (int i = 0; i < a.n_exp; ++i) {
-        const double2 h = (i == 0) ? nw : a.nwh[i][e];
-        rhs.x -= dt * (a.w_exp[i] * h.x); rhs.y -= dt * (a.w_exp[i] * h.y);
+      rhs.x = fma(-c_exp[0], nw.x, rhs.x); rhs.y = fma(-c_exp[0], nw.y, rhs.y);
+      for (int i = 1; i < a.n_exp; ++i) {
+        const double2 h = a.nwh[i][e];
+        rhs.x = fma(-c_exp[i], h.x, rhs.x); rhs.y = fma(-c_exp[i], h.y, rhs.y);
       }
-      if (r == 0 || r == a.R - 1) rhs = make_double2(0.0, 0.0);
+      if (r == 0 || r == (unsigned)a.R - 1) rhs = make_double2(0.0, 0.0);
       a.rhs_w[e] = rhs;
     } else {
       // mean azimuthal flow: rhs_construct_uphi_bar
-      const size_t rb = (size_t)r * a.B + b;
+      const size_t rb = (size_t)r * B + b;
       const double urom = a.nwr[e].x;  // mode-0 coefficient of ur*omg = its azimuthal mean
       a.urom_new[rb] = urom;
       double rhs;
       if (a.scheme_cn) {
         const double u = a.ubh[0][rb];
         const double lu = a.lu0[rb].x;
-        rhs = u + (1.0 - a.w_imp[0]) * dt * (lu - ir2 * u);
+        rhs = fma(c_cn, fma(-a.inv_r2[r], u, lu), u);
       } else {
-        rhs = 0.0;
-        for (int i = 0; i < a.n_imp; ++i) rhs += a.w_imp[i] * a.ubh[i][rb];
+        rhs = a.w_imp[0] * a.ubh[0][rb];
+        for (int i = 1; i < a.n_imp; ++i) rhs = fma(a.w_imp[i], a.ubh[i][rb], rhs);
       }
-      for (int i = 0; i < a.n_exp; ++i) {
-        const double h = (i == 0) ? urom : a.uromh[i][rb];
-        rhs -= dt * (a.w_exp[i] * h);
-      }
-      if (r == 0 || r == a.R - 1) rhs = 0.0;
+      rhs = fma(-c_exp[0], urom, rhs);
+      for (int i = 1; i < a.n_exp; ++i) rhs = fma(-c_exp[i], a.uromh[i][rb], rhs);
+      if (r == 0 || r == (unsigned)a.R - 1) rhs = 0.0;
       a.rhs_w[e] = make_double2(rhs, 0.0);
     }
   }

@@ -169,13 +169,16 @@ __device__ __forceinline__ void ldsm_x2t(unsigned (&r)[2], const void* p) {
 }  // namespace
 
 // Tiled slice GEMM.  Block: MT row tiles (16 rows) x NQ column groups (16
-// columns), one warp per (row tile, column group), K in chunks of 16 staged
-// in shared memory by cp.async two chunks deep (slices of A and X for all
-// kOzS slices of the chunk); fragments by ldmatrix from padded rows (48 and
-// NQ*32+16 bytes: conflict-free).  Per chunk a warp does the 55 slice-pair
-// products s + t <= kOzD on its two 16x8 tiles.
-template <int MT, int NQ>
-__global__ void __launch_bounds__(32 * MT * NQ) oz_mma_kernel(GemmArgs q) {
+// columns), each (row tile, column group) taken by 2 / NT warps of NT 16x8
+// tiles each; K in chunks of 16 staged in shared memory by cp.async two
+// chunks deep (slices of A and X for all kOzS slices of the chunk);
+// fragments by ldmatrix from padded rows (48 and NQ*32+16 bytes:
+// conflict-free).  Per chunk a warp does the 55 slice-pair products
+// s + t <= kOzD on each of its tiles.  NT = 1 halves the accumulator
+// registers (10 diagonals x 4 per tile), so twice the warps fit on an SM.
+template <int MT, int NQ, int NT, int MINB>
+__global__ void __launch_bounds__(32 * MT * NQ * (2 / NT), MINB) oz_mma_kernel(GemmArgs q) {
+  constexpr int SPLIT = 2 / NT;  // warps per (row tile, column group)
   constexpr int AROW = 24, XROW = NQ * 16 + 8;           // padded row lengths (bf16)
   constexpr int ASTAGE = kOzS * MT * 16 * AROW, XSTAGE = kOzS * 16 * XROW;
   extern __shared__ __align__(16) uint16_t oz_panel[];   // [2][ASTAGE + XSTAGE]
@@ -185,7 +188,7 @@ __global__ void __launch_bounds__(32 * MT * NQ) oz_mma_kernel(GemmArgs q) {
   const size_t aslice = (size_t)q.oz_rowsP * q.oz_KP;
   const uint16_t* Xz = q.oz_xs + (size_t)z * kOzS * q.oz_KP * q.oz_Np + col0;
   const size_t xslice = (size_t)q.oz_KP * q.oz_Np;
-  const int tid = threadIdx.x, nthr = 32 * MT * NQ;
+  const int tid = threadIdx.x, nthr = 32 * MT * NQ * SPLIT;
   auto stage = [&](int k0, int buf) {
     uint16_t* Ap = oz_panel + buf * (ASTAGE + XSTAGE);
     uint16_t* Xp = Ap + ASTAGE;
@@ -200,12 +203,12 @@ __global__ void __launch_bounds__(32 * MT * NQ) oz_mma_kernel(GemmArgs q) {
     cp_commit();
   };
   const int warp = tid >> 5, lane = tid & 31, gid = lane >> 2, tig = lane & 3;
-  const int wm = warp % MT, wn = warp / MT;
-  float acc[kOzD + 1][2][4];
+  const int wm = warp % MT, wr = warp / MT, wn = wr / SPLIT, nt0 = (wr % SPLIT) * NT;
+  float acc[kOzD + 1][NT][4];
 #pragma unroll
   for (int d = 0; d <= kOzD; ++d)
 #pragma unroll
-    for (int nt = 0; nt < 2; ++nt)
+    for (int nt = 0; nt < NT; ++nt)
 #pragma unroll
       for (int i = 0; i < 4; ++i) acc[d][nt][i] = 0.f;
   const int nk = q.oz_KP / 16;
@@ -220,12 +223,12 @@ __global__ void __launch_bounds__(32 * MT * NQ) oz_mma_kernel(GemmArgs q) {
     __syncthreads();
     const uint16_t* Ap = oz_panel + (kc & 1) * (ASTAGE + XSTAGE);
     const uint16_t* Xp = Ap + ASTAGE;
-    unsigned bf[kOzS][2][2];
+    unsigned bf[kOzS][NT][2];
 #pragma unroll
     for (int t = 0; t < kOzS; ++t)
 #pragma unroll
-      for (int nt = 0; nt < 2; ++nt)
-        ldsm_x2t(bf[t][nt], Xp + (t * 16 + (lane & 15)) * XROW + wn * 16 + nt * 8);
+      for (int nt = 0; nt < NT; ++nt)
+        ldsm_x2t(bf[t][nt], Xp + (t * 16 + (lane & 15)) * XROW + wn * 16 + (nt0 + nt) * 8);
 #pragma unroll
     for (int sl = 0; sl < kOzS; ++sl) {
       unsigned af[4];
@@ -233,7 +236,7 @@ __global__ void __launch_bounds__(32 * MT * NQ) oz_mma_kernel(GemmArgs q) {
 #pragma unroll
       for (int t = 0; t < kOzS && sl + t <= kOzD; ++t)
 #pragma unroll
-        for (int nt = 0; nt < 2; ++nt) mma_bf16(acc[sl + t][nt], af[0], af[1], af[2], af[3], bf[t][nt][0], bf[t][nt][1]);
+        for (int nt = 0; nt < NT; ++nt) mma_bf16(acc[sl + t][nt], af[0], af[1], af[2], af[3], bf[t][nt][0], bf[t][nt][1]);
     }
     __syncthreads();  // every warp is done with this buffer before it is refilled
   }
@@ -242,8 +245,8 @@ __global__ void __launch_bounds__(32 * MT * NQ) oz_mma_kernel(GemmArgs q) {
   const int* cex = q.oz_cexp + (size_t)z * q.oz_Np;
   double* Y = q.Y + (size_t)z * q.sY;
 #pragma unroll
-  for (int nt = 0; nt < 2; ++nt) {
-    const int n = col0 + wn * 16 + nt * 8 + tig * 2;
+  for (int nt = 0; nt < NT; ++nt) {
+    const int n = col0 + wn * 16 + (nt0 + nt) * 8 + tig * 2;
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
       const int r = row0b + wm * 16 + gid + 8 * h;
@@ -260,7 +263,8 @@ __global__ void __launch_bounds__(32 * MT * NQ) oz_mma_kernel(GemmArgs q) {
         for (int d = 5; d <= kOzD; ++d) L = L * 64 + (long long)__float2int_rn(acc[d][nt][i]);
         const int fb = cex[n + j];
         const double y = fma((double)L, 0x1p-30, (double)H);
-        out[j] = (fb > 0 && (H != 0 || L != 0)) ? q.alpha * scale2(y, er + (fb - 1022) - 36) : 0.0;
+        out[j] = (fb > 0 && (H != 0 || L != 0)) ? scale2(y, er + (fb - 1022) - 36) : 0.0;
+        if (q.alpha != 1.0) out[j] *= q.alpha;
       }
       double* yp = Y + (size_t)r * q.ldy + n;
       if (n + 1 < q.N) {
@@ -277,20 +281,20 @@ __global__ void __launch_bounds__(32 * MT * NQ) oz_mma_kernel(GemmArgs q) {
   }
 }
 
-template <int MT, int NQ>
+template <int MT, int NQ, int NT = 2, int MINB = 1>
 static cudaError_t launch_oz_mt(const GemmArgs& g, cudaStream_t s) {
   constexpr size_t smem = 2 * ((size_t)kOzS * MT * 16 * 24 + (size_t)kOzS * 16 * (NQ * 16 + 8)) * sizeof(uint16_t);
   static bool opted[64] = {false};
   int dev = 0;
   cudaGetDevice(&dev);
   if (dev >= 0 && dev < 64 && !opted[dev]) {
-    const cudaError_t e = cudaFuncSetAttribute(oz_mma_kernel<MT, NQ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    const cudaError_t e = cudaFuncSetAttribute(oz_mma_kernel<MT, NQ, NT, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                (int)smem);
     if (e != cudaSuccess) return e;
     opted[dev] = true;
   }
   dim3 grid((g.N + NQ * 16 - 1) / (NQ * 16), (g.rows + MT * 16 - 1) / (MT * 16), g.batch);
-  oz_mma_kernel<MT, NQ><<<grid, 32 * MT * NQ, smem, s>>>(g);
+  oz_mma_kernel<MT, NQ, NT, MINB><<<grid, 32 * MT * NQ * (2 / NT), smem, s>>>(g);
   return cudaGetLastError();
 }
 
@@ -303,10 +307,10 @@ cudaError_t launch_oz_gemm(const GemmArgs& g, cudaStream_t s) {
   const int rt = (g.rows + 15) / 16;
   if (rt >= 5 && rt <= 8) {
     switch (rt) {
-      case 5: return launch_oz_mt<5, 1>(g, s);
-      case 6: return launch_oz_mt<6, 1>(g, s);
-      case 7: return launch_oz_mt<7, 1>(g, s);
-      default: return launch_oz_mt<8, 1>(g, s);
+      case 5: return launch_oz_mt<5, 1, 1, 2>(g, s);
+      case 6: return launch_oz_mt<6, 1, 1, 1>(g, s);
+      case 7: return launch_oz_mt<7, 1, 1, 1>(g, s);
+      default: return launch_oz_mt<8, 1, 1, 1>(g, s);
     }
   }
   const int groups = (rt + 3) / 4, mt = (rt + groups - 1) / groups;
