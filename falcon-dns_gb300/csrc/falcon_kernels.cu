@@ -13,6 +13,7 @@
 #include <unordered_map>
 
 #include "falcon_internal.h"
+#include "falcon_slices.cuh"
 
 namespace falcon {
 
@@ -215,6 +216,9 @@ __device__ void generic_stage(double2* A, double2* Bf, int P, int p, int m, int 
   }
 }
 
+template <int p>
+__device__ void dft_mma_stage(double2* A, double2* Bf, int P, int m, int lane, int warp, int nw);
+
 // MAXP bounds the radices compiled into one kernel instance, so a plan
 // with small radices is not held to the register budget of radix 31.
 template <int MAXP>
@@ -231,6 +235,14 @@ __device__ __forceinline__ void run_stage(int p, bool dif, bool twid, double2* A
       return;                                                                \
     }                                                                        \
     break;
+  if constexpr (MAXP == 17) {  // plans with a prime above 17 keep the FMA butterflies
+    if (!twid && (p == 11 || p == 13 || p == 17)) {
+      if (p == 11) dft_mma_stage<11>(A, Bf, P, m, lane, 0, 1);
+      else if (p == 13) dft_mma_stage<13>(A, Bf, P, m, lane, 0, 1);
+      else dft_mma_stage<17>(A, Bf, P, m, lane, 0, 1);
+      return;
+    }
+  }
   switch (p) {
     FALCON_CASE2(2) FALCON_CASE2(3) FALCON_CASE2(4) FALCON_CASE2(5) FALCON_CASE2(7)
     FALCON_CASE1(11) FALCON_CASE1(13) FALCON_CASE1(17)
@@ -324,6 +336,144 @@ __device__ void fft_stage_split(double2* A, double2* Bf, int P, int m, int tid, 
   }
 }
 
+// Odd-prime stage (p = 11, 13, 17, so h = (p - 1)/2 <= 8) of a prime-factor
+// plan on the bf16 tensor cores, with the exact integer slicing of the
+// operator GEMMs (falcon_ozaki.cu).  In the symmetric form of dft_odd_store
+// the butterfly's FP64 work is the 2h real sums A_j = sum_q a_q cos(2 pi jq/p)
+// and B_j = sum_q b_q sin(2 pi jq/p), a_q = v_q + v_{p-q}, b_q = v_q - v_{p-q}:
+// per component, one product of the block-diagonal [C 0; 0 S] (rows j; K =
+// the h values a_q, then the h values b_q) with a column.  One m16n8k16 MMA
+// per slice pair takes 8 columns, 4 butterflies x (re, im).  The
+// coefficient rows are scaled by their own maxima and each column by its
+// own, and every FP32 sum is exact, so a butterfly's outputs depend only on
+// its inputs: any tiling (warp or block form) gives the same bits.  Lane
+// (g, t) of a tile forms a_q, b_q for q = 2t + 1, 2t + 2 of column g and
+// receives A_{g+1}, B_{g+1} of butterfly t, re and im, from which it stores
+// y_j = A_j - i B_j and y_{p-j} = A_j + i B_j; the y_0 sums are FP64.
+// FP64 instructions per tile and lane: ~18, against ~42 for the same 4
+// butterflies in dft_odd_store.  Tiles over both buffers go to warps
+// warp, warp + nw, ...; the caller synchronises before (inputs complete)
+// and after (outputs stored).
+template <int p>
+__device__ void dft_mma_stage(double2* A, double2* Bf, int P, int m, int lane, int warp, int nw) {
+  constexpr int h = (p - 1) / 2;
+  static_assert(h <= 8, "the block-diagonal form holds h <= 8");
+  constexpr unsigned FULL = 0xffffffffu;
+  const int gid = lane >> 2, tig = lane & 3;
+  const int nb = P / p, mp = m * p, nbt = 2 * nb, ntile = (nbt + 3) / 4;
+  const float inv_m = 1.0f / (float)m;
+  const int q1 = 2 * tig + 1, q2 = 2 * tig + 2;  // K rows 2t, 2t + 1 (a) and 2t + 8, 2t + 9 (b)
+  const bool has1 = q1 <= h, has2 = q2 <= h;
+  // coefficient fragments: a0 = C(row g; q1, q2), a3 = S(row g; q1, q2), j = g + 1
+  uint32_t fc[kOzS], fs[kOzS];
+  int erc, ers;
+  {
+    const int j = gid + 1;
+    double c1 = 0.0, c2 = 0.0, s1 = 0.0, s2 = 0.0;
+    if (j <= h) {
+      if (has1) { c1 = DftTab<p>::c((j * q1) % p); s1 = DftTab<p>::s((j * q1) % p); }
+      if (has2) { c2 = DftTab<p>::c((j * q2) % p); s2 = DftTab<p>::s((j * q2) % p); }
+    }
+    int mc = max(biased_exp(c1), biased_exp(c2)), ms = max(biased_exp(s1), biased_exp(s2));
+    mc = max(mc, __shfl_xor_sync(FULL, mc, 1));
+    mc = max(mc, __shfl_xor_sync(FULL, mc, 2));
+    ms = max(ms, __shfl_xor_sync(FULL, ms, 1));
+    ms = max(ms, __shfl_xor_sync(FULL, ms, 2));
+    erc = mc - 1022;
+    ers = ms - 1022;
+    const unsigned long long tc1 = oz_mag(c1, erc), tc2 = oz_mag(c2, erc), ts1 = oz_mag(s1, ers),
+                             ts2 = oz_mag(s2, ers);
+#pragma unroll
+    for (int sl = 0; sl < kOzS; ++sl) {
+      fc[sl] = oz_slice_bits(tc1, c1 < 0.0, sl) | (oz_slice_bits(tc2, c2 < 0.0, sl) << 16);
+      fs[sl] = oz_slice_bits(ts1, s1 < 0.0, sl) | (oz_slice_bits(ts2, s2 < 0.0, sl) << 16);
+    }
+  }
+  for (int tile = warp; tile < ntile; tile += nw) {
+    // column g: butterfly bi (over both buffers), component g & 1
+    const int bi = tile * 4 + (gid >> 1), comp = gid & 1;
+    double av1 = 0.0, av2 = 0.0, bv1 = 0.0, bv2 = 0.0, v0c = 0.0;
+    double* pi = nullptr;
+    if (bi < nbt) {
+      const int sel = bi >= nb, t = bi - sel * nb;
+      const int g = (int)(((float)t + 0.5f) * inv_m);
+      pi = reinterpret_cast<double*>((sel ? Bf : A) + g * mp + (t - g * m)) + comp;
+      if (has1) {
+        const double x = pi[2 * q1 * m], y = pi[2 * (p - q1) * m];
+        av1 = x + y; bv1 = x - y;
+      }
+      if (has2) {
+        const double x = pi[2 * q2 * m], y = pi[2 * (p - q2) * m];
+        av2 = x + y; bv2 = x - y;
+      }
+      v0c = pi[0];
+    }
+    // outputs of this lane: butterfly bo, both components
+    const int bo = tile * 4 + tig;
+    double2* po = nullptr;
+    double2 v0o = make_double2(0.0, 0.0);
+    if (bo < nbt) {
+      const int sel = bo >= nb, t = bo - sel * nb;
+      const int g = (int)(((float)t + 0.5f) * inv_m);
+      po = (sel ? Bf : A) + g * mp + (t - g * m);
+      v0o = po[0];
+    }
+    // y_0 = v_0 + sum_q a_q per component (the same sum on the four lanes)
+    double ys = av1 + av2;
+    ys += __shfl_xor_sync(FULL, ys, 1);
+    ys += __shfl_xor_sync(FULL, ys, 2);
+    // column exponent and slices of a, b
+    int fb = max(max(biased_exp(av1), biased_exp(av2)), max(biased_exp(bv1), biased_exp(bv2)));
+    fb = max(fb, __shfl_xor_sync(FULL, fb, 1));
+    fb = max(fb, __shfl_xor_sync(FULL, fb, 2));
+    const int ec = fb - 1022;
+    uint32_t fa[kOzS], fbq[kOzS];
+    {
+      const unsigned long long ta1 = oz_mag(av1, ec), ta2 = oz_mag(av2, ec), tb1 = oz_mag(bv1, ec),
+                               tb2 = oz_mag(bv2, ec);
+      const bool na1 = __double_as_longlong(av1) < 0, na2 = __double_as_longlong(av2) < 0;
+      const bool nb1 = __double_as_longlong(bv1) < 0, nb2 = __double_as_longlong(bv2) < 0;
+#pragma unroll
+      for (int sl = 0; sl < kOzS; ++sl) {
+        fa[sl] = oz_slice_bits(ta1, na1, sl) | (oz_slice_bits(ta2, na2, sl) << 16);
+        fbq[sl] = oz_slice_bits(tb1, nb1, sl) | (oz_slice_bits(tb2, nb2, sl) << 16);
+      }
+    }
+    __syncwarp();  // every load of the tile precedes its stores
+    if (tig == 0 && pi) pi[0] = v0c + ys;
+    float acc[kOzD + 1][4];
+#pragma unroll
+    for (int d = 0; d <= kOzD; ++d)
+#pragma unroll
+      for (int i = 0; i < 4; ++i) acc[d][i] = 0.f;
+#pragma unroll
+    for (int sl = 0; sl < kOzS; ++sl)
+#pragma unroll
+      for (int t = 0; t < kOzS && sl + t <= kOzD; ++t) mma_bf16(acc[sl + t], fc[sl], 0u, 0u, fs[sl], fa[t], fbq[t]);
+    // column exponents of this lane's output columns 2t (re) and 2t + 1 (im)
+    const int fre = __shfl_sync(FULL, fb, 8 * tig), fim = __shfl_sync(FULL, fb, 8 * tig + 4);
+    if (gid < h && po) {
+      double o[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const int f = (i & 1) ? fim : fre;
+        long long H = 0, L = 0;
+#pragma unroll
+        for (int d = 0; d <= 4; ++d) H = H * 64 + oz_f32_int(acc[d][i]);
+#pragma unroll
+        for (int d = 5; d <= kOzD; ++d) L = L * 64 + oz_f32_int(acc[d][i]);
+        const int k = (i < 2 ? erc : ers) + (f - 1022) - 36;
+        o[i] = oz_i64_scaled(H, k) + oz_i64_scaled(L, k - 30);
+        if (f == 2047) o[i] = __longlong_as_double(0x7ff8000000000000LL);  // Inf or NaN in the column
+      }
+      const double ar = o[0] + v0o.x, ai = o[1] + v0o.y;
+      const int j = gid + 1;
+      po[j * m] = make_double2(ar + o[3], ai - o[2]);
+      po[(p - j) * m] = make_double2(ar - o[3], ai + o[2]);
+    }
+  }
+}
+
 // One stage of the block-per-line form: large odd primes of a prime-factor
 // plan through fft_stage_split over the whole block, the rest per buffer
 // half (run_stage1).  Called by every thread of the block.
@@ -331,6 +481,15 @@ template <int MAXP>
 __device__ __forceinline__ void run_stage_block(int p, bool dif, bool twid, double2* A, double2* Bf, double2* mine,
                                                 int P, int m, int stride, const double2* tw, int tid, int nt, int hl,
                                                 int nl) {
+  if constexpr (MAXP == 17) {  // plans with a prime above 17 keep the FMA butterflies
+    if (!twid && (p == 11 || p == 13 || p == 17)) {
+      if (p == 11) dft_mma_stage<11>(A, Bf, P, m, tid & 31, tid >> 5, nt >> 5);
+      else if (p == 13) dft_mma_stage<13>(A, Bf, P, m, tid & 31, tid >> 5, nt >> 5);
+      else dft_mma_stage<17>(A, Bf, P, m, tid & 31, tid >> 5, nt >> 5);
+      __syncthreads();
+      return;
+    }
+  }
   if (!twid) {
     switch (p) {
 #define FALCON_SPLIT(q, g)                                  \

@@ -27,40 +27,11 @@
 #include <stdint.h>
 
 #include "falcon_internal.h"
+#include "falcon_slices.cuh"
 
 namespace falcon {
 
 namespace {
-
-__device__ __forceinline__ int biased_exp(double a) {
-  return (int)((__double_as_longlong(a) >> 52) & 0x7ff);
-}
-
-// |a| * 2^(60 - e) truncated to an integer (< 2^60 when |a| < 2^e); zero and
-// subnormal inputs give 0.
-__device__ __forceinline__ unsigned long long oz_mag(double a, int e) {
-  const long long bits = __double_as_longlong(a);
-  const int eb = (int)((bits >> 52) & 0x7ff);
-  if (eb == 0) return 0ull;
-  const unsigned long long m = (unsigned long long)(bits & 0xfffffffffffffLL) | (1ull << 52);
-  const int sh = eb - 1015 - e;  // a = m 2^(eb-1075): T = m 2^(eb - 1075 + 60 - e)
-  if (sh >= 0) return m << sh;   // sh <= 7 because |a| < 2^e
-  if (sh <= -64) return 0ull;
-  return m >> (-sh);
-}
-
-__device__ __forceinline__ uint16_t bf16_bits_of_int(int q) {
-  return __bfloat16_as_ushort(__float2bfloat16_rn((float)q));
-}
-
-__device__ __forceinline__ void mma_bf16(float (&c)[4], unsigned a0, unsigned a1, unsigned a2, unsigned a3,
-                                         unsigned b0, unsigned b1) {
-  asm volatile(
-      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-      "{%0,%1,%2,%3};\n"
-      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
-      : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
-}
 
 // 2^k as a double for the normal range, else a scaled fallback
 __device__ __forceinline__ double scale2(double y, int k) {

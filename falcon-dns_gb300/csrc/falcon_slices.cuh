@@ -1,0 +1,69 @@
+// Device helpers shared by the integer-slice products (operator GEMMs in
+// falcon_ozaki.cu, odd-prime DFT stages in falcon_kernels.cu): an FP64
+// value cut into signed 6-bit integers relative to a power of two that
+// bounds its row or column, bf16 encoding of the slices, and the bf16
+// mma.sync used on them.
+#pragma once
+#include <cuda_bf16.h>
+#include <stdint.h>
+
+#include "falcon_internal.h"
+
+namespace falcon {
+namespace {
+
+__device__ __forceinline__ int biased_exp(double a) {
+  return (int)((__double_as_longlong(a) >> 52) & 0x7ff);
+}
+
+// |a| * 2^(60 - e) truncated to an integer (< 2^60 when |a| < 2^e); zero and
+// subnormal inputs give 0.
+__device__ __forceinline__ unsigned long long oz_mag(double a, int e) {
+  const long long bits = __double_as_longlong(a);
+  const int eb = (int)((bits >> 52) & 0x7ff);
+  if (eb == 0) return 0ull;
+  const unsigned long long m = (unsigned long long)(bits & 0xfffffffffffffLL) | (1ull << 52);
+  const int sh = eb - 1015 - e;  // a = m 2^(eb-1075): T = m 2^(eb - 1075 + 60 - e)
+  if (sh >= 0) return m << sh;   // sh <= 7 because |a| < 2^e
+  if (sh <= -64) return 0ull;
+  return m >> (-sh);
+}
+
+__device__ __forceinline__ uint16_t bf16_bits_of_int(int q) {
+  return __bfloat16_as_ushort(__float2bfloat16_rn((float)q));
+}
+
+// Slice s (0 = most significant) of a value cut by oz_mag, with its sign.
+__device__ __forceinline__ uint32_t oz_slice_bits(unsigned long long T, bool neg, int s) {
+  const int q = (int)((T >> (kOzW * (kOzS - 1 - s))) & ((1u << kOzW) - 1));
+  return bf16_bits_of_int(neg ? -q : q);
+}
+
+// An exact FP32 integer sum (|x| < 2^22) as an int: x + 1.5 2^23 puts the
+// integer in the low mantissa bits.
+__device__ __forceinline__ int oz_f32_int(float x) { return __float_as_int(x + 12582912.0f) - 0x4B400000; }
+
+// v 2^k for |v| < 2^53 built from its bits (integer instructions only:
+// no FP64 pipe), when the result is a normal number; else from ldexp.
+__device__ __forceinline__ double oz_i64_scaled(long long v, int k) {
+  if (v == 0) return 0.0;
+  const unsigned long long sgn = (unsigned long long)v & (1ull << 63);
+  const unsigned long long a = v < 0 ? 0ull - (unsigned long long)v : (unsigned long long)v;
+  const int lz = __clzll((long long)a);
+  const long long ex = (long long)(63 - lz) + 1023 + k;
+  if (ex < 1 || ex > 2046) return ldexp((double)v, k);
+  const unsigned long long frac = ((a << lz) << 1) >> 12;
+  return __longlong_as_double((long long)(sgn | ((unsigned long long)ex << 52) | frac));
+}
+
+__device__ __forceinline__ void mma_bf16(float (&c)[4], unsigned a0, unsigned a1, unsigned a2, unsigned a3,
+                                         unsigned b0, unsigned b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
+}  // namespace
+}  // namespace falcon
