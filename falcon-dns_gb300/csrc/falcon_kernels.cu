@@ -337,23 +337,25 @@ __device__ void fft_stage_split(double2* A, double2* Bf, int P, int m, int tid, 
 }
 
 // Odd-prime stage (p = 11, 13, 17, so h = (p - 1)/2 <= 8) of a prime-factor
-// plan on the bf16 tensor cores, with the exact integer slicing of the
-// operator GEMMs (falcon_ozaki.cu).  In the symmetric form of dft_odd_store
-// the butterfly's FP64 work is the 2h real sums A_j = sum_q a_q cos(2 pi jq/p)
-// and B_j = sum_q b_q sin(2 pi jq/p), a_q = v_q + v_{p-q}, b_q = v_q - v_{p-q}:
-// per component, one product of the block-diagonal [C 0; 0 S] (rows j; K =
-// the h values a_q, then the h values b_q) with a column.  One m16n8k16 MMA
-// per slice pair takes 8 columns, 4 butterflies x (re, im).  The
-// coefficient rows are scaled by their own maxima and each column by its
-// own, and every FP32 sum is exact, so a butterfly's outputs depend only on
-// its inputs: any tiling (warp or block form) gives the same bits.  Lane
-// (g, t) of a tile forms a_q, b_q for q = 2t + 1, 2t + 2 of column g and
-// receives A_{g+1}, B_{g+1} of butterfly t, re and im, from which it stores
-// y_j = A_j - i B_j and y_{p-j} = A_j + i B_j; the y_0 sums are FP64.
-// FP64 instructions per tile and lane: ~18, against ~42 for the same 4
-// butterflies in dft_odd_store.  Tiles over both buffers go to warps
-// warp, warp + nw, ...; the caller synchronises before (inputs complete)
-// and after (outputs stored).
+// plan on the fp16 tensor cores, by exact integer slicing.  In the
+// symmetric form of dft_odd_store the butterfly's FP64 work is the 2h real
+// sums A_j = sum_q a_q cos(2 pi jq/p) and B_j = sum_q b_q sin(2 pi jq/p),
+// a_q = v_q + v_{p-q}, b_q = v_q - v_{p-q}: per component, one product of
+// the block-diagonal [C 0; 0 S] (rows j; K = the h values a_q, then the h
+// values b_q) with a column.  One m16n8k16 MMA per slice pair takes 8
+// columns, 4 butterflies x (re, im).  Each operand is cut into kDftS = 7
+// signed 9-bit slices (63 bits; fp16 holds them exactly) relative to its
+// row's (coefficients) or column's (data) largest power of two, and the 28
+// pairs s + t <= 6 are summed in FP32: at most 8 products per output keep
+// every sum exact, and the dropped terms are below 2^-59 of the largest
+// product, so the outputs are the exact sums rounded once to FP64.  A butterfly's outputs depend only on its inputs, so any tiling
+// (warp or block form) gives the same bits.  Lane (g, t) of a tile forms
+// a_q, b_q for q = 2t + 1, 2t + 2 of column g and receives A_{g+1}, B_{g+1}
+// of butterfly t, re and im, from which it stores y_j = A_j - i B_j and
+// y_{p-j} = A_j + i B_j; the y_0 sums are FP64.  FP64 instructions per tile
+// and lane: ~18, against ~42 for the same 4 butterflies in dft_odd_store.
+// Tiles over both buffers go to warps warp, warp + nw, ...; the caller
+// synchronises before (inputs complete) and after (outputs stored).
 template <int p>
 __device__ void dft_mma_stage(double2* A, double2* Bf, int P, int m, int lane, int warp, int nw) {
   constexpr int h = (p - 1) / 2;
@@ -365,7 +367,7 @@ __device__ void dft_mma_stage(double2* A, double2* Bf, int P, int m, int lane, i
   const int q1 = 2 * tig + 1, q2 = 2 * tig + 2;  // K rows 2t, 2t + 1 (a) and 2t + 8, 2t + 9 (b)
   const bool has1 = q1 <= h, has2 = q2 <= h;
   // coefficient fragments: a0 = C(row g; q1, q2), a3 = S(row g; q1, q2), j = g + 1
-  uint32_t fc[kOzS], fs[kOzS];
+  uint32_t fc[kDftS], fs[kDftS];
   int erc, ers;
   {
     const int j = gid + 1;
@@ -381,12 +383,14 @@ __device__ void dft_mma_stage(double2* A, double2* Bf, int P, int m, int lane, i
     ms = max(ms, __shfl_xor_sync(FULL, ms, 2));
     erc = mc - 1022;
     ers = ms - 1022;
-    const unsigned long long tc1 = oz_mag(c1, erc), tc2 = oz_mag(c2, erc), ts1 = oz_mag(s1, ers),
-                             ts2 = oz_mag(s2, ers);
+    const unsigned long long tc1 = dft_mag(c1, erc), tc2 = dft_mag(c2, erc), ts1 = dft_mag(s1, ers),
+                             ts2 = dft_mag(s2, ers);
+    const uint32_t sc = (__double_as_longlong(c1) < 0 ? 0x8000u : 0u) | (__double_as_longlong(c2) < 0 ? 0x80000000u : 0u);
+    const uint32_t ss = (__double_as_longlong(s1) < 0 ? 0x8000u : 0u) | (__double_as_longlong(s2) < 0 ? 0x80000000u : 0u);
 #pragma unroll
-    for (int sl = 0; sl < kOzS; ++sl) {
-      fc[sl] = oz_slice_bits(tc1, c1 < 0.0, sl) | (oz_slice_bits(tc2, c2 < 0.0, sl) << 16);
-      fs[sl] = oz_slice_bits(ts1, s1 < 0.0, sl) | (oz_slice_bits(ts2, s2 < 0.0, sl) << 16);
+    for (int sl = 0; sl < kDftS; ++sl) {
+      fc[sl] = dft_slice2(tc1, tc2, sc, sl);
+      fs[sl] = dft_slice2(ts1, ts2, ss, sl);
     }
   }
   for (int tile = warp; tile < ntile; tile += nw) {
@@ -427,29 +431,31 @@ __device__ void dft_mma_stage(double2* A, double2* Bf, int P, int m, int lane, i
     fb = max(fb, __shfl_xor_sync(FULL, fb, 1));
     fb = max(fb, __shfl_xor_sync(FULL, fb, 2));
     const int ec = fb - 1022;
-    uint32_t fa[kOzS], fbq[kOzS];
+    uint32_t fa[kDftS], fbq[kDftS];
     {
-      const unsigned long long ta1 = oz_mag(av1, ec), ta2 = oz_mag(av2, ec), tb1 = oz_mag(bv1, ec),
-                               tb2 = oz_mag(bv2, ec);
-      const bool na1 = __double_as_longlong(av1) < 0, na2 = __double_as_longlong(av2) < 0;
-      const bool nb1 = __double_as_longlong(bv1) < 0, nb2 = __double_as_longlong(bv2) < 0;
+      const unsigned long long ta1 = dft_mag(av1, ec), ta2 = dft_mag(av2, ec), tb1 = dft_mag(bv1, ec),
+                               tb2 = dft_mag(bv2, ec);
+      const uint32_t sa = (__double_as_longlong(av1) < 0 ? 0x8000u : 0u) |
+                          (__double_as_longlong(av2) < 0 ? 0x80000000u : 0u);
+      const uint32_t sb = (__double_as_longlong(bv1) < 0 ? 0x8000u : 0u) |
+                          (__double_as_longlong(bv2) < 0 ? 0x80000000u : 0u);
 #pragma unroll
-      for (int sl = 0; sl < kOzS; ++sl) {
-        fa[sl] = oz_slice_bits(ta1, na1, sl) | (oz_slice_bits(ta2, na2, sl) << 16);
-        fbq[sl] = oz_slice_bits(tb1, nb1, sl) | (oz_slice_bits(tb2, nb2, sl) << 16);
+      for (int sl = 0; sl < kDftS; ++sl) {
+        fa[sl] = dft_slice2(ta1, ta2, sa, sl);
+        fbq[sl] = dft_slice2(tb1, tb2, sb, sl);
       }
     }
     __syncwarp();  // every load of the tile precedes its stores
     if (tig == 0 && pi) pi[0] = v0c + ys;
-    float acc[kOzD + 1][4];
+    float acc[kDftD + 1][4];
 #pragma unroll
-    for (int d = 0; d <= kOzD; ++d)
+    for (int d = 0; d <= kDftD; ++d)
 #pragma unroll
       for (int i = 0; i < 4; ++i) acc[d][i] = 0.f;
 #pragma unroll
-    for (int sl = 0; sl < kOzS; ++sl)
+    for (int sl = 0; sl < kDftS; ++sl)
 #pragma unroll
-      for (int t = 0; t < kOzS && sl + t <= kOzD; ++t) mma_bf16(acc[sl + t], fc[sl], 0u, 0u, fs[sl], fa[t], fbq[t]);
+      for (int t = 0; t < kDftS && sl + t <= kDftD; ++t) mma_f16(acc[sl + t], fc[sl], 0u, 0u, fs[sl], fa[t], fbq[t]);
     // column exponents of this lane's output columns 2t (re) and 2t + 1 (im)
     const int fre = __shfl_sync(FULL, fb, 8 * tig), fim = __shfl_sync(FULL, fb, 8 * tig + 4);
     if (gid < h && po) {
@@ -457,13 +463,14 @@ __device__ void dft_mma_stage(double2* A, double2* Bf, int P, int m, int lane, i
 #pragma unroll
       for (int i = 0; i < 4; ++i) {
         const int f = (i & 1) ? fim : fre;
-        long long H = 0, L = 0;
-#pragma unroll
-        for (int d = 0; d <= 4; ++d) H = H * 64 + oz_f32_int(acc[d][i]);
-#pragma unroll
-        for (int d = 5; d <= kOzD; ++d) L = L * 64 + oz_f32_int(acc[d][i]);
+        // sum = 2^(e_row + e_col - 36) H + 2^(e_row + e_col - 72) L,
+        // H = sum_{d<=2} Q_d 512^(2-d), L = sum_{d=3..6} Q_d 512^(6-d), both exact in int64
+        const long long H = ((long long)__float2int_rn(acc[0][i]) << 18) + ((long long)__float2int_rn(acc[1][i]) << 9) +
+                            __float2int_rn(acc[2][i]);
+        const long long L = ((long long)__float2int_rn(acc[3][i]) << 27) + ((long long)__float2int_rn(acc[4][i]) << 18) +
+                            ((long long)__float2int_rn(acc[5][i]) << 9) + __float2int_rn(acc[6][i]);
         const int k = (i < 2 ? erc : ers) + (f - 1022) - 36;
-        o[i] = oz_i64_scaled(H, k) + oz_i64_scaled(L, k - 30);
+        o[i] = oz_i64_scaled(H, k) + oz_i64_scaled(L, k - 36);
         if (f == 2047) o[i] = __longlong_as_double(0x7ff8000000000000LL);  // Inf or NaN in the column
       }
       const double ar = o[0] + v0o.x, ai = o[1] + v0o.y;

@@ -5,6 +5,7 @@
 // mma.sync used on them.
 #pragma once
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <stdint.h>
 
 #include "falcon_internal.h"
@@ -54,6 +55,45 @@ __device__ __forceinline__ double oz_i64_scaled(long long v, int k) {
   if (ex < 1 || ex > 2046) return ldexp((double)v, k);
   const unsigned long long frac = ((a << lz) << 1) >> 12;
   return __longlong_as_double((long long)(sgn | ((unsigned long long)ex << 52) | frac));
+}
+
+// fp16 slices of 9 bits for short sums (the DFT butterflies: at most 8
+// products per output): kDftS slices of kDftW bits hold 63 bits of each
+// operand, and the pairs s + t <= kDftD keep every FP32 sum exact
+// (7 pairs x 8 products x 511^2 < 2^24) while the dropped pairs weigh less
+// than 2^-59 of the largest product.
+constexpr int kDftS = 7, kDftW = 9, kDftD = 6;
+
+// |a| * 2^(63 - e) truncated (< 2^63 when |a| < 2^e); zero and subnormal
+// inputs give 0.
+__device__ __forceinline__ unsigned long long dft_mag(double a, int e) {
+  const long long bits = __double_as_longlong(a);
+  const int eb = (int)((bits >> 52) & 0x7ff);
+  if (eb == 0) return 0ull;
+  const unsigned long long m = (unsigned long long)(bits & 0xfffffffffffffLL) | (1ull << 52);
+  const int sh = eb - 1012 - e;  // a = m 2^(eb-1075): T = m 2^(eb - 1075 + 63 - e), sh <= 10
+  if (sh >= 0) return m << sh;
+  if (sh <= -64) return 0ull;
+  return m >> (-sh);
+}
+
+// Slice s (0 = most significant) of two values as an fp16 pair: fp16(1536 +
+// q) has the bits 0x6600 + q for 0 <= q < 512, so q = fp16(0x6600 + q) -
+// 1536 exactly; the signs (bits 15 and 31 of sgn) are applied to the result.
+__device__ __forceinline__ uint32_t dft_slice2(unsigned long long tlo, unsigned long long thi, uint32_t sgn, int s) {
+  const int sh = kDftW * (kDftS - 1 - s);
+  const uint32_t biased = (((uint32_t)(tlo >> sh) & 511u) | (((uint32_t)(thi >> sh) & 511u) << 16)) + 0x66006600u;
+  const __half2 v = __hsub2(*reinterpret_cast<const __half2*>(&biased), __floats2half2_rn(1536.f, 1536.f));
+  return *reinterpret_cast<const uint32_t*>(&v) ^ sgn;
+}
+
+__device__ __forceinline__ void mma_f16(float (&c)[4], unsigned a0, unsigned a1, unsigned a2, unsigned a3,
+                                        unsigned b0, unsigned b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
 }
 
 __device__ __forceinline__ void mma_bf16(float (&c)[4], unsigned a0, unsigned a1, unsigned a2, unsigned a3,
