@@ -522,18 +522,29 @@ __device__ __forceinline__ void run_stage_block(int p, bool dif, bool twid, doub
 // two forward FFTs that return u_phi*T, u_r*T, u_phi*omega, u_r*omega
 // truncated to modes 0..Nm and divided by P.
 // ---------------------------------------------------------------------------
+// A prime-factor plan of radices <= 17 reads no twiddles (its butterflies
+// take their coefficients from constant memory), so its blocks carry only
+// the index table and the line buffers: 3 blocks of 4 lines fit an SM.
 template <int MAXP>
-__global__ void __launch_bounds__(128) nonlin_kernel(NonlinArgs a) {
+constexpr int nonlin_min_blocks() { return MAXP == 17 ? 3 : 1; }
+
+template <int MAXP>
+__global__ void __launch_bounds__(128, nonlin_min_blocks<MAXP>()) nonlin_kernel(NonlinArgs a) {
   extern __shared__ double2 smem[];
   const int P = a.plan.P;
+  const bool no_tw = MAXP == 17 && a.plan.pfa;
+  const int tw_len = no_tw ? 0 : P;
   double2* tw = smem;
-  int* pos = reinterpret_cast<int*>(smem + P);
+  int* pos = reinterpret_cast<int*>(smem + tw_len);
   const int pos_pad = (P + 3) / 4;  // ints rounded up to double2 units (16 B)
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nwarp = blockDim.x >> 5;
-  double2* bufA = smem + P + pos_pad + (size_t)warp * 2 * P;
+  double2* bufA = smem + tw_len + pos_pad + (size_t)warp * 2 * P;
   double2* bufB = bufA + P;
-  for (int i = threadIdx.x; i < P; i += blockDim.x) { tw[i] = a.tw[i]; pos[i] = a.pos[i]; }
+  for (int i = threadIdx.x; i < P; i += blockDim.x) {
+    if (!no_tw) tw[i] = a.tw[i];
+    pos[i] = a.pos[i];
+  }
   __syncthreads();
   const int nlines = a.R * a.B;
   const int line = blockIdx.x * nwarp + warp;
@@ -718,11 +729,11 @@ __global__ void __launch_bounds__(64 * S) nonlin_line_kernel(NonlinArgs a) {
   }
 }
 
-static int nonlin_warps(int P, int* smem_bytes) {
+static int nonlin_warps(int P, bool no_tw, int* smem_bytes) {
   int dev = 0, maxsm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-  const int fixed = (P + (P + 3) / 4) * 16;
+  const int fixed = ((no_tw ? 0 : P) + (P + 3) / 4) * 16;
   int w = 4;
   while (w > 1 && fixed + w * 2 * P * 16 > maxsm) --w;
   *smem_bytes = fixed + w * 2 * P * 16;
@@ -751,7 +762,7 @@ static cudaError_t launch_nonlin_t(const NonlinArgs& a, cudaStream_t s) {
   if (nlines <= nsm) return launch_nonlin_line<MAXP, 4>(a, s);
   if (nlines <= 2 * nsm) return launch_nonlin_line<MAXP, 2>(a, s);
   int smem = 0;
-  const int w = nonlin_warps(a.plan.P, &smem);
+  const int w = nonlin_warps(a.plan.P, MAXP == 17 && a.plan.pfa, &smem);
   cudaError_t e = cudaFuncSetAttribute(nonlin_kernel<MAXP>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return e;
   const int grid = (nlines + w - 1) / w;
