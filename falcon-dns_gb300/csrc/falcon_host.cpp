@@ -214,7 +214,7 @@ struct OpSet {
   struct Oz {
     const double* base = nullptr;
     long lda = 0, sA = 0;
-    int rows = 0, K = 0, nb = 0, rowsP = 0, KP = 0;
+    int rows = 0, K = 0, nb = 0, rowsP = 0, KP = 0, w = 6;
     uint16_t* s = nullptr;
     int* ex = nullptr;
   };
@@ -240,12 +240,13 @@ int add_oz(OpSet* ops, const double* base, int rows, int K, int nb, long sA) {
   o.base = base; o.lda = rows; o.sA = sA; o.rows = rows; o.K = K; o.nb = nb;
   o.rowsP = oz_rows_padded(rows);
   o.KP = ((K + 15) / 16) * 16;
-  const size_t ns = (size_t)nb * kOzS * o.rowsP * o.KP, ne = (size_t)nb * o.rowsP;
+  o.w = oz_width_for(o.KP);
+  const size_t ns = (size_t)nb * oz_slices(o.w) * o.rowsP * o.KP, ne = (size_t)nb * o.rowsP;
   CK(cudaMalloc(&o.s, ns * sizeof(uint16_t)));
   CK(cudaMalloc(&o.ex, ne * sizeof(int)));
   CK(cudaMemset(o.s, 0, ns * sizeof(uint16_t)));
   CK(cudaMemset(o.ex, 0, ne * sizeof(int)));
-  CK(launch_oz_slice_rows(base, rows, sA, rows, K, nb, o.s, o.ex, o.rowsP, o.KP, 0));
+  CK(launch_oz_slice_rows(base, rows, sA, rows, K, nb, o.s, o.ex, o.rowsP, o.KP, o.w, 0));
   ops->bytes += ns * sizeof(uint16_t) + ne * sizeof(int);
   ops->oz.push_back(o);
   return 0;
@@ -836,7 +837,7 @@ struct Group {
   uint16_t* oz_xs = nullptr;
   int* oz_cexp = nullptr;
   size_t oz_xs_cap = 0, oz_cexp_cap = 0;
-  struct { const double* X = nullptr; long ldx = 0, sX = 0; int K = 0, N = 0, batch = 0; bool valid = false; } oz_key;
+  struct { const double* X = nullptr; long ldx = 0, sX = 0; int K = 0, N = 0, batch = 0, w = 0; bool valid = false; } oz_key;
   double dt_array[4] = {0, 0, 0, 0};
   double dt_new = 0.0;
   double* umax = nullptr;
@@ -1075,9 +1076,10 @@ bool attach_oz(const OpSet* o, GemmArgs* q) {
     const long row0 = delta - z0 * z.sA;
     if (q->lda != z.lda || q->K != z.K || row0 >= z.lda || row0 + q->rows > z.rows) return false;
     if (q->batch > 1 && (q->sA != z.sA || z0 + q->batch > z.nb)) return false;
-    q->oz_s = z.s + (size_t)z0 * kOzS * z.rowsP * z.KP;
+    q->oz_s = z.s + (size_t)z0 * oz_slices(z.w) * z.rowsP * z.KP;
     q->oz_ex = z.ex + (size_t)z0 * z.rowsP;
-    q->oz_sz = (long)kOzS * z.rowsP * z.KP;
+    q->oz_sz = (long)oz_slices(z.w) * z.rowsP * z.KP;
+    q->oz_w = z.w;
     q->oz_rowsP = z.rowsP;
     q->oz_KP = z.KP;
     q->oz_row0 = (int)row0;
@@ -1105,19 +1107,21 @@ int gemm(Group* g, int cls, const GemmArgs& q0, bool reuse = false) {
   }
   if (ok) {
     const int KP = q.oz_KP, Np = (int)(((long)q.N + 31) / 32 * 32);
-    if ((size_t)kOzS * KP * Np * q.batch > g->oz_xs_cap || (size_t)Np * q.batch > g->oz_cexp_cap) {
+    if ((size_t)oz_slices(q.oz_w) * KP * Np * q.batch > g->oz_xs_cap || (size_t)Np * q.batch > g->oz_cexp_cap) {
       ok = false;  // beyond the scratch sized for this group: FMA tiles
       q.oz_s = nullptr;
     } else {
       auto& k = g->oz_key;
       const bool same = reuse && k.valid && k.X == q.X && k.ldx == q.ldx && k.sX == q.sX && k.K == q.K &&
-                        k.N == q.N && k.batch == q.batch;
+                        k.N == q.N && k.batch == q.batch && k.w == q.oz_w;
       if (!same) {
         int rc = launch(g, KC_ELEMENTWISE, 0.0, [&]() {
-          return launch_oz_slice_cols(q.X, q.ldx, q.sX, q.K, q.N, q.batch, g->oz_xs, g->oz_cexp, KP, Np, g->stream);
+          return launch_oz_slice_cols(q.X, q.ldx, q.sX, q.K, q.N, q.batch, g->oz_xs, g->oz_cexp, KP, Np, q.oz_w,
+                                      g->stream);
         });
         if (rc) return rc;
-        k.X = q.X; k.ldx = q.ldx; k.sX = q.sX; k.K = q.K; k.N = q.N; k.batch = q.batch; k.valid = true;
+        k.X = q.X; k.ldx = q.ldx; k.sX = q.sX; k.K = q.K; k.N = q.N; k.batch = q.batch; k.w = q.oz_w;
+        k.valid = true;
       }
       q.oz_xs = g->oz_xs;
       q.oz_cexp = g->oz_cexp;

@@ -127,7 +127,8 @@ struct GemmArgs {
   const int* oz_ex;
   long oz_sz;
   int oz_rowsP, oz_KP, oz_row0;
-  // slices of X made by launch_oz_slice_cols: [batch][kOzS][oz_KP][oz_Np]
+  int oz_w;  // slice format (bits per slice) of A and X: 6 or 7
+  // slices of X made by launch_oz_slice_cols: [batch][S][oz_KP][oz_Np]
   // bf16 and column exponents [batch][oz_Np]
   const uint16_t* oz_xs;
   const int* oz_cexp;
@@ -135,22 +136,26 @@ struct GemmArgs {
 };
 
 // ---- FP64 GEMM on bf16 tensor cores by exact slicing (falcon_ozaki.cu) ----
-// An FP64 operand row (or column) with |a| < 2^e is cut into kOzS signed
-// integers of kOzW bits, a = 2^e sum_s q_s 2^(-kOzW (s+1)) up to 2^(e-60).
+// An FP64 operand row (or column) with |a| < 2^e is cut into S signed
+// integers of W bits, a = 2^e sum_s q_s 2^(-W (s+1)) up to 2^(e - S W).
 // Slice products are exact in bf16 x bf16 -> FP32 and their sums stay
-// below 2^24 (exact) for K <= 257; the pairs s + t <= kOzD are summed per
-// s + t and recombined in 64-bit integers and one FP64 FMA.
+// below 2^24 (exact); the pairs s + t <= D are summed per s + t and
+// recombined in 64-bit integers and one FP64 add.  Formats: W = 6 (S = 10,
+// D = 9) for K <= 257, W = 7 (S = 9, D = 8) for K <= 112.  kOzS is the
+// largest slice count (buffer sizes).
 constexpr int kOzS = 10, kOzW = 6, kOzD = 9;
+inline int oz_width_for(int KP) { return KP <= 112 ? 7 : 6; }
+inline int oz_slices(int w) { return w == 7 ? 9 : 10; }
 // Slices of a column-major FP64 operator (rows x K, lda, nb entries of
-// stride sA) into S [nb][kOzS][rowsP][KP] (bf16 bits, zero padded) and row
+// stride sA) into S [nb][S][rowsP][KP] (bf16 bits, zero padded) and row
 // exponents ex [nb][rowsP].
 cudaError_t launch_oz_slice_rows(const double* A, long lda, long sA, int rows, int K, int nb, uint16_t* S, int* ex,
-                                 int rowsP, int KP, cudaStream_t s);
+                                 int rowsP, int KP, int w, cudaStream_t s);
 // Slices of the columns of X (K x N, row stride ldx, batch stride sX) into
-// Xs [batch][kOzS][KP][Np] (zero for k >= K, n >= N) and column exponents
+// Xs [batch][S][KP][Np] (zero for k >= K, n >= N) and column exponents
 // cexp [batch][Np].  Np is a multiple of 32.
 cudaError_t launch_oz_slice_cols(const double* X, long ldx, long sX, int K, int N, int batch, uint16_t* Xs,
-                                 int* cexp, int KP, int Np, cudaStream_t s);
+                                 int* cexp, int KP, int Np, int w, cudaStream_t s);
 // Y = alpha A X from the slices of A (oz_s, oz_ex) and of X (oz_xs, oz_cexp).
 cudaError_t launch_oz_gemm(const GemmArgs& g, cudaStream_t s);
 // Row padding of operator slices: rows_total rounded up to 16, plus 64

@@ -5,16 +5,18 @@
 // (~600 TFLOP/s measured for mma.sync), and DMMA shares the FP64 rate.  So
 // the operator contractions of the time step run as integer products:
 //   - A row i with |a| < 2^e_i and an X column n with |x| < 2^f_n are cut
-//     into kOzS = 10 signed 6-bit integers (|q| <= 63, exact in bf16):
-//       a = 2^e_i sum_s alpha_s 2^(-6(s+1)),  x = 2^f_n sum_t beta_t 2^(-6(t+1)),
-//     dropping bits below 2^(e-60);
-//   - P_st = sum_k alpha_s beta_t is exact in FP32: |alpha beta| < 2^12, K <=
-//     257 and at most 10 pairs per s + t keep every partial sum below 2^24;
-//   - Q_d = sum_{s+t=d} P_st for d <= 9 accumulates in one FP32 register set
-//     per d (still exact), the pairs s + t > 9 are dropped (< K 2^(e+f-56));
-//   - Y = 2^(e_i + f_n - 36) (H + 2^-30 L), H = sum_{d<=4} Q_d 64^(4-d) and
-//     L = sum_{d>=5} Q_d 64^(9-d) formed exactly in 64-bit integers, one
-//     FP64 FMA and an exact power-of-two scale.
+//     into S signed W-bit integers (exact in bf16):
+//       a = 2^e_i sum_s alpha_s 2^(-W(s+1)),  x = 2^f_n sum_t beta_t 2^(-W(t+1)),
+//     dropping bits below 2^(e - S W);
+//   - P_st = sum_k alpha_s beta_t is exact in FP32, and so is
+//     Q_d = sum_{s+t=d} P_st for d <= D, one FP32 register set per d: with
+//     W = 6, S = 10, D = 9 for K <= 257 (10 pairs x 257 x 63^2 < 2^24), with
+//     W = 7, S = 9, D = 8 for K <= 112 (9 x 112 x 127^2 < 2^24; 45 pairs
+//     instead of 55).  The pairs s + t > D weigh less than 2^-56 of
+//     max|A_ik| max|X_kn| per product;
+//   - Y = 2^kH H + 2^kL L, H and L the high and low diagonals combined
+//     exactly in 64-bit integers, scaled exactly through their bits and
+//     added once in FP64 (OzCfg in falcon_slices.cuh).
 // The error is of the order of K 2^-56 max_k|A_ik| max_k|X_kn|, the level of
 // an FP64 GEMM's rounding; each output depends only on its own row and
 // column, and every FP32 sum is exact, so results do not depend on the
@@ -33,18 +35,15 @@ namespace falcon {
 
 namespace {
 
-// 2^k as a double for the normal range, else a scaled fallback
-__device__ __forceinline__ double scale2(double y, int k) {
-  if (k >= -1022 && k <= 1023) return y * __longlong_as_double((long long)(k + 1023) << 52);
-  return ldexp(y, k);
-}
-
 }  // namespace
 
 // One thread per (entry, row): the row exponent, then the slices of each
-// element.  The caller zeroes S (padding rows and K columns stay zero).
+// element (format W).  The caller zeroes S (padding rows and K columns stay
+// zero).
+template <int W>
 __global__ void oz_slice_rows_kernel(const double* A, long lda, long sA, int rows, int K, int nb, uint16_t* S,
                                      int* ex, int rowsP, int KP) {
+  using C = OzCfg<W>;
   const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (t >= (long)nb * rows) return;
   const int z = (int)(t / rows), r = (int)(t - (long)z * rows);
@@ -53,33 +52,34 @@ __global__ void oz_slice_rows_kernel(const double* A, long lda, long sA, int row
   for (int k = 0; k < K; ++k) mx = max(mx, biased_exp(a[(size_t)k * lda]));
   const int e = mx - 1022;  // |a| < 2^e for every entry of the row
   ex[(size_t)z * rowsP + r] = mx ? e : 0;
-  uint16_t* s0 = S + (size_t)z * kOzS * rowsP * KP + (size_t)r * KP;
+  uint16_t* s0 = S + (size_t)z * C::S * rowsP * KP + (size_t)r * KP;
   const size_t sls = (size_t)rowsP * KP;
   for (int k = 0; k < K; ++k) {
     const double v = a[(size_t)k * lda];
-    const unsigned long long T = mx ? oz_mag(v, e) : 0ull;
+    const unsigned long long T = mx ? oz_magb<C::MAGB>(v, e) : 0ull;
 #pragma unroll
-    for (int s = 0; s < kOzS; ++s) {
-      const int q = (int)((T >> (kOzW * (kOzS - 1 - s))) & ((1u << kOzW) - 1));
-      s0[s * sls + k] = bf16_bits_of_int(v < 0 ? -q : q);
-    }
+    for (int sl = 0; sl < C::S; ++sl) s0[sl * sls + k] = (uint16_t)oz_slice_w<W>(T, v < 0, sl);
   }
 }
 
 cudaError_t launch_oz_slice_rows(const double* A, long lda, long sA, int rows, int K, int nb, uint16_t* S, int* ex,
-                                 int rowsP, int KP, cudaStream_t s) {
+                                 int rowsP, int KP, int w, cudaStream_t s) {
   const long n = (long)nb * rows;
   if (n <= 0) return cudaSuccess;
-  oz_slice_rows_kernel<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(A, lda, sA, rows, K, nb, S, ex, rowsP, KP);
+  const unsigned grid = (unsigned)((n + 127) / 128);
+  if (w == 7) oz_slice_rows_kernel<7><<<grid, 128, 0, s>>>(A, lda, sA, rows, K, nb, S, ex, rowsP, KP);
+  else oz_slice_rows_kernel<6><<<grid, 128, 0, s>>>(A, lda, sA, rows, K, nb, S, ex, rowsP, KP);
   return cudaGetLastError();
 }
 
 // Column slices of X: block (64 columns, batch entry); the column
 // exponent from four strided partial maxima, then every (k, column) element
-// cut into its kOzS slices, written slice plane by slice plane (coalesced
-// along the columns).
+// cut into its slices (format W), written slice plane by slice plane
+// (coalesced along the columns).
+template <int W>
 __global__ void __launch_bounds__(256) oz_slice_cols_kernel(const double* X, long ldx, long sX, int K, int N,
                                                             uint16_t* Xs, int* cexp, int KP, int Np) {
+  using C = OzCfg<W>;
   __shared__ int ex[4][64];
   const int c = threadIdx.x & 63, kq = threadIdx.x >> 6;
   const int z = blockIdx.y, n = blockIdx.x * 64 + c;
@@ -92,28 +92,26 @@ __global__ void __launch_bounds__(256) oz_slice_cols_kernel(const double* X, lon
   const int fb = max(max(ex[0][c], ex[1][c]), max(ex[2][c], ex[3][c]));
   if (kq == 0 && n < Np) cexp[(size_t)z * Np + n] = fb;
   if (n >= Np) return;
-  uint16_t* xz = Xs + (size_t)z * kOzS * KP * Np;
+  uint16_t* xz = Xs + (size_t)z * C::S * KP * Np;
   for (int k = kq; k < KP; k += 4) {
     unsigned long long T = 0ull;
     bool neg = false;
     if (k < K && n < N && fb > 0) {
       const double v = Xz[(size_t)k * ldx + n];
-      T = oz_mag(v, fb - 1022);
+      T = oz_magb<C::MAGB>(v, fb - 1022);
       neg = __double_as_longlong(v) < 0;
     }
 #pragma unroll
-    for (int sl = 0; sl < kOzS; ++sl) {
-      const int q = (int)((T >> (kOzW * (kOzS - 1 - sl))) & ((1u << kOzW) - 1));
-      xz[((size_t)sl * KP + k) * Np + n] = bf16_bits_of_int(neg ? -q : q);
-    }
+    for (int sl = 0; sl < C::S; ++sl) xz[((size_t)sl * KP + k) * Np + n] = (uint16_t)oz_slice_w<W>(T, neg, sl);
   }
 }
 
 cudaError_t launch_oz_slice_cols(const double* X, long ldx, long sX, int K, int N, int batch, uint16_t* Xs,
-                                 int* cexp, int KP, int Np, cudaStream_t s) {
+                                 int* cexp, int KP, int Np, int w, cudaStream_t s) {
   if (N <= 0 || batch <= 0) return cudaSuccess;
   dim3 grid((Np + 63) / 64, batch);
-  oz_slice_cols_kernel<<<grid, 256, 0, s>>>(X, ldx, sX, K, N, Xs, cexp, KP, Np);
+  if (w == 7) oz_slice_cols_kernel<7><<<grid, 256, 0, s>>>(X, ldx, sX, K, N, Xs, cexp, KP, Np);
+  else oz_slice_cols_kernel<6><<<grid, 256, 0, s>>>(X, ldx, sX, K, N, Xs, cexp, KP, Np);
   return cudaGetLastError();
 }
 
@@ -147,27 +145,28 @@ __device__ __forceinline__ void ldsm_x2t(unsigned (&r)[2], const void* p) {
 // conflict-free).  Per chunk a warp does the 55 slice-pair products
 // s + t <= kOzD on each of its tiles.  NT = 1 halves the accumulator
 // registers (10 diagonals x 4 per tile), so twice the warps fit on an SM.
-template <int MT, int NQ, int NT, int MINB>
+template <int MT, int NQ, int NT, int MINB, int W>
 __global__ void __launch_bounds__(32 * MT * NQ * (2 / NT), MINB) oz_mma_kernel(GemmArgs q) {
+  using C = OzCfg<W>;
   constexpr int SPLIT = 2 / NT;  // warps per (row tile, column group)
   constexpr int AROW = 24, XROW = NQ * 16 + 8;           // padded row lengths (bf16)
-  constexpr int ASTAGE = kOzS * MT * 16 * AROW, XSTAGE = kOzS * 16 * XROW;
+  constexpr int ASTAGE = C::S * MT * 16 * AROW, XSTAGE = C::S * 16 * XROW;
   extern __shared__ __align__(16) uint16_t oz_panel[];   // [2][ASTAGE + XSTAGE]
   const int z = blockIdx.z;
   const int col0 = blockIdx.x * NQ * 16, row0b = blockIdx.y * MT * 16;
   const uint16_t* Az = q.oz_s + (size_t)z * q.oz_sz + (size_t)(q.oz_row0 + row0b) * q.oz_KP;
   const size_t aslice = (size_t)q.oz_rowsP * q.oz_KP;
-  const uint16_t* Xz = q.oz_xs + (size_t)z * kOzS * q.oz_KP * q.oz_Np + col0;
+  const uint16_t* Xz = q.oz_xs + (size_t)z * C::S * q.oz_KP * q.oz_Np + col0;
   const size_t xslice = (size_t)q.oz_KP * q.oz_Np;
   const int tid = threadIdx.x, nthr = 32 * MT * NQ * SPLIT;
   auto stage = [&](int k0, int buf) {
     uint16_t* Ap = oz_panel + buf * (ASTAGE + XSTAGE);
     uint16_t* Xp = Ap + ASTAGE;
-    for (int i = tid; i < kOzS * MT * 16 * 2; i += nthr) {        // A: (slice, row, half)
+    for (int i = tid; i < C::S * MT * 16 * 2; i += nthr) {        // A: (slice, row, half)
       const int h = i & 1, rr = (i >> 1) % (MT * 16), sl = (i >> 1) / (MT * 16);
       cp_async16(Ap + (sl * MT * 16 + rr) * AROW + 8 * h, Az + sl * aslice + (size_t)rr * q.oz_KP + k0 + 8 * h);
     }
-    for (int i = tid; i < kOzS * 16 * 2 * NQ; i += nthr) {        // X: (slice, k, 8-column chunk)
+    for (int i = tid; i < C::S * 16 * 2 * NQ; i += nthr) {        // X: (slice, k, 8-column chunk)
       const int cq = i % (2 * NQ), kk = (i / (2 * NQ)) % 16, sl = i / (2 * NQ * 16);
       cp_async16(Xp + (sl * 16 + kk) * XROW + 8 * cq, Xz + sl * xslice + (size_t)(k0 + kk) * q.oz_Np + 8 * cq);
     }
@@ -175,9 +174,9 @@ __global__ void __launch_bounds__(32 * MT * NQ * (2 / NT), MINB) oz_mma_kernel(G
   };
   const int warp = tid >> 5, lane = tid & 31, gid = lane >> 2, tig = lane & 3;
   const int wm = warp % MT, wr = warp / MT, wn = wr / SPLIT, nt0 = (wr % SPLIT) * NT;
-  float acc[kOzD + 1][NT][4];
+  float acc[C::D + 1][NT][4];
 #pragma unroll
-  for (int d = 0; d <= kOzD; ++d)
+  for (int d = 0; d <= C::D; ++d)
 #pragma unroll
     for (int nt = 0; nt < NT; ++nt)
 #pragma unroll
@@ -194,24 +193,24 @@ __global__ void __launch_bounds__(32 * MT * NQ * (2 / NT), MINB) oz_mma_kernel(G
     __syncthreads();
     const uint16_t* Ap = oz_panel + (kc & 1) * (ASTAGE + XSTAGE);
     const uint16_t* Xp = Ap + ASTAGE;
-    unsigned bf[kOzS][NT][2];
+    unsigned bf[C::S][NT][2];
 #pragma unroll
-    for (int t = 0; t < kOzS; ++t)
+    for (int t = 0; t < C::S; ++t)
 #pragma unroll
       for (int nt = 0; nt < NT; ++nt)
         ldsm_x2t(bf[t][nt], Xp + (t * 16 + (lane & 15)) * XROW + wn * 16 + (nt0 + nt) * 8);
 #pragma unroll
-    for (int sl = 0; sl < kOzS; ++sl) {
+    for (int sl = 0; sl < C::S; ++sl) {
       unsigned af[4];
       ldsm_x4(af, Ap + (sl * MT * 16 + wm * 16 + (lane & 15)) * AROW + (lane >> 4) * 8);
 #pragma unroll
-      for (int t = 0; t < kOzS && sl + t <= kOzD; ++t)
+      for (int t = 0; t < C::S && sl + t <= C::D; ++t)
 #pragma unroll
         for (int nt = 0; nt < NT; ++nt) mma_bf16(acc[sl + t][nt], af[0], af[1], af[2], af[3], bf[t][nt][0], bf[t][nt][1]);
     }
     __syncthreads();  // every warp is done with this buffer before it is refilled
   }
-  // recombination: Y = 2^(e_r + f_n - 36) (H + 2^-30 L)
+  // recombination: Y = 2^kH H + 2^kL L (OzCfg), exact scalings and one FP64 add
   const int* aex = q.oz_ex + (size_t)z * q.oz_rowsP + q.oz_row0;
   const int* cex = q.oz_cexp + (size_t)z * q.oz_Np;
   double* Y = q.Y + (size_t)z * q.sY;
@@ -229,13 +228,14 @@ __global__ void __launch_bounds__(32 * MT * NQ * (2 / NT), MINB) oz_mma_kernel(G
         const int i = 2 * h + j;
         long long H = 0, L = 0;
 #pragma unroll
-        for (int d = 0; d <= 4; ++d) H = H * 64 + (long long)__float2int_rn(acc[d][nt][i]);
+        for (int d = 0; d <= C::HD; ++d) H = H * (1 << W) + (long long)__float2int_rn(acc[d][nt][i]);
 #pragma unroll
-        for (int d = 5; d <= kOzD; ++d) L = L * 64 + (long long)__float2int_rn(acc[d][nt][i]);
+        for (int d = C::HD + 1; d <= C::D; ++d) L = L * (1 << W) + (long long)__float2int_rn(acc[d][nt][i]);
         const int fb = cex[n + j];
-        const double y = fma((double)L, 0x1p-30, (double)H);
-        out[j] = (fb > 0 && (H != 0 || L != 0)) ? scale2(y, er + (fb - 1022) - 36) : 0.0;
-        if (q.alpha != 1.0) out[j] *= q.alpha;
+        const int kL = er + (fb - 1022) - 2 * C::MAGB + W * (2 * C::S - 2 - C::D);
+        double y = fb > 0 ? oz_i64_scaled(H, kL + W * (C::D - C::HD)) + oz_i64_scaled(L, kL) : 0.0;
+        if (fb == 2047) y = __longlong_as_double(0x7ff8000000000000LL);  // Inf or NaN in the column
+        out[j] = q.alpha != 1.0 ? q.alpha * y : y;
       }
       double* yp = Y + (size_t)r * q.ldy + n;
       if (n + 1 < q.N) {
@@ -252,26 +252,34 @@ __global__ void __launch_bounds__(32 * MT * NQ * (2 / NT), MINB) oz_mma_kernel(G
   }
 }
 
-template <int MT, int NQ, int NT = 2, int MINB = 1>
-static cudaError_t launch_oz_mt(const GemmArgs& g, cudaStream_t s) {
-  constexpr size_t smem = 2 * ((size_t)kOzS * MT * 16 * 24 + (size_t)kOzS * 16 * (NQ * 16 + 8)) * sizeof(uint16_t);
+template <int MT, int NQ, int NT, int MINB, int W>
+static cudaError_t launch_oz_w(const GemmArgs& g, cudaStream_t s) {
+  constexpr int S = OzCfg<W>::S;
+  constexpr size_t smem = 2 * ((size_t)S * MT * 16 * 24 + (size_t)S * 16 * (NQ * 16 + 8)) * sizeof(uint16_t);
   static bool opted[64] = {false};
   int dev = 0;
   cudaGetDevice(&dev);
   if (dev >= 0 && dev < 64 && !opted[dev]) {
-    const cudaError_t e = cudaFuncSetAttribute(oz_mma_kernel<MT, NQ, NT, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    const cudaError_t e = cudaFuncSetAttribute(oz_mma_kernel<MT, NQ, NT, MINB, W>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                (int)smem);
     if (e != cudaSuccess) return e;
     opted[dev] = true;
   }
   dim3 grid((g.N + NQ * 16 - 1) / (NQ * 16), (g.rows + MT * 16 - 1) / (MT * 16), g.batch);
-  oz_mma_kernel<MT, NQ, NT, MINB><<<grid, 32 * MT * NQ * (2 / NT), smem, s>>>(g);
+  oz_mma_kernel<MT, NQ, NT, MINB, W><<<grid, 32 * MT * NQ * (2 / NT), smem, s>>>(g);
   return cudaGetLastError();
+}
+
+template <int MT, int NQ, int NT = 2, int MINB = 1>
+static cudaError_t launch_oz_mt(const GemmArgs& g, cudaStream_t s) {
+  return g.oz_w == 7 ? launch_oz_w<MT, NQ, NT, MINB, 7>(g, s) : launch_oz_w<MT, NQ, NT, MINB, 6>(g, s);
 }
 
 cudaError_t launch_oz_gemm(const GemmArgs& g, cudaStream_t s) {
   if (g.rows <= 0 || g.N <= 0 || g.batch <= 0) return cudaSuccess;
-  if (g.K > 257 || g.oz_KP < g.K || !g.oz_xs || (g.oz_Np % 32) != 0) return cudaErrorInvalidValue;
+  if (g.K > 257 || g.oz_KP < g.K || !g.oz_xs || (g.oz_Np % 32) != 0 || (g.oz_w != 6 && g.oz_w != 7) ||
+      (g.oz_w == 7 && g.oz_KP > 112))
+    return cudaErrorInvalidValue;
   // Row tiles per block: all of them up to 8 (one column group of 16, so
   // the operator panel is staged once for every row of the block), else the
   // fewest balanced blocks of at most 4 tiles with two column groups.

@@ -1,8 +1,8 @@
 // Device helpers shared by the integer-slice products (operator GEMMs in
 // falcon_ozaki.cu, odd-prime DFT stages in falcon_kernels.cu): an FP64
-// value cut into signed 6-bit integers relative to a power of two that
-// bounds its row or column, bf16 encoding of the slices, and the bf16
-// mma.sync used on them.
+// value cut into signed integers of a few bits relative to a power of two
+// that bounds its row or column, their bf16 / fp16 encodings, the exact
+// recombination, and the mma.sync used on them.
 #pragma once
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
@@ -17,26 +17,40 @@ __device__ __forceinline__ int biased_exp(double a) {
   return (int)((__double_as_longlong(a) >> 52) & 0x7ff);
 }
 
-// |a| * 2^(60 - e) truncated to an integer (< 2^60 when |a| < 2^e); zero and
-// subnormal inputs give 0.
-__device__ __forceinline__ unsigned long long oz_mag(double a, int e) {
-  const long long bits = __double_as_longlong(a);
-  const int eb = (int)((bits >> 52) & 0x7ff);
-  if (eb == 0) return 0ull;
-  const unsigned long long m = (unsigned long long)(bits & 0xfffffffffffffLL) | (1ull << 52);
-  const int sh = eb - 1015 - e;  // a = m 2^(eb-1075): T = m 2^(eb - 1075 + 60 - e)
-  if (sh >= 0) return m << sh;   // sh <= 7 because |a| < 2^e
-  if (sh <= -64) return 0ull;
-  return m >> (-sh);
-}
-
 __device__ __forceinline__ uint16_t bf16_bits_of_int(int q) {
   return __bfloat16_as_ushort(__float2bfloat16_rn((float)q));
 }
 
-// Slice s (0 = most significant) of a value cut by oz_mag, with its sign.
-__device__ __forceinline__ uint32_t oz_slice_bits(unsigned long long T, bool neg, int s) {
-  const int q = (int)((T >> (kOzW * (kOzS - 1 - s))) & ((1u << kOzW) - 1));
+// Slice formats of the operator GEMMs.  Width W bits per slice, S slices
+// (MAGB = S W bits of each operand, relative to the power of two that
+// bounds its row or column), the pairs s + t <= D summed per diagonal d in
+// FP32, exact while K (D + 1 - ...) (2^W - 1)^2 < 2^24: W = 6 for K <= 257,
+// W = 7 for K <= 112 (nine pairs per diagonal at most).  Recombination:
+// sum_k a_k x_k = 2^(kH) H + 2^(kL) L with H = sum_{d<=HD} Q_d 2^(W(HD-d)),
+// L = sum_{HD<d<=D} Q_d 2^(W(D-d)) (both exact in 64-bit integers) and
+// kL = e_row + e_col - 2 MAGB + W (2S - 2 - D), kH = kL + W (D - HD).
+template <int W> struct OzCfg;
+template <> struct OzCfg<6> { static constexpr int S = 10, D = 9, HD = 4, MAGB = 60; };
+template <> struct OzCfg<7> { static constexpr int S = 9, D = 8, HD = 3, MAGB = 63; };
+
+// |a| * 2^(MAGB - e) truncated (< 2^MAGB when |a| < 2^e); zero and subnormal
+// inputs give 0.
+template <int MAGB>
+__device__ __forceinline__ unsigned long long oz_magb(double a, int e) {
+  const long long bits = __double_as_longlong(a);
+  const int eb = (int)((bits >> 52) & 0x7ff);
+  if (eb == 0) return 0ull;
+  const unsigned long long m = (unsigned long long)(bits & 0xfffffffffffffLL) | (1ull << 52);
+  const int sh = eb - 1075 + MAGB - e;  // <= MAGB - 53 because |a| < 2^e
+  if (sh >= 0) return m << sh;
+  if (sh <= -64) return 0ull;
+  return m >> (-sh);
+}
+
+// Slice s (0 = most significant) of T in format W, with a sign, as bf16 bits.
+template <int W>
+__device__ __forceinline__ uint32_t oz_slice_w(unsigned long long T, bool neg, int s) {
+  const int q = (int)((T >> (W * (OzCfg<W>::S - 1 - s))) & ((1u << W) - 1));
   return bf16_bits_of_int(neg ? -q : q);
 }
 
