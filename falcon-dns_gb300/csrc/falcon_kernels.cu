@@ -1792,17 +1792,23 @@ __global__ void __launch_bounds__(256) diag_rows_kernel(DiagArgs a) {
   P[7 * ks] = up2;
 }
 
-// Phase 2, one thread per instance: the radial sums in row order and the
-// eight diagnostics of writeKE_spectral / Nusselt (8 doubles per instance).
+// Phase 2, one warp per instance: lane l sums the radial rows l, l + 32,
+// ..., then a fixed shuffle tree; then the eight diagnostics of
+// writeKE_spectral / Nusselt (8 doubles per instance).
 __global__ void diag_sum_kernel(DiagArgs a) {
-  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  const int b = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
   const int R = a.R, B = a.B;
   if (b >= B) return;
   const size_t ks = (size_t)R * B;
   double t[7] = {0, 0, 0, 0, 0, 0, 0};
-  for (int r = 0; r < R; ++r)
+  for (int r = lane; r < R; r += 32)
 #pragma unroll
     for (int k = 0; k < 7; ++k) t[k] += a.part[k * ks + (size_t)r * B + b];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+    for (int k = 0; k < 7; ++k) t[k] += __shfl_xor_sync(0xffffffffu, t[k], o);
+  if (lane != 0) return;
   const double s_in = a.part[7 * ks + b], s_out = a.part[7 * ks + (size_t)(R - 1) * B + b];
   const double two_pi = 2.0 * a.pi;
   double* o = a.out + (size_t)b * 8;
@@ -1818,7 +1824,7 @@ __global__ void diag_sum_kernel(DiagArgs a) {
 
 cudaError_t launch_diagnostics(const DiagArgs& a, cudaStream_t s) {
   diag_rows_kernel<<<dim3(a.R, (a.B + 31) / 32), dim3(32, 8), 0, s>>>(a);
-  diag_sum_kernel<<<(a.B + 127) / 128, 128, 0, s>>>(a);
+  diag_sum_kernel<<<(a.B + 3) / 4, 128, 0, s>>>(a);
   return cudaGetLastError();
 }
 

@@ -23,7 +23,8 @@ def smooth(rng, R, M, decay=0.05):
     return (rng.standard_normal((R, M)) + 1j * rng.standard_normal((R, M))) * d
 
 
-@pytest.mark.parametrize("R,Nm", [(9, 4), (33, 42), (65, 85), (65, 170), (97, 341), (33, 512), (17, 7)])
+@pytest.mark.parametrize("R,Nm", [(9, 4), (33, 42), (65, 85), (65, 170), (97, 341), (33, 512), (17, 7),
+                                  (17, 10), (33, 35)])
 def test_nonlinear_pass_matches_oracle(orc, fg, R, Nm):
     rng = np.random.default_rng(R * 1000 + Nm)
     M = Nm + 1
