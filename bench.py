@@ -334,10 +334,14 @@ def gpu_warmup(args):
 # launch class -> kernel function
 KERNEL_OF_CLASS = {"gemm_radial": "oz_mma_kernel", "gemm_mode_solve": "oz_mma_kernel",
                    "nonlin_fft": "nonlin_kernel", "elementwise": "elementwise kernels"}
-# The operator GEMMs of this workload (N >= 16 columns each) run as products
-# of 6-bit integer slices on the bf16 tensor cores: 10 slices per operand and
-# the 55 slice pairs s + t <= 9, i.e. 55 bf16 products per FP64 product.
-OZ_SLICE_PAIRS = 55
+
+
+def oz_slice_pairs(nr):
+    """bf16 slice products per FP64 product of the operator GEMMs (N >= 16
+    columns each, contraction length K = Nr): 7-bit slices, 9 per operand and
+    the 45 pairs s + t <= 8, when K padded to 16 is at most 112; else 6-bit
+    slices, 10 per operand and the 55 pairs s + t <= 9."""
+    return 45 if (nr + 15) // 16 * 16 <= 112 else 55
 
 
 def tensor_peak():
@@ -434,8 +438,9 @@ def run_gpu(args):
         if k == "oz_mma_kernel":
             # bf16 slice products executed per second against the tensor
             # peak; the FP64-equivalent rate against the DFMA peak beside it
-            r.update({"bound": "tensor", "achieved": ach * OZ_SLICE_PAIRS, "peak": tpeak,
-                      "frac": ach * OZ_SLICE_PAIRS / tpeak, "peak_source": tpeak_src,
+            pairs = oz_slice_pairs(W["nr"])
+            r.update({"bound": "tensor", "achieved": ach * pairs, "peak": tpeak,
+                      "frac": ach * pairs / tpeak, "peak_source": tpeak_src, "slice_pairs": pairs,
                       "fp64_equivalent_tflops": ach, "fp64_equivalent_over_dfma_peak": ach / (peak / 1e3),
                       "note": "time includes the per-call slicing of the X columns (oz_slice_cols_kernel)"})
         return r
