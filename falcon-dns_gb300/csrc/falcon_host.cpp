@@ -1105,7 +1105,9 @@ int gemm(Group* g, int cls, const GemmArgs& q0, bool reuse = false) {
     ok = attach_oz(g->ops.get(), &q);
     for (int st = 0; !ok && st < kMaxStages; ++st) ok = attach_oz(g->stage_ops[st].get(), &q);
   }
-  if (ok) {
+  if (ok && oz_fused_x(q.rows, q.N, q.batch)) {
+    // the kernel slices its own X columns
+  } else if (ok) {
     const int KP = q.oz_KP, Np = (int)(((long)q.N + 31) / 32 * 32);
     if ((size_t)oz_slices(q.oz_w) * KP * Np * q.batch > g->oz_xs_cap || (size_t)Np * q.batch > g->oz_cexp_cap) {
       ok = false;  // beyond the scratch sized for this group: FMA tiles

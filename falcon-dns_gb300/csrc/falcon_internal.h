@@ -145,6 +145,16 @@ struct GemmArgs {
 // largest slice count (buffer sizes).
 constexpr int kOzS = 10, kOzW = 6, kOzD = 9;
 inline int oz_width_for(int KP) { return KP <= 112 ? 7 : 6; }
+// Contractions of operators of 5 to 8 row tiles (65 <= rows <= 128) with
+// few columns in all (N x batch <= 16384: one instance, small groups) take a
+// kernel that slices its X columns itself: one launch fewer per contraction
+// where launches dominate.  Larger ones read slice planes made once by
+// launch_oz_slice_cols (shared by the contractions of one X), which costs
+// less than slicing in every block.
+inline bool oz_fused_x(int rows, int N, int batch) {
+  const int rt = (rows + 15) / 16;
+  return rt >= 5 && rt <= 8 && (long)N * batch <= 16384;
+}
 inline int oz_slices(int w) { return w == 7 ? 9 : 10; }
 // Slices of a column-major FP64 operator (rows x K, lda, nb entries of
 // stride sA) into S [nb][S][rowsP][KP] (bf16 bits, zero padded) and row

@@ -145,20 +145,27 @@ __device__ __forceinline__ void ldsm_x2t(unsigned (&r)[2], const void* p) {
 // conflict-free).  Per chunk a warp does the 55 slice-pair products
 // s + t <= kOzD on each of its tiles.  NT = 1 halves the accumulator
 // registers (10 diagonals x 4 per tile), so twice the warps fit on an SM.
-template <int MT, int NQ, int NT, int MINB, int W>
+// FX: the block cuts its own X columns (all of K, from the FP64 operand)
+// into slice planes resident in shared memory, with the column exponents,
+// instead of reading planes made by oz_slice_cols_kernel: the same slices,
+// one launch and the planes' HBM round trip fewer.
+template <int MT, int NQ, int NT, int MINB, int W, bool FX>
 __global__ void __launch_bounds__(32 * MT * NQ * (2 / NT), MINB) oz_mma_kernel(GemmArgs q) {
   using C = OzCfg<W>;
   constexpr int SPLIT = 2 / NT;  // warps per (row tile, column group)
   constexpr int AROW = 24, XROW = NQ * 16 + 8;           // padded row lengths (bf16)
-  constexpr int ASTAGE = C::S * MT * 16 * AROW, XSTAGE = C::S * 16 * XROW;
-  extern __shared__ __align__(16) uint16_t oz_panel[];   // [2][ASTAGE + XSTAGE]
+  constexpr int CW = NQ * 16;                            // columns of the block
+  constexpr int ASTAGE = C::S * MT * 16 * AROW, XSTAGE = FX ? 0 : C::S * 16 * XROW;
+  extern __shared__ __align__(16) uint16_t oz_panel[];   // [2][ASTAGE + XSTAGE] (+ FX: planes, exponents)
   const int z = blockIdx.z;
-  const int col0 = blockIdx.x * NQ * 16, row0b = blockIdx.y * MT * 16;
+  const int col0 = blockIdx.x * CW, row0b = blockIdx.y * MT * 16;
   const uint16_t* Az = q.oz_s + (size_t)z * q.oz_sz + (size_t)(q.oz_row0 + row0b) * q.oz_KP;
   const size_t aslice = (size_t)q.oz_rowsP * q.oz_KP;
-  const uint16_t* Xz = q.oz_xs + (size_t)z * C::S * q.oz_KP * q.oz_Np + col0;
+  const uint16_t* Xz = FX ? nullptr : q.oz_xs + (size_t)z * C::S * q.oz_KP * q.oz_Np + col0;
   const size_t xslice = (size_t)q.oz_KP * q.oz_Np;
   const int tid = threadIdx.x, nthr = 32 * MT * NQ * SPLIT;
+  uint16_t* xres = oz_panel + 2 * (ASTAGE + XSTAGE);                          // FX: [S][KP][XROW]
+  int* cex_s = reinterpret_cast<int*>(xres + (FX ? (size_t)C::S * q.oz_KP * XROW : 0));  // FX: [CW]
   auto stage = [&](int k0, int buf) {
     uint16_t* Ap = oz_panel + buf * (ASTAGE + XSTAGE);
     uint16_t* Xp = Ap + ASTAGE;
@@ -166,9 +173,11 @@ __global__ void __launch_bounds__(32 * MT * NQ * (2 / NT), MINB) oz_mma_kernel(G
       const int h = i & 1, rr = (i >> 1) % (MT * 16), sl = (i >> 1) / (MT * 16);
       cp_async16(Ap + (sl * MT * 16 + rr) * AROW + 8 * h, Az + sl * aslice + (size_t)rr * q.oz_KP + k0 + 8 * h);
     }
-    for (int i = tid; i < C::S * 16 * 2 * NQ; i += nthr) {        // X: (slice, k, 8-column chunk)
-      const int cq = i % (2 * NQ), kk = (i / (2 * NQ)) % 16, sl = i / (2 * NQ * 16);
-      cp_async16(Xp + (sl * 16 + kk) * XROW + 8 * cq, Xz + sl * xslice + (size_t)(k0 + kk) * q.oz_Np + 8 * cq);
+    if constexpr (!FX) {
+      for (int i = tid; i < C::S * 16 * 2 * NQ; i += nthr) {      // X: (slice, k, 8-column chunk)
+        const int cq = i % (2 * NQ), kk = (i / (2 * NQ)) % 16, sl = i / (2 * NQ * 16);
+        cp_async16(Xp + (sl * 16 + kk) * XROW + 8 * cq, Xz + sl * xslice + (size_t)(k0 + kk) * q.oz_Np + 8 * cq);
+      }
     }
     cp_commit();
   };
@@ -183,6 +192,32 @@ __global__ void __launch_bounds__(32 * MT * NQ * (2 / NT), MINB) oz_mma_kernel(G
       for (int i = 0; i < 4; ++i) acc[d][nt][i] = 0.f;
   const int nk = q.oz_KP / 16;
   stage(0, 0);
+  if constexpr (FX) {
+    // thread (row group g, column c): rows k = g, g + ng, ... of column c
+    constexpr int NG = 32 * MT * NQ * SPLIT / CW;
+    int* pmax = cex_s + CW;  // [NG][CW]
+    const int c = tid % CW, g = tid / CW, n = col0 + c;
+    const double* xc = q.X + (size_t)z * q.sX + n;
+    int mx = 0;
+    if (n < q.N)
+      for (int k = g; k < q.K; k += NG) mx = max(mx, biased_exp(xc[(size_t)k * q.ldx]));
+    pmax[g * CW + c] = mx;
+    __syncthreads();
+    int fb = 0;
+    for (int j = 0; j < NG; ++j) fb = max(fb, pmax[j * CW + c]);
+    if (g == 0) cex_s[c] = fb;
+    for (int k = g; k < q.oz_KP; k += NG) {
+      unsigned long long T = 0ull;
+      bool neg = false;
+      if (k < q.K && n < q.N && fb > 0) {
+        const double v = xc[(size_t)k * q.ldx];
+        T = oz_magb<C::MAGB>(v, fb - 1022);
+        neg = __double_as_longlong(v) < 0;
+      }
+#pragma unroll
+      for (int sl = 0; sl < C::S; ++sl) xres[((size_t)sl * q.oz_KP + k) * XROW + c] = (uint16_t)oz_slice_w<W>(T, neg, sl);
+    }
+  }
   for (int kc = 0; kc < nk; ++kc) {
     if (kc + 1 < nk) {
       stage((kc + 1) * 16, (kc + 1) & 1);
@@ -192,13 +227,15 @@ __global__ void __launch_bounds__(32 * MT * NQ * (2 / NT), MINB) oz_mma_kernel(G
     }
     __syncthreads();
     const uint16_t* Ap = oz_panel + (kc & 1) * (ASTAGE + XSTAGE);
-    const uint16_t* Xp = Ap + ASTAGE;
+    // X rows of this chunk: slice t at Xp + t * xts (16 rows of XROW)
+    const uint16_t* Xp = FX ? xres + (size_t)kc * 16 * XROW : Ap + ASTAGE;
+    const size_t xts = FX ? (size_t)q.oz_KP * XROW : (size_t)16 * XROW;
     unsigned bf[C::S][NT][2];
 #pragma unroll
     for (int t = 0; t < C::S; ++t)
 #pragma unroll
       for (int nt = 0; nt < NT; ++nt)
-        ldsm_x2t(bf[t][nt], Xp + (t * 16 + (lane & 15)) * XROW + wn * 16 + (nt0 + nt) * 8);
+        ldsm_x2t(bf[t][nt], Xp + t * xts + (lane & 15) * XROW + wn * 16 + (nt0 + nt) * 8);
 #pragma unroll
     for (int sl = 0; sl < C::S; ++sl) {
       unsigned af[4];
@@ -212,7 +249,7 @@ __global__ void __launch_bounds__(32 * MT * NQ * (2 / NT), MINB) oz_mma_kernel(G
   }
   // recombination: Y = 2^kH H + 2^kL L (OzCfg), exact scalings and one FP64 add
   const int* aex = q.oz_ex + (size_t)z * q.oz_rowsP + q.oz_row0;
-  const int* cex = q.oz_cexp + (size_t)z * q.oz_Np;
+  const int* cex = FX ? cex_s - col0 : q.oz_cexp + (size_t)z * q.oz_Np;
   double* Y = q.Y + (size_t)z * q.sY;
 #pragma unroll
   for (int nt = 0; nt < NT; ++nt) {
@@ -252,32 +289,38 @@ __global__ void __launch_bounds__(32 * MT * NQ * (2 / NT), MINB) oz_mma_kernel(G
   }
 }
 
-template <int MT, int NQ, int NT, int MINB, int W>
+template <int MT, int NQ, int NT, int MINB, int W, bool FX>
 static cudaError_t launch_oz_w(const GemmArgs& g, cudaStream_t s) {
-  constexpr int S = OzCfg<W>::S;
-  constexpr size_t smem = 2 * ((size_t)S * MT * 16 * 24 + (size_t)S * 16 * (NQ * 16 + 8)) * sizeof(uint16_t);
-  static bool opted[64] = {false};
+  constexpr int S = OzCfg<W>::S, XROW = NQ * 16 + 8;
+  constexpr int NG = 32 * MT * NQ * (2 / NT) / (NQ * 16);
+  const size_t smem =
+      FX ? 2 * (size_t)S * MT * 16 * 24 * sizeof(uint16_t) + (size_t)S * g.oz_KP * XROW * sizeof(uint16_t) +
+               (size_t)(NQ * 16) * (1 + NG) * sizeof(int)
+         : 2 * ((size_t)S * MT * 16 * 24 + (size_t)S * 16 * XROW) * sizeof(uint16_t);
+  if (smem > 227 * 1024) return cudaErrorInvalidValue;
+  static int opted[64] = {0};  // shared-memory size opted in, per device
   int dev = 0;
   cudaGetDevice(&dev);
-  if (dev >= 0 && dev < 64 && !opted[dev]) {
-    const cudaError_t e = cudaFuncSetAttribute(oz_mma_kernel<MT, NQ, NT, MINB, W>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                               (int)smem);
+  if (dev >= 0 && dev < 64 && opted[dev] < (int)smem) {
+    const cudaError_t e = cudaFuncSetAttribute(oz_mma_kernel<MT, NQ, NT, MINB, W, FX>,
+                                               cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
     if (e != cudaSuccess) return e;
-    opted[dev] = true;
+    opted[dev] = 227 * 1024;
   }
   dim3 grid((g.N + NQ * 16 - 1) / (NQ * 16), (g.rows + MT * 16 - 1) / (MT * 16), g.batch);
-  oz_mma_kernel<MT, NQ, NT, MINB, W><<<grid, 32 * MT * NQ * (2 / NT), smem, s>>>(g);
+  oz_mma_kernel<MT, NQ, NT, MINB, W, FX><<<grid, 32 * MT * NQ * (2 / NT), smem, s>>>(g);
   return cudaGetLastError();
 }
 
-template <int MT, int NQ, int NT = 2, int MINB = 1>
+template <int MT, int NQ, int NT = 2, int MINB = 1, bool FX = false>
 static cudaError_t launch_oz_mt(const GemmArgs& g, cudaStream_t s) {
-  return g.oz_w == 7 ? launch_oz_w<MT, NQ, NT, MINB, 7>(g, s) : launch_oz_w<MT, NQ, NT, MINB, 6>(g, s);
+  return g.oz_w == 7 ? launch_oz_w<MT, NQ, NT, MINB, 7, FX>(g, s) : launch_oz_w<MT, NQ, NT, MINB, 6, FX>(g, s);
 }
 
 cudaError_t launch_oz_gemm(const GemmArgs& g, cudaStream_t s) {
   if (g.rows <= 0 || g.N <= 0 || g.batch <= 0) return cudaSuccess;
-  if (g.K > 257 || g.oz_KP < g.K || !g.oz_xs || (g.oz_Np % 32) != 0 || (g.oz_w != 6 && g.oz_w != 7) ||
+  const bool fx = oz_fused_x(g.rows, g.N, g.batch);
+  if (g.K > 257 || g.oz_KP < g.K || (!fx && (!g.oz_xs || (g.oz_Np % 32) != 0)) || (g.oz_w != 6 && g.oz_w != 7) ||
       (g.oz_w == 7 && g.oz_KP > 112))
     return cudaErrorInvalidValue;
   // Row tiles per block: all of them up to 8 (one column group of 16, so
@@ -286,10 +329,10 @@ cudaError_t launch_oz_gemm(const GemmArgs& g, cudaStream_t s) {
   const int rt = (g.rows + 15) / 16;
   if (rt >= 5 && rt <= 8) {
     switch (rt) {
-      case 5: return launch_oz_mt<5, 1, 1, 2>(g, s);
-      case 6: return launch_oz_mt<6, 1, 1, 1>(g, s);
-      case 7: return launch_oz_mt<7, 1, 1, 1>(g, s);
-      default: return launch_oz_mt<8, 1, 1, 1>(g, s);
+      case 5: return fx ? launch_oz_mt<5, 1, 1, 2, true>(g, s) : launch_oz_mt<5, 1, 1, 2, false>(g, s);
+      case 6: return fx ? launch_oz_mt<6, 1, 1, 1, true>(g, s) : launch_oz_mt<6, 1, 1, 1, false>(g, s);
+      case 7: return fx ? launch_oz_mt<7, 1, 1, 1, true>(g, s) : launch_oz_mt<7, 1, 1, 1, false>(g, s);
+      default: return fx ? launch_oz_mt<8, 1, 1, 1, true>(g, s) : launch_oz_mt<8, 1, 1, 1, false>(g, s);
     }
   }
   const int groups = (rt + 3) / 4, mt = (rt + groups - 1) / groups;
