@@ -28,16 +28,19 @@ def run(fg, params, seeds, nsteps, mode):
     return out
 
 
+# Batches up to a few dozen instances take the kernel that slices its own X
+# columns (N x batch <= 16384 columns); the 200-instance case takes the slice
+# planes of oz_slice_cols_kernel, as the bench's 256-instance batch does.
 @pytest.mark.parametrize("scheme,R,Nm,B,dt", [("SBDF3", 65, 42, 12, 1e-5), ("ARS443", 33, 20, 10, 1e-5),
                                               ("CNAB2", 97, 42, 6, 1e-5), ("RK4", 33, 20, 8, 1e-6),
-                                              ("BPR353", 33, 20, 9, 1e-5)])
+                                              ("BPR353", 33, 20, 9, 1e-5), ("SBDF3", 65, 42, 200, 1e-5)])
 def test_sliced_contractions_match_fma_tiles(fg, scheme, R, Nm, B, dt):
     ras = np.geomspace(1e4, 1e6, B)
     ps = [fg.make_params(R, Nm, scheme, ra=float(ra), dt=dt) for ra in ras]
     seeds = list(range(100, 100 + B))
     a = run(fg, ps, seeds, 20, 1)
     f = run(fg, ps, seeds, 20, 0)
-    for i in range(B):
+    for i in (range(B) if B <= 12 else (0, 1, B // 2, B - 1)):
         for k in FIELDS:
             assert rel(a[i][k], f[i][k]) < 1e-12, (i, k, rel(a[i][k], f[i][k]))
 
