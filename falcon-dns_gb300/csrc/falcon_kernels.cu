@@ -218,6 +218,8 @@ __device__ void generic_stage(double2* A, double2* Bf, int P, int p, int m, int 
 
 template <int p>
 __device__ void dft_mma_stage(double2* A, double2* Bf, int P, int m, int lane, int warp, int nw);
+template <int p>
+__device__ void dft_mma_stage_wide(double2* A, double2* Bf, int P, int m, int lane, int warp, int nw);
 
 // MAXP bounds the radices compiled into one kernel instance, so a plan
 // with small radices is not held to the register budget of radix 31.
@@ -235,6 +237,15 @@ __device__ __forceinline__ void run_stage(int p, bool dif, bool twid, double2* A
       return;                                                                \
     }                                                                        \
     break;
+  if constexpr (MAXP == 31) {  // the wide primes of prime-factor plans on the tensor cores
+    if (!twid && (p == 19 || p == 23 || p == 29 || p == 31)) {
+      if (p == 19) dft_mma_stage_wide<19>(A, Bf, P, m, lane, 0, 1);
+      else if (p == 23) dft_mma_stage_wide<23>(A, Bf, P, m, lane, 0, 1);
+      else if (p == 29) dft_mma_stage_wide<29>(A, Bf, P, m, lane, 0, 1);
+      else dft_mma_stage_wide<31>(A, Bf, P, m, lane, 0, 1);
+      return;
+    }
+  }
   if constexpr (MAXP == 17) {  // plans with a prime above 17 keep the FMA butterflies
     if (!twid && (p == 11 || p == 13 || p == 17)) {
       if (p == 11) dft_mma_stage<11>(A, Bf, P, m, lane, 0, 1);
@@ -481,6 +492,158 @@ __device__ void dft_mma_stage(double2* A, double2* Bf, int P, int m, int lane, i
   }
 }
 
+// Wide odd-prime stage (p = 19, 23, 29, 31: h = 9..15) of a prime-factor
+// plan on the fp16 tensor cores: the same symmetric butterfly as
+// dft_mma_stage with the cos and sin products as two 16 x 16 tiles (rows
+// j, K = q, padded), 8 signed 8-bit slices per operand (64 bits) and the 36
+// pairs s + t <= 7 per tile; at most 15 products per output keep every FP32
+// sum exact, the dropped pairs weigh less than 2^-61 of the largest
+// product.  Lane (g, t) forms a_q, b_q for q = 2t + 1, 2t + 2, 2t + 9,
+// 2t + 10 of column g and receives A_j, B_j for j = g + 1 and g + 9 of
+// butterfly t.  FP64 instructions: ~34 per lane per tile of 4 butterflies,
+// against ~131 (p = 31) in dft_odd_store.
+template <int p>
+__device__ void dft_mma_stage_wide(double2* A, double2* Bf, int P, int m, int lane, int warp, int nw) {
+  constexpr int h = (p - 1) / 2;
+  static_assert(h > 8 && h <= 15, "two 16 x 16 tiles");
+  constexpr unsigned FULL = 0xffffffffu;
+  const int gid = lane >> 2, tig = lane & 3;
+  const int nb = P / p, mp = m * p, nbt = 2 * nb, ntile = (nbt + 3) / 4;
+  const float inv_m = 1.0f / (float)m;
+  const int qa = 2 * tig + 1;  // K rows 2t, 2t + 1 -> q = qa, qa + 1; rows 2t + 8, 2t + 9 -> q = qa + 8, qa + 9
+  // coefficient fragments of the cos (C) and sin (S) tiles: per slice
+  // [0] = (j0; qa, qa+1), [1] = (j1; qa, qa+1), [2] = (j0; qa+8, qa+9), [3] = (j1; qa+8, qa+9),
+  // j0 = g + 1, j1 = g + 9
+  uint32_t fc[kDwS][4], fs[kDwS][4];
+  int erc[2], ers[2];
+  {
+    double c[2][4], sn[2][4];  // [row j0 / j1][q slot]
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+      const int j = gid + 1 + 8 * r;
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const int q = qa + (i & 1) + 8 * (i >> 1);
+        const bool ok = j <= h && q <= h;
+        c[r][i] = ok ? DftTab<p>::c((j * q) % p) : 0.0;
+        sn[r][i] = ok ? DftTab<p>::s((j * q) % p) : 0.0;
+      }
+      int mc = 0, ms = 0;
+#pragma unroll
+      for (int i = 0; i < 4; ++i) { mc = max(mc, biased_exp(c[r][i])); ms = max(ms, biased_exp(sn[r][i])); }
+      mc = max(mc, __shfl_xor_sync(FULL, mc, 1));
+      mc = max(mc, __shfl_xor_sync(FULL, mc, 2));
+      ms = max(ms, __shfl_xor_sync(FULL, ms, 1));
+      ms = max(ms, __shfl_xor_sync(FULL, ms, 2));
+      erc[r] = mc - 1022;
+      ers[r] = ms - 1022;
+    }
+#pragma unroll
+    for (int f = 0; f < 4; ++f) {
+      const int r = f & 1, i0 = 2 * (f >> 1);
+      const unsigned long long c0 = dft_mag64(c[r][i0], erc[r]), c1 = dft_mag64(c[r][i0 + 1], erc[r]);
+      const unsigned long long s0 = dft_mag64(sn[r][i0], ers[r]), s1 = dft_mag64(sn[r][i0 + 1], ers[r]);
+      const uint32_t sgc = sign2(c[r][i0], c[r][i0 + 1]), sgs = sign2(sn[r][i0], sn[r][i0 + 1]);
+#pragma unroll
+      for (int sl = 0; sl < kDwS; ++sl) {
+        fc[sl][f] = dft_slice2w(c0, c1, sgc, sl);
+        fs[sl][f] = dft_slice2w(s0, s1, sgs, sl);
+      }
+    }
+  }
+  for (int tile = warp; tile < ntile; tile += nw) {
+    const int bi = tile * 4 + (gid >> 1), comp = gid & 1;
+    double av[4] = {0.0, 0.0, 0.0, 0.0}, bv[4] = {0.0, 0.0, 0.0, 0.0}, v0c = 0.0;
+    double* pi = nullptr;
+    if (bi < nbt) {
+      const int sel = bi >= nb, t = bi - sel * nb;
+      const int g = (int)(((float)t + 0.5f) * inv_m);
+      pi = reinterpret_cast<double*>((sel ? Bf : A) + g * mp + (t - g * m)) + comp;
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const int q = qa + (i & 1) + 8 * (i >> 1);
+        if (q <= h) {
+          const double x = pi[2 * q * m], y = pi[2 * (p - q) * m];
+          av[i] = x + y; bv[i] = x - y;
+        }
+      }
+      v0c = pi[0];
+    }
+    const int bo = tile * 4 + tig;
+    double2* po = nullptr;
+    double2 v0o = make_double2(0.0, 0.0);
+    if (bo < nbt) {
+      const int sel = bo >= nb, t = bo - sel * nb;
+      const int g = (int)(((float)t + 0.5f) * inv_m);
+      po = (sel ? Bf : A) + g * mp + (t - g * m);
+      v0o = po[0];
+    }
+    double ys = (av[0] + av[1]) + (av[2] + av[3]);
+    ys += __shfl_xor_sync(FULL, ys, 1);
+    ys += __shfl_xor_sync(FULL, ys, 2);
+    int fb = 0;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) fb = max(fb, max(biased_exp(av[i]), biased_exp(bv[i])));
+    fb = max(fb, __shfl_xor_sync(FULL, fb, 1));
+    fb = max(fb, __shfl_xor_sync(FULL, fb, 2));
+    const int ec = fb - 1022;
+    __syncwarp();  // every load of the tile precedes its stores
+    if (tig == 0 && pi) pi[0] = v0c + ys;
+    const int fre = __shfl_sync(FULL, fb, 8 * tig), fim = __shfl_sync(FULL, fb, 8 * tig + 4);
+    double o[2][4];  // [C / S][(j0 re, j0 im, j1 re, j1 im)]
+#pragma unroll
+    for (int part = 0; part < 2; ++part) {
+      const double* v = part ? bv : av;
+      uint32_t fx[kDwS][2];
+      {
+        const unsigned long long t0 = dft_mag64(v[0], ec), t1 = dft_mag64(v[1], ec), t2 = dft_mag64(v[2], ec),
+                                 t3 = dft_mag64(v[3], ec);
+        const uint32_t s01 = sign2(v[0], v[1]), s23 = sign2(v[2], v[3]);
+#pragma unroll
+        for (int sl = 0; sl < kDwS; ++sl) {
+          fx[sl][0] = dft_slice2w(t0, t1, s01, sl);
+          fx[sl][1] = dft_slice2w(t2, t3, s23, sl);
+        }
+      }
+      float acc[kDwD + 1][4];
+#pragma unroll
+      for (int d = 0; d <= kDwD; ++d)
+#pragma unroll
+        for (int i = 0; i < 4; ++i) acc[d][i] = 0.f;
+#pragma unroll
+      for (int sl = 0; sl < kDwS; ++sl) {
+        const uint32_t* f = part ? fs[sl] : fc[sl];
+#pragma unroll
+        for (int t = 0; t < kDwS && sl + t <= kDwD; ++t) mma_f16(acc[sl + t], f[0], f[1], f[2], f[3], fx[t][0], fx[t][1]);
+      }
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const int fcol = (i & 1) ? fim : fre;
+        const int er = part ? ers[i >> 1] : erc[i >> 1];
+        long long H = 0, L = 0;
+#pragma unroll
+        for (int d = 0; d <= 3; ++d) H = H * 256 + __float2int_rn(acc[d][i]);
+#pragma unroll
+        for (int d = 4; d <= kDwD; ++d) L = L * 256 + __float2int_rn(acc[d][i]);
+        const int kL = er + (fcol - 1022) - 72;
+        o[part][i] = oz_i64_scaled(H, kL + 32) + oz_i64_scaled(L, kL);
+        if (fcol == 2047) o[part][i] = __longlong_as_double(0x7ff8000000000000LL);
+      }
+    }
+    if (po) {
+#pragma unroll
+      for (int r = 0; r < 2; ++r) {
+        const int j = gid + 1 + 8 * r;
+        if (j <= h) {
+          const double ar = o[0][2 * r] + v0o.x, ai = o[0][2 * r + 1] + v0o.y;
+          po[j * m] = make_double2(ar + o[1][2 * r + 1], ai - o[1][2 * r]);
+          po[(p - j) * m] = make_double2(ar - o[1][2 * r + 1], ai + o[1][2 * r]);
+        }
+      }
+    }
+  }
+}
+
 // One stage of the block-per-line form: large odd primes of a prime-factor
 // plan through fft_stage_split over the whole block, the rest per buffer
 // half (run_stage1).  Called by every thread of the block.
@@ -488,6 +651,16 @@ template <int MAXP>
 __device__ __forceinline__ void run_stage_block(int p, bool dif, bool twid, double2* A, double2* Bf, double2* mine,
                                                 int P, int m, int stride, const double2* tw, int tid, int nt, int hl,
                                                 int nl) {
+  if constexpr (MAXP == 31) {
+    if (!twid && (p == 19 || p == 23 || p == 29 || p == 31)) {
+      if (p == 19) dft_mma_stage_wide<19>(A, Bf, P, m, tid & 31, tid >> 5, nt >> 5);
+      else if (p == 23) dft_mma_stage_wide<23>(A, Bf, P, m, tid & 31, tid >> 5, nt >> 5);
+      else if (p == 29) dft_mma_stage_wide<29>(A, Bf, P, m, tid & 31, tid >> 5, nt >> 5);
+      else dft_mma_stage_wide<31>(A, Bf, P, m, tid & 31, tid >> 5, nt >> 5);
+      __syncthreads();
+      return;
+    }
+  }
   if constexpr (MAXP == 17) {  // plans with a prime above 17 keep the FMA butterflies
     if (!twid && (p == 11 || p == 13 || p == 17)) {
       if (p == 11) dft_mma_stage<11>(A, Bf, P, m, tid & 31, tid >> 5, nt >> 5);

@@ -101,6 +101,35 @@ __device__ __forceinline__ uint32_t dft_slice2(unsigned long long tlo, unsigned 
   return *reinterpret_cast<const uint32_t*>(&v) ^ sgn;
 }
 
+// The wider odd primes (h = (p-1)/2 up to 15 products per output): 8 slices
+// of 8 bits (64 bits), pairs s + t <= 7 (8 pairs x 15 x 255^2 < 2^24).
+constexpr int kDwS = 8, kDwW = 8, kDwD = 7;
+
+// |a| * 2^(64 - e) truncated (< 2^64 when |a| < 2^e).
+__device__ __forceinline__ unsigned long long dft_mag64(double a, int e) {
+  const long long bits = __double_as_longlong(a);
+  const int eb = (int)((bits >> 52) & 0x7ff);
+  if (eb == 0) return 0ull;
+  const unsigned long long m = (unsigned long long)(bits & 0xfffffffffffffLL) | (1ull << 52);
+  const int sh = eb - 1011 - e;  // <= 11
+  if (sh >= 0) return m << sh;
+  if (sh <= -64) return 0ull;
+  return m >> (-sh);
+}
+
+// Slice s of two 64-bit magnitudes in the 8-bit format as an fp16 pair
+// (same construction as dft_slice2).
+__device__ __forceinline__ uint32_t dft_slice2w(unsigned long long tlo, unsigned long long thi, uint32_t sgn, int s) {
+  const int sh = kDwW * (kDwS - 1 - s);
+  const uint32_t biased = (((uint32_t)(tlo >> sh) & 255u) | (((uint32_t)(thi >> sh) & 255u) << 16)) + 0x66006600u;
+  const __half2 v = __hsub2(*reinterpret_cast<const __half2*>(&biased), __floats2half2_rn(1536.f, 1536.f));
+  return *reinterpret_cast<const uint32_t*>(&v) ^ sgn;
+}
+
+__device__ __forceinline__ uint32_t sign2(double lo, double hi) {
+  return (__double_as_longlong(lo) < 0 ? 0x8000u : 0u) | (__double_as_longlong(hi) < 0 ? 0x80000000u : 0u);
+}
+
 __device__ __forceinline__ void mma_f16(float (&c)[4], unsigned a0, unsigned a1, unsigned a2, unsigned a3,
                                         unsigned b0, unsigned b1) {
   asm volatile(

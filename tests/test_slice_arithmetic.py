@@ -6,8 +6,9 @@ Mirrors falcon-dns_gb300/csrc/falcon_slices.cuh: an FP64 value with
 slice pairs s + t <= D are summed per diagonal (the FP32 sums on the GPU,
 which must stay below 2^24 to be exact), then recombined as
 2^kH H + 2^kL L.  Operator GEMM formats (W, S, D) = (6, 10, 9) for K <= 257
-and (7, 9, 8) for K <= 112; the odd-prime DFT stage (9, 7, 6) with at most
-8 products per output."""
+and (7, 9, 8) for K <= 112; the odd-prime DFT stages (9, 7, 6) with at
+most 8 products per output (p <= 17) and (8, 8, 7) with at most 15
+(p = 19 .. 31)."""
 import math
 import random
 import struct
@@ -15,7 +16,8 @@ from fractions import Fraction
 
 import pytest
 
-FORMATS = {6: dict(S=10, D=9, HD=4, MAGB=60), 7: dict(S=9, D=8, HD=3, MAGB=63), 9: dict(S=7, D=6, HD=2, MAGB=63)}
+FORMATS = {6: dict(S=10, D=9, HD=4, MAGB=60), 7: dict(S=9, D=8, HD=3, MAGB=63), 9: dict(S=7, D=6, HD=2, MAGB=63),
+           8: dict(S=8, D=7, HD=3, MAGB=64)}
 
 
 def bexp(x):
@@ -77,7 +79,7 @@ def test_sliced_dot_is_exact_to_one_rounding(W, K):
         assert abs(Fraction(y) - exact) <= bound
 
 
-@pytest.mark.parametrize("p", [11, 13, 17])
+@pytest.mark.parametrize("p", [11, 13, 17, 19, 31])
 def test_dft_butterfly_sums(p):
     # A_j = sum_q a_q cos(2 pi jq/p) and B_j = sum_q b_q sin(2 pi jq/p) of the
     # symmetric odd-prime butterfly through the 9-bit format
@@ -96,7 +98,7 @@ def test_dft_butterfly_sums(p):
                 # append it with a zero coefficient
                 col = max(map(abs, a + b))
                 for vals, coef in ((a, c), (b, s)):
-                    y, qmax = sliced_dot(coef + [0.0], vals + [col], 9)
+                    y, qmax = sliced_dot(coef + [0.0], vals + [col], 9 if h <= 8 else 8)
                     assert qmax < 2 ** 24
                     exact = sum(Fraction(u) * Fraction(w) for u, w in zip(coef, vals))
                     assert abs(Fraction(y) - exact) <= abs(exact) * Fraction(1, 2 ** 52) + Fraction(col) * Fraction(1, 2 ** 57)
