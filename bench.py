@@ -55,6 +55,28 @@ def dist_info():
     return rank, world, local
 
 
+def max_over_ranks(x, world, device):
+    """The largest x over the ranks of the process group (x itself alone):
+    the timed region ends when the slowest rank ends."""
+    if world <= 1:
+        return float(x)
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(world, n_per_rank, steps, ms):
+    """Instance-steps per second of the whole job: every rank steps its own
+    shard of n_per_rank instances `steps` times in `ms` (the max over ranks)."""
+    return world * n_per_rank * steps / (ms / 1e3)
+
+
+def shard(rank, n):
+    """Rank `rank`'s instances: Ra values and noise seeds of its own shard."""
+    return workload_ras(n, rank), [WORKLOAD["noise_seed0"] + rank * n + k for k in range(n)]
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
 
@@ -378,9 +400,8 @@ def run_gpu(args):
     stream = torch.cuda.Stream()
     W = WORKLOAD
     n = args.instances or W["n"]
-    ras = workload_ras(n, rank)
+    ras, seeds = shard(rank, n)
     params = [fg.make_params(W["nr"], W["nm"], W["scheme"], ra=ra, dt=W["dt"], pr=W["pr"]) for ra in ras]
-    seeds = [W["noise_seed0"] + rank * n + k for k in range(n)]
     peak = fg.fp64_peak_gflops()
     mma_peak = fg.fp64_mma_peak_gflops()
 
@@ -403,11 +424,8 @@ def run_gpu(args):
         torch.cuda.synchronize()
     ms = ev0.elapsed_time(ev1)
     launches = fg.launch_count() - launches0
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * n * args.steps / (ms / 1e3)
+    ms = max_over_ranks(ms, world, "cuda")
+    value = whole_job_rate(world, n, args.steps, ms)
     finite = all(np.isfinite(b.get_state(i)["T"]).all() for i in (0, n - 1))
 
     # ---- kernel classes (CUDA events per launch on the same stream) ----
