@@ -429,6 +429,7 @@ def run_gpu(args):
     finite = all(np.isfinite(b.get_state(i)["T"]).all() for i in (0, n - 1))
 
     # ---- kernel classes (CUDA events per launch on the same stream) ----
+    ngroups = b.ngroups
     prof = b.profile(3)
     tot = sum(v["ms"] for v in prof.values())
     # the launch classes by kernel function: both GEMM classes are launches
@@ -442,7 +443,9 @@ def run_gpu(args):
         if t is None:
             e["traffic_ok"] = False
         else:
-            e["traffic_sum"] += t * v["launches"]
+            # profiles/traffic.json holds bytes per call of a 256-instance
+            # group; a call here covers one group of n / ngroups instances
+            e["traffic_sum"] += t * (n / ngroups) / 256.0 * v["launches"]
     dom = max(kern, key=lambda k: kern[k]["ms"])
 
     tpeak, tpeak_src = tensor_peak()
@@ -553,7 +556,11 @@ def run_gpu(args):
         "config": {"workload": WORKLOAD_NAME, "instances_per_gpu": n, "nr": W["nr"], "nm": W["nm"],
                    "np": 3 * W["nm"], "scheme": W["scheme"], "dt": W["dt"],
                    "l2": "working set ~1.1 GB per GPU, larger than L2 (129 MB); no flush needed",
-                   "parallelism": f"replicas x{world}"},
+                   "parallelism": f"replicas x{world}",
+                   "groups_per_gpu": ngroups,
+                   "groups": "the instances run as groups of at most 128 sharing the operators, one stream each "
+                             "(falcon_set_max_group_size default), so one group's nonlinear pass overlaps "
+                             "another's contractions; the roofline classes time the groups one after another"},
         "one_at_a_time": {"value": one_rate, "unit": "instance-steps/s", "instances": n1, "steps": k1,
                           "batched_over_one_at_a_time": value / world / one_rate},
         "e2e": e2e,

@@ -93,7 +93,7 @@ EXPORTS = (
     "falcon_create", "falcon_destroy", "falcon_init_state", "falcon_set_state", "falcon_get_state",
     "falcon_step", "falcon_diagnostics", "falcon_batch_create", "falcon_batch_destroy",
     "falcon_batch_size", "falcon_batch_ngroups", "falcon_batch_init_state", "falcon_batch_set_state",
-    "falcon_batch_set_states",
+    "falcon_batch_set_states", "falcon_set_max_group_size",
     "falcon_batch_get_state", "falcon_batch_step", "falcon_batch_diagnostics", "falcon_batch_set_stream",
     "falcon_batch_device_bytes", "falcon_nonlin_dev", "falcon_nonlin", "falcon_getrs_batched_dev",
     "falcon_cheb_fwd_dev", "falcon_cheb_inv_dev", "falcon_cheb_d1_dev", "falcon_cheb_d2_dev",
@@ -138,6 +138,7 @@ def lib():
     L.falcon_batch_init_state.argtypes = [vp, ip, ctypes.c_double, P(ctypes.c_uint64)]
     L.falcon_batch_set_state.argtypes = [vp, ip, dp, dp, dp, dp]
     L.falcon_batch_set_states.argtypes = [vp, dp, dp, dp, dp]
+    L.falcon_set_max_group_size.argtypes = [ip]
     L.falcon_batch_get_state.argtypes = [vp, ip, dp, dp, dp, dp, dp]
     L.falcon_batch_step.argtypes = [vp, ip]
     L.falcon_batch_diagnostics.argtypes = [vp, P(FalconDiag)]
@@ -433,6 +434,13 @@ def fp64_mma_peak_gflops():
 
 def launch_count():
     return lib().falcon_launch_count()
+
+
+def set_max_group_size(n):
+    """Largest group of batches created afterwards (default 128; 0: one group
+    per operator key); groups of one key share operators and run on separate
+    streams.  Returns the previous value."""
+    return lib().falcon_set_max_group_size(int(n))
 
 
 def set_gemm_mode(mode):

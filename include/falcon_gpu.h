@@ -181,6 +181,14 @@ int falcon_store_snapshot(falcon_handle* h, const char* path);
 /* Instances are grouped by operator key (Nr, Nm, mBC, scheme, dt, Pr);
  * each group shares its implicit operators. */
 int falcon_batch_create(const falcon_params* params, int n, falcon_batch** out);
+/* Batches created after the call split the instances of one operator key
+ * into balanced groups of at most n instances (default 128; 0: one group
+ * per key).  The groups share the operators and step on separate streams,
+ * so one group's nonlinear pass (FP64 pipe) can run beside another's
+ * operator contractions (tensor cores).  Results do not change.  Returns
+ * the previous value.  No reference counterpart (the reference steps one
+ * run). */
+int falcon_set_max_group_size(int n);
 void falcon_batch_destroy(falcon_batch* b);
 int falcon_batch_size(const falcon_batch* b);
 int falcon_batch_ngroups(const falcon_batch* b);
@@ -272,8 +280,8 @@ int falcon_server_poll(falcon_server* s, int64_t id, int* done, falcon_diag* out
 
 /* ---- measurement hooks ---- */
 /* Per-kernel-class statistics of `nsteps` steps of a batch, timed with CUDA
- * events around every launch on the batch's stream (the steps advance the
- * state like falcon_batch_step).  flops is the algorithmic FP64 operation
+ * events around every launch on its group's stream, the groups of a step
+ * one after another (the steps advance the state like falcon_batch_step).  flops is the algorithmic FP64 operation
  * count of the launches: 2*rows*K*N per GEMM, 5 P log2 P per complex FFT of
  * length P (four per radial line) plus the grid products. */
 typedef struct falcon_kernel_stat {

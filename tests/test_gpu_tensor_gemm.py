@@ -29,11 +29,12 @@ def run(fg, params, seeds, nsteps, mode):
 
 
 # Batches up to a few dozen instances take the kernel that slices its own X
-# columns (N x batch <= 16384 columns); the 200-instance case takes the slice
-# planes of oz_slice_cols_kernel, as the bench's 256-instance batch does.
+# columns (N x batch <= 16384 columns); the 200-instance case (two groups of
+# 100, N x batch = 200 x 86 per-mode columns) takes the slice planes of
+# oz_slice_cols_kernel, as the bench's 256-instance batch does.
 @pytest.mark.parametrize("scheme,R,Nm,B,dt", [("SBDF3", 65, 42, 12, 1e-5), ("ARS443", 33, 20, 10, 1e-5),
                                               ("CNAB2", 97, 42, 6, 1e-5), ("RK4", 33, 20, 8, 1e-6),
-                                              ("BPR353", 33, 20, 9, 1e-5), ("SBDF3", 65, 42, 200, 1e-5)])
+                                              ("BPR353", 33, 20, 9, 1e-5), ("SBDF3", 65, 85, 200, 1e-5)])
 def test_sliced_contractions_match_fma_tiles(fg, scheme, R, Nm, B, dt):
     ras = np.geomspace(1e4, 1e6, B)
     ps = [fg.make_params(R, Nm, scheme, ra=float(ra), dt=dt) for ra in ras]
