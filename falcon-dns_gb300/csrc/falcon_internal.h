@@ -141,9 +141,9 @@ struct GemmArgs {
 // Slice products are exact in bf16 x bf16 -> FP32 and their sums stay
 // below 2^24 (exact); the pairs s + t <= D are summed per s + t and
 // recombined in 64-bit integers and one FP64 add.  Formats: W = 6 (S = 10,
-// D = 9) for K <= 257, W = 7 (S = 9, D = 8) for K <= 112.  kOzS is the
-// largest slice count (buffer sizes).
-constexpr int kOzS = 10, kOzW = 6, kOzD = 9;
+// D = 9) for K <= 257, W = 7 (S = 9, D = 8) for K <= 112 (OzCfg in
+// falcon_slices.cuh).  kOzS is the largest slice count (buffer sizes).
+constexpr int kOzS = 10;
 inline int oz_width_for(int KP) { return KP <= 112 ? 7 : 6; }
 // Contractions of operators of 5 to 8 row tiles (65 <= rows <= 128) with
 // few columns in all (N x batch <= 16384: one instance, small groups) take a

@@ -137,14 +137,15 @@ __device__ __forceinline__ void ldsm_x2t(unsigned (&r)[2], const void* p) {
 
 }  // namespace
 
-// Tiled slice GEMM.  Block: MT row tiles (16 rows) x NQ column groups (16
-// columns), each (row tile, column group) taken by 2 / NT warps of NT 16x8
-// tiles each; K in chunks of 16 staged in shared memory by cp.async two
-// chunks deep (slices of A and X for all kOzS slices of the chunk);
-// fragments by ldmatrix from padded rows (48 and NQ*32+16 bytes:
-// conflict-free).  Per chunk a warp does the 55 slice-pair products
-// s + t <= kOzD on each of its tiles.  NT = 1 halves the accumulator
-// registers (10 diagonals x 4 per tile), so twice the warps fit on an SM.
+// Tiled slice GEMM (format W, OzCfg<W>).  Block: MT row tiles (16 rows) x
+// NQ column groups (16 columns), each (row tile, column group) taken by
+// 2 / NT warps of NT 16x8 tiles each; K in chunks of 16 staged in shared
+// memory by cp.async two chunks deep (slices of A and X for all S slices of
+// the chunk); fragments by ldmatrix from padded rows (48 and NQ*32+16 bytes:
+// conflict-free).  Per chunk a warp does the slice-pair products s + t <= D
+// (55 for W = 6, 45 for W = 7) on each of its tiles.  NT = 1 halves the
+// accumulator registers (D + 1 diagonals x 4 per tile), so twice the warps
+// fit on an SM.
 // FX: the block cuts its own X columns (all of K, from the FP64 operand)
 // into slice planes resident in shared memory, with the column exponents,
 // instead of reading planes made by oz_slice_cols_kernel: the same slices,

@@ -54,10 +54,6 @@ __device__ __forceinline__ uint32_t oz_slice_w(unsigned long long T, bool neg, i
   return bf16_bits_of_int(neg ? -q : q);
 }
 
-// An exact FP32 integer sum (|x| < 2^22) as an int: x + 1.5 2^23 puts the
-// integer in the low mantissa bits.
-__device__ __forceinline__ int oz_f32_int(float x) { return __float_as_int(x + 12582912.0f) - 0x4B400000; }
-
 // v 2^k for |v| < 2^53 built from its bits (integer instructions only:
 // no FP64 pipe), when the result is a normal number; else from ldexp.
 __device__ __forceinline__ double oz_i64_scaled(long long v, int k) {
