@@ -10,6 +10,7 @@
 #include <stdio.h>
 
 #include <algorithm>
+#include <atomic>
 #include <unordered_map>
 
 #include "falcon_internal.h"
@@ -63,17 +64,16 @@ static cudaError_t set_tab(const void* csym, const void* ssym) {
 }
 
 cudaError_t init_dft_tables() {
-  static bool done = false;
-  static int done_dev = -1;
+  static std::atomic<bool> done[64];  // tables uploaded, per device
   int dev = 0;
   cudaGetDevice(&dev);
-  if (done && done_dev == dev) return cudaSuccess;
+  if (dev >= 0 && dev < 64 && done[dev].load()) return cudaSuccess;
   cudaError_t e = cudaSuccess;
 #define FALCON_SET(p) if (e == cudaSuccess) e = set_tab<p>(kC##p, kS##p);
   FALCON_SET(3) FALCON_SET(5) FALCON_SET(7) FALCON_SET(11) FALCON_SET(13)
   FALCON_SET(17) FALCON_SET(19) FALCON_SET(23) FALCON_SET(29) FALCON_SET(31)
 #undef FALCON_SET
-  if (e == cudaSuccess) { done = true; done_dev = dev; }
+  if (e == cudaSuccess && dev >= 0 && dev < 64) done[dev].store(true);
   return e;
 }
 
@@ -1127,14 +1127,14 @@ __global__ void __launch_bounds__(32) gemv_kernel(GemmArgs g) {
 template <int RPT, int NCOL>
 static cudaError_t launch_tile(const GemmArgs& g, int nw, int row_blocks, cudaStream_t s) {
   // two K-chunk buffers; above 48 KB the kernel is opted in once per device
-  static bool opted[64] = {false};
+  static std::atomic<bool> opted[64];
   int dev = 0;
   cudaGetDevice(&dev);
-  if (dev >= 0 && dev < 64 && !opted[dev]) {
+  if (!(dev >= 0 && dev < 64 && opted[dev].load())) {
     const cudaError_t e = cudaFuncSetAttribute(gemm_tile_kernel<RPT, NCOL>,
                                                cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024);
     if (e != cudaSuccess) return e;
-    opted[dev] = true;
+    if (dev >= 0 && dev < 64) opted[dev].store(true);
   }
   dim3 grid((g.N + NCOL - 1) / NCOL, row_blocks, g.batch);
   const size_t smem = (size_t)2 * kKC * (nw * (64 / NCOL) * RPT + NCOL) * sizeof(double);

@@ -28,6 +28,8 @@
 #include <cuda_bf16.h>
 #include <stdint.h>
 
+#include <atomic>
+
 #include "falcon_internal.h"
 #include "falcon_slices.cuh"
 
@@ -299,14 +301,14 @@ static cudaError_t launch_oz_w(const GemmArgs& g, cudaStream_t s) {
                (size_t)(NQ * 16) * (1 + NG) * sizeof(int)
          : 2 * ((size_t)S * MT * 16 * 24 + (size_t)S * 16 * XROW) * sizeof(uint16_t);
   if (smem > 227 * 1024) return cudaErrorInvalidValue;
-  static int opted[64] = {0};  // shared-memory size opted in, per device
+  static std::atomic<bool> opted[64];  // opted in to the largest shared memory, per device
   int dev = 0;
   cudaGetDevice(&dev);
-  if (dev >= 0 && dev < 64 && opted[dev] < (int)smem) {
+  if (!(dev >= 0 && dev < 64 && opted[dev].load())) {
     const cudaError_t e = cudaFuncSetAttribute(oz_mma_kernel<MT, NQ, NT, MINB, W, FX>,
                                                cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
     if (e != cudaSuccess) return e;
-    opted[dev] = 227 * 1024;
+    if (dev >= 0 && dev < 64) opted[dev].store(true);
   }
   dim3 grid((g.N + NQ * 16 - 1) / (NQ * 16), (g.rows + MT * 16 - 1) / (MT * 16), g.batch);
   oz_mma_kernel<MT, NQ, NT, MINB, W, FX><<<grid, 32 * MT * NQ * (2 / NT), smem, s>>>(g);
