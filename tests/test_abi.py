@@ -85,3 +85,14 @@ def test_no_cpu_fallback_without_gpu(fg):
         pytest.skip("a GPU is present")
     with pytest.raises(fg.FalconError, match="no CPU fallback"):
         fg.Instance(fg.make_params(9, 4))
+
+
+def test_process_wide_switches_round_trip(fg):
+    # defaults: sliced tensor-core contractions, step graphs, groups of <= 128
+    L = fg.lib()
+    assert fg.set_gemm_mode(0) == 1 and fg.set_gemm_mode(1) == 0
+    assert fg.set_max_group_size(64) == 128
+    assert fg.set_max_group_size(-5) == 64      # negative means one group per key
+    assert fg.set_max_group_size(128) == 0
+    L.falcon_set_step_graphs.argtypes = [ctypes.c_int]
+    assert L.falcon_set_step_graphs(0) == 1 and L.falcon_set_step_graphs(1) == 0
