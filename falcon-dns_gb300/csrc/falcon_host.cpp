@@ -748,6 +748,20 @@ int scheme_weights(int type, int imp, int exp, Scheme* s) {
 // ---------------------------------------------------------------------------
 // Azimuthal FFT plan (P = 3 Nm) and its device tables
 // ---------------------------------------------------------------------------
+}  // namespace
+
+void falcon::fft_tables_host(const FftPlan& plan, double2* tw, int* pos) {
+  const int P = plan.P;
+  const double two_pi = 8.0 * std::atan(1.0);
+  for (int i = 0; i < P; ++i) {
+    pos[i] = fft_position(plan, i);
+    const double a = two_pi * (double)i / (double)P;
+    tw[i] = make_double2(std::cos(a), -std::sin(a));
+  }
+}
+
+namespace {
+
 struct FftTables {
   FftPlan plan{};
   double2* tw = nullptr;
@@ -760,13 +774,8 @@ int make_fft(int P, std::unique_ptr<FftTables>* out) {
   if (make_fft_plan(P, &f->plan) != 0)
     return fail(FALCON_EINVAL, "azimuthal length 3*Nm has a prime factor above 64 or too many factors");
   std::vector<int> pos(P);
-  for (int i = 0; i < P; ++i) pos[i] = fft_position(f->plan, i);
   std::vector<double2> tw(P);
-  const double two_pi = 8.0 * std::atan(1.0);
-  for (int i = 0; i < P; ++i) {
-    const double a = two_pi * (double)i / (double)P;
-    tw[i] = make_double2(std::cos(a), -std::sin(a));
-  }
+  fft_tables_host(f->plan, tw.data(), pos.data());
   int rc;
   if ((rc = upload(&f->tw, tw, nullptr))) return rc;
   if ((rc = upload(&f->pos, pos, nullptr))) return rc;

@@ -99,6 +99,12 @@ inline int fft_position(const FftPlan& f, int k) {
   return pp;
 }
 
+// Tables of the transform of length plan.P, built on the host (falcon_host.cpp):
+// tw[k] = exp(-2 pi i k/P) from the host's cos/sin and pos[k] =
+// fft_position(plan, k).  Every entry point that runs the nonlinear pass
+// takes its tables from here, so they all use the same bits.
+void fft_tables_host(const FftPlan& plan, double2* tw, int* pos);
+
 // Arguments of the nonlinear-pass kernel (Nr_maxLOOP, src/nonlin.F90:35-91).
 struct NonlinArgs {
   int R, M, B, Nm;

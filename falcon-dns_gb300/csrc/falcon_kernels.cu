@@ -11,6 +11,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <mutex>
 #include <unordered_map>
 
 #include "falcon_internal.h"
@@ -1075,7 +1076,7 @@ __global__ void __launch_bounds__(512) gemm_tile_kernel(GemmArgs g) {
 
 // Small-N form (N <= 8 columns per batch entry): one thread per output row.
 template <int NC>
-__global__ void __launch_bounds__(32) gemv_kernel(GemmArgs g) {
+__global__ void __launch_bounds__(32) dfma_gemv_kernel(GemmArgs g) {
   extern __shared__ double xs[];  // K x NC
   const int z = blockIdx.y;
   const double* A = g.A + (size_t)z * g.sA;
@@ -1214,9 +1215,9 @@ cudaError_t launch_gemm(const GemmArgs& g, cudaStream_t s) {
     // one warp of rows per block, so small problems spread over the SMs
     dim3 grid((g.rows + 31) / 32, g.batch);
     const size_t sm = (size_t)g.K * 8 * sizeof(double);
-    if (g.N <= 2) gemv_kernel<2><<<grid, 32, (size_t)g.K * 2 * sizeof(double), s>>>(g);
-    else if (g.N <= 4) gemv_kernel<4><<<grid, 32, (size_t)g.K * 4 * sizeof(double), s>>>(g);
-    else gemv_kernel<8><<<grid, 32, sm, s>>>(g);
+    if (g.N <= 2) dfma_gemv_kernel<2><<<grid, 32, (size_t)g.K * 2 * sizeof(double), s>>>(g);
+    else if (g.N <= 4) dfma_gemv_kernel<4><<<grid, 32, (size_t)g.K * 4 * sizeof(double), s>>>(g);
+    else dfma_gemv_kernel<8><<<grid, 32, sm, s>>>(g);
     return cudaGetLastError();
   }
   static int nsm_dev[64] = {0};
@@ -1828,31 +1829,36 @@ constexpr size_t kNoAllocScratchBytes = (size_t)kNoAllocMaxP * (sizeof(double2) 
 static __device__ __align__(256) unsigned char g_nonlin_scratch[kNoAllocScratchBytes];
 
 // Per-device address of g_nonlin_scratch (host code may not use the symbol
-// itself as a device pointer).
+// itself as a device pointer), looked up once per device under a
+// std::once_flag, so host threads making their first call together do not
+// race on it.
+static std::once_flag g_scratch_once[64];
 static void* g_scratch_addr[64] = {nullptr};
 
-// tw[k] = exp(-2 pi i k/P); pos[n] = sum_s d_s(n) P/(p_0..p_s) for the radices
-// of `plan`, written into the scratch array.
-__global__ void noalloc_tables_kernel(FftPlan plan, double2* tw, int* pos) {
-  const int P = plan.P;
-  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < P; k += gridDim.x * blockDim.x) {
-    double s, c;
-    sincospi(-2.0 * (double)k / (double)P, &s, &c);
-    tw[k] = make_double2(c, s);
-    pos[k] = fft_position(plan, k);
-  }
-}
+// Host staging of the tables: filled and copied under the mutex.  A copy from
+// pageable host memory has consumed its source when cudaMemcpyAsync returns,
+// so the buffer is free again once the copies are issued.
+static std::mutex g_noalloc_host_mu;
+static double2 g_noalloc_tw_h[kNoAllocMaxP];
+static int g_noalloc_pos_h[kNoAllocMaxP];
 
 }  // namespace falcon
 
 extern "C" const char* falcon_last_error(void);
 namespace falcon { int set_error_message(const char* msg); }
 
-// Same computation and device layout as falcon_nonlin_dev, without any
-// device allocation: the FFT tables go to a fixed static device array.
+// Same computation, device layout and bits as falcon_nonlin_dev, without any
+// device allocation: the FFT tables are built on the host by the same code
+// as the allocating form (fft_tables_host) and copied into a fixed static
+// device array.
+//  - Asynchronous on `stream`: the call returns once the table copies and
+//    the kernel are queued (the table copies, from pageable host memory,
+//    wait for earlier work on the stream).  Synchronise the stream before
+//    reading the outputs; a kernel fault is reported there, not in the
+//    return code.  (falcon_nonlin_dev synchronises before it returns.)
 //  - The first call on a device looks up that device's address of the array
-//    (cudaGetSymbolAddress, with the device current); make that first call
-//    before any stream capture on that device.
+//    (cudaGetSymbolAddress, with the device current, once per device); make
+//    that first call before any stream capture on that device.
 //  - Every call overwrites the whole table region it uses, so no state
 //    carries over between calls; but all calls on a device share the one
 //    array, so calls whose kernels overlap on the GPU (different streams, or
@@ -1878,14 +1884,13 @@ extern "C" int falcon_nonlin_noalloc_dev(int nr, int nm, int nb, const double* t
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess || dev < 0 || dev >= 64) { set_error_message("falcon_nonlin_noalloc_dev: no current device"); return -2; }
-  if (!g_scratch_addr[dev]) {
+  std::call_once(g_scratch_once[dev], [dev] {
     void* ptr = nullptr;
-    e = cudaGetSymbolAddress(&ptr, g_nonlin_scratch);
-    if (e != cudaSuccess || !ptr) {
-      set_error_message("falcon_nonlin_noalloc_dev: cudaGetSymbolAddress failed");
-      return -2;
-    }
-    g_scratch_addr[dev] = ptr;
+    if (cudaGetSymbolAddress(&ptr, g_nonlin_scratch) == cudaSuccess) g_scratch_addr[dev] = ptr;
+  });
+  if (!g_scratch_addr[dev]) {
+    set_error_message("falcon_nonlin_noalloc_dev: cudaGetSymbolAddress failed on this device");
+    return -2;
   }
   e = init_dft_tables();
   if (e != cudaSuccess) { set_error_message(cudaGetErrorString(e)); return -2; }
@@ -1893,8 +1898,13 @@ extern "C" int falcon_nonlin_noalloc_dev(int nr, int nm, int nb, const double* t
   int* pos = reinterpret_cast<int*>(reinterpret_cast<unsigned char*>(g_scratch_addr[dev]) +
                                     (size_t)kNoAllocMaxP * sizeof(double2));
   cudaStream_t s = (cudaStream_t)stream;
-  noalloc_tables_kernel<<<(P + 255) / 256, 256, 0, s>>>(plan, tw, pos);
-  e = cudaGetLastError();
+  {
+    std::lock_guard<std::mutex> lk(g_noalloc_host_mu);
+    fft_tables_host(plan, g_noalloc_tw_h, g_noalloc_pos_h);
+    e = cudaMemcpyAsync(tw, g_noalloc_tw_h, sizeof(double2) * (size_t)P, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(pos, g_noalloc_pos_h, sizeof(int) * (size_t)P, cudaMemcpyHostToDevice, s);
+  }
   if (e != cudaSuccess) { set_error_message(cudaGetErrorString(e)); return -2; }
   NonlinArgs a{};
   a.R = nr; a.M = nm + 1; a.B = nb; a.Nm = nm;

@@ -8,8 +8,8 @@
  * `Nr_maxLOOP` (src/nonlin.F90:35) followed by the per-mode implicit solves
  * (`Nm_maxLOOP`, src/fourierloop.F90:156; `Get_stage_var`,
  * src/fourierloop_imexrk.F90:75).  This header is the drop-in boundary a
- * Fortran host binds through ISO_C_BINDING and the C++
- * driver and Python harness bind directly.
+ * Fortran host binds through ISO_C_BINDING, and that the C++ driver
+ * `falcon_run` and the Python harness bind directly.
  *
  * Conventions
  *  - Every call returns 0 on success or a negative FALCON_E* code; the text
@@ -232,14 +232,18 @@ int falcon_nonlin_dev(int nr, int nm, int nb, const double* t_dev, const double*
                       const double* up_dev, const double* ur_dev, double* uphi_t_dev,
                       double* ur_t_dev, double* uphi_omg_dev, double* ur_omg_dev, void* stream);
 /* Allocation-free form of falcon_nonlin_dev (no counterpart in the
- * reference): same arguments, layout and results, but the library allocates
- * no device memory -- its FFT tables go to a fixed 80 KiB static device
- * array -- for hosts that own all device memory through their own budgeted
- * pool, or that step in loops where cudaMalloc/cudaFree would synchronise
- * the device.  Limit: 3*nm <= 4096, else FALCON_EINVAL.  The first call on a
- * device resolves the array's device address (make it before any stream
- * capture); every call overwrites the table region it uses; calls whose
- * kernels overlap on the GPU share the array and race, so serialise them. */
+ * reference): same arguments, layout and bits, but the library allocates no
+ * device memory -- its FFT tables are built on the host and copied into a
+ * fixed 80 KiB static device array -- for hosts that own all device memory
+ * through their own budgeted pool, or that step in loops where
+ * cudaMalloc/cudaFree would synchronise the device.  Limit: 3*nm <= 4096,
+ * else FALCON_EINVAL.  Unlike falcon_nonlin_dev it is asynchronous on
+ * `stream`: it returns once the table copies and the kernel are queued, so
+ * synchronise the stream before reading the outputs (a kernel fault shows
+ * there, not in the return code).  The first call on a device resolves the
+ * array's device address (make it before any stream capture); every call
+ * overwrites the table region it uses; calls whose kernels overlap on the
+ * GPU share the array and race, so serialise them. */
 int falcon_nonlin_noalloc_dev(int nr, int nm, int nb, const double* t_dev, const double* omg_dev,
                               const double* up_dev, const double* ur_dev, double* uphi_t_dev,
                               double* ur_t_dev, double* uphi_omg_dev, double* ur_omg_dev, void* stream);

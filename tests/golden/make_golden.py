@@ -1,7 +1,8 @@
 """Generate the golden vectors that pin the CPU oracle to the reference.
 
-Run in a container where the FAlCon-DNS reference tree is mounted (default
-/root/reference, override with FALCON_REFERENCE).  It imports the
+Run where the FAlCon-DNS reference tree is available, with the environment
+variable FALCON_REFERENCE naming its root (the directory holding src/ and
+python/).  It imports the
 reference's own Python restatement of the Chebyshev transforms
 (python/annulus/cheblib.py: chebtransform, chebinvtran, chebinvtranD1,
 chebinvtranD2, lines 467-585) and evaluates them on seeded inputs.  The
@@ -17,7 +18,9 @@ import os
 import numpy as np
 import scipy.linalg.lapack as lapack
 
-REF = os.environ.get("FALCON_REFERENCE", "/root/reference")
+REF = os.environ.get("FALCON_REFERENCE")
+if not REF or not os.path.isdir(os.path.join(REF, "src")):
+    raise SystemExit("set FALCON_REFERENCE to the root of the FAlCon-DNS source tree")
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 

@@ -1,8 +1,9 @@
 """Generate tests/golden/imexrk_tables.json: every IMEXRK Butcher pair of the
 reference evaluated in IEEE double from its own Fortran source.
 
-Run in a container where the FAlCon-DNS reference tree is mounted (default
-/root/reference, override with FALCON_REFERENCE).  The script reads
+Run where the FAlCon-DNS reference tree is available, with the environment
+variable FALCON_REFERENCE naming its root (the directory holding src/ and
+python/).  The script reads
 src/timeschemes.F90 as text (nothing of the reference is executed):
 
   init_time_schemes      (:37-973)    the named constants of each scheme
@@ -30,7 +31,9 @@ import re
 
 import numpy as np
 
-REF = os.environ.get("FALCON_REFERENCE", "/root/reference")
+REF = os.environ.get("FALCON_REFERENCE")
+if not REF or not os.path.isdir(os.path.join(REF, "src")):
+    raise SystemExit("set FALCON_REFERENCE to the root of the FAlCon-DNS source tree")
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 IDENT = re.compile(r"(?<![\w.])([A-Za-z]\w*)")
