@@ -394,6 +394,16 @@ int upload(T** dst, const std::vector<T>& v, size_t* acc) {
   return 0;
 }
 
+// LU factors and 1-based pivots of the implicit operators made by the
+// caller's own mat_build* + dgetrf, in the reference's layouts
+// (src/mat_assembly.F90): AT_all (R,R,M), IPIV1 (R,M); AF_all (2R,2R,M),
+// IPIV2 (2R,M); A_uphi_all (R,R,1), IPIV_uphi (R); LAPpsi_all (R,R,M),
+// IPIV1_lap (R,M).  A null block is built on the device instead.
+struct HostFactors {
+  const double *AT = nullptr, *AF = nullptr, *Au = nullptr, *LAP = nullptr;
+  const int *pT = nullptr, *pF = nullptr, *pu = nullptr, *pL = nullptr;
+};
+
 // The per-mode combined operators of one key, built on the device:
 //   ST[m] = chebinvtran o AT_m^-1                          (R x R)
 //   G[m]  = [chebinvtran; chebinvtran; -chebinvtranD1] o the omega, psi and
@@ -402,7 +412,7 @@ int upload(T** dst, const std::vector<T>& v, size_t* acc) {
 // Factorisations: batched dgetf2/dgetrs (falcon_ops.cu) on modes in chunks
 // that keep the workspace near 256 MB.  Products: the DFMA GEMM.  G[0] and
 // LAP[0] stay zero (the m = 0 flow is the u_phi_bar equation).
-int build_mode_operators(const OpKey& k, const Cheb& c, OpSet* ops) {
+int build_mode_operators(const OpKey& k, const Cheb& c, OpSet* ops, const HostFactors* hf) {
   const int R = c.R, M = k.Nm + 1;
   const size_t RR = (size_t)R * R;
   cudaStream_t s = nullptr;
@@ -430,10 +440,10 @@ int build_mode_operators(const OpKey& k, const Cheb& c, OpSet* ops) {
   const int mc = (int)std::max<size_t>(1, std::min<size_t>((size_t)M, ((size_t)256 << 20) / (per_mode * 8)));
   double *d_t = nullptr, *d_D = nullptr, *d_D2 = nullptr, *d_ir = nullptr, *d_ir2 = nullptr, *d_tinv = nullptr,
          *d_mdinv = nullptr, *d_pin = nullptr, *d_pout = nullptr, *Wm = nullptr, *Wr = nullptr;
-  int* d_info = nullptr;
+  int *d_info = nullptr, *d_piv = nullptr;
   auto cleanup = [&]() {
     for (void* q : {(void*)d_t, (void*)d_D, (void*)d_D2, (void*)d_ir, (void*)d_ir2, (void*)d_tinv, (void*)d_mdinv,
-                    (void*)d_pin, (void*)d_pout, (void*)Wm, (void*)Wr, (void*)d_info})
+                    (void*)d_pin, (void*)d_pout, (void*)Wm, (void*)Wr, (void*)d_info, (void*)d_piv})
       cudaFree(q);
   };
   int rc = 0;
@@ -459,6 +469,22 @@ int build_mode_operators(const OpKey& k, const Cheb& c, OpSet* ops) {
   }
   ops->bytes += (implicit ? sizeof(double) * 4 * RR * M : 0) + (k.needs_lap ? sizeof(double) * lap_rows * R * M : 0);
   if (cudaMalloc(&d_info, sizeof(int) * mc) != cudaSuccess) { cleanup(); return fail(FALCON_ENOMEM, "info"); }
+  if (hf && cudaMalloc(&d_piv, sizeof(int) * 2 * (size_t)R * mc) != cudaSuccess) {
+    cleanup();
+    return fail(FALCON_ENOMEM, "pivots");
+  }
+  // the caller's factors of modes [m, m + nb) of one operator (order n):
+  // factors into Wm, pivots into d_piv, then dgetrs on the unit right-hand
+  // sides in Wr
+  auto solve_given = [&](const double* lu, const int* piv, int n, int m, int nb, int off) -> int {
+    const size_t nn = (size_t)n * n;
+    cudaError_t e = cudaMemcpy(Wm, lu + (size_t)m * nn, sizeof(double) * nn * nb, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(d_piv, piv + (size_t)m * n, sizeof(int) * (size_t)n * nb, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = launch_unit_rhs(n, R, off, nb, Wr, s);
+    if (e == cudaSuccess) e = launch_getrs_rows(n, nb, Wm, nn, d_piv, (size_t)n, Wr, (size_t)n * R, R, s);
+    if (e != cudaSuccess) return fail(FALCON_ECUDA, std::string("solve with given factors: ") + cudaGetErrorString(e));
+    return 0;
+  };
   auto ck = [&](cudaError_t e, const char* what) -> int {
     if (e != cudaSuccess) return fail(FALCON_ECUDA, std::string(what) + ": " + cudaGetErrorString(e));
     return 0;
@@ -489,7 +515,11 @@ int build_mode_operators(const OpKey& k, const Cheb& c, OpSet* ops) {
     const int nm = std::min(mc, M - m0);
     const int a0 = std::max(m0, 1), na = m0 + nm - a0;
     // temperature: ST[m] = Tinv AT_m^-1
-    if (implicit && ((rc = ck(launch_assemble(0, R, m0, nm, d_t, d_D, d_D2, d_ir, d_ir2, wdt, 1.0 / k.pr, C, Wm, s), "assemble AT")) ||
+    if (implicit && hf && hf->AT) {
+      if ((rc = solve_given(hf->AT, hf->pT, R, m0, nm, 0)) ||
+          (rc = ck(prod(Wr, (long)RR, d_tinv, ops->ST + (size_t)m0 * RR, R, R, nm), "ST product")))
+        break;
+    } else if (implicit && ((rc = ck(launch_assemble(0, R, m0, nm, d_t, d_D, d_D2, d_ir, d_ir2, wdt, 1.0 / k.pr, C, Wm, s), "assemble AT")) ||
         (rc = ck(launch_unit_rhs(R, R, 0, nm, Wr, s), "unit rhs")) ||
         (rc = ck(launch_lu_solve(R, nm, Wm, RR, Wr, RR, R, d_info, s), "lu AT")) ||
         (rc = check_info(nm, m0, "AT")) ||
@@ -498,20 +528,24 @@ int build_mode_operators(const OpKey& k, const Cheb& c, OpSet* ops) {
     if (na <= 0) continue;
     // psi-omega: AF_m^-1 on [0; e_j], unknowns [psi; omega]
     double* Gm = implicit ? ops->G + (size_t)a0 * L3 : nullptr;
-    if (implicit && ((rc = ck(launch_assemble_af(R, a0, na, k.mbc, irk, d_t, d_D, d_D2, d_ir, d_ir2, wdt, C, Wm, s), "assemble AF")) ||
+    const bool given_af = hf && hf->AF;
+    if (implicit && given_af && (rc = solve_given(hf->AF, hf->pF, 2 * R, a0, na, R))) break;
+    if (implicit && ((!given_af && ((rc = ck(launch_assemble_af(R, a0, na, k.mbc, irk, d_t, d_D, d_D2, d_ir, d_ir2, wdt, C, Wm, s), "assemble AF")) ||
         (rc = ck(launch_unit_rhs(2 * R, R, R, na, Wr, s), "unit rhs")) ||
         (rc = ck(launch_lu_solve(2 * R, na, Wm, 4 * RR, Wr, L2, R, d_info, s), "lu AF")) ||
-        (rc = check_info(na, a0, "psi-omega operator")) ||
+        (rc = check_info(na, a0, "psi-omega operator")))) ||
         (rc = ck(prod(Wr + RR, L2, d_tinv, Gm, 3L * R, R, na), "G omega")) ||
         (rc = ck(prod(Wr, L2, d_tinv, Gm + R, 3L * R, R, na), "G psi")) ||
         (rc = ck(prod(Wr, L2, d_mdinv, Gm + 2 * R, 3L * R, R, na), "G uphi"))))
       break;
     if (!k.needs_lap) continue;
     double* Lm = ops->LAP + (size_t)a0 * lap_rows * R;
-    if ((rc = ck(launch_assemble(4, R, a0, na, d_t, d_D, d_D2, d_ir, d_ir2, 0.0, 1.0, C, Wm, s), "assemble LAPpsi")) ||
+    const bool given_lap = hf && hf->LAP;
+    if (given_lap && (rc = solve_given(hf->LAP, hf->pL, R, a0, na, 0))) break;
+    if ((!given_lap && ((rc = ck(launch_assemble(4, R, a0, na, d_t, d_D, d_D2, d_ir, d_ir2, 0.0, 1.0, C, Wm, s), "assemble LAPpsi")) ||
         (rc = ck(launch_unit_rhs(R, R, 0, na, Wr, s), "unit rhs")) ||
         (rc = ck(launch_lu_solve(R, na, Wm, RR, Wr, RR, R, d_info, s), "lu LAPpsi")) ||
-        (rc = check_info(na, a0, "psi Poisson operator")) ||
+        (rc = check_info(na, a0, "psi Poisson operator")))) ||
         (rc = ck(prod(Wr, (long)RR, d_tinv, Lm, lap_rows, R, na), "LAP psi")) ||
         (rc = ck(prod(Wr, (long)RR, d_mdinv, Lm + R, lap_rows, R, na), "LAP uphi")) ||
         (rc = ck(prod(Wr, (long)RR, d_pin, Lm + 2 * R, lap_rows, 1, na), "LAP wall in")) ||
@@ -523,8 +557,11 @@ int build_mode_operators(const OpKey& k, const Cheb& c, OpSet* ops) {
   return rc;
 }
 
-int build_opset(const OpKey& k, std::shared_ptr<OpSet>* out) {
-  {
+// The operator set of key k: from the process-wide cache, else built on the
+// device (and cached); with host factors hf, built from them and not cached
+// (the set belongs to the one caller that gave them).
+int build_opset(const OpKey& k, std::shared_ptr<OpSet>* out, const HostFactors* hf = nullptr) {
+  if (!hf) {
     std::lock_guard<std::mutex> lk(g_ops_mu);
     auto it = g_ops.find(k);
     if (it != g_ops.end()) {
@@ -540,12 +577,17 @@ int build_opset(const OpKey& k, std::shared_ptr<OpSet>* out) {
   phys_deriv(c, D1p, Lp);
   std::vector<double> U((size_t)2 * R * R);
   int rc;
-  if ((rc = build_mode_operators(k, c, ops.get()))) return rc;
+  if ((rc = build_mode_operators(k, c, ops.get(), hf))) return rc;
   {
     std::vector<double> Au;
-    assemble_Au(c, k.mbc, k.dt, k.wt, Au);
     std::vector<int> pu(R);
-    if (host_dgetrf(R, Au.data(), pu.data()) != 0) return fail(FALCON_ESINGULAR, "dgetrf: singular uphi_bar operator");
+    if (hf && hf->Au) {
+      Au.assign(hf->Au, hf->Au + (size_t)R * R);
+      pu.assign(hf->pu, hf->pu + R);
+    } else {
+      assemble_Au(c, k.mbc, k.dt, k.wt, Au);
+      if (host_dgetrf(R, Au.data(), pu.data()) != 0) return fail(FALCON_ESINGULAR, "dgetrf: singular uphi_bar operator");
+    }
     std::vector<double> x(R), v(R), dv(R);
     for (int j = 0; j < R; ++j) {
       std::fill(x.begin(), x.end(), 0.0);
@@ -611,7 +653,7 @@ int build_opset(const OpKey& k, std::shared_ptr<OpSet>* out) {
       return rc;
     CK(cudaDeviceSynchronize());
   }
-  {
+  if (!hf) {
     std::lock_guard<std::mutex> lk(g_ops_mu);
     g_ops[k] = ops;
   }
@@ -3033,6 +3075,40 @@ int falcon_get_state(falcon_handle* h, double* tFR, double* omgFR, double* upFR,
   return falcon_batch_get_state(h->b, 0, tFR, omgFR, upFR, urFR, psi);
 }
 
+int falcon_upload_factors(falcon_handle* h, const double* AT, const int* ipiv_T, const double* AF, const int* ipiv_F,
+                          const double* A_uphi, const int* ipiv_uphi, const double* LAPpsi, const int* ipiv_lap) {
+  if (!h || !h->b || h->b->groups.size() != 1) return fail(FALCON_EINVAL, "null or invalid handle");
+  Group* g = h->b->groups[0].get();
+  if ((!AT) != (!ipiv_T) || (!AF) != (!ipiv_F) || (!A_uphi) != (!ipiv_uphi) || (!LAPpsi) != (!ipiv_lap))
+    return fail(FALCON_EINVAL, "falcon_upload_factors: each factor array needs its pivots");
+  if (g->sch.type == FALCON_IMEXRK && g->sch.diag_diff)
+    return fail(FALCON_EINVAL, "falcon_upload_factors: this scheme solves each stage with its own operators "
+                               "(stage-dependent implicit diagonal); one set of factors cannot serve them");
+  if (g->sch.type == FALCON_RK && (AT || AF || A_uphi))
+    return fail(FALCON_EINVAL, "falcon_upload_factors: explicit RK has no implicit AT, AF or A_uphi operators");
+  const OpKey k = g->ops->key;
+  if (LAPpsi && !k.needs_lap)
+    return fail(FALCON_EINVAL, "falcon_upload_factors: this scheme does not solve the psi Poisson operator LAPpsi");
+  const int R = g->R, M = g->M;
+  auto pivots_ok = [](const int* piv, int n, int nb) {
+    for (size_t i = 0; i < (size_t)n * nb; ++i)
+      if (piv[i] < 1 || piv[i] > n) return false;
+    return true;
+  };
+  if ((ipiv_T && !pivots_ok(ipiv_T, R, M)) || (ipiv_F && !pivots_ok(ipiv_F + 2 * R, 2 * R, M - 1)) ||
+      (ipiv_uphi && !pivots_ok(ipiv_uphi, R, 1)) || (ipiv_lap && !pivots_ok(ipiv_lap + R, R, M - 1)))
+    return fail(FALCON_EINVAL, "falcon_upload_factors: a pivot lies outside [1, n]");
+  HostFactors hf;
+  hf.AT = AT; hf.pT = ipiv_T; hf.AF = AF; hf.pF = ipiv_F;
+  hf.Au = A_uphi; hf.pu = ipiv_uphi; hf.LAP = LAPpsi; hf.pL = ipiv_lap;
+  std::shared_ptr<OpSet> fresh;
+  int rc = build_opset(k, &fresh, &hf);
+  if (rc) return rc;
+  g->ops = fresh;
+  g->drop_graphs();  // captured steps hold the previous operators
+  return 0;
+}
+
 int falcon_step(falcon_handle* h, int nsteps) {
   if (!h) return fail(FALCON_EINVAL, "null handle");
   return falcon_batch_step(h->b, nsteps);
@@ -3337,6 +3413,13 @@ int falcon_cheb_d1_dev(int nr, int ncol, const double* in_dev, double* out_dev, 
 }
 int falcon_cheb_d2_dev(int nr, int ncol, const double* in_dev, double* out_dev, void* stream) {
   return cheb_apply(3, nr, ncol, in_dev, out_dev, stream);
+}
+
+int falcon_cheb_d1d2_dev(int nr, int ncol, const double* in_dev, double* d1_dev, double* d2_dev, void* stream) {
+  if (!d1_dev || !d2_dev || d1_dev == d2_dev || d1_dev == in_dev || d2_dev == in_dev)
+    return fail(FALCON_EINVAL, "falcon_cheb_d1d2_dev: outputs must be two arrays apart from the input");
+  const int rc = cheb_apply(2, nr, ncol, in_dev, d1_dev, stream);
+  return rc ? rc : cheb_apply(3, nr, ncol, in_dev, d2_dev, stream);
 }
 
 int falcon_server_create(size_t hbm_budget_bytes, int max_active, falcon_server** out) {

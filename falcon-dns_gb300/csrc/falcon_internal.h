@@ -321,6 +321,10 @@ cudaError_t launch_assemble_af(int R, int m0, int nmodes, int mbc, int irk, cons
 cudaError_t launch_lu_solve(int n, int nb, double* mats, size_t mstride, double* rhs, size_t rstride, int nrhs,
                             int* info, cudaStream_t s);
 cudaError_t launch_unit_rhs(int n, int nrhs, int off, int nb, double* out, cudaStream_t s);
+// dgetrs only, with given factors (column-major n x n, stride mstride) and
+// 1-based pivots (stride pstride); rhs row-major (n x nrhs), stride rstride
+cudaError_t launch_getrs_rows(int n, int nb, const double* lu, size_t mstride, const int* ipiv, size_t pstride,
+                              double* rhs, size_t rstride, int nrhs, cudaStream_t s);
 // Self-timed FP64 FMA throughput kernel (returns GFLOP/s, or < 0 on error).
 double measure_fp64_peak();
 // Same for the FP64 tensor-core MMA (mma.sync m8n8k4 f64).

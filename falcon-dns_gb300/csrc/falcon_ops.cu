@@ -83,6 +83,38 @@ __global__ void assemble_af_kernel(int R, int m0, int nmodes, int mbc, int irk, 
 
 constexpr int kMaxLu = 520;  // largest order factorised (2 Nr_max for Nr_max <= 257)
 
+// dgetrs 'N' on nrhs right-hand sides stored row-major (n x nrhs) in place,
+// with the LU factors `a` (column-major n x n) and 0-based pivots `piv`: row
+// interchanges, unit-lower forward, upper backward; the right-hand sides are
+// independent columns, one thread each (threads tid of nt).
+__device__ void dgetrs_rows(int n, const double* a, const int* piv, double* X, int nrhs, int tid, int nt) {
+  for (int c = tid; c < nrhs; c += nt) {
+    for (int i = 0; i < n; ++i) {
+      const int p = piv[i];
+      if (p != i) {
+        const double tmp = X[(size_t)i * nrhs + c];
+        X[(size_t)i * nrhs + c] = X[(size_t)p * nrhs + c];
+        X[(size_t)p * nrhs + c] = tmp;
+      }
+    }
+    for (int j = 0; j < n; ++j) {
+      const double bj = X[(size_t)j * nrhs + c];
+      if (bj != 0.0)
+        for (int i = j + 1; i < n; ++i)
+          X[(size_t)i * nrhs + c] = __dadd_rn(X[(size_t)i * nrhs + c], -__dmul_rn(bj, a[i + (size_t)n * j]));
+    }
+    for (int j = n - 1; j >= 0; --j) {
+      double bj = X[(size_t)j * nrhs + c];
+      if (bj != 0.0) {
+        bj = bj / a[j + (size_t)n * j];
+        X[(size_t)j * nrhs + c] = bj;
+        for (int i = 0; i < j; ++i)
+          X[(size_t)i * nrhs + c] = __dadd_rn(X[(size_t)i * nrhs + c], -__dmul_rn(bj, a[i + (size_t)n * j]));
+      }
+    }
+  }
+}
+
 // One block per matrix: dgetf2 on the n x n column-major matrix (in shared
 // memory when SMEM, else in place in global memory, where it stays L1/L2
 // resident), then dgetrs 'N' on nrhs right-hand sides stored row-major
@@ -164,33 +196,7 @@ __global__ void __launch_bounds__(512) lu_solve_kernel(int n, double* mats, size
     __syncthreads();
   }
   if (tid == 0 && info) info[b] = first_zero;
-  // dgetrs 'N': row interchanges, unit-lower forward, upper backward; the
-  // right-hand sides are independent columns, one thread each.
-  for (int c = tid; c < nrhs; c += nt) {
-    for (int i = 0; i < n; ++i) {
-      const int p = s_piv_all[i];
-      if (p != i) {
-        const double tmp = X[(size_t)i * nrhs + c];
-        X[(size_t)i * nrhs + c] = X[(size_t)p * nrhs + c];
-        X[(size_t)p * nrhs + c] = tmp;
-      }
-    }
-    for (int j = 0; j < n; ++j) {
-      const double bj = X[(size_t)j * nrhs + c];
-      if (bj != 0.0)
-        for (int i = j + 1; i < n; ++i)
-          X[(size_t)i * nrhs + c] = __dadd_rn(X[(size_t)i * nrhs + c], -__dmul_rn(bj, a[i + (size_t)n * j]));
-    }
-    for (int j = n - 1; j >= 0; --j) {
-      double bj = X[(size_t)j * nrhs + c];
-      if (bj != 0.0) {
-        bj = bj / a[j + (size_t)n * j];
-        X[(size_t)j * nrhs + c] = bj;
-        for (int i = 0; i < j; ++i)
-          X[(size_t)i * nrhs + c] = __dadd_rn(X[(size_t)i * nrhs + c], -__dmul_rn(bj, a[i + (size_t)n * j]));
-      }
-    }
-  }
+  dgetrs_rows(n, a, s_piv_all, X, nrhs, tid, nt);
 }
 
 // Unit right-hand sides, row-major (n x nrhs) per batch entry: column c has
@@ -229,6 +235,39 @@ cudaError_t launch_assemble_af(int R, int m0, int nmodes, int mbc, int irk, cons
 
 // Shared-memory form up to 160 x 160 (200 KB); larger orders factorise in
 // place in global memory (the matrices are overwritten).
+// The solve phase of lu_solve_kernel for factors made elsewhere (a host's
+// own dgetrf): one block per matrix, factors (column-major n x n, stride
+// mstride; in shared memory when SMEM) and 1-based pivots (stride pstride)
+// as LAPACK returns them, right-hand sides row-major (n x nrhs) in place.
+// The pivots were checked to lie in [1, n] on the host.
+template <bool SMEM>
+__global__ void __launch_bounds__(512) getrs_rows_kernel(int n, const double* lus, size_t mstride, const int* ipivs,
+                                                         size_t pstride, double* rhs, size_t rstride, int nrhs) {
+  extern __shared__ double sm_f[];
+  __shared__ int s_piv[kMaxLu];
+  const int b = blockIdx.x, tid = threadIdx.x, nt = blockDim.x;
+  const double* A = lus + (size_t)b * mstride;
+  for (int i = tid; i < n; i += nt) s_piv[i] = ipivs[(size_t)b * pstride + i] - 1;
+  if (SMEM)
+    for (int e = tid; e < n * n; e += nt) sm_f[e] = A[e];
+  __syncthreads();
+  dgetrs_rows(n, SMEM ? sm_f : A, s_piv, rhs + (size_t)b * rstride, nrhs, tid, nt);
+}
+
+cudaError_t launch_getrs_rows(int n, int nb, const double* lu, size_t mstride, const int* ipiv, size_t pstride,
+                              double* rhs, size_t rstride, int nrhs, cudaStream_t s) {
+  if (n > kMaxLu) return cudaErrorInvalidValue;
+  const size_t smem = sizeof(double) * (size_t)n * n;
+  if (smem <= 160 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(getrs_rows_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    getrs_rows_kernel<true><<<nb, 512, smem, s>>>(n, lu, mstride, ipiv, pstride, rhs, rstride, nrhs);
+  } else {
+    getrs_rows_kernel<false><<<nb, 512, 0, s>>>(n, lu, mstride, ipiv, pstride, rhs, rstride, nrhs);
+  }
+  return cudaGetLastError();
+}
+
 cudaError_t launch_lu_solve(int n, int nb, double* mats, size_t mstride, double* rhs, size_t rstride, int nrhs,
                             int* info, cudaStream_t s) {
   if (n < 1 || n > kMaxLu) return cudaErrorInvalidValue;

@@ -103,6 +103,7 @@ EXPORTS = (
     "falcon_nonlin_noalloc_dev", "falcon_set_step_graphs", "falcon_store_checkpoint", "falcon_load_checkpoint",
     "falcon_store_snapshot", "falcon_batch_store_checkpoint", "falcon_batch_load_checkpoint",
     "falcon_batch_store_snapshot", "falcon_restart", "falcon_batch_restart", "falcon_set_gemm_mode",
+    "falcon_upload_factors", "falcon_cheb_d1d2_dev",
 )
 
 
@@ -167,6 +168,9 @@ def lib():
     for f in ("falcon_batch_store_checkpoint", "falcon_batch_load_checkpoint", "falcon_batch_store_snapshot"):
         getattr(L, f).argtypes = [vp, ip, ctypes.c_char_p]
     L.falcon_restart.argtypes = [vp, ctypes.c_char_p]
+    L.falcon_upload_factors.argtypes = [vp, dp, P(ctypes.c_int), dp, P(ctypes.c_int), dp, P(ctypes.c_int), dp,
+                                        P(ctypes.c_int)]
+    L.falcon_cheb_d1d2_dev.argtypes = [ip, ip, vp, vp, vp, vp]
     L.falcon_batch_restart.argtypes = [vp, P(ctypes.c_char_p)]
     _lib = L
     return L
@@ -453,3 +457,45 @@ def set_gemm_mode(mode):
 def set_step_graphs(enable):
     """Replay steady-state steps as CUDA graphs (default on); returns the previous setting."""
     return lib().falcon_set_step_graphs(1 if enable else 0)
+
+
+def _ip(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int)) if a is not None else None
+
+
+class Handle:
+    """One instance through the single-run entry points a Fortran host binds
+    (falcon_create, falcon_init_state, falcon_upload_factors, falcon_step,
+    falcon_get_state, falcon_destroy)."""
+
+    def __init__(self, params):
+        self.params = params
+        h = ctypes.c_void_p()
+        check(lib().falcon_create(ctypes.byref(params), ctypes.byref(h)))
+        self.h = h
+
+    def init_noise(self, seed, amp=1e-3):
+        check(lib().falcon_init_state(self.h, 1, amp, seed))
+
+    def upload_factors(self, AT=None, ipiv_T=None, AF=None, ipiv_F=None, A_uphi=None, ipiv_uphi=None,
+                       LAPpsi=None, ipiv_lap=None):
+        """Factors (n, n, Nm+1) and 1-based pivots (n, Nm+1) in Fortran
+        order, as numpy arrays indexed [i, j, m] and [i, m]."""
+        f = [None if a is None else np.asfortranarray(a, np.float64) for a in (AT, AF, A_uphi, LAPpsi)]
+        q = [None if a is None else np.asfortranarray(a, np.int32) for a in (ipiv_T, ipiv_F, ipiv_uphi, ipiv_lap)]
+        check(lib().falcon_upload_factors(self.h, _dp(f[0]), _ip(q[0]), _dp(f[1]), _ip(q[1]), _dp(f[2]), _ip(q[2]),
+                                          _dp(f[3]), _ip(q[3])))
+
+    def step(self, n=1):
+        check(lib().falcon_step(self.h, n))
+
+    def get_state(self):
+        shape = (self.params.nr_max, self.params.nm_max + 1)
+        arrs = [_field(shape) for _ in range(5)]
+        check(lib().falcon_get_state(self.h, *[_dp(a) for a in arrs]))
+        return dict(zip(("T", "omg", "up", "ur", "psi"), arrs))
+
+    def close(self):
+        if self.h:
+            lib().falcon_destroy(self.h)
+            self.h = None

@@ -137,6 +137,26 @@ int falcon_set_state(falcon_handle* h, const double* tFR, const double* omgFR,
                      const double* upFR, const double* urFR);
 int falcon_get_state(falcon_handle* h, double* tFR, double* omgFR, double* upFR,
                      double* urFR, double* psi);
+/* The implicit operators from the caller's own LU factors: the output of
+ * its mat_build / mat_build_IRK / mat_build_uphibar / mat_build_rk + dgetrf
+ * (src/mat_assembly.F90:68-462, factorize at src/algebra_lapack.F90:14-24),
+ * in the reference's arrays: AT = AT_all (Nr,Nr,Nm+1) with ipiv_T = IPIV1
+ * (Nr,Nm+1); AF = AF_all (2Nr,2Nr,Nm+1) with ipiv_F = IPIV2 (2Nr,Nm+1; mode
+ * 0 unused); A_uphi = A_uphi_all(:,:,1) (Nr,Nr) with ipiv_uphi (Nr);
+ * LAPpsi = LAPpsi_all (Nr,Nr,Nm+1) with ipiv_lap (Nr,Nm+1; mode 0 unused),
+ * for the schemes that solve it (IMEXRK not stiffly accurate, RK).  Column-
+ * major factors, 1-based pivots, as LAPACK dgetrf returns them.  Replaces
+ * the solves of matsolve / matsolve_real (src/algebra_lapack.F90:26-53):
+ * the library applies dgetrs to unit right-hand sides on the device with
+ * these factors and folds the solutions into its per-mode operators.  A
+ * NULL array (with its pivots) keeps the library's own factors of that
+ * operator.  Built for the handle's current dt and scheme weight (IMEX
+ * wt_lhs, IMEXRK butcher_aD(diag,diag)); a later operator rebuild (a dt
+ * change of a variable-dt run) uses the library's own assembly again.
+ * Schemes with stage-dependent implicit diagonals are refused. */
+int falcon_upload_factors(falcon_handle* h, const double* AT, const int* ipiv_T, const double* AF,
+                          const int* ipiv_F, const double* A_uphi, const int* ipiv_uphi,
+                          const double* LAPpsi, const int* ipiv_lap);
 /* Advances nsteps time steps (the loop bodies of src/steptime.F90:196-251 /
  * src/steptime_imexrk.F90:96-190). */
 int falcon_step(falcon_handle* h, int nsteps);
@@ -265,6 +285,9 @@ int falcon_cheb_fwd_dev(int nr, int ncol, const double* in_dev, double* out_dev,
 int falcon_cheb_inv_dev(int nr, int ncol, const double* in_dev, double* out_dev, void* stream);
 int falcon_cheb_d1_dev(int nr, int ncol, const double* in_dev, double* out_dev, void* stream);
 int falcon_cheb_d2_dev(int nr, int ncol, const double* in_dev, double* out_dev, void* stream);
+/* chebinvtranD1D2 (src/chebyshev_fftw.F90:369-427): first and second radial
+ * derivatives of the same coefficient columns in one call. */
+int falcon_cheb_d1d2_dev(int nr, int ncol, const double* in_dev, double* d1_dev, double* d2_dev, void* stream);
 
 /* ---- serving ---- */
 /* A request loop that admits simulation requests by device-memory

@@ -114,6 +114,13 @@ int orc_sim_store_snapshot(const orc_sim* s, const char* path);
  * missing or malformed), -3 (smaller grid), -4 (grid change with multistep
  * histories), -5 (no usable multistep histories in the file). */
 int orc_sim_restart(orc_sim* s, const char* dir, int npoint, int add_pert, double ampT);
+/* The operator matrices of mode n before factorisation (column-major), on
+ * the grid and walls of p: kind 0 AT (R x R), 1 AF (2R x 2R), 2 A_uphi
+ * (R x R), 3 LAPpsi (R x R); irk = 1 gives mat_build_IRK's boundary-row
+ * order of AF (src/mat_assembly.F90:68-240 against :242-413; LAPpsi is
+ * mat_build_rk, :415-462).  dt and wt multiply the diffusion operator as in
+ * the reference (wt = wt_lhs_tscheme_imp).  Returns 0, or -1. */
+int orc_mat_assemble(const orc_params* p, int kind, int n, double dt, double wt, int irk, double* out);
 /* Number of OpenMP threads the oracle uses (0 = runtime default). */
 void orc_set_threads(int n);
 

@@ -101,6 +101,8 @@ def lib():
         L.orc_sim_dt.restype = ctypes.c_double
         L.orc_noise_pair.argtypes = [ctypes.c_uint64, ctypes.c_int, ctypes.c_int, dp, dp]
         L.orc_set_threads.argtypes = [ctypes.c_int]
+        L.orc_mat_assemble.argtypes = [ctypes.POINTER(OrcParams), ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                       ctypes.c_double, ctypes.c_int, dp]
         _lib = L
     return _lib
 
@@ -188,6 +190,20 @@ def nonlin(nm, t, om, up, ur):
     outs = [np.empty_like(t) for _ in range(4)]
     lib().orc_nonlin(nm, nr, _dp(t), _dp(om), _dp(up), _dp(ur), *[_dp(o) for o in outs])
     return outs
+
+
+MAT_KINDS = {"AT": 0, "AF": 1, "A_uphi": 2, "LAPpsi": 3}
+
+
+def mat_assemble(nr, kind, n, dt, wt, pr=1.0, mbc="NS", irk=False):
+    """Operator matrix `kind` (AT, AF, A_uphi, LAPpsi) of mode n before its
+    LU factorisation, as a numpy array indexed [i, j] (row, column)."""
+    p = make_params(nr, 4, "CNAB2", pr=pr, dt=dt, mbc=mbc)
+    size = 2 * nr if kind == "AF" else nr
+    out = np.zeros(size * size)
+    if lib().orc_mat_assemble(ctypes.byref(p), MAT_KINDS[kind], n, dt, wt, 1 if irk else 0, _dp(out)) != 0:
+        raise RuntimeError("orc_mat_assemble failed")
+    return out.reshape(size, size).T  # column-major -> [row, column]
 
 
 def make_params(nr, nm, scheme="CNAB2", eta=0.35, ra=1e5, pr=1.0, dt=1e-5, mbc="NS",

@@ -854,8 +854,7 @@ int orc_sim_get_state(const orc_sim* s, double* tFR, double* omgFR, double* upFR
 /* mat_build (:242-359) when irk == 0; mat_build_IRK (:68-187) when irk == 1.
  * The two differ only in which boundary rows of AF carry psi=0 and the
  * second psi condition (:143-150 vs :316-323). */
-static void mat_build(orc_sim* s, double dt, int n, double wt, int irk, double* AT, int* piv1,
-                      double* AF, int* piv2) {
+static void assemble_at_af(orc_sim* s, double dt, int n, double wt, int irk, double* AT, double* AF) {
   int R = s->R, R2 = 2 * R;
   const double *t = s->t, *D = s->D, *D2 = s->D2, *rr = s->r_radius, *rr2 = s->r_radius2;
   double C = pow(2.0 / (double)(R - 1), 0.5);
@@ -910,14 +909,19 @@ static void mat_build(orc_sim* s, double dt, int n, double wt, int irk, double* 
     F2(AF, R + i, R) *= 0.5; F2(AF, R + i, R2 - 1) *= 0.5;
   }
   for (int k = 0; k < R2 * R2; ++k) AF[k] = C * AF[k];
-  orc_dgetrf(R, AT, piv1);
-  orc_dgetrf(R2, AF, piv2);
 #undef F2
   free(bcp2);
 }
 
+static void mat_build(orc_sim* s, double dt, int n, double wt, int irk, double* AT, int* piv1,
+                      double* AF, int* piv2) {
+  assemble_at_af(s, dt, n, wt, irk, AT, AF);
+  orc_dgetrf(s->R, AT, piv1);
+  orc_dgetrf(2 * s->R, AF, piv2);
+}
+
 /* mat_build_uphibar (:361-413) / mat_build_uphibar_IRK (:189-240). */
-static void mat_build_uphibar(orc_sim* s, double dt, double wt, double* A, int* piv) {
+static void assemble_uphibar(orc_sim* s, double dt, double wt, double* A) {
   int R = s->R;
   const double *t = s->t, *D = s->D, *D2 = s->D2, *rr = s->r_radius, *rr2 = s->r_radius2;
   double C = pow(2.0 / (double)(R - 1), 0.5);
@@ -933,11 +937,15 @@ static void mat_build_uphibar(orc_sim* s, double dt, double wt, double* A, int* 
   }
   for (int i = 0; i < R; ++i) { M2(A, i, 0) *= 0.5; M2(A, i, R - 1) *= 0.5; }
   for (int k = 0; k < R * R; ++k) A[k] = C * A[k];
-  orc_dgetrf(R, A, piv);
+}
+
+static void mat_build_uphibar(orc_sim* s, double dt, double wt, double* A, int* piv) {
+  assemble_uphibar(s, dt, wt, A);
+  orc_dgetrf(s->R, A, piv);
 }
 
 /* mat_build_rk (:415-462): the psi Poisson operator with psi=0 rows. */
-static void mat_build_rk(orc_sim* s, int n, double* L, int* piv) {
+static void assemble_rk(orc_sim* s, int n, double* L) {
   int R = s->R;
   const double *t = s->t, *D = s->D, *D2 = s->D2, *rr = s->r_radius, *rr2 = s->r_radius2;
   double C = pow(2.0 / (double)(R - 1), 0.5);
@@ -950,9 +958,36 @@ static void mat_build_rk(orc_sim* s, int n, double* L, int* piv) {
   }
   for (int i = 0; i < R; ++i) { M2(L, i, 0) *= 0.5; M2(L, i, R - 1) *= 0.5; }
   for (int k = 0; k < R * R; ++k) L[k] = 1.0 * C * L[k];
-  orc_dgetrf(R, L, piv);
+}
+
+static void mat_build_rk(orc_sim* s, int n, double* L, int* piv) {
+  assemble_rk(s, n, L);
+  orc_dgetrf(s->R, L, piv);
 }
 #undef M2
+
+int orc_mat_assemble(const orc_params* p, int kind, int n, double dt, double wt, int irk, double* out) {
+  orc_sim* s = orc_sim_create(p);
+  if (!s) return -1;
+  switch (kind) {
+    case 0:
+    case 1: {
+      const int R = s->R;
+      double* AT = zalloc((size_t)R * R);
+      double* AF = zalloc((size_t)4 * R * R);
+      assemble_at_af(s, dt, n, wt, irk, AT, AF);
+      memcpy(out, kind == 0 ? AT : AF, sizeof(double) * (kind == 0 ? (size_t)R * R : (size_t)4 * R * R));
+      free(AT);
+      free(AF);
+      break;
+    }
+    case 2: assemble_uphibar(s, dt, wt, out); break;
+    case 3: assemble_rk(s, n, out); break;
+    default: orc_sim_destroy(s); return -1;
+  }
+  orc_sim_destroy(s);
+  return 0;
+}
 
 /* matsolve (src/algebra_lapack.F90:26-38): two dgetrs on the re/im parts. */
 static void matsolve_cplx(int n, const double* A, const int* piv, double* x /*complex n*/,

@@ -96,3 +96,19 @@ def test_process_wide_switches_round_trip(fg):
     assert fg.set_max_group_size(128) == 0
     L.falcon_set_step_graphs.argtypes = [ctypes.c_int]
     assert L.falcon_set_step_graphs(0) == 1 and L.falcon_set_step_graphs(1) == 0
+
+
+def test_namelist_reader_on_the_reference_input(fg):
+    # the reference's own src/input.txt, copied verbatim by make_golden.py
+    p = fg.read_namelist(os.path.join(ROOT, "tests", "golden", "input_reference.txt"))
+    assert (p.nr_max, p.nm_max) == (32, 32)
+    assert p.eta == 0.35 and p.ra == 2000.0 and p.pr == 1.0 and p.mbc == 0
+    assert p.ampT == 0.01 and p.l_add_pert == 0 and p.lagpts == 16 and p.n_init == 0 and p.buo_imp == 1
+    assert p.n_time_steps == 1000000 and p.dt == 1e-5 and p.totaltime == 100.0
+    assert p.l_vartimestep == 1 and p.l_optimizedt == 0
+    assert (p.scheme_type, p.scheme_imp, p.scheme_exp) == (1, 44, 44)   # IMEXRK BHR553 / expBHR553
+    assert p.l_imexrk_started == 0
+    assert p.dt_coef == 1.0 and p.dt_max == 1e-2 and p.cfl == 0.1
+    assert (p.l_restart, p.n_restart, p.n_restart_point, p.n_snapshot_point) == (0, 0, 1, 0)
+    assert p.tag == b"BHR553"
+    assert (p.n_checkpoint, p.n_snapshot, p.n_KE, p.n_KEspec) == (10000, 100000, 10, 100000)

@@ -95,3 +95,50 @@ def test_schemes_agree_at_small_dt(orc, scheme):
     s.init_noise(3)
     s.step(20)
     assert rel(s.get_state()["T"], ref.get_state()["T"]) < 1e-6
+
+
+MAT_CASES = [(nr, n) for nr, n in ((9, 0), (9, 3), (9, 4), (33, 0), (33, 3), (33, 16), (65, 32))]
+MAT_DT, MAT_WT, MAT_PR = 2e-5, 0.4358665215, 0.7
+
+
+@pytest.mark.parametrize("nr,n", MAT_CASES)
+@pytest.mark.parametrize("mbc", ["NS", "SF"])
+def test_operator_matrices_match_independent_restatement(orc, golden, nr, n, mbc):
+    # AT, A_uphi, LAPpsi and AF in both boundary-row orders (mat_build and
+    # mat_build_IRK, src/mat_assembly.F90:143-150 vs :316-323) against the
+    # numpy restatement of tests/golden/make_golden.py
+    for kind, irk in (("AT", 0), ("A_uphi", 0), ("LAPpsi", 0), ("AF", 0), ("AF", 1)):
+        want = golden[f"mat_{kind}_{nr}_{n}_{mbc}_{irk}"]
+        got = orc.mat_assemble(nr, kind, n, MAT_DT, MAT_WT, pr=MAT_PR, mbc=mbc, irk=bool(irk))
+        assert got.shape == want.shape
+        assert rel(got, want) < 1e-13, (kind, irk)
+    # the two AF orders are different matrices with the same rows
+    a0 = orc.mat_assemble(nr, "AF", n, MAT_DT, MAT_WT, pr=MAT_PR, mbc=mbc, irk=False)
+    a1 = orc.mat_assemble(nr, "AF", n, MAT_DT, MAT_WT, pr=MAT_PR, mbc=mbc, irk=True)
+    assert not np.array_equal(a0, a1)
+    assert np.array_equal(np.sort(a0, axis=0), np.sort(a1, axis=0))
+
+
+@pytest.mark.parametrize("case", [(17, 8, 17, 12), (17, 8, 33, 8), (17, 8, 33, 12)])
+def test_restart_resampling_matches_reference_padding(orc, golden, tmp_path, case):
+    # get_checkpoint_data's grid change (src/init.F90:726-861) against the
+    # reference's Python resampling: chebforward, padding, chebinverse
+    nr0, nm0, nr1, nm1 = case
+    key = "resample_%d_%d_%d_%d" % case
+    old = {f: golden[f"{key}_{f}_old"] for f in ("T", "omg", "ur", "up")}
+    o = orc.Sim(orc.make_params(nr0, nm0, "ARS443"))
+    o.set_state(old["T"], old["omg"], old["up"], old["ur"])
+    o.store_checkpoint(str(tmp_path / "checkpoint_00003"))
+    n = orc.Sim(orc.make_params(nr1, nm1, "ARS443"))
+    n.restart(tmp_path, 3)
+    st = n.get_state()
+    for f in ("T", "omg", "ur", "up"):
+        assert rel(st[f], golden[f"{key}_{f}_new"]) < 1e-13, f
+
+
+@pytest.mark.parametrize("k", [0, 1, 2])
+def test_error_norm_restatement_matches_reference(golden, k):
+    from conftest import rel_l2_reference
+    got = rel_l2_reference(golden[f"norm_{k}_comp"], golden[f"norm_{k}_ref"])
+    want = float(golden[f"norm_{k}_rel_l2"])
+    assert abs(got - want) <= 1e-12 * want
