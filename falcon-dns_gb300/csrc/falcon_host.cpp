@@ -24,6 +24,7 @@
 
 #include "../../include/falcon_gpu.h"
 #include "falcon_internal.h"
+#include "falcon_tc.h"
 #include "imexrk_tables.h"
 
 using namespace falcon;
@@ -217,6 +218,8 @@ struct OpSet {
     int rows = 0, K = 0, nb = 0, rowsP = 0, KP = 0, w = 6;
     uint16_t* s = nullptr;
     int* ex = nullptr;
+    CUtensorMap tmap{};     // the slices for the tcgen05 kernel's copies
+    bool tmap_ok = false;
   };
   std::vector<Oz> oz;
   size_t bytes = 0;
@@ -247,6 +250,8 @@ int add_oz(OpSet* ops, const double* base, int rows, int K, int nb, long sA) {
   CK(cudaMemset(o.s, 0, ns * sizeof(uint16_t)));
   CK(cudaMemset(o.ex, 0, ne * sizeof(int)));
   CK(launch_oz_slice_rows(base, rows, sA, rows, K, nb, o.s, o.ex, o.rowsP, o.KP, o.w, 0));
+  o.tmap_ok = tc_stage_layout_check(o.w, o.KP) == 0 &&
+              tc_make_operator_map(&o.tmap, o.s, nb, oz_slices(o.w), o.KP, o.rowsP) == 0;
   ops->bytes += ns * sizeof(uint16_t) + ne * sizeof(int);
   ops->oz.push_back(o);
   return 0;
@@ -1134,9 +1139,23 @@ bool attach_oz(const OpSet* o, GemmArgs* q) {
     q->oz_rowsP = z.rowsP;
     q->oz_KP = z.KP;
     q->oz_row0 = (int)row0;
+    q->oz_tmap = z.tmap_ok ? &z.tmap : nullptr;
+    q->oz_z0 = (int)z0;
     return true;
   }
   return false;
+}
+
+// The tcgen05 contraction of one GEMM with an attached slice view.
+TcArgs tc_args(const GemmArgs& q) {
+  TcArgs t{};
+  t.X = q.X; t.ldx = q.ldx; t.sX = q.sX;
+  t.K = q.K; t.KP = q.oz_KP; t.N = q.N; t.batch = q.batch; t.rows = q.rows; t.w = q.oz_w;
+  t.nout = 1; t.rend[0] = q.rows; t.Y[0] = q.Y; t.ldy = q.ldy; t.sY = q.sY;
+  t.alpha = q.alpha;
+  t.aex = q.oz_ex + q.oz_row0; t.rowsP = q.oz_rowsP;
+  t.row0 = q.oz_row0; t.z0 = q.oz_z0;
+  return t;
 }
 
 // reuse: the call follows a contraction with the same X operand, unchanged
@@ -1155,6 +1174,12 @@ int gemm(Group* g, int cls, const GemmArgs& q0, bool reuse = false) {
   if (g_gemm_mode.load() && g->oz_xs && q.N >= 16) {
     ok = attach_oz(g->ops.get(), &q);
     for (int st = 0; !ok && st < kMaxStages; ++st) ok = attach_oz(g->stage_ops[st].get(), &q);
+  }
+  if (ok && g_gemm_mode.load() == 2 && q.oz_tmap) {
+    // tcgen05: the kernel slices its own X columns
+    const TcArgs t = tc_args(q);
+    const CUtensorMap* map = static_cast<const CUtensorMap*>(q.oz_tmap);
+    return launch(g, cls, gemm_flops(q), [&]() { return launch_tc_gemm(t, *map, g->stream); });
   }
   if (ok && oz_fused_x(q.rows, q.N, q.batch)) {
     // the kernel slices its own X columns
@@ -1182,6 +1207,56 @@ int gemm(Group* g, int cls, const GemmArgs& q0, bool reuse = false) {
     }
   }
   return launch(g, cls, gemm_flops(q), [&]() { return launch_gemm(q, g->stream); });
+}
+
+// Consecutive row blocks of one operator applied to one X, each written to
+// its own output (G: omega, psi, u_phi; LAP: psi, u_phi and the two wall
+// vorticity rows).  With the tcgen05 contractions they run as one launch
+// over all the rows (fewer, fuller 128-row tiles, X sliced once), unless an
+// output overlaps X (then a later block reads what an earlier one wrote,
+// and the blocks run one after another as before).
+int gemm_blocks(Group* g, int cls, std::initializer_list<GemmArgs> blocks) {
+  const std::vector<GemmArgs> v(blocks);
+  if (g_gemm_mode.load() == 2 && g->oz_xs && !v.empty() && v.size() <= 4 && v[0].N >= 16) {
+    const GemmArgs& f = v[0];
+    const char* x0 = reinterpret_cast<const char*>(f.X);
+    const char* x1 = reinterpret_cast<const char*>(f.X + (size_t)(f.batch - 1) * f.sX + (size_t)f.K * f.ldx);
+    bool merge = true;
+    int rows = 0;
+    for (const GemmArgs& q : v) {
+      const char* y = reinterpret_cast<const char*>(q.Y);
+      if (q.A != f.A + rows || q.lda != f.lda || q.sA != f.sA || q.X != f.X || q.ldx != f.ldx || q.sX != f.sX ||
+          q.K != f.K || q.N != f.N || q.batch != f.batch || q.ldy != f.ldy || q.sY != f.sY || q.alpha != f.alpha ||
+          (y >= x0 && y < x1))
+        merge = false;
+      rows += q.rows;
+    }
+    if (merge) {
+      GemmArgs all = f;
+      all.rows = rows;
+      all.oz_s = nullptr;
+      all.oz_xs = nullptr;
+      bool ok = attach_oz(g->ops.get(), &all);
+      for (int st = 0; !ok && st < kMaxStages; ++st) ok = attach_oz(g->stage_ops[st].get(), &all);
+      if (ok && all.oz_tmap) {
+        TcArgs t = tc_args(all);
+        t.nout = (int)v.size();
+        int r = 0;
+        for (size_t o = 0; o < v.size(); ++o) {
+          r += v[o].rows;
+          t.rend[o] = r;
+          t.Y[o] = v[o].Y;
+        }
+        const CUtensorMap* map = static_cast<const CUtensorMap*>(all.oz_tmap);
+        return launch(g, cls, gemm_flops(all), [&]() { return launch_tc_gemm(t, *map, g->stream); });
+      }
+    }
+  }
+  for (size_t o = 0; o < v.size(); ++o) {
+    const int rc = gemm(g, cls, v[o], o > 0);
+    if (rc) return rc;
+  }
+  return 0;
 }
 
 int elementwise(Group* g, double flops_per_el, std::function<cudaError_t()> f) {
@@ -1215,9 +1290,9 @@ int solve_all(Group* g, double2* t_out, double2* w_out, double buo_scale, double
     return rc;
   if (M > 1) {
     const long sG = 3L * R * R;
-    if ((rc = gemm(g, KC_GEMM_MODE, per_mode(o->G, 3 * R, sG, g->rhs_w, w_out, R, M, B, 1, M - 1, R))) ||
-        (rc = gemm(g, KC_GEMM_MODE, per_mode(o->G + R, 3 * R, sG, g->rhs_w, g->psi, R, M, B, 1, M - 1, R), true)) ||
-        (rc = gemm(g, KC_GEMM_MODE, per_mode(o->G + 2 * R, 3 * R, sG, g->rhs_w, g->up, R, M, B, 1, M - 1, R), true)))
+    if ((rc = gemm_blocks(g, KC_GEMM_MODE, {per_mode(o->G, 3 * R, sG, g->rhs_w, w_out, R, M, B, 1, M - 1, R),
+                                            per_mode(o->G + R, 3 * R, sG, g->rhs_w, g->psi, R, M, B, 1, M - 1, R),
+                                            per_mode(o->G + 2 * R, 3 * R, sG, g->rhs_w, g->up, R, M, B, 1, M - 1, R)})))
       return rc;
   }
   GemmArgs gu{};
@@ -1478,12 +1553,12 @@ int step_imexrk(Group* g) {
       const int rows = 2 * R + 2;
       const long sL = (long)rows * R;
       double2* psi_tmp = g->rhs_t;  // the reference leaves psii at its last-stage value
-      if ((rc = gemm(g, KC_GEMM_MODE, per_mode(o->LAP, rows, sL, g->rhs_w, psi_tmp, R, M, B, 1, M - 1, R))) ||
-          (rc = gemm(g, KC_GEMM_MODE, per_mode(o->LAP + R, rows, sL, g->rhs_w, g->up, R, M, B, 1, M - 1, R), true)) ||
-          (rc = gemm(g, KC_GEMM_MODE, per_mode(o->LAP + 2 * R, rows, sL, g->rhs_w, g->w0, R, M, B, 1, M - 1, 1),
-                     true)) ||
-          (rc = gemm(g, KC_GEMM_MODE, per_mode(o->LAP + 2 * R + 1, rows, sL, g->rhs_w, g->w0 + (size_t)(R - 1) * M * B,
-                                               R, M, B, 1, M - 1, 1), true)))
+      if ((rc = gemm_blocks(g, KC_GEMM_MODE,
+                            {per_mode(o->LAP, rows, sL, g->rhs_w, psi_tmp, R, M, B, 1, M - 1, R),
+                             per_mode(o->LAP + R, rows, sL, g->rhs_w, g->up, R, M, B, 1, M - 1, R),
+                             per_mode(o->LAP + 2 * R, rows, sL, g->rhs_w, g->w0, R, M, B, 1, M - 1, 1),
+                             per_mode(o->LAP + 2 * R + 1, rows, sL, g->rhs_w, g->w0 + (size_t)(R - 1) * M * B, R, M,
+                                      B, 1, M - 1, 1)})))
         return rc;
     }
     GemmArgs gd{};
@@ -2988,11 +3063,23 @@ int falcon_batch_init_state(falcon_batch* b, int kind, double amp, const uint64_
   return b->sync();
 }
 
+// The tensor-core contraction's bounded waits record a timeout in a device
+// error word instead of hanging; read (and clear) it after a
+// synchronisation.
+static int check_device_waits() {
+  const int v = tc_error_read_and_clear();
+  if (v > 0)
+    return fail(FALCON_ECUDA, "tensor-core contraction: a wait inside the kernel timed out (code " +
+                                  std::to_string(v) + "); its results are invalid");
+  return 0;
+}
+
 int falcon_batch_get_state(falcon_batch* b, int i, double* tFR, double* omgFR, double* upFR, double* urFR,
                            double* psi) {
   if (!b || i < 0 || i >= (int)b->params.size()) return fail(FALCON_EINVAL, "instance index out of range");
   Group* g = b->groups[b->where[i].first].get();
-  return group_get_instance(g, b->where[i].second, tFR, omgFR, upFR, urFR, psi);
+  const int rc = group_get_instance(g, b->where[i].second, tFR, omgFR, upFR, urFR, psi);
+  return rc ? rc : check_device_waits();
 }
 
 int falcon_batch_step(falcon_batch* b, int nsteps) {
@@ -3039,7 +3126,8 @@ int falcon_batch_diagnostics(falcon_batch* b, falcon_diag* out) {
       status = fail(FALCON_EBLOWUP, "kinetic energy above 1e10 in instance " + std::to_string(i));
     }
   }
-  return status;
+  const int wr = check_device_waits();
+  return wr ? wr : status;
 }
 
 int falcon_create(const falcon_params* p, falcon_handle** out) {
@@ -3557,7 +3645,7 @@ extern "C" {
 long long falcon_launch_count(void) { return g_launches.load(); }
 
 int falcon_set_step_graphs(int enable) { return g_graphs.exchange(enable ? 1 : 0); }
-int falcon_set_gemm_mode(int mode) { return g_gemm_mode.exchange(mode ? 1 : 0); }
+int falcon_set_gemm_mode(int mode) { return g_gemm_mode.exchange(mode < 0 || mode > 2 ? 1 : mode); }
 
 int falcon_batch_profile(falcon_batch* b, int nsteps, falcon_kernel_stat* stats, int max_stats, int* nstats) {
   if (!b || nsteps <= 0 || !stats || !nstats) return fail(FALCON_EINVAL, "invalid profile arguments");

@@ -139,6 +139,10 @@ struct GemmArgs {
   const uint16_t* oz_xs;
   const int* oz_cexp;
   int oz_Np;
+  // tensor map (CUtensorMap) of the whole slice array of the operator and
+  // this GEMM's first batch entry in it, for the tcgen05 kernel
+  const void* oz_tmap;
+  int oz_z0;
 };
 
 // ---- FP64 GEMM on bf16 tensor cores by exact slicing (falcon_ozaki.cu) ----
@@ -163,8 +167,9 @@ inline bool oz_fused_x(int rows, int N, int batch) {
 }
 inline int oz_slices(int w) { return w == 7 ? 9 : 10; }
 // Slices of a column-major FP64 operator (rows x K, lda, nb entries of
-// stride sA) into S [nb][S][rowsP][KP] (bf16 bits, zero padded) and row
-// exponents ex [nb][rowsP].
+// stride sA) into S [nb][S][KP/8][rowsP][8] (bf16 bits, zero padded; row r,
+// column k of a slice plane at ((k/8) rowsP + r) 8 + k%8) and row exponents
+// ex [nb][rowsP].
 cudaError_t launch_oz_slice_rows(const double* A, long lda, long sA, int rows, int K, int nb, uint16_t* S, int* ex,
                                  int rowsP, int KP, int w, cudaStream_t s);
 // Slices of the columns of X (K x N, row stride ldx, batch stride sX) into

@@ -40,8 +40,11 @@ namespace {
 }  // namespace
 
 // One thread per (entry, row): the row exponent, then the slices of each
-// element (format W).  The caller zeroes S (padding rows and K columns stay
-// zero).
+// element (format W).  Layout [nb][S][KP/8][rowsP][8]: element (row r, k)
+// of a slice plane at ((k/8) rowsP + r) 8 + k%8, so that 8 consecutive k
+// of a row are 16 contiguous bytes and a k group of all rows is one
+// contiguous block (the tile shape both tensor-core kernels stage).  The
+// caller zeroes S (padding rows and K columns stay zero).
 template <int W>
 __global__ void oz_slice_rows_kernel(const double* A, long lda, long sA, int rows, int K, int nb, uint16_t* S,
                                      int* ex, int rowsP, int KP) {
@@ -54,13 +57,14 @@ __global__ void oz_slice_rows_kernel(const double* A, long lda, long sA, int row
   for (int k = 0; k < K; ++k) mx = max(mx, biased_exp(a[(size_t)k * lda]));
   const int e = mx - 1022;  // |a| < 2^e for every entry of the row
   ex[(size_t)z * rowsP + r] = mx ? e : 0;
-  uint16_t* s0 = S + (size_t)z * C::S * rowsP * KP + (size_t)r * KP;
+  uint16_t* s0 = S + (size_t)z * C::S * rowsP * KP + (size_t)r * 8;
   const size_t sls = (size_t)rowsP * KP;
   for (int k = 0; k < K; ++k) {
     const double v = a[(size_t)k * lda];
     const unsigned long long T = mx ? oz_magb<C::MAGB>(v, e) : 0ull;
+    const size_t at = (size_t)(k >> 3) * rowsP * 8 + (k & 7);
 #pragma unroll
-    for (int sl = 0; sl < C::S; ++sl) s0[sl * sls + k] = (uint16_t)oz_slice_w<W>(T, v < 0, sl);
+    for (int sl = 0; sl < C::S; ++sl) s0[sl * sls + at] = (uint16_t)oz_slice_w<W>(T, v < 0, sl);
   }
 }
 
@@ -162,7 +166,7 @@ __global__ void __launch_bounds__(32 * MT * NQ * (2 / NT), MINB) oz_mma_kernel(G
   extern __shared__ __align__(16) uint16_t oz_panel[];   // [2][ASTAGE + XSTAGE] (+ FX: planes, exponents)
   const int z = blockIdx.z;
   const int col0 = blockIdx.x * CW, row0b = blockIdx.y * MT * 16;
-  const uint16_t* Az = q.oz_s + (size_t)z * q.oz_sz + (size_t)(q.oz_row0 + row0b) * q.oz_KP;
+  const uint16_t* Az = q.oz_s + (size_t)z * q.oz_sz + (size_t)(q.oz_row0 + row0b) * 8;
   const size_t aslice = (size_t)q.oz_rowsP * q.oz_KP;
   const uint16_t* Xz = FX ? nullptr : q.oz_xs + (size_t)z * C::S * q.oz_KP * q.oz_Np + col0;
   const size_t xslice = (size_t)q.oz_KP * q.oz_Np;
@@ -174,7 +178,8 @@ __global__ void __launch_bounds__(32 * MT * NQ * (2 / NT), MINB) oz_mma_kernel(G
     uint16_t* Xp = Ap + ASTAGE;
     for (int i = tid; i < C::S * MT * 16 * 2; i += nthr) {        // A: (slice, row, half)
       const int h = i & 1, rr = (i >> 1) % (MT * 16), sl = (i >> 1) / (MT * 16);
-      cp_async16(Ap + (sl * MT * 16 + rr) * AROW + 8 * h, Az + sl * aslice + (size_t)rr * q.oz_KP + k0 + 8 * h);
+      cp_async16(Ap + (sl * MT * 16 + rr) * AROW + 8 * h,
+                 Az + sl * aslice + ((size_t)((k0 >> 3) + h) * q.oz_rowsP + rr) * 8);
     }
     if constexpr (!FX) {
       for (int i = tid; i < C::S * 16 * 2 * NQ; i += nthr) {      // X: (slice, k, 8-column chunk)

@@ -448,10 +448,11 @@ def set_max_group_size(n):
 
 
 def set_gemm_mode(mode):
-    """1: operator contractions on the tensor cores by exact slicing; 0: FP64 FMA tiles.
-    Returns the previous mode."""
+    """Operator contractions: 2 on the tcgen05 tensor cores by exact slicing
+    (accumulators in tensor memory), 1 on the mma.sync tensor-core path with
+    the same slices, 0 as FP64 FMA tiles.  Returns the previous mode."""
     lib().falcon_set_gemm_mode.argtypes = [ctypes.c_int]
-    return lib().falcon_set_gemm_mode(1 if mode else 0)
+    return lib().falcon_set_gemm_mode(int(mode))
 
 
 def set_step_graphs(enable):
