@@ -228,6 +228,31 @@ def mixed_requests(fg, n, seed):
     return out
 
 
+def run_plain(args, fg, stream, torch):
+    """The plain reference run: one instance, Nr=33, Ntheta=128 (Nm=42,
+    Np=126), CNAB2, dt=1e-5, Ra=1e5, Pr=1, seed 1, stepped alone (its
+    latency per step and rate)."""
+    p = fg.make_params(33, 42, "CNAB2", ra=1e5, dt=1e-5, pr=1.0)
+    it = fg.Instance(p)
+    it.set_stream(stream.cuda_stream)
+    it.init_noise(1, 1e-3)
+    with torch.cuda.stream(stream):
+        it.step(gpu_warmup(args))
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    k = args.plain_steps
+    ev0.record(stream)
+    it.step(k)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    finite = bool(np.isfinite(it.get_state()["T"]).all())
+    it.close()
+    return {"value": k / (ms / 1e3), "unit": "instance-steps/s", "steps": k, "ms_per_step": ms / k,
+            "state_finite": finite,
+            "workload": "one instance Nr=33, Ntheta=128 (Nm=42, Np=126), CNAB2, dt=1e-5, Ra=1e5, Pr=1, seed 1"}
+
+
 def run_uneven(args, fg, stream, torch):
     """The uneven batch: 512 mixed instances stepped together (one group per
     operator key, groups on concurrent streams, steady steps replayed from
@@ -398,6 +423,7 @@ def run_gpu(args):
     falcon_build.build()
     fg.lib()
     stream = torch.cuda.Stream()
+    fg.set_gemm_mode(args.gemm_mode)
     W = WORKLOAD
     n = args.instances or W["n"]
     ras, seeds = shard(rank, n)
@@ -534,6 +560,7 @@ def run_gpu(args):
         it.close()
 
     uneven = serving = None
+    plain = run_plain(args, fg, stream, torch)
     single = run_single(args, fg, stream, torch)
     if not args.no_mixed:
         uneven = run_uneven(args, fg, stream, torch)
@@ -546,9 +573,12 @@ def run_gpu(args):
     cpu = None
     if not args.no_cpu:
         rate, nst, secs = cpu_port_rate(args.cpu_seconds)
+        rate1, nst1, secs1 = cpu_port_rate(args.cpu_seconds, threads=1)
         cpu = {"value": rate, "unit": "instance-steps/s", "cores": os.cpu_count(), "kind": "port",
                "sample": f"{nst} time steps of one workload instance (Nr=65, Nm=170, SBDF3) in {secs:.1f} s, "
-                         "CPU oracle with OpenMP over modes on all host threads"}
+                         "CPU oracle with OpenMP over modes on all host threads",
+               "one_thread": {"value": rate1, "unit": "instance-steps/s", "cores": 1,
+                              "sample": f"{nst1} time steps in {secs1:.1f} s, OMP_NUM_THREADS=1"}}
     line = {
         "metric": METRIC, "value": value, "unit": "instance-steps/s", "n_gpus": world, "steps": args.steps,
         "warmup": gpu_warmup(args), "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -561,9 +591,8 @@ def run_gpu(args):
                    "groups": "the instances run as groups of at most 128 sharing the operators, one stream each "
                              "(falcon_set_max_group_size default), so one group's nonlinear pass overlaps "
                              "another's contractions; the roofline classes time the groups one after another"},
-        "one_at_a_time": {"value": one_rate, "unit": "instance-steps/s", "instances": n1, "steps": k1,
-                          "batched_over_one_at_a_time": value / world / one_rate},
         "e2e": e2e,
+        "plain_reference_run": plain,
         "single_instance": single,
         "uneven_batch": uneven,
         "serving": serving,
@@ -571,8 +600,11 @@ def run_gpu(args):
         "cpu_baseline": cpu,
         "clocks": clk.summary(),
         "gpu_launches": launches,
-        "device_bytes_per_batch": None,
+        "gemm_mode": {2: "tcgen05 (tensor memory accumulators)", 1: "mma.sync", 0: "FP64 FMA"}[args.gemm_mode],
         "state_finite": bool(finite),
+        # last, so that a reader of the line's tail sees the target ratio
+        "one_at_a_time": {"value": one_rate, "unit": "instance-steps/s", "instances": n1, "steps": k1},
+        "batched_over_one_at_a_time": value / world / one_rate,
     }
     print(json.dumps(line), flush=True)
     if world > 1:
@@ -591,6 +623,9 @@ def main():
     ap.add_argument("--no-cpu", dest="no_cpu", action="store_true")
     ap.add_argument("--no-mixed", dest="no_mixed", action="store_true", help="skip the uneven batch and serving")
     ap.add_argument("--single-steps", dest="single_steps", type=int, default=200)
+    ap.add_argument("--plain-steps", dest="plain_steps", type=int, default=500)
+    ap.add_argument("--gemm-mode", dest="gemm_mode", type=int, default=1, choices=[0, 1, 2],
+                    help="operator contractions: 2 tcgen05, 1 mma.sync slices, 0 FP64 FMA")
     ap.add_argument("--uneven-instances", dest="uneven_instances", type=int, default=512)
     ap.add_argument("--uneven-steps", dest="uneven_steps", type=int, default=100)
     ap.add_argument("--serve-rate", dest="serve_rate", type=float, default=50.0)

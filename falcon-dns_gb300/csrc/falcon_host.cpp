@@ -863,6 +863,10 @@ struct Group {
   double* u0 = nullptr;
   double* us = nullptr;        // explicit RK: stage uphi_bar (R x B)
   double2* t_grid = nullptr;   // temperature seen by the last nonlinear pass (IMEXRK)
+  double* up0_prev = nullptr;  // [r][b] Re u_phi(m = 0) at the start of the step (upFR_prev)
+  double* spec_dev = nullptr;  // [2][b][m] KE and temperature spectra
+  double* ubal_dev = nullptr;  // [b][r][3] u_phi balance
+  double2* d1up = nullptr;     // d(u_phi)/dr of every mode (made on the first balance request)
   double* diag_dev = nullptr;  // 8 per instance
   double* diag_part = nullptr;  // 8 R per instance: diagnostics partial sums
   std::vector<double> diag_host;
@@ -898,6 +902,7 @@ struct Group {
   double dt_new = 0.0;
   double* umax = nullptr;
   std::vector<double> umax_h, dr_h, radius_h;
+  std::vector<double> spec_host, ubal_host;
   double cur_dt() const { return vardt ? dt_new : p.dt; }
 
   void drop_graphs() {
@@ -1056,7 +1061,9 @@ int group_init(Group* g, const std::vector<falcon_params>& ps, const std::vector
       (rc = g->alloc(&g->lt, n)) || (rc = g->alloc(&g->lw, n)) || (rc = g->alloc(&g->lu0, (size_t)R * B)) ||
       (rc = g->alloc(&g->rhs_t, n)) || (rc = g->alloc(&g->rhs_w, n)) ||
       (rc = g->alloc(&g->ub2, (size_t)2 * R * B)) || (rc = g->alloc(&g->ra_pr, (size_t)B)) ||
-      (rc = g->alloc(&g->diag_dev, (size_t)8 * B)) || (rc = g->alloc(&g->diag_part, (size_t)8 * R * B)))
+      (rc = g->alloc(&g->diag_dev, (size_t)8 * B)) || (rc = g->alloc(&g->diag_part, (size_t)8 * R * B)) ||
+      (rc = g->alloc(&g->up0_prev, (size_t)R * B)) || (rc = g->alloc(&g->spec_dev, (size_t)2 * g->M * B)) ||
+      (rc = g->alloc(&g->ubal_dev, (size_t)3 * R * B)))
     return rc;
   g->ub = reinterpret_cast<double*>(g->ub2);
   if (g->p.l_vartimestep) {
@@ -1426,6 +1433,7 @@ int step_imex(Group* g) {
   const int h_new = (g->head + ni - 1) % ni;
   RhsArgs a{};
   a.R = R; a.M = M; a.B = B;
+  a.up = g->up; a.up0_prev = g->up0_prev;
   a.inv_r = o->inv_r; a.inv_r2 = o->inv_r2; a.ra_pr = g->ra_pr;
   a.dt = g->cur_dt(); a.inv_pr = 1.0 / g->p.pr;
   a.scheme_cn = cn ? 1 : 0;
@@ -1700,6 +1708,11 @@ void group_advance(Group* g) {
 // CUDA graph and replayed: one launch instead of 11 (IMEX) to ~60 (IMEXRK)
 // kernel launches, which lets many small groups keep the GPU busy.
 int group_step(Group* g) {
+  // upFR_prev = upFR at the start of a run (src/init.F90:253); the IMEX
+  // loop renews it every step after the nonlinear pass (in imex_rhs_kernel),
+  // the IMEXRK and RK loops keep it
+  if (g->n_step == 0 || g->restart_first)
+    CK(launch_extract_mode0(g->R, g->M, g->B, g->up, g->up0_prev, g->stream));
   if (!g_graphs.load() || g->prof || g->n_step < 1 || g->vardt) return group_step_direct(g);
   const int phase = g->head * 8 + g->head_e;
   for (auto& sg : g->graphs)
@@ -2547,6 +2560,40 @@ int group_diagnostics(Group* g) {
   return 0;
 }
 
+// calculate_spectra (src/output.F90:327-355) of every instance of the
+// group, to the host: spec_host [2][B][M].
+int group_spectra(Group* g) {
+  OpSet* o = g->ops.get();
+  const double four_pi = 16.0 * std::atan(1.0);
+  const size_t nm = (size_t)g->M * g->B;
+  CK(launch_spectra(g->R, g->M, g->B, g->T(), g->ur, g->up, o->wq, four_pi, g->spec_dev, g->spec_dev + nm,
+                    g->stream));
+  g->spec_host.resize(2 * nm);
+  CK(cudaMemcpyAsync(g->spec_host.data(), g->spec_dev, sizeof(double) * 2 * nm, cudaMemcpyDeviceToHost, g->stream));
+  CK(cudaStreamSynchronize(g->stream));
+  return 0;
+}
+
+// The u_phi balance (src/output.F90:145-228) of every instance, to the host:
+// ubal_host [B][R][3].
+int group_upbalance(Group* g) {
+  OpSet* o = g->ops.get();
+  const int R = g->R, M = g->M, B = g->B;
+  if (!g->d1up) {
+    int rc = g->alloc(&g->d1up, g->nel());
+    if (rc) return rc;
+  }
+  GemmArgs q = radial(o->D1p, g->up, g->d1up, R, M, B);  // FP64 FMA tiles (no slice view attached)
+  CK(launch_gemm(q, g->stream));
+  CK(launch_upbalance(R, M, B, g->ur, g->up, g->d1up, g->up0_prev, o->Lp, o->inv_r, o->inv_r2, g->cur_dt(),
+                      g->ubal_dev, g->stream));
+  g->ubal_host.resize((size_t)3 * R * B);
+  CK(cudaMemcpyAsync(g->ubal_host.data(), g->ubal_dev, sizeof(double) * 3 * R * B, cudaMemcpyDeviceToHost,
+                     g->stream));
+  CK(cudaStreamSynchronize(g->stream));
+  return 0;
+}
+
 void fill_diag(const Group* g, int b, double time, falcon_diag* d) {
   const double* v = &g->diag_host[(size_t)8 * b];
   d->time = time; d->dt = g->cur_dt();
@@ -3205,6 +3252,47 @@ int falcon_step(falcon_handle* h, int nsteps) {
 int falcon_diagnostics(falcon_handle* h, falcon_diag* out) {
   if (!h) return fail(FALCON_EINVAL, "null handle");
   return falcon_batch_diagnostics(h->b, out);
+}
+
+int falcon_batch_spectra(falcon_batch* b, int i, double* kespec, double* tspec) {
+  if (!b || i < 0 || i >= (int)b->params.size() || !kespec || !tspec)
+    return fail(FALCON_EINVAL, "falcon_batch_spectra: invalid arguments");
+  Group* g = b->groups[b->where[i].first].get();
+  int rc = group_spectra(g);
+  if (rc) return rc;
+  const int slot = b->where[i].second, M = g->M;
+  const double* ke = g->spec_host.data() + (size_t)slot * M;
+  const double* ts = g->spec_host.data() + (size_t)g->B * M + (size_t)slot * M;
+  std::copy(ke, ke + M, kespec);
+  std::copy(ts, ts + M, tspec);
+  return check_device_waits();
+}
+
+int falcon_batch_upbalance(falcon_batch* b, int i, double* out) {
+  if (!b || i < 0 || i >= (int)b->params.size() || !out) return fail(FALCON_EINVAL, "falcon_batch_upbalance: invalid arguments");
+  Group* g = b->groups[b->where[i].first].get();
+  int rc = group_upbalance(g);
+  if (rc) return rc;
+  const int slot = b->where[i].second, R = g->R;
+  const Cheb c = make_cheb(R, g->p.eta);
+  for (int r = 0; r < R; ++r) {
+    const double* v = g->ubal_host.data() + ((size_t)slot * R + r) * 3;
+    out[4 * r + 0] = c.radius[r];
+    out[4 * r + 1] = v[0];
+    out[4 * r + 2] = v[1];
+    out[4 * r + 3] = v[2];
+  }
+  return check_device_waits();
+}
+
+int falcon_spectra(falcon_handle* h, double* kespec, double* tspec) {
+  if (!h) return fail(FALCON_EINVAL, "null handle");
+  return falcon_batch_spectra(h->b, 0, kespec, tspec);
+}
+
+int falcon_upbalance(falcon_handle* h, double* out) {
+  if (!h) return fail(FALCON_EINVAL, "null handle");
+  return falcon_batch_upbalance(h->b, 0, out);
 }
 
 int falcon_batch_store_checkpoint(falcon_batch* b, int i, const char* path) {

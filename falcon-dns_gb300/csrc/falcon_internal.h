@@ -207,6 +207,8 @@ struct RhsArgs {
   const double2 *lt, *lw;   // L T and L omega (CN)
   const double2* lu0;       // L applied to uphi_bar, [r][b] complex (CN)
   double2 *rhs_t, *rhs_w;
+  const double2* up;        // u_phi at the start of the step
+  double* up0_prev;         // [r][b]: Re u_phi(m = 0) recorded there (optional)
 };
 
 // IMEXRK stage arguments (src/fourierloop_imexrk.F90).
@@ -284,6 +286,13 @@ cudaError_t launch_remap_cols(const double* src, double* dst, size_t rows, int b
 // Column b of a [rows][B] array: dst = src (or zero when src is null).
 cudaError_t launch_col_op(const double* src, double* dst, size_t rows, int B, int b, int ew, cudaStream_t s);
 cudaError_t launch_diagnostics(const DiagArgs& a, cudaStream_t s);
+// calculate_spectra of every instance: ke, ts [b][m] (x four_pi)
+cudaError_t launch_spectra(int R, int M, int B, const double2* t, const double2* ur, const double2* up,
+                           const double* wq, double four_pi, double* ke, double* ts, cudaStream_t s);
+// u_phi balance of every instance: out [b][r][3] = d(up_0)/dt, advection, diffusion
+cudaError_t launch_upbalance(int R, int M, int B, const double2* ur, const double2* up, const double2* d1up,
+                             const double* up0_prev, const double* Lp, const double* inv_r, const double* inv_r2,
+                             double dt, double* out, cudaStream_t s);
 cudaError_t launch_assembly(const AsmArgs& a, cudaStream_t s);
 cudaError_t launch_assembly_post(int R, int M, int B, const double* inv_r, const double2* psi, const double* u0,
                                  const double* du0, double2* ur, double2* up, double2* w0, cudaStream_t s);

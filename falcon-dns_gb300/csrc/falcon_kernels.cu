@@ -1273,6 +1273,9 @@ __global__ void imex_rhs_kernel(RhsArgs a) {
     const unsigned r = (unsigned)(rm / M), m = (unsigned)(rm - (size_t)r * M);
     const double ir = a.inv_r[r];
     const double dm = (double)(int)m, dmir = dm * ir;
+    // upFR_prev = upFR after the nonlinear pass (src/steptime.F90:212), for
+    // the u_phi balance of the diagnostics
+    if (m == 0 && a.up0_prev) a.up0_prev[(size_t)r * B + b] = a.up[e].x;
     // explicit (advective) term of T: i m r^-1 (uphi T) + d(ur T)/dr + r^-1 (ur T)
     {
       const double2 p = a.ntp[e], q = a.ntr[e], dq = a.dntr[e];
@@ -2008,6 +2011,77 @@ __global__ void diag_sum_kernel(DiagArgs a) {
 cudaError_t launch_diagnostics(const DiagArgs& a, cudaStream_t s) {
   diag_rows_kernel<<<dim3(a.R, (a.B + 31) / 32), dim3(32, 8), 0, s>>>(a);
   diag_sum_kernel<<<(a.B + 3) / 4, 128, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+// calculate_spectra (src/output.F90:327-355) of every instance, one thread
+// per (mode, instance): 4 pi radInt of |ur_m ur_m + up_m up_m| (complex
+// squares, as the reference forms them) and of |T_m|; wq are the radInt
+// weights on the values.  Output [b][m].
+__global__ void spectra_kernel(int R, int M, int B, const double2* t, const double2* ur, const double2* up,
+                               const double* wq, double four_pi, double* ke, double* ts) {
+  const long idx = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (idx >= (long)M * B) return;
+  const int m = (int)(idx / B), b = (int)(idx - (long)m * B);
+  double sk = 0.0, st = 0.0;
+  for (int r = 0; r < R; ++r) {
+    const size_t e = ((size_t)r * M + m) * B + b;
+    const double2 u = ur[e], v = up[e], T = t[e];
+    const double ar = u.x * u.x - u.y * u.y, ai = u.x * u.y + u.y * u.x;
+    const double br = v.x * v.x - v.y * v.y, bi = v.x * v.y + v.y * v.x;
+    sk += wq[r] * hypot(ar + br, ai + bi);
+    st += wq[r] * hypot(T.x, T.y);
+  }
+  ke[(size_t)b * M + m] = four_pi * sk;
+  ts[(size_t)b * M + m] = four_pi * st;
+}
+
+cudaError_t launch_spectra(int R, int M, int B, const double2* t, const double2* ur, const double2* up,
+                           const double* wq, double four_pi, double* ke, double* ts, cudaStream_t s) {
+  spectra_kernel<<<ew_grid((size_t)M * B), 256, 0, s>>>(R, M, B, t, ur, up, wq, four_pi, ke, ts);
+  return cudaGetLastError();
+}
+
+// The u_phi balance of writeKE_spectral (src/output.F90:145-228), one thread
+// per (radius, instance): d(up_0)/dt against the value at the start of the
+// step (up0_prev), the advection -(ur d(up)/dr + ur up / r) summed over
+// modes as the reference forms it (the m = 0 product, conjugate pairs for
+// m >= 1; real parts), and the diffusion d2 up_0/dr2 + (d up_0/dr) / r -
+// up_0 / r^2 = (Lp up_0) - up_0 / r^2.  d1up = d(up)/dr of every mode.
+// Output [b][r][3].
+__global__ void upbalance_kernel(int R, int M, int B, const double2* ur, const double2* up, const double2* d1up,
+                                 const double* up0_prev, const double* Lp, const double* inv_r,
+                                 const double* inv_r2, double dt, double* out) {
+  const long idx = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (idx >= (long)R * B) return;
+  const int r = (int)(idx / B), b = (int)(idx - (long)r * B);
+  double p = 0.0, q = 0.0;
+  for (int m = 0; m < M; ++m) {
+    const size_t e = ((size_t)r * M + m) * B + b;
+    const double2 u = ur[e], w = up[e], dw = d1up[e];
+    if (m == 0) {
+      p += u.x * w.x - u.y * w.y;
+      q += u.x * dw.x - u.y * dw.y;
+    } else {
+      p += 2.0 * (u.x * w.x + u.y * w.y);
+      q += 2.0 * (u.x * dw.x + u.y * dw.y);
+    }
+  }
+  const size_t e0 = ((size_t)r * M) * B + b;
+  const double u0 = up[e0].x;
+  double lap = 0.0;
+  for (int k = 0; k < R; ++k) lap += Lp[r + (size_t)R * k] * up[((size_t)k * M) * B + b].x;
+  double* o = out + ((size_t)b * R + r) * 3;
+  o[0] = (u0 - up0_prev[(size_t)r * B + b]) / dt;
+  o[1] = -(q + inv_r[r] * p);
+  o[2] = lap - inv_r2[r] * u0;
+}
+
+cudaError_t launch_upbalance(int R, int M, int B, const double2* ur, const double2* up, const double2* d1up,
+                             const double* up0_prev, const double* Lp, const double* inv_r, const double* inv_r2,
+                             double dt, double* out, cudaStream_t s) {
+  upbalance_kernel<<<ew_grid((size_t)R * B), 256, 0, s>>>(R, M, B, ur, up, d1up, up0_prev, Lp, inv_r, inv_r2, dt,
+                                                          out);
   return cudaGetLastError();
 }
 

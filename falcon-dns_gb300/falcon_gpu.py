@@ -103,7 +103,8 @@ EXPORTS = (
     "falcon_nonlin_noalloc_dev", "falcon_set_step_graphs", "falcon_store_checkpoint", "falcon_load_checkpoint",
     "falcon_store_snapshot", "falcon_batch_store_checkpoint", "falcon_batch_load_checkpoint",
     "falcon_batch_store_snapshot", "falcon_restart", "falcon_batch_restart", "falcon_set_gemm_mode",
-    "falcon_upload_factors", "falcon_cheb_d1d2_dev",
+    "falcon_upload_factors", "falcon_cheb_d1d2_dev", "falcon_spectra", "falcon_upbalance",
+    "falcon_batch_spectra", "falcon_batch_upbalance",
 )
 
 
@@ -171,6 +172,10 @@ def lib():
     L.falcon_upload_factors.argtypes = [vp, dp, P(ctypes.c_int), dp, P(ctypes.c_int), dp, P(ctypes.c_int), dp,
                                         P(ctypes.c_int)]
     L.falcon_cheb_d1d2_dev.argtypes = [ip, ip, vp, vp, vp, vp]
+    L.falcon_spectra.argtypes = [vp, dp, dp]
+    L.falcon_upbalance.argtypes = [vp, dp]
+    L.falcon_batch_spectra.argtypes = [vp, ip, dp, dp]
+    L.falcon_batch_upbalance.argtypes = [vp, ip, dp]
     L.falcon_batch_restart.argtypes = [vp, P(ctypes.c_char_p)]
     _lib = L
     return L
@@ -309,6 +314,19 @@ class Batch:
         check(lib().falcon_batch_diagnostics(self.h, out))
         return [d.as_dict() for d in out]
 
+    def spectra(self, i):
+        """calculate_spectra of instance i: (KEspec, Temp_spec), Nm_max + 1 modes."""
+        M = self.params[i].nm_max + 1
+        ke, ts = np.zeros(M), np.zeros(M)
+        check(lib().falcon_batch_spectra(self.h, i, _dp(ke), _dp(ts)))
+        return ke, ts
+
+    def upbalance(self, i):
+        """The u_phi balance of instance i: (Nr, 4) = radius, d(up_0)/dt, advection, diffusion."""
+        out = np.zeros((self.params[i].nr_max, 4))
+        check(lib().falcon_batch_upbalance(self.h, i, _dp(out)))
+        return out
+
     def diagnostics_array(self):
         """The same values as diagnostics() in one numpy structured array
         (fields time, dt, ke, ...; one record per instance), without the
@@ -360,6 +378,12 @@ class Instance(Batch):
 
     def diagnostics(self):
         return super().diagnostics()[0]
+
+    def spectra(self, i=0):
+        return super().spectra(0)
+
+    def upbalance(self, i=0):
+        return super().upbalance(0)
 
     def store_checkpoint(self, path):
         super().store_checkpoint(0, path)

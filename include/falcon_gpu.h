@@ -161,6 +161,19 @@ int falcon_upload_factors(falcon_handle* h, const double* AT, const int* ipiv_T,
  * src/steptime_imexrk.F90:96-190). */
 int falcon_step(falcon_handle* h, int nsteps);
 int falcon_diagnostics(falcon_handle* h, falcon_diag* out);
+/* calculate_spectra (src/output.F90:327-355) of the current state:
+ * kespec[m] = 4 pi radInt(|ur_m ur_m + up_m up_m|) and tspec[m] =
+ * 4 pi radInt(|T_m|) for m = 0..Nm_max (the KEspec_<tag> and
+ * Temp_spec_<tag> columns). */
+int falcon_spectra(falcon_handle* h, double* kespec, double* tspec);
+/* The u_phi force balance that writeKE_spectral appends to upbalance_<tag>
+ * (src/output.F90:145-228): out[4 r + 0..3] for r = 0..Nr_max-1 = radius,
+ * real(up_0 - upFR_prev_0)/dt, the advection -(ur d(up)/dr + ur up / r)
+ * over all modes and the diffusion d2 up_0/dr2 - up_0/r^2 + (d up_0/dr)/r.
+ * upFR_prev is u_phi at the start of a run and, in the IMEX multistep
+ * loop, after each step's nonlinear pass (src/init.F90:253,
+ * src/steptime.F90:212). */
+int falcon_upbalance(falcon_handle* h, double* out);
 /* Checkpoint file in the layout of store_checkpoint (src/output.F90:359-447,
  * Fortran unformatted sequential records): dt_new, tot_time, Nm_max, Nr_max
  * and the time-scheme orders; dt_array; tFR, omgFR, urFR, upFR; the history
@@ -228,6 +241,9 @@ int falcon_batch_get_state(falcon_batch* b, int i, double* tFR, double* omgFR, d
                            double* urFR, double* psi);
 int falcon_batch_step(falcon_batch* b, int nsteps);
 int falcon_batch_diagnostics(falcon_batch* b, falcon_diag* out /* n entries */);
+/* falcon_spectra / falcon_upbalance of instance i. */
+int falcon_batch_spectra(falcon_batch* b, int i, double* kespec, double* tspec);
+int falcon_batch_upbalance(falcon_batch* b, int i, double* out);
 /* Checkpoint / snapshot of instance i (as the falcon_handle forms).  A load
  * sets the time and step count of instance i's group: load every instance
  * of a group from checkpoints of the same run time. */

@@ -97,6 +97,13 @@ int orc_sim_step(orc_sim* s, int nsteps);
  * out[0]=KE_tot out[1]=KE_r out[2]=KE_phi out[3]=KE_upbar out[4]=Nu_top
  * out[5]=Nu_bot out[6]=viscous dissipation out[7]=buoyancy power out[8]=time */
 int orc_sim_diagnostics(orc_sim* s, double* out);
+/* calculate_spectra (src/output.F90:327-355): kespec, tspec of Nm_max+1
+ * modes (already x 4 pi). */
+int orc_sim_spectra(orc_sim* s, double* kespec, double* tspec);
+/* The u_phi balance written to upbalance_<tag> by writeKE_spectral
+ * (src/output.F90:145-228): out[4 r + 0..3] = radius, d(up_0)/dt from
+ * upFR_prev, advection, diffusion. */
+int orc_sim_upbalance(orc_sim* s, double* out);
 int orc_sim_nstep(const orc_sim* s);
 /* Current time step (dt_new; changes with l_vartimestep). */
 double orc_sim_dt(const orc_sim* s);

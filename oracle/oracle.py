@@ -101,6 +101,8 @@ def lib():
         L.orc_sim_dt.restype = ctypes.c_double
         L.orc_noise_pair.argtypes = [ctypes.c_uint64, ctypes.c_int, ctypes.c_int, dp, dp]
         L.orc_set_threads.argtypes = [ctypes.c_int]
+        L.orc_sim_spectra.argtypes = [ctypes.c_void_p, dp, dp]
+        L.orc_sim_upbalance.argtypes = [ctypes.c_void_p, dp]
         L.orc_mat_assemble.argtypes = [ctypes.POINTER(OrcParams), ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                        ctypes.c_double, ctypes.c_int, dp]
         _lib = L
@@ -270,6 +272,21 @@ class Sim:
         rc = lib().orc_sim_step(self.h, n)
         if rc != 0:
             raise RuntimeError("oracle step failed")
+
+    def spectra(self):
+        """calculate_spectra: (KEspec, Temp_spec) of modes 0..Nm_max (x 4 pi)."""
+        M = self.p.nm_max + 1
+        ke = np.zeros(M)
+        ts = np.zeros(M)
+        lib().orc_sim_spectra(self.h, _dp(ke), _dp(ts))
+        return ke, ts
+
+    def upbalance(self):
+        """The u_phi balance columns of upbalance_<tag>: (Nr, 4) = radius,
+        d(up_0)/dt, advection, diffusion."""
+        out = np.zeros((self.p.nr_max, 4))
+        lib().orc_sim_upbalance(self.h, _dp(out))
+        return out
 
     def diagnostics(self):
         out = np.empty(9)

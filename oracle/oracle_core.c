@@ -2225,6 +2225,80 @@ int orc_sim_diagnostics(orc_sim* s, double* out) {
   return 0;
 }
 
+/* calculate_spectra (src/output.F90:327-355): per mode m, 4 pi radInt of
+ * |ur_m ur_m + up_m up_m| (complex squares) and of |T_m|. */
+int orc_sim_spectra(orc_sim* s, double* kespec, double* tspec) {
+  int R = s->R, M = s->M;
+  const double pi = PI_;
+  double* ek = zalloc(R);
+  double* ts = zalloc(R);
+  for (int m = 0; m < M; ++m) {
+    for (int r = 0; r < R; ++r) {
+      const double* u = CX(s->urFR, m, r); const double* v = CX(s->upFR, m, r); const double* t = CX(s->tFR, m, r);
+      double ar, ai, br, bi;
+      cmul(u[0], u[1], u[0], u[1], &ar, &ai);
+      cmul(v[0], v[1], v[0], v[1], &br, &bi);
+      ek[r] = hypot(ar + br, ai + bi);
+      ts[r] = hypot(t[0], t[1]);
+    }
+    kespec[m] = 4.0 * pi * radint(s, ek);
+    tspec[m] = 4.0 * pi * radint(s, ts);
+  }
+  free(ek);
+  free(ts);
+  return 0;
+}
+
+/* The u_phi force balance of writeKE_spectral (src/output.F90:145-228):
+ * per radius r (out[4 r + 0..3]): radius, real((upFR(0) - upFR_prev(0))/dt),
+ * the advection real(-(ur d(up)/dr + ur up / r)) summed over modes as the
+ * reference forms it (m = 0 product, conjugate pairs for m >= 1), and the
+ * diffusion real(d2 up_0/dr2 - up_0/r^2 + d up_0/dr / r), the derivatives
+ * from chebinvtranD1/D2 of upFC. */
+int orc_sim_upbalance(orc_sim* s, double* out) {
+  int R = s->R, M = s->M;
+  double* d1 = zalloc(2 * (size_t)M * R);
+  double* d2 = zalloc(2 * (size_t)M * R);
+  double* c = zalloc(2 * (size_t)R);
+  double* v = zalloc(2 * (size_t)R);
+  for (int m = 0; m < M; ++m) {
+    get_mode(s, s->upFC, m, c);
+    orc_chebinvtranD1(R, c, v);
+    put_mode(s, d1, m, v);
+    orc_chebinvtranD2(R, c, v);
+    put_mode(s, d2, m, v);
+  }
+  for (int r = 0; r < R; ++r) {
+    double pr = 0.0, pi_ = 0.0, qr = 0.0, qi = 0.0;  /* ur_up_FR, ur_d1up_FR */
+    for (int m = 0; m < M; ++m) {
+      const double* u = CX(s->urFR, m, r); const double* w = CX(s->upFR, m, r);
+      const double* dw = d1 + 2 * ((size_t)m + (size_t)M * r);
+      double ar, ai, br, bi;
+      if (m == 0) {
+        cmul(u[0], u[1], w[0], w[1], &ar, &ai);
+        pr = pr + ar; pi_ = pi_ + ai;
+        cmul(u[0], u[1], dw[0], dw[1], &ar, &ai);
+        qr = qr + ar; qi = qi + ai;
+      } else {
+        cmul(u[0], u[1], w[0], -w[1], &ar, &ai);
+        cmul(u[0], -u[1], w[0], w[1], &br, &bi);
+        pr = pr + (ar + br); pi_ = pi_ + (ai + bi);
+        cmul(u[0], u[1], dw[0], -dw[1], &ar, &ai);
+        cmul(u[0], -u[1], dw[0], dw[1], &br, &bi);
+        qr = qr + (ar + br); qi = qi + (ai + bi);
+      }
+    }
+    const double* u0 = CX(s->upFR, 0, r); const double* up0 = CX(s->upFR_prev, 0, r);
+    const double* d10 = d1 + 2 * ((size_t)M * r); const double* d20 = d2 + 2 * ((size_t)M * r);
+    out[4 * r + 0] = s->radius[r];
+    out[4 * r + 1] = (u0[0] - up0[0]) / s->dt_new;
+    out[4 * r + 2] = -(qr + s->r_radius[r] * pr);
+    out[4 * r + 3] = d20[0] - s->r_radius2[r] * u0[0] + s->r_radius[r] * d10[0];
+  }
+  free(d1); free(d2); free(c); free(v);
+  return 0;
+}
+
 /* ------------------------------------------------------------------------ */
 /* Checkpoint and snapshot files: store_checkpoint / store_checkpoint_imexrk */
 /* and store_snapshot (src/output.F90:359-516), Fortran unformatted          */
