@@ -1,8 +1,9 @@
 """Builds libfalcon_gpu.so (sm_103a) in-tree under falcon-dns_gb300/_build/.
 
-Two translation units compiled in parallel: the CUDA kernels with nvcc
-(-gencode arch=compute_103a,code=sm_103a) and the host runtime with g++,
-then linked with nvcc.  Host code is compiled with -ffp-contract=off so that
+The CUDA translation units (nvcc, -gencode arch=compute_103a,code=sm_103a)
+and the host runtime (g++) compile in parallel and are linked with nvcc;
+then the namelist-driven executable falcon_run (driver/falcon_run.cpp,
+C ABI only) is linked against the library.  Host code is compiled with -ffp-contract=off so that
 operator construction gives identical results on x86_64 and aarch64.
 """
 import os
@@ -31,15 +32,19 @@ def _run(cmd):
     return r.stdout + r.stderr
 
 
+DRIVER_SRC = os.path.join(HERE, "driver", "falcon_run.cpp")
+DRIVER = os.path.join(OUT, "falcon_run")
+
+
 def sources():
     return [os.path.join(SRC, f) for f in sorted(os.listdir(SRC))] + [
-        os.path.join(HERE, "..", "include", "falcon_gpu.h")]
+        os.path.join(HERE, "..", "include", "falcon_gpu.h"), DRIVER_SRC]
 
 
 def up_to_date():
-    if not os.path.exists(LIB):
+    if not os.path.exists(LIB) or not os.path.exists(DRIVER):
         return False
-    t = os.path.getmtime(LIB)
+    t = min(os.path.getmtime(LIB), os.path.getmtime(DRIVER))
     return all(os.path.getmtime(s) <= t for s in sources())
 
 
@@ -62,6 +67,10 @@ def build(force=False, verbose=False):
     tmp = LIB + ".tmp"
     _run([nvcc] + ARCH + ["-shared", "-o", tmp] + objs + [host_o, "-lcudart", "-lpthread"])
     os.replace(tmp, LIB)
+    # the namelist-driven executable (C ABI only), next to the library
+    _run(["g++", "-O2", "-std=c++17", DRIVER_SRC, "-o", DRIVER + ".tmp", "-L" + OUT, "-lfalcon_gpu",
+          "-Wl,-rpath,$ORIGIN"])
+    os.replace(DRIVER + ".tmp", DRIVER)
     return LIB
 
 

@@ -3285,6 +3285,15 @@ int falcon_batch_upbalance(falcon_batch* b, int i, double* out) {
   return check_device_waits();
 }
 
+int falcon_time(falcon_handle* h, double* tot_time, double* dt, int* n_step) {
+  if (!h || !h->b || h->b->groups.empty()) return fail(FALCON_EINVAL, "null handle");
+  const Group* g = h->b->groups[0].get();
+  if (tot_time) *tot_time = g->tot_time;
+  if (dt) *dt = g->cur_dt();
+  if (n_step) *n_step = g->n_step;
+  return 0;
+}
+
 int falcon_spectra(falcon_handle* h, double* kespec, double* tspec) {
   if (!h) return fail(FALCON_EINVAL, "null handle");
   return falcon_batch_spectra(h->b, 0, kespec, tspec);
@@ -3469,10 +3478,12 @@ struct ServerRequest {
   uint64_t seed = 0;
   int horizon = 0;
   int steps = 0;
-  int state = 0;  // 0 queued, 1 active, 2 done
+  int state = 0;  // 0 queued, 1 active, 2 done (horizon reached or retired)
+  int status = 0; // FALCON_OK, or FALCON_EBLOWUP / FALCON_ENONFINITE when retired early
   size_t foot = 0;
   falcon_diag diag{};
-  std::vector<double> tfr;
+  std::vector<double> tfr, omg, upf, urf;  // final fields (Fortran layout)
+  std::vector<double> init_t, init_w, init_up, init_ur;  // caller's initial state (empty: seeded noise)
   OpKey key{};
 };
 
@@ -3528,6 +3539,18 @@ size_t opset_bytes(const falcon_params& p) {
   return 8 * (2 * R * R + M * R * R + M * 3 * R * R + 2 * R * R + 2 * R);
 }
 
+// Request r's initial state into slot j of its group: the caller's fields,
+// or the conductive profile plus seeded noise of amplitude 1e-3.
+int server_set_initial(Group* g, int j, const ServerRequest& r) {
+  if (!r.init_t.empty())
+    return group_set_instance(g, j, r.init_t.data(), r.init_w.empty() ? nullptr : r.init_w.data(),
+                              r.init_up.empty() ? nullptr : r.init_up.data(),
+                              r.init_ur.empty() ? nullptr : r.init_ur.data());
+  std::vector<double> t;
+  initial_temperature(r.p, 1, 1e-3, r.seed, t);
+  return group_set_instance(g, j, t.data(), nullptr, nullptr, nullptr);
+}
+
 int server_admit_group(falcon_server* s, const OpKey& key, ServerGroup& sg) {
   // repack: keep current ids (minus retired), append pending
   std::vector<int64_t> new_ids;
@@ -3548,12 +3571,8 @@ int server_admit_group(falcon_server* s, const OpKey& key, ServerGroup& sg) {
     sg.g->stream = s->streams[s->next_stream++ % s->streams.size()];
     if ((rc = group_init(sg.g.get(), ps, mem))) return rc;
     sg.ids = new_ids;
-    for (size_t j = 0; j < new_ids.size(); ++j) {
-      ServerRequest& r = s->reqs[new_ids[j]];
-      std::vector<double> t;
-      initial_temperature(r.p, 1, 1e-3, r.seed, t);
-      if ((rc = group_set_instance(sg.g.get(), (int)j, t.data(), nullptr, nullptr, nullptr))) return rc;
-    }
+    for (size_t j = 0; j < new_ids.size(); ++j)
+      if ((rc = server_set_initial(sg.g.get(), (int)j, s->reqs[new_ids[j]]))) return rc;
     return group_reset(sg.g.get());
   }
   if ((rc = group_resize(sg.g.get(), map))) return rc;
@@ -3564,10 +3583,7 @@ int server_admit_group(falcon_server* s, const OpKey& key, ServerGroup& sg) {
   CK(cudaMemcpy(sg.g->ra_pr, ra.data(), sizeof(double) * ra.size(), cudaMemcpyHostToDevice));
   for (size_t j = 0; j < new_ids.size(); ++j) {
     if (map[j] >= 0) continue;
-    ServerRequest& r = s->reqs[new_ids[j]];
-    std::vector<double> t;
-    initial_temperature(r.p, 1, 1e-3, r.seed, t);
-    if ((rc = group_set_instance(sg.g.get(), (int)j, t.data(), nullptr, nullptr, nullptr))) return rc;
+    if ((rc = server_set_initial(sg.g.get(), (int)j, s->reqs[new_ids[j]]))) return rc;
     if ((rc = group_reset_instance(sg.g.get(), (int)j))) return rc;
   }
   (void)key;
@@ -3625,6 +3641,22 @@ void falcon_server_destroy(falcon_server* s) {
   delete s;
 }
 
+int falcon_server_submit_state(falcon_server* s, const falcon_params* p, const double* tFR, const double* omgFR,
+                               const double* upFR, const double* urFR, int horizon, int64_t* id) {
+  if (!tFR) return fail(FALCON_EINVAL, "falcon_server_submit_state: tFR is required");
+  int64_t rid = 0;
+  int rc = falcon_server_submit(s, p, 0, horizon, &rid);
+  if (rc) return rc;
+  ServerRequest& r = s->reqs[rid];
+  const size_t n = (size_t)2 * (p->nm_max + 1) * p->nr_max;
+  r.init_t.assign(tFR, tFR + n);
+  if (omgFR) r.init_w.assign(omgFR, omgFR + n);
+  if (upFR) r.init_up.assign(upFR, upFR + n);
+  if (urFR) r.init_ur.assign(urFR, urFR + n);
+  if (id) *id = rid;
+  return 0;
+}
+
 int falcon_server_submit(falcon_server* s, const falcon_params* p, uint64_t seed, int horizon, int64_t* id) {
   if (!s || !p || horizon <= 0) return fail(FALCON_EINVAL, "invalid request");
   int rc = validate(*p);
@@ -3670,38 +3702,51 @@ int falcon_server_iterate(falcon_server* s, int* n_active, int* n_queued) {
     int rc = server_admit_group(s, kv.first, kv.second);
     if (rc) return rc;
   }
-  // 3. one step of every active group
+  // 3. one step of every active group, queued on the group streams without
+  // waiting: the host goes on while the device works, and synchronises
+  // (in 4.) only the groups it reads this iteration
   for (auto& kv : s->groups) {
     if (!kv.second.g) continue;
     int rc = group_step(kv.second.g.get());
     if (rc) return rc;
   }
-  if (int rc = s->sync()) return rc;
-  // 4. retire finished requests
+  // 4. retire finished requests: at the horizon, or early at a check of
+  // the request's n_KE cadence (the reference's writeKE_spectral cadence)
+  // that finds a non-finite state or KE > 1e10 (src/output.F90:321-323);
+  // the rest of the group keeps running
   for (auto& kv : s->groups) {
     ServerGroup& sg = kv.second;
     if (!sg.g) continue;
-    bool changed = false;
-    sg.g->diag_host.clear();
+    bool changed = false, have_diag = false;
     for (size_t j = 0; j < sg.ids.size(); ++j) {
       ServerRequest& r = s->reqs[sg.ids[j]];
       if (r.state != 1) continue;
       r.steps++;
-      if (r.steps >= r.horizon) {
-        const size_t n = (size_t)2 * (r.p.nm_max + 1) * r.p.nr_max;
-        std::vector<double> t(n), w(n), up(n), ur(n);
-        int rc = group_get_instance(sg.g.get(), (int)j, t.data(), nullptr, nullptr, nullptr, nullptr);
-        if (rc) return rc;
-        if (sg.g->diag_host.size() != (size_t)8 * sg.g->B) {
-          if ((rc = group_diagnostics(sg.g.get()))) return rc;
-        }
-        fill_diag(sg.g.get(), (int)j, r.steps * r.p.dt, &r.diag);
-        r.tfr = std::move(t);
-        r.state = 2;
-        s->active--;
-        s->used -= r.foot;
-        changed = true;
+      const int every = r.p.n_KE > 0 ? r.p.n_KE : 1;
+      const bool at_horizon = r.steps >= r.horizon;
+      if (!at_horizon && r.steps % every != 0) continue;
+      int rc;
+      if (!have_diag) {  // synchronises this group's stream only
+        if ((rc = group_diagnostics(sg.g.get()))) return rc;
+        have_diag = true;
       }
+      falcon_diag d;
+      fill_diag(sg.g.get(), (int)j, r.steps * r.p.dt, &d);
+      int status = FALCON_OK;
+      if (!std::isfinite(d.ke) || !std::isfinite(d.nu_top) || !std::isfinite(d.nu_bot)) status = FALCON_ENONFINITE;
+      else if (d.ke > 1e10) status = FALCON_EBLOWUP;
+      if (!at_horizon && status == FALCON_OK) continue;
+      const size_t n = (size_t)2 * (r.p.nm_max + 1) * r.p.nr_max;
+      r.tfr.resize(n); r.omg.resize(n); r.upf.resize(n); r.urf.resize(n);
+      if ((rc = group_get_instance(sg.g.get(), (int)j, r.tfr.data(), r.omg.data(), r.upf.data(), r.urf.data(),
+                                   nullptr)))
+        return rc;
+      r.diag = d;
+      r.status = status;
+      r.state = 2;
+      s->active--;
+      s->used -= r.foot;
+      changed = true;
     }
     if (changed) {
       int rc = server_admit_group(s, kv.first, sg);
@@ -3723,6 +3768,32 @@ int falcon_server_poll(falcon_server* s, int64_t id, int* done, falcon_diag* out
     if (out) *out = it->second.diag;
     if (tFR) std::memcpy(tFR, it->second.tfr.data(), sizeof(double) * it->second.tfr.size());
   }
+  return 0;
+}
+
+int falcon_server_result(falcon_server* s, int64_t id, int* done, int* status, falcon_diag* out, double* tFR,
+                         double* omgFR, double* upFR, double* urFR) {
+  if (!s || !done) return fail(FALCON_EINVAL, "null argument");
+  auto it = s->reqs.find(id);
+  if (it == s->reqs.end()) return fail(FALCON_EINVAL, "unknown request id");
+  const ServerRequest& r = it->second;
+  *done = r.state == 2;
+  if (status) *status = r.status;
+  if (!*done) return 0;
+  if (out) *out = r.diag;
+  const size_t bytes = sizeof(double) * r.tfr.size();
+  if (tFR) std::memcpy(tFR, r.tfr.data(), bytes);
+  if (omgFR) std::memcpy(omgFR, r.omg.data(), bytes);
+  if (upFR) std::memcpy(upFR, r.upf.data(), bytes);
+  if (urFR) std::memcpy(urFR, r.urf.data(), bytes);
+  return 0;
+}
+
+int falcon_server_steps(falcon_server* s, int64_t id, int* steps) {
+  if (!s || !steps) return fail(FALCON_EINVAL, "null argument");
+  auto it = s->reqs.find(id);
+  if (it == s->reqs.end()) return fail(FALCON_EINVAL, "unknown request id");
+  *steps = it->second.steps;
   return 0;
 }
 

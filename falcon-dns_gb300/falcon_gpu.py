@@ -104,7 +104,8 @@ EXPORTS = (
     "falcon_store_snapshot", "falcon_batch_store_checkpoint", "falcon_batch_load_checkpoint",
     "falcon_batch_store_snapshot", "falcon_restart", "falcon_batch_restart", "falcon_set_gemm_mode",
     "falcon_upload_factors", "falcon_cheb_d1d2_dev", "falcon_spectra", "falcon_upbalance",
-    "falcon_batch_spectra", "falcon_batch_upbalance",
+    "falcon_batch_spectra", "falcon_batch_upbalance", "falcon_time", "falcon_server_submit_state",
+    "falcon_server_result", "falcon_server_steps",
 )
 
 
@@ -159,6 +160,10 @@ def lib():
     L.falcon_server_submit.argtypes = [vp, pp, ctypes.c_uint64, ip, P(ctypes.c_int64)]
     L.falcon_server_iterate.argtypes = [vp, P(ctypes.c_int), P(ctypes.c_int)]
     L.falcon_server_poll.argtypes = [vp, ctypes.c_int64, P(ctypes.c_int), P(FalconDiag), dp]
+    L.falcon_server_submit_state.argtypes = [vp, pp, dp, dp, dp, dp, ip, P(ctypes.c_int64)]
+    L.falcon_server_result.argtypes = [vp, ctypes.c_int64, P(ctypes.c_int), P(ctypes.c_int), P(FalconDiag), dp, dp,
+                                       dp, dp]
+    L.falcon_server_steps.argtypes = [vp, ctypes.c_int64, P(ctypes.c_int)]
     L.falcon_fp64_peak_gflops.restype = ctypes.c_double
     L.falcon_fp64_mma_peak_gflops.restype = ctypes.c_double
     L.falcon_batch_profile.argtypes = [vp, ip, P(KernelStat), ip, P(ctypes.c_int)]
@@ -416,6 +421,32 @@ class Server:
         check(lib().falcon_server_submit(self.h, ctypes.byref(params), int(seed), int(horizon), ctypes.byref(i)))
         self.shape[i.value] = (params.nr_max, params.nm_max + 1)
         return i.value
+
+    def submit_state(self, params, t, om=None, up=None, ur=None, horizon=1):
+        """A request from a given initial state (Fortran-layout (Nr, Nm+1) complex arrays)."""
+        arrs = [None if a is None else np.ascontiguousarray(a, np.complex128) for a in (t, om, up, ur)]
+        i = ctypes.c_int64()
+        check(lib().falcon_server_submit_state(self.h, ctypes.byref(params), *[_dp(a) for a in arrs], int(horizon),
+                                               ctypes.byref(i)))
+        self.shape[i.value] = (params.nr_max, params.nm_max + 1)
+        return i.value
+
+    def result(self, rid):
+        """(done, status, diagnostics, fields dict) of a request; status 0 at
+        its horizon, FALCON_EBLOWUP (-6) / FALCON_ENONFINITE (-5) when
+        retired early."""
+        done, status, diag = ctypes.c_int(), ctypes.c_int(), FalconDiag()
+        f = [np.empty(self.shape[rid], np.complex128) for _ in range(4)]
+        check(lib().falcon_server_result(self.h, rid, ctypes.byref(done), ctypes.byref(status), ctypes.byref(diag),
+                                         *[_dp(a) for a in f]))
+        if not done.value:
+            return False, status.value, None, None
+        return True, status.value, diag.as_dict(), dict(zip(("T", "omg", "up", "ur"), f))
+
+    def steps(self, rid):
+        n = ctypes.c_int()
+        check(lib().falcon_server_steps(self.h, rid, ctypes.byref(n)))
+        return n.value
 
     def iterate(self):
         na, nq = ctypes.c_int(), ctypes.c_int()

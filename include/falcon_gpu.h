@@ -161,6 +161,11 @@ int falcon_upload_factors(falcon_handle* h, const double* AT, const int* ipiv_T,
  * src/steptime_imexrk.F90:96-190). */
 int falcon_step(falcon_handle* h, int nsteps);
 int falcon_diagnostics(falcon_handle* h, falcon_diag* out);
+/* The run's clock after the last step: tot_time (accumulated as the
+ * reference does, tot_time = tot_time + dt_new), the dt_new of that step and
+ * the step count n_step.  Host bookkeeping, no device work; any pointer may
+ * be NULL. */
+int falcon_time(falcon_handle* h, double* tot_time, double* dt, int* n_step);
 /* calculate_spectra (src/output.F90:327-355) of the current state:
  * kespec[m] = 4 pi radInt(|ur_m ur_m + up_m up_m|) and tspec[m] =
  * 4 pi radInt(|T_m|) for m = 0..Nm_max (the KEspec_<tag> and
@@ -314,12 +319,28 @@ void falcon_server_destroy(falcon_server* s);
 /* Queues a request; *id receives its identifier. */
 int falcon_server_submit(falcon_server* s, const falcon_params* p, uint64_t seed, int horizon,
                          int64_t* id);
-/* One serving iteration: admit what fits, step the active set once,
- * retire finished requests.  *n_active / *n_queued report the sizes. */
+/* One serving iteration: admit what fits, queue one step of every active
+ * group on its stream, retire finished requests (synchronising only the
+ * groups read this iteration).  *n_active / *n_queued report the sizes. */
 int falcon_server_iterate(falcon_server* s, int* n_active, int* n_queued);
+/* Queues a request whose initial state is given (Fortran-layout host
+ * arrays, copied; omgFR, upFR, urFR may be NULL for zeros) instead of the
+ * seeded conductive-plus-noise state. */
+int falcon_server_submit_state(falcon_server* s, const falcon_params* p, const double* tFR, const double* omgFR,
+                               const double* upFR, const double* urFR, int horizon, int64_t* id);
 /* 1 when request `id` has finished; its final diagnostics in *out and, if
  * tFR is not NULL, its final temperature field (Fortran layout). */
 int falcon_server_poll(falcon_server* s, int64_t id, int* done, falcon_diag* out, double* tFR);
+/* A finished request's status and fields: *status is FALCON_OK when it
+ * reached its horizon, FALCON_EBLOWUP (kinetic energy above 1e10, the
+ * reference's stop at src/output.F90:321-323) or FALCON_ENONFINITE when a
+ * check at its n_KE cadence retired it early (the other requests of its
+ * group keep running); the fields are its state at that step (any pointer
+ * may be NULL).  *done = 0 while it runs. */
+int falcon_server_result(falcon_server* s, int64_t id, int* done, int* status, falcon_diag* out, double* tFR,
+                         double* omgFR, double* upFR, double* urFR);
+/* Steps request `id` has taken so far. */
+int falcon_server_steps(falcon_server* s, int64_t id, int* steps);
 
 /* ---- measurement hooks ---- */
 /* Per-kernel-class statistics of `nsteps` steps of a batch, timed with CUDA
