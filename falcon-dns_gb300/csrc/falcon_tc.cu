@@ -20,14 +20,17 @@
 //  - X: four producer warps read the FP64 columns, take each column's
 //    exponent over all of K and cut the values into slices directly in
 //    shared memory (no slice planes in HBM).
-// Warp roles (320 threads, one CTA per SM, persistent over a contiguous
+// Warp roles (448 threads, one CTA per SM, persistent over a contiguous
 // range of (entry, row tile, column tile) work items):
-//   0-3  epilogue: tcgen05.ld of the diagonals (warp q reads tensor-memory
-//        lanes 32q..32q+31, i.e. operator rows), exact recombination, FP64
-//        stores;
-//   4-7  X producers;
-//   8    tensor-memory allocation and the operator's TMA copies (lane 0);
-//   9    MMA issue (lane 0).
+//   0-7   epilogue: tcgen05.ld of the diagonals (warp w reads tensor-memory
+//         lanes 32 (w%4).. (operator rows), half w/4 of the columns), exact
+//         recombination, FP64 stores;
+//   8-11  X producers;
+//   12    tensor-memory allocation and the operator's TMA copies (lane 0);
+//   13    MMA issue (lane 0): per K chunk and operator slice s one MMA of
+//         A_s against the X slices 0..D-s side by side along N (up to 13 or
+//         15 MMAs of N <= 256 per chunk instead of 45 or 55 of N = 48, so the
+//         operator slice is read from shared memory once per chunk).
 // Every wait on an mbarrier is bounded: after ~1 s a wait sets an error
 // word in global memory and the CTA's abort flag, and every role leaves
 // its loop; the MMA warp waits (bounded) for its own products and the TMA
@@ -56,8 +59,11 @@ struct TcCfg {
   static constexpr int NX = 3;                 // X stages
   static constexpr int A_SLICE = BM * BK * 2;  // 4096 bytes: 2 k groups x 128 rows x 16 B
   static constexpr int A_STAGE = S * A_SLICE;
-  static constexpr int X_SLICE = BN * BK * 2;  // 1536 bytes: 2 k groups x 6 column groups x 128 B
-  static constexpr int X_STAGE = S * X_SLICE;
+  // X stage: [k group (2)][column group (S x 6)][8 columns][16 B]: slice t's
+  // column n is stage column 48 t + n, so the slices lie side by side along N
+  static constexpr int XGROUPS = S * (BN / 8);
+  static constexpr uint32_t XLBO = tc_x_lbo(S);  // between the two k groups (XGROUPS x 128 B)
+  static constexpr int X_STAGE = 2 * XGROUPS * 128;
   static constexpr int OFF_A = 0;
   static constexpr int OFF_X = NA * A_STAGE;
   static constexpr int OFF_CEX = OFF_X + NX * X_STAGE;  // int [4][BN] column exponents
@@ -152,8 +158,27 @@ __device__ __forceinline__ TileIdx tile_of(long t, int n_mt, int n_nt) {
   return r;
 }
 
+// The MMA products of one K chunk for operator slice s: A_s times the X
+// slices t = 0..D-s laid side by side along N (stage column t*48 + n),
+// accumulated into the diagonals s..D, whose accumulators are contiguous in
+// tensor memory (diagonal d at column 48 d): one MMA of N = 48 (D + 1 - s)
+// columns, split into parts of at most 256 (the largest N of an M = 128
+// MMA); every part's N is a multiple of 16.
 template <int W>
-__global__ void __launch_bounds__(320, 1) tc_gemm_kernel(const __grid_constant__ CUtensorMap amap, const TcArgs q) {
+__device__ __forceinline__ void tc_slice_products(int s, uint32_t tmem, uint32_t a_addr, uint32_t x_addr,
+                                                  uint32_t acc) {
+  using C = TcCfg<W>;
+  const uint64_t adesc = tc_smem_desc(a_addr, kTcALbo, kTcSbo);
+  const int ntot = (C::D + 1 - s) * C::BN;
+  for (int c = 0; c < ntot; c += 256) {
+    const int n = ntot - c < 256 ? ntot - c : 256;
+    const uint64_t bdesc = tc_smem_desc(x_addr + (uint32_t)(c / 8) * 128u, C::XLBO, kTcSbo);
+    tc_mma(tmem + (uint32_t)(s * C::BN + c), adesc, bdesc, tc_idesc_bf16(C::BM, n), acc);
+  }
+}
+
+template <int W>
+__global__ void __launch_bounds__(448, 1) tc_gemm_kernel(const __grid_constant__ CUtensorMap amap, const TcArgs q) {
   using C = TcCfg<W>;
   extern __shared__ uint8_t tc_smem_raw[];
   uint8_t* sm = tc_smem_raw + ((1024 - (su32(tc_smem_raw) & 1023)) & 1023);
@@ -175,15 +200,15 @@ __global__ void __launch_bounds__(320, 1) tc_gemm_kernel(const __grid_constant__
 
   if (tid == 0) {
     for (int i = 0; i < C::NA; ++i) { mbar_init(&full_a[i], 1); mbar_init(&empty_a[i], 1); }
-    for (int i = 0; i < C::NX; ++i) { mbar_init(&full_x[i], 128); mbar_init(&empty_x[i], 1); }
+    for (int i = 0; i < C::NX; ++i) { mbar_init(&full_x[i], kTcProducers); mbar_init(&empty_x[i], 1); }
     mbar_init(acc_full, 1);
-    mbar_init(acc_empty, 128);
-    for (int i = 0; i < 4; ++i) { mbar_init(&cex_full[i], 128); mbar_init(&cex_empty[i], 128); }
+    mbar_init(acc_empty, kTcEpilogue);
+    for (int i = 0; i < 4; ++i) { mbar_init(&cex_full[i], kTcProducers); mbar_init(&cex_empty[i], kTcEpilogue); }
     mbar_init(drain, 1);
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (warp == 8) {
+  if (warp == kTcWarpTma) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(su32(tmem_slot)),
                  "r"(C::TMEM_COLS)
                  : "memory");
@@ -201,10 +226,12 @@ __global__ void __launch_bounds__(320, 1) tc_gemm_kernel(const __grid_constant__
   const bool resident = nk <= C::NA;
   const uint32_t sm_base = su32(sm);
 
-  if (warp < 4) {
+  if (warp < kTcEpilogue / 32) {
     // ---------------- epilogue ----------------
-    // waits are taken by lane 0 and broadcast, so a warp leaves together
-    // (tcgen05.ld is warp-collective)
+    // warp (q, h): tensor-memory lanes 32q..32q+31 (operator rows), columns
+    // h*24..h*24+23 of the tile; waits are taken by lane 0 and broadcast, so
+    // a warp leaves together (tcgen05.ld is warp-collective)
+    const int qd = warp & 3, half = warp >> 2;
     long u = 0;
     for (long t = t_begin; t < t_end; ++t, ++u) {
       const TileIdx ti = tile_of(t, n_mt, n_nt);
@@ -217,7 +244,7 @@ __global__ void __launch_bounds__(320, 1) tc_gemm_kernel(const __grid_constant__
       if (!ok) break;
       tc_fence_after();
       const int* cex = cex_ring + (u & 3) * C::BN;
-      const int r = ti.mt * C::BM + warp * 32 + lane;
+      const int r = ti.mt * C::BM + qd * 32 + lane;
       const bool valid = r < q.rows;
       int er = 0;
       double* yrow = nullptr;
@@ -229,9 +256,9 @@ __global__ void __launch_bounds__(320, 1) tc_gemm_kernel(const __grid_constant__
         yrow = q.Y[o] + (size_t)ti.z * q.sY + (size_t)(r - r0) * q.ldy;
       }
       const int n0 = ti.nt * C::BN;
-      const uint32_t lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
+      const uint32_t lane_addr = tmem + ((uint32_t)(qd * 32) << 16);
 #pragma unroll 1
-      for (int c0 = 0; c0 < C::BN; c0 += 8) {
+      for (int c0 = half * (C::BN / 2); c0 < (half + 1) * (C::BN / 2); c0 += 8) {
         uint32_t v[C::D + 1][8];
 #pragma unroll
         for (int d = 0; d <= C::D; ++d) tmem_ld8(lane_addr + (uint32_t)(d * C::BN + c0), v[d]);
@@ -272,63 +299,71 @@ __global__ void __launch_bounds__(320, 1) tc_gemm_kernel(const __grid_constant__
       mbar_arrive(acc_empty);
       mbar_arrive(&cex_empty[u & 3]);
     }
-  } else if (warp < 8) {
+  } else if (warp < (kTcEpilogue + kTcProducers) / 32) {
     // ---------------- X producers ----------------
-    // waits are taken by thread 0 and passed on through prod_ok (two slots
-    // by wait parity) at a named barrier, so the 128 threads always leave
-    // together and the named barriers stay matched
-    const int tp = tid - 128;
+    // Thread (column n, k group kg) owns the values k = 16 c + 8 kg + i of
+    // its column: it reads them once per tile (the first RC chunks stay in
+    // registers), takes the column exponent with its partner, then cuts
+    // them into slices chunk by chunk.  Waits are taken by thread 0 and
+    // passed on through prod_ok (two slots by wait parity) at a named
+    // barrier, so the producers always leave together and the named
+    // barriers stay matched.
+    constexpr int RC = 5;
+    const int tp = tid - kTcEpilogue;
     volatile int* prod_ok = reinterpret_cast<volatile int*>(sm + C::OFF_MISC + 8);
+    const int n = tp % C::BN, kg = tp / C::BN;
+    const bool act = tp < 2 * C::BN;
     long xc = 0, u = 0, nw = 0;
     bool stop = false;
     for (long t = t_begin; t < t_end && !stop; ++t, ++u) {
       const TileIdx ti = tile_of(t, n_mt, n_nt);
-      const int n0 = ti.nt * C::BN;
+      const int n0 = ti.nt * C::BN, nn = n0 + n;
       const double* Xz = q.X + (size_t)ti.z * q.sX;
+      const bool col = act && nn < q.N;
+      double v[RC][8];
+      int mx = 0;
+#pragma unroll
+      for (int c = 0; c < RC; ++c)
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+          const int k = c * C::BK + kg * 8 + i;
+          v[c][i] = (col && c < nk && k < q.K) ? Xz[(size_t)k * q.ldx + nn] : 0.0;
+        }
+      for (int c = RC; c < nk; ++c)
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+          const int k = c * C::BK + kg * 8 + i;
+          if (col && k < q.K) mx = max(mx, biased_exp(Xz[(size_t)k * q.ldx + nn]));
+        }
+#pragma unroll
+      for (int c = 0; c < RC; ++c)
+#pragma unroll
+        for (int i = 0; i < 8; ++i) mx = max(mx, biased_exp(v[c][i]));
       if (tp == 0)
         prod_ok[nw & 1] = mbar_wait(&cex_empty[u & 3], (uint32_t)(((u >> 2) & 1) ^ 1), abort_flag, q.err, 3) ? 1 : 0;
-      named_sync(1, 128);
+      if (act) pm[kg * C::BN + n] = mx;
+      named_sync(1, kTcProducers);
       if (!prod_ok[(nw++) & 1]) break;
-      // column exponents: the largest biased exponent over all K of each column
-      if (tp < 2 * C::BN) {
-        const int c = tp % C::BN, h = tp / C::BN, n = n0 + c;
-        int mx = 0;
-        if (n < q.N)
-          for (int k = h; k < q.K; k += 2) mx = max(mx, biased_exp(Xz[(size_t)k * q.ldx + n]));
-        pm[h * C::BN + c] = mx;
-      }
-      named_sync(1, 128);
       int* cex = cex_ring + (u & 3) * C::BN;
-      if (tp < C::BN) cex[tp] = max(pm[tp], pm[C::BN + tp]);
-      named_sync(1, 128);
+      const int fb = act ? max(pm[n], pm[C::BN + n]) : 0;
+      if (tp < C::BN) cex[tp] = fb;
       mbar_arrive(&cex_full[u & 3]);
-      // unit (column n, k group kg) of each chunk: 8 values -> S slices of 16 bytes
-      const int n = tp % C::BN, kg = tp / C::BN;
-      const int nn = n0 + n, fb = (tp < 2 * C::BN) ? cex[n] : 0;
-      for (int c = 0; c < nk; ++c) {
+      auto produce = [&](int c, const double (&vals)[8]) -> bool {
         const long j = xc++;
         const int st = (int)(j % C::NX);
         if (tp == 0)
           prod_ok[nw & 1] = mbar_wait(&empty_x[st], (uint32_t)(((j / C::NX) & 1) ^ 1), abort_flag, q.err, 4) ? 1 : 0;
-        named_sync(1, 128);
-        if (!prod_ok[(nw++) & 1]) {
-          stop = true;
-          break;
-        }
-        if (tp < 2 * C::BN) {
+        named_sync(1, kTcProducers);
+        if (!prod_ok[(nw++) & 1]) return false;
+        if (act) {
           unsigned long long Tm[8];
           uint32_t sg = 0;
 #pragma unroll
           for (int i = 0; i < 8; ++i) {
-            const int k = c * C::BK + kg * 8 + i;
-            Tm[i] = 0ull;
-            if (k < q.K && nn < q.N && fb > 0) {
-              const double v = Xz[(size_t)k * q.ldx + nn];
-              Tm[i] = oz_magb<C::MAGB>(v, fb - 1022);
-              if (__double_as_longlong(v) < 0) sg |= 1u << i;
-            }
+            Tm[i] = fb > 0 ? oz_magb<C::MAGB>(vals[i], fb - 1022) : 0ull;
+            if (__double_as_longlong(vals[i]) < 0) sg |= 1u << i;
           }
-          uint8_t* xs = sm + C::OFF_X + st * C::X_STAGE + (kg * (C::BN / 8) + n / 8) * 128 + (n % 8) * 16;
+          uint8_t* xs = sm + C::OFF_X + st * C::X_STAGE + (kg * C::XGROUPS + n / 8) * 128 + (n % 8) * 16;
 #pragma unroll
           for (int s = 0; s < C::S; ++s) {
             uint32_t w4[4];
@@ -336,14 +371,27 @@ __global__ void __launch_bounds__(320, 1) tc_gemm_kernel(const __grid_constant__
             for (int p = 0; p < 4; ++p)
               w4[p] = oz_slice_w<W>(Tm[2 * p], (sg >> (2 * p)) & 1, s) |
                       (oz_slice_w<W>(Tm[2 * p + 1], (sg >> (2 * p + 1)) & 1, s) << 16);
-            *reinterpret_cast<uint4*>(xs + s * C::X_SLICE) = make_uint4(w4[0], w4[1], w4[2], w4[3]);
+            *reinterpret_cast<uint4*>(xs + s * (C::BN / 8) * 128) = make_uint4(w4[0], w4[1], w4[2], w4[3]);
           }
         }
         fence_async_smem();
         mbar_arrive(&full_x[st]);
+        return true;
+      };
+#pragma unroll
+      for (int c = 0; c < RC; ++c)
+        if (c < nk && !stop && !produce(c, v[c])) stop = true;
+      for (int c = RC; c < nk && !stop; ++c) {
+        double w8[8];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+          const int k = c * C::BK + kg * 8 + i;
+          w8[i] = (col && k < q.K) ? Xz[(size_t)k * q.ldx + nn] : 0.0;
+        }
+        if (!produce(c, w8)) stop = true;
       }
     }
-  } else if (warp == 8) {
+  } else if (warp == kTcWarpTma) {
     // ---------------- operator TMA copies ----------------
     if (lane == 0) {
       long ac = 0;
@@ -367,7 +415,7 @@ __global__ void __launch_bounds__(320, 1) tc_gemm_kernel(const __grid_constant__
       // wait for the copies this thread issued (bounded), so none is in
       // flight when the CTA ends
       for (long j = (issued > C::NA ? issued - C::NA : 0); j < issued; ++j) {
-        const long t0 = clock64();
+        const long long t0 = clock64();
         while (!mbar_try(&full_a[j % C::NA], (uint32_t)((j / C::NA) & 1)) && clock64() - t0 < kSpinCycles) {
         }
       }
@@ -375,9 +423,6 @@ __global__ void __launch_bounds__(320, 1) tc_gemm_kernel(const __grid_constant__
   } else {
     // ---------------- MMA issue ----------------
     if (lane == 0) {
-      // instruction descriptor: FP32 accumulate, bf16 A and B, both K-major,
-      // N = 48, M = 128
-      const uint32_t idesc = tc_idesc_bf16(C::BM, C::BN);
       long ac = 0, xc = 0, u = 0, abase = 0;
       long last = -1;
       bool any = false;
@@ -413,17 +458,13 @@ __global__ void __launch_bounds__(320, 1) tc_gemm_kernel(const __grid_constant__
             break;
           }
           tc_fence_after();
-          const uint32_t abase_addr = sm_base + C::OFF_A + sa * C::A_STAGE;
-          const uint32_t xbase_addr = sm_base + C::OFF_X + sx * C::X_STAGE;
+          const uint32_t a_stage = sm_base + C::OFF_A + sa * C::A_STAGE;
+          const uint32_t x_stage = sm_base + C::OFF_X + sx * C::X_STAGE;
+          // s = 0 writes every diagonal fresh in the first chunk of a tile;
+          // the rest accumulate
 #pragma unroll 1
-          for (int s = 0; s < C::S; ++s) {
-            const uint64_t adesc = tc_smem_desc(abase_addr + s * C::A_SLICE, kTcALbo, kTcSbo);
-#pragma unroll 1
-            for (int tt = 0; s + tt <= C::D; ++tt) {
-              const uint64_t bdesc = tc_smem_desc(xbase_addr + tt * C::X_SLICE, kTcXLbo, kTcSbo);
-              tc_mma(tmem + (uint32_t)((s + tt) * C::BN), adesc, bdesc, idesc, (c > 0 || s > 0) ? 1u : 0u);
-            }
-          }
+          for (int s = 0; s < C::S; ++s)
+            tc_slice_products<W>(s, tmem, a_stage + s * C::A_SLICE, x_stage, (c > 0 || s > 0) ? 1u : 0u);
           any = true;
           tc_commit(&empty_x[sx]);
           if (!resident || last_of_item) tc_commit(&empty_a[sa]);
@@ -435,7 +476,7 @@ __global__ void __launch_bounds__(320, 1) tc_gemm_kernel(const __grid_constant__
       // tensor memory is freed
       if (any) {
         tc_commit(drain);
-        const long t0 = clock64();
+        const long long t0 = clock64();
         while (!mbar_try(drain, 0) && clock64() - t0 < kSpinCycles) {
         }
       }
@@ -443,7 +484,7 @@ __global__ void __launch_bounds__(320, 1) tc_gemm_kernel(const __grid_constant__
   }
   tc_fence_before();
   __syncthreads();
-  if (warp == 8) {
+  if (warp == kTcWarpTma) {
     tc_fence_after();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(C::TMEM_COLS) : "memory");
   }
@@ -481,7 +522,7 @@ cudaError_t launch_tc_w(const TcArgs& a, const CUtensorMap& map, cudaStream_t s)
   if (!q.err) return cudaErrorInvalidSymbol;
   const long T = (long)q.batch * ((q.rows + C::BM - 1) / C::BM) * ((q.N + C::BN - 1) / C::BN);
   const int grid = (int)(T < nsm ? T : nsm);
-  tc_gemm_kernel<W><<<grid, 320, C::SMEM, s>>>(map, q);
+  tc_gemm_kernel<W><<<grid, kTcThreads, C::SMEM, s>>>(map, q);
   return cudaGetLastError();
 }
 
@@ -516,28 +557,36 @@ int tc_make_operator_map(CUtensorMap* map, const uint16_t* slices, int nb, int S
 }
 
 int tc_stage_layout_check(int w, int KP) {
-  // every descriptor of the kernel stays inside its shared-memory stage:
-  // decode start, leading and stride offsets back from the encodings and
-  // bound the last byte of the last core matrix an MMA reads
+  // every descriptor of the kernel stays inside its shared-memory stage and
+  // every accumulator inside the allocated tensor memory: decode start,
+  // leading and stride offsets back from the encodings and bound the last
+  // byte of the last core matrix an MMA reads
   auto last_byte = [](uint64_t d, int row_groups, int k_groups) -> long {
     const long start = (long)(d & 0x3FFF) << 4, lbo = (long)((d >> 16) & 0x3FFF) << 4,
                sbo = (long)((d >> 32) & 0x3FFF) << 4;
     return start + (row_groups - 1) * sbo + (k_groups - 1) * lbo + 127;
   };
-  const int S = w == 7 ? 9 : 10, NA = w == 7 ? 5 : 3, NX = 3;
-  const long a_slice = kTcBM * 16 * 2, x_slice = kTcBN * 16 * 2;
-  const long a_stage = S * a_slice, x_stage = S * x_slice;
+  const int S = w == 7 ? 9 : 10, D = w == 7 ? 8 : 9, NA = w == 7 ? 5 : 3, NX = 3;
+  const long a_slice = kTcBM * 16 * 2;
+  const long a_stage = S * a_slice;
+  const long x_stage = 2L * S * (kTcBN / 8) * 128;
   const long off_x = NA * a_stage;
   if (KP % 16 != 0 || KP > 272) return -1;
+  if ((D + 1) * kTcBN > 512) return -4;
   for (int st = 0; st < NA; ++st)
     for (int s = 0; s < S; ++s) {
       const uint64_t d = tc_smem_desc((uint32_t)(st * a_stage + s * a_slice), kTcALbo, kTcSbo);
       if (last_byte(d, kTcBM / 8, 2) >= (st * a_stage + (s + 1) * a_slice)) return -2;
     }
   for (int st = 0; st < NX; ++st)
-    for (int t = 0; t < S; ++t) {
-      const uint64_t d = tc_smem_desc((uint32_t)(off_x + st * x_stage + t * x_slice), kTcXLbo, kTcSbo);
-      if (last_byte(d, kTcBN / 8, 2) >= off_x + st * x_stage + (t + 1) * x_slice) return -3;
+    for (int s = 0; s <= D; ++s) {
+      const int ntot = (D + 1 - s) * kTcBN;
+      for (int c = 0; c < ntot; c += 256) {
+        const int n = ntot - c < 256 ? ntot - c : 256;
+        if (n % 16 != 0 || s * kTcBN + c + n > 512) return -4;
+        const uint64_t d = tc_smem_desc((uint32_t)(off_x + st * x_stage + (c / 8) * 128), tc_x_lbo(S), kTcSbo);
+        if (last_byte(d, n / 8, 2) >= off_x + (st + 1) * x_stage) return -3;
+      }
     }
   return 0;
 }

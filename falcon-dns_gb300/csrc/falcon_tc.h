@@ -10,15 +10,20 @@
 namespace falcon {
 
 constexpr int kTcBM = 128;  // operator rows per tile (the MMA's M)
-constexpr int kTcBN = 48;   // X columns per tile (the MMA's N)
+constexpr int kTcBN = 48;   // X columns per tile (one slice's share of the MMA's N)
+constexpr int kTcEpilogue = 256;   // epilogue threads (warps 0-7)
+constexpr int kTcProducers = 128;  // X producer threads (warps 8-11)
+constexpr int kTcWarpTma = 12;     // tensor-memory allocation and operator copies
+constexpr int kTcThreads = 448;    // + the MMA warp (13)
 // Shared-memory layouts (no swizzle, K-major, core matrix = 8 rows x 16 B
 // stored as 128 contiguous bytes): the operator stage holds per slice two
 // k groups of 128 rows (stride-dimension offset 128 B between 8-row
 // groups, leading-dimension offset 2048 B between the k groups); the X
-// stage per slice two k groups of 48 columns (128 B, 768 B).
+// stage holds two k groups of all S slices' 48 columns side by side (128 B
+// between 8-column groups, S x 768 B between the k groups).
 constexpr uint32_t kTcSbo = 128;
 constexpr uint32_t kTcALbo = kTcBM * 16;
-constexpr uint32_t kTcXLbo = kTcBN * 16;
+__host__ __device__ constexpr uint32_t tc_x_lbo(int S) { return (uint32_t)S * kTcBN * 16; }
 
 // Shared-memory matrix descriptor of tcgen05.mma: start address, leading
 // and stride byte offsets (each >> 4, 14 bits), descriptor version 1 (bits

@@ -40,11 +40,11 @@ def encoder(tmp_path_factory, fg):
 #include "falcon_tc.h"
 int main() {
   using namespace falcon;
-  std::printf("%d %d %u %u %u\n", kTcBM, kTcBN, kTcSbo, kTcALbo, kTcXLbo);
+  std::printf("%d %d %u %u %u %u\n", kTcBM, kTcBN, kTcSbo, kTcALbo, tc_x_lbo(9), tc_x_lbo(10));
   const unsigned starts[] = {0u, 4096u, 36864u, 184320u, 227136u};
   for (unsigned s : starts)
     std::printf("%llu %llu\n", (unsigned long long)tc_smem_desc(s, kTcALbo, kTcSbo),
-                (unsigned long long)tc_smem_desc(s, kTcXLbo, kTcSbo));
+                (unsigned long long)tc_smem_desc(s, tc_x_lbo(9), kTcSbo));
   std::printf("%u %u\n", tc_idesc_bf16(128, 48), tc_idesc_bf16(128, 16));
   const int cases[][2] = {{7, 16}, {7, 48}, {7, 80}, {7, 112}, {6, 128}, {6, 144}, {6, 272}, {7, 20}};
   for (auto& c : cases) std::printf("%d\n", tc_stage_layout_check(c[0], c[1]));
@@ -62,8 +62,8 @@ int main() {
 
 
 def test_descriptor_encodings(encoder):
-    bm, bn, sbo, alob, xlbo = (int(x) for x in encoder[0].split())
-    assert (bm, bn, sbo, alob, xlbo) == (128, 48, 128, 128 * 16, 48 * 16)
+    bm, bn, sbo, alob, xlbo, xlbo10 = (int(x) for x in encoder[0].split())
+    assert (bm, bn, sbo, alob, xlbo, xlbo10) == (128, 48, 128, 128 * 16, 9 * 48 * 16, 10 * 48 * 16)
     for line, s in zip(encoder[1:6], (0, 4096, 36864, 184320, 227136)):
         a, x = (int(v) for v in line.split())
         assert a == smem_desc(s, alob, sbo)
@@ -96,11 +96,32 @@ def test_operator_stage_matches_tma_box_order(S):
 
 @pytest.mark.parametrize("S", [9, 10])
 def test_x_stage_matches_producer_stores(S):
-    # producer: unit (column n, k group kg) stores 8 k values as 16 bytes at
-    # slice t: t X_SLICE + (kg 6 + n/8) 128 + (n%8) 16
-    xs = 48 * 16 * 2
+    # producer: unit (column n, k group kg) stores 8 k values of slice t as
+    # 16 bytes at (kg S 6 + t 6 + n/8) 128 + (n%8) 16: slice t's column n is
+    # stage column 48 t + n, k groups S x 768 bytes apart
+    lbo = S * 48 * 16
     for t in range(S):
         for n in range(48):
             for j in range(16):
-                prod = t * xs + ((j // 8) * 6 + n // 8) * 128 + (n % 8) * 16 + (j % 8) * 2
-                assert canonical(t * xs, 48 * 16, 128, n, j) == prod
+                prod = ((j // 8) * S * 6 + t * 6 + n // 8) * 128 + (n % 8) * 16 + (j % 8) * 2
+                assert canonical(0, lbo, 128, 48 * t + n, j) == prod
+
+
+@pytest.mark.parametrize("S", [9, 10])
+def test_concatenated_products_land_on_their_diagonals(S):
+    # the MMA of operator slice s multiplies the stage columns 0 .. 48 (S - s)
+    # (slices t = 0 .. S-1-s) into tensor-memory columns 48 s + c: column
+    # 48 t + n of the product must land in diagonal s + t, column n, in parts
+    # of at most 256 columns whose widths are multiples of 16
+    D = S - 1
+    for s in range(S):
+        ntot = (D + 1 - s) * 48
+        covered = []
+        for c in range(0, ntot, 256):
+            n = min(256, ntot - c)
+            assert n % 16 == 0 and 48 * s + c + n <= 512
+            covered.extend(range(c, c + n))
+        assert covered == list(range(ntot))
+        for i in range(ntot):
+            t, n = divmod(i, 48)
+            assert divmod(48 * s + i, 48) == (s + t, n)
