@@ -54,6 +54,31 @@ __device__ __forceinline__ uint32_t oz_slice_w(unsigned long long T, bool neg, i
   return bf16_bits_of_int(neg ? -q : q);
 }
 
+// Slice s of two magnitudes (T0, T1 < 2^MAGB, each held as 32-bit halves
+// lo:hi) in format W, as a bf16 pair with the signs sgn2 (bits 15 and 31):
+// bf16(128 + q) has the bits 0x4300 + q for 0 <= q < 128, so one packed
+// subtraction of 128 turns the two W-bit fields into bf16 (q0, q1) exactly.
+// The same slices as oz_slice_w, except that a zero slice of a negative
+// value is -0 instead of +0 (both give the same exact products and sums).
+template <int W>
+__device__ __forceinline__ uint32_t oz_slice_pair(uint32_t lo0, uint32_t hi0, uint32_t lo1, uint32_t hi1,
+                                                  uint32_t sgn2, int s) {
+  constexpr uint32_t mask = (1u << W) - 1;
+  const int sh = W * (OzCfg<W>::S - 1 - s);
+  uint32_t a, b;
+  if (sh >= 32) {
+    a = hi0 >> (sh - 32);
+    b = hi1 >> (sh - 32);
+  } else {
+    a = __funnelshift_r(lo0, hi0, sh);
+    b = __funnelshift_r(lo1, hi1, sh);
+  }
+  const uint32_t biased = ((a & mask) | ((b & mask) << 16)) | 0x43004300u;
+  const __nv_bfloat162 v = __hsub2(*reinterpret_cast<const __nv_bfloat162*>(&biased),
+                                   __floats2bfloat162_rn(128.f, 128.f));
+  return *reinterpret_cast<const uint32_t*>(&v) ^ sgn2;
+}
+
 // v 2^k for |v| < 2^53 built from its bits (integer instructions only:
 // no FP64 pipe), when the result is a normal number; else from ldexp.
 __device__ __forceinline__ double oz_i64_scaled(long long v, int k) {

@@ -4,11 +4,16 @@
 // (falcon_ozaki.cu, OzCfg in falcon_slices.cuh): every FP32 sum of slice
 // products is exact, so both kernels give the same bits.
 //
-// Tile: 128 operator rows (the MMA's M) x 48 X columns (N).  Per slice
-// diagonal d = s + t one FP32 accumulator of 128 x 48 in tensor memory
-// (9 or 10 diagonals: 432 or 480 of the 512 columns).  Per 16-wide K chunk
-// the MMA warp issues the slice-pair products s + t <= D (45 or 55
-// tcgen05.mma.kind::f16 of 128 x 48 x 16, bf16 in, FP32 accumulate).
+// Tile: 128 operator rows (the MMA's M) x 24 X columns.  Per slice diagonal
+// d = s + t one FP32 accumulator of 128 x 24 in tensor memory, the S
+// diagonals side by side (diagonal d at column 24 d of its buffer), and two
+// such buffers (columns 0 and 256), so the epilogue of one tile runs while
+// the next tile multiplies.  Per 16-wide K chunk and operator slice s the
+// MMA warp issues ONE tcgen05.mma.kind::f16 (bf16 in, FP32 accumulate): A_s
+// against the X slices 0..S-1-s laid side by side along N, whose products
+// land exactly on the diagonals s..S-1 (N rounded up to a multiple of 16;
+// the extra columns' products fall in a spill strip after the last
+// diagonal).  The operator slice is read from shared memory once per chunk.
 //
 // Operands in shared memory, no swizzle, K-major core matrices (8 rows x
 // 16 bytes):
@@ -17,24 +22,23 @@
 //    K chunk brings all S slices of a 128-row tile.  When the whole K fits
 //    in the stage ring (KP <= 80 for 7-bit slices) a tile's operator stays
 //    resident while the CTA walks its column tiles;
-//  - X: four producer warps read the FP64 columns, take each column's
-//    exponent over all of K and cut the values into slices directly in
-//    shared memory (no slice planes in HBM).
+//  - X: four producer warps read the FP64 columns (kept in registers), take
+//    each column's exponent over all of K and cut the values into slices
+//    directly in shared memory (no slice planes in HBM), two slices per
+//    packed bf16 subtraction.
 // Warp roles (448 threads, one CTA per SM, persistent over a contiguous
 // range of (entry, row tile, column tile) work items):
 //   0-7   epilogue: tcgen05.ld of the diagonals (warp w reads tensor-memory
-//         lanes 32 (w%4).. (operator rows), half w/4 of the columns), exact
+//         lanes 32 (w%4).. = operator rows, half w/4 of the columns), exact
 //         recombination, FP64 stores;
 //   8-11  X producers;
 //   12    tensor-memory allocation and the operator's TMA copies (lane 0);
-//   13    MMA issue (lane 0): per K chunk and operator slice s one MMA of
-//         A_s against the X slices 0..D-s side by side along N (up to 13 or
-//         15 MMAs of N <= 256 per chunk instead of 45 or 55 of N = 48, so the
-//         operator slice is read from shared memory once per chunk).
+//   13    MMA issue (lane 0).
 // Every wait on an mbarrier is bounded: after ~1 s a wait sets an error
 // word in global memory and the CTA's abort flag, and every role leaves
 // its loop; the MMA warp waits (bounded) for its own products and the TMA
-// warp for its own copies before the tensor memory is freed.
+// warp for its own copies before the tensor memory is freed.  Waiting
+// threads sleep in hardware (try_wait with a suspend-time hint).
 #include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -56,25 +60,26 @@ struct TcCfg {
   static constexpr int S = OzCfg<W>::S, D = OzCfg<W>::D, HD = OzCfg<W>::HD, MAGB = OzCfg<W>::MAGB;
   static constexpr int BM = kTcBM, BN = kTcBN, BK = 16;
   static constexpr int NA = (W == 7) ? 5 : 3;  // operator stages (16 k each)
-  static constexpr int NX = 3;                 // X stages
+  static constexpr int NX = 4;                 // X stages
   static constexpr int A_SLICE = BM * BK * 2;  // 4096 bytes: 2 k groups x 128 rows x 16 B
   static constexpr int A_STAGE = S * A_SLICE;
-  // X stage: [k group (2)][column group (S x 6)][8 columns][16 B]: slice t's
-  // column n is stage column 48 t + n, so the slices lie side by side along N
-  static constexpr int XGROUPS = S * (BN / 8);
-  static constexpr uint32_t XLBO = tc_x_lbo(S);  // between the two k groups (XGROUPS x 128 B)
+  // X stage: [k group (2)][column group (XCOLS / 8)][8 columns][16 B]
+  static constexpr int XCOLS = tc_x_cols(S);
+  static constexpr int XGROUPS = XCOLS / 8;
+  static constexpr uint32_t XLBO = tc_x_lbo(S);  // between the two k groups
   static constexpr int X_STAGE = 2 * XGROUPS * 128;
   static constexpr int OFF_A = 0;
   static constexpr int OFF_X = NA * A_STAGE;
   static constexpr int OFF_CEX = OFF_X + NX * X_STAGE;  // int [4][BN] column exponents
-  static constexpr int OFF_PM = OFF_CEX + 4 * BN * 4;   // int [2][BN] partial maxima
-  static constexpr int NBAR = 2 * NA + 2 * NX + 2 + 8 + 1;
-  static constexpr int OFF_BAR = OFF_PM + 2 * BN * 4;
-  static constexpr int OFF_MISC = OFF_BAR + NBAR * 8;   // tensor-memory address, abort flag
+  static constexpr int OFF_PM = OFF_CEX + 4 * BN * 4;   // int [4][BN] partial maxima
+  static constexpr int NBAR = 2 * NA + 2 * NX + 4 + 8 + 1;
+  static constexpr int OFF_BAR = OFF_PM + 4 * BN * 4;
+  static constexpr int OFF_MISC = OFF_BAR + NBAR * 8;   // tensor-memory address, abort flag, producer flags
   static constexpr int BYTES = OFF_MISC + 16;
   static constexpr int SMEM = BYTES + 1024;             // + alignment of the base to 1 KiB
   static constexpr uint32_t TMEM_COLS = 512;
-  static_assert((D + 1) * BN <= (int)TMEM_COLS, "diagonal accumulators exceed tensor memory");
+  static_assert(S * BN + 8 <= kTcAccStride && 2 * kTcAccStride <= (int)TMEM_COLS, "accumulator buffers");
+  static_assert(tc_mma_n(S, 0) <= 256, "MMA N");
   static_assert(SMEM <= 227 * 1024, "shared memory");
 };
 
@@ -91,12 +96,15 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t* b, uint32_t bytes) {
                "r"(bytes)
                : "memory");
 }
-__device__ __forceinline__ bool mbar_try(uint64_t* b, uint32_t parity) {
+// try_wait with a suspend-time hint: the thread sleeps in hardware until the
+// phase completes or ~20 us pass, so waiting warps take no issue slots from
+// the producer and epilogue warps on their sub-partition.
+__device__ __forceinline__ bool mbar_try_sleep(uint64_t* b, uint32_t parity) {
   uint32_t ok;
   asm volatile(
-      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\tselp.u32 %0, 1, 0, p;\n\t}"
       : "=r"(ok)
-      : "r"(su32(b)), "r"(parity)
+      : "r"(su32(b)), "r"(parity), "r"(20000u)
       : "memory");
   return ok != 0;
 }
@@ -104,7 +112,7 @@ __device__ __forceinline__ bool mbar_try(uint64_t* b, uint32_t parity) {
 // (this wait timed out, or another role's did).
 __device__ __noinline__ bool mbar_wait(uint64_t* b, uint32_t parity, volatile int* abort_flag, int* err, int code) {
   const long long t0 = clock64();
-  while (!mbar_try(b, parity)) {
+  while (!mbar_try_sleep(b, parity)) {
     if (*abort_flag) return false;
     if (clock64() - t0 > kSpinCycles) {
       *abort_flag = 1;
@@ -138,9 +146,9 @@ __device__ __forceinline__ void tc_commit(uint64_t* b) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(su32(b)) : "memory");
 }
 
-__device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t (&r)[8]) {
-  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
-               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+__device__ __forceinline__ void tmem_ld4(uint32_t taddr, uint32_t (&r)[4]) {
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0, %1, %2, %3}, [%4];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
                : "r"(taddr));
 }
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
@@ -158,25 +166,6 @@ __device__ __forceinline__ TileIdx tile_of(long t, int n_mt, int n_nt) {
   return r;
 }
 
-// The MMA products of one K chunk for operator slice s: A_s times the X
-// slices t = 0..D-s laid side by side along N (stage column t*48 + n),
-// accumulated into the diagonals s..D, whose accumulators are contiguous in
-// tensor memory (diagonal d at column 48 d): one MMA of N = 48 (D + 1 - s)
-// columns, split into parts of at most 256 (the largest N of an M = 128
-// MMA); every part's N is a multiple of 16.
-template <int W>
-__device__ __forceinline__ void tc_slice_products(int s, uint32_t tmem, uint32_t a_addr, uint32_t x_addr,
-                                                  uint32_t acc) {
-  using C = TcCfg<W>;
-  const uint64_t adesc = tc_smem_desc(a_addr, kTcALbo, kTcSbo);
-  const int ntot = (C::D + 1 - s) * C::BN;
-  for (int c = 0; c < ntot; c += 256) {
-    const int n = ntot - c < 256 ? ntot - c : 256;
-    const uint64_t bdesc = tc_smem_desc(x_addr + (uint32_t)(c / 8) * 128u, C::XLBO, kTcSbo);
-    tc_mma(tmem + (uint32_t)(s * C::BN + c), adesc, bdesc, tc_idesc_bf16(C::BM, n), acc);
-  }
-}
-
 template <int W>
 __global__ void __launch_bounds__(448, 1) tc_gemm_kernel(const __grid_constant__ CUtensorMap amap, const TcArgs q) {
   using C = TcCfg<W>;
@@ -188,10 +177,10 @@ __global__ void __launch_bounds__(448, 1) tc_gemm_kernel(const __grid_constant__
   uint64_t* empty_a = full_a + C::NA;
   uint64_t* full_x = empty_a + C::NA;
   uint64_t* empty_x = full_x + C::NX;
-  uint64_t* acc_full = empty_x + C::NX;
-  uint64_t* acc_empty = acc_full + 1;
-  uint64_t* cex_full = acc_empty + 1;  // [4]
-  uint64_t* cex_empty = cex_full + 4;  // [4]
+  uint64_t* acc_full = empty_x + C::NX;  // [2]
+  uint64_t* acc_empty = acc_full + 2;    // [2]
+  uint64_t* cex_full = acc_empty + 2;    // [4]
+  uint64_t* cex_empty = cex_full + 4;    // [4]
   uint64_t* drain = cex_empty + 4;
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(sm + C::OFF_MISC);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(sm + C::OFF_MISC + 4);
@@ -201,19 +190,28 @@ __global__ void __launch_bounds__(448, 1) tc_gemm_kernel(const __grid_constant__
   if (tid == 0) {
     for (int i = 0; i < C::NA; ++i) { mbar_init(&full_a[i], 1); mbar_init(&empty_a[i], 1); }
     for (int i = 0; i < C::NX; ++i) { mbar_init(&full_x[i], kTcProducers); mbar_init(&empty_x[i], 1); }
-    mbar_init(acc_full, 1);
-    mbar_init(acc_empty, kTcEpilogue);
+    for (int i = 0; i < 2; ++i) { mbar_init(&acc_full[i], 1); mbar_init(&acc_empty[i], kTcEpilogue); }
     for (int i = 0; i < 4; ++i) { mbar_init(&cex_full[i], kTcProducers); mbar_init(&cex_empty[i], kTcEpilogue); }
     mbar_init(drain, 1);
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
+  // the X stages' padding columns (read only by the rounded-up MMAs, whose
+  // products there land in the spill strip) hold zeros
+  if constexpr (C::XCOLS > C::S * C::BN)
+    for (int i = tid; i < C::NX * 2 * (C::XCOLS - C::S * C::BN) * 4; i += blockDim.x) {
+      const int words = (C::XCOLS - C::S * C::BN) * 4;  // 32-bit words of the padding per k group
+      const int st = i / (2 * words), kg = (i / words) % 2, w = i % words;
+      reinterpret_cast<uint32_t*>(sm + C::OFF_X + st * C::X_STAGE + kg * C::XGROUPS * 128 +
+                                  C::S * C::BN * 16)[w] = 0u;
+    }
   if (warp == kTcWarpTma) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(su32(tmem_slot)),
                  "r"(C::TMEM_COLS)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
+  fence_async_smem();
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
@@ -229,15 +227,16 @@ __global__ void __launch_bounds__(448, 1) tc_gemm_kernel(const __grid_constant__
   if (warp < kTcEpilogue / 32) {
     // ---------------- epilogue ----------------
     // warp (q, h): tensor-memory lanes 32q..32q+31 (operator rows), columns
-    // h*24..h*24+23 of the tile; waits are taken by lane 0 and broadcast, so
-    // a warp leaves together (tcgen05.ld is warp-collective)
+    // 12h..12h+11 of the tile; waits are taken by lane 0 and broadcast, so a
+    // warp leaves together (tcgen05.ld is warp-collective)
     const int qd = warp & 3, half = warp >> 2;
     long u = 0;
     for (long t = t_begin; t < t_end; ++t, ++u) {
       const TileIdx ti = tile_of(t, n_mt, n_nt);
+      const int buf = (int)(u & 1);
       int ok = 1;
       if (lane == 0)
-        ok = mbar_wait(acc_full, (uint32_t)(u & 1), abort_flag, q.err, 1) &&
+        ok = mbar_wait(&acc_full[buf], (uint32_t)((u >> 1) & 1), abort_flag, q.err, 1) &&
              mbar_wait(&cex_full[u & 3], (uint32_t)((u >> 2) & 1), abort_flag, q.err, 2);
       ok = __shfl_sync(0xffffffffu, ok, 0);
       __syncwarp();
@@ -256,21 +255,21 @@ __global__ void __launch_bounds__(448, 1) tc_gemm_kernel(const __grid_constant__
         yrow = q.Y[o] + (size_t)ti.z * q.sY + (size_t)(r - r0) * q.ldy;
       }
       const int n0 = ti.nt * C::BN;
-      const uint32_t lane_addr = tmem + ((uint32_t)(qd * 32) << 16);
+      const uint32_t lane_addr = tmem + ((uint32_t)(qd * 32) << 16) + (uint32_t)(buf * kTcAccStride);
 #pragma unroll 1
-      for (int c0 = half * (C::BN / 2); c0 < (half + 1) * (C::BN / 2); c0 += 8) {
-        uint32_t v[C::D + 1][8];
+      for (int c0 = half * (C::BN / 2); c0 < (half + 1) * (C::BN / 2); c0 += 4) {
+        uint32_t v[C::D + 1][4];
 #pragma unroll
-        for (int d = 0; d <= C::D; ++d) tmem_ld8(lane_addr + (uint32_t)(d * C::BN + c0), v[d]);
+        for (int d = 0; d <= C::D; ++d) tmem_ld4(lane_addr + (uint32_t)(d * C::BN + c0), v[d]);
         tmem_wait_ld();
 #pragma unroll
         for (int d = 0; d <= C::D; ++d)
 #pragma unroll
-          for (int j = 0; j < 8; ++j) asm volatile("" : "+r"(v[d][j]));
+          for (int j = 0; j < 4; ++j) asm volatile("" : "+r"(v[d][j]));
         if (valid) {
-          double out[8];
+          double out[4];
 #pragma unroll
-          for (int j = 0; j < 8; ++j) {
+          for (int j = 0; j < 4; ++j) {
             long long H = 0, L = 0;
 #pragma unroll
             for (int d = 0; d <= C::HD; ++d) H = H * (1 << W) + (long long)__float2int_rn(__uint_as_float(v[d][j]));
@@ -285,34 +284,35 @@ __global__ void __launch_bounds__(448, 1) tc_gemm_kernel(const __grid_constant__
           }
           const int n = n0 + c0;
           double* yp = yrow + n;
-          if (n + 8 <= q.N && (reinterpret_cast<uintptr_t>(yp) & 15) == 0) {
-#pragma unroll
-            for (int j = 0; j < 8; j += 2) *reinterpret_cast<double2*>(yp + j) = make_double2(out[j], out[j + 1]);
+          if (n + 4 <= q.N && (reinterpret_cast<uintptr_t>(yp) & 15) == 0) {
+            *reinterpret_cast<double2*>(yp) = make_double2(out[0], out[1]);
+            *reinterpret_cast<double2*>(yp + 2) = make_double2(out[2], out[3]);
           } else {
 #pragma unroll
-            for (int j = 0; j < 8; ++j)
+            for (int j = 0; j < 4; ++j)
               if (n + j < q.N) yp[j] = out[j];
           }
         }
       }
       tc_fence_before();
-      mbar_arrive(acc_empty);
+      mbar_arrive(&acc_empty[buf]);
       mbar_arrive(&cex_empty[u & 3]);
     }
   } else if (warp < (kTcEpilogue + kTcProducers) / 32) {
     // ---------------- X producers ----------------
-    // Thread (column n, k group kg) owns the values k = 16 c + 8 kg + i of
-    // its column: it reads them once per tile (the first RC chunks stay in
-    // registers), takes the column exponent with its partner, then cuts
-    // them into slices chunk by chunk.  Waits are taken by thread 0 and
-    // passed on through prod_ok (two slots by wait parity) at a named
-    // barrier, so the producers always leave together and the named
-    // barriers stay matched.
-    constexpr int RC = 5;
+    // Thread (column n, k group kg, half h) owns the values k = 16 c + 8 kg +
+    // 4 h + i (i < 4) of its column: it reads them once per tile (the first
+    // RC chunks stay in registers), takes the column exponent with its three
+    // partners, then cuts them into slices chunk by chunk (8 bytes per
+    // slice).  Waits are taken by thread 0 and passed on through prod_ok
+    // (two slots by wait parity) at a named barrier, so the producers always
+    // leave together and the named barriers stay matched.
+    constexpr int RC = 9;  // K up to 144 (Nr = 129) held in registers
     const int tp = tid - kTcEpilogue;
     volatile int* prod_ok = reinterpret_cast<volatile int*>(sm + C::OFF_MISC + 8);
-    const int n = tp % C::BN, kg = tp / C::BN;
-    const bool act = tp < 2 * C::BN;
+    const bool act = tp < 4 * C::BN;
+    const int hq = tp / (2 * C::BN), rem = tp % (2 * C::BN), kg = rem / C::BN, n = rem % C::BN;
+    const int part = kg * 2 + hq;  // partner index for the column maximum
     long xc = 0, u = 0, nw = 0;
     bool stop = false;
     for (long t = t_begin; t < t_end && !stop; ++t, ++u) {
@@ -320,35 +320,35 @@ __global__ void __launch_bounds__(448, 1) tc_gemm_kernel(const __grid_constant__
       const int n0 = ti.nt * C::BN, nn = n0 + n;
       const double* Xz = q.X + (size_t)ti.z * q.sX;
       const bool col = act && nn < q.N;
-      double v[RC][8];
+      double v[RC][4];
       int mx = 0;
 #pragma unroll
       for (int c = 0; c < RC; ++c)
 #pragma unroll
-        for (int i = 0; i < 8; ++i) {
-          const int k = c * C::BK + kg * 8 + i;
+        for (int i = 0; i < 4; ++i) {
+          const int k = c * C::BK + kg * 8 + hq * 4 + i;
           v[c][i] = (col && c < nk && k < q.K) ? Xz[(size_t)k * q.ldx + nn] : 0.0;
         }
       for (int c = RC; c < nk; ++c)
 #pragma unroll
-        for (int i = 0; i < 8; ++i) {
-          const int k = c * C::BK + kg * 8 + i;
+        for (int i = 0; i < 4; ++i) {
+          const int k = c * C::BK + kg * 8 + hq * 4 + i;
           if (col && k < q.K) mx = max(mx, biased_exp(Xz[(size_t)k * q.ldx + nn]));
         }
 #pragma unroll
       for (int c = 0; c < RC; ++c)
 #pragma unroll
-        for (int i = 0; i < 8; ++i) mx = max(mx, biased_exp(v[c][i]));
+        for (int i = 0; i < 4; ++i) mx = max(mx, biased_exp(v[c][i]));
       if (tp == 0)
         prod_ok[nw & 1] = mbar_wait(&cex_empty[u & 3], (uint32_t)(((u >> 2) & 1) ^ 1), abort_flag, q.err, 3) ? 1 : 0;
-      if (act) pm[kg * C::BN + n] = mx;
+      if (act) pm[part * C::BN + n] = mx;
       named_sync(1, kTcProducers);
       if (!prod_ok[(nw++) & 1]) break;
       int* cex = cex_ring + (u & 3) * C::BN;
-      const int fb = act ? max(pm[n], pm[C::BN + n]) : 0;
+      const int fb = act ? max(max(pm[n], pm[C::BN + n]), max(pm[2 * C::BN + n], pm[3 * C::BN + n])) : 0;
       if (tp < C::BN) cex[tp] = fb;
       mbar_arrive(&cex_full[u & 3]);
-      auto produce = [&](int c, const double (&vals)[8]) -> bool {
+      auto produce = [&](const double (&vals)[4]) -> bool {
         const long j = xc++;
         const int st = (int)(j % C::NX);
         if (tp == 0)
@@ -356,22 +356,23 @@ __global__ void __launch_bounds__(448, 1) tc_gemm_kernel(const __grid_constant__
         named_sync(1, kTcProducers);
         if (!prod_ok[(nw++) & 1]) return false;
         if (act) {
-          unsigned long long Tm[8];
-          uint32_t sg = 0;
+          uint32_t lo[4], hi[4], sg[2];
 #pragma unroll
-          for (int i = 0; i < 8; ++i) {
-            Tm[i] = fb > 0 ? oz_magb<C::MAGB>(vals[i], fb - 1022) : 0ull;
-            if (__double_as_longlong(vals[i]) < 0) sg |= 1u << i;
+          for (int i = 0; i < 4; ++i) {
+            const unsigned long long Tm = fb > 0 ? oz_magb<C::MAGB>(vals[i], fb - 1022) : 0ull;
+            lo[i] = (uint32_t)Tm;
+            hi[i] = (uint32_t)(Tm >> 32);
           }
-          uint8_t* xs = sm + C::OFF_X + st * C::X_STAGE + (kg * C::XGROUPS + n / 8) * 128 + (n % 8) * 16;
+#pragma unroll
+          for (int p = 0; p < 2; ++p)
+            sg[p] = (__double_as_longlong(vals[2 * p]) < 0 ? 0x8000u : 0u) |
+                    (__double_as_longlong(vals[2 * p + 1]) < 0 ? 0x80000000u : 0u);
+          uint8_t* xs = sm + C::OFF_X + st * C::X_STAGE + (kg * C::XGROUPS + n / 8) * 128 + (n % 8) * 16 + hq * 8;
 #pragma unroll
           for (int s = 0; s < C::S; ++s) {
-            uint32_t w4[4];
-#pragma unroll
-            for (int p = 0; p < 4; ++p)
-              w4[p] = oz_slice_w<W>(Tm[2 * p], (sg >> (2 * p)) & 1, s) |
-                      (oz_slice_w<W>(Tm[2 * p + 1], (sg >> (2 * p + 1)) & 1, s) << 16);
-            *reinterpret_cast<uint4*>(xs + s * (C::BN / 8) * 128) = make_uint4(w4[0], w4[1], w4[2], w4[3]);
+            const uint32_t w0 = oz_slice_pair<W>(lo[0], hi[0], lo[1], hi[1], sg[0], s);
+            const uint32_t w1 = oz_slice_pair<W>(lo[2], hi[2], lo[3], hi[3], sg[1], s);
+            *reinterpret_cast<uint2*>(xs + s * (C::BN / 8) * 128) = make_uint2(w0, w1);
           }
         }
         fence_async_smem();
@@ -380,15 +381,15 @@ __global__ void __launch_bounds__(448, 1) tc_gemm_kernel(const __grid_constant__
       };
 #pragma unroll
       for (int c = 0; c < RC; ++c)
-        if (c < nk && !stop && !produce(c, v[c])) stop = true;
+        if (c < nk && !stop && !produce(v[c])) stop = true;
       for (int c = RC; c < nk && !stop; ++c) {
-        double w8[8];
+        double w4[4];
 #pragma unroll
-        for (int i = 0; i < 8; ++i) {
-          const int k = c * C::BK + kg * 8 + i;
-          w8[i] = (col && k < q.K) ? Xz[(size_t)k * q.ldx + nn] : 0.0;
+        for (int i = 0; i < 4; ++i) {
+          const int k = c * C::BK + kg * 8 + hq * 4 + i;
+          w4[i] = (col && k < q.K) ? Xz[(size_t)k * q.ldx + nn] : 0.0;
         }
-        if (!produce(c, w8)) stop = true;
+        if (!produce(w4)) stop = true;
       }
     }
   } else if (warp == kTcWarpTma) {
@@ -416,7 +417,7 @@ __global__ void __launch_bounds__(448, 1) tc_gemm_kernel(const __grid_constant__
       // flight when the CTA ends
       for (long j = (issued > C::NA ? issued - C::NA : 0); j < issued; ++j) {
         const long long t0 = clock64();
-        while (!mbar_try(&full_a[j % C::NA], (uint32_t)((j / C::NA) & 1)) && clock64() - t0 < kSpinCycles) {
+        while (!mbar_try_sleep(&full_a[j % C::NA], (uint32_t)((j / C::NA) & 1)) && clock64() - t0 < kSpinCycles) {
         }
       }
     }
@@ -440,8 +441,10 @@ __global__ void __launch_bounds__(448, 1) tc_gemm_kernel(const __grid_constant__
           abase = ac;
           ac += nk;
         }
-        if (u > 0 && !mbar_wait(acc_empty, (uint32_t)((u - 1) & 1), abort_flag, q.err, 6)) break;
+        const int buf = (int)(u & 1);
+        if (u > 1 && !mbar_wait(&acc_empty[buf], (uint32_t)(((u - 2) >> 1) & 1), abort_flag, q.err, 6)) break;
         tc_fence_after();
+        const uint32_t acc_base = tmem + (uint32_t)(buf * kTcAccStride);
         bool ok = true;
         for (int c = 0; c < nk && ok; ++c) {
           const long ja = resident ? abase + c : ac++;
@@ -459,25 +462,27 @@ __global__ void __launch_bounds__(448, 1) tc_gemm_kernel(const __grid_constant__
           }
           tc_fence_after();
           const uint32_t a_stage = sm_base + C::OFF_A + sa * C::A_STAGE;
-          const uint32_t x_stage = sm_base + C::OFF_X + sx * C::X_STAGE;
-          // s = 0 writes every diagonal fresh in the first chunk of a tile;
-          // the rest accumulate
+          const uint64_t bdesc = tc_smem_desc(sm_base + C::OFF_X + sx * C::X_STAGE, C::XLBO, kTcSbo);
+          // operator slice s against the X slices 0..S-1-s side by side:
+          // products on the diagonals s..S-1 (s = 0 writes every diagonal
+          // fresh in the first chunk of a tile; the rest accumulate)
 #pragma unroll 1
           for (int s = 0; s < C::S; ++s)
-            tc_slice_products<W>(s, tmem, a_stage + s * C::A_SLICE, x_stage, (c > 0 || s > 0) ? 1u : 0u);
+            tc_mma(acc_base + (uint32_t)(s * C::BN), tc_smem_desc(a_stage + s * C::A_SLICE, kTcALbo, kTcSbo), bdesc,
+                   tc_idesc_bf16(C::BM, tc_mma_n(C::S, s)), (c > 0 || s > 0) ? 1u : 0u);
           any = true;
           tc_commit(&empty_x[sx]);
           if (!resident || last_of_item) tc_commit(&empty_a[sa]);
         }
         if (!ok) break;
-        tc_commit(acc_full);
+        tc_commit(&acc_full[buf]);
       }
       // wait for every product this thread issued (bounded) before the
       // tensor memory is freed
       if (any) {
         tc_commit(drain);
         const long long t0 = clock64();
-        while (!mbar_try(drain, 0) && clock64() - t0 < kSpinCycles) {
+        while (!mbar_try_sleep(drain, 0) && clock64() - t0 < kSpinCycles) {
         }
       }
     }
@@ -558,7 +563,7 @@ int tc_make_operator_map(CUtensorMap* map, const uint16_t* slices, int nb, int S
 
 int tc_stage_layout_check(int w, int KP) {
   // every descriptor of the kernel stays inside its shared-memory stage and
-  // every accumulator inside the allocated tensor memory: decode start,
+  // every accumulator inside its tensor-memory buffer: decode start,
   // leading and stride offsets back from the encodings and bound the last
   // byte of the last core matrix an MMA reads
   auto last_byte = [](uint64_t d, int row_groups, int k_groups) -> long {
@@ -566,27 +571,24 @@ int tc_stage_layout_check(int w, int KP) {
                sbo = (long)((d >> 32) & 0x3FFF) << 4;
     return start + (row_groups - 1) * sbo + (k_groups - 1) * lbo + 127;
   };
-  const int S = w == 7 ? 9 : 10, D = w == 7 ? 8 : 9, NA = w == 7 ? 5 : 3, NX = 3;
+  const int S = tc_slices(w), NA = w == 7 ? 5 : 3, NX = 4;
   const long a_slice = kTcBM * 16 * 2;
   const long a_stage = S * a_slice;
-  const long x_stage = 2L * S * (kTcBN / 8) * 128;
+  const long x_stage = 2L * tc_x_cols(S) * 16;
   const long off_x = NA * a_stage;
   if (KP % 16 != 0 || KP > 272) return -1;
-  if ((D + 1) * kTcBN > 512) return -4;
+  if (S * kTcBN + 8 > kTcAccStride || 2 * kTcAccStride > 512) return -4;
   for (int st = 0; st < NA; ++st)
     for (int s = 0; s < S; ++s) {
       const uint64_t d = tc_smem_desc((uint32_t)(st * a_stage + s * a_slice), kTcALbo, kTcSbo);
       if (last_byte(d, kTcBM / 8, 2) >= (st * a_stage + (s + 1) * a_slice)) return -2;
     }
   for (int st = 0; st < NX; ++st)
-    for (int s = 0; s <= D; ++s) {
-      const int ntot = (D + 1 - s) * kTcBN;
-      for (int c = 0; c < ntot; c += 256) {
-        const int n = ntot - c < 256 ? ntot - c : 256;
-        if (n % 16 != 0 || s * kTcBN + c + n > 512) return -4;
-        const uint64_t d = tc_smem_desc((uint32_t)(off_x + st * x_stage + (c / 8) * 128), tc_x_lbo(S), kTcSbo);
-        if (last_byte(d, n / 8, 2) >= off_x + (st + 1) * x_stage) return -3;
-      }
+    for (int s = 0; s < S; ++s) {
+      const int n = tc_mma_n(S, s);
+      if (n % 16 != 0 || n > 256 || n > tc_x_cols(S) || s * kTcBN + n > kTcAccStride) return -4;
+      const uint64_t d = tc_smem_desc((uint32_t)(off_x + st * x_stage), tc_x_lbo(S), kTcSbo);
+      if (last_byte(d, n / 8, 2) >= off_x + (st + 1) * x_stage) return -3;
     }
   return 0;
 }

@@ -10,12 +10,22 @@
  * stored mode-fastest, element (m, r) at X[m + M*r], each complex as two
  * doubles (re, im).  A real (R,R) matrix A(i,j) is column-major A[i + R*j].
  *
- * Parity status: transforms pinned against the reference's own Python
- * restatements (python/annulus/cheblib.py) through committed golden vectors;
- * LU pinned against LAPACK dgetrf/dgetrs (SciPy); time stepping pinned by
- * analytic known answers (conductive steady state, linear decay).  FFTW and
- * LAPACK are not vendored by the reference, so bitwise equality with the
- * reference binary is not claimed: agreement is to rounding.
+ * Parity status (tests/golden/make_golden.py writes the fixtures from the
+ * reference tree; tests/test_oracle_golden.py checks them):
+ *  - transforms against the reference's own Python restatements
+ *    (python/annulus/cheblib.py: chebtransform, chebinvtran, D1, D2);
+ *  - azimuthal transforms against the explicit sums of src/fourier_GG.F90;
+ *  - LU against LAPACK dgetrf/dgetrs (SciPy), identical pivots;
+ *  - operator assembly (orc_mat_assemble: AT, AF in both boundary-row
+ *    orders, A_uphi, LAPpsi, no-slip and stress-free) against an
+ *    independent numpy restatement of src/mat_assembly.F90;
+ *  - restart resampling against the reference's cheblib padding;
+ *  - the namelist reader against the reference's own src/input.txt;
+ *  - time stepping by analytic known answers (conductive steady state,
+ *    linear decay, schemes consistent in dt, scheme orders).
+ * FFTW and LAPACK are not vendored by the reference and no Fortran compiler
+ * exists here, so bitwise equality with the reference binary is not
+ * claimed: agreement is to rounding.
  */
 #ifndef FALCON_ORACLE_H
 #define FALCON_ORACLE_H

@@ -102,3 +102,14 @@ def test_dft_butterfly_sums(p):
                     assert qmax < 2 ** 24
                     exact = sum(Fraction(u) * Fraction(w) for u, w in zip(coef, vals))
                     assert abs(Fraction(y) - exact) <= abs(exact) * Fraction(1, 2 ** 52) + Fraction(col) * Fraction(1, 2 ** 57)
+
+
+def test_bf16_bias_trick_of_the_packed_slices():
+    # oz_slice_pair (falcon_slices.cuh): bf16(128 + q) has the bits 0x4300 + q
+    # for 0 <= q < 128 (exactly representable), so subtracting 128 in bf16
+    # gives q exactly (Sterbenz: 128 <= 128 + q < 256)
+    import numpy as np
+    for q in range(128):
+        b = int(np.float32(128 + q).view(np.uint32))
+        assert b & 0xFFFF == 0 and b >> 16 == 0x4300 + q
+        assert float(np.float32(128 + q) - np.float32(128)) == q

@@ -63,7 +63,8 @@ int main() {
 
 def test_descriptor_encodings(encoder):
     bm, bn, sbo, alob, xlbo, xlbo10 = (int(x) for x in encoder[0].split())
-    assert (bm, bn, sbo, alob, xlbo, xlbo10) == (128, 48, 128, 128 * 16, 9 * 48 * 16, 10 * 48 * 16)
+    # X stages: 9 x 24 = 216 columns rounded up to 224, 10 x 24 = 240
+    assert (bm, bn, sbo, alob, xlbo, xlbo10) == (128, 24, 128, 128 * 16, 224 * 16, 240 * 16)
     for line, s in zip(encoder[1:6], (0, 4096, 36864, 184320, 227136)):
         a, x = (int(v) for v in line.split())
         assert a == smem_desc(s, alob, sbo)
@@ -94,34 +95,48 @@ def test_operator_stage_matches_tma_box_order(S):
                 assert canonical(start, 128 * 16, 128, i, j) == tma
 
 
+def x_cols(S):
+    return (S * 24 + 15) // 16 * 16
+
+
+def mma_n(S, s):
+    return ((S - s) * 24 + 15) // 16 * 16
+
+
 @pytest.mark.parametrize("S", [9, 10])
 def test_x_stage_matches_producer_stores(S):
-    # producer: unit (column n, k group kg) stores 8 k values of slice t as
-    # 16 bytes at (kg S 6 + t 6 + n/8) 128 + (n%8) 16: slice t's column n is
-    # stage column 48 t + n, k groups S x 768 bytes apart
-    lbo = S * 48 * 16
+    # producer: thread (column n, k group kg, half h) stores the 4 k values
+    # 8 kg + 4 h + i of slice t as 8 bytes at (kg XG + 3 t + n/8) 128 +
+    # (n%8) 16 + 8 h, XG = x_cols(S) / 8: slice t's column n is stage column
+    # 24 t + n, the k groups x_cols(S) x 16 bytes apart
+    lbo = x_cols(S) * 16
+    xg = x_cols(S) // 8
     for t in range(S):
-        for n in range(48):
+        for n in range(24):
             for j in range(16):
-                prod = ((j // 8) * S * 6 + t * 6 + n // 8) * 128 + (n % 8) * 16 + (j % 8) * 2
-                assert canonical(0, lbo, 128, 48 * t + n, j) == prod
+                kg, h, i = j // 8, (j % 8) // 4, j % 4
+                prod = (kg * xg + 3 * t + n // 8) * 128 + (n % 8) * 16 + 8 * h + 2 * i
+                assert canonical(0, lbo, 128, 24 * t + n, j) == prod
+    # the padding columns (zeroed once) lie after every slice and inside the stage
+    assert x_cols(S) >= S * 24 and 2 * x_cols(S) * 16 == 2 * xg * 128
 
 
 @pytest.mark.parametrize("S", [9, 10])
 def test_concatenated_products_land_on_their_diagonals(S):
-    # the MMA of operator slice s multiplies the stage columns 0 .. 48 (S - s)
-    # (slices t = 0 .. S-1-s) into tensor-memory columns 48 s + c: column
-    # 48 t + n of the product must land in diagonal s + t, column n, in parts
-    # of at most 256 columns whose widths are multiples of 16
-    D = S - 1
+    # the MMA of operator slice s multiplies stage columns 0 .. N-1 (the X
+    # slices 0 .. S-1-s, N rounded up to a multiple of 16) into
+    # accumulator columns 24 s .. 24 s + N - 1: column 24 t + n of the
+    # product lands in diagonal s + t, column n; the rounding columns land
+    # in the spill strip [24 S, 24 S + 8), which the epilogue never reads;
+    # everything stays inside the 256-column buffer and N <= 256
     for s in range(S):
-        ntot = (D + 1 - s) * 48
-        covered = []
-        for c in range(0, ntot, 256):
-            n = min(256, ntot - c)
-            assert n % 16 == 0 and 48 * s + c + n <= 512
-            covered.extend(range(c, c + n))
-        assert covered == list(range(ntot))
-        for i in range(ntot):
-            t, n = divmod(i, 48)
-            assert divmod(48 * s + i, 48) == (s + t, n)
+        n_mma = mma_n(S, s)
+        assert n_mma % 16 == 0 and n_mma <= 256 and n_mma <= x_cols(S)
+        assert 24 * s + n_mma <= 24 * S + 8 <= 256
+        for i in range(n_mma):
+            col = 24 * s + i
+            if i < 24 * (S - s):
+                t, n = divmod(i, 24)
+                assert divmod(col, 24) == (s + t, n)
+            else:
+                assert 24 * S <= col < 24 * S + 8
