@@ -231,9 +231,11 @@ struct OpSet {
   }
 };
 
-// Contractions through the tensor-core slices (1, default) or the FP64 FMA
-// tiles (0); both are FP64-accurate, the first is several times faster.
-std::atomic<int> g_gemm_mode{1};
+// Contractions through the tensor-core slices, on the tcgen05 kernel where
+// a contraction fills the GPU and on the mma.sync kernels otherwise (2,
+// default), on the mma.sync kernels only (1), or as FP64 FMA tiles (0).
+// The two sliced paths give the same bits; all are FP64-accurate.
+std::atomic<int> g_gemm_mode{2};
 
 // Slices of one column-major operator array (rows x K, lda = rows, nb
 // entries of stride sA) for the tensor-core GEMM.
@@ -1153,6 +1155,23 @@ bool attach_oz(const OpSet* o, GemmArgs* q) {
   return false;
 }
 
+// Contractions that take the tcgen05 kernel: at least two of its
+// 128 x 24 tiles per SM.  Smaller ones (one instance, small groups) are
+// faster on the mma.sync kernel that slices its own X columns, whose
+// per-launch cost is lower; both give the same bits.
+bool tc_worth_it(const GemmArgs& q) {
+  static std::atomic<int> nsm{0};
+  int n = nsm.load();
+  if (n == 0) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+      n = 152;
+    nsm.store(n);
+  }
+  const long tiles = (long)q.batch * ((q.rows + kTcBM - 1) / kTcBM) * ((q.N + kTcBN - 1) / kTcBN);
+  return tiles >= 2L * n;
+}
+
 // The tcgen05 contraction of one GEMM with an attached slice view.
 TcArgs tc_args(const GemmArgs& q) {
   TcArgs t{};
@@ -1182,7 +1201,7 @@ int gemm(Group* g, int cls, const GemmArgs& q0, bool reuse = false) {
     ok = attach_oz(g->ops.get(), &q);
     for (int st = 0; !ok && st < kMaxStages; ++st) ok = attach_oz(g->stage_ops[st].get(), &q);
   }
-  if (ok && g_gemm_mode.load() == 2 && q.oz_tmap) {
+  if (ok && g_gemm_mode.load() == 2 && q.oz_tmap && tc_worth_it(q)) {
     // tcgen05: the kernel slices its own X columns
     const TcArgs t = tc_args(q);
     const CUtensorMap* map = static_cast<const CUtensorMap*>(q.oz_tmap);
@@ -1245,7 +1264,7 @@ int gemm_blocks(Group* g, int cls, std::initializer_list<GemmArgs> blocks) {
       all.oz_xs = nullptr;
       bool ok = attach_oz(g->ops.get(), &all);
       for (int st = 0; !ok && st < kMaxStages; ++st) ok = attach_oz(g->stage_ops[st].get(), &all);
-      if (ok && all.oz_tmap) {
+      if (ok && all.oz_tmap && tc_worth_it(all)) {
         TcArgs t = tc_args(all);
         t.nout = (int)v.size();
         int r = 0;

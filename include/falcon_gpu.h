@@ -365,14 +365,17 @@ long long falcon_launch_count(void);
  * No reference counterpart (launch mechanics of the GPU step). */
 int falcon_set_step_graphs(int enable);
 /* Operator contractions (the radial derivative / Laplacian and per-mode
- * solve products) on the bf16 tensor cores by exact integer slicing of the
- * FP64 operands (mode 1, the default) or as FP64 FMA tiles (mode 0).  Both
- * give FP64-accurate results (error of the order of K 2^-56 max|A_row|
- * max|X_col| for the slices); the first is several times faster on GB300,
- * whose FP64 pipe is ~500x slower than its bf16 tensor cores.  Applies to
- * launches after the call (step graphs already captured keep their mode).
- * Returns the previous mode.  No counterpart in the reference, which uses
- * LAPACK dgetrs (src/algebra_lapack.F90). */
+ * solve products): mode 2 (the default) on the bf16 tensor cores by exact
+ * integer slicing of the FP64 operands, with the 5th-generation tcgen05
+ * MMA (accumulators in tensor memory) for contractions that fill the GPU
+ * and warp-level mma.sync for smaller ones; mode 1 the same slices on
+ * mma.sync only (the same bits as mode 2); mode 0 as FP64 FMA tiles.  All
+ * give FP64-accurate results (the slices: error of the order of K 2^-56
+ * max|A_row| max|X_col|); the sliced forms are several times faster on
+ * GB300, whose FP64 pipe is ~500x slower than its bf16 tensor cores.
+ * Applies to launches after the call (step graphs already captured keep
+ * their mode).  Returns the previous mode.  No counterpart in the
+ * reference, which uses LAPACK dgetrs (src/algebra_lapack.F90). */
 int falcon_set_gemm_mode(int mode);
 
 /* ---- misc ---- */

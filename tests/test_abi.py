@@ -88,9 +88,10 @@ def test_no_cpu_fallback_without_gpu(fg):
 
 
 def test_process_wide_switches_round_trip(fg):
-    # defaults: sliced tensor-core contractions, step graphs, groups of <= 128
+    # defaults: sliced tensor-core contractions (tcgen05 where they fill the
+    # GPU), step graphs, groups of <= 128
     L = fg.lib()
-    assert fg.set_gemm_mode(0) == 1 and fg.set_gemm_mode(1) == 0
+    assert fg.set_gemm_mode(0) == 2 and fg.set_gemm_mode(1) == 0 and fg.set_gemm_mode(2) == 1
     assert fg.set_max_group_size(64) == 128
     assert fg.set_max_group_size(-5) == 64      # negative means one group per key
     assert fg.set_max_group_size(128) == 0
