@@ -285,6 +285,7 @@ def run_uneven(args, fg, stream, torch):
            "operator_groups": b.ngroups, "device_bytes": b.device_bytes, "setup_s": setup_s,
            "gpu_launches": launches, "instances_finite": finite,
            "gflop_per_step": step_flops / 1e9, "tflops": step_flops / (ms / args.uneven_steps / 1e3) / 1e12,
+           "classes_serialised_ms": {c: round(v["ms"], 3) for c, v in prof.items()},
            "workload": "512 instances (seed 4): Nr {33,65,97,129}, Ntheta {128,256,512,1024,1536} (Nm=Ntheta//3), "
                        "scheme {CNAB2,SBDF3,ARS343,BPR353}, Ra log-uniform [1e5,1e8], Pr {0.1,1,10}, "
                        "dt = 0.2 x CFL estimate, FP64"}
@@ -632,10 +633,10 @@ def main():
     ap.add_argument("--gemm-mode", dest="gemm_mode", type=int, default=2, choices=[0, 1, 2],
                     help="operator contractions: 2 tcgen05 (mma.sync for small ones), 1 mma.sync slices, 0 FP64 FMA")
     ap.add_argument("--uneven-instances", dest="uneven_instances", type=int, default=512)
-    ap.add_argument("--uneven-steps", dest="uneven_steps", type=int, default=100)
+    ap.add_argument("--uneven-steps", dest="uneven_steps", type=int, default=500)
     ap.add_argument("--serve-rate", dest="serve_rate", type=float, default=50.0)
-    ap.add_argument("--serve-seconds", dest="serve_seconds", type=float, default=10.0)
-    ap.add_argument("--serve-horizon-scale", dest="serve_horizon_scale", type=float, default=0.1)
+    ap.add_argument("--serve-seconds", dest="serve_seconds", type=float, default=15.0)
+    ap.add_argument("--serve-horizon-scale", dest="serve_horizon_scale", type=float, default=0.15)
     ap.add_argument("--serve-budget-gb", dest="serve_budget_gb", type=int, default=64)
     args = ap.parse_args()
     if args.warmup < 3:

@@ -912,6 +912,8 @@ struct Group {
     graphs.clear();
   }
   ~Group() {
+    // work queued on the stream may still read or write the arrays
+    if (stream) cudaStreamSynchronize(stream);
     drop_graphs();
     cudaFree(oz_xs);
     cudaFree(oz_cexp);
@@ -2759,6 +2761,7 @@ struct falcon_batch {
   bool own_stream = false;
   cudaEvent_t start = nullptr;  // fans the batch's stream out to the group streams
   ~falcon_batch() {
+    if (stream) cudaStreamSynchronize(stream);
     groups.clear();
     if (start) cudaEventDestroy(start);
     if (own_stream && stream) cudaStreamDestroy(stream);
@@ -3526,6 +3529,7 @@ struct falcon_server {
   int next_stream = 0;
   int active = 0;
   ~falcon_server() {
+    for (cudaStream_t q : streams) cudaStreamSynchronize(q);
     groups.clear();
     for (cudaStream_t q : streams) cudaStreamDestroy(q);
   }
