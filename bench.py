@@ -383,7 +383,7 @@ def gpu_warmup(args):
 # groups take the tcgen05 kernel in gemm mode 2, the mma.sync one in mode 1)
 def kernel_of_class(c, gemm_mode):
     if c in ("gemm_radial", "gemm_mode_solve"):
-        return "tc_gemm_kernel" if gemm_mode == 2 else "oz_mma_kernel"
+        return "tc_gemm_kernel" if gemm_mode >= 2 else "oz_mma_kernel"
     return {"nonlin_fft": "nonlin_kernel", "elementwise": "elementwise kernels"}.get(c, c)
 
 
@@ -605,8 +605,12 @@ def run_gpu(args):
         "cpu_baseline": cpu,
         "clocks": clk.summary(),
         "gpu_launches": launches,
-        "gemm_mode": {2: "tcgen05 (tensor memory accumulators) for contractions that fill the GPU, mma.sync below",
+        "gemm_mode": {4: "autotuned: per contraction shape the fastest measured of FP64 FMA, mma.sync slices and "
+                         "tcgen05 slices (tensor memory accumulators), measured at the first warm-up step",
+                      3: "tcgen05 for every sliced contraction",
+                      2: "fixed rules: tcgen05 for contractions that fill the GPU, mma.sync below, FMA under 16 columns",
                       1: "mma.sync", 0: "FP64 FMA"}[args.gemm_mode],
+        "tuned_shapes": fg.tune_entries()[0],
         "state_finite": bool(finite),
         # last, so that a reader of the line's tail sees the target ratio
         "one_at_a_time": {"value": one_rate, "unit": "instance-steps/s", "instances": n1, "steps": k1},
@@ -630,8 +634,9 @@ def main():
     ap.add_argument("--no-mixed", dest="no_mixed", action="store_true", help="skip the uneven batch and serving")
     ap.add_argument("--single-steps", dest="single_steps", type=int, default=200)
     ap.add_argument("--plain-steps", dest="plain_steps", type=int, default=500)
-    ap.add_argument("--gemm-mode", dest="gemm_mode", type=int, default=2, choices=[0, 1, 2],
-                    help="operator contractions: 2 tcgen05 (mma.sync for small ones), 1 mma.sync slices, 0 FP64 FMA")
+    ap.add_argument("--gemm-mode", dest="gemm_mode", type=int, default=4, choices=[0, 1, 2, 3, 4],
+                    help="operator contractions: 4 autotuned per shape (FMA / mma.sync / tcgen05), 3 tcgen05, "
+                         "2 fixed rules, 1 mma.sync slices, 0 FP64 FMA")
     ap.add_argument("--uneven-instances", dest="uneven_instances", type=int, default=512)
     ap.add_argument("--uneven-steps", dest="uneven_steps", type=int, default=500)
     ap.add_argument("--serve-rate", dest="serve_rate", type=float, default=50.0)

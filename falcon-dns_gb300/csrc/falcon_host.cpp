@@ -231,11 +231,12 @@ struct OpSet {
   }
 };
 
-// Contractions through the tensor-core slices, on the tcgen05 kernel where
-// a contraction fills the GPU and on the mma.sync kernels otherwise (2,
-// default), on the mma.sync kernels only (1), or as FP64 FMA tiles (0).
-// The two sliced paths give the same bits; all are FP64-accurate.
-std::atomic<int> g_gemm_mode{2};
+// Contraction paths (the modes of gemm() below): 4 (default) measured per
+// shape by the autotuner; 3 tcgen05 wherever possible; 2 tcgen05 where a
+// contraction fills the GPU, mma.sync otherwise; 1 mma.sync only; 0 FP64
+// FMA tiles.  The two sliced kernels give the same bits; all paths are
+// FP64-accurate.
+std::atomic<int> g_gemm_mode{4};
 
 // Slices of one column-major operator array (rows x K, lda = rows, nb
 // entries of stride sA) for the tensor-core GEMM.
@@ -907,9 +908,14 @@ struct Group {
   std::vector<double> spec_host, ubal_host;
   double cur_dt() const { return vardt ? dt_new : p.dt; }
 
+  // The next step runs uncaptured (its contraction shapes may be new to
+  // the autotuner, which measures only outside capture): set when the
+  // captured steps are dropped.
+  bool direct_next = false;
   void drop_graphs() {
     for (auto& sg : graphs) cudaGraphExecDestroy(sg.exec);
     graphs.clear();
+    direct_next = true;
   }
   ~Group() {
     // work queued on the stream may still read or write the arrays
@@ -1186,55 +1192,250 @@ TcArgs tc_args(const GemmArgs& q) {
   return t;
 }
 
-// reuse: the call follows a contraction with the same X operand, unchanged
-// since (the blocks of one operator applied to one right-hand side); its
-// slice planes are reused when they match.
-int gemm(Group* g, int cls, const GemmArgs& q0, bool reuse = false) {
-  GemmArgs q = q0;
-  q.oz_s = nullptr;
-  q.oz_xs = nullptr;
-  // Contractions with at least 16 columns per batch entry take the tensor
-  // cores; narrower ones (the per-mode solves of groups of up to 7
-  // instances) stay on the FP64 FMA path, where the operator's FP64 bytes
-  // (fewer than its slices) bound the time.  Radial contractions cover all
-  // modes and always take the slices.
-  bool ok = false;
-  if (g_gemm_mode.load() && g->oz_xs && q.N >= 16) {
-    ok = attach_oz(g->ops.get(), &q);
-    for (int st = 0; !ok && st < kMaxStages; ++st) ok = attach_oz(g->stage_ops[st].get(), &q);
+// ---------------------------------------------------------------------------
+// Contraction paths and their autotuner.  A contraction with an attached
+// slice view can run as FP64 FMA tiles (PATH_FMA), on the mma.sync slice
+// kernel (PATH_MMA; X sliced in the kernel, or into slice planes first) or on
+// the tcgen05 kernel (PATH_TC).  PATH_MMA and PATH_TC give the same bits;
+// PATH_FMA differs from them by rounding (all are FP64-accurate).
+// ---------------------------------------------------------------------------
+enum { PATH_FMA = 0, PATH_MMA = 1, PATH_TC = 2, PATH_COUNT = 3 };
+
+// Slice planes of q.X for the mma.sync kernel when it does not slice X
+// itself (made unless `reuse` finds them already made for the same X).
+// false: they do not fit the group's scratch (the FMA tiles then run).
+int mma_planes(Group* g, GemmArgs* q, bool reuse, bool* fits) {
+  *fits = true;
+  if (oz_fused_x(q->rows, q->N, q->batch)) return 0;
+  const int KP = q->oz_KP, Np = (int)(((long)q->N + 31) / 32 * 32);
+  if ((size_t)oz_slices(q->oz_w) * KP * Np * q->batch > g->oz_xs_cap || (size_t)Np * q->batch > g->oz_cexp_cap) {
+    *fits = false;
+    return 0;
   }
-  if (ok && g_gemm_mode.load() == 2 && q.oz_tmap && tc_worth_it(q)) {
-    // tcgen05: the kernel slices its own X columns
+  auto& k = g->oz_key;
+  const bool same = reuse && k.valid && k.X == q->X && k.ldx == q->ldx && k.sX == q->sX && k.K == q->K &&
+                    k.N == q->N && k.batch == q->batch && k.w == q->oz_w;
+  if (!same) {
+    int rc = launch(g, KC_ELEMENTWISE, 0.0, [&]() {
+      return launch_oz_slice_cols(q->X, q->ldx, q->sX, q->K, q->N, q->batch, g->oz_xs, g->oz_cexp, KP, Np, q->oz_w,
+                                  g->stream);
+    });
+    if (rc) return rc;
+    k.X = q->X; k.ldx = q->ldx; k.sX = q->sX; k.K = q->K; k.N = q->N; k.batch = q->batch; k.w = q->oz_w;
+    k.valid = true;
+  }
+  q->oz_xs = g->oz_xs;
+  q->oz_cexp = g->oz_cexp;
+  q->oz_Np = Np;
+  return 0;
+}
+
+// One contraction on the given path (q carries its slice view for MMA/TC).
+int run_path(Group* g, int cls, GemmArgs q, int path, bool reuse) {
+  if (path == PATH_TC) {
     const TcArgs t = tc_args(q);
     const CUtensorMap* map = static_cast<const CUtensorMap*>(q.oz_tmap);
     return launch(g, cls, gemm_flops(q), [&]() { return launch_tc_gemm(t, *map, g->stream); });
   }
-  if (ok && oz_fused_x(q.rows, q.N, q.batch)) {
-    // the kernel slices its own X columns
-  } else if (ok) {
-    const int KP = q.oz_KP, Np = (int)(((long)q.N + 31) / 32 * 32);
-    if ((size_t)oz_slices(q.oz_w) * KP * Np * q.batch > g->oz_xs_cap || (size_t)Np * q.batch > g->oz_cexp_cap) {
-      ok = false;  // beyond the scratch sized for this group: FMA tiles
-      q.oz_s = nullptr;
-    } else {
-      auto& k = g->oz_key;
-      const bool same = reuse && k.valid && k.X == q.X && k.ldx == q.ldx && k.sX == q.sX && k.K == q.K &&
-                        k.N == q.N && k.batch == q.batch && k.w == q.oz_w;
-      if (!same) {
-        int rc = launch(g, KC_ELEMENTWISE, 0.0, [&]() {
-          return launch_oz_slice_cols(q.X, q.ldx, q.sX, q.K, q.N, q.batch, g->oz_xs, g->oz_cexp, KP, Np, q.oz_w,
-                                      g->stream);
-        });
-        if (rc) return rc;
-        k.X = q.X; k.ldx = q.ldx; k.sX = q.sX; k.K = q.K; k.N = q.N; k.batch = q.batch; k.w = q.oz_w;
-        k.valid = true;
-      }
-      q.oz_xs = g->oz_xs;
-      q.oz_cexp = g->oz_cexp;
-      q.oz_Np = Np;
-    }
+  if (path == PATH_MMA) {
+    bool fits = true;
+    int rc = mma_planes(g, &q, reuse, &fits);
+    if (rc) return rc;
+    if (!fits) path = PATH_FMA;
+  }
+  if (path == PATH_FMA) {
+    q.oz_s = nullptr;
+    q.oz_xs = nullptr;
   }
   return launch(g, cls, gemm_flops(q), [&]() { return launch_gemm(q, g->stream); });
+}
+
+// The autotuner's decisions, per device and contraction shape: the path
+// measured fastest the first time the shape ran (outside graph capture),
+// kept for the process and, with a cache file, across processes.  Cache file
+// (text): a header line "falcon-contraction-tuning 1", then one decision per
+// line:
+//   <device> <rows> <K> <N> <batch> <w> <per_mode> <reuse> <path> <us_fma> <us_mma> <us_tc>
+// device = the CUDA device name with blanks as '_' and "_sm<SM count>";
+// per_mode = 1 when the batch entries have their own X (sX != 0); reuse = 1
+// when X's slice planes were made by the contraction before; w = the slice
+// format (6 or 7); path 0 FMA, 1 mma.sync, 2 tcgen05; the times are the
+// measured microseconds per contraction (-1: candidate not available).
+struct TuneKey {
+  std::string dev;
+  int rows, K, N, batch, w, per_mode, reuse;
+  bool operator<(const TuneKey& o) const {
+    return std::tie(dev, rows, K, N, batch, w, per_mode, reuse) <
+           std::tie(o.dev, o.rows, o.K, o.N, o.batch, o.w, o.per_mode, o.reuse);
+  }
+};
+struct TuneEntry { int path; float us[PATH_COUNT]; };
+std::mutex g_tune_mu;
+std::map<TuneKey, TuneEntry> g_tune;
+std::string g_tune_path;          // cache file ("" none)
+bool g_tune_env_checked = false;
+std::atomic<long long> g_tune_measured(0);
+constexpr const char* kTuneHeader = "falcon-contraction-tuning 1";
+
+int tune_load_locked(const std::string& path) {
+  std::ifstream f(path);
+  if (!f) return 0;  // no file yet: it is created with the first decision
+  std::string line;
+  if (!std::getline(f, line) || line != kTuneHeader)
+    return fail(FALCON_EINVAL, "tuning cache " + path + ": not a falcon contraction tuning file (header)");
+  int n = 0;
+  while (std::getline(f, line)) {
+    if (line.empty() || line[0] == '#') continue;
+    std::istringstream is(line);
+    TuneKey k;
+    TuneEntry e;
+    if (!(is >> k.dev >> k.rows >> k.K >> k.N >> k.batch >> k.w >> k.per_mode >> k.reuse >> e.path >> e.us[0] >>
+          e.us[1] >> e.us[2]) ||
+        e.path < 0 || e.path >= PATH_COUNT || k.rows <= 0 || k.K <= 0 || k.N <= 0 || k.batch <= 0)
+      return fail(FALCON_EINVAL, "tuning cache " + path + ": malformed line " + std::to_string(n + 2));
+    g_tune[k] = e;
+    ++n;
+  }
+  return 0;
+}
+
+void tune_store_locked(const TuneKey& k, const TuneEntry& e) {
+  if (g_tune_path.empty()) return;
+  std::FILE* f = std::fopen(g_tune_path.c_str(), "a+");
+  if (!f) return;
+  std::fseek(f, 0, SEEK_END);
+  if (std::ftell(f) == 0) std::fprintf(f, "%s\n", kTuneHeader);
+  std::fprintf(f, "%s %d %d %d %d %d %d %d %d %.3f %.3f %.3f\n", k.dev.c_str(), k.rows, k.K, k.N, k.batch, k.w,
+               k.per_mode, k.reuse, e.path, e.us[0], e.us[1], e.us[2]);
+  std::fclose(f);
+}
+
+const std::string& device_tag() {
+  static std::mutex mu;
+  static std::map<int, std::string> tags;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lk(mu);
+  auto it = tags.find(dev);
+  if (it != tags.end()) return it->second;
+  cudaDeviceProp pr{};
+  std::string t = cudaGetDeviceProperties(&pr, dev) == cudaSuccess ? std::string(pr.name) : std::string("device");
+  for (auto& ch : t)
+    if (std::isspace((unsigned char)ch)) ch = '_';
+  t += "_sm" + std::to_string(pr.multiProcessorCount);
+  return tags[dev] = t;
+}
+
+bool spans_overlap(const double* a, long na, const double* b, long nb) {
+  const double *a1 = a + na, *b1 = b + nb;
+  return a < b1 && b < a1;
+}
+
+// Extent in doubles of an operand addressed as base[k*ld + n + z*sz].
+long operand_span(long ld, long sz, int K, int N, int batch) {
+  return (long)(K - 1) * ld + N + (long)(batch - 1) * sz;
+}
+
+// The path of a contraction under mode 4: the cached decision, or a
+// measurement of every available path (each run once to warm up, then three
+// times between CUDA events on the group's stream, the device otherwise
+// idle).  Shapes met inside graph capture or profiling, or whose output
+// overlaps X, are not measured: they take the fixed rule of mode 2.
+int tuned_path(Group* g, int cls, const GemmArgs& q, bool reuse, bool tc_ok, int fixed, int* path) {
+  *path = fixed;
+  TuneKey k{device_tag(), q.rows, q.K, q.N, q.batch, q.oz_w, q.sX != 0 ? 1 : 0, reuse ? 1 : 0};
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    if (!g_tune_env_checked) {
+      g_tune_env_checked = true;
+      const char* env = std::getenv("FALCON_TUNE_CACHE");
+      if (g_tune_path.empty() && env && *env) {
+        g_tune_path = env;
+        int rc = tune_load_locked(g_tune_path);
+        if (rc) return rc;
+      }
+    }
+    auto it = g_tune.find(k);
+    if (it != g_tune.end()) {
+      *path = it->second.path;
+      if (*path == PATH_TC && !tc_ok) *path = PATH_MMA;
+      return 0;
+    }
+  }
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  CK(cudaStreamIsCapturing(g->stream, &cs));
+  if (cs != cudaStreamCaptureStatusNone || g->prof) return 0;
+  const long xs = operand_span(q.ldx, q.sX, q.K, q.N, q.batch), ys = operand_span(q.ldy, q.sY, q.rows, q.N, q.batch);
+  if (spans_overlap(q.X, xs, q.Y, ys)) return 0;
+  TuneEntry e{};
+  CK(cudaDeviceSynchronize());
+  cudaEvent_t a = nullptr, b = nullptr;
+  CK(cudaEventCreate(&a));
+  CK(cudaEventCreate(&b));
+  float best = 0.f;
+  int rc = 0;
+  for (int p = 0; p < PATH_COUNT && !rc; ++p) {
+    e.us[p] = -1.f;
+    if (p == PATH_TC && !tc_ok) continue;
+    if ((rc = run_path(g, cls, q, p, reuse))) break;
+    if ((rc = cudaEventRecord(a, g->stream) == cudaSuccess ? 0 : fail(FALCON_ECUDA, "tuning event"))) break;
+    for (int r = 0; r < 3 && !rc; ++r) rc = run_path(g, cls, q, p, reuse);
+    if (rc) break;
+    float ms = 0.f;
+    if (cudaEventRecord(b, g->stream) != cudaSuccess || cudaEventSynchronize(b) != cudaSuccess ||
+        cudaEventElapsedTime(&ms, a, b) != cudaSuccess) {
+      rc = fail(FALCON_ECUDA, "tuning timing");
+      break;
+    }
+    e.us[p] = ms * 1000.f / 3.f;
+    if (p == PATH_FMA || e.us[p] < best) {
+      best = e.us[p];
+      e.path = p;
+    }
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  if (rc) return rc;
+  g_tune_measured++;
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tune[k] = e;
+  tune_store_locked(k, e);
+  *path = e.path;
+  return 0;
+}
+
+// reuse: the call follows a contraction with the same X operand, unchanged
+// since (the blocks of one operator applied to one right-hand side); its
+// slice planes are reused when they match.
+//
+// Modes: 0 FP64 FMA tiles; 1 mma.sync for every contraction with a slice
+// view; 2 fixed rules: tcgen05 for contractions that fill the GPU (at least
+// two 128 x 24 tiles per SM), mma.sync for the other ones of at least 16
+// columns per batch entry, FMA for narrower ones (the per-mode solves of
+// groups of up to 7 instances); 3 tcgen05 for every contraction with a
+// slice view (the same bits as 1); 4 (default) the measured fastest of FMA,
+// mma.sync and tcgen05 per shape.
+int gemm(Group* g, int cls, const GemmArgs& q0, bool reuse = false) {
+  GemmArgs q = q0;
+  q.oz_s = nullptr;
+  q.oz_xs = nullptr;
+  const int mode = g_gemm_mode.load();
+  bool ok = false;
+  if (mode && g->oz_xs && (q.N >= 16 || mode != 2)) {
+    ok = attach_oz(g->ops.get(), &q);
+    for (int st = 0; !ok && st < kMaxStages; ++st) ok = attach_oz(g->stage_ops[st].get(), &q);
+  }
+  if (!ok) return run_path(g, cls, q, PATH_FMA, reuse);
+  const bool tc_ok = mode >= 2 && q.oz_tmap != nullptr;
+  int path = PATH_MMA;
+  if (mode == 3 && tc_ok) path = PATH_TC;
+  if ((mode == 2 || mode == 4) && tc_ok && tc_worth_it(q)) path = PATH_TC;
+  if (mode == 4) {
+    const int fixed = q.N >= 16 ? path : PATH_FMA;
+    int rc = tuned_path(g, cls, q, reuse, tc_ok, fixed, &path);
+    if (rc) return rc;
+  }
+  return run_path(g, cls, q, path, reuse);
 }
 
 // Consecutive row blocks of one operator applied to one X, each written to
@@ -1245,7 +1446,8 @@ int gemm(Group* g, int cls, const GemmArgs& q0, bool reuse = false) {
 // and the blocks run one after another as before).
 int gemm_blocks(Group* g, int cls, std::initializer_list<GemmArgs> blocks) {
   const std::vector<GemmArgs> v(blocks);
-  if (g_gemm_mode.load() == 2 && g->oz_xs && !v.empty() && v.size() <= 4 && v[0].N >= 16) {
+  const int mode = g_gemm_mode.load();
+  if (mode >= 2 && g->oz_xs && !v.empty() && v.size() <= 4 && (v[0].N >= 16 || mode != 2)) {
     const GemmArgs& f = v[0];
     const char* x0 = reinterpret_cast<const char*>(f.X);
     const char* x1 = reinterpret_cast<const char*>(f.X + (size_t)(f.batch - 1) * f.sX + (size_t)f.K * f.ldx);
@@ -1266,7 +1468,7 @@ int gemm_blocks(Group* g, int cls, std::initializer_list<GemmArgs> blocks) {
       all.oz_xs = nullptr;
       bool ok = attach_oz(g->ops.get(), &all);
       for (int st = 0; !ok && st < kMaxStages; ++st) ok = attach_oz(g->stage_ops[st].get(), &all);
-      if (ok && all.oz_tmap && tc_worth_it(all)) {
+      if (ok && all.oz_tmap && (mode == 3 || tc_worth_it(all))) {
         TcArgs t = tc_args(all);
         t.nout = (int)v.size();
         int r = 0;
@@ -1734,7 +1936,10 @@ int group_step(Group* g) {
   // the IMEXRK and RK loops keep it
   if (g->n_step == 0 || g->restart_first)
     CK(launch_extract_mode0(g->R, g->M, g->B, g->up, g->up0_prev, g->stream));
-  if (!g_graphs.load() || g->prof || g->n_step < 1 || g->vardt) return group_step_direct(g);
+  if (!g_graphs.load() || g->prof || g->n_step < 1 || g->vardt || g->direct_next) {
+    g->direct_next = false;
+    return group_step_direct(g);
+  }
   const int phase = g->head * 8 + g->head_e;
   for (auto& sg : g->graphs)
     if (sg.phase == phase) {
@@ -3827,7 +4032,40 @@ extern "C" {
 long long falcon_launch_count(void) { return g_launches.load(); }
 
 int falcon_set_step_graphs(int enable) { return g_graphs.exchange(enable ? 1 : 0); }
-int falcon_set_gemm_mode(int mode) { return g_gemm_mode.exchange(mode < 0 || mode > 2 ? 1 : mode); }
+int falcon_set_gemm_mode(int mode) { return g_gemm_mode.exchange(mode < 0 || mode > 4 ? 4 : mode); }
+
+int falcon_set_tune_cache(const char* path) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tune_env_checked = true;
+  g_tune_path = path ? path : "";
+  return g_tune_path.empty() ? 0 : tune_load_locked(g_tune_path);
+}
+
+int falcon_tune_clear(void) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  const int n = (int)g_tune.size();
+  g_tune.clear();
+  return n;
+}
+
+int falcon_tune_entries(long long* measured) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  if (measured) *measured = g_tune_measured.load();
+  return (int)g_tune.size();
+}
+
+int falcon_tune_lookup(const char* device, int rows, int K, int N, int batch, int w, int per_mode, int reuse,
+                       float* us) {
+  if (!device) return fail(FALCON_EINVAL, "null device");
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  auto it = g_tune.find(TuneKey{device, rows, K, N, batch, w, per_mode, reuse});
+  if (it == g_tune.end()) return -1;
+  if (us)
+    for (int p = 0; p < PATH_COUNT; ++p) us[p] = it->second.us[p];
+  return it->second.path;
+}
+
+const char* falcon_device_tag(void) { return device_tag().c_str(); }
 
 int falcon_batch_profile(falcon_batch* b, int nsteps, falcon_kernel_stat* stats, int max_stats, int* nstats) {
   if (!b || nsteps <= 0 || !stats || !nstats) return fail(FALCON_EINVAL, "invalid profile arguments");

@@ -105,7 +105,8 @@ EXPORTS = (
     "falcon_batch_store_snapshot", "falcon_restart", "falcon_batch_restart", "falcon_set_gemm_mode",
     "falcon_upload_factors", "falcon_cheb_d1d2_dev", "falcon_spectra", "falcon_upbalance",
     "falcon_batch_spectra", "falcon_batch_upbalance", "falcon_time", "falcon_server_submit_state",
-    "falcon_server_result", "falcon_server_steps",
+    "falcon_server_result", "falcon_server_steps", "falcon_set_tune_cache", "falcon_tune_entries",
+    "falcon_tune_clear", "falcon_tune_lookup", "falcon_device_tag",
 )
 
 
@@ -182,6 +183,11 @@ def lib():
     L.falcon_batch_spectra.argtypes = [vp, ip, dp, dp]
     L.falcon_batch_upbalance.argtypes = [vp, ip, dp]
     L.falcon_batch_restart.argtypes = [vp, P(ctypes.c_char_p)]
+    L.falcon_set_gemm_mode.argtypes = [ip]
+    L.falcon_set_tune_cache.argtypes = [ctypes.c_char_p]
+    L.falcon_tune_entries.argtypes = [P(ctypes.c_longlong)]
+    L.falcon_tune_lookup.argtypes = [ctypes.c_char_p, ip, ip, ip, ip, ip, ip, ip, P(ctypes.c_float)]
+    L.falcon_device_tag.restype = ctypes.c_char_p
     _lib = L
     return L
 
@@ -503,11 +509,49 @@ def set_max_group_size(n):
 
 
 def set_gemm_mode(mode):
-    """Operator contractions: 2 on the tcgen05 tensor cores by exact slicing
-    (accumulators in tensor memory), 1 on the mma.sync tensor-core path with
-    the same slices, 0 as FP64 FMA tiles.  Returns the previous mode."""
-    lib().falcon_set_gemm_mode.argtypes = [ctypes.c_int]
+    """Operator contraction paths: 4 (default) the fastest measured per shape
+    (autotuned, see set_tune_cache); 3 tcgen05 for every sliced contraction;
+    2 fixed rules (tcgen05 where a contraction fills the GPU, mma.sync for
+    other ones of >= 16 columns, FMA below); 1 mma.sync for every sliced
+    contraction (the same bits as 3); 0 FP64 FMA tiles.  Returns the
+    previous mode."""
     return lib().falcon_set_gemm_mode(int(mode))
+
+
+PATHS = ("fma", "mma_sync", "tcgen05")
+
+
+def set_tune_cache(path):
+    """Read the autotuner's decisions from `path` and append new ones to it
+    (None detaches the file)."""
+    check(lib().falcon_set_tune_cache(os.fsencode(str(path)) if path else None))
+
+
+def tune_entries():
+    """(decisions held, decisions this process measured)."""
+    m = ctypes.c_longlong()
+    n = lib().falcon_tune_entries(ctypes.byref(m))
+    return n, m.value
+
+
+def tune_clear():
+    """Forget the decisions held in memory; returns their number."""
+    return lib().falcon_tune_clear()
+
+
+def tune_lookup(device, rows, K, N, batch, w, per_mode, reuse):
+    """The decision for one contraction shape: (path name, {path: microseconds})
+    or None."""
+    us = (ctypes.c_float * 3)()
+    p = lib().falcon_tune_lookup(device.encode(), rows, K, N, batch, w, per_mode, reuse, us)
+    if p < 0:
+        return None
+    return PATHS[p], {PATHS[i]: float(us[i]) for i in range(3) if us[i] >= 0}
+
+
+def device_tag():
+    """Device key of the tuning cache for the current device."""
+    return lib().falcon_device_tag().decode()
 
 
 def set_step_graphs(enable):

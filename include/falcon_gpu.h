@@ -365,18 +365,56 @@ long long falcon_launch_count(void);
  * No reference counterpart (launch mechanics of the GPU step). */
 int falcon_set_step_graphs(int enable);
 /* Operator contractions (the radial derivative / Laplacian and per-mode
- * solve products): mode 2 (the default) on the bf16 tensor cores by exact
- * integer slicing of the FP64 operands, with the 5th-generation tcgen05
- * MMA (accumulators in tensor memory) for contractions that fill the GPU
- * and warp-level mma.sync for smaller ones; mode 1 the same slices on
- * mma.sync only (the same bits as mode 2); mode 0 as FP64 FMA tiles.  All
- * give FP64-accurate results (the slices: error of the order of K 2^-56
- * max|A_row| max|X_col|); the sliced forms are several times faster on
- * GB300, whose FP64 pipe is ~500x slower than its bf16 tensor cores.
+ * solve products) run on one of three paths: FP64 FMA tiles; the bf16
+ * tensor cores by exact integer slicing of the FP64 operands on warp-level
+ * mma.sync; the same slices on the 5th-generation tcgen05 MMA with
+ * accumulators in tensor memory.  The two sliced paths give the same bits;
+ * all give FP64-accurate results (the slices: error of the order of
+ * K 2^-56 max|A_row| max|X_col|), and the sliced ones are several times
+ * faster on GB300, whose FP64 pipe is ~500x slower than its bf16 tensor
+ * cores.  Modes:
+ *   4 (default) autotuned: the first time a contraction shape runs outside
+ *     graph capture, every available path is timed on it (the device
+ *     otherwise idle) and the fastest is kept for that shape (see
+ *     falcon_set_tune_cache);
+ *   3 tcgen05 for every contraction with a slice view of its operator
+ *     (mma.sync where that view has no tensor map): the same bits as 1;
+ *   2 fixed rules: tcgen05 for contractions of at least two 128 x 24 tiles
+ *     per SM, mma.sync for the other ones of at least 16 columns per batch
+ *     entry, FMA for narrower ones;
+ *   1 mma.sync for every contraction with a slice view;
+ *   0 FMA only.
  * Applies to launches after the call (step graphs already captured keep
- * their mode).  Returns the previous mode.  No counterpart in the
- * reference, which uses LAPACK dgetrs (src/algebra_lapack.F90). */
+ * their paths).  Returns the previous mode; an unknown mode selects 4.
+ * No counterpart in the reference, which uses LAPACK dgetrs
+ * (src/algebra_lapack.F90). */
 int falcon_set_gemm_mode(int mode);
+/* Contraction tuning cache of mode 4: decisions are read from `path` (if it
+ * exists) and every new decision is appended to it, so that later processes
+ * take the same paths without measuring.  Text format: the header line
+ * "falcon-contraction-tuning 1", then one line per decision
+ *   <device> <rows> <K> <N> <batch> <w> <per_mode> <reuse> <path> <us_fma> <us_mma> <us_tc>
+ * device = CUDA device name with blanks as '_' plus "_sm<SM count>"
+ * (falcon_device_tag); rows, K, N, batch = the contraction's shape (rows x K
+ * operator, N columns per batch entry); w = slice format in bits (6 or 7);
+ * per_mode = 1 when every batch entry has its own columns; reuse = 1 when
+ * the X slice planes were made by the contraction before; path 0 FMA,
+ * 1 mma.sync, 2 tcgen05; us_* = measured microseconds per contraction (-1:
+ * path not available).  NULL or "" detaches the file (decisions stay in
+ * memory).  The environment variable FALCON_TUNE_CACHE names a file when
+ * this is not called.  Returns FALCON_EINVAL for a file with another
+ * header or a malformed line. */
+int falcon_set_tune_cache(const char* path);
+/* Decisions held (and, in *measured, how many this process measured). */
+int falcon_tune_entries(long long* measured);
+/* Forget every decision held in memory (the file is kept); returns their number. */
+int falcon_tune_clear(void);
+/* The decision for one shape (path 0-2, -1 if none), with the measured times
+ * (3 floats, may be NULL). */
+int falcon_tune_lookup(const char* device, int rows, int K, int N, int batch, int w, int per_mode, int reuse,
+                       float* us);
+/* The device key of the tuning cache for the current device. */
+const char* falcon_device_tag(void);
 
 /* ---- misc ---- */
 const char* falcon_last_error(void);

@@ -88,10 +88,11 @@ def test_no_cpu_fallback_without_gpu(fg):
 
 
 def test_process_wide_switches_round_trip(fg):
-    # defaults: sliced tensor-core contractions (tcgen05 where they fill the
-    # GPU), step graphs, groups of <= 128
+    # defaults: autotuned contraction paths, step graphs, groups of <= 128
     L = fg.lib()
-    assert fg.set_gemm_mode(0) == 2 and fg.set_gemm_mode(1) == 0 and fg.set_gemm_mode(2) == 1
+    assert fg.set_gemm_mode(0) == 4 and fg.set_gemm_mode(1) == 0 and fg.set_gemm_mode(2) == 1
+    assert fg.set_gemm_mode(3) == 2 and fg.set_gemm_mode(9) == 3   # unknown: autotuned
+    assert fg.set_gemm_mode(4) == 4
     assert fg.set_max_group_size(64) == 128
     assert fg.set_max_group_size(-5) == 64      # negative means one group per key
     assert fg.set_max_group_size(128) == 0

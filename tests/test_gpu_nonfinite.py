@@ -9,7 +9,7 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("gemm_mode", [1, 0])
+@pytest.mark.parametrize("gemm_mode", [1, 3, 0])
 def test_nonfinite_instance_is_reported_and_isolated(fg, gemm_mode):
     n, bad = 20, 7
     prev = fg.set_gemm_mode(gemm_mode)
