@@ -849,6 +849,18 @@ struct Group {
   std::unique_ptr<FftTables> fft;
   std::vector<int> members;    // batch indices
   std::vector<double> ra_pr_h; // per instance Ra/Pr
+  std::vector<double> pr_h;    // per instance Pr
+  // Pr enters only the temperature operator (AT, src/mat_assembly.F90), so
+  // instances of one grid, dt and scheme that differ in Pr step together:
+  // each run of equal Pr (a "sub", instance columns [b0, b1)) has its own
+  // temperature solve, and every other kernel covers all of them.  Sub 0
+  // takes its operators from ops / stage_ops; subs[k].ops for k >= 1.
+  struct Sub {
+    int b0 = 0, b1 = 0;
+    std::shared_ptr<OpSet> ops;
+    std::shared_ptr<OpSet> stage_ops[kMaxStages];
+  };
+  std::vector<Sub> subs;
   cudaStream_t stream = nullptr;
   // device state
   std::vector<void*> allocs;
@@ -860,6 +872,7 @@ struct Group {
   double* ub = nullptr;        // 2R x 2B doubles (alias of ub2)
   double2* ub2 = nullptr;
   double* ra_pr = nullptr;
+  double* inv_pr = nullptr;    // [b] 1/Pr
   double2 *fat[kMaxStages] = {}, *fdt[kMaxStages] = {}, *faw[kMaxStages] = {}, *fdw[kMaxStages] = {},
           *buo[kMaxStages] = {};
   double2 *t0 = nullptr, *w0 = nullptr;
@@ -1005,17 +1018,55 @@ int oz_scratch_init(Group* g) {
 // built with the weight butcher_aD(rk_stage,rk_stage) at time step dt.
 // Stages with equal diagonals share one set through the operator cache;
 // LAPpsi comes from the main set.
-int build_stage_ops(Group* g, double dt) {
+int build_stage_ops_for(const Group* g, double pr, double dt, std::shared_ptr<OpSet> (&out)[kMaxStages]) {
   const Scheme& sc = g->sch;
-  for (auto& so : g->stage_ops) so.reset();
+  for (auto& so : out) so.reset();
   if (g->p.scheme_type != FALCON_IMEXRK || !sc.diag_diff) return 0;
   for (int st = 1; st < sc.n_exp; ++st) {
     if (sc.aD[st][st] == sc.aD[sc.diag][sc.diag]) continue;
     OpKey k = key_of(g->p, sc);
-    k.dt = dt; k.wt = sc.aD[st][st]; k.needs_lap = 0; k.lagpts = 0;
-    const int rc = build_opset(k, &g->stage_ops[st]);
+    k.pr = pr; k.dt = dt; k.wt = sc.aD[st][st]; k.needs_lap = 0; k.lagpts = 0;
+    const int rc = build_opset(k, &out[st]);
     if (rc) return rc;
   }
+  return 0;
+}
+
+int build_stage_ops(Group* g, double dt) {
+  int rc = build_stage_ops_for(g, g->p.pr, dt, g->stage_ops);
+  for (size_t k = 1; k < g->subs.size() && !rc; ++k)
+    rc = build_stage_ops_for(g, g->pr_h[g->subs[k].b0], dt, g->subs[k].stage_ops);
+  return rc;
+}
+
+// Operators of sub k (stage st of an IMEXRK step with stage-dependent
+// diagonal, or -1): its temperature solve; the Pr-free operators of sub 0
+// serve every sub.
+const OpSet* sub_ops(const Group* g, int k, int st) {
+  if (k == 0) return (st >= 0 && g->stage_ops[st]) ? g->stage_ops[st].get() : g->ops.get();
+  const Group::Sub& u = g->subs[k];
+  return (st >= 0 && u.stage_ops[st]) ? u.stage_ops[st].get() : u.ops.get();
+}
+
+// Subs of a group from its instances' Pr (runs of equal Pr).
+void make_subs(Group* g) {
+  g->subs.clear();
+  for (int b = 0; b < g->B; ++b)
+    if (b == 0 || g->pr_h[b] != g->pr_h[b - 1]) {
+      if (!g->subs.empty()) g->subs.back().b1 = b;
+      g->subs.push_back(Group::Sub{});
+      g->subs.back().b0 = b;
+    }
+  if (!g->subs.empty()) g->subs.back().b1 = g->B;
+}
+
+// Per-instance Ra/Pr and 1/Pr of the group's columns, uploaded.
+int upload_instance_params(Group* g) {
+  const int B = g->B;
+  std::vector<double> ip(B);
+  for (int b = 0; b < B; ++b) ip[b] = 1.0 / g->pr_h[b];
+  CK(cudaMemcpy(g->ra_pr, g->ra_pr_h.data(), sizeof(double) * B, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(g->inv_pr, ip.data(), sizeof(double) * B, cudaMemcpyHostToDevice));
   return 0;
 }
 
@@ -1026,8 +1077,17 @@ int group_init(Group* g, const std::vector<falcon_params>& ps, const std::vector
   g->B = (int)members.size();
   if (scheme_weights(g->p.scheme_type, g->p.scheme_imp, g->p.scheme_exp, &g->sch) != 0)
     return fail(FALCON_EINVAL, "unsupported scheme");
+  g->ra_pr_h.resize(g->B);
+  g->pr_h.resize(g->B);
+  for (int i = 0; i < g->B; ++i) {
+    g->ra_pr_h[i] = ps[members[i]].ra / ps[members[i]].pr;
+    g->pr_h[i] = ps[members[i]].pr;
+  }
+  make_subs(g);
   int rc;
   if ((rc = build_opset(key_of(g->p, g->sch), &g->ops))) return rc;
+  for (size_t k = 1; k < g->subs.size(); ++k)
+    if ((rc = build_opset(key_of(ps[members[g->subs[k].b0]], g->sch), &g->subs[k].ops))) return rc;
   if ((rc = build_stage_ops(g, g->p.dt))) return rc;
   if ((rc = make_fft(g->P, &g->fft))) return rc;
   if ((rc = oz_scratch_init(g))) return rc;
@@ -1071,6 +1131,7 @@ int group_init(Group* g, const std::vector<falcon_params>& ps, const std::vector
       (rc = g->alloc(&g->lt, n)) || (rc = g->alloc(&g->lw, n)) || (rc = g->alloc(&g->lu0, (size_t)R * B)) ||
       (rc = g->alloc(&g->rhs_t, n)) || (rc = g->alloc(&g->rhs_w, n)) ||
       (rc = g->alloc(&g->ub2, (size_t)2 * R * B)) || (rc = g->alloc(&g->ra_pr, (size_t)B)) ||
+      (rc = g->alloc(&g->inv_pr, (size_t)B)) ||
       (rc = g->alloc(&g->diag_dev, (size_t)8 * B)) || (rc = g->alloc(&g->diag_part, (size_t)8 * R * B)) ||
       (rc = g->alloc(&g->up0_prev, (size_t)R * B)) || (rc = g->alloc(&g->spec_dev, (size_t)2 * g->M * B)) ||
       (rc = g->alloc(&g->ubal_dev, (size_t)3 * R * B)))
@@ -1087,9 +1148,7 @@ int group_init(Group* g, const std::vector<falcon_params>& ps, const std::vector
     for (int i = 0; i < 4; ++i) g->dt_array[i] = g->p.dt;
     g->dt_new = g->p.dt;
   }
-  g->ra_pr_h.resize(B);
-  for (int i = 0; i < B; ++i) g->ra_pr_h[i] = ps[members[i]].ra / ps[members[i]].pr;
-  CK(cudaMemcpy(g->ra_pr, g->ra_pr_h.data(), sizeof(double) * B, cudaMemcpyHostToDevice));
+  if ((rc = upload_instance_params(g))) return rc;
   CK(cudaMallocHost(&g->stage_buf, sizeof(double2) * (size_t)g->M * R * 2));
   return 0;
 }
@@ -1159,6 +1218,20 @@ bool attach_oz(const OpSet* o, GemmArgs* q) {
     q->oz_tmap = z.tmap_ok ? &z.tmap : nullptr;
     q->oz_z0 = (int)z0;
     return true;
+  }
+  return false;
+}
+
+// The slice view of q.A in any operator set of the group (its subs' and
+// their stages' included).
+bool attach_group(const Group* g, GemmArgs* q) {
+  for (size_t k = 0; k < std::max<size_t>(g->subs.size(), 1); ++k) {
+    if (k > 0 && attach_oz(g->subs[k].ops.get(), q)) return true;
+    if (k == 0 && attach_oz(g->ops.get(), q)) return true;
+    for (int st = 0; st < kMaxStages; ++st) {
+      const OpSet* o = k == 0 ? g->stage_ops[st].get() : g->subs[k].stage_ops[st].get();
+      if (attach_oz(o, q)) return true;
+    }
   }
   return false;
 }
@@ -1421,10 +1494,7 @@ int gemm(Group* g, int cls, const GemmArgs& q0, bool reuse = false) {
   q.oz_xs = nullptr;
   const int mode = g_gemm_mode.load();
   bool ok = false;
-  if (mode && g->oz_xs && (q.N >= 16 || mode != 2)) {
-    ok = attach_oz(g->ops.get(), &q);
-    for (int st = 0; !ok && st < kMaxStages; ++st) ok = attach_oz(g->stage_ops[st].get(), &q);
-  }
+  if (mode && g->oz_xs && (q.N >= 16 || mode != 2)) ok = attach_group(g, &q);
   if (!ok) return run_path(g, cls, q, PATH_FMA, reuse);
   const bool tc_ok = mode >= 2 && q.oz_tmap != nullptr;
   int path = PATH_MMA;
@@ -1466,8 +1536,7 @@ int gemm_blocks(Group* g, int cls, std::initializer_list<GemmArgs> blocks) {
       all.rows = rows;
       all.oz_s = nullptr;
       all.oz_xs = nullptr;
-      bool ok = attach_oz(g->ops.get(), &all);
-      for (int st = 0; !ok && st < kMaxStages; ++st) ok = attach_oz(g->stage_ops[st].get(), &all);
+      const bool ok = attach_group(g, &all);
       if (ok && all.oz_tmap && (mode == 3 || tc_worth_it(all))) {
         TcArgs t = tc_args(all);
         t.nout = (int)v.size();
@@ -1507,13 +1576,21 @@ int run_nonlin(Group* g) {
 
 // The implicit solves shared by IMEX and IMEXRK: temperature, then
 // buoyancy, then (omega, psi, u_phi) for m >= 1 and uphi_bar for m = 0.
+// st: the IMEXRK stage whose own implicit diagonal the operators take (-1:
+// the scheme's diagonal).  The temperature solve runs once per sub (its Pr),
+// the rest once for all instances.
 int solve_all(Group* g, double2* t_out, double2* w_out, double buo_scale, double2* buo_store,
-              double* ubar_store, const OpSet* o = nullptr) {
+              double* ubar_store, int st = -1) {
   const int R = g->R, M = g->M, B = g->B;
-  if (!o) o = g->ops.get();
+  const OpSet* o = sub_ops(g, 0, st);
   cudaStream_t s = g->stream;
   int rc;
-  if ((rc = gemm(g, KC_GEMM_MODE, per_mode(o->ST, R, (long)R * R, g->rhs_t, t_out, R, M, B, 0, M, R)))) return rc;
+  for (size_t k = 0; k < g->subs.size(); ++k) {
+    const Group::Sub& u = g->subs[k];
+    GemmArgs q = per_mode(sub_ops(g, (int)k, st)->ST, R, (long)R * R, g->rhs_t + u.b0, t_out + u.b0, R, M, B, 0, M, R);
+    q.N = 2 * (u.b1 - u.b0);
+    if ((rc = gemm(g, KC_GEMM_MODE, q))) return rc;
+  }
   if ((rc = elementwise(g, 6.0, [&]() {
          return launch_add_buoyancy(R, M, B, o->inv_r, g->ra_pr, buo_scale, t_out, g->rhs_w, buo_store, s);
        })))
@@ -1658,7 +1735,7 @@ int step_imex(Group* g) {
   a.R = R; a.M = M; a.B = B;
   a.up = g->up; a.up0_prev = g->up0_prev;
   a.inv_r = o->inv_r; a.inv_r2 = o->inv_r2; a.ra_pr = g->ra_pr;
-  a.dt = g->cur_dt(); a.inv_pr = 1.0 / g->p.pr;
+  a.dt = g->cur_dt(); a.inv_pr = g->inv_pr;
   a.scheme_cn = cn ? 1 : 0;
   a.n_imp = ni; a.n_exp = ne; a.wt_lhs = sc.wt_lhs;
   for (int i = 0; i < 4; ++i) { a.w_imp[i] = sc.w_imp[i]; a.w_exp[i] = sc.w_exp[i]; }
@@ -1723,7 +1800,7 @@ int step_imexrk(Group* g) {
   StageArgs a{};
   a.R = R; a.M = M; a.B = B;
   a.inv_r = o->inv_r; a.inv_r2 = o->inv_r2; a.ra_pr = g->ra_pr;
-  a.dt = g->cur_dt(); a.inv_pr = 1.0 / g->p.pr; a.buo_imp = g->p.buo_imp;
+  a.dt = g->cur_dt(); a.inv_pr = g->inv_pr; a.buo_imp = g->p.buo_imp;
   a.t0 = g->t0; a.w0 = g->w0; a.u0 = g->u0;
   for (int i = 0; i < ns; ++i) {
     a.fat[i] = g->fat[i]; a.fdt[i] = g->fdt[i]; a.faw[i] = g->faw[i]; a.fdw[i] = g->fdw[i]; a.buo[i] = g->buo[i];
@@ -1738,8 +1815,7 @@ int step_imexrk(Group* g) {
     if (st > 0) {
       if ((rc = elementwise(g, 12.0 * st + 8.0, [&]() { return launch_stage_rhs(a, s); }))) return rc;
       const double scale = g->p.buo_imp ? g->cur_dt() * sc.aD[st][st] : 0.0;
-      const OpSet* so = g->stage_ops[st] ? g->stage_ops[st].get() : o;
-      if ((rc = solve_all(g, g->T(), g->W(), scale, g->buo[st], nullptr, so))) return rc;
+      if ((rc = solve_all(g, g->T(), g->W(), scale, g->buo[st], nullptr, st))) return rc;
     }
     double colsum = 0.0;
     for (int i = 0; i < ns; ++i) colsum += sc.aA[i][st];
@@ -1889,7 +1965,7 @@ int step_rk(Group* g) {
         (rc = gemm(g, KC_GEMM_RADIAL, gl)))
       return rc;
     RkRhsArgs a{};
-    a.R = R; a.M = M; a.B = B; a.inv_pr = 1.0 / g->p.pr;
+    a.R = R; a.M = M; a.B = B; a.inv_pr = g->inv_pr;
     a.inv_r = o->inv_r; a.inv_r2 = o->inv_r2; a.ra_pr = g->ra_pr;
     a.t = g->T(); a.w = g->W(); a.lt = g->lt; a.lw = g->lw;
     a.ntp = g->ntp; a.ntr = g->ntr; a.dntr = g->dntr; a.nwp = g->nwp; a.nwr = g->nwr; a.dnwr = g->dnwr;
@@ -2099,10 +2175,13 @@ int group_resize(Group* g, const std::vector<int>& map) {
   }
   cudaFree(dmap);
   g->ub = reinterpret_cast<double*>(g->ub2);
-  std::vector<double> ra(Bn, 0.0);
-  for (int j = 0; j < Bn; ++j) ra[j] = map[j] >= 0 ? g->ra_pr_h[map[j]] : 0.0;
+  std::vector<double> ra(Bn, 0.0), pr(Bn, g->p.pr);
+  for (int j = 0; j < Bn; ++j)
+    if (map[j] >= 0) { ra[j] = g->ra_pr_h[map[j]]; pr[j] = g->pr_h[map[j]]; }
   g->ra_pr_h = ra;
+  g->pr_h = pr;
   g->B = Bn;
+  make_subs(g);
   g->bytes = bytes;
   return 0;
 }
@@ -2653,7 +2732,7 @@ int group_restart(Group* g, const std::vector<std::string>& dirs, const std::vec
       RhsArgs a{};
       a.R = R; a.M = M; a.B = B;
       a.inv_r = o->inv_r; a.inv_r2 = o->inv_r2; a.ra_pr = g->ra_pr;
-      a.dt = g->cur_dt(); a.inv_pr = 1.0 / g->p.pr;
+      a.dt = g->cur_dt(); a.inv_pr = g->inv_pr;
       a.scheme_cn = cn ? 1 : 0;
       a.n_imp = ni; a.n_exp = ne; a.wt_lhs = g->sch.wt_lhs;
       for (int i = 0; i < ni; ++i) { a.th[i] = g->th[i]; a.wh[i] = g->wh[i]; a.ubh[i] = g->ubh[i]; }
@@ -2743,7 +2822,7 @@ int group_store_snapshot(Group* g, int b, const char* path) {
   auto done = [&](int e) { std::fclose(f); return e; };
   RecordWriter w;
   w.f = f;
-  w.put(g->ra_pr_h[b] * g->p.pr); w.put(g->p.pr); w.put(g->p.eta);
+  w.put(g->ra_pr_h[b] * g->pr_h[b]); w.put(g->pr_h[b]); w.put(g->p.eta);
   if (!w.end_record()) return done(fail(FALCON_EIO, "snapshot write failed"));
   w.put(g->cur_dt()); w.put(g->tot_time);
   if (!w.end_record()) return done(fail(FALCON_EIO, "snapshot write failed"));
@@ -3004,14 +3083,21 @@ static int batch_create(const falcon_params* ps, int n, falcon_batch** out) {
   b->params.assign(ps, ps + n);
   CK(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
   b->own_stream = true;
+  // Instances step together whenever grid, dt and scheme match: Ra enters
+  // only the buoyancy term, Pr only the temperature operator (one solve per
+  // Pr within the group), both taken per instance.  Within a key the
+  // instances are ordered by Pr, so that equal Pr form contiguous columns.
   std::map<OpKey, std::vector<int>> byk;
   for (int i = 0; i < n; ++i) {
     Scheme s;
     scheme_weights(ps[i].scheme_type, ps[i].scheme_imp, ps[i].scheme_exp, &s);
-    OpKey k = key_of(ps[i], s);  // operators shared whenever the key matches (Ra may differ)
+    OpKey k = key_of(ps[i], s);
+    k.pr = 0.0;
     if (ps[i].l_vartimestep) k.tag = i + 1;
     byk[k].push_back(i);
   }
+  for (auto& kv : byk)
+    std::stable_sort(kv.second.begin(), kv.second.end(), [&](int a, int c) { return ps[a].pr < ps[c].pr; });
   b->where.resize(n);
   const int gmax = g_max_group.load();
   for (auto& kv : byk) {
@@ -3805,10 +3891,11 @@ int server_admit_group(falcon_server* s, const OpKey& key, ServerGroup& sg) {
   }
   if ((rc = group_resize(sg.g.get(), map))) return rc;
   sg.ids = new_ids;
-  std::vector<double> ra(new_ids.size());
-  for (size_t j = 0; j < new_ids.size(); ++j) ra[j] = s->reqs[new_ids[j]].p.ra / s->reqs[new_ids[j]].p.pr;
-  sg.g->ra_pr_h = ra;
-  CK(cudaMemcpy(sg.g->ra_pr, ra.data(), sizeof(double) * ra.size(), cudaMemcpyHostToDevice));
+  for (size_t j = 0; j < new_ids.size(); ++j) {
+    sg.g->ra_pr_h[j] = s->reqs[new_ids[j]].p.ra / s->reqs[new_ids[j]].p.pr;
+    sg.g->pr_h[j] = s->reqs[new_ids[j]].p.pr;
+  }
+  if ((rc = upload_instance_params(sg.g.get()))) return rc;
   for (size_t j = 0; j < new_ids.size(); ++j) {
     if (map[j] >= 0) continue;
     if ((rc = server_set_initial(sg.g.get(), (int)j, s->reqs[new_ids[j]]))) return rc;

@@ -189,7 +189,8 @@ struct RhsArgs {
   const double* inv_r;      // R
   const double* inv_r2;     // R
   const double* ra_pr;      // B: Ra/Pr per instance
-  double dt, inv_pr;
+  const double* inv_pr;     // B: 1/Pr per instance
+  double dt;
   // IMEX multistep
   int scheme_cn;            // 1: Crank-Nicolson implicit part, 0: BDF
   int n_imp, n_exp;
@@ -217,7 +218,8 @@ struct StageArgs {
   const double* inv_r;
   const double* inv_r2;
   const double* ra_pr;
-  double dt, inv_pr;
+  const double* inv_pr;     // B: 1/Pr per instance
+  double dt;
   double aD[kMaxStages], aA[kMaxStages];   // row `st` of the Butcher tables
   double aD_ss;
   int buo_imp;
@@ -313,7 +315,7 @@ struct RkCombineArgs {
 // every mode, vorticity for m >= 1, and uphi_bar into fw[(r, 0, b)].
 struct RkRhsArgs {
   int R, M, B;
-  double inv_pr;
+  const double* inv_pr;     // B: 1/Pr per instance
   const double *inv_r, *inv_r2, *ra_pr;
   const double2 *t, *w, *lt, *lw, *ntp, *ntr, *dntr, *nwp, *nwr, *dnwr;
   const double2 *up, *ur, *dup, *lub;  // lub: radial Laplacian of the m = 0 column, R x B

@@ -1284,7 +1284,7 @@ __global__ void imex_rhs_kernel(RhsArgs a) {
       double2 rhs;
       if (a.scheme_cn) {
         const double2 T = a.th[0][e], L = a.lt[e];
-        const double c = c_cn * a.inv_pr, k2 = dm * dm * a.inv_r2[r];
+        const double c = c_cn * a.inv_pr[b], k2 = dm * dm * a.inv_r2[r];
         rhs = make_double2(fma(c, fma(-k2, T.x, L.x), T.x), fma(c, fma(-k2, T.y, L.y), T.y));
       } else {
         const double2 h0 = a.th[0][e];
@@ -1505,7 +1505,8 @@ __global__ void stage_deriv_kernel(StageArgs a) {
       const double2 p = a.ntp[e], q = a.ntr[e], dq = a.dntr[e];
       a.fat_out[e] = make_double2(-(-dm * ir * p.y + dq.x + ir * q.x), -(dm * ir * p.x + dq.y + ir * q.y));
       const double2 T = a.t[e], L = a.lt[e];
-      a.fdt_out[e] = make_double2(a.inv_pr * (L.x - mm * ir2 * T.x), a.inv_pr * (L.y - mm * ir2 * T.y));
+      const double ip = a.inv_pr[b];
+      a.fdt_out[e] = make_double2(ip * (L.x - mm * ir2 * T.x), ip * (L.y - mm * ir2 * T.y));
     }
     if (m == 0) {
       const size_t rb = (size_t)r * a.B + b;

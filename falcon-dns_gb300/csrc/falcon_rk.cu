@@ -72,7 +72,8 @@ __global__ void rk_rhs_kernel(RkRhsArgs a) {
     const double2 p = a.ntp[e], q = a.ntr[e], dq = a.dntr[e];
     const double lx = LT.x - mm * rr2 * T.x, ly = LT.y - mm * rr2 * T.y;
     const double ox = -((-mr * p.y) + dq.x + rr * q.x), oy = -((mr * p.x) + dq.y + rr * q.y);
-    a.ft[e] = make_double2(a.inv_pr * lx + ox, a.inv_pr * ly + oy);
+    const double ip = a.inv_pr[b];
+    a.ft[e] = make_double2(ip * lx + ox, ip * ly + oy);
     if (m == 0) continue;
     const double2 W = a.w[e], LW = a.lw[e];
     const double2 pw = a.nwp[e], qw = a.nwr[e], dqw = a.dnwr[e];

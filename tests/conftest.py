@@ -31,6 +31,19 @@ def fg():
     return falcon_gpu
 
 
+@pytest.fixture
+def fixed_paths(fg):
+    """Contraction paths by the fixed rules (falcon_set_gemm_mode(2)) instead
+    of the autotuner: the path of a contraction then depends only on its
+    kind and on whether it has 16 columns per batch entry, and every path is
+    exact per column, so an instance of a small batch steps to the same bits
+    alone and in the batch.  (Under the autotuner the paths of different
+    shapes may differ, and such results agree to FP64 rounding.)"""
+    prev = fg.set_gemm_mode(2)
+    yield
+    fg.set_gemm_mode(prev)
+
+
 @pytest.fixture(scope="session")
 def golden():
     import numpy as np

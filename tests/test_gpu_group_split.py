@@ -20,7 +20,7 @@ def run(fg, ps, seeds, gmax, nsteps):
     return out
 
 
-def test_split_groups_step_to_the_same_bits(fg):
+def test_split_groups_step_to_the_same_bits(fg, fixed_paths):
     R, Nm, n = 65, 42, 20
     ps = [fg.make_params(R, Nm, "SBDF3", ra=1e5 * (1 + 0.1 * k), dt=1e-5) for k in range(n)]
     seeds = list(range(300, 300 + n))

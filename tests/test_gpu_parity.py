@@ -206,7 +206,7 @@ def test_instance_close_alone_and_in_large_batch(fg):
         assert rel(sb[f], sa[f]) < 1e-12, f
 
 
-def test_instance_identical_alone_and_in_batch(fg):
+def test_instance_identical_alone_and_in_batch(fg, fixed_paths):
     R, Nm, n = 65, 170, 6
     ras = [10 ** (6 + 2 * u) for u in np.linspace(0.1, 0.9, n)]
     ps = [fg.make_params(R, Nm, "SBDF3", ra=ra, dt=1e-6) for ra in ras]

@@ -79,7 +79,7 @@ def test_variable_dt_restart(orc, fg, tmp_path, scheme, started, optimize):
     assert max(errs.values()) < TOL, errs
 
 
-def test_batch_restart_from_two_directories(orc, fg, tmp_path):
+def test_batch_restart_from_two_directories(orc, fg, tmp_path, fixed_paths):
     d1, d2 = tmp_path / "a", tmp_path / "b"
     d1.mkdir()
     d2.mkdir()

@@ -67,7 +67,7 @@ def test_rk_diagnostics_match_oracle(orc, fg):
         assert abs(dg[kg] - do[ko]) <= 1e-9 * max(abs(do[ko]), 1e-300), (kg, dg[kg], do[ko])
 
 
-def test_rk_in_mixed_batch_bitwise_alone(fg):
+def test_rk_in_mixed_batch_bitwise_alone(fg, fixed_paths):
     ps = [fg.make_params(17, 10, "RK4", ra=1e4, dt=1e-6), fg.make_params(17, 8, "SBDF3", ra=1e4, dt=1e-4),
           fg.make_params(17, 10, "RK4", ra=3e4, dt=1e-6)]
     b = fg.Batch(ps)

@@ -59,7 +59,7 @@ def test_diag_diff_stress_free(orc, fg, scheme):
     assert max(errs.values()) < STEP_TOL, errs
 
 
-def test_diag_diff_group_shares_stage_operators_bitwise(fg):
+def test_diag_diff_group_shares_stage_operators_bitwise(fg, fixed_paths):
     # two SMR333 instances (different Ra) form one group with one set of
     # stage operators; each equals its own run alone
     ps = [fg.make_params(17, 10, "SMR333", ra=1e4, dt=1e-5), fg.make_params(17, 10, "SMR333", ra=3e4, dt=1e-5),
