@@ -45,6 +45,7 @@ FALCON_DEF_TAB(5)
 FALCON_DEF_TAB(7)
 FALCON_DEF_TAB(11)
 FALCON_DEF_TAB(13)
+FALCON_DEF_TAB(15)
 FALCON_DEF_TAB(17)
 FALCON_DEF_TAB(19)
 FALCON_DEF_TAB(23)
@@ -71,7 +72,7 @@ cudaError_t init_dft_tables() {
   if (dev >= 0 && dev < 64 && done[dev].load()) return cudaSuccess;
   cudaError_t e = cudaSuccess;
 #define FALCON_SET(p) if (e == cudaSuccess) e = set_tab<p>(kC##p, kS##p);
-  FALCON_SET(3) FALCON_SET(5) FALCON_SET(7) FALCON_SET(11) FALCON_SET(13)
+  FALCON_SET(3) FALCON_SET(5) FALCON_SET(7) FALCON_SET(11) FALCON_SET(13) FALCON_SET(15)
   FALCON_SET(17) FALCON_SET(19) FALCON_SET(23) FALCON_SET(29) FALCON_SET(31)
 #undef FALCON_SET
   if (e == cudaSuccess && dev >= 0 && dev < 64) done[dev].store(true);
@@ -248,9 +249,10 @@ __device__ __forceinline__ void run_stage(int p, bool dif, bool twid, double2* A
     }
   }
   if constexpr (MAXP == 17) {  // plans with a prime above 17 keep the FMA butterflies
-    if (!twid && (p == 11 || p == 13 || p == 17)) {
+    if (!twid && (p == 11 || p == 13 || p == 15 || p == 17)) {
       if (p == 11) dft_mma_stage<11>(A, Bf, P, m, lane, 0, 1);
       else if (p == 13) dft_mma_stage<13>(A, Bf, P, m, lane, 0, 1);
+      else if (p == 15) dft_mma_stage<15>(A, Bf, P, m, lane, 0, 1);
       else dft_mma_stage<17>(A, Bf, P, m, lane, 0, 1);
       return;
     }
@@ -663,9 +665,10 @@ __device__ __forceinline__ void run_stage_block(int p, bool dif, bool twid, doub
     }
   }
   if constexpr (MAXP == 17) {  // plans with a prime above 17 keep the FMA butterflies
-    if (!twid && (p == 11 || p == 13 || p == 17)) {
+    if (!twid && (p == 11 || p == 13 || p == 15 || p == 17)) {
       if (p == 11) dft_mma_stage<11>(A, Bf, P, m, tid & 31, tid >> 5, nt >> 5);
       else if (p == 13) dft_mma_stage<13>(A, Bf, P, m, tid & 31, tid >> 5, nt >> 5);
+      else if (p == 15) dft_mma_stage<15>(A, Bf, P, m, tid & 31, tid >> 5, nt >> 5);
       else dft_mma_stage<17>(A, Bf, P, m, tid & 31, tid >> 5, nt >> 5);
       __syncthreads();
       return;
