@@ -1070,6 +1070,27 @@ int upload_instance_params(Group* g) {
   return 0;
 }
 
+// After the members of a group changed (serving): its subs from the
+// instances' Pr, and the operator sets of each (built or taken from the
+// operator cache).  The group's parameters take the Pr of its first column.
+int group_refresh_subs(Group* g) {
+  make_subs(g);
+  if (g->B == 0) return 0;
+  int rc;
+  if (g->pr_h[0] != g->p.pr) {
+    g->p.pr = g->pr_h[0];
+    if ((rc = build_opset(key_of(g->p, g->sch), &g->ops))) return rc;
+  }
+  for (size_t k = 1; k < g->subs.size(); ++k) {
+    falcon_params q = g->p;
+    q.pr = g->pr_h[g->subs[k].b0];
+    if ((rc = build_opset(key_of(q, g->sch), &g->subs[k].ops))) return rc;
+  }
+  if ((rc = build_stage_ops(g, g->p.dt))) return rc;
+  g->drop_graphs();
+  return 0;
+}
+
 int group_init(Group* g, const std::vector<falcon_params>& ps, const std::vector<int>& members) {
   g->p = ps[members[0]];
   g->members = members;
@@ -3797,7 +3818,8 @@ struct ServerRequest {
   falcon_diag diag{};
   std::vector<double> tfr, omg, upf, urf;  // final fields (Fortran layout)
   std::vector<double> init_t, init_w, init_up, init_ur;  // caller's initial state (empty: seeded noise)
-  OpKey key{};
+  OpKey key{};   // its group: grid, dt, scheme (any Pr)
+  OpKey fkey{};  // its operator set (Pr included)
 };
 
 struct ServerGroup {
@@ -3815,6 +3837,7 @@ struct falcon_server {
   std::deque<int64_t> queue;
   std::map<int64_t, ServerRequest> reqs;
   std::map<OpKey, ServerGroup> groups;
+  std::map<OpKey, int> per_opset;  // active requests per operator set (Pr included)
   // groups are spread over a pool of streams so that their steps overlap
   std::vector<cudaStream_t> streams;
   int next_stream = 0;
@@ -3866,14 +3889,20 @@ int server_set_initial(Group* g, int j, const ServerRequest& r) {
 }
 
 int server_admit_group(falcon_server* s, const OpKey& key, ServerGroup& sg) {
-  // repack: keep current ids (minus retired), append pending
-  std::vector<int64_t> new_ids;
-  std::vector<int> map;
+  // repack: keep current ids (minus retired), append pending, ordered by Pr
+  // (equal Pr in contiguous columns: one temperature solve per Pr)
+  std::vector<std::pair<int64_t, int>> slots;
   for (size_t j = 0; j < sg.ids.size(); ++j) {
     auto it = s->reqs.find(sg.ids[j]);
-    if (it != s->reqs.end() && it->second.state == 1) { new_ids.push_back(sg.ids[j]); map.push_back((int)j); }
+    if (it != s->reqs.end() && it->second.state == 1) slots.push_back({sg.ids[j], (int)j});
   }
-  for (int64_t id : sg.pending) { new_ids.push_back(id); map.push_back(-1); }
+  for (int64_t id : sg.pending) slots.push_back({id, -1});
+  std::stable_sort(slots.begin(), slots.end(), [&](const std::pair<int64_t, int>& a, const std::pair<int64_t, int>& b) {
+    return s->reqs[a.first].p.pr < s->reqs[b.first].p.pr;
+  });
+  std::vector<int64_t> new_ids;
+  std::vector<int> map;
+  for (auto& sl : slots) { new_ids.push_back(sl.first); map.push_back(sl.second); }
   sg.pending.clear();
   if (new_ids.empty()) { sg.g.reset(); sg.ids.clear(); return 0; }
   int rc;
@@ -3895,7 +3924,7 @@ int server_admit_group(falcon_server* s, const OpKey& key, ServerGroup& sg) {
     sg.g->ra_pr_h[j] = s->reqs[new_ids[j]].p.ra / s->reqs[new_ids[j]].p.pr;
     sg.g->pr_h[j] = s->reqs[new_ids[j]].p.pr;
   }
-  if ((rc = upload_instance_params(sg.g.get()))) return rc;
+  if ((rc = upload_instance_params(sg.g.get())) || (rc = group_refresh_subs(sg.g.get()))) return rc;
   for (size_t j = 0; j < new_ids.size(); ++j) {
     if (map[j] >= 0) continue;
     if ((rc = server_set_initial(sg.g.get(), (int)j, s->reqs[new_ids[j]]))) return rc;
@@ -3986,6 +4015,8 @@ int falcon_server_submit(falcon_server* s, const falcon_params* p, uint64_t seed
   scheme_weights(p->scheme_type, p->scheme_imp, p->scheme_exp, &sc);
   r.key = key_of(*p, sc);
   if (p->l_vartimestep) r.key.tag = r.id;
+  r.fkey = r.key;
+  r.key.pr = 0.0;
   if (r.foot + opset_bytes(*p) > s->budget) return fail(FALCON_EBUSY, "request larger than the device budget");
   s->reqs[r.id] = r;
   s->queue.push_back(r.id);
@@ -3999,11 +4030,11 @@ int falcon_server_iterate(falcon_server* s, int* n_active, int* n_queued) {
   std::map<OpKey, bool> touched;
   while (!s->queue.empty() && s->active < s->max_active) {
     ServerRequest& r = s->reqs[s->queue.front()];
-    auto git = s->groups.find(r.key);
-    const bool resident = (git != s->groups.end() && (git->second.g || !git->second.pending.empty()));
+    const bool resident = s->per_opset[r.fkey] > 0;  // its operator set is on the device
     const size_t need = r.foot + (resident ? 0 : opset_bytes(r.p));
     if (s->used + need > s->budget) break;
     s->used += need;
+    s->per_opset[r.fkey]++;
     r.state = 1;
     s->groups[r.key].pending.push_back(r.id);
     s->groups[r.key].rep = r.p;
@@ -4061,12 +4092,12 @@ int falcon_server_iterate(falcon_server* s, int* n_active, int* n_queued) {
       r.state = 2;
       s->active--;
       s->used -= r.foot;
+      if (--s->per_opset[r.fkey] == 0) s->used -= std::min(s->used, opset_bytes(r.p));
       changed = true;
     }
     if (changed) {
       int rc = server_admit_group(s, kv.first, sg);
       if (rc) return rc;
-      if (!sg.g) s->used -= std::min(s->used, opset_bytes(sg.rep));
     }
   }
   if (n_active) *n_active = s->active;

@@ -76,3 +76,35 @@ def test_snapshot_of_a_mixed_group_carries_the_instance_pr(fg, tmp_path):
         s = parse_snapshot(path, 33, 21)
         assert s["pr"] == ps[i].pr and s["ra"] == ps[i].ra, i
     b.close()
+
+
+def test_served_pr_mix_shares_a_group_and_matches_alone(fg, fixed_paths):
+    # requests of one grid, dt and scheme with Pr 10, 0.1 and 1 arriving at
+    # different iterations and with different horizons: they step in one
+    # server group (sorted by Pr, one temperature solve per Pr), columns
+    # leave and join as requests finish and arrive, and each result equals
+    # the request served alone
+    p = [fg.make_params(17, 8, "SBDF3", ra=ra, dt=1e-4, pr=pr) for ra, pr in ((2e4, 10.0), (1e4, 0.1), (3e4, 1.0),
+                                                                           (1.5e4, 0.1), (2.5e4, 10.0))]
+    horizons = (9, 14, 6, 11, 8)
+    seeds = (31, 32, 33, 34, 35)
+    srv = fg.Server(1 << 30)
+    ids = [srv.submit(p[i], seeds[i], horizons[i]) for i in range(3)]
+    srv.iterate()
+    srv.iterate()
+    ids += [srv.submit(p[i], seeds[i], horizons[i]) for i in (3, 4)]   # arrive while the others run
+    for _ in range(40):
+        srv.iterate()
+        if all(srv.result(i)[0] for i in ids):
+            break
+    res = [srv.result(i) for i in ids]
+    srv.close()
+    for i, (done, status, diag, fields) in enumerate(res):
+        assert done and status == 0, i
+        alone = fg.Instance(p[i])
+        alone.init_noise(seeds[i])
+        alone.step(horizons[i])
+        st = alone.get_state()
+        alone.close()
+        for k in FIELDS:
+            assert np.array_equal(fields[k], st[k]), (i, k)
