@@ -1513,6 +1513,11 @@ int gemm(Group* g, int cls, const GemmArgs& q0, bool reuse = false) {
   GemmArgs q = q0;
   q.oz_s = nullptr;
   q.oz_xs = nullptr;
+  // X may have changed since the planes were made: only a call that follows
+  // one on the same, unchanged X may reuse them (the paths of two such
+  // calls can differ under the autotuner, so the first one need not have
+  // made them)
+  if (!reuse) g->oz_key.valid = false;
   const int mode = g_gemm_mode.load();
   bool ok = false;
   if (mode && g->oz_xs && (q.N >= 16 || mode != 2)) ok = attach_group(g, &q);

@@ -70,7 +70,7 @@ def test_graph_replay_after_reset_and_new_state(fg):
         assert np.array_equal(s1[f], s2[f]), f
 
 
-def test_block_per_line_and_warp_per_line_transforms_agree_bitwise(fg):
+def test_block_per_line_and_warp_per_line_transforms_agree_bitwise(fg, fixed_paths):
     # one instance of Nr=97, Np=1023 (radix 3, 11, 31) runs the block-per-line
     # nonlinear pass, four of them the warp-per-line one: the same bits
     p = fg.make_params(97, 341, "ARS443", ra=1e6, dt=1e-7)
