@@ -1,0 +1,90 @@
+// Recombination of exact integer-slice sums into one FP64 value, with
+// integer instructions only (GB300's FP64 pipe issues ~2 instructions per
+// clock per SM, so one FP64 add per output of a tensor-core contraction or
+// DFT stage costs as much as the rest of its epilogue).  Host and device:
+// the CPU tests compile this header with g++ and compare the two forms bit
+// for bit.
+#pragma once
+#include <math.h>
+#include <stdint.h>
+#include <string.h>
+
+#ifdef __CUDACC__
+#define FALCON_HD __host__ __device__ __forceinline__
+#else
+#define FALCON_HD inline
+#endif
+
+namespace falcon {
+
+FALCON_HD int clz64(unsigned long long x) {
+#ifdef __CUDA_ARCH__
+  return __clzll((long long)x);
+#else
+  return x ? __builtin_clzll(x) : 64;
+#endif
+}
+
+FALCON_HD double double_of_bits(unsigned long long b) {
+#ifdef __CUDA_ARCH__
+  return __longlong_as_double((long long)b);
+#else
+  double d;
+  memcpy(&d, &b, sizeof d);
+  return d;
+#endif
+}
+
+// v 2^k for |v| < 2^53 built from its bits when the result is a normal
+// number (exact), else from ldexp.
+FALCON_HD double i64_scaled(long long v, int k) {
+  if (v == 0) return 0.0;
+  const unsigned long long sgn = (unsigned long long)v & (1ull << 63);
+  const unsigned long long a = v < 0 ? 0ull - (unsigned long long)v : (unsigned long long)v;
+  const int lz = clz64(a);
+  const long long ex = (long long)(63 - lz) + 1023 + k;
+  if (ex < 1 || ex > 2046) return ldexp((double)v, k);
+  const unsigned long long frac = ((a << lz) << 1) >> 12;
+  return double_of_bits(sgn | ((unsigned long long)ex << 52) | frac);
+}
+
+// RN(H 2^(k + sh) + L 2^k) for |H|, |L| < 2^53 and 0 < sh < 40: the sum
+// formed exactly as a 128-bit integer and rounded once to nearest even.
+// With k >= -1022 and k + sh + 55 <= 1024 both terms and every nonzero sum
+// are normal numbers, so this is bit for bit i64_scaled(H, k + sh) +
+// i64_scaled(L, k) (two exact terms, one correctly rounded FP64 add); out
+// of that range it returns exactly that two-term form.
+FALCON_HD double combine_rn(long long H, long long L, int k, int sh) {
+  if (k < -1022 || k + sh + 55 > 1024) return i64_scaled(H, k + sh) + i64_scaled(L, k);
+  // S = H 2^sh + L in two's complement (hi:lo)
+  const unsigned long long hl = (unsigned long long)H << sh;
+  unsigned long long lo = hl + (unsigned long long)L;
+  unsigned long long hi = (unsigned long long)(H >> (64 - sh)) + (L < 0 ? ~0ull : 0ull) + (lo < hl ? 1ull : 0ull);
+  const bool neg = (long long)hi < 0;
+  if (neg) {  // magnitude
+    lo = ~lo + 1ull;
+    hi = ~hi + (lo == 0ull ? 1ull : 0ull);
+  }
+  if (hi == 0ull && lo == 0ull) return 0.0;
+  const int n = hi ? 128 - clz64(hi) : 64 - clz64(lo);  // bit length, <= 54 + sh < 94
+  int e = n - 1 + k;                                     // exponent of the leading bit
+  unsigned long long mant;
+  if (n <= 53) {
+    mant = lo << (53 - n);
+  } else {
+    const int s = n - 53;  // dropped bits, 1..40
+    mant = (lo >> s) | (hi << (64 - s));
+    const unsigned long long dropped = lo & ((1ull << s) - 1ull), half = 1ull << (s - 1);
+    if (dropped > half || (dropped == half && (mant & 1ull))) {
+      ++mant;
+      if (mant == (1ull << 53)) {
+        mant >>= 1;
+        ++e;
+      }
+    }
+  }
+  return double_of_bits((neg ? (1ull << 63) : 0ull) | ((unsigned long long)(e + 1023) << 52) |
+                        (mant & ((1ull << 52) - 1ull)));
+}
+
+}  // namespace falcon

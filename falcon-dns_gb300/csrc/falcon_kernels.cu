@@ -484,7 +484,7 @@ __device__ void dft_mma_stage(double2* A, double2* Bf, int P, int m, int lane, i
         const long long L = ((long long)__float2int_rn(acc[3][i]) << 27) + ((long long)__float2int_rn(acc[4][i]) << 18) +
                             ((long long)__float2int_rn(acc[5][i]) << 9) + __float2int_rn(acc[6][i]);
         const int k = (i < 2 ? erc : ers) + (f - 1022) - 36;
-        o[i] = oz_i64_scaled(H, k) + oz_i64_scaled(L, k - 36);
+        o[i] = combine_rn(H, L, k - 36, 36);
         if (f == 2047) o[i] = __longlong_as_double(0x7ff8000000000000LL);  // Inf or NaN in the column
       }
       const double ar = o[0] + v0o.x, ai = o[1] + v0o.y;
@@ -629,7 +629,7 @@ __device__ void dft_mma_stage_wide(double2* A, double2* Bf, int P, int m, int la
 #pragma unroll
         for (int d = 4; d <= kDwD; ++d) L = L * 256 + __float2int_rn(acc[d][i]);
         const int kL = er + (fcol - 1022) - 72;
-        o[part][i] = oz_i64_scaled(H, kL + 32) + oz_i64_scaled(L, kL);
+        o[part][i] = combine_rn(H, L, kL, 32);
         if (fcol == 2047) o[part][i] = __longlong_as_double(0x7ff8000000000000LL);
       }
     }

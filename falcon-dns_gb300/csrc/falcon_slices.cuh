@@ -8,6 +8,7 @@
 #include <cuda_fp16.h>
 #include <stdint.h>
 
+#include "falcon_combine.h"
 #include "falcon_internal.h"
 
 namespace falcon {
@@ -79,18 +80,10 @@ __device__ __forceinline__ uint32_t oz_slice_pair(uint32_t lo0, uint32_t hi0, ui
   return *reinterpret_cast<const uint32_t*>(&v) ^ sgn2;
 }
 
-// v 2^k for |v| < 2^53 built from its bits (integer instructions only:
-// no FP64 pipe), when the result is a normal number; else from ldexp.
-__device__ __forceinline__ double oz_i64_scaled(long long v, int k) {
-  if (v == 0) return 0.0;
-  const unsigned long long sgn = (unsigned long long)v & (1ull << 63);
-  const unsigned long long a = v < 0 ? 0ull - (unsigned long long)v : (unsigned long long)v;
-  const int lz = __clzll((long long)a);
-  const long long ex = (long long)(63 - lz) + 1023 + k;
-  if (ex < 1 || ex > 2046) return ldexp((double)v, k);
-  const unsigned long long frac = ((a << lz) << 1) >> 12;
-  return __longlong_as_double((long long)(sgn | ((unsigned long long)ex << 52) | frac));
-}
+// The recombination of a slice product's two partial sums, H of the
+// leading diagonals and L of the rest: RN(H 2^(k + sh) + L 2^k), each sum
+// exact, one rounding, by integer instructions (combine_rn,
+// falcon_combine.h).
 
 // fp16 slices of 9 bits for short sums (the DFT butterflies: at most 8
 // products per output): kDftS slices of kDftW bits hold 63 bits of each

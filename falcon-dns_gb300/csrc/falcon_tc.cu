@@ -278,7 +278,7 @@ __global__ void __launch_bounds__(448, 1) tc_gemm_kernel(const __grid_constant__
               L = L * (1 << W) + (long long)__float2int_rn(__uint_as_float(v[d][j]));
             const int fb = cex[c0 + j];
             const int kL = er + (fb - 1022) - 2 * C::MAGB + W * (2 * C::S - 2 - C::D);
-            double y = fb > 0 ? oz_i64_scaled(H, kL + W * (C::D - C::HD)) + oz_i64_scaled(L, kL) : 0.0;
+            double y = fb > 0 ? combine_rn(H, L, kL, W * (C::D - C::HD)) : 0.0;
             if (fb == 2047) y = __longlong_as_double(0x7ff8000000000000LL);  // Inf or NaN in the column
             out[j] = q.alpha != 1.0 ? q.alpha * y : y;
           }

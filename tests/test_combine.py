@@ -1,0 +1,90 @@
+"""The integer-only recombination combine_rn (falcon-dns_gb300/csrc/
+falcon_combine.h) of the tensor-core contractions and DFT stages against
+the two-term form it replaces (two exact power-of-two scalings and one FP64
+add): the same bits on random sums of every sign, on exact ties of the
+rounding (to nearest even), on cancellations to zero, at the edges of its
+exponent range and beyond them (where it takes the two-term form itself).
+Compiled on the host with g++: no GPU."""
+import os
+import subprocess
+
+import pytest
+
+from conftest import PKG
+
+HARNESS = r'''
+#include <cstdio>
+#include <cstring>
+#include <random>
+#include "falcon_combine.h"
+using namespace falcon;
+static bool same(double a, double b) { return std::memcmp(&a, &b, sizeof a) == 0; }
+int main() {
+  std::mt19937_64 rng(12345);
+  long long checked = 0, bad = 0, fast = 0;
+  const int shifts[] = {30, 32, 35, 36};
+  auto check = [&](long long H, long long L, int k, int sh) {
+    const double ref = i64_scaled(H, k + sh) + i64_scaled(L, k);
+    const double got = combine_rn(H, L, k, sh);
+    ++checked;
+    if (!(k < -1022 || k + sh + 55 > 1024)) ++fast;
+    if (!same(ref, got)) {
+      if (bad < 5) std::printf("MISMATCH H=%lld L=%lld k=%d sh=%d ref=%a got=%a\n", H, L, k, sh, ref, got);
+      ++bad;
+    }
+  };
+  for (int it = 0; it < 2000000; ++it) {
+    const int sh = shifts[rng() % 4];
+    const int hb = (int)(rng() % 50), lb = (int)(rng() % 54);   // bit lengths up to 2^49, 2^53
+    long long H = hb ? (long long)(rng() >> (64 - hb)) : 0, L = lb ? (long long)(rng() >> (64 - lb)) : 0;
+    if (rng() & 1) H = -H;
+    if (rng() & 1) L = -L;
+    int k;
+    switch (rng() % 4) {
+      case 0: k = (int)(rng() % 200) - 150; break;            // the usual range
+      case 1: k = -1022 + (int)(rng() % 8) - 4; break;        // lower edge
+      case 2: k = 1024 - 55 - sh + (int)(rng() % 8) - 4; break;  // upper edge
+      default: k = (int)(rng() % 2100) - 1100; break;         // anywhere, fallbacks included
+    }
+    check(H, L, k, sh);
+  }
+  // exact ties: S = m 2^s + 2^(s-1) with 53-bit m, even and odd
+  for (int it = 0; it < 200000; ++it) {
+    const int sh = shifts[rng() % 4];
+    const int s = 1 + (int)(rng() % (sh - 1));
+    const long long m = (long long)((rng() >> 11) | (1ull << 52));
+    // split S = H 2^sh + L with |L| < 2^53: H = S >> sh, L = S - H 2^sh
+    const unsigned __int128 S = ((unsigned __int128)m << s) + ((unsigned __int128)1 << (s - 1));
+    const long long H = (long long)(S >> sh), L = (long long)(S - ((unsigned __int128)H << sh));
+    const int sg = (rng() & 1) ? -1 : 1;
+    check(sg * H, sg * L, (int)(rng() % 100) - 80, sh);
+  }
+  // cancellations and one-sided terms
+  for (int it = 0; it < 100000; ++it) {
+    const int sh = shifts[rng() % 4];
+    const long long H = (long long)(rng() >> 20) - (1ll << 43);
+    check(H, -(H * (1ll << 9)), 0, 9 + 0 * sh);  // H 2^9 - H 2^9 = 0 (sh = 9 here)
+    check(H, 0, -50, sh);
+    check(0, H, -50, sh);
+  }
+  std::printf("%lld %lld %lld\n", checked, fast, bad);
+  return 0;
+}
+'''
+
+
+@pytest.fixture(scope="module")
+def harness(tmp_path_factory):
+    d = tmp_path_factory.mktemp("combine")
+    (d / "h.cpp").write_text(HARNESS)
+    exe = d / "h"
+    subprocess.run(["g++", "-O2", "-std=c++17", "-I" + os.path.join(PKG, "csrc"), str(d / "h.cpp"), "-o", str(exe)],
+                   check=True)
+    return subprocess.run([str(exe)], check=True, capture_output=True, text=True, timeout=300).stdout
+
+
+def test_combine_rn_is_bit_identical_to_the_two_term_form(harness):
+    last = harness.strip().splitlines()[-1]
+    checked, fast, bad = (int(x) for x in last.split())
+    assert bad == 0, harness
+    assert checked > 2_000_000 and fast > checked // 2   # most cases take the integer path
