@@ -49,23 +49,6 @@ inline int make_fft_plan(int P, FftPlan* plan) {
     if (primes[i] > 64) return -1;
   }
   if (squarefree && small && np <= kMaxRadix) {
-    // 3 x 5 as one radix-15 stage when every factor is at most 17: the odd
-    // radices 11..17 of such plans run on the tensor cores (one symmetric
-    // 15-point butterfly there costs about half the FP64 instructions of a
-    // radix-3 and a radix-5 FMA stage)
-    bool has3 = false, has5 = false, le17 = true;
-    for (int i = 0; i < np; ++i) {
-      has3 = has3 || primes[i] == 3;
-      has5 = has5 || primes[i] == 5;
-      le17 = le17 && primes[i] <= 17;
-    }
-    if (has3 && has5 && le17) {
-      int j = 0;
-      for (int i = 0; i < np; ++i)
-        if (primes[i] == 3) primes[j++] = 15;
-        else if (primes[i] != 5) primes[j++] = primes[i];
-      np = j;
-    }
     f.pfa = 1;
     f.nrad = np;
     for (int i = 0; i < np; ++i) {

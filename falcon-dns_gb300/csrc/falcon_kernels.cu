@@ -13,6 +13,7 @@
 #include <atomic>
 #include <mutex>
 #include <unordered_map>
+#include <vector>
 
 #include "falcon_internal.h"
 #include "falcon_slices.cuh"
@@ -45,7 +46,6 @@ FALCON_DEF_TAB(5)
 FALCON_DEF_TAB(7)
 FALCON_DEF_TAB(11)
 FALCON_DEF_TAB(13)
-FALCON_DEF_TAB(15)
 FALCON_DEF_TAB(17)
 FALCON_DEF_TAB(19)
 FALCON_DEF_TAB(23)
@@ -72,7 +72,7 @@ cudaError_t init_dft_tables() {
   if (dev >= 0 && dev < 64 && done[dev].load()) return cudaSuccess;
   cudaError_t e = cudaSuccess;
 #define FALCON_SET(p) if (e == cudaSuccess) e = set_tab<p>(kC##p, kS##p);
-  FALCON_SET(3) FALCON_SET(5) FALCON_SET(7) FALCON_SET(11) FALCON_SET(13) FALCON_SET(15)
+  FALCON_SET(3) FALCON_SET(5) FALCON_SET(7) FALCON_SET(11) FALCON_SET(13)
   FALCON_SET(17) FALCON_SET(19) FALCON_SET(23) FALCON_SET(29) FALCON_SET(31)
 #undef FALCON_SET
   if (e == cudaSuccess && dev >= 0 && dev < 64) done[dev].store(true);
@@ -249,10 +249,9 @@ __device__ __forceinline__ void run_stage(int p, bool dif, bool twid, double2* A
     }
   }
   if constexpr (MAXP == 17) {  // plans with a prime above 17 keep the FMA butterflies
-    if (!twid && (p == 11 || p == 13 || p == 15 || p == 17)) {
+    if (!twid && (p == 11 || p == 13 || p == 17)) {
       if (p == 11) dft_mma_stage<11>(A, Bf, P, m, lane, 0, 1);
       else if (p == 13) dft_mma_stage<13>(A, Bf, P, m, lane, 0, 1);
-      else if (p == 15) dft_mma_stage<15>(A, Bf, P, m, lane, 0, 1);
       else dft_mma_stage<17>(A, Bf, P, m, lane, 0, 1);
       return;
     }
@@ -665,10 +664,9 @@ __device__ __forceinline__ void run_stage_block(int p, bool dif, bool twid, doub
     }
   }
   if constexpr (MAXP == 17) {  // plans with a prime above 17 keep the FMA butterflies
-    if (!twid && (p == 11 || p == 13 || p == 15 || p == 17)) {
+    if (!twid && (p == 11 || p == 13 || p == 17)) {
       if (p == 11) dft_mma_stage<11>(A, Bf, P, m, tid & 31, tid >> 5, nt >> 5);
       else if (p == 13) dft_mma_stage<13>(A, Bf, P, m, tid & 31, tid >> 5, nt >> 5);
-      else if (p == 15) dft_mma_stage<15>(A, Bf, P, m, tid & 31, tid >> 5, nt >> 5);
       else dft_mma_stage<17>(A, Bf, P, m, tid & 31, tid >> 5, nt >> 5);
       __syncthreads();
       return;
@@ -927,9 +925,34 @@ static cudaError_t launch_nonlin_line(const NonlinArgs& a, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+// Resident warps per SM of the warp-per-line form (w warps a block, smem
+// bytes) and of the block-per-line form with 8 warps a line, from the
+// occupancy calculator; memoised per (form, P).
+template <int MAXP>
+static bool line_form_holds_more_warps(int P, int w, int smem) {
+  struct Memo { int P, w, smem; bool line; };
+  thread_local std::vector<Memo> memo;
+  for (const Memo& m : memo)
+    if (m.P == P && m.w == w && m.smem == smem) return m.line;
+  const int smem_line = (P + (P + 3) / 4 + 2 * P) * 16;
+  int nb_warp = 0, nb_line = 0;
+  bool line = false;
+  if (cudaFuncSetAttribute(nonlin_kernel<MAXP>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) == cudaSuccess &&
+      cudaFuncSetAttribute(nonlin_line_kernel<MAXP, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_line) ==
+          cudaSuccess &&
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb_warp, nonlin_kernel<MAXP>, 32 * w, smem) == cudaSuccess &&
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb_line, nonlin_line_kernel<MAXP, 4>, 256, smem_line) ==
+          cudaSuccess)
+    line = nb_line * 8 > nb_warp * w;
+  memo.push_back(Memo{P, w, smem, line});
+  return line;
+}
+
 // Lines that one warp each cannot spread over the GPU (fewer than two per
 // SM) go to the block-per-line form: 8 warps per line up to one line per
-// SM, 4 up to two.
+// SM, 4 up to two.  So do long lines whose warp-per-line blocks (a whole
+// line per warp in shared memory) would leave fewer warps on an SM than the
+// block-per-line form (Np = 1023, 1536: 3-4 against 16 warps per SM).
 template <int MAXP>
 static cudaError_t launch_nonlin_t(const NonlinArgs& a, cudaStream_t s) {
   int dev = 0, nsm = 152;
@@ -940,6 +963,7 @@ static cudaError_t launch_nonlin_t(const NonlinArgs& a, cudaStream_t s) {
   if (nlines <= 2 * nsm) return launch_nonlin_line<MAXP, 2>(a, s);
   int smem = 0;
   const int w = nonlin_warps(a.plan.P, MAXP == 17 && a.plan.pfa, &smem);
+  if (line_form_holds_more_warps<MAXP>(a.plan.P, w, smem)) return launch_nonlin_line<MAXP, 4>(a, s);
   cudaError_t e = cudaFuncSetAttribute(nonlin_kernel<MAXP>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return e;
   const int grid = (nlines + w - 1) / w;

@@ -375,8 +375,10 @@ int falcon_set_step_graphs(int enable);
  * cores.  Modes:
  *   4 (default) autotuned: the first time a contraction shape runs outside
  *     graph capture, every available path is timed on it (the device
- *     otherwise idle) and the fastest is kept for that shape (see
- *     falcon_set_tune_cache);
+ *     otherwise idle, L2 flushed before each timed run, as a step's
+ *     operators come from HBM) and the fastest is kept for that shape (see
+ *     falcon_set_tune_cache; the library holds a 256 MiB device buffer
+ *     for the flush from the first measurement on);
  *   3 tcgen05 for every contraction with a slice view of its operator
  *     (mma.sync where that view has no tensor map): the same bits as 1;
  *   2 fixed rules: tcgen05 for contractions of at least two 128 x 24 tiles

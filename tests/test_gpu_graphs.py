@@ -70,15 +70,22 @@ def test_graph_replay_after_reset_and_new_state(fg):
         assert np.array_equal(s1[f], s2[f]), f
 
 
-def test_block_per_line_and_warp_per_line_transforms_agree_bitwise(fg, fixed_paths):
-    # one instance of Nr=97, Np=1023 (radix 3, 11, 31) runs the block-per-line
-    # nonlinear pass, four of them the warp-per-line one: the same bits
-    p = fg.make_params(97, 341, "ARS443", ra=1e6, dt=1e-7)
+@pytest.mark.parametrize("R,Nm,scheme,dt,nb", [
+    # Np = 510 (radix 2, 3, 5, 17): one instance (65 lines) runs the
+    # block-per-line pass, five (325 lines) the warp-per-line one
+    (65, 170, "SBDF3", 1e-6, 5),
+    # Np = 1023 (radix 3, 11, 31): one instance with 8 warps per line, three
+    # (291 lines) with 4; longer batches keep the block-per-line form here
+    # (it holds 16 warps per SM against 4)
+    (97, 341, "ARS443", 1e-7, 3),
+])
+def test_block_per_line_and_warp_per_line_transforms_agree_bitwise(fg, fixed_paths, R, Nm, scheme, dt, nb):
+    p = fg.make_params(R, Nm, scheme, ra=1e6, dt=dt)
     alone = fg.Instance(p)
     alone.init_noise(9)
     alone.step(3)
-    b = fg.Batch([p] * 4)
-    b.init_noise([9, 10, 11, 12])
+    b = fg.Batch([p] * nb)
+    b.init_noise(list(range(9, 9 + nb)))
     b.step(3)
     sa, sb = alone.get_state(), b.get_state(0)
     for f in FIELDS:
