@@ -1450,7 +1450,8 @@ void* tune_flush_buffer() {
 // The path of a contraction under mode 4: the cached decision, or a
 // measurement of every available path (each run once to warm up, then three
 // times with L2 flushed before each, timed by CUDA events on the group's
-// stream with the device otherwise idle; the fastest of the three counts).
+// stream with the device otherwise idle; the fastest of the three counts),
+// keeping the fixed rule's path unless another is at least 10 % faster.
 // Shapes met inside graph capture or profiling, or whose output overlaps
 // X, are not measured: they take the fixed rule of mode 2.
 int tuned_path(Group* g, int cls, const GemmArgs& q, bool reuse, bool tc_ok, int fixed, int* path) {
@@ -1518,6 +1519,10 @@ int tuned_path(Group* g, int cls, const GemmArgs& q, bool reuse, bool tc_ok, int
   cudaEventDestroy(a);
   cudaEventDestroy(b);
   if (rc) return rc;
+  // the fixed rule's path unless another is at least 10 % faster: a
+  // contraction inside a step pays launch and dependency costs that the
+  // isolated timing does not see, so near-ties keep the rule's choice
+  if (e.path != fixed && e.us[fixed] >= 0.f && e.us[fixed] <= 1.1f * e.us[e.path]) e.path = fixed;
   g_tune_measured++;
   std::lock_guard<std::mutex> lk(g_tune_mu);
   g_tune[k] = e;

@@ -376,7 +376,8 @@ int falcon_set_step_graphs(int enable);
  *   4 (default) autotuned: the first time a contraction shape runs outside
  *     graph capture, every available path is timed on it (the device
  *     otherwise idle, L2 flushed before each timed run, as a step's
- *     operators come from HBM) and the fastest is kept for that shape (see
+ *     operators come from HBM) and the fastest is kept for that shape (the
+ *     path of mode 2's rules unless another is at least 10 % faster; see
  *     falcon_set_tune_cache; the library holds a 256 MiB device buffer
  *     for the flush from the first measurement on);
  *   3 tcgen05 for every contraction with a slice view of its operator

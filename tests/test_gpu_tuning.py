@@ -6,7 +6,8 @@ fastest is kept.  Checked here:
 - a run that measures gives the same bits as a later run that only reads
   the decisions (the chosen path runs last), in this process and in one
   that reads them back from the cache file;
-- every decision is the fastest of its measured times, and narrow per-mode
+- every decision is within 10 % of the fastest of its measured times (the
+  fixed rule's path is kept unless another is 10 % faster), and narrow per-mode
   contractions (groups of a few instances, N < 16) were measured on the
   sliced paths too;
 - the tuned run agrees with the oracle after 100 steps (1e-10).
@@ -74,7 +75,8 @@ def test_tuned_runs_are_reproducible_and_pick_the_fastest(fg, tuned):
         assert d == dev
         avail = [t for t in us if t >= 0]
         assert us[0] > 0 and us[1] > 0                       # FMA and mma.sync always measured
-        assert us[path] == min(avail), (r, K, N, batch, us, path)
+        # the fastest, or the fixed rule's path within 10 % of it
+        assert us[path] <= 1.1 * min(avail), (r, K, N, batch, us, path)
         if per_mode and N < 16:
             narrow += 1
     assert narrow > 0
