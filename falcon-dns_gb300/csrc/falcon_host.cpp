@@ -224,6 +224,9 @@ struct OpSet {
   std::vector<Oz> oz;
   size_t bytes = 0;
   ~OpSet() {
+    // the last group holding the set is gone, but a kernel of any group's
+    // stream that read it may still run: every stream drains first
+    cudaDeviceSynchronize();
     cudaFree(D1p); cudaFree(Lp); cudaFree(ST); cudaFree(G); cudaFree(U); cudaFree(LAP);
     cudaFree(inv_r); cudaFree(inv_r2); cudaFree(wq); cudaFree(d1_0); cudaFree(d1_R);
     cudaFree(D1c); cudaFree(Lc);
@@ -926,6 +929,8 @@ struct Group {
   // captured steps are dropped.
   bool direct_next = false;
   void drop_graphs() {
+    // a step launched from one of these graphs may still run on the stream
+    if (stream && !graphs.empty()) cudaStreamSynchronize(stream);
     for (auto& sg : graphs) cudaGraphExecDestroy(sg.exec);
     graphs.clear();
     direct_next = true;
@@ -1206,7 +1211,8 @@ int launch(Group* g, int cls, double flops, F f) {
     CK(cudaEventRecord(a, g->stream));
   }
   cudaError_t e = f();
-  if (e != cudaSuccess) return fail(FALCON_ECUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
+  if (e != cudaSuccess)
+    return fail(FALCON_ECUDA, std::string("kernel launch (") + kClassNames[cls] + "): " + cudaGetErrorString(e));
   g_launches++;
   if (g->prof) {
     CK(cudaEventRecord(b, g->stream));
@@ -1560,8 +1566,12 @@ int gemm(Group* g, int cls, const GemmArgs& q0, bool reuse = false) {
   if (mode == 3 && tc_ok) path = PATH_TC;
   if ((mode == 2 || mode == 4) && tc_ok && tc_worth_it(q)) path = PATH_TC;
   if (mode == 4) {
+    // the tuner weighs tcgen05 only for contractions that fill the GPU (at
+    // least two tiles per SM): below that one 448-thread CTA per SM idles
+    // most of its warps, and the narrow shapes stay on the kernels whose
+    // launch cost is lower
     const int fixed = q.N >= 16 ? path : PATH_FMA;
-    int rc = tuned_path(g, cls, q, reuse, tc_ok, fixed, &path);
+    int rc = tuned_path(g, cls, q, reuse, tc_ok && tc_worth_it(q), fixed, &path);
     if (rc) return rc;
   }
   return run_path(g, cls, q, path, reuse);
@@ -2214,6 +2224,7 @@ int group_get_instance(Group* g, int b, double* t, double* w, double* up, double
 // new layout takes old slot map[j] (or zeros when map[j] < 0).
 int group_resize(Group* g, const std::vector<int>& map) {
   const int Bn = (int)map.size();
+  CK(cudaStreamSynchronize(g->stream));  // the last step of the group reads the arrays
   g->drop_graphs();  // the arrays move
   int* dmap = nullptr;
   CK(cudaMalloc(&dmap, sizeof(int) * std::max(Bn, 1)));
