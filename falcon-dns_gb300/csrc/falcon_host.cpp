@@ -1331,7 +1331,17 @@ int mma_planes(Group* g, GemmArgs* q, bool reuse, bool* fits) {
 }
 
 // One contraction on the given path (q carries its slice view for MMA/TC).
+int run_path_once(Group* g, int cls, GemmArgs q, int path, bool reuse);
 int run_path(Group* g, int cls, GemmArgs q, int path, bool reuse) {
+  const int rc = run_path_once(g, cls, q, path, reuse);
+  if (rc == FALCON_ECUDA)  // the shape and path of the failed contraction
+    g_err += " [contraction path " + std::to_string(path) + ": rows " + std::to_string(q.rows) + ", K " +
+             std::to_string(q.K) + ", N " + std::to_string(q.N) + ", batch " + std::to_string(q.batch) + ", w " +
+             std::to_string(q.oz_w) + ", group of " + std::to_string(g->B) + " at Nr " + std::to_string(g->R) +
+             ", Nm " + std::to_string(g->Nm) + "]";
+  return rc;
+}
+int run_path_once(Group* g, int cls, GemmArgs q, int path, bool reuse) {
   if (path == PATH_TC) {
     const TcArgs t = tc_args(q);
     const CUtensorMap* map = static_cast<const CUtensorMap*>(q.oz_tmap);
@@ -1640,7 +1650,11 @@ int run_nonlin(Group* g) {
   a.umax = g->vardt ? g->umax : nullptr;
   const double P = g->P;
   const double flops = (double)g->R * g->B * (4.0 * 5.0 * P * std::log2(P) + 6.0 * P);
-  return launch(g, KC_NONLIN, flops, [&]() { return launch_nonlin(a, g->stream); });
+  const int rc = launch(g, KC_NONLIN, flops, [&]() { return launch_nonlin(a, g->stream); });
+  if (rc == FALCON_ECUDA)
+    g_err += " [nonlinear pass: group of " + std::to_string(g->B) + " at Nr " + std::to_string(g->R) + ", Np " +
+             std::to_string(g->P) + "]";
+  return rc;
 }
 
 // The implicit solves shared by IMEX and IMEXRK: temperature, then
