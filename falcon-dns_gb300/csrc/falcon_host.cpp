@@ -401,6 +401,10 @@ template <class T>
 int upload(T** dst, const std::vector<T>& v, size_t* acc) {
   CK(cudaMalloc(dst, sizeof(T) * v.size()));
   CK(cudaMemcpy(*dst, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice));
+  // a copy from pageable memory may return before its DMA has landed, and
+  // the kernels that read these tables run on non-blocking streams, which
+  // do not wait for the legacy stream
+  CK(cudaStreamSynchronize(0));
   if (acc) *acc += sizeof(T) * v.size();
   return 0;
 }
@@ -955,7 +959,9 @@ struct Group {
   template <class T>
   int alloc(T** q, size_t n) {
     CK(cudaMalloc(q, sizeof(T) * (n ? n : 1)));
-    CK(cudaMemset(*q, 0, sizeof(T) * (n ? n : 1)));
+    // on the group's stream: its kernels (on a non-blocking stream) would
+    // not wait for a legacy-stream memset
+    CK(cudaMemsetAsync(*q, 0, sizeof(T) * (n ? n : 1), stream));
     allocs.push_back(*q);
     bytes += sizeof(T) * n;
     const int ew = (int)(sizeof(T) / sizeof(double));
@@ -1070,8 +1076,11 @@ int upload_instance_params(Group* g) {
   const int B = g->B;
   std::vector<double> ip(B);
   for (int b = 0; b < B; ++b) ip[b] = 1.0 / g->pr_h[b];
-  CK(cudaMemcpy(g->ra_pr, g->ra_pr_h.data(), sizeof(double) * B, cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(g->inv_pr, ip.data(), sizeof(double) * B, cudaMemcpyHostToDevice));
+  // stream-ordered before the group's kernels (a legacy-stream copy from
+  // pageable memory may land after a kernel of a non-blocking stream read it)
+  CK(cudaMemcpyAsync(g->ra_pr, g->ra_pr_h.data(), sizeof(double) * B, cudaMemcpyHostToDevice, g->stream));
+  CK(cudaMemcpyAsync(g->inv_pr, ip.data(), sizeof(double) * B, cudaMemcpyHostToDevice, g->stream));
+  CK(cudaStreamSynchronize(g->stream));
   return 0;
 }
 
@@ -2240,9 +2249,14 @@ int group_resize(Group* g, const std::vector<int>& map) {
   const int Bn = (int)map.size();
   CK(cudaStreamSynchronize(g->stream));  // the last step of the group reads the arrays
   g->drop_graphs();  // the arrays move
+  for (int j = 0; j < Bn; ++j)
+    if (map[j] < -1 || map[j] >= g->B) return fail(FALCON_EINVAL, "column map entry out of range");
   int* dmap = nullptr;
   CK(cudaMalloc(&dmap, sizeof(int) * std::max(Bn, 1)));
-  CK(cudaMemcpy(dmap, map.data(), sizeof(int) * Bn, cudaMemcpyHostToDevice));
+  // on the group's stream, so that the remap kernels below read the map
+  // only after it has landed (a legacy-stream copy from pageable memory may
+  // return before its DMA completes, and this stream does not wait for it)
+  CK(cudaMemcpyAsync(dmap, map.data(), sizeof(int) * Bn, cudaMemcpyHostToDevice, g->stream));
   size_t bytes = 0;
   for (auto& f : g->fields) {
     double* old = reinterpret_cast<double*>(*f.ptr);

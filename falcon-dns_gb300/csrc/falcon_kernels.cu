@@ -75,6 +75,9 @@ cudaError_t init_dft_tables() {
   FALCON_SET(3) FALCON_SET(5) FALCON_SET(7) FALCON_SET(11) FALCON_SET(13)
   FALCON_SET(17) FALCON_SET(19) FALCON_SET(23) FALCON_SET(29) FALCON_SET(31)
 #undef FALCON_SET
+  // the copies may return before they land; the kernels reading the tables
+  // run on non-blocking streams
+  if (e == cudaSuccess) e = cudaStreamSynchronize(0);
   if (e == cudaSuccess && dev >= 0 && dev < 64) done[dev].store(true);
   return e;
 }
