@@ -1605,7 +1605,10 @@ int gemm(Group* g, int cls, const GemmArgs& q0, bool reuse = false) {
 int gemm_blocks(Group* g, int cls, std::initializer_list<GemmArgs> blocks) {
   const std::vector<GemmArgs> v(blocks);
   const int mode = g_gemm_mode.load();
-  if (mode >= 2 && g->oz_xs && !v.empty() && v.size() <= 4 && (v[0].N >= 16 || mode != 2)) {
+  // (narrow blocks merge only when every contraction goes to tcgen05, mode
+  // 3: a merged launch of 2-14 columns per 24-column tile is slower than
+  // the blocks on the FMA or mma.sync paths)
+  if (mode >= 2 && g->oz_xs && !v.empty() && v.size() <= 4 && (v[0].N >= 16 || mode == 3)) {
     const GemmArgs& f = v[0];
     const char* x0 = reinterpret_cast<const char*>(f.X);
     const char* x1 = reinterpret_cast<const char*>(f.X + (size_t)(f.batch - 1) * f.sX + (size_t)f.K * f.ldx);
