@@ -473,9 +473,9 @@ def run_gpu(args):
         if t is None:
             e["traffic_ok"] = False
         else:
-            # profiles/traffic.json holds bytes per call of a 256-instance
+            # profiles/traffic.json holds bytes per call of a 128-instance
             # group; a call here covers one group of n / ngroups instances
-            e["traffic_sum"] += t * (n / ngroups) / 256.0 * v["launches"]
+            e["traffic_sum"] += t * (n / ngroups) / 128.0 * v["launches"]
     dom = max(kern, key=lambda k: kern[k]["ms"])
 
     tpeak, tpeak_src = tensor_peak()
@@ -512,7 +512,7 @@ def run_gpu(args):
 
     # ---- end to end through the C ABI from host arrays ----
     e2e = None
-    if rank == 0 or True:
+    if not args.uniform_only:
         b2 = fg.Batch(params)
         b2.set_stream(stream.cuda_stream)
         # host initial conditions (Fortran layout), pinned
@@ -543,7 +543,7 @@ def run_gpu(args):
         b2.close()
 
     # ---- plain one-instance-at-a-time GPU path ----
-    n1 = min(args.one_at_a_time, n)
+    n1 = 0 if args.uniform_only else min(args.one_at_a_time, n)
     insts = []
     for k in range(n1):
         it = fg.Instance(params[k])
@@ -560,14 +560,15 @@ def run_gpu(args):
             it.step(1)
     ev1.record(stream)
     torch.cuda.synchronize()
-    one_rate = n1 * k1 / (ev0.elapsed_time(ev1) / 1e3)
+    one_rate = n1 * k1 / (ev0.elapsed_time(ev1) / 1e3) if n1 else None
     for it in insts:
         it.close()
 
-    uneven = serving = None
-    plain = run_plain(args, fg, stream, torch)
-    single = run_single(args, fg, stream, torch)
-    if not args.no_mixed:
+    uneven = serving = plain = single = None
+    if not args.uniform_only:
+        plain = run_plain(args, fg, stream, torch)
+        single = run_single(args, fg, stream, torch)
+    if not args.no_mixed and not args.uniform_only:
         uneven = run_uneven(args, fg, stream, torch)
         serving = run_serving(args, fg, torch)
 
@@ -614,7 +615,7 @@ def run_gpu(args):
         "state_finite": bool(finite),
         # last, so that a reader of the line's tail sees the target ratio
         "one_at_a_time": {"value": one_rate, "unit": "instance-steps/s", "instances": n1, "steps": k1},
-        "batched_over_one_at_a_time": value / world / one_rate,
+        "batched_over_one_at_a_time": (value / world / one_rate) if one_rate else None,
     }
     print(json.dumps(line), flush=True)
     if world > 1:
@@ -632,6 +633,8 @@ def main():
     ap.add_argument("--cpu-seconds", dest="cpu_seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", dest="no_cpu", action="store_true")
     ap.add_argument("--no-mixed", dest="no_mixed", action="store_true", help="skip the uneven batch and serving")
+    ap.add_argument("--uniform-only", dest="uniform_only", action="store_true",
+                    help="the uniform batch alone (profiling captures): no e2e, one-at-a-time, plain, single, mixed")
     ap.add_argument("--single-steps", dest="single_steps", type=int, default=200)
     ap.add_argument("--plain-steps", dest="plain_steps", type=int, default=500)
     ap.add_argument("--gemm-mode", dest="gemm_mode", type=int, default=4, choices=[0, 1, 2, 3, 4],

@@ -3918,6 +3918,12 @@ struct falcon_server {
   std::map<int64_t, ServerRequest> reqs;
   std::map<OpKey, ServerGroup> groups;
   std::map<OpKey, int> per_opset;  // active requests per operator set (Pr included)
+  // Operator sets of past requests, kept after their last request left
+  // (a set costs its assembly, LU factorisation and slicing to rebuild when
+  // a request of its key arrives again), least recently used out first
+  // beyond half the device budget.
+  std::map<OpKey, std::pair<std::shared_ptr<OpSet>, long long>> keep;
+  long long keep_clock = 0;
   // groups are spread over a pool of streams so that their steps overlap
   std::vector<cudaStream_t> streams;
   int next_stream = 0;
@@ -3968,6 +3974,32 @@ int server_set_initial(Group* g, int j, const ServerRequest& r) {
   return group_set_instance(g, j, t.data(), nullptr, nullptr, nullptr);
 }
 
+// The operator sets a group holds, into the server's kept sets; the least
+// recently used kept sets that no group holds are released while the kept
+// bytes exceed half the budget.
+void server_keep(falcon_server* s, const Group* g) {
+  auto add = [&](const std::shared_ptr<OpSet>& o) {
+    if (o) s->keep[o->key] = {o, ++s->keep_clock};
+  };
+  add(g->ops);
+  for (const auto& so : g->stage_ops) add(so);
+  for (size_t k = 1; k < g->subs.size(); ++k) {
+    add(g->subs[k].ops);
+    for (const auto& so : g->subs[k].stage_ops) add(so);
+  }
+  for (;;) {
+    size_t total = 0;
+    auto oldest = s->keep.end();
+    for (auto it = s->keep.begin(); it != s->keep.end(); ++it) {
+      total += it->second.first->bytes;
+      if (it->second.first.use_count() == 1 && (oldest == s->keep.end() || it->second.second < oldest->second.second))
+        oldest = it;
+    }
+    if (total <= s->budget / 2 || oldest == s->keep.end()) break;
+    s->keep.erase(oldest);
+  }
+}
+
 int server_admit_group(falcon_server* s, const OpKey& key, ServerGroup& sg) {
   // repack: keep current ids (minus retired), append pending, ordered by Pr
   // (equal Pr in contiguous columns: one temperature solve per Pr)
@@ -3993,6 +4025,7 @@ int server_admit_group(falcon_server* s, const OpKey& key, ServerGroup& sg) {
     sg.g = std::make_unique<Group>();
     sg.g->stream = s->streams[s->next_stream++ % s->streams.size()];
     if ((rc = group_init(sg.g.get(), ps, mem))) return rc;
+    server_keep(s, sg.g.get());
     sg.ids = new_ids;
     for (size_t j = 0; j < new_ids.size(); ++j)
       if ((rc = server_set_initial(sg.g.get(), (int)j, s->reqs[new_ids[j]]))) return rc;
@@ -4005,6 +4038,7 @@ int server_admit_group(falcon_server* s, const OpKey& key, ServerGroup& sg) {
     sg.g->pr_h[j] = s->reqs[new_ids[j]].p.pr;
   }
   if ((rc = upload_instance_params(sg.g.get())) || (rc = group_refresh_subs(sg.g.get()))) return rc;
+  server_keep(s, sg.g.get());
   for (size_t j = 0; j < new_ids.size(); ++j) {
     if (map[j] >= 0) continue;
     if ((rc = server_set_initial(sg.g.get(), (int)j, s->reqs[new_ids[j]]))) return rc;
