@@ -87,4 +87,17 @@ FALCON_HD double combine_rn(long long H, long long L, int k, int sh) {
                         (mant & ((1ull << 52) - 1ull)));
 }
 
+// The exact integer sum_{d=A..B} q(d) 2^(W (B - d)) of the diagonal sums
+// q(d) of a slice product (Horner's sum of its diagonals), two diagonals per
+// 32-bit multiply-add: every |q(d)| is at most 9 x 112 x 127^2 (W = 7) or
+// 10 x 272 x 63^2 (W = 6), so q(d) 2^W + q(d + 1) stays below 2^31.
+template <int W, int A, int B, class Q>
+FALCON_HD long long diag_sum(Q q) {
+  long long s = 0;
+#pragma unroll
+  for (int d = A; d + 1 <= B; d += 2) s += (long long)(q(d) * (1 << W) + q(d + 1)) * (1LL << (W * (B - d - 1)));
+  if constexpr (((B - A + 1) & 1) != 0) s += q(B);
+  return s;
+}
+
 }  // namespace falcon

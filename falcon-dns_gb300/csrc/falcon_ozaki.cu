@@ -271,14 +271,11 @@ __global__ void __launch_bounds__(32 * MT * NQ * (2 / NT), MINB) oz_mma_kernel(G
 #pragma unroll
       for (int j = 0; j < 2; ++j) {
         const int i = 2 * h + j;
-        long long H = 0, L = 0;
-#pragma unroll
-        for (int d = 0; d <= C::HD; ++d) H = H * (1 << W) + (long long)__float2int_rn(acc[d][nt][i]);
-#pragma unroll
-        for (int d = C::HD + 1; d <= C::D; ++d) L = L * (1 << W) + (long long)__float2int_rn(acc[d][nt][i]);
+        auto qd = [&](int d) { return __float2int_rn(acc[d][nt][i]); };
+        const long long H = oz_diag_sum<W, 0, C::HD>(qd), L = oz_diag_sum<W, C::HD + 1, C::D>(qd);
         const int fb = cex[n + j];
         const int kL = er + (fb - 1022) - 2 * C::MAGB + W * (2 * C::S - 2 - C::D);
-        double y = fb > 0 ? combine_rn(H, L, kL, W * (C::D - C::HD)) : 0.0;
+        double y = fb > 0 ? oz_recombine_2t(H, L, kL, W * (C::D - C::HD)) : 0.0;
         if (fb == 2047) y = __longlong_as_double(0x7ff8000000000000LL);  // Inf or NaN in the column
         out[j] = q.alpha != 1.0 ? q.alpha * y : y;
       }

@@ -82,8 +82,19 @@ __device__ __forceinline__ uint32_t oz_slice_pair(uint32_t lo0, uint32_t hi0, ui
 
 // The recombination of a slice product's two partial sums, H of the
 // leading diagonals and L of the rest: RN(H 2^(k + sh) + L 2^k), each sum
-// exact, one rounding, by integer instructions (combine_rn,
-// falcon_combine.h).
+// exact, one rounding: by integer instructions (combine_rn,
+// falcon_combine.h) where the FP64 pipe bounds the kernel (the DFT stages),
+// as two exact scalings and one FP64 add where it is idle (the
+// contraction epilogues, which are bound by integer work).  The same bits.
+__device__ __forceinline__ double oz_recombine_2t(long long H, long long L, int k, int sh) {
+  return i64_scaled(H, k + sh) + i64_scaled(L, k);
+}
+
+// The exact integer sum of the diagonal sums: diag_sum (falcon_combine.h).
+template <int W, int A, int B, class Q>
+__device__ __forceinline__ long long oz_diag_sum(Q q) {
+  return diag_sum<W, A, B>(q);
+}
 
 // fp16 slices of 9 bits for short sums (the DFT butterflies: at most 8
 // products per output): kDftS slices of kDftW bits hold 63 bits of each

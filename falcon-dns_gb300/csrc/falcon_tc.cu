@@ -270,15 +270,11 @@ __global__ void __launch_bounds__(448, 1) tc_gemm_kernel(const __grid_constant__
           double out[4];
 #pragma unroll
           for (int j = 0; j < 4; ++j) {
-            long long H = 0, L = 0;
-#pragma unroll
-            for (int d = 0; d <= C::HD; ++d) H = H * (1 << W) + (long long)__float2int_rn(__uint_as_float(v[d][j]));
-#pragma unroll
-            for (int d = C::HD + 1; d <= C::D; ++d)
-              L = L * (1 << W) + (long long)__float2int_rn(__uint_as_float(v[d][j]));
+            auto qd = [&](int d) { return __float2int_rn(__uint_as_float(v[d][j])); };
+            const long long H = oz_diag_sum<W, 0, C::HD>(qd), L = oz_diag_sum<W, C::HD + 1, C::D>(qd);
             const int fb = cex[c0 + j];
             const int kL = er + (fb - 1022) - 2 * C::MAGB + W * (2 * C::S - 2 - C::D);
-            double y = fb > 0 ? combine_rn(H, L, kL, W * (C::D - C::HD)) : 0.0;
+            double y = fb > 0 ? oz_recombine_2t(H, L, kL, W * (C::D - C::HD)) : 0.0;
             if (fb == 2047) y = __longlong_as_double(0x7ff8000000000000LL);  // Inf or NaN in the column
             out[j] = q.alpha != 1.0 ? q.alpha * y : y;
           }

@@ -1,6 +1,8 @@
-"""The integer-only recombination combine_rn (falcon-dns_gb300/csrc/
-falcon_combine.h) of the tensor-core contractions and DFT stages against
-the two-term form it replaces (two exact power-of-two scalings and one FP64
+"""The exact recombination helpers of falcon-dns_gb300/csrc/falcon_combine.h:
+diag_sum (the diagonal sums of a slice product, two per 32-bit
+multiply-add) against Horner's sum at the largest diagonal magnitudes of
+both slice formats, and the integer-only combine_rn of the tensor-core DFT
+stages against the two-term form (two exact power-of-two scalings and one FP64
 add): the same bits on random sums of every sign, on exact ties of the
 rounding (to nearest even), on cancellations to zero, at the edges of its
 exponent range and beyond them (where it takes the two-term form itself).
@@ -67,6 +69,33 @@ int main() {
     check(H, 0, -50, sh);
     check(0, H, -50, sh);
   }
+  // diag_sum against Horner's sum for both slice formats and their splits,
+  // diagonals at their largest magnitudes included
+  long long dbad = 0, dchecked = 0;
+  auto horner = [](const int* q, int a, int b, int w) {
+    long long s = 0;
+    for (int d = a; d <= b; ++d) s = s * (1LL << w) + q[d];
+    return s;
+  };
+  const int m7 = 9 * 112 * 127 * 127, m6 = 10 * 272 * 63 * 63;
+  for (int it = 0; it < 400000; ++it) {
+    int q[10];
+    const int w = (it & 1) ? 7 : 6, m = w == 7 ? m7 : m6;
+    for (int d = 0; d < 10; ++d) {
+      const unsigned long long r = rng();
+      q[d] = (r % 8 == 0) ? ((r & 8) ? m : -m) : (int)(r % (2ull * m + 1)) - m;
+    }
+    auto Q = [&](int d) { return q[d]; };
+    long long h, l, hh, ll;
+    if (w == 7) { h = diag_sum<7, 0, 3>(Q); l = diag_sum<7, 4, 8>(Q); hh = horner(q, 0, 3, 7); ll = horner(q, 4, 8, 7); }
+    else { h = diag_sum<6, 0, 4>(Q); l = diag_sum<6, 5, 9>(Q); hh = horner(q, 0, 4, 6); ll = horner(q, 5, 9, 6); }
+    dchecked += 2;
+    if (h != hh || l != ll) {
+      if (dbad < 5) std::printf("DIAG MISMATCH w=%d\n", w);
+      ++dbad;
+    }
+  }
+  std::printf("%lld %lld\n", dchecked, dbad);
   std::printf("%lld %lld %lld\n", checked, fast, bad);
   return 0;
 }
@@ -81,6 +110,11 @@ def harness(tmp_path_factory):
     subprocess.run(["g++", "-O2", "-std=c++17", "-I" + os.path.join(PKG, "csrc"), str(d / "h.cpp"), "-o", str(exe)],
                    check=True)
     return subprocess.run([str(exe)], check=True, capture_output=True, text=True, timeout=300).stdout
+
+
+def test_pairwise_diagonal_sums_equal_horner(harness):
+    dchecked, dbad = (int(x) for x in harness.strip().splitlines()[-2].split())
+    assert dbad == 0 and dchecked == 800_000, harness
 
 
 def test_combine_rn_is_bit_identical_to_the_two_term_form(harness):
