@@ -256,6 +256,7 @@ __global__ void __launch_bounds__(32 * MT * NQ * (2 / NT), MINB) oz_mma_kernel(G
     __syncthreads();  // every warp is done with this buffer before it is refilled
   }
   // recombination: Y = 2^kH H + 2^kL L (OzCfg), exact scalings and one FP64 add
+  const bool scale_y = q.alpha != 1.0;  // one FP64 compare, not one per output
   const int* aex = q.oz_ex + (size_t)z * q.oz_rowsP + q.oz_row0;
   const int* cex = FX ? cex_s - col0 : q.oz_cexp + (size_t)z * q.oz_Np;
   double* Y = q.Y + (size_t)z * q.sY;
@@ -277,7 +278,7 @@ __global__ void __launch_bounds__(32 * MT * NQ * (2 / NT), MINB) oz_mma_kernel(G
         const int kL = er + (fb - 1022) - 2 * C::MAGB + W * (2 * C::S - 2 - C::D);
         double y = fb > 0 ? oz_recombine_2t(H, L, kL, W * (C::D - C::HD)) : 0.0;
         if (fb == 2047) y = __longlong_as_double(0x7ff8000000000000LL);  // Inf or NaN in the column
-        out[j] = q.alpha != 1.0 ? q.alpha * y : y;
+        out[j] = scale_y ? q.alpha * y : y;
       }
       double* yp = Y + (size_t)r * q.ldy + n;
       if (n + 1 < q.N) {

@@ -230,6 +230,7 @@ __global__ void __launch_bounds__(448, 1) tc_gemm_kernel(const __grid_constant__
     // 12h..12h+11 of the tile; waits are taken by lane 0 and broadcast, so a
     // warp leaves together (tcgen05.ld is warp-collective)
     const int qd = warp & 3, half = warp >> 2;
+    const bool scale_y = q.alpha != 1.0;  // one FP64 compare, not one per output
     long u = 0;
     for (long t = t_begin; t < t_end; ++t, ++u) {
       const TileIdx ti = tile_of(t, n_mt, n_nt);
@@ -276,7 +277,7 @@ __global__ void __launch_bounds__(448, 1) tc_gemm_kernel(const __grid_constant__
             const int kL = er + (fb - 1022) - 2 * C::MAGB + W * (2 * C::S - 2 - C::D);
             double y = fb > 0 ? oz_recombine_2t(H, L, kL, W * (C::D - C::HD)) : 0.0;
             if (fb == 2047) y = __longlong_as_double(0x7ff8000000000000LL);  // Inf or NaN in the column
-            out[j] = q.alpha != 1.0 ? q.alpha * y : y;
+            out[j] = scale_y ? q.alpha * y : y;
           }
           const int n = n0 + c0;
           double* yp = yrow + n;
