@@ -5,8 +5,7 @@ subs and their operator sets refreshed, graphs dropped and recaptured)
 dozens of times while other groups keep stepping on their streams.  Every
 request must reach its horizon with the state of the same request run
 alone (to FP64 rounding: the contraction paths of the changing group sizes
-may differ from the lone run's), and the server must account its device
-budget back to zero operator sets in use."""
+may differ from the lone run's)."""
 import numpy as np
 import pytest
 
