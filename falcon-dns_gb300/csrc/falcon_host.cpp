@@ -1596,19 +1596,106 @@ int gemm(Group* g, int cls, const GemmArgs& q0, bool reuse = false) {
   return run_path(g, cls, q, path, reuse);
 }
 
+// The merged tcgen05 launch of the row blocks v (one X, outputs after one
+// another), from the merged view `all`.
+int run_merged_tc(Group* g, int cls, const std::vector<GemmArgs>& v, const GemmArgs& all) {
+  TcArgs t = tc_args(all);
+  t.nout = (int)v.size();
+  int r = 0;
+  for (size_t o = 0; o < v.size(); ++o) {
+    r += v[o].rows;
+    t.rend[o] = r;
+    t.Y[o] = v[o].Y;
+  }
+  const CUtensorMap* map = static_cast<const CUtensorMap*>(all.oz_tmap);
+  return launch(g, cls, gemm_flops(all), [&]() { return launch_tc_gemm(t, *map, g->stream); });
+}
+
+// Mode 4, row blocks narrower than 16 columns per batch entry: one merged
+// tcgen05 launch, or the blocks one after another on their own (autotuned)
+// paths, whichever measures faster (the blocks unless the merged launch is
+// 10 % faster) with the autotuner's method; cached under per_mode = 2 + the
+// number of blocks (path 2: merged, 0: the blocks).  The blocks run once
+// untimed first, so that their own paths are measured before they are
+// timed together.
+int tuned_merge(Group* g, int cls, const std::vector<GemmArgs>& v, const GemmArgs& all, bool* merged) {
+  *merged = false;
+  TuneKey k{device_tag(), all.rows, all.K, all.N, all.batch, all.oz_w, 2 + (int)v.size(), 0};
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune.find(k);
+    if (it != g_tune.end()) {
+      *merged = it->second.path == PATH_TC;
+      return 0;
+    }
+  }
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  CK(cudaStreamIsCapturing(g->stream, &cs));
+  if (cs != cudaStreamCaptureStatusNone || g->prof) return 0;
+  void* flush = tune_flush_buffer();
+  if (!flush) return fail(FALCON_ENOMEM, "contraction tuning: no device memory for the L2 flush buffer");
+  auto blocks = [&]() {
+    for (size_t o = 0; o < v.size(); ++o) {
+      const int rc = gemm(g, cls, v[o], o > 0);
+      if (rc) return rc;
+    }
+    return 0;
+  };
+  int rc0 = blocks();  // the blocks' own paths, measured where new
+  if (rc0) return rc0;
+  auto one = [&]() { return run_merged_tc(g, cls, v, all); };
+  TuneEntry e{};
+  e.us[PATH_MMA] = -1.f;
+  CK(cudaDeviceSynchronize());
+  cudaEvent_t a = nullptr, b = nullptr;
+  CK(cudaEventCreate(&a));
+  CK(cudaEventCreate(&b));
+  int rc = 0;
+  for (int p : {PATH_FMA, PATH_TC}) {
+    auto run = [&]() { return p == PATH_TC ? one() : blocks(); };
+    if ((rc = run())) break;
+    float fastest = 0.f;
+    for (int r = 0; r < 3 && !rc; ++r) {
+      float ms = 0.f;
+      if (cudaMemsetAsync(flush, r + 1, kTuneFlushBytes, g->stream) != cudaSuccess ||
+          cudaEventRecord(a, g->stream) != cudaSuccess) {
+        rc = fail(FALCON_ECUDA, "tuning: flush or event");
+        break;
+      }
+      if ((rc = run())) break;
+      if (cudaEventRecord(b, g->stream) != cudaSuccess || cudaEventSynchronize(b) != cudaSuccess ||
+          cudaEventElapsedTime(&ms, a, b) != cudaSuccess) {
+        rc = fail(FALCON_ECUDA, "tuning timing");
+        break;
+      }
+      if (r == 0 || ms < fastest) fastest = ms;
+    }
+    if (rc) break;
+    e.us[p] = fastest * 1000.f;
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  if (rc) return rc;
+  e.path = e.us[PATH_TC] * 1.1f < e.us[PATH_FMA] ? PATH_TC : PATH_FMA;
+  g_tune_measured++;
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tune[k] = e;
+  tune_store_locked(k, e);
+  *merged = e.path == PATH_TC;
+  return 0;
+}
+
 // Consecutive row blocks of one operator applied to one X, each written to
 // its own output (G: omega, psi, u_phi; LAP: psi, u_phi and the two wall
 // vorticity rows).  With the tcgen05 contractions they run as one launch
 // over all the rows (fewer, fuller 128-row tiles, X sliced once), unless an
 // output overlaps X (then a later block reads what an earlier one wrote,
-// and the blocks run one after another as before).
+// and the blocks run one after another as before).  Blocks narrower than
+// 16 columns merge under mode 3, and under mode 4 where measured faster.
 int gemm_blocks(Group* g, int cls, std::initializer_list<GemmArgs> blocks) {
   const std::vector<GemmArgs> v(blocks);
   const int mode = g_gemm_mode.load();
-  // (narrow blocks merge only when every contraction goes to tcgen05, mode
-  // 3: a merged launch of 2-14 columns per 24-column tile is slower than
-  // the blocks on the FMA or mma.sync paths)
-  if (mode >= 2 && g->oz_xs && !v.empty() && v.size() <= 4 && (v[0].N >= 16 || mode == 3)) {
+  if (mode >= 2 && g->oz_xs && !v.empty() && v.size() <= 4 && (v[0].N >= 16 || mode >= 3)) {
     const GemmArgs& f = v[0];
     const char* x0 = reinterpret_cast<const char*>(f.X);
     const char* x1 = reinterpret_cast<const char*>(f.X + (size_t)(f.batch - 1) * f.sX + (size_t)f.K * f.ldx);
@@ -1628,18 +1715,13 @@ int gemm_blocks(Group* g, int cls, std::initializer_list<GemmArgs> blocks) {
       all.oz_s = nullptr;
       all.oz_xs = nullptr;
       const bool ok = attach_group(g, &all);
-      if (ok && all.oz_tmap && (mode == 3 || tc_worth_it(all))) {
-        TcArgs t = tc_args(all);
-        t.nout = (int)v.size();
-        int r = 0;
-        for (size_t o = 0; o < v.size(); ++o) {
-          r += v[o].rows;
-          t.rend[o] = r;
-          t.Y[o] = v[o].Y;
-        }
-        const CUtensorMap* map = static_cast<const CUtensorMap*>(all.oz_tmap);
-        return launch(g, cls, gemm_flops(all), [&]() { return launch_tc_gemm(t, *map, g->stream); });
+      bool use = ok && all.oz_tmap && (mode == 3 || tc_worth_it(all));
+      if (use && mode == 4 && f.N < 16) {
+        g->oz_key.valid = false;  // the blocks' own X slicing starts afresh
+        const int rc = tuned_merge(g, cls, v, all, &use);
+        if (rc) return rc;
       }
+      if (use) return run_merged_tc(g, cls, v, all);
     }
   }
   for (size_t o = 0; o < v.size(); ++o) {

@@ -400,7 +400,9 @@ int falcon_set_gemm_mode(int mode);
  * device = CUDA device name with blanks as '_' plus "_sm<SM count>"
  * (falcon_device_tag); rows, K, N, batch = the contraction's shape (rows x K
  * operator, N columns per batch entry); w = slice format in bits (6 or 7);
- * per_mode = 1 when every batch entry has its own columns; reuse = 1 when
+ * per_mode = 1 when every batch entry has its own columns (2 + n: n row
+ * blocks of one operator narrower than 16 columns, merged into one tcgen05
+ * launch, path 2, or run one after another, path 0); reuse = 1 when
  * the X slice planes were made by the contraction before; path 0 FMA,
  * 1 mma.sync, 2 tcgen05; us_* = measured microseconds per contraction (-1:
  * path not available).  NULL or "" detaches the file (decisions stay in

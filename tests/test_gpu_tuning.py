@@ -74,6 +74,10 @@ def test_tuned_runs_are_reproducible_and_pick_the_fastest(fg, tuned):
     for d, (r, K, N, batch, w, per_mode, reuse, path), us in rows:
         assert d == dev
         avail = [t for t in us if t >= 0]
+        if per_mode >= 2:   # narrow row blocks: one tcgen05 launch (2) or the blocks (0)
+            assert path in (0, 2) and us[0] > 0 and us[2] > 0
+            assert us[path] <= 1.1 * min(avail), (r, K, N, batch, us, path)
+            continue
         assert us[0] > 0 and us[1] > 0                       # FMA and mma.sync always measured
         # the fastest, or the fixed rule's path within 10 % of it
         assert us[path] <= 1.1 * min(avail), (r, K, N, batch, us, path)
