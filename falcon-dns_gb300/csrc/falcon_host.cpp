@@ -1308,7 +1308,10 @@ TcArgs tc_args(const GemmArgs& q) {
 // the tcgen05 kernel (PATH_TC).  PATH_MMA and PATH_TC give the same bits;
 // PATH_FMA differs from them by rounding (all are FP64-accurate).
 // ---------------------------------------------------------------------------
-enum { PATH_FMA = 0, PATH_MMA = 1, PATH_TC = 2, PATH_COUNT = 3 };
+// PATH_FMA16/32/64: the FMA tiles with the best tile shape of that column
+// width (the same bits as PATH_FMA, whose shape a cost model picks).
+enum { PATH_FMA = 0, PATH_MMA = 1, PATH_TC = 2, PATH_FMA16 = 3, PATH_FMA32 = 4, PATH_FMA64 = 5, PATH_COUNT = 6 };
+inline bool is_fma_path(int p) { return p == PATH_FMA || p >= PATH_FMA16; }
 
 // Slice planes of q.X for the mma.sync kernel when it does not slice X
 // itself (made unless `reuse` finds them already made for the same X).
@@ -1362,9 +1365,10 @@ int run_path_once(Group* g, int cls, GemmArgs q, int path, bool reuse) {
     if (rc) return rc;
     if (!fits) path = PATH_FMA;
   }
-  if (path == PATH_FMA) {
+  if (is_fma_path(path)) {
     q.oz_s = nullptr;
     q.oz_xs = nullptr;
+    q.fma_ncol = path == PATH_FMA16 ? 16 : path == PATH_FMA32 ? 32 : path == PATH_FMA64 ? 64 : 0;
   }
   return launch(g, cls, gemm_flops(q), [&]() { return launch_gemm(q, g->stream); });
 }
@@ -1372,14 +1376,15 @@ int run_path_once(Group* g, int cls, GemmArgs q, int path, bool reuse) {
 // The autotuner's decisions, per device and contraction shape: the path
 // measured fastest the first time the shape ran (outside graph capture),
 // kept for the process and, with a cache file, across processes.  Cache file
-// (text): a header line "falcon-contraction-tuning 1", then one decision per
+// (text): a header line "falcon-contraction-tuning 2", then one decision per
 // line:
-//   <device> <rows> <K> <N> <batch> <w> <per_mode> <reuse> <path> <us_fma> <us_mma> <us_tc>
+//   <device> <rows> <K> <N> <batch> <w> <per_mode> <reuse> <path> <us_0> ... <us_5>
 // device = the CUDA device name with blanks as '_' and "_sm<SM count>";
 // per_mode = 1 when the batch entries have their own X (sX != 0); reuse = 1
 // when X's slice planes were made by the contraction before; w = the slice
-// format (6 or 7); path 0 FMA, 1 mma.sync, 2 tcgen05; the times are the
-// measured microseconds per contraction (-1: candidate not available).
+// format (6 or 7); path 0 FMA (cost-model tile shape), 1 mma.sync, 2
+// tcgen05, 3/4/5 FMA with tiles of 16/32/64 columns; us_p = the measured
+// microseconds per contraction on path p (-1: not measured).
 struct TuneKey {
   std::string dev;
   int rows, K, N, batch, w, per_mode, reuse;
@@ -1394,7 +1399,7 @@ std::map<TuneKey, TuneEntry> g_tune;
 std::string g_tune_path;          // cache file ("" none)
 bool g_tune_env_checked = false;
 std::atomic<long long> g_tune_measured(0);
-constexpr const char* kTuneHeader = "falcon-contraction-tuning 1";
+constexpr const char* kTuneHeader = "falcon-contraction-tuning 2";
 
 int tune_load_locked(const std::string& path) {
   std::ifstream f(path);
@@ -1408,9 +1413,9 @@ int tune_load_locked(const std::string& path) {
     std::istringstream is(line);
     TuneKey k;
     TuneEntry e;
-    if (!(is >> k.dev >> k.rows >> k.K >> k.N >> k.batch >> k.w >> k.per_mode >> k.reuse >> e.path >> e.us[0] >>
-          e.us[1] >> e.us[2]) ||
-        e.path < 0 || e.path >= PATH_COUNT || k.rows <= 0 || k.K <= 0 || k.N <= 0 || k.batch <= 0)
+    bool good = (bool)(is >> k.dev >> k.rows >> k.K >> k.N >> k.batch >> k.w >> k.per_mode >> k.reuse >> e.path);
+    for (int p = 0; p < PATH_COUNT && good; ++p) good = (bool)(is >> e.us[p]);
+    if (!good || e.path < 0 || e.path >= PATH_COUNT || k.rows <= 0 || k.K <= 0 || k.N <= 0 || k.batch <= 0)
       return fail(FALCON_EINVAL, "tuning cache " + path + ": malformed line " + std::to_string(n + 2));
     g_tune[k] = e;
     ++n;
@@ -1424,8 +1429,10 @@ void tune_store_locked(const TuneKey& k, const TuneEntry& e) {
   if (!f) return;
   std::fseek(f, 0, SEEK_END);
   if (std::ftell(f) == 0) std::fprintf(f, "%s\n", kTuneHeader);
-  std::fprintf(f, "%s %d %d %d %d %d %d %d %d %.3f %.3f %.3f\n", k.dev.c_str(), k.rows, k.K, k.N, k.batch, k.w,
-               k.per_mode, k.reuse, e.path, e.us[0], e.us[1], e.us[2]);
+  std::fprintf(f, "%s %d %d %d %d %d %d %d %d", k.dev.c_str(), k.rows, k.K, k.N, k.batch, k.w, k.per_mode, k.reuse,
+               e.path);
+  for (int p = 0; p < PATH_COUNT; ++p) std::fprintf(f, " %.3f", e.us[p]);
+  std::fprintf(f, "\n");
   std::fclose(f);
 }
 
@@ -1517,6 +1524,7 @@ int tuned_path(Group* g, int cls, const GemmArgs& q, bool reuse, bool tc_ok, int
   for (int p = 0; p < PATH_COUNT && !rc; ++p) {
     e.us[p] = -1.f;
     if (p == PATH_TC && !tc_ok) continue;
+    if (p >= PATH_FMA16 && q.N <= 8) continue;  // one-warp GEMV, no tile shapes
     if ((rc = run_path(g, cls, q, p, reuse))) break;
     float fastest = 0.f;
     for (int r = 0; r < 3 && !rc; ++r) {
@@ -1614,7 +1622,9 @@ int run_merged_tc(Group* g, int cls, const std::vector<GemmArgs>& v, const GemmA
 // Mode 4, row blocks narrower than 16 columns per batch entry: one merged
 // tcgen05 launch, or the blocks one after another on their own (autotuned)
 // paths, whichever measures faster (the blocks unless the merged launch is
-// 10 % faster) with the autotuner's method; cached under per_mode = 2 + the
+// 25 % faster: in a step graph the merged launch's 215 KB shared-memory
+// configuration costs more than its isolated timing shows) with the
+// autotuner's method; cached under per_mode = 2 + the
 // number of blocks (path 2: merged, 0: the blocks).  The blocks run once
 // untimed first, so that their own paths are measured before they are
 // timed together.
@@ -1645,7 +1655,7 @@ int tuned_merge(Group* g, int cls, const std::vector<GemmArgs>& v, const GemmArg
   if (rc0) return rc0;
   auto one = [&]() { return run_merged_tc(g, cls, v, all); };
   TuneEntry e{};
-  e.us[PATH_MMA] = -1.f;
+  for (float& t : e.us) t = -1.f;
   CK(cudaDeviceSynchronize());
   cudaEvent_t a = nullptr, b = nullptr;
   CK(cudaEventCreate(&a));
@@ -1676,7 +1686,7 @@ int tuned_merge(Group* g, int cls, const std::vector<GemmArgs>& v, const GemmArg
   cudaEventDestroy(a);
   cudaEventDestroy(b);
   if (rc) return rc;
-  e.path = e.us[PATH_TC] * 1.1f < e.us[PATH_FMA] ? PATH_TC : PATH_FMA;
+  e.path = e.us[PATH_TC] * 1.25f < e.us[PATH_FMA] ? PATH_TC : PATH_FMA;
   g_tune_measured++;
   std::lock_guard<std::mutex> lk(g_tune_mu);
   g_tune[k] = e;

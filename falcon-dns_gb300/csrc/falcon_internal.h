@@ -143,6 +143,10 @@ struct GemmArgs {
   // this GEMM's first batch entry in it, for the tcgen05 kernel
   const void* oz_tmap;
   int oz_z0;
+  // FP64 FMA tiles (no slice view): 0 = the tile shape of the cost model,
+  // 16 / 32 / 64 = the cost model's best shape of that column width (every
+  // shape sums each output over k in the same order: the same bits)
+  int fma_ncol;
 };
 
 // ---- FP64 GEMM on bf16 tensor cores by exact slicing (falcon_ozaki.cu) ----

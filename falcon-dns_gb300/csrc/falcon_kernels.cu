@@ -1186,6 +1186,7 @@ static TileShape pick_shape(const GemmArgs& g, int nsm) {
   double bcost = 1e300;
   int brpt = 0;
   for (int ncol = 16; ncol <= 64; ncol *= 2) {
+    if (g.fma_ncol && ncol != g.fma_ncol) continue;
     const int rg = 64 / ncol, maxr = (ncol == 64) ? 16 : 8;
     const long cb = (long)((g.N + ncol - 1) / ncol) * g.batch;
     for (int rb = 1; rb <= 16; ++rb)
@@ -1259,22 +1260,24 @@ cudaError_t launch_gemm(const GemmArgs& g, cudaStream_t s) {
     if (nsm <= 0) nsm = 152;
     if (dev >= 0 && dev < 64) nsm_dev[dev] = nsm;
   }
-  // shapes are memoised per (rows, N, batch, SM count): the search runs on
-  // the host once per problem size
-  struct Memo { int rows, N, batch, nsm; TileShape t; };
+  // shapes are memoised per (rows, N, batch, SM count, column width asked
+  // for): the search runs on the host once per problem size
+  struct Memo { int rows, N, batch, nsm, ncol; TileShape t; };
   thread_local std::unordered_map<unsigned long long, Memo> memo;
   // (a hash; the entry is checked against the full sizes)
   const unsigned long long key = (unsigned long long)(g.rows & 0xfff) | ((unsigned long long)(g.N & 0xffffff) << 12) |
                                  ((unsigned long long)(g.batch & 0xffff) << 36) |
-                                 ((unsigned long long)(nsm & 0xfff) << 52);
+                                 ((unsigned long long)(nsm & 0x3ff) << 52) |
+                                 ((unsigned long long)(g.fma_ncol == 0 ? 0 : g.fma_ncol == 16 ? 1 : g.fma_ncol == 32 ? 2 : 3)
+                                  << 62);
   auto it = memo.find(key);
   TileShape t;
   if (it != memo.end() && it->second.rows == g.rows && it->second.N == g.N && it->second.batch == g.batch &&
-      it->second.nsm == nsm) {
+      it->second.nsm == nsm && it->second.ncol == g.fma_ncol) {
     t = it->second.t;
   } else {
     t = pick_shape(g, nsm);
-    memo[key] = Memo{g.rows, g.N, g.batch, nsm, t};
+    memo[key] = Memo{g.rows, g.N, g.batch, nsm, g.fma_ncol, t};
   }
   if (t.ncol == 16) return launch_ncol<16>(g, t, s);
   if (t.ncol == 32) return launch_ncol<32>(g, t, s);

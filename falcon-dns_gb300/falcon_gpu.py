@@ -518,7 +518,7 @@ def set_gemm_mode(mode):
     return lib().falcon_set_gemm_mode(int(mode))
 
 
-PATHS = ("fma", "mma_sync", "tcgen05")
+PATHS = ("fma", "mma_sync", "tcgen05", "fma_ncol16", "fma_ncol32", "fma_ncol64")
 
 
 def set_tune_cache(path):
@@ -542,11 +542,11 @@ def tune_clear():
 def tune_lookup(device, rows, K, N, batch, w, per_mode, reuse):
     """The decision for one contraction shape: (path name, {path: microseconds})
     or None."""
-    us = (ctypes.c_float * 3)()
+    us = (ctypes.c_float * len(PATHS))()
     p = lib().falcon_tune_lookup(device.encode(), rows, K, N, batch, w, per_mode, reuse, us)
     if p < 0:
         return None
-    return PATHS[p], {PATHS[i]: float(us[i]) for i in range(3) if us[i] >= 0}
+    return PATHS[p], {PATHS[i]: float(us[i]) for i in range(len(PATHS)) if us[i] >= 0}
 
 
 def device_tag():

@@ -395,17 +395,19 @@ int falcon_set_gemm_mode(int mode);
 /* Contraction tuning cache of mode 4: decisions are read from `path` (if it
  * exists) and every new decision is appended to it, so that later processes
  * take the same paths without measuring.  Text format: the header line
- * "falcon-contraction-tuning 1", then one line per decision
- *   <device> <rows> <K> <N> <batch> <w> <per_mode> <reuse> <path> <us_fma> <us_mma> <us_tc>
+ * "falcon-contraction-tuning 2", then one line per decision
+ *   <device> <rows> <K> <N> <batch> <w> <per_mode> <reuse> <path> <us_0> <us_1> <us_2> <us_3> <us_4> <us_5>
  * device = CUDA device name with blanks as '_' plus "_sm<SM count>"
  * (falcon_device_tag); rows, K, N, batch = the contraction's shape (rows x K
  * operator, N columns per batch entry); w = slice format in bits (6 or 7);
  * per_mode = 1 when every batch entry has its own columns (2 + n: n row
  * blocks of one operator narrower than 16 columns, merged into one tcgen05
  * launch, path 2, or run one after another, path 0); reuse = 1 when
- * the X slice planes were made by the contraction before; path 0 FMA,
- * 1 mma.sync, 2 tcgen05; us_* = measured microseconds per contraction (-1:
- * path not available).  NULL or "" detaches the file (decisions stay in
+ * the X slice planes were made by the contraction before; path 0 FMA
+ * tiles of the cost model's shape, 1 mma.sync, 2 tcgen05, 3 / 4 / 5 FMA
+ * tiles of the best shape 16 / 32 / 64 columns wide (the same bits as 0);
+ * us_p = measured microseconds per contraction on path p (-1: not
+ * measured).  NULL or "" detaches the file (decisions stay in
  * memory).  The environment variable FALCON_TUNE_CACHE names a file when
  * this is not called.  Returns FALCON_EINVAL for a file with another
  * header or a malformed line. */
@@ -414,8 +416,8 @@ int falcon_set_tune_cache(const char* path);
 int falcon_tune_entries(long long* measured);
 /* Forget every decision held in memory (the file is kept); returns their number. */
 int falcon_tune_clear(void);
-/* The decision for one shape (path 0-2, -1 if none), with the measured times
- * (3 floats, may be NULL). */
+/* The decision for one shape (path 0-5, -1 if none), with the measured times
+ * (6 floats, may be NULL). */
 int falcon_tune_lookup(const char* device, int rows, int K, int N, int batch, int w, int per_mode, int reuse,
                        float* us);
 /* The device key of the tuning cache for the current device. */

@@ -1,7 +1,8 @@
 """The contraction autotuner (falcon_set_gemm_mode(4), the default): the first
 time a contraction shape runs outside graph capture every available path
-(FP64 FMA tiles, mma.sync slices, tcgen05 slices) is timed on it and the
-fastest is kept.  Checked here:
+(FP64 FMA tiles of the cost model's shape and of the best 16-, 32- and
+64-column shapes, mma.sync slices, tcgen05 slices where the contraction
+fills the GPU) is timed on it and the fastest is kept.  Checked here:
 
 - a run that measures gives the same bits as a later run that only reads
   the decisions (the chosen path runs last), in this process and in one
@@ -33,11 +34,11 @@ def run(fg, params, seeds, nsteps):
 
 def read_cache(path):
     lines = open(path).read().splitlines()
-    assert lines[0] == "falcon-contraction-tuning 1"
+    assert lines[0] == "falcon-contraction-tuning 2"
     rows = []
     for ln in lines[1:]:
         f = ln.split()
-        assert len(f) == 12, ln
+        assert len(f) == 15, ln
         rows.append((f[0], [int(x) for x in f[1:9]], [float(x) for x in f[9:]]))
     return rows
 
@@ -76,7 +77,7 @@ def test_tuned_runs_are_reproducible_and_pick_the_fastest(fg, tuned):
         avail = [t for t in us if t >= 0]
         if per_mode >= 2:   # narrow row blocks: one tcgen05 launch (2) or the blocks (0)
             assert path in (0, 2) and us[0] > 0 and us[2] > 0
-            assert us[path] <= 1.1 * min(avail), (r, K, N, batch, us, path)
+            assert us[path] <= 1.25 * min(avail), (r, K, N, batch, us, path)
             continue
         assert us[0] > 0 and us[1] > 0                       # FMA and mma.sync always measured
         # the fastest, or the fixed rule's path within 10 % of it
