@@ -1479,6 +1479,28 @@ void* tune_flush_buffer() {
   return b;
 }
 
+// The fastest of three timed runs of `run` (after one untimed run), each
+// after a write of the flush buffer that evicts L2, timed by CUDA events on
+// the group's stream: microseconds in *us.
+int time_fastest(Group* g, void* flush, cudaEvent_t a, cudaEvent_t b, const std::function<int()>& run, float* us) {
+  int rc = run();
+  if (rc) return rc;
+  float fastest = 0.f;
+  for (int r = 0; r < 3; ++r) {
+    float ms = 0.f;
+    if (cudaMemsetAsync(flush, r + 1, kTuneFlushBytes, g->stream) != cudaSuccess ||
+        cudaEventRecord(a, g->stream) != cudaSuccess)
+      return fail(FALCON_ECUDA, "tuning: flush or event");
+    if ((rc = run())) return rc;
+    if (cudaEventRecord(b, g->stream) != cudaSuccess || cudaEventSynchronize(b) != cudaSuccess ||
+        cudaEventElapsedTime(&ms, a, b) != cudaSuccess)
+      return fail(FALCON_ECUDA, "tuning timing");
+    if (r == 0 || ms < fastest) fastest = ms;
+  }
+  *us = fastest * 1000.f;
+  return 0;
+}
+
 // The path of a contraction under mode 4: the cached decision, or a
 // measurement of every available path (each run once to warm up, then three
 // times with L2 flushed before each, timed by CUDA events on the group's
@@ -1525,25 +1547,7 @@ int tuned_path(Group* g, int cls, const GemmArgs& q, bool reuse, bool tc_ok, int
     e.us[p] = -1.f;
     if (p == PATH_TC && !tc_ok) continue;
     if (p >= PATH_FMA16 && q.N <= 8) continue;  // one-warp GEMV, no tile shapes
-    if ((rc = run_path(g, cls, q, p, reuse))) break;
-    float fastest = 0.f;
-    for (int r = 0; r < 3 && !rc; ++r) {
-      float ms = 0.f;
-      if (cudaMemsetAsync(flush, r + 1, kTuneFlushBytes, g->stream) != cudaSuccess ||
-          cudaEventRecord(a, g->stream) != cudaSuccess) {
-        rc = fail(FALCON_ECUDA, "tuning: flush or event");
-        break;
-      }
-      if ((rc = run_path(g, cls, q, p, reuse))) break;
-      if (cudaEventRecord(b, g->stream) != cudaSuccess || cudaEventSynchronize(b) != cudaSuccess ||
-          cudaEventElapsedTime(&ms, a, b) != cudaSuccess) {
-        rc = fail(FALCON_ECUDA, "tuning timing");
-        break;
-      }
-      if (r == 0 || ms < fastest) fastest = ms;
-    }
-    if (rc) break;
-    e.us[p] = fastest * 1000.f;
+    if ((rc = time_fastest(g, flush, a, b, [&]() { return run_path(g, cls, q, p, reuse); }, &e.us[p]))) break;
     if (p == PATH_FMA || e.us[p] < best) {
       best = e.us[p];
       e.path = p;
@@ -1660,29 +1664,8 @@ int tuned_merge(Group* g, int cls, const std::vector<GemmArgs>& v, const GemmArg
   cudaEvent_t a = nullptr, b = nullptr;
   CK(cudaEventCreate(&a));
   CK(cudaEventCreate(&b));
-  int rc = 0;
-  for (int p : {PATH_FMA, PATH_TC}) {
-    auto run = [&]() { return p == PATH_TC ? one() : blocks(); };
-    if ((rc = run())) break;
-    float fastest = 0.f;
-    for (int r = 0; r < 3 && !rc; ++r) {
-      float ms = 0.f;
-      if (cudaMemsetAsync(flush, r + 1, kTuneFlushBytes, g->stream) != cudaSuccess ||
-          cudaEventRecord(a, g->stream) != cudaSuccess) {
-        rc = fail(FALCON_ECUDA, "tuning: flush or event");
-        break;
-      }
-      if ((rc = run())) break;
-      if (cudaEventRecord(b, g->stream) != cudaSuccess || cudaEventSynchronize(b) != cudaSuccess ||
-          cudaEventElapsedTime(&ms, a, b) != cudaSuccess) {
-        rc = fail(FALCON_ECUDA, "tuning timing");
-        break;
-      }
-      if (r == 0 || ms < fastest) fastest = ms;
-    }
-    if (rc) break;
-    e.us[p] = fastest * 1000.f;
-  }
+  int rc = time_fastest(g, flush, a, b, blocks, &e.us[PATH_FMA]);
+  if (!rc) rc = time_fastest(g, flush, a, b, one, &e.us[PATH_TC]);
   cudaEventDestroy(a);
   cudaEventDestroy(b);
   if (rc) return rc;
