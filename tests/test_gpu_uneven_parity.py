@@ -4,7 +4,9 @@ Ra log-uniform; dt = 0.2 x the t=0 CFL estimate), restricted to the grids
 the oracle steps in seconds (Nr 33 and 65, Ntheta 128 and 256), stepped
 100 times as groups of one grid, dt and scheme with mixed Pr on the default
 autotuned contraction paths, every instance against the oracle (relative
-spectral error <= 1e-10)."""
+spectral error <= 1e-10; omega of the not stiffly accurate ARS343 within
+ten times the oracle's own sensitivity to a 1e-16 perturbation, as on the
+Nr = 129 grid)."""
 import os
 import sys
 
@@ -39,6 +41,18 @@ def test_uneven_mix_matches_oracle_after_100_steps(fg, orc):
         o.init_noise(seed)
         o.step(100)
         got, want = b.get_state(i), o.get_state()
-        errs = {k: rel(got[k], want[k]) for k in ("T", "omg", "up", "ur")}
-        assert max(errs.values()) < 1e-10, (i, nr, nm, s, pr, errs)
+        tol = {k: 1e-10 for k in ("T", "omg", "up", "ur")}
+        if s == "ARS343":
+            # not stiffly accurate: the psi Poisson solve with Johnston's
+            # wall vorticity amplifies rounding; omega is held to ten times
+            # the oracle's own change under a 1e-16 perturbation of T
+            q = orc.Sim(orc.make_params(nr, nm, s, ra=ra, dt=dt, pr=pr))
+            q.init_noise(seed)
+            st = q.get_state()
+            pert = np.random.default_rng(1).standard_normal(st["T"].shape)
+            q.set_state(st["T"] * (1.0 + 1e-16 * pert), st["omg"], st["up"], st["ur"])
+            q.step(100)
+            tol["omg"] = max(1e-10, 10.0 * rel(q.get_state()["omg"], want["omg"]))
+        errs = {k: rel(got[k], want[k]) for k in tol}
+        assert all(errs[k] < tol[k] for k in tol), (i, nr, nm, s, pr, errs, tol)
     b.close()
