@@ -428,6 +428,10 @@ def run_gpu(args):
     fg.lib()
     stream = torch.cuda.Stream()
     fg.set_gemm_mode(args.gemm_mode)
+    if args.uneven_only:  # profiling captures of the uneven batch
+        if rank == 0:
+            print(json.dumps({"uneven_batch": run_uneven(args, fg, stream, torch)}), flush=True)
+        return
     W = WORKLOAD
     n = args.instances or W["n"]
     ras, seeds = shard(rank, n)
@@ -633,6 +637,8 @@ def main():
     ap.add_argument("--cpu-seconds", dest="cpu_seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", dest="no_cpu", action="store_true")
     ap.add_argument("--no-mixed", dest="no_mixed", action="store_true", help="skip the uneven batch and serving")
+    ap.add_argument("--uneven-only", dest="uneven_only", action="store_true",
+                    help="the uneven batch alone (profiling captures)")
     ap.add_argument("--uniform-only", dest="uniform_only", action="store_true",
                     help="the uniform batch alone (profiling captures): no e2e, one-at-a-time, plain, single, mixed")
     ap.add_argument("--single-steps", dest="single_steps", type=int, default=200)
