@@ -87,6 +87,39 @@ FALCON_HD double combine_rn(long long H, long long L, int k, int sh) {
                         (mant & ((1ull << 52) - 1ull)));
 }
 
+FALCON_HD long long bits_of_double(double a) {
+#ifdef __CUDA_ARCH__
+  return __double_as_longlong(a);
+#else
+  long long b;
+  memcpy(&b, &a, sizeof b);
+  return b;
+#endif
+}
+
+// a 2^(FB - e) truncated toward zero, as a signed integer, for |a| < 2^e
+// (so below 2^FB in magnitude; FB <= 62); zero and subnormal a give 0.
+// The fixed-point form of the DFT stages: every value of a butterfly at
+// the scale of its largest, so sums and differences are exact integer adds.
+template <int FB>
+FALCON_HD long long fix_of(double a, int e) {
+  const long long bits = bits_of_double(a);
+  const int eb = (int)((bits >> 52) & 0x7ff);
+  if (eb == 0) return 0;
+  const unsigned long long m = (unsigned long long)(bits & 0xfffffffffffffLL) | (1ull << 52);
+  const int sh = eb - 1075 + FB - e;  // <= FB - 53 because |a| < 2^e
+  unsigned long long t;
+  if (sh >= 0) t = m << sh;
+  else if (sh <= -64) t = 0ull;
+  else t = m >> (-sh);
+  return bits < 0 ? -(long long)t : (long long)t;
+}
+
+// RN(v 2^k) for any 64-bit v (its two halves through combine_rn).
+FALCON_HD double dbl_of_fix(long long v, int k) {
+  return combine_rn(v >> 26, v & ((1LL << 26) - 1), k, 26);
+}
+
 // The exact integer sum_{d=A..B} q(d) 2^(W (B - d)) of the diagonal sums
 // q(d) of a slice product (Horner's sum of its diagonals), two diagonals per
 // 32-bit multiply-add: every |q(d)| is at most 9 x 112 x 127^2 (W = 7) or

@@ -353,38 +353,49 @@ __device__ void fft_stage_split(double2* A, double2* Bf, int P, int m, int tid, 
 }
 
 // Odd-prime stage (p = 11, 13, 17, so h = (p - 1)/2 <= 8) of a prime-factor
-// plan on the fp16 tensor cores, by exact integer slicing.  In the
-// symmetric form of dft_odd_store the butterfly's FP64 work is the 2h real
-// sums A_j = sum_q a_q cos(2 pi jq/p) and B_j = sum_q b_q sin(2 pi jq/p),
-// a_q = v_q + v_{p-q}, b_q = v_q - v_{p-q}: per component, one product of
-// the block-diagonal [C 0; 0 S] (rows j; K = the h values a_q, then the h
-// values b_q) with a column.  One m16n8k16 MMA per slice pair takes 8
-// columns, 4 butterflies x (re, im).  Each operand is cut into kDftS = 7
-// signed 9-bit slices (63 bits; fp16 holds them exactly) relative to its
-// row's (coefficients) or column's (data) largest power of two, and the 28
-// pairs s + t <= 6 are summed in FP32: at most 8 products per output keep
-// every sum exact, and the dropped terms are below 2^-59 of the largest
-// product, so the outputs are the exact sums rounded once to FP64.  A butterfly's outputs depend only on its inputs, so any tiling
-// (warp or block form) gives the same bits.  Lane (g, t) of a tile forms
-// a_q, b_q for q = 2t + 1, 2t + 2 of column g and receives A_{g+1}, B_{g+1}
-// of butterfly t, re and im, from which it stores y_j = A_j - i B_j and
-// y_{p-j} = A_j + i B_j; the y_0 sums are FP64.  FP64 instructions per tile
-// and lane: ~18, against ~42 for the same 4 butterflies in dft_odd_store.
-// Tiles over both buffers go to warps warp, warp + nw, ...; the caller
-// synchronises before (inputs complete) and after (outputs stored).
+// plan on the fp16 tensor cores, in fixed point: no FP64 arithmetic.  The
+// symmetric butterfly of dft_odd_store,
+//   y_0 = v_0 + sum a_q,  y_j = A_j - i B_j,  y_{p-j} = A_j + i B_j,
+//   A_j = v_0 + sum_q a_q cos(2 pi jq/p),  B_j = sum_q b_q sin(2 pi jq/p),
+//   a_q = v_q + v_{p-q},  b_q = v_q - v_{p-q},
+// with every value of a butterfly (both components) as an integer at the
+// scale of its largest, 2^e: V = trunc(v 2^(kDftFB - e)), |V| < 2^58.  The
+// pre-adds and the y_0 sum are then exact 64-bit integer adds (|y_0| <
+// 2^63), and A_j, B_j come from one product of the block-diagonal [C 0; 0 S]
+// (rows j; K = the h values a_q, then the h values b_q) with a column per
+// component: one m16n8k16 MMA per slice pair takes 8 columns, 4
+// butterflies x (re, im).  The coefficients (|cos|, |sin| < 1) and the
+// integers 2^4 a, 2^4 b (< 2^63) are cut into kDftS = 7 signed 9-bit slices
+// (fp16 holds them exactly), and the 28 pairs s + t <= 6 are summed in
+// FP32: at most 8 products per output keep every sum exact (7 pairs x 8
+// products x 511^2 < 2^24).  The diagonal sums give A_j - v_0 and B_j as
+// exact integers H 2^36 + L in units of 2^(e - 71); v_0 and the output
+// pairs A_j +- i B_j are added in those integers and each output is
+// rounded once to FP64 (combine_rn).  Errors: the inputs' truncation
+// (2^(e - 58) each), the dropped pairs (below 2^(e - 56) per output) and the
+// final rounding; a butterfly with an Inf or NaN gives NaN.  A butterfly's
+// outputs depend only on its inputs, so any tiling (warp or block form)
+// gives the same bits.  Lane (g, t) of a tile holds v_q, v_{p-q} for q =
+// 2t + 1, 2t + 2 and v_0 of column g, and receives A_{g+1}, B_{g+1} of
+// butterfly t, re and im, from which it stores y_j and y_{p-j}.  Tiles over
+// both buffers go to warps warp, warp + nw, ...; the caller synchronises
+// before (inputs complete) and after (outputs stored).
+constexpr int kDftFB = 58;
+
 template <int p>
 __device__ void dft_mma_stage(double2* A, double2* Bf, int P, int m, int lane, int warp, int nw) {
   constexpr int h = (p - 1) / 2;
   static_assert(h <= 8, "the block-diagonal form holds h <= 8");
   constexpr unsigned FULL = 0xffffffffu;
+  constexpr int UP = 63 - (kDftFB + 1);  // |a|, |b| < 2^(kDftFB + 1): 2^UP |a| < 2^63
   const int gid = lane >> 2, tig = lane & 3;
   const int nb = P / p, mp = m * p, nbt = 2 * nb, ntile = (nbt + 3) / 4;
   const float inv_m = 1.0f / (float)m;
   const int q1 = 2 * tig + 1, q2 = 2 * tig + 2;  // K rows 2t, 2t + 1 (a) and 2t + 8, 2t + 9 (b)
   const bool has1 = q1 <= h, has2 = q2 <= h;
-  // coefficient fragments: a0 = C(row g; q1, q2), a3 = S(row g; q1, q2), j = g + 1
+  // coefficient fragments: a0 = C(row g; q1, q2), a3 = S(row g; q1, q2), j = g + 1,
+  // as 63-bit fractions (every |cos|, |sin| here is below 1)
   uint32_t fc[kDftS], fs[kDftS];
-  int erc, ers;
   {
     const int j = gid + 1;
     double c1 = 0.0, c2 = 0.0, s1 = 0.0, s2 = 0.0;
@@ -392,17 +403,8 @@ __device__ void dft_mma_stage(double2* A, double2* Bf, int P, int m, int lane, i
       if (has1) { c1 = DftTab<p>::c((j * q1) % p); s1 = DftTab<p>::s((j * q1) % p); }
       if (has2) { c2 = DftTab<p>::c((j * q2) % p); s2 = DftTab<p>::s((j * q2) % p); }
     }
-    int mc = max(biased_exp(c1), biased_exp(c2)), ms = max(biased_exp(s1), biased_exp(s2));
-    mc = max(mc, __shfl_xor_sync(FULL, mc, 1));
-    mc = max(mc, __shfl_xor_sync(FULL, mc, 2));
-    ms = max(ms, __shfl_xor_sync(FULL, ms, 1));
-    ms = max(ms, __shfl_xor_sync(FULL, ms, 2));
-    erc = mc - 1022;
-    ers = ms - 1022;
-    const unsigned long long tc1 = dft_mag(c1, erc), tc2 = dft_mag(c2, erc), ts1 = dft_mag(s1, ers),
-                             ts2 = dft_mag(s2, ers);
-    const uint32_t sc = (__double_as_longlong(c1) < 0 ? 0x8000u : 0u) | (__double_as_longlong(c2) < 0 ? 0x80000000u : 0u);
-    const uint32_t ss = (__double_as_longlong(s1) < 0 ? 0x8000u : 0u) | (__double_as_longlong(s2) < 0 ? 0x80000000u : 0u);
+    const unsigned long long tc1 = dft_mag(c1, 0), tc2 = dft_mag(c2, 0), ts1 = dft_mag(s1, 0), ts2 = dft_mag(s2, 0);
+    const uint32_t sc = sign2(c1, c2), ss = sign2(s1, s2);
 #pragma unroll
     for (int sl = 0; sl < kDftS; ++sl) {
       fc[sl] = dft_slice2(tc1, tc2, sc, sl);
@@ -412,49 +414,37 @@ __device__ void dft_mma_stage(double2* A, double2* Bf, int P, int m, int lane, i
   for (int tile = warp; tile < ntile; tile += nw) {
     // column g: butterfly bi (over both buffers), component g & 1
     const int bi = tile * 4 + (gid >> 1), comp = gid & 1;
-    double av1 = 0.0, av2 = 0.0, bv1 = 0.0, bv2 = 0.0, v0c = 0.0;
+    double x1 = 0.0, y1 = 0.0, x2 = 0.0, y2 = 0.0, v0 = 0.0;
     double* pi = nullptr;
     if (bi < nbt) {
       const int sel = bi >= nb, t = bi - sel * nb;
       const int g = (int)(((float)t + 0.5f) * inv_m);
       pi = reinterpret_cast<double*>((sel ? Bf : A) + g * mp + (t - g * m)) + comp;
-      if (has1) {
-        const double x = pi[2 * q1 * m], y = pi[2 * (p - q1) * m];
-        av1 = x + y; bv1 = x - y;
-      }
-      if (has2) {
-        const double x = pi[2 * q2 * m], y = pi[2 * (p - q2) * m];
-        av2 = x + y; bv2 = x - y;
-      }
-      v0c = pi[0];
+      if (has1) { x1 = pi[2 * q1 * m]; y1 = pi[2 * (p - q1) * m]; }
+      if (has2) { x2 = pi[2 * q2 * m]; y2 = pi[2 * (p - q2) * m]; }
+      v0 = pi[0];
     }
-    // outputs of this lane: butterfly bo, both components
-    const int bo = tile * 4 + tig;
-    double2* po = nullptr;
-    double2 v0o = make_double2(0.0, 0.0);
-    if (bo < nbt) {
-      const int sel = bo >= nb, t = bo - sel * nb;
-      const int g = (int)(((float)t + 0.5f) * inv_m);
-      po = (sel ? Bf : A) + g * mp + (t - g * m);
-      v0o = po[0];
-    }
-    // y_0 = v_0 + sum_q a_q per component (the same sum on the four lanes)
-    double ys = av1 + av2;
-    ys += __shfl_xor_sync(FULL, ys, 1);
-    ys += __shfl_xor_sync(FULL, ys, 2);
-    // column exponent and slices of a, b
-    int fb = max(max(biased_exp(av1), biased_exp(av2)), max(biased_exp(bv1), biased_exp(bv2)));
+    // the butterfly's exponent: |v| < 2^e over its 2p values (8 lanes)
+    int fb = max(max(max(biased_exp(x1), biased_exp(y1)), max(biased_exp(x2), biased_exp(y2))), biased_exp(v0));
     fb = max(fb, __shfl_xor_sync(FULL, fb, 1));
     fb = max(fb, __shfl_xor_sync(FULL, fb, 2));
-    const int ec = fb - 1022;
+    fb = max(fb, __shfl_xor_sync(FULL, fb, 4));
+    const int e = fb - 1022;
+    const long long X1 = fix_of<kDftFB>(x1, e), Y1 = fix_of<kDftFB>(y1, e), X2 = fix_of<kDftFB>(x2, e),
+                    Y2 = fix_of<kDftFB>(y2, e), V0 = fix_of<kDftFB>(v0, e);
+    const long long a1 = X1 + Y1, b1 = X1 - Y1, a2 = X2 + Y2, b2 = X2 - Y2;
+    // y_0 = v_0 + sum_q a_q per component (the same sum on the four lanes)
+    long long ys = a1 + a2;
+    ys += __shfl_xor_sync(FULL, ys, 1);
+    ys += __shfl_xor_sync(FULL, ys, 2);
     uint32_t fa[kDftS], fbq[kDftS];
     {
-      const unsigned long long ta1 = dft_mag(av1, ec), ta2 = dft_mag(av2, ec), tb1 = dft_mag(bv1, ec),
-                               tb2 = dft_mag(bv2, ec);
-      const uint32_t sa = (__double_as_longlong(av1) < 0 ? 0x8000u : 0u) |
-                          (__double_as_longlong(av2) < 0 ? 0x80000000u : 0u);
-      const uint32_t sb = (__double_as_longlong(bv1) < 0 ? 0x8000u : 0u) |
-                          (__double_as_longlong(bv2) < 0 ? 0x80000000u : 0u);
+      const unsigned long long ta1 = (unsigned long long)(a1 < 0 ? -a1 : a1) << UP,
+                               ta2 = (unsigned long long)(a2 < 0 ? -a2 : a2) << UP,
+                               tb1 = (unsigned long long)(b1 < 0 ? -b1 : b1) << UP,
+                               tb2 = (unsigned long long)(b2 < 0 ? -b2 : b2) << UP;
+      const uint32_t sa = (a1 < 0 ? 0x8000u : 0u) | (a2 < 0 ? 0x80000000u : 0u);
+      const uint32_t sb = (b1 < 0 ? 0x8000u : 0u) | (b2 < 0 ? 0x80000000u : 0u);
 #pragma unroll
       for (int sl = 0; sl < kDftS; ++sl) {
         fa[sl] = dft_slice2(ta1, ta2, sa, sl);
@@ -462,7 +452,8 @@ __device__ void dft_mma_stage(double2* A, double2* Bf, int P, int m, int lane, i
       }
     }
     __syncwarp();  // every load of the tile precedes its stores
-    if (tig == 0 && pi) pi[0] = v0c + ys;
+    if (tig == 0 && pi)
+      pi[0] = fb == 2047 ? __longlong_as_double(0x7ff8000000000000LL) : dbl_of_fix(V0 + ys, e - kDftFB);
     float acc[kDftD + 1][4];
 #pragma unroll
     for (int d = 0; d <= kDftD; ++d)
@@ -472,55 +463,66 @@ __device__ void dft_mma_stage(double2* A, double2* Bf, int P, int m, int lane, i
     for (int sl = 0; sl < kDftS; ++sl)
 #pragma unroll
       for (int t = 0; t < kDftS && sl + t <= kDftD; ++t) mma_f16(acc[sl + t], fc[sl], 0u, 0u, fs[sl], fa[t], fbq[t]);
-    // column exponents of this lane's output columns 2t (re) and 2t + 1 (im)
-    const int fre = __shfl_sync(FULL, fb, 8 * tig), fim = __shfl_sync(FULL, fb, 8 * tig + 4);
-    if (gid < h && po) {
-      double o[4];
+    // this lane's butterfly bo: its exponent and v_0 (lanes 8t, 8t + 4 loaded them)
+    const int bo = tile * 4 + tig;
+    const int eo = __shfl_sync(FULL, e, 8 * tig);
+    const long long w_re = __shfl_sync(FULL, V0, 8 * tig), w_im = __shfl_sync(FULL, V0, 8 * tig + 4);
+    if (gid < h && bo < nbt) {
+      const int sel = bo >= nb, t = bo - sel * nb;
+      const int g = (int)(((float)t + 0.5f) * inv_m);
+      double2* po = (sel ? Bf : A) + g * mp + (t - g * m);
+      // (A_j - v_0).re, .im, B_j.re, .im = 2^(e - 71) (H 2^36 + L),
+      // H = sum_{d<=2} Q_d 512^(2-d), L = sum_{d=3..6} Q_d 512^(6-d)
+      long long H[4], L[4];
 #pragma unroll
       for (int i = 0; i < 4; ++i) {
-        const int f = (i & 1) ? fim : fre;
-        // sum = 2^(e_row + e_col - 36) H + 2^(e_row + e_col - 72) L,
-        // H = sum_{d<=2} Q_d 512^(2-d), L = sum_{d=3..6} Q_d 512^(6-d), both exact in int64
-        const long long H = ((long long)__float2int_rn(acc[0][i]) << 18) + ((long long)__float2int_rn(acc[1][i]) << 9) +
-                            __float2int_rn(acc[2][i]);
-        const long long L = ((long long)__float2int_rn(acc[3][i]) << 27) + ((long long)__float2int_rn(acc[4][i]) << 18) +
-                            ((long long)__float2int_rn(acc[5][i]) << 9) + __float2int_rn(acc[6][i]);
-        const int k = (i < 2 ? erc : ers) + (f - 1022) - 36;
-        o[i] = combine_rn(H, L, k - 36, 36);
-        if (f == 2047) o[i] = __longlong_as_double(0x7ff8000000000000LL);  // Inf or NaN in the column
+        H[i] = ((long long)__float2int_rn(acc[0][i]) << 18) + ((long long)__float2int_rn(acc[1][i]) << 9) +
+               __float2int_rn(acc[2][i]);
+        L[i] = ((long long)__float2int_rn(acc[3][i]) << 27) + ((long long)__float2int_rn(acc[4][i]) << 18) +
+               ((long long)__float2int_rn(acc[5][i]) << 9) + __float2int_rn(acc[6][i]);
       }
-      const double ar = o[0] + v0o.x, ai = o[1] + v0o.y;
+      // v_0 (units 2^(e - 58)) in the same integers: 2^13 V = (V >> 23) 2^36 + (V mod 2^23) 2^13
+      const long long hr = H[0] + (w_re >> 23), lr = L[0] + ((w_re & ((1LL << 23) - 1)) << 13);
+      const long long hi = H[1] + (w_im >> 23), li = L[1] + ((w_im & ((1LL << 23) - 1)) << 13);
+      const int k = eo - 71;
+      double2 yj = make_double2(combine_rn(hr + H[3], lr + L[3], k, 36), combine_rn(hi - H[2], li - L[2], k, 36));
+      double2 yk = make_double2(combine_rn(hr - H[3], lr - L[3], k, 36), combine_rn(hi + H[2], li + L[2], k, 36));
+      if (eo == 2047 - 1022) {  // Inf or NaN in the butterfly
+        yj = make_double2(__longlong_as_double(0x7ff8000000000000LL), __longlong_as_double(0x7ff8000000000000LL));
+        yk = yj;
+      }
       const int j = gid + 1;
-      po[j * m] = make_double2(ar + o[3], ai - o[2]);
-      po[(p - j) * m] = make_double2(ar - o[3], ai + o[2]);
+      po[j * m] = yj;
+      po[(p - j) * m] = yk;
     }
   }
 }
 
 // Wide odd-prime stage (p = 19, 23, 29, 31: h = 9..15) of a prime-factor
-// plan on the fp16 tensor cores: the same symmetric butterfly as
-// dft_mma_stage with the cos and sin products as two 16 x 16 tiles (rows
-// j, K = q, padded), 8 signed 8-bit slices per operand (64 bits) and the 36
-// pairs s + t <= 7 per tile; at most 15 products per output keep every FP32
-// sum exact, the dropped pairs weigh less than 2^-61 of the largest
-// product.  Lane (g, t) forms a_q, b_q for q = 2t + 1, 2t + 2, 2t + 9,
-// 2t + 10 of column g and receives A_j, B_j for j = g + 1 and g + 9 of
-// butterfly t.  FP64 instructions: ~34 per lane per tile of 4 butterflies,
-// against ~131 (p = 31) in dft_odd_store.
+// plan on the fp16 tensor cores: the fixed-point butterfly of
+// dft_mma_stage (integers |V| < 2^57, |y_0| < 2^63 for h <= 15) with the
+// cos and sin products as two 16 x 16 tiles (rows j, K = q, padded), 8
+// signed 8-bit slices of the coefficients and of 2^6 a, 2^6 b (64 bits)
+// and the 36 pairs s + t <= 7 per tile; at most 15 products per output keep
+// every FP32 sum exact (8 pairs x 15 x 255^2 < 2^24).  Lane (g, t) holds
+// v_q, v_{p-q} for q = 2t + 1, 2t + 2, 2t + 9, 2t + 10 of column g and
+// receives A_j, B_j for j = g + 1 and g + 9 of butterfly t.
+constexpr int kDwFB = 57;
+
 template <int p>
 __device__ void dft_mma_stage_wide(double2* A, double2* Bf, int P, int m, int lane, int warp, int nw) {
   constexpr int h = (p - 1) / 2;
   static_assert(h > 8 && h <= 15, "two 16 x 16 tiles");
   constexpr unsigned FULL = 0xffffffffu;
+  constexpr int UP = 64 - (kDwFB + 1);  // 2^UP |a| < 2^64
   const int gid = lane >> 2, tig = lane & 3;
   const int nb = P / p, mp = m * p, nbt = 2 * nb, ntile = (nbt + 3) / 4;
   const float inv_m = 1.0f / (float)m;
   const int qa = 2 * tig + 1;  // K rows 2t, 2t + 1 -> q = qa, qa + 1; rows 2t + 8, 2t + 9 -> q = qa + 8, qa + 9
-  // coefficient fragments of the cos (C) and sin (S) tiles: per slice
-  // [0] = (j0; qa, qa+1), [1] = (j1; qa, qa+1), [2] = (j0; qa+8, qa+9), [3] = (j1; qa+8, qa+9),
-  // j0 = g + 1, j1 = g + 9
+  // coefficient fragments of the cos (C) and sin (S) tiles as 64-bit
+  // fractions: per slice [0] = (j0; qa, qa+1), [1] = (j1; qa, qa+1),
+  // [2] = (j0; qa+8, qa+9), [3] = (j1; qa+8, qa+9), j0 = g + 1, j1 = g + 9
   uint32_t fc[kDwS][4], fs[kDwS][4];
-  int erc[2], ers[2];
   {
     double c[2][4], sn[2][4];  // [row j0 / j1][q slot]
 #pragma unroll
@@ -533,21 +535,12 @@ __device__ void dft_mma_stage_wide(double2* A, double2* Bf, int P, int m, int la
         c[r][i] = ok ? DftTab<p>::c((j * q) % p) : 0.0;
         sn[r][i] = ok ? DftTab<p>::s((j * q) % p) : 0.0;
       }
-      int mc = 0, ms = 0;
-#pragma unroll
-      for (int i = 0; i < 4; ++i) { mc = max(mc, biased_exp(c[r][i])); ms = max(ms, biased_exp(sn[r][i])); }
-      mc = max(mc, __shfl_xor_sync(FULL, mc, 1));
-      mc = max(mc, __shfl_xor_sync(FULL, mc, 2));
-      ms = max(ms, __shfl_xor_sync(FULL, ms, 1));
-      ms = max(ms, __shfl_xor_sync(FULL, ms, 2));
-      erc[r] = mc - 1022;
-      ers[r] = ms - 1022;
     }
 #pragma unroll
     for (int f = 0; f < 4; ++f) {
       const int r = f & 1, i0 = 2 * (f >> 1);
-      const unsigned long long c0 = dft_mag64(c[r][i0], erc[r]), c1 = dft_mag64(c[r][i0 + 1], erc[r]);
-      const unsigned long long s0 = dft_mag64(sn[r][i0], ers[r]), s1 = dft_mag64(sn[r][i0 + 1], ers[r]);
+      const unsigned long long c0 = dft_mag64(c[r][i0], 0), c1 = dft_mag64(c[r][i0 + 1], 0);
+      const unsigned long long s0 = dft_mag64(sn[r][i0], 0), s1 = dft_mag64(sn[r][i0 + 1], 0);
       const uint32_t sgc = sign2(c[r][i0], c[r][i0 + 1]), sgs = sign2(sn[r][i0], sn[r][i0 + 1]);
 #pragma unroll
       for (int sl = 0; sl < kDwS; ++sl) {
@@ -558,7 +551,7 @@ __device__ void dft_mma_stage_wide(double2* A, double2* Bf, int P, int m, int la
   }
   for (int tile = warp; tile < ntile; tile += nw) {
     const int bi = tile * 4 + (gid >> 1), comp = gid & 1;
-    double av[4] = {0.0, 0.0, 0.0, 0.0}, bv[4] = {0.0, 0.0, 0.0, 0.0}, v0c = 0.0;
+    double x[4] = {0.0, 0.0, 0.0, 0.0}, y[4] = {0.0, 0.0, 0.0, 0.0}, v0 = 0.0;
     double* pi = nullptr;
     if (bi < nbt) {
       const int sel = bi >= nb, t = bi - sel * nb;
@@ -567,47 +560,46 @@ __device__ void dft_mma_stage_wide(double2* A, double2* Bf, int P, int m, int la
 #pragma unroll
       for (int i = 0; i < 4; ++i) {
         const int q = qa + (i & 1) + 8 * (i >> 1);
-        if (q <= h) {
-          const double x = pi[2 * q * m], y = pi[2 * (p - q) * m];
-          av[i] = x + y; bv[i] = x - y;
-        }
+        if (q <= h) { x[i] = pi[2 * q * m]; y[i] = pi[2 * (p - q) * m]; }
       }
-      v0c = pi[0];
+      v0 = pi[0];
     }
-    const int bo = tile * 4 + tig;
-    double2* po = nullptr;
-    double2 v0o = make_double2(0.0, 0.0);
-    if (bo < nbt) {
-      const int sel = bo >= nb, t = bo - sel * nb;
-      const int g = (int)(((float)t + 0.5f) * inv_m);
-      po = (sel ? Bf : A) + g * mp + (t - g * m);
-      v0o = po[0];
-    }
-    double ys = (av[0] + av[1]) + (av[2] + av[3]);
-    ys += __shfl_xor_sync(FULL, ys, 1);
-    ys += __shfl_xor_sync(FULL, ys, 2);
-    int fb = 0;
+    int fb = biased_exp(v0);
 #pragma unroll
-    for (int i = 0; i < 4; ++i) fb = max(fb, max(biased_exp(av[i]), biased_exp(bv[i])));
+    for (int i = 0; i < 4; ++i) fb = max(fb, max(biased_exp(x[i]), biased_exp(y[i])));
     fb = max(fb, __shfl_xor_sync(FULL, fb, 1));
     fb = max(fb, __shfl_xor_sync(FULL, fb, 2));
-    const int ec = fb - 1022;
+    fb = max(fb, __shfl_xor_sync(FULL, fb, 4));
+    const int e = fb - 1022;
+    long long av[4], bv[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const long long X = fix_of<kDwFB>(x[i], e), Y = fix_of<kDwFB>(y[i], e);
+      av[i] = X + Y;
+      bv[i] = X - Y;
+    }
+    const long long V0 = fix_of<kDwFB>(v0, e);
+    long long ys = (av[0] + av[1]) + (av[2] + av[3]);
+    ys += __shfl_xor_sync(FULL, ys, 1);
+    ys += __shfl_xor_sync(FULL, ys, 2);
     __syncwarp();  // every load of the tile precedes its stores
-    if (tig == 0 && pi) pi[0] = v0c + ys;
-    const int fre = __shfl_sync(FULL, fb, 8 * tig), fim = __shfl_sync(FULL, fb, 8 * tig + 4);
-    double o[2][4];  // [C / S][(j0 re, j0 im, j1 re, j1 im)]
+    if (tig == 0 && pi)
+      pi[0] = fb == 2047 ? __longlong_as_double(0x7ff8000000000000LL) : dbl_of_fix(V0 + ys, e - kDwFB);
+    long long H[2][4], L[2][4];  // [C / S][(j0 re, j0 im, j1 re, j1 im)]: 2^(e - 71) (H 2^32 + L)
 #pragma unroll
     for (int part = 0; part < 2; ++part) {
-      const double* v = part ? bv : av;
+      const long long* v = part ? bv : av;
       uint32_t fx[kDwS][2];
       {
-        const unsigned long long t0 = dft_mag64(v[0], ec), t1 = dft_mag64(v[1], ec), t2 = dft_mag64(v[2], ec),
-                                 t3 = dft_mag64(v[3], ec);
-        const uint32_t s01 = sign2(v[0], v[1]), s23 = sign2(v[2], v[3]);
+        unsigned long long t[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) t[i] = (unsigned long long)(v[i] < 0 ? -v[i] : v[i]) << UP;
+        const uint32_t s01 = (v[0] < 0 ? 0x8000u : 0u) | (v[1] < 0 ? 0x80000000u : 0u);
+        const uint32_t s23 = (v[2] < 0 ? 0x8000u : 0u) | (v[3] < 0 ? 0x80000000u : 0u);
 #pragma unroll
         for (int sl = 0; sl < kDwS; ++sl) {
-          fx[sl][0] = dft_slice2w(t0, t1, s01, sl);
-          fx[sl][1] = dft_slice2w(t2, t3, s23, sl);
+          fx[sl][0] = dft_slice2w(t[0], t[1], s01, sl);
+          fx[sl][1] = dft_slice2w(t[2], t[3], s23, sl);
         }
       }
       float acc[kDwD + 1][4];
@@ -623,26 +615,40 @@ __device__ void dft_mma_stage_wide(double2* A, double2* Bf, int P, int m, int la
       }
 #pragma unroll
       for (int i = 0; i < 4; ++i) {
-        const int fcol = (i & 1) ? fim : fre;
-        const int er = part ? ers[i >> 1] : erc[i >> 1];
-        long long H = 0, L = 0;
+        long long hh = 0, ll = 0;
 #pragma unroll
-        for (int d = 0; d <= 3; ++d) H = H * 256 + __float2int_rn(acc[d][i]);
+        for (int d = 0; d <= 3; ++d) hh = hh * 256 + __float2int_rn(acc[d][i]);
 #pragma unroll
-        for (int d = 4; d <= kDwD; ++d) L = L * 256 + __float2int_rn(acc[d][i]);
-        const int kL = er + (fcol - 1022) - 72;
-        o[part][i] = combine_rn(H, L, kL, 32);
-        if (fcol == 2047) o[part][i] = __longlong_as_double(0x7ff8000000000000LL);
+        for (int d = 4; d <= kDwD; ++d) ll = ll * 256 + __float2int_rn(acc[d][i]);
+        H[part][i] = hh;
+        L[part][i] = ll;
       }
     }
-    if (po) {
+    const int bo = tile * 4 + tig;
+    const int eo = __shfl_sync(FULL, e, 8 * tig);
+    const long long w_re = __shfl_sync(FULL, V0, 8 * tig), w_im = __shfl_sync(FULL, V0, 8 * tig + 4);
+    if (bo < nbt) {
+      const int sel = bo >= nb, t = bo - sel * nb;
+      const int g = (int)(((float)t + 0.5f) * inv_m);
+      double2* po = (sel ? Bf : A) + g * mp + (t - g * m);
+      // v_0 (units 2^(e - 57)) as 2^14 V = (V >> 18) 2^32 + (V mod 2^18) 2^14
+      const long long vhr = w_re >> 18, vlr = (w_re & ((1LL << 18) - 1)) << 14;
+      const long long vhi = w_im >> 18, vli = (w_im & ((1LL << 18) - 1)) << 14;
+      const int k = eo - 71;
+      const double nan = __longlong_as_double(0x7ff8000000000000LL);
 #pragma unroll
       for (int r = 0; r < 2; ++r) {
         const int j = gid + 1 + 8 * r;
         if (j <= h) {
-          const double ar = o[0][2 * r] + v0o.x, ai = o[0][2 * r + 1] + v0o.y;
-          po[j * m] = make_double2(ar + o[1][2 * r + 1], ai - o[1][2 * r]);
-          po[(p - j) * m] = make_double2(ar - o[1][2 * r + 1], ai + o[1][2 * r]);
+          const long long hr = H[0][2 * r] + vhr, lr = L[0][2 * r] + vlr;
+          const long long hi = H[0][2 * r + 1] + vhi, li = L[0][2 * r + 1] + vli;
+          double2 yj = make_double2(combine_rn(hr + H[1][2 * r + 1], lr + L[1][2 * r + 1], k, 32),
+                                    combine_rn(hi - H[1][2 * r], li - L[1][2 * r], k, 32));
+          double2 yk = make_double2(combine_rn(hr - H[1][2 * r + 1], lr - L[1][2 * r + 1], k, 32),
+                                    combine_rn(hi + H[1][2 * r], li + L[1][2 * r], k, 32));
+          if (eo == 2047 - 1022) yj = yk = make_double2(nan, nan);
+          po[j * m] = yj;
+          po[(p - j) * m] = yk;
         }
       }
     }

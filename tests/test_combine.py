@@ -5,7 +5,8 @@ both slice formats, and the integer-only combine_rn of the tensor-core DFT
 stages against the two-term form (two exact power-of-two scalings and one FP64
 add): the same bits on random sums of every sign, on exact ties of the
 rounding (to nearest even), on cancellations to zero, at the edges of its
-exponent range and beyond them (where it takes the two-term form itself).
+exponent range and beyond them (where it takes the two-term form itself);
+and the fixed-point conversions of the DFT stages (fix_of, dbl_of_fix).
 Compiled on the host with g++: no GPU."""
 import os
 import subprocess
@@ -16,6 +17,7 @@ from conftest import PKG
 
 HARNESS = r'''
 #include <cstdio>
+#include <cmath>
 #include <cstring>
 #include <random>
 #include "falcon_combine.h"
@@ -95,6 +97,33 @@ int main() {
       ++dbad;
     }
   }
+  // fix_of (a 2^(FB - e) truncated, |a| < 2^e) against the exact scaling
+  // and cast; dbl_of_fix (RN(v 2^k) of any 64-bit v) against ldexp of the
+  // correctly rounded conversion
+  long long fbad = 0, fchecked = 0;
+  for (int it = 0; it < 1000000; ++it) {
+    const int e = (int)(rng() % 200) - 100;
+    double a = std::ldexp((double)(rng() >> 11) / 9007199254740992.0, e - (int)(rng() % 70));
+    if (rng() & 1) a = -a;
+    const int fb = (it & 1) ? 58 : 57;
+    const long long got = fb == 58 ? fix_of<58>(a, e) : fix_of<57>(a, e);
+    const long long ref = (long long)std::ldexp(a, fb - e);
+    ++fchecked;
+    if (got != ref) {
+      if (fbad < 5) std::printf("FIX MISMATCH a=%a e=%d\n", a, e);
+      ++fbad;
+    }
+    long long v = (long long)rng();
+    v >>= (int)(rng() % 63);
+    if (rng() & 1) v = -v;
+    const int k = (int)(rng() % 400) - 200;
+    ++fchecked;
+    if (!same(dbl_of_fix(v, k), std::ldexp((double)v, k))) {
+      if (fbad < 5) std::printf("DBL MISMATCH v=%lld k=%d\n", v, k);
+      ++fbad;
+    }
+  }
+  std::printf("%lld %lld\n", fchecked, fbad);
   std::printf("%lld %lld\n", dchecked, dbad);
   std::printf("%lld %lld %lld\n", checked, fast, bad);
   return 0;
@@ -115,6 +144,11 @@ def harness(tmp_path_factory):
 def test_pairwise_diagonal_sums_equal_horner(harness):
     dchecked, dbad = (int(x) for x in harness.strip().splitlines()[-2].split())
     assert dbad == 0 and dchecked == 800_000, harness
+
+
+def test_fixed_point_conversions_are_exact(harness):
+    fchecked, fbad = (int(x) for x in harness.strip().splitlines()[-3].split())
+    assert fbad == 0 and fchecked == 2_000_000, harness
 
 
 def test_combine_rn_is_bit_identical_to_the_two_term_form(harness):

@@ -9,12 +9,14 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("gemm_mode", [1, 3, 0])
-def test_nonfinite_instance_is_reported_and_isolated(fg, gemm_mode):
+# Nm = 42: Np = 126 (FMA butterflies); 85: Np = 255 (radix 17 on the tensor
+# cores); 19: Np = 57 (radix 19, the wide tensor-core stage)
+@pytest.mark.parametrize("gemm_mode,Nm", [(1, 42), (3, 42), (0, 42), (4, 85), (4, 19)])
+def test_nonfinite_instance_is_reported_and_isolated(fg, gemm_mode, Nm):
     n, bad = 20, 7
     prev = fg.set_gemm_mode(gemm_mode)
     try:
-        ps = [fg.make_params(65, 42, "SBDF3", ra=1e5 * (1 + 0.05 * k), dt=1e-5) for k in range(n)]
+        ps = [fg.make_params(65, Nm, "SBDF3", ra=1e5 * (1 + 0.05 * k), dt=1e-5) for k in range(n)]
         b = fg.Batch(ps)
         b.init_noise(list(range(40, 40 + n)))
         b.step(2)

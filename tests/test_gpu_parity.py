@@ -24,7 +24,7 @@ def smooth(rng, R, M, decay=0.05):
 
 
 @pytest.mark.parametrize("R,Nm", [(9, 4), (33, 42), (65, 85), (65, 170), (97, 341), (33, 512), (17, 7),
-                                  (17, 10), (33, 35)])
+                                  (17, 10), (33, 35), (17, 13), (17, 19), (17, 23), (33, 29), (33, 110)])
 def test_nonlinear_pass_matches_oracle(orc, fg, R, Nm):
     rng = np.random.default_rng(R * 1000 + Nm)
     M = Nm + 1
