@@ -1,9 +1,9 @@
-// Recombination of exact integer-slice sums into one FP64 value, with
-// integer instructions only (GB300's FP64 pipe issues ~2 instructions per
-// clock per SM, so one FP64 add per output of a tensor-core contraction or
-// DFT stage costs as much as the rest of its epilogue).  Host and device:
-// the CPU tests compile this header with g++ and compare the two forms bit
-// for bit.
+// Recombination of exact integer-slice sums into one FP64 value, and the
+// fixed-point conversions of the tensor-core DFT stages, with integer
+// instructions only (GB300's FP64 pipe issues ~2 instructions per clock
+// per SM, so one FP64 add per output of a tensor-core contraction or DFT
+// stage costs as much as the rest of its epilogue).  Host and device: the
+// CPU tests compile this header with g++ and check it bit for bit.
 #pragma once
 #include <math.h>
 #include <stdint.h>
