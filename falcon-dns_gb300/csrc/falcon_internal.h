@@ -49,6 +49,18 @@ inline int make_fft_plan(int P, FftPlan* plan) {
     if (primes[i] > 64) return -1;
   }
   if (squarefree && small && np <= kMaxRadix) {
+    // 2 x 3 as one axis of 6 (its butterfly a Good-Thomas 2 x 3 in
+    // registers, dft_small<6>): one pass over the line in shared memory
+    // fewer, the same FP64 operations
+    bool has2 = false, has3 = false;
+    for (int i = 0; i < np; ++i) { has2 = has2 || primes[i] == 2; has3 = has3 || primes[i] == 3; }
+    if (has2 && has3) {
+      int j = 0;
+      for (int i = 0; i < np; ++i)
+        if (primes[i] == 2) primes[j++] = 6;
+        else if (primes[i] != 3) primes[j++] = primes[i];
+      np = j;
+    }
     f.pfa = 1;
     f.nrad = np;
     for (int i = 0; i < np; ++i) {

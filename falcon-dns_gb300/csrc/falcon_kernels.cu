@@ -83,10 +83,30 @@ cudaError_t init_dft_tables() {
 }
 
 // Forward DFT of length p in registers: v_j <- sum_q v_q exp(-2 pi i j q/p)
-// (radix 2 and 4; odd primes go through dft_odd_store below).
+// (radix 2, 4 and 6; odd primes go through dft_odd_store below).  Radix 6
+// is the 6-point axis of a prime-factor plan, computed as a Good-Thomas
+// 2 x 3: inputs n = (3 n1 + 2 n2) mod 6, two 3-point DFTs over n2 in the
+// symmetric form of dft_odd_store (cos(2 pi/3) = -1/2 exactly), then
+// y_k = W_0[k mod 3] +- W_1[k mod 3] with the sign (-1)^(k mod 2).
 template <int p>
 __device__ __forceinline__ void dft_small(double2 (&v)[p]) {
-  if constexpr (p == 2) {
+  if constexpr (p == 6) {
+    const double c = -0.5, sn = DftTab<3>::s(1);
+    double2 w0[3], w1[3];
+    {
+      const double2 v0 = v[0], a = cadd(v[2], v[4]), b = csub(v[2], v[4]);
+      const double2 A = make_double2(fma(a.x, c, v0.x), fma(a.y, c, v0.y)), B = make_double2(b.x * sn, b.y * sn);
+      w0[0] = cadd(v0, a); w0[1] = make_double2(A.x + B.y, A.y - B.x); w0[2] = make_double2(A.x - B.y, A.y + B.x);
+    }
+    {
+      const double2 v0 = v[3], a = cadd(v[5], v[1]), b = csub(v[5], v[1]);
+      const double2 A = make_double2(fma(a.x, c, v0.x), fma(a.y, c, v0.y)), B = make_double2(b.x * sn, b.y * sn);
+      w1[0] = cadd(v0, a); w1[1] = make_double2(A.x + B.y, A.y - B.x); w1[2] = make_double2(A.x - B.y, A.y + B.x);
+    }
+    v[0] = cadd(w0[0], w1[0]); v[3] = csub(w0[0], w1[0]);
+    v[4] = cadd(w0[1], w1[1]); v[1] = csub(w0[1], w1[1]);
+    v[2] = cadd(w0[2], w1[2]); v[5] = csub(w0[2], w1[2]);
+  } else if constexpr (p == 2) {
     double2 a = v[0], b = v[1];
     v[0] = cadd(a, b); v[1] = csub(a, b);
   } else {
@@ -169,7 +189,7 @@ __device__ __forceinline__ void fft_stage(double2* __restrict__ A, double2* __re
         if (NB == 2) vb[q] = cmul(vb[q], w);
       }
     }
-    if constexpr (p == 2 || p == 4) {
+    if constexpr (p == 2 || p == 4 || p == 6) {
       dft_small<p>(va);
       if (NB == 2) dft_small<p>(vb);
       if (tk && dif) {
@@ -260,7 +280,7 @@ __device__ __forceinline__ void run_stage(int p, bool dif, bool twid, double2* A
     }
   }
   switch (p) {
-    FALCON_CASE2(2) FALCON_CASE2(3) FALCON_CASE2(4) FALCON_CASE2(5) FALCON_CASE2(7)
+    FALCON_CASE2(2) FALCON_CASE2(3) FALCON_CASE2(4) FALCON_CASE2(5) FALCON_CASE2(6) FALCON_CASE2(7)
     FALCON_CASE1(11) FALCON_CASE1(13) FALCON_CASE1(17)
     FALCON_CASE1(19) FALCON_CASE1(23) FALCON_CASE1(29) FALCON_CASE1(31)
     default: break;
@@ -282,7 +302,7 @@ __device__ __forceinline__ void run_stage1(int p, bool dif, bool twid, double2* 
     }                                                                    \
     break;
   switch (p) {
-    FALCON_CASE(2) FALCON_CASE(3) FALCON_CASE(4) FALCON_CASE(5) FALCON_CASE(7)
+    FALCON_CASE(2) FALCON_CASE(3) FALCON_CASE(4) FALCON_CASE(5) FALCON_CASE(6) FALCON_CASE(7)
     FALCON_CASE(11) FALCON_CASE(13) FALCON_CASE(17) FALCON_CASE(19) FALCON_CASE(23)
     FALCON_CASE(29) FALCON_CASE(31)
     default: break;
