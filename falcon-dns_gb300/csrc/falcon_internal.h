@@ -1,5 +1,5 @@
 // Internal interfaces between the host runtime (falcon_host.cpp) and the
-// sm_103a kernels (falcon_kernels.cu).  Not part of the C ABI.
+// sm_103a kernels (falcon_kernels.cu, falcon_fft.cuh, ...).  Not part of the C ABI.
 //
 // Device layout of every complex field of a group of B instances that share
 // (Nr, Nm): X[r][m][b] (instance fastest), one double2 per element, so that
@@ -271,7 +271,7 @@ struct AsmArgs {
   double* u0;
 };
 
-// ---- launchers (falcon_kernels.cu) ----
+// ---- launchers (falcon_kernels.cu; the nonlinear pass dispatches to falcon_fft*.cu) ----
 cudaError_t launch_nonlin(const NonlinArgs& a, cudaStream_t s);
 cudaError_t launch_gemm(const GemmArgs& g, cudaStream_t s);
 cudaError_t launch_imex_rhs(const RhsArgs& a, cudaStream_t s);

@@ -1,5 +1,5 @@
 // Device helpers shared by the integer-slice products (operator GEMMs in
-// falcon_ozaki.cu, odd-prime DFT stages in falcon_kernels.cu): an FP64
+// falcon_ozaki.cu, odd-prime DFT stages in falcon_fft.cuh): an FP64
 // value cut into signed integers of a few bits relative to a power of two
 // that bounds its row or column, their bf16 / fp16 encodings, the exact
 // recombination, and the mma.sync used on them.

@@ -1,5 +1,5 @@
 """The fixed-point odd-prime butterfly of the tensor-core DFT stages
-(dft_mma_stage / dft_mma_stage_wide, falcon-dns_gb300/csrc/falcon_kernels.cu)
+(dft_mma_stage / dft_mma_stage_wide, falcon-dns_gb300/csrc/falcon_fft.cuh)
 restated in exact integer arithmetic on the CPU:
 - every value of a butterfly as trunc(v 2^(FB - e)) at the scale 2^e of its
   largest, the pre-adds a = V_q + V_{p-q}, b = V_q - V_{p-q} and y_0 exact;
